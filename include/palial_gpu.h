@@ -1,0 +1,200 @@
+/*
+ * palial_gpu.h -- C ABI of libpalial_gpu.so, the GB300 (sm_103a) implementation of PALIAL's
+ * tiled dense Cholesky / LU / QR.
+ *
+ * Plain C types only: host or device pointers, sizes, small POD structs.  Every call is
+ * synchronous (results are valid on return) unless it takes a `stream` argument, in which
+ * case it is ordered on that CUDA stream (a cudaStream_t passed as void*, NULL = legacy
+ * default stream).  Calls are not re-entrant: use one host thread per device.
+ *
+ * Return value of every entry point: PALIAL_OK (0), or a negative PALIAL_ERR_* code with
+ * details in the optional palial_status out-parameter.
+ *
+ * Storage is the reference's tile layout (reference include/tile_address.h:9-17): tile (m,n)
+ * of an N x N matrix with tile size NB is an NB x NB column-major block at element offset
+ * NB*NB*(m + (N/NB)*n).  N % NB must be 0 (reference palial_src/main.c:101-105).
+ */
+#ifndef PALIAL_GPU_H
+#define PALIAL_GPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes -------------------------------------------------------------------- */
+#define PALIAL_OK 0
+#define PALIAL_ERR_ARG -1          /* bad argument (N % NB, NULL buffer, unsupported size)   */
+#define PALIAL_ERR_CUDA -2         /* a CUDA runtime call failed; status.cuda_error has it   */
+#define PALIAL_ERR_NOT_SPD -3      /* Cholesky met a non-positive pivot (status.tile/column) */
+#define PALIAL_ERR_TIMEOUT -4      /* a device dependency wait passed its deadline          */
+#define PALIAL_ERR_NO_DEVICE -5    /* no CUDA device / library not initialised             */
+#define PALIAL_ERR_NOT_CONVERGED -6 /* iterative refinement stopped above its tolerance     */
+#define PALIAL_ERR_NOMEM -7        /* device allocation failed                              */
+#define PALIAL_WARN_ZERO_PIVOT 1   /* LU met an exact zero pivot and skipped it (as the
+                                      reference does, src/srclu/dgetrf_no_pivot.h:21)       */
+
+/* ---- algorithms, precisions ------------------------------------------------------------ */
+#define PALIAL_ALG_CHOLESKY 0
+#define PALIAL_ALG_LU 1
+#define PALIAL_ALG_QR 2
+
+#define PALIAL_PREC_FP64 0         /* every task in FP64                                    */
+#define PALIAL_PREC_BF16 1         /* trailing updates in BF16 on tcgen05, FP32 accumulate  */
+#define PALIAL_PREC_FP8 2          /* trailing updates in FP8 e4m3, per-tile scale          */
+#define PALIAL_PREC_BF16X3 3       /* trailing updates as 3 BF16 products (split operands)  */
+
+/* ---- descriptor ------------------------------------------------------------------------ */
+/* Same field order, types and meaning as the reference's MATRIX_desc
+ * (reference include/descriptor.h:13-20), so a MATRIX_desc* may be passed where a
+ * palial_desc* is expected. */
+typedef struct palial_desc {
+    int tile_size;          /* NB                                   */
+    long matrix_nelements;  /* N * N                                */
+    long tile_nelements;    /* NB * NB                              */
+    int matrix_size;        /* N                                    */
+    void *matrix;           /* N*N doubles in tile layout (host)    */
+} palial_desc;
+
+/* ---- options / status ------------------------------------------------------------------ */
+typedef struct palial_opts {
+    int precision;          /* PALIAL_PREC_*, plain FP64 = 0                          */
+    int block;              /* scheduler block size (divides NB); 0 = automatic       */
+    int workers_per_sm;     /* persistent CTAs per SM (1 or 2); 0 = automatic         */
+    int max_sms;            /* use at most this many SMs; 0 = all                     */
+    int priority;           /* 0 = critical-path list order, 1 = program order,
+                               2 = caller-supplied costs (palial_gpu_set_task_costs)  */
+    int trace;              /* 1 = record a per-task device trace                     */
+    double timeout_s;       /* deadline of every device dependency wait; 0 = 120 s    */
+    unsigned int shuffle_seed; /* nonzero: randomise ties in the dispatch order (tests) */
+    int ir_max_iter;        /* refinement iteration cap (0 = 50)                      */
+    double ir_tol;          /* target normwise backward error (0 = 1e-14 * N)         */
+    int gmres;              /* -1 never, 0 automatic (kappa estimate > 1e8), 1 always */
+    int reserved[8];
+} palial_opts;
+
+typedef struct palial_status {
+    int code;               /* same as the return value                               */
+    int cuda_error;         /* cudaError_t of the failing call, if any                */
+    int task;               /* task index (dispatch order) of a device error          */
+    int tile_m, tile_n;     /* tile of a numerical error                              */
+    int column;             /* column inside the tile (NOT_SPD)                       */
+    long long ntasks;       /* tasks executed                                         */
+    double seconds;         /* device time of the factorization (CUDA events)         */
+    double total_seconds;   /* wall time of the call, host copies included            */
+    double tflops;          /* algorithmic flops / seconds * 1e-12                    */
+    int ir_iters;           /* refinement iterations (solve_ir)                       */
+    int gmres_iters;        /* total inner GMRES iterations (solve_ir)                */
+    double backward_error;  /* final normwise backward error (solve_ir)               */
+    double kappa_est;       /* condition estimate used to choose the method           */
+    char message[160];
+} palial_status;
+
+void palial_opts_default(palial_opts *opts);
+
+/* ---- library ---------------------------------------------------------------------------- */
+int palial_gpu_init(int device);      /* select device, query SM count; idempotent     */
+int palial_gpu_finalize(void);        /* release cached device buffers                  */
+int palial_gpu_sm_count(void);
+const char *palial_gpu_error_string(int code);
+
+/* ---- whole factorizations on HOST buffers (drop-in for src/{cholesky,lu,qr}.h) ------------
+ * Replace reference src/cholesky.h:12 `void cholesky(MATRIX_desc A)`,
+ *         reference src/lu.h:11       `void lu(MATRIX_desc A)`,
+ *         reference src/qr.h:15       `void qr(MATRIX_desc A, MATRIX_desc S)`.
+ * In place on A->matrix (and S->matrix), same output layout and meaning as the reference:
+ *  Cholesky: U (A = U^T U) in the upper triangle of tiles A(k,m), k <= m; lower tiles
+ *            untouched.
+ *  LU:       no pivoting (reference src/srclu/dgetrf.h:11-59); L strictly lower (unit
+ *            diagonal implicit), U upper.  ipiv (optional, N ints) receives the identity
+ *            permutation ipiv[i] = i + 1, LAPACK style.
+ *  QR:       flat-tree TS tile QR; R in the upper triangle, V in the strictly lower part of
+ *            A(k,k) and in A(m,k), m > k; T factors in the upper triangles of S(k,k), S(m,k).
+ */
+int palial_gpu_cholesky(const palial_desc *A, const palial_opts *opts, palial_status *st);
+int palial_gpu_lu(const palial_desc *A, int *ipiv, const palial_opts *opts, palial_status *st);
+int palial_gpu_qr(const palial_desc *A, const palial_desc *S, const palial_opts *opts,
+                  palial_status *st);
+
+/* ---- same, on DEVICE-resident tile buffers (no host copies) ------------------------------ */
+int palial_gpu_factor_dev(int alg, double *dA, double *dS, int n, int nb, const palial_opts *opts,
+                          palial_status *st, void *stream);
+
+/* ---- single-tile kernels on device pointers (reference tile-kernel ABI, for unit tests) ----
+ * Each runs one tile task on one CTA of the persistent scheduler's kernels.
+ * Replace reference src/srclu/dgetrf.h:11 PALIAL_dgetrf, src/srcqr/dgeqrt.h:9 PALIAL_dgeqrt,
+ * src/srcqr/dormqr.h:9 PALIAL_dormqr, src/srcqr/dtsqrt.h:11 PALIAL_dtsqrt,
+ * src/srcqr/dtsmqr.h:11 PALIAL_dtsmqr, and the LAPACKE/CBLAS tile calls of src/cholesky.h:40,
+ * :73, :115, :156 and src/lu.h:67, :109, :151.  lda = ld of every tile argument.      */
+int palial_gpu_tile_dpotrf(int nb, double *dA, int lda);
+int palial_gpu_tile_dgetrf(int nb, double *dA, int lda);
+int palial_gpu_tile_dtrsm(int kind, int nb, const double *dT, double *dB, int lda);
+int palial_gpu_tile_dsyrk(int nb, const double *dA, double *dC, int lda);
+int palial_gpu_tile_dgemm(int kind, int nb, const double *dA, const double *dB, double *dC, int lda);
+int palial_gpu_tile_dgeqrt(int nb, double *dA, double *dT, int lda);
+int palial_gpu_tile_dormqr(int nb, const double *dV, const double *dT, double *dC, int lda);
+int palial_gpu_tile_dtsqrt(int nb, double *dA1, double *dA2, double *dT, int lda);
+int palial_gpu_tile_dtsmqr(int nb, double *dA1, double *dA2, const double *dV, const double *dT,
+                           int lda);
+/* kind for dtrsm: 0 = left upper trans non-unit (Cholesky), 1 = right upper no-trans non-unit
+ * (LU), 2 = left lower no-trans unit (LU).  kind for dgemm: 0 = C -= A^T B (Cholesky),
+ * 1 = C -= A B (LU). */
+
+/* ---- generators (counter-based; the same bytes as the CPU oracle's generators) ------------ */
+/* uniform [-1,1): entry (i,j) from splitmix64 of seed/stream and i + j*rows.  Tile layout. */
+int palial_gpu_gen_uniform(double *dA, int n, int nb, uint64_t seed, void *stream);
+/* A = B B^T + n I, B = K/128, K integer in [-128,127] (exact integer arithmetic). */
+int palial_gpu_gen_spd(double *dA, int n, int nb, uint64_t seed, void *stream);
+
+/* The reference generator's pattern (reference include/populate.h:36-67) made reproducible:
+ * 0.5 everywhere, diagonal 173*u + 173 in [173, 346) with u = (x_i + 1)/2 and x_i the
+ * uniform [-1,1) number of index i (seed, stream 0).  SPD and diagonally dominant. */
+int palial_gpu_gen_refpattern(double *dA, int n, int nb, uint64_t seed, void *stream);
+/* Generate into a HOST tile buffer (generated on the device, then copied):
+ * kind 0 = uniform, 1 = SPD B B^T + n I, 2 = reference pattern. */
+int palial_gpu_generate(int kind, uint64_t seed, const palial_desc *A);
+
+/* ---- checks on device buffers --------------------------------------------------------------- */
+/* Normwise relative residual of the factorization against the original matrix dA0 using
+ * `nprobe` random probe vectors: ||A0 X - F(X)||_F / (||A0||_F ||X||_F), F = U^T U X, L U X or
+ * Q R X.  Exact for nprobe >= n (identity columns are not used; a probe estimates). */
+int palial_gpu_residual_probe(int alg, const double *dA0, const double *dF, const double *dS, int n,
+                              int nb, int nprobe, uint64_t seed, double *out);
+
+/* Same from HOST tile buffers (original matrix a0_host, factors in F). */
+int palial_gpu_residual_host(int alg, const double *a0_host, const palial_desc *F, int nprobe,
+                             uint64_t seed, double *out);
+
+/* ---- device trace (reference palial_trace/log.h:43-50 format) ------------------------------- */
+/* Writes one "name, ms" line per task of the last traced factorization, in creation order,
+ * with the reference's naming rule (type + k + m + n, stale loop variables,
+ * src/cholesky.h:19-28).  path NULL = stdout.  A side-car CSV with
+ * start/end ns, SM id and dispatch index is written to `csv_path` if not NULL. */
+int palial_gpu_trace_dump(const char *path, const char *csv_path);
+long long palial_gpu_trace_count(void);
+
+/* ---- GPU clock reporting (replaces the reference's palial_power CPU frequency control) ----- */
+typedef struct palial_clock_report {
+    double sm_mhz_start, sm_mhz_end, sm_mhz_max; /* via NVML when available, else -1     */
+    double sm_mhz_device;                         /* clock64 / globaltimer during the run */
+    int throttle_reasons;                         /* NVML bit mask, -1 if unavailable     */
+} palial_clock_report;
+int palial_gpu_clock_report(palial_clock_report *out);
+
+/* ---- DAG builder (host only; exported for tests) -------------------------------------------- */
+/* Build the task list the scheduler would run; returns the number of tasks, fills counts per
+ * task type (array of 16) and the critical-path length estimate (seconds, model costs). */
+long long palial_dag_info(int alg, int n, int nb, int block, int priority, int nworkers,
+                          long long *type_counts, double *critical_path_s, double *makespan_s);
+/* Validate a built DAG on the host: every wait is satisfiable by earlier tasks in dispatch
+ * order, updates to each object are totally ordered, no read/write race; then emulate the
+ * dispatch with `nworkers` workers and random durations (seed).  Returns 0 if valid. */
+int palial_dag_validate(int alg, int n, int nb, int block, int priority, int nworkers,
+                        unsigned int seed, char *msg, int msglen);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* PALIAL_GPU_H */

@@ -1,0 +1,201 @@
+"""palial_gb300 -- GB300 (sm_103a) tiled dense Cholesky / LU / QR behind PALIAL's interface.
+
+Python mirror of the reference's entry points (reference src/cholesky.h:12 ``cholesky(A)``,
+src/lu.h:11 ``lu(A)``, src/qr.h:15 ``qr(A, S)``) over the C ABI of libpalial_gpu.so
+(include/palial_gpu.h).  Matrices are flat float64 buffers in the reference's tile layout
+(include/tile_address.h:9-17); factorizations run in place, on the GPU only.  There is no CPU
+fallback: if the library or a device is missing, every call raises.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "lib", "libpalial_gpu.so")
+
+PALIAL_OK = 0
+ERR = {
+    -1: "bad argument", -2: "CUDA error", -3: "matrix is not positive definite",
+    -4: "device dependency wait timed out", -5: "no CUDA device", -6: "refinement did not converge",
+    -7: "device allocation failed", 1: "exact zero pivot skipped",
+}
+ALG = {"cholesky": 0, "lu": 1, "qr": 2}
+PREC = {"fp64": 0, "bf16": 1, "fp8": 2, "bf16x3": 3}
+
+
+class PalialError(RuntimeError):
+    def __init__(self, code: int, msg: str = ""):
+        super().__init__(f"palial error {code} ({ERR.get(code, '?')}): {msg}")
+        self.code = code
+
+
+class Desc(ctypes.Structure):
+    """Same layout as the reference's MATRIX_desc (include/descriptor.h:13-20)."""
+    _fields_ = [("tile_size", ctypes.c_int), ("matrix_nelements", ctypes.c_long),
+                ("tile_nelements", ctypes.c_long), ("matrix_size", ctypes.c_int),
+                ("matrix", ctypes.c_void_p)]
+
+
+class Opts(ctypes.Structure):
+    _fields_ = [("precision", ctypes.c_int), ("block", ctypes.c_int), ("workers_per_sm", ctypes.c_int),
+                ("max_sms", ctypes.c_int), ("priority", ctypes.c_int), ("trace", ctypes.c_int),
+                ("timeout_s", ctypes.c_double), ("shuffle_seed", ctypes.c_uint), ("ir_max_iter", ctypes.c_int),
+                ("ir_tol", ctypes.c_double), ("gmres", ctypes.c_int), ("reserved", ctypes.c_int * 8)]
+
+
+class Status(ctypes.Structure):
+    _fields_ = [("code", ctypes.c_int), ("cuda_error", ctypes.c_int), ("task", ctypes.c_int),
+                ("tile_m", ctypes.c_int), ("tile_n", ctypes.c_int), ("column", ctypes.c_int),
+                ("ntasks", ctypes.c_longlong), ("seconds", ctypes.c_double), ("total_seconds", ctypes.c_double),
+                ("tflops", ctypes.c_double), ("ir_iters", ctypes.c_int), ("gmres_iters", ctypes.c_int),
+                ("backward_error", ctypes.c_double), ("kappa_est", ctypes.c_double),
+                ("message", ctypes.c_char * 160)]
+
+    def as_dict(self) -> dict:
+        d = {f: getattr(self, f) for f, _ in self._fields_ if f != "message"}
+        d["message"] = self.message.decode(errors="replace")
+        return d
+
+
+_lib = None
+
+
+def lib() -> ctypes.CDLL:
+    """Load libpalial_gpu.so (built by palial_gb300/build.py); raises if it is missing."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise PalialError(-5, f"{LIB_PATH} not built (run __graft_entry__.build())")
+        h = ctypes.CDLL(LIB_PATH)
+        vp, i, d = ctypes.c_void_p, ctypes.c_int, ctypes.c_double
+        h.palial_gpu_init.argtypes = [i]
+        h.palial_gpu_factor_dev.argtypes = [i, vp, vp, i, i, ctypes.POINTER(Opts), ctypes.POINTER(Status), vp]
+        h.palial_gpu_cholesky.argtypes = [ctypes.POINTER(Desc), ctypes.POINTER(Opts), ctypes.POINTER(Status)]
+        h.palial_gpu_lu.argtypes = [ctypes.POINTER(Desc), vp, ctypes.POINTER(Opts), ctypes.POINTER(Status)]
+        h.palial_gpu_qr.argtypes = [ctypes.POINTER(Desc), ctypes.POINTER(Desc), ctypes.POINTER(Opts),
+                                    ctypes.POINTER(Status)]
+        h.palial_gpu_gen_uniform.argtypes = [vp, i, i, ctypes.c_uint64, vp]
+        h.palial_gpu_gen_spd.argtypes = [vp, i, i, ctypes.c_uint64, vp]
+        h.palial_gpu_residual_probe.argtypes = [i, vp, vp, vp, i, i, i, ctypes.c_uint64, ctypes.POINTER(d)]
+        h.palial_gpu_trace_dump.argtypes = [ctypes.c_char_p, ctypes.c_char_p]
+        h.palial_gpu_trace_count.restype = ctypes.c_longlong
+        h.palial_dag_info.restype = ctypes.c_longlong
+        h.palial_dag_info.argtypes = [i, i, i, i, i, i, ctypes.POINTER(ctypes.c_longlong), ctypes.POINTER(d),
+                                      ctypes.POINTER(d)]
+        h.palial_dag_validate.argtypes = [i, i, i, i, i, i, ctypes.c_uint, ctypes.c_char_p, i]
+        for name in ("palial_gpu_tile_dpotrf", "palial_gpu_tile_dgetrf"):
+            getattr(h, name).argtypes = [i, vp, i]
+        h.palial_gpu_tile_dtrsm.argtypes = [i, i, vp, vp, i]
+        h.palial_gpu_tile_dsyrk.argtypes = [i, vp, vp, i]
+        h.palial_gpu_tile_dgemm.argtypes = [i, i, vp, vp, vp, i]
+        h.palial_gpu_tile_dgeqrt.argtypes = [i, vp, vp, i]
+        h.palial_gpu_tile_dormqr.argtypes = [i, vp, vp, vp, i]
+        h.palial_gpu_tile_dtsqrt.argtypes = [i, vp, vp, vp, i]
+        h.palial_gpu_tile_dtsmqr.argtypes = [i, vp, vp, vp, vp, i]
+        h.palial_gpu_error_string.restype = ctypes.c_char_p
+        _lib = h
+    return _lib
+
+
+def make_opts(precision: str | int = "fp64", block: int = 0, workers_per_sm: int = 0, max_sms: int = 0,
+              priority: int = 0, trace: bool = False, timeout_s: float = 0.0, shuffle_seed: int = 0,
+              ir_max_iter: int = 0, ir_tol: float = 0.0, gmres: int = 0) -> Opts:
+    o = Opts()
+    o.precision = PREC[precision] if isinstance(precision, str) else int(precision)
+    o.block, o.workers_per_sm, o.max_sms, o.priority = block, workers_per_sm, max_sms, priority
+    o.trace, o.timeout_s, o.shuffle_seed = int(trace), timeout_s, shuffle_seed
+    o.ir_max_iter, o.ir_tol, o.gmres = ir_max_iter, ir_tol, gmres
+    return o
+
+
+def _check(rc: int, st: Status | None, allow=(PALIAL_OK,)) -> None:
+    if rc not in allow:
+        raise PalialError(rc, st.message.decode(errors="replace") if st is not None else "")
+
+
+def init(device: int = 0) -> None:
+    _check(lib().palial_gpu_init(device), None)
+
+
+def desc(buf: np.ndarray, n: int, nb: int) -> Desc:
+    assert buf.dtype == np.float64 and buf.flags["C_CONTIGUOUS"] and buf.size == n * n
+    return Desc(nb, n * n, nb * nb, n, buf.ctypes.data)
+
+
+# ---- reference entry points (host buffers, in place) ------------------------------------
+def cholesky(a_tiles: np.ndarray, n: int, nb: int, **kw) -> Status:
+    """Upper tile Cholesky A = U^T U in place (reference src/cholesky.h:12)."""
+    st = Status()
+    rc = lib().palial_gpu_cholesky(ctypes.byref(desc(a_tiles, n, nb)), ctypes.byref(make_opts(**kw)),
+                                   ctypes.byref(st))
+    _check(rc, st)
+    return st
+
+
+def lu(a_tiles: np.ndarray, n: int, nb: int, **kw) -> tuple[Status, np.ndarray]:
+    """No-pivot tile LU in place (reference src/lu.h:11); returns (status, ipiv = 1..N)."""
+    st = Status()
+    ipiv = np.zeros(n, dtype=np.int32)
+    rc = lib().palial_gpu_lu(ctypes.byref(desc(a_tiles, n, nb)), ipiv.ctypes.data, ctypes.byref(make_opts(**kw)),
+                             ctypes.byref(st))
+    _check(rc, st, allow=(PALIAL_OK, 1))
+    return st, ipiv
+
+
+def qr(a_tiles: np.ndarray, s_tiles: np.ndarray, n: int, nb: int, **kw) -> Status:
+    """Flat-tree TS tile QR in place (reference src/qr.h:15); T factors go to S."""
+    st = Status()
+    rc = lib().palial_gpu_qr(ctypes.byref(desc(a_tiles, n, nb)), ctypes.byref(desc(s_tiles, n, nb)),
+                             ctypes.byref(make_opts(**kw)), ctypes.byref(st))
+    _check(rc, st)
+    return st
+
+
+def factor_dev(alg: str, d_a: int, d_s: int | None, n: int, nb: int, stream: int = 0, allow_warn: bool = True,
+               **kw) -> Status:
+    """Factor a DEVICE-resident tile matrix (pointer from e.g. torch's data_ptr())."""
+    st = Status()
+    rc = lib().palial_gpu_factor_dev(ALG[alg], d_a, d_s or None, n, nb, ctypes.byref(make_opts(**kw)),
+                                     ctypes.byref(st), stream or None)
+    _check(rc, st, allow=(PALIAL_OK, 1) if allow_warn else (PALIAL_OK,))
+    return st
+
+
+def gen_uniform(d_a: int, n: int, nb: int, seed: int, stream: int = 0) -> None:
+    _check(lib().palial_gpu_gen_uniform(d_a, n, nb, seed, stream or None), None)
+
+
+def gen_spd(d_a: int, n: int, nb: int, seed: int, stream: int = 0) -> None:
+    _check(lib().palial_gpu_gen_spd(d_a, n, nb, seed, stream or None), None)
+
+
+def residual_probe(alg: str, d_a0: int, d_f: int, n: int, nb: int, nprobe: int = 8, seed: int = 7,
+                   d_s: int | None = None) -> float:
+    out = ctypes.c_double()
+    _check(lib().palial_gpu_residual_probe(ALG[alg], d_a0, d_f, d_s or None, n, nb, nprobe, seed,
+                                           ctypes.byref(out)), None)
+    return out.value
+
+
+def trace_dump(path: str | None = None, csv_path: str | None = None) -> None:
+    _check(lib().palial_gpu_trace_dump(path.encode() if path else None, csv_path.encode() if csv_path else None), None)
+
+
+def dag_info(alg: str, n: int, nb: int, block: int = 0, priority: int = 0, nworkers: int = 152) -> dict:
+    counts = (ctypes.c_longlong * 16)()
+    cp, ms = ctypes.c_double(), ctypes.c_double()
+    nrec = lib().palial_dag_info(ALG[alg], n, nb, block, priority, nworkers, counts, ctypes.byref(cp),
+                                 ctypes.byref(ms))
+    if nrec < 0:
+        raise PalialError(-1, "invalid DAG parameters")
+    return {"records": nrec, "type_counts": list(counts), "critical_path_s": cp.value, "makespan_s": ms.value}
+
+
+def dag_validate(alg: str, n: int, nb: int, block: int = 0, priority: int = 0, nworkers: int = 152,
+                 seed: int = 1) -> str:
+    buf = ctypes.create_string_buffer(256)
+    rc = lib().palial_dag_validate(ALG[alg], n, nb, block, priority, nworkers, seed, buf, 256)
+    return "" if rc == 0 else (buf.value.decode() or f"rc={rc}")

@@ -1,0 +1,618 @@
+// runtime.cu -- host side of libpalial_gpu.so: the C ABI of include/palial_gpu.h.
+//
+// Owns the device state (one device per process), caches DAGs and device buffers, launches
+// the persistent scheduler and reports status.  No CPU fallback exists: every entry point
+// fails with PALIAL_ERR_NO_DEVICE / PALIAL_ERR_CUDA when the GPU path cannot run.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <memory>
+#include <string>
+#include <tuple>
+#include <vector>
+
+#include "../../include/palial_gpu.h"
+#include "common.cuh"
+#include "dag.hpp"
+
+namespace palial {
+// sched_f64.cu
+int sched_smem_bytes();
+cudaError_t sched_configure();
+int sched_occupancy();
+cudaError_t sched_launch(const SchedParams &p, int grid, cudaStream_t s);
+long long sched_scratch_doubles(int alg, int n, int nb, int bs, int workers, long long *per_worker);
+cudaError_t tile_task_launch(int type, int nb, int ld, double *p0, double *p1, double *p2, double *p3, double *scratch,
+                             int *status, cudaStream_t s);
+// gen_check.cu
+cudaError_t launch_gen_uniform(double *A, int n, int nb, uint64_t seed, cudaStream_t s);
+cudaError_t launch_gen_refpattern(double *A, int n, int nb, uint64_t seed, cudaStream_t s);
+cudaError_t launch_gen_dense(double *X, long long rows, int cols, uint64_t seed, int stream, cudaStream_t s);
+cudaError_t launch_gen_spd(double *A, int n, int nb, uint64_t seed, int8_t *kbuf, cudaStream_t s);
+cudaError_t launch_tiled_mm(const double *A, const double *X, double *Y, int n, int nb, int r, int mode, int trans,
+                            cudaStream_t s);
+cudaError_t launch_sumsq(const double *X, long long len, double *partial, int blocks, cudaStream_t s);
+cudaError_t launch_sub(const double *X, const double *Y, double *Z, long long len, cudaStream_t s);
+}  // namespace palial
+
+using namespace palial;
+
+namespace {
+
+// grow-only device buffer
+struct DevBuf {
+    void *ptr = nullptr;
+    size_t bytes = 0;
+    cudaError_t ensure(size_t want) {
+        if (want <= bytes) return cudaSuccess;
+        if (ptr) cudaFree(ptr);
+        ptr = nullptr;
+        bytes = 0;
+        cudaError_t e = cudaMalloc(&ptr, want);
+        if (e == cudaSuccess) bytes = want;
+        return e;
+    }
+    void release() {
+        if (ptr) cudaFree(ptr);
+        ptr = nullptr;
+        bytes = 0;
+    }
+    template <class T>
+    T *as() const { return static_cast<T *>(ptr); }
+};
+
+struct TraceState {
+    Dag dag;                       // the DAG of the last traced run (records in dispatch order)
+    std::vector<TraceRec> recs;    // by dispatch index
+    bool valid = false;
+};
+
+struct State {
+    bool init = false;
+    int device = -1;
+    int sms = 0;
+    int occupancy = 1;
+    DevBuf tasks, counters, status, ticket, trace, scratch, mat, smat, kbuf, probe;
+    std::map<std::tuple<int, int, int, int, int, int, unsigned>, std::shared_ptr<Dag>> dags;
+    unsigned long long uploaded = 0;    // uid of the DAG whose records are on the device
+    unsigned long long next_uid = 1;
+    TraceState last_trace;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+};
+State g;
+
+int set_status(palial_status *st, int code, const char *fmt = nullptr, ...) {
+    if (st) {
+        st->code = code;
+        if (fmt) {
+            va_list ap;
+            va_start(ap, fmt);
+            vsnprintf(st->message, sizeof st->message, fmt, ap);
+            va_end(ap);
+        }
+    }
+    return code;
+}
+
+int cuda_fail(palial_status *st, cudaError_t e, const char *what) {
+    if (st) st->cuda_error = (int)e;
+    return set_status(st, PALIAL_ERR_CUDA, "%s: %s", what, cudaGetErrorString(e));
+}
+
+#define CK(call, what)                                    \
+    do {                                                  \
+        cudaError_t _e = (call);                          \
+        if (_e != cudaSuccess) return cuda_fail(st, _e, what); \
+    } while (0)
+
+int ensure_init(palial_status *st) {
+    if (g.init) {
+        cudaSetDevice(g.device);
+        return PALIAL_OK;
+    }
+    int rc = palial_gpu_init(0);
+    if (rc != PALIAL_OK) return set_status(st, rc, "no CUDA device available");
+    return PALIAL_OK;
+}
+
+int auto_block(int alg, int n, int nb) {
+    if (alg == 2) return nb;
+    // blocks of 256 keep the FP64 critical path short at the reference's NB = 512
+    int bs = std::min(nb, 256);
+    while (nb % bs) bs -= 64;
+    (void)n;
+    return std::max(64, bs);
+}
+
+std::shared_ptr<Dag> get_dag(int alg, int n, int nb, int bs, int priority, int workers, unsigned seed,
+                             palial_status *st) {
+    auto key = std::make_tuple(alg, n, nb, bs, priority, workers, seed);
+    auto it = g.dags.find(key);
+    if (it != g.dags.end()) return it->second;
+    auto d = std::make_shared<Dag>(build_dag(alg, n, nb, bs));
+    order_dag(*d, priority, workers, seed);
+    d->uid = g.next_uid++;
+    if (g.dags.size() > 16) g.dags.clear();
+    g.dags[key] = d;
+    (void)st;
+    return d;
+}
+
+}  // namespace
+
+extern "C" {
+
+void palial_opts_default(palial_opts *o) {
+    if (!o) return;
+    memset(o, 0, sizeof *o);
+}
+
+const char *palial_gpu_error_string(int code) {
+    switch (code) {
+        case PALIAL_OK: return "ok";
+        case PALIAL_ERR_ARG: return "bad argument";
+        case PALIAL_ERR_CUDA: return "CUDA error";
+        case PALIAL_ERR_NOT_SPD: return "matrix is not positive definite";
+        case PALIAL_ERR_TIMEOUT: return "device dependency wait timed out";
+        case PALIAL_ERR_NO_DEVICE: return "no CUDA device";
+        case PALIAL_ERR_NOT_CONVERGED: return "iterative refinement did not converge";
+        case PALIAL_ERR_NOMEM: return "device allocation failed";
+        case PALIAL_WARN_ZERO_PIVOT: return "exact zero pivot met and skipped";
+        default: return "unknown";
+    }
+}
+
+int palial_gpu_init(int device) {
+    if (g.init && g.device == device) return PALIAL_OK;
+    int count = 0;
+    if (cudaGetDeviceCount(&count) != cudaSuccess || count <= device || device < 0) {
+        cudaGetLastError();
+        return PALIAL_ERR_NO_DEVICE;
+    }
+    if (cudaSetDevice(device) != cudaSuccess) return PALIAL_ERR_NO_DEVICE;
+    cudaDeviceProp prop;
+    if (cudaGetDeviceProperties(&prop, device) != cudaSuccess) return PALIAL_ERR_NO_DEVICE;
+    g.device = device;
+    g.sms = prop.multiProcessorCount;
+    if (sched_configure() != cudaSuccess) return PALIAL_ERR_CUDA;
+    g.occupancy = std::max(1, sched_occupancy());
+    if (!g.ev0) cudaEventCreate(&g.ev0);
+    if (!g.ev1) cudaEventCreate(&g.ev1);
+    g.init = true;
+    return PALIAL_OK;
+}
+
+int palial_gpu_finalize(void) {
+    if (!g.init) return PALIAL_OK;
+    for (DevBuf *b : {&g.tasks, &g.counters, &g.status, &g.ticket, &g.trace, &g.scratch, &g.mat, &g.smat, &g.kbuf,
+                      &g.probe})
+        b->release();
+    g.dags.clear();
+    g.uploaded = 0;
+    return PALIAL_OK;
+}
+
+int palial_gpu_sm_count(void) { return g.init ? g.sms : 0; }
+
+int palial_gpu_factor_dev(int alg, double *dA, double *dS, int n, int nb, const palial_opts *opts,
+                          palial_status *st, void *stream) {
+    palial_opts o;
+    palial_opts_default(&o);
+    if (opts) o = *opts;
+    if (st) {
+        memset(st, 0, sizeof *st);
+    }
+    if (alg < 0 || alg > 2) return set_status(st, PALIAL_ERR_ARG, "unknown algorithm %d", alg);
+    if (n <= 0 || nb <= 0 || n % nb) return set_status(st, PALIAL_ERR_ARG, "N %% NB != 0 (N=%d, NB=%d)", n, nb);
+    if (nb % 64) return set_status(st, PALIAL_ERR_ARG, "NB must be a multiple of 64 (NB=%d)", nb);
+    if (n / nb > 65535) return set_status(st, PALIAL_ERR_ARG, "too many tiles");
+    if (!dA || (alg == 2 && !dS)) return set_status(st, PALIAL_ERR_ARG, "NULL matrix");
+    int rc = ensure_init(st);
+    if (rc) return rc;
+    const int bs = o.block > 0 ? o.block : auto_block(alg, n, nb);
+    if (alg != 2 && (bs % 64 || nb % bs)) return set_status(st, PALIAL_ERR_ARG, "block %d must divide NB and be a multiple of 64", bs);
+    int sms = g.sms;
+    if (o.max_sms > 0) sms = std::min(sms, o.max_sms);
+    int wps = o.workers_per_sm > 0 ? std::min(o.workers_per_sm, g.occupancy) : 1;
+    const int workers = sms * wps;
+    std::shared_ptr<Dag> dag;
+    try {
+        dag = get_dag(alg, n, nb, bs, o.priority, workers, o.shuffle_seed, st);
+    } catch (const std::exception &ex) {
+        return set_status(st, PALIAL_ERR_ARG, "%s", ex.what());
+    }
+    const int ntasks = (int)dag->records.size();
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    void *old_tasks = g.tasks.ptr;
+    CK(g.tasks.ensure(sizeof(Task) * (size_t)std::max(1, ntasks)), "alloc tasks");
+    if (g.tasks.ptr != old_tasks) g.uploaded = 0;  // reallocated: contents gone
+    if (g.uploaded != dag->uid) {
+        g.uploaded = 0;
+        CK(cudaMemcpy(g.tasks.ptr, dag->records.data(), sizeof(Task) * ntasks, cudaMemcpyHostToDevice), "upload tasks");
+        g.uploaded = dag->uid;
+    }
+    // one spare counter past the objects: nothing ever signals it (used by the stall test)
+    CK(g.counters.ensure(sizeof(unsigned) * (size_t)(dag->nobj + 1)), "alloc counters");
+    CK(g.status.ensure(sizeof(int) * ST_NSLOTS + 64), "alloc status");
+    CK(g.ticket.ensure(64), "alloc ticket");
+    long long per_worker = 0;
+    const long long scr = sched_scratch_doubles(alg, n, nb, dag->bs, workers, &per_worker);
+    CK(g.scratch.ensure(sizeof(double) * (size_t)std::max<long long>(1, scr)), "alloc scratch");
+    if (o.trace) CK(g.trace.ensure(sizeof(TraceRec) * (size_t)ntasks), "alloc trace");
+    CK(cudaMemsetAsync(g.counters.ptr, 0, sizeof(unsigned) * (dag->nobj + 1), s), "clear counters");
+    // Fault injection for tests (opts.reserved[0] = r + 1): record r additionally waits on the
+    // spare counter, which nothing signals, so its wait must end by deadline with
+    // PALIAL_ERR_TIMEOUT.  The uploaded copy is patched and restored afterwards.
+    const int stall = o.reserved[0] - 1;
+    Task saved{};
+    if (stall >= 0 && stall < ntasks) {
+        saved = dag->records[stall];
+        Task t = saved;
+        if (t.nwait < 3) {
+            t.wait_obj[t.nwait] = (uint32_t)dag->nobj;
+            t.wait_cnt[t.nwait] = 1;
+            t.nwait++;
+        } else {
+            t.wait_obj[2] = (uint32_t)dag->nobj;
+            t.wait_cnt[2] = 1;
+        }
+        CK(cudaMemcpy(g.tasks.as<Task>() + stall, &t, sizeof(Task), cudaMemcpyHostToDevice), "inject stall");
+    }
+    CK(cudaMemsetAsync(g.status.ptr, 0, sizeof(int) * ST_NSLOTS, s), "clear status");
+    CK(cudaMemsetAsync(g.ticket.ptr, 0, 64, s), "clear ticket");
+
+    SchedParams p{};
+    p.tasks = g.tasks.as<Task>();
+    p.ntasks = ntasks;
+    p.ticket = g.ticket.as<unsigned>();
+    p.counters = g.counters.as<unsigned>();
+    p.status = g.status.as<int>();
+    p.trace = o.trace ? g.trace.as<TraceRec>() : nullptr;
+    p.A = dA;
+    p.S = dS;
+    p.scratch = g.scratch.as<double>();
+    p.scratch_per_worker = per_worker;
+    p.n = n;
+    p.nb = nb;
+    p.bs = dag->bs;
+    const double to = o.timeout_s > 0 ? o.timeout_s : 120.0;
+    p.timeout_ns = (unsigned long long)(to * 1e9);
+
+    const auto w0 = std::chrono::steady_clock::now();
+    CK(cudaEventRecord(g.ev0, s), "event");
+    CK(sched_launch(p, workers, s), "launch scheduler");
+    CK(cudaEventRecord(g.ev1, s), "event");
+    CK(cudaEventSynchronize(g.ev1), "scheduler run");
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, g.ev0, g.ev1);
+    int hs[ST_NSLOTS];
+    CK(cudaMemcpy(hs, g.status.ptr, sizeof hs, cudaMemcpyDeviceToHost), "read status");
+    unsigned tick = 0;
+    CK(cudaMemcpy(&tick, g.ticket.ptr, sizeof tick, cudaMemcpyDeviceToHost), "read ticket");
+    if (stall >= 0 && stall < ntasks)
+        CK(cudaMemcpy(g.tasks.as<Task>() + stall, &saved, sizeof(Task), cudaMemcpyHostToDevice), "restore record");
+    const auto w1 = std::chrono::steady_clock::now();
+    if (st) {
+        st->ntasks = std::min<long long>(tick, ntasks);
+        st->seconds = ms * 1e-3;
+        st->total_seconds = std::chrono::duration<double>(w1 - w0).count();
+        st->tflops = algorithmic_flops(alg, n) / std::max(1e-12, st->seconds) * 1e-12;
+        st->task = hs[ST_TASK];
+        st->tile_m = hs[ST_M];
+        st->tile_n = hs[ST_N];
+        st->column = hs[ST_COL];
+    }
+    if (o.trace && hs[ST_CODE] == 0) {
+        g.last_trace.dag = *dag;
+        g.last_trace.recs.resize(ntasks);
+        CK(cudaMemcpy(g.last_trace.recs.data(), g.trace.ptr, sizeof(TraceRec) * ntasks, cudaMemcpyDeviceToHost),
+           "read trace");
+        g.last_trace.valid = true;
+    }
+    if (hs[ST_CODE] == PALIAL_ERR_NOT_SPD)
+        return set_status(st, PALIAL_ERR_NOT_SPD, "non-positive pivot in tile (%d,%d) column %d", hs[ST_M], hs[ST_N],
+                          hs[ST_COL]);
+    if (hs[ST_CODE] == PALIAL_ERR_TIMEOUT)
+        return set_status(st, PALIAL_ERR_TIMEOUT, "dependency wait timed out in task %d (object %d)", hs[ST_TASK],
+                          hs[ST_COL]);
+    if (hs[ST_CODE] != 0) return set_status(st, hs[ST_CODE], "device error %d", hs[ST_CODE]);
+    if (hs[ST_ZEROPIV]) return set_status(st, PALIAL_WARN_ZERO_PIVOT, "exact zero pivot skipped");
+    return set_status(st, PALIAL_OK);
+}
+
+static int factor_host(int alg, const palial_desc *A, const palial_desc *S, int *ipiv, const palial_opts *opts,
+                       palial_status *st) {
+    if (st) memset(st, 0, sizeof *st);
+    if (!A || !A->matrix) return set_status(st, PALIAL_ERR_ARG, "NULL descriptor");
+    if (alg == 2 && (!S || !S->matrix)) return set_status(st, PALIAL_ERR_ARG, "QR needs the S workspace");
+    const int n = A->matrix_size, nb = A->tile_size;
+    if (n <= 0 || nb <= 0 || n % nb) return set_status(st, PALIAL_ERR_ARG, "N %% NB != 0 (N=%d, NB=%d)", n, nb);
+    if (alg == 2 && (S->matrix_size != n || S->tile_size != nb))
+        return set_status(st, PALIAL_ERR_ARG, "S must have the same N and NB as A");
+    int rc = ensure_init(st);
+    if (rc) return rc;
+    const auto w0 = std::chrono::steady_clock::now();
+    const size_t bytes = sizeof(double) * (size_t)n * n;
+    CK(g.mat.ensure(bytes), "alloc matrix");
+    CK(cudaMemcpy(g.mat.ptr, A->matrix, bytes, cudaMemcpyHostToDevice), "copy A to device");
+    double *dS = nullptr;
+    if (alg == 2) {
+        CK(g.smat.ensure(bytes), "alloc S");
+        CK(cudaMemcpy(g.smat.ptr, S->matrix, bytes, cudaMemcpyHostToDevice), "copy S to device");
+        dS = g.smat.as<double>();
+    }
+    rc = palial_gpu_factor_dev(alg, g.mat.as<double>(), dS, n, nb, opts, st, nullptr);
+    if (rc < 0 && rc != PALIAL_ERR_NOT_SPD) return rc;
+    CK(cudaMemcpy(A->matrix, g.mat.ptr, bytes, cudaMemcpyDeviceToHost), "copy A to host");
+    if (alg == 2) CK(cudaMemcpy(S->matrix, g.smat.ptr, bytes, cudaMemcpyDeviceToHost), "copy S to host");
+    if (ipiv)
+        for (int i = 0; i < n; i++) ipiv[i] = i + 1;
+    if (st) st->total_seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - w0).count();
+    return rc;
+}
+
+int palial_gpu_cholesky(const palial_desc *A, const palial_opts *opts, palial_status *st) {
+    return factor_host(0, A, nullptr, nullptr, opts, st);
+}
+int palial_gpu_lu(const palial_desc *A, int *ipiv, const palial_opts *opts, palial_status *st) {
+    return factor_host(1, A, nullptr, ipiv, opts, st);
+}
+int palial_gpu_qr(const palial_desc *A, const palial_desc *S, const palial_opts *opts, palial_status *st) {
+    return factor_host(2, A, S, nullptr, opts, st);
+}
+
+// ---- single-tile kernels ----------------------------------------------------------------
+static int tile_call(int type, int nb, int ld, double *p0, double *p1, double *p2, double *p3) {
+    palial_status *st = nullptr;
+    int rc = ensure_init(nullptr);
+    if (rc) return rc;
+    if (nb <= 0 || nb % 64 || ld < nb) return PALIAL_ERR_ARG;
+    // scratch: 2 inverse sets of nb/64 blocks + 2 strips of nb x 64
+    const size_t need = sizeof(double) * ((size_t)2 * (nb / 64) * 4096 + (size_t)2 * nb * 64);
+    CK(g.scratch.ensure(need), "alloc scratch");
+    CK(g.status.ensure(sizeof(int) * ST_NSLOTS + 64), "alloc status");
+    CK(cudaMemset(g.status.ptr, 0, sizeof(int) * ST_NSLOTS), "clear status");
+    CK(tile_task_launch(type, nb, ld, p0, p1, p2, p3, g.scratch.as<double>(), g.status.as<int>(), nullptr), "launch");
+    CK(cudaDeviceSynchronize(), "tile kernel");
+    int hs[ST_NSLOTS];
+    CK(cudaMemcpy(hs, g.status.ptr, sizeof hs, cudaMemcpyDeviceToHost), "status");
+    if (hs[ST_CODE]) return hs[ST_CODE];
+    if (hs[ST_ZEROPIV]) return PALIAL_WARN_ZERO_PIVOT;
+    return PALIAL_OK;
+}
+
+int palial_gpu_tile_dpotrf(int nb, double *dA, int lda) { return tile_call(T_POTRF, nb, lda, dA, 0, 0, 0); }
+int palial_gpu_tile_dgetrf(int nb, double *dA, int lda) { return tile_call(T_GETRF, nb, lda, dA, 0, 0, 0); }
+int palial_gpu_tile_dtrsm(int kind, int nb, const double *dT, double *dB, int lda) {
+    const int ty = kind == 0 ? T_TRSM_LUT : kind == 1 ? T_TRSM_RUN : kind == 2 ? T_TRSM_LLU : -1;
+    if (ty < 0) return PALIAL_ERR_ARG;
+    return tile_call(ty, nb, lda, const_cast<double *>(dT), dB, 0, 0);
+}
+int palial_gpu_tile_dsyrk(int nb, const double *dA, double *dC, int lda) {
+    return tile_call(T_SYRK, nb, lda, const_cast<double *>(dA), dC, 0, 0);
+}
+int palial_gpu_tile_dgemm(int kind, int nb, const double *dA, const double *dB, double *dC, int lda) {
+    if (kind != 0 && kind != 1) return PALIAL_ERR_ARG;
+    return tile_call(kind == 0 ? T_GEMM_TN : T_GEMM_NN, nb, lda, const_cast<double *>(dA), const_cast<double *>(dB),
+                     dC, 0);
+}
+int palial_gpu_tile_dgeqrt(int nb, double *dA, double *dT, int lda) {
+    return tile_call(T_GEQRT, nb, lda, dA, dT, 0, 0);
+}
+int palial_gpu_tile_dormqr(int nb, const double *dV, const double *dT, double *dC, int lda) {
+    return tile_call(T_UNMQR, nb, lda, const_cast<double *>(dV), const_cast<double *>(dT), dC, 0);
+}
+int palial_gpu_tile_dtsqrt(int nb, double *dA1, double *dA2, double *dT, int lda) {
+    return tile_call(T_TSQRT, nb, lda, dA1, dA2, dT, 0);
+}
+int palial_gpu_tile_dtsmqr(int nb, double *dA1, double *dA2, const double *dV, const double *dT, int lda) {
+    return tile_call(T_TSMQR, nb, lda, dA1, dA2, const_cast<double *>(dV), const_cast<double *>(dT));
+}
+
+// ---- generators --------------------------------------------------------------------------
+int palial_gpu_gen_uniform(double *dA, int n, int nb, uint64_t seed, void *stream) {
+    palial_status *st = nullptr;
+    int rc = ensure_init(nullptr);
+    if (rc) return rc;
+    if (!dA || n <= 0 || nb <= 0 || n % nb) return PALIAL_ERR_ARG;
+    CK(launch_gen_uniform(dA, n, nb, seed, static_cast<cudaStream_t>(stream)), "gen uniform");
+    return PALIAL_OK;
+}
+
+int palial_gpu_gen_spd(double *dA, int n, int nb, uint64_t seed, void *stream) {
+    palial_status *st = nullptr;
+    int rc = ensure_init(nullptr);
+    if (rc) return rc;
+    if (!dA || n <= 0 || nb <= 0 || n % nb || n % 64) return PALIAL_ERR_ARG;
+    CK(g.kbuf.ensure((size_t)n * n), "alloc K");
+    CK(launch_gen_spd(dA, n, nb, seed, g.kbuf.as<int8_t>(), static_cast<cudaStream_t>(stream)), "gen spd");
+    return PALIAL_OK;
+}
+
+int palial_gpu_gen_refpattern(double *dA, int n, int nb, uint64_t seed, void *stream) {
+    palial_status *st = nullptr;
+    int rc = ensure_init(nullptr);
+    if (rc) return rc;
+    if (!dA || n <= 0 || nb <= 0 || n % nb) return PALIAL_ERR_ARG;
+    CK(launch_gen_refpattern(dA, n, nb, seed, static_cast<cudaStream_t>(stream)), "gen pattern");
+    return PALIAL_OK;
+}
+
+int palial_gpu_generate(int kind, uint64_t seed, const palial_desc *A) {
+    palial_status *st = nullptr;
+    if (!A || !A->matrix) return PALIAL_ERR_ARG;
+    const int n = A->matrix_size, nb = A->tile_size;
+    if (n <= 0 || nb <= 0 || n % nb) return PALIAL_ERR_ARG;
+    int rc = ensure_init(nullptr);
+    if (rc) return rc;
+    const size_t bytes = sizeof(double) * (size_t)n * n;
+    CK(g.mat.ensure(bytes), "alloc matrix");
+    if (kind == 0) rc = palial_gpu_gen_uniform(g.mat.as<double>(), n, nb, seed, nullptr);
+    else if (kind == 1) rc = palial_gpu_gen_spd(g.mat.as<double>(), n, nb, seed, nullptr);
+    else if (kind == 2) rc = palial_gpu_gen_refpattern(g.mat.as<double>(), n, nb, seed, nullptr);
+    else return PALIAL_ERR_ARG;
+    if (rc) return rc;
+    CK(cudaMemcpy(A->matrix, g.mat.ptr, bytes, cudaMemcpyDeviceToHost), "copy to host");
+    return PALIAL_OK;
+}
+
+// ---- residual probe ------------------------------------------------------------------------
+int palial_gpu_residual_probe(int alg, const double *dA0, const double *dF, const double *dS, int n, int nb,
+                              int nprobe, uint64_t seed, double *out) {
+    palial_status *st = nullptr;
+    (void)dS;
+    int rc = ensure_init(nullptr);
+    if (rc) return rc;
+    if (!dA0 || !dF || !out || n % 64 || nprobe <= 0 || nprobe > 64) return PALIAL_ERR_ARG;
+    const size_t v = (size_t)n * nprobe;
+    CK(g.probe.ensure(sizeof(double) * (4 * v + 4096)), "alloc probe");
+    double *X = g.probe.as<double>(), *Y = X + v, *Z = Y + v, *W = Z + v, *part = W + v;
+    CK(launch_gen_dense(X, n, nprobe, seed, 5, nullptr), "probe gen");
+    // Y = A0 X (or A0^T A0 X for QR), Z = F(X)
+    if (alg == 0) {
+        CK(launch_tiled_mm(dA0, X, Y, n, nb, nprobe, 0, 0, nullptr), "A X");
+        CK(launch_tiled_mm(dF, X, W, n, nb, nprobe, 1, 0, nullptr), "U X");
+        CK(launch_tiled_mm(dF, W, Z, n, nb, nprobe, 1, 1, nullptr), "U^T U X");
+    } else if (alg == 1) {
+        CK(launch_tiled_mm(dA0, X, Y, n, nb, nprobe, 0, 0, nullptr), "A X");
+        CK(launch_tiled_mm(dF, X, W, n, nb, nprobe, 1, 0, nullptr), "U X");
+        CK(launch_tiled_mm(dF, W, Z, n, nb, nprobe, 2, 0, nullptr), "L U X");
+    } else {
+        // R^T R = A^T A: compare A^T (A X) with R^T (R X)
+        CK(launch_tiled_mm(dA0, X, W, n, nb, nprobe, 0, 0, nullptr), "A X");
+        CK(launch_tiled_mm(dA0, W, Y, n, nb, nprobe, 0, 1, nullptr), "A^T A X");
+        CK(launch_tiled_mm(dF, X, W, n, nb, nprobe, 1, 0, nullptr), "R X");
+        CK(launch_tiled_mm(dF, W, Z, n, nb, nprobe, 1, 1, nullptr), "R^T R X");
+    }
+    CK(launch_sub(Y, Z, W, (long long)v, nullptr), "diff");
+    const int blocks = 512;
+    std::vector<double> hp(blocks);
+    auto sumsq = [&](const double *p, long long len) -> double {
+        if (launch_sumsq(p, len, part, blocks, nullptr) != cudaSuccess) return NAN;
+        cudaMemcpy(hp.data(), part, sizeof(double) * blocks, cudaMemcpyDeviceToHost);
+        double s = 0;
+        for (double x : hp) s += x;
+        return s;
+    };
+    const double dn = sqrt(sumsq(W, (long long)v));
+    const double yn = sqrt(sumsq(Y, (long long)v));
+    CK(cudaGetLastError(), "probe");
+    *out = dn / yn;
+    return PALIAL_OK;
+}
+
+int palial_gpu_residual_host(int alg, const double *a0_host, const palial_desc *F, int nprobe, uint64_t seed,
+                             double *out) {
+    palial_status *st = nullptr;
+    if (!a0_host || !F || !F->matrix || !out) return PALIAL_ERR_ARG;
+    const int n = F->matrix_size, nb = F->tile_size;
+    int rc = ensure_init(nullptr);
+    if (rc) return rc;
+    const size_t bytes = sizeof(double) * (size_t)n * n;
+    DevBuf a0, f;
+    CK(a0.ensure(bytes), "alloc");
+    CK(f.ensure(bytes), "alloc");
+    CK(cudaMemcpy(a0.ptr, a0_host, bytes, cudaMemcpyHostToDevice), "copy");
+    CK(cudaMemcpy(f.ptr, F->matrix, bytes, cudaMemcpyHostToDevice), "copy");
+    rc = palial_gpu_residual_probe(alg, a0.as<double>(), f.as<double>(), nullptr, n, nb, nprobe, seed, out);
+    a0.release();
+    f.release();
+    return rc;
+}
+
+// ---- trace ----------------------------------------------------------------------------------
+long long palial_gpu_trace_count(void) {
+    return g.last_trace.valid ? (long long)g.last_trace.dag.logical.size() : 0;
+}
+
+int palial_gpu_trace_dump(const char *path, const char *csv_path) {
+    if (!g.last_trace.valid) return PALIAL_ERR_ARG;
+    const Dag &d = g.last_trace.dag;
+    const auto names = reference_names(d);
+    const size_t nl = d.logical.size();
+    std::vector<unsigned long long> t0(nl, ~0ull), t1(nl, 0);
+    for (size_t r = 0; r < d.records.size(); r++) {
+        const TraceRec &x = g.last_trace.recs[r];
+        const uint32_t l = d.rec_logical[r];
+        t0[l] = std::min(t0[l], x.t0);
+        t1[l] = std::max(t1[l], x.t1);
+    }
+    FILE *f = path ? fopen(path, "w") : stdout;
+    if (!f) return PALIAL_ERR_ARG;
+    for (size_t l = 0; l < nl; l++) fprintf(f, "%s, %f\n", names[l].c_str(), (double)(t1[l] - t0[l]) * 1e-6);
+    if (path) fclose(f);
+    if (csv_path) {
+        FILE *c = fopen(csv_path, "w");
+        if (!c) return PALIAL_ERR_ARG;
+        static const char *tn[] = {"potrf", "trsm", "syrk", "gemm", "getrf", "trsm", "trsm", "gemm",
+                                   "geqrt", "ormqr", "tsqrt", "tsmqr"};
+        fprintf(c, "dispatch,logical,name,type,k,m,n,part,nparts,t0_ns,t1_ns,smid,clk\n");
+        for (size_t r = 0; r < d.records.size(); r++) {
+            const TraceRec &x = g.last_trace.recs[r];
+            const Task &t = d.records[r];
+            fprintf(c, "%zu,%u,%s,%s,%d,%d,%d,%d,%d,%llu,%llu,%u,%lld\n", r, d.rec_logical[r],
+                    names[d.rec_logical[r]].c_str(), tn[t.type], t.k, t.m, t.n, t.part, t.nparts, x.t0, x.t1, x.smid,
+                    x.clk);
+        }
+        fclose(c);
+    }
+    return PALIAL_OK;
+}
+
+// ---- DAG (host only) ------------------------------------------------------------------------
+long long palial_dag_info(int alg, int n, int nb, int block, int priority, int nworkers, long long *type_counts,
+                          double *critical_path_s, double *makespan_s) {
+    try {
+        const int bs = block > 0 ? block : auto_block(alg, n, nb);
+        Dag d = build_dag(alg, n, nb, bs);
+        order_dag(d, priority, nworkers, 0);
+        if (type_counts) {
+            for (int i = 0; i < 16; i++) type_counts[i] = 0;
+            for (const auto &t : d.logical) type_counts[t.type]++;
+        }
+        if (critical_path_s) *critical_path_s = d.critical_path;
+        if (makespan_s) *makespan_s = d.sim_makespan;
+        return (long long)d.records.size();
+    } catch (const std::exception &) {
+        return -1;
+    }
+}
+
+int palial_dag_validate(int alg, int n, int nb, int block, int priority, int nworkers, unsigned int seed, char *msg,
+                        int msglen) {
+    try {
+        const int bs = block > 0 ? block : auto_block(alg, n, nb);
+        Dag d = build_dag(alg, n, nb, bs);
+        order_dag(d, priority, nworkers, seed);
+        const std::string r = validate_dag(d, nworkers, seed);
+        if (msg && msglen > 0) snprintf(msg, msglen, "%s", r.c_str());
+        return r.empty() ? 0 : 1;
+    } catch (const std::exception &ex) {
+        if (msg && msglen > 0) snprintf(msg, msglen, "%s", ex.what());
+        return -1;
+    }
+}
+
+int palial_gpu_clock_report(palial_clock_report *out) {
+    if (!out) return PALIAL_ERR_ARG;
+    out->sm_mhz_start = out->sm_mhz_end = out->sm_mhz_max = -1;
+    out->throttle_reasons = -1;
+    out->sm_mhz_device = -1;
+    if (g.last_trace.valid) {
+        double cyc = 0, ns = 0;
+        for (const auto &r : g.last_trace.recs) {
+            cyc += (double)r.clk;
+            ns += (double)(r.t1 - r.t0);
+        }
+        if (ns > 0) out->sm_mhz_device = cyc / ns * 1e3;
+    }
+    return PALIAL_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,65 @@
+"""Host logic of the device scheduler: task counts, dependence validity, emulation with
+random durations, and the C ABI exports.  No GPU needed (no compute calls)."""
+import re
+import os
+
+import pytest
+
+import palial_gb300 as P
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def test_library_exports_every_declared_symbol():
+    names = set()
+    for hdr in os.listdir(os.path.join(ROOT, "include")):
+        if hdr.endswith(".h"):
+            src = open(os.path.join(ROOT, "include", hdr)).read()
+            src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+            # prototypes only (header-defined helpers of palial_entry.h are not exports)
+            names |= set(re.findall(r"\b(palial_\w+)\s*\([^;{)]*\)\s*;", src))
+    assert names
+    lib = P.lib()
+    missing = [n for n in sorted(names) if not hasattr(lib, n)]
+    assert not missing, missing
+
+
+@pytest.mark.parametrize("mt", [1, 2, 3, 5, 8])
+def test_cholesky_task_counts(mt):
+    d = P.dag_info("cholesky", 512 * mt, 512, block=512)
+    c = d["type_counts"]
+    assert c[0] == mt and c[1] == mt * (mt - 1) // 2 and c[2] == mt * (mt - 1) // 2
+    assert c[3] == mt * (mt - 1) * (mt - 2) // 6
+
+
+@pytest.mark.parametrize("mt", [1, 2, 4, 7])
+def test_lu_task_counts(mt):
+    c = P.dag_info("lu", 256 * mt, 256, block=256)["type_counts"]
+    assert c[4] == mt and c[5] == mt * (mt - 1) // 2 and c[6] == mt * (mt - 1) // 2
+    assert c[7] == (mt - 1) * mt * (2 * mt - 1) // 6
+
+
+@pytest.mark.parametrize("mt", [1, 2, 4, 6])
+def test_qr_task_counts(mt):
+    c = P.dag_info("qr", 128 * mt, 128)["type_counts"]
+    assert c[8] == mt and c[9] == mt * (mt - 1) // 2 and c[10] == mt * (mt - 1) // 2
+    assert c[11] == sum((mt - 1 - k) ** 2 for k in range(mt))
+
+
+@pytest.mark.parametrize("alg", ["cholesky", "lu", "qr"])
+@pytest.mark.parametrize("priority", [0, 1])
+@pytest.mark.parametrize("workers", [1, 3, 152])
+def test_dag_validates(alg, priority, workers):
+    assert P.dag_validate(alg, 2048, 256, block=128 if alg != "qr" else 0, priority=priority,
+                          nworkers=workers, seed=workers) == ""
+
+
+def test_critical_path_order_beats_program_order_in_model():
+    a = P.dag_info("cholesky", 16384, 512, priority=0, nworkers=152)
+    b = P.dag_info("cholesky", 16384, 512, priority=1, nworkers=152)
+    assert a["makespan_s"] <= b["makespan_s"] * 1.0001
+
+
+def test_bad_sizes_rejected():
+    with pytest.raises(P.PalialError):
+        P.dag_info("cholesky", 1000, 512)
