@@ -373,8 +373,8 @@ static int tile_call(int type, int nb, int ld, double *p0, double *p1, double *p
     int rc = ensure_init(nullptr);
     if (rc) return rc;
     if (nb <= 0 || nb % 64 || ld < nb) return PALIAL_ERR_ARG;
-    // scratch: 2 inverse sets of nb/64 blocks + 2 strips of nb x 64
-    const size_t need = sizeof(double) * ((size_t)2 * (nb / 64) * 4096 + (size_t)2 * nb * 64);
+    // scratch: 2 strips of nb x 64 (QR update kernels)
+    const size_t need = sizeof(double) * ((size_t)2 * nb * 64);
     CK(g.scratch.ensure(need), "alloc scratch");
     CK(g.status.ensure(sizeof(int) * ST_NSLOTS + 64), "alloc status");
     CK(cudaMemset(g.status.ptr, 0, sizeof(int) * ST_NSLOTS), "clear status");

@@ -18,6 +18,7 @@ using namespace f64;
 
 // Dynamic shared memory layout of a worker (doubles):
 //   Ds[64][65] | Is[64][65] | U[union: gemm staging (2*KC*SP) or Bs[64][65]] | misc
+// (Is is spare room for a second 64x64 block.)
 constexpr int SM_DS = 0;
 constexpr int SM_IS = SM_DS + 64 * DP;
 constexpr int SM_U = SM_IS + 64 * DP;
@@ -49,84 +50,61 @@ __device__ __forceinline__ Worker make_worker(double *smem) {
 }
 
 // ---------------------------------------------------------------------------------------
-// 64x64 products with a shared-memory operand I (Is, column-major Is[c][r]).
-//   left:  B <- op(I) * B   (op = I^T if TR)      right: B <- B * I
-// B is a 64x64 block in global memory (ld).  Staged through w.Bs.
+// 64 x 64 triangular solves by substitution (the column-oriented order of BLAS dtrsm),
+// with the triangle in w.Ds (Ds[c][r] = T(r,c)) and the right-hand sides B (64 x 64, global,
+// ld) staged in w.Bs.  No explicit inverse: no-pivot LU can meet ill-conditioned diagonal
+// blocks, and substitution keeps the reference's backward error.
+//   KIND 0: U^T X = B (U upper, non-unit)   -- Cholesky TRSM (left, upper, trans)
+//   KIND 1: X U = B   (U upper, non-unit)   -- LU TRSM (right, upper, no-trans)
+//   KIND 2: L X = B   (L unit lower)        -- LU TRSM (left, lower, unit)
 // ---------------------------------------------------------------------------------------
-template <bool TR>
-__device__ void left_mul64(const Worker &w, double *B, int ld) {
+template <int KIND>
+__device__ void solve64(const Worker &w, double *B, int ld) {
+    // Bs[c][r] = B(r, c)
     for (int e = threadIdx.x; e < 4096; e += NT) {
         const int r = e & 63, c = e >> 6;
         w.Bs[c][r] = ldg(B + r + (size_t)c * ld);
     }
     __syncthreads();
-    const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
-    double acc[4][4] = {};
     for (int p = 0; p < 64; p++) {
-        double av[4], bv[4];
-#pragma unroll
-        for (int a = 0; a < 4; a++) {
-            const int i = ty * 4 + a;
-            av[a] = TR ? w.Is[i][p] : w.Is[p][i];  // op(I)(i,p)
+        if (KIND == 0) {
+            if (threadIdx.x < 64) w.Bs[threadIdx.x][p] = w.Bs[threadIdx.x][p] / w.Ds[p][p];
+            __syncthreads();
+            // rows i > p of every column c: B(i,c) -= U(p,i) X(p,c)
+            for (int e = threadIdx.x; e < 64 * 64; e += NT) {
+                const int i = e & 63, c = e >> 6;
+                if (i > p) w.Bs[c][i] = fma(-w.Ds[i][p], w.Bs[c][p], w.Bs[c][i]);
+            }
+        } else if (KIND == 1) {
+            // unknown column p: X(:,p) = B(:,p) / U(p,p); then B(:,q) -= X(:,p) U(p,q), q > p
+            if (threadIdx.x < 64) w.Bs[p][threadIdx.x] = w.Bs[p][threadIdx.x] / w.Ds[p][p];
+            __syncthreads();
+            for (int e = threadIdx.x; e < 64 * 64; e += NT) {
+                const int r = e & 63, q = e >> 6;
+                if (q > p) w.Bs[q][r] = fma(-w.Bs[p][r], w.Ds[q][p], w.Bs[q][r]);
+            }
+        } else {
+            for (int e = threadIdx.x; e < 64 * 64; e += NT) {
+                const int i = e & 63, c = e >> 6;
+                if (i > p) w.Bs[c][i] = fma(-w.Ds[p][i], w.Bs[c][p], w.Bs[c][i]);
+            }
         }
-#pragma unroll
-        for (int b = 0; b < 4; b++) bv[b] = w.Bs[tx * 4 + b][p];
-#pragma unroll
-        for (int a = 0; a < 4; a++)
-#pragma unroll
-            for (int b = 0; b < 4; b++) acc[a][b] = fma(av[a], bv[b], acc[a][b]);
+        __syncthreads();
     }
-    __syncthreads();
-#pragma unroll
-    for (int b = 0; b < 4; b++)
-#pragma unroll
-        for (int a = 0; a < 4; a++) B[(ty * 4 + a) + (size_t)(tx * 4 + b) * ld] = acc[a][b];
-    __syncthreads();
-}
-
-__device__ void right_mul64(const Worker &w, double *B, int ld) {
     for (int e = threadIdx.x; e < 4096; e += NT) {
         const int r = e & 63, c = e >> 6;
-        w.Bs[c][r] = ldg(B + r + (size_t)c * ld);
+        B[r + (size_t)c * ld] = w.Bs[c][r];
     }
-    __syncthreads();
-    const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
-    double acc[4][4] = {};
-    for (int p = 0; p < 64; p++) {
-        double av[4], bv[4];
-#pragma unroll
-        for (int a = 0; a < 4; a++) av[a] = w.Bs[p][ty * 4 + a];      // B(i,p)
-#pragma unroll
-        for (int b = 0; b < 4; b++) bv[b] = w.Is[tx * 4 + b][p];      // I(p,j)
-#pragma unroll
-        for (int a = 0; a < 4; a++)
-#pragma unroll
-            for (int b = 0; b < 4; b++) acc[a][b] = fma(av[a], bv[b], acc[a][b]);
-    }
-    __syncthreads();
-#pragma unroll
-    for (int b = 0; b < 4; b++)
-#pragma unroll
-        for (int a = 0; a < 4; a++) B[(ty * 4 + a) + (size_t)(tx * 4 + b) * ld] = acc[a][b];
-    __syncthreads();
-}
-
-__device__ void store_inv64(const Worker &w, double *dst) {
-    for (int e = threadIdx.x; e < 4096; e += NT) dst[e] = w.Is[e >> 6][e & 63];
-    __syncthreads();
-}
-__device__ void load_inv64(const Worker &w, const double *src) {
-    for (int e = threadIdx.x; e < 4096; e += NT) w.Is[e >> 6][e & 63] = ldg(src + e);
     __syncthreads();
 }
 
 // ---------------------------------------------------------------------------------------
 // POTRF (upper) of an n x n block, n multiple of 64.  Blocked by 64: factor the diagonal
-// block in shared memory, invert it (kept in dinv for the TRSM tasks), solve the row panel
-// with the inverse, then the upper-triangular rank-64 update of the trailing block.
+// block in shared memory, solve the row panel by substitution, then the upper-triangular
+// rank-64 update of the trailing block.
 // Returns -1, or the first column with a non-positive pivot.
 // ---------------------------------------------------------------------------------------
-__device__ int potrf_upper(const Worker &w, double *A, int n, int ld, double *dinv) {
+__device__ int potrf_upper(const Worker &w, double *A, int n, int ld) {
     for (int j0 = 0; j0 < n; j0 += 64) {
         double *D = A + j0 + (size_t)j0 * ld;
         load_diag64(w.Ds, D, ld);
@@ -136,10 +114,9 @@ __device__ int potrf_upper(const Worker &w, double *A, int n, int ld, double *di
             const int r = e & 63, c = e >> 6;
             if (r <= c) D[r + (size_t)c * ld] = w.Ds[c][r];
         }
-        tri_inv64<false, false>(w.Ds, w.Is);
-        if (dinv) store_inv64(w, dinv + (size_t)(j0 / 64) * 4096);
+        __syncthreads();
         if (j0 + 64 < n) {
-            for (int c0 = j0 + 64; c0 < n; c0 += 64) left_mul64<true>(w, A + j0 + (size_t)c0 * ld, ld);
+            for (int c0 = j0 + 64; c0 < n; c0 += 64) solve64<0>(w, A + j0 + (size_t)c0 * ld, ld);
             const int m = n - j0 - 64;
             const double *X = A + j0 + (size_t)(j0 + 64) * ld;
             cta_gemm<true, false, M_NONE, M_NONE, true>(m, m, 64, -1.0, X, ld, X, ld, 1.0,
@@ -152,11 +129,10 @@ __device__ int potrf_upper(const Worker &w, double *A, int n, int ld, double *di
 // ---------------------------------------------------------------------------------------
 // GETRF without pivoting (reference src/srclu/dgetrf_no_pivot.h:11-57 rule: scale the column
 // by the reciprocal pivot when |pivot| > DBL_MIN, divide otherwise, skip an exact zero),
-// blocked by 64 columns: panel LU in global memory, U12 = L11^-1 A12, A22 -= L21 U12.
-// dinvL/dinvU receive the inverses of the 64x64 diagonal blocks of L (unit) and U.
-// Returns 1 if an exact zero pivot was met, else 0.
+// blocked by 64 columns: panel LU in global memory, U12 = L11^-1 A12 by substitution,
+// A22 -= L21 U12.  Returns 1 if an exact zero pivot was met, else 0.
 // ---------------------------------------------------------------------------------------
-__device__ int getrf_nopiv(const Worker &w, double *A, int n, int ld, double *dinvL, double *dinvU) {
+__device__ int getrf_nopiv(const Worker &w, double *A, int n, int ld) {
     const double sfmin = 2.2250738585072014e-308;  // dlamch('S') for IEEE double
     int zero_piv = 0;
     for (int j0 = 0; j0 < n; j0 += 64) {
@@ -183,14 +159,8 @@ __device__ int getrf_nopiv(const Worker &w, double *A, int n, int ld, double *di
         }
         double *D = A + j0 + (size_t)j0 * ld;
         load_diag64(w.Ds, D, ld);
-        tri_inv64<true, true>(w.Ds, w.Is);
-        if (dinvL) store_inv64(w, dinvL + (size_t)(j0 / 64) * 4096);
         if (j0 + 64 < n) {
-            for (int c0 = j0 + 64; c0 < n; c0 += 64) left_mul64<false>(w, A + j0 + (size_t)c0 * ld, ld);
-        }
-        tri_inv64<false, false>(w.Ds, w.Is);
-        if (dinvU) store_inv64(w, dinvU + (size_t)(j0 / 64) * 4096);
-        if (j0 + 64 < n) {
+            for (int c0 = j0 + 64; c0 < n; c0 += 64) solve64<2>(w, A + j0 + (size_t)c0 * ld, ld);
             const int m = n - j0 - 64;
             cta_gemm<false, false>(m, m, 64, -1.0, A + (j0 + 64) + (size_t)j0 * ld, ld,
                                    A + j0 + (size_t)(j0 + 64) * ld, ld, 1.0,
@@ -201,34 +171,34 @@ __device__ int getrf_nopiv(const Worker &w, double *A, int n, int ld, double *di
 }
 
 // ---------------------------------------------------------------------------------------
-// Triangular solves on a 64-wide strip, with the diagonal-block inverses made by POTRF /
-// GETRF.  n = block size, B = strip origin.
+// Triangular solves on a 64-wide strip: GEMM updates from the solved blocks, then
+// substitution against the diagonal 64x64 block.  n = block size, B = strip origin.
 // ---------------------------------------------------------------------------------------
 // X = U^-T B (U upper, B n x 64): row blocks top-down.
-__device__ void trsm_lut(const Worker &w, const double *U, double *B, int n, int ld, const double *dinv) {
+__device__ void trsm_lut(const Worker &w, const double *U, double *B, int n, int ld) {
     for (int rb = 0; rb < n; rb += 64) {
         if (rb > 0)
             cta_gemm<true, false>(64, 64, rb, -1.0, U + (size_t)rb * ld, ld, B, ld, 1.0, B + rb, ld, w.gsm);
-        load_inv64(w, dinv + (size_t)(rb / 64) * 4096);
-        left_mul64<true>(w, B + rb, ld);
+        load_diag64(w.Ds, U + rb + (size_t)rb * ld, ld);
+        solve64<0>(w, B + rb, ld);
     }
 }
 // X = B U^-1 (B 64 x n row strip): column blocks left to right.
-__device__ void trsm_run(const Worker &w, const double *U, double *B, int n, int ld, const double *dinv) {
+__device__ void trsm_run(const Worker &w, const double *U, double *B, int n, int ld) {
     for (int cb = 0; cb < n; cb += 64) {
         if (cb > 0)
             cta_gemm<false, false>(64, 64, cb, -1.0, B, ld, U + (size_t)cb * ld, ld, 1.0, B + (size_t)cb * ld, ld,
                                    w.gsm);
-        load_inv64(w, dinv + (size_t)(cb / 64) * 4096);
-        right_mul64(w, B + (size_t)cb * ld, ld);
+        load_diag64(w.Ds, U + cb + (size_t)cb * ld, ld);
+        solve64<1>(w, B + (size_t)cb * ld, ld);
     }
 }
 // X = L^-1 B (L unit lower, B n x 64): row blocks top-down.
-__device__ void trsm_llu(const Worker &w, const double *L, double *B, int n, int ld, const double *dinv) {
+__device__ void trsm_llu(const Worker &w, const double *L, double *B, int n, int ld) {
     for (int rb = 0; rb < n; rb += 64) {
         if (rb > 0) cta_gemm<false, false>(64, 64, rb, -1.0, L + rb, ld, B, ld, 1.0, B + rb, ld, w.gsm);
-        load_inv64(w, dinv + (size_t)(rb / 64) * 4096);
-        left_mul64<false>(w, B + rb, ld);
+        load_diag64(w.Ds, L + rb + (size_t)rb * ld, ld);
+        solve64<2>(w, B + rb, ld);
     }
 }
 
@@ -431,14 +401,6 @@ __device__ __forceinline__ double *tile_ptr(double *A, int n, int nb, int m, int
     return A + (size_t)nb * nb * ((size_t)m + (size_t)(n / nb) * k);
 }
 
-// diagonal-inverse store: per diagonal block k of size bs: (bs/64) inverses of 64x64.
-// L inverses follow all U inverses.
-__device__ __forceinline__ double *dinv_ptr(const SchedParams &p, int k, bool lower) {
-    const long long per = (long long)(p.bs / 64) * 4096;
-    const long long nblk = p.n / p.bs;
-    return p.scratch + (lower ? nblk * per : 0) + (long long)k * per;
-}
-
 __device__ void record_error(const SchedParams &p, int code, int task, int m, int n, int col) {
     if (atomicCAS(p.status + ST_CODE, 0, code) == 0) {
         p.status[ST_TASK] = task;
@@ -455,7 +417,7 @@ __device__ void run_task(const SchedParams &p, const Worker &w, const Task &t, i
     switch (t.type) {
         case T_POTRF: {
             double *D = block_ptr(A, n, nb, bs, t.k, t.k);
-            const int bad = potrf_upper(w, D, bs, ld, dinv_ptr(p, t.k, false));
+            const int bad = potrf_upper(w, D, bs, ld);
             if (bad >= 0 && threadIdx.x == 0) {
                 const long long r = (long long)t.k * bs + bad;
                 record_error(p, -3 /*PALIAL_ERR_NOT_SPD*/, tid, (int)(r / nb), (int)(r / nb), (int)(r % nb));
@@ -465,7 +427,7 @@ __device__ void run_task(const SchedParams &p, const Worker &w, const Task &t, i
         case T_TRSM_LUT: {
             const double *U = block_ptr(A, n, nb, bs, t.k, t.k);
             double *B = block_ptr(A, n, nb, bs, t.k, t.m) + (size_t)t.part * 64 * ld;
-            trsm_lut(w, U, B, bs, ld, dinv_ptr(p, t.k, false));
+            trsm_lut(w, U, B, bs, ld);
             break;
         }
         case T_SYRK: {
@@ -487,20 +449,20 @@ __device__ void run_task(const SchedParams &p, const Worker &w, const Task &t, i
         }
         case T_GETRF: {
             double *D = block_ptr(A, n, nb, bs, t.k, t.k);
-            const int z = getrf_nopiv(w, D, bs, ld, dinv_ptr(p, t.k, true), dinv_ptr(p, t.k, false));
+            const int z = getrf_nopiv(w, D, bs, ld);
             if (z && threadIdx.x == 0) atomicOr(p.status + ST_ZEROPIV, 1);
             break;
         }
         case T_TRSM_RUN: {
             const double *U = block_ptr(A, n, nb, bs, t.k, t.k);
             double *B = block_ptr(A, n, nb, bs, t.m, t.k) + t.part * 64;
-            trsm_run(w, U, B, bs, ld, dinv_ptr(p, t.k, false));
+            trsm_run(w, U, B, bs, ld);
             break;
         }
         case T_TRSM_LLU: {
             const double *L = block_ptr(A, n, nb, bs, t.k, t.k);
             double *B = block_ptr(A, n, nb, bs, t.k, t.n) + (size_t)t.part * 64 * ld;
-            trsm_llu(w, L, B, bs, ld, dinv_ptr(p, t.k, true));
+            trsm_llu(w, L, B, bs, ld);
             break;
         }
         case T_GEMM_NN: {
@@ -544,9 +506,8 @@ __global__ void __launch_bounds__(NT, 1) sched_f64_kernel(SchedParams p) {
     extern __shared__ __align__(16) double smem[];
     Worker w = make_worker(smem);
     __shared__ int s_task, s_abort;
-    // worker-private scratch after the diagonal-inverse store
-    const long long dinv_doubles = 2LL * (p.n / p.bs) * (p.bs / 64) * 4096;
-    double *wscr = p.scratch + dinv_doubles + (long long)blockIdx.x * p.scratch_per_worker;
+    // worker-private scratch (QR strips)
+    double *wscr = p.scratch + (long long)blockIdx.x * p.scratch_per_worker;
     for (;;) {
         if (threadIdx.x == 0) {
             int tk = p.ntasks;
@@ -600,29 +561,18 @@ __global__ void __launch_bounds__(NT, 1) sched_f64_kernel(SchedParams p) {
 // ---------------------------------------------------------------------------------------
 // One whole tile task (all strips) on one CTA, for the single-tile C ABI entry points.
 // p0..p3 are the tile arguments in the order of the reference's tile kernels; ld >= nb.
-// scratch: 2 * (nb/64) inverses of 64x64, then two nb x 64 strips.
+// scratch: two nb x 64 strips (QR update kernels).
 // ---------------------------------------------------------------------------------------
-__device__ void make_inverses(const Worker &w, const double *T, int nb, int ld, double *dst, bool lower) {
-    for (int j0 = 0; j0 < nb; j0 += 64) {
-        load_diag64(w.Ds, T + j0 + (size_t)j0 * ld, ld);
-        if (lower) tri_inv64<true, true>(w.Ds, w.Is);
-        else tri_inv64<false, false>(w.Ds, w.Is);
-        store_inv64(w, dst + (size_t)(j0 / 64) * 4096);
-    }
-}
-
 __global__ void __launch_bounds__(NT, 1) tile_task_kernel(int type, int nb, int ld, double *p0, double *p1,
                                                           double *p2, double *p3, double *scratch, int *status) {
     extern __shared__ __align__(16) double smem[];
     Worker w = make_worker(smem);
-    double *dinvU = scratch;
-    double *dinvL = scratch + (size_t)(nb / 64) * 4096;
-    double *W = scratch + (size_t)2 * (nb / 64) * 4096;
+    double *W = scratch;
     double *W2 = W + (size_t)nb * 64;
     const int parts = nb / 64;
     switch (type) {
         case T_POTRF: {
-            const int bad = potrf_upper(w, p0, nb, ld, dinvU);
+            const int bad = potrf_upper(w, p0, nb, ld);
             if (bad >= 0 && threadIdx.x == 0) {
                 status[ST_COL] = bad;
                 status[ST_CODE] = -3;
@@ -630,21 +580,18 @@ __global__ void __launch_bounds__(NT, 1) tile_task_kernel(int type, int nb, int 
             break;
         }
         case T_GETRF: {
-            const int z = getrf_nopiv(w, p0, nb, ld, dinvL, dinvU);
+            const int z = getrf_nopiv(w, p0, nb, ld);
             if (z && threadIdx.x == 0) status[ST_ZEROPIV] = 1;
             break;
         }
         case T_TRSM_LUT:
-            make_inverses(w, p0, nb, ld, dinvU, false);
-            for (int q = 0; q < parts; q++) trsm_lut(w, p0, p1 + (size_t)q * 64 * ld, nb, ld, dinvU);
+            for (int q = 0; q < parts; q++) trsm_lut(w, p0, p1 + (size_t)q * 64 * ld, nb, ld);
             break;
         case T_TRSM_RUN:
-            make_inverses(w, p0, nb, ld, dinvU, false);
-            for (int q = 0; q < parts; q++) trsm_run(w, p0, p1 + q * 64, nb, ld, dinvU);
+            for (int q = 0; q < parts; q++) trsm_run(w, p0, p1 + q * 64, nb, ld);
             break;
         case T_TRSM_LLU:
-            make_inverses(w, p0, nb, ld, dinvL, true);
-            for (int q = 0; q < parts; q++) trsm_llu(w, p0, p1 + (size_t)q * 64 * ld, nb, ld, dinvL);
+            for (int q = 0; q < parts; q++) trsm_llu(w, p0, p1 + (size_t)q * 64 * ld, nb, ld);
             break;
         case T_SYRK:
             for (int q = 0; q < parts; q++) {
@@ -708,12 +655,13 @@ cudaError_t sched_launch(const SchedParams &p, int grid, cudaStream_t s) {
     return cudaGetLastError();
 }
 
-// Scratch (doubles) the scheduler needs: diagonal inverses + per-worker QR strips.
+// Scratch (doubles) the scheduler needs: per-worker strips for the QR update tasks.
 long long sched_scratch_doubles(int alg, int n, int nb, int bs, int workers, long long *per_worker) {
-    const long long dinv = 2LL * (n / bs) * (bs / 64) * 4096;
+    (void)n;
+    (void)bs;
     const long long pw = (alg == 2) ? 2LL * nb * 64 : 0;
     if (per_worker) *per_worker = pw;
-    return dinv + pw * workers;
+    return pw * workers;
 }
 
 }  // namespace palial

@@ -204,34 +204,5 @@ __device__ inline int chol64_upper(double (*Ds)[DP], int *s_flag) {
     return -1;
 }
 
-// Inverse of an upper-triangular 64x64 block (Ds) into Is (upper; lower part zeroed).
-// unit: treat the diagonal as 1.  transpose_lower: Ds holds a lower-triangular matrix L
-// (L(r,c) = Ds[c][r], r >= c) and the inverse of L is written (lower).
-template <bool LOWER, bool UNIT>
-__device__ inline void tri_inv64(const double (*Ds)[DP], double (*Is)[DP]) {
-    const int t = threadIdx.x;
-    for (int e = t; e < 64 * 64; e += NT) Is[e >> 6][e & 63] = 0.0;
-    __syncthreads();
-    if (t < 64) {
-        const int c = t;  // column c of the inverse
-        if (!LOWER) {
-            // U X = e_c: X(i,c) for i = c..0
-            for (int i = c; i >= 0; i--) {
-                double s = (i == c) ? 1.0 : 0.0;
-                for (int p = i + 1; p <= c; p++) s = fma(-Ds[p][i], Is[c][p], s);
-                Is[c][i] = UNIT ? s : s / Ds[i][i];
-            }
-        } else {
-            // L X = e_c: X(i,c) for i = c..63
-            for (int i = c; i < 64; i++) {
-                double s = (i == c) ? 1.0 : 0.0;
-                for (int p = c; p < i; p++) s = fma(-Ds[p][i], Is[c][p], s);
-                Is[c][i] = UNIT ? s : s / Ds[i][i];
-            }
-        }
-    }
-    __syncthreads();
-}
-
 }  // namespace f64
 }  // namespace palial
