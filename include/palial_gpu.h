@@ -138,6 +138,19 @@ int palial_gpu_tile_dormqr(int nb, const double *dV, const double *dT, double *d
 int palial_gpu_tile_dtsqrt(int nb, double *dA1, double *dA2, double *dT, int lda);
 int palial_gpu_tile_dtsmqr(int nb, double *dA1, double *dA2, const double *dV, const double *dT,
                            int lda);
+/* TSMQR without any device allocation.  No counterpart in the reference: it exists for
+ * callers that may not allocate device memory themselves -- code inside an application that
+ * owns all device memory (its own pool or allocator, a fixed budget), or latency-critical
+ * code that must avoid cudaMalloc/cudaFree and the device-wide synchronization they can
+ * cause.  Same arguments and result as palial_gpu_tile_dtsmqr, plus a stream (a
+ * cudaStream_t as void*, NULL = default stream); the call only enqueues the kernel.
+ * Limit: nb <= 512 (a multiple of 64); larger tiles return PALIAL_ERR_ARG.  Its scratch is a
+ * fixed 512 KiB array inside the library, held by every GPU that loads it until the process
+ * exits.  The first call on a device looks up that array's device address, so make that
+ * first call before capturing a stream.  All calls share the one array: calls whose kernels
+ * overlap on the GPU (unordered streams, other host threads) race on it. */
+int palial_gpu_tile_dtsmqr_noalloc(int nb, double *dA1, double *dA2, const double *dV,
+                                   const double *dT, int lda, void *stream);
 /* kind for dtrsm: 0 = left upper trans non-unit (Cholesky), 1 = right upper no-trans non-unit
  * (LU), 2 = left lower no-trans unit (LU).  kind for dgemm: 0 = C -= A^T B (Cholesky),
  * 1 = C -= A B (LU). */

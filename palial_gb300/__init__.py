@@ -95,6 +95,7 @@ def lib() -> ctypes.CDLL:
         h.palial_gpu_tile_dormqr.argtypes = [i, vp, vp, vp, i]
         h.palial_gpu_tile_dtsqrt.argtypes = [i, vp, vp, vp, i]
         h.palial_gpu_tile_dtsmqr.argtypes = [i, vp, vp, vp, vp, i]
+        h.palial_gpu_tile_dtsmqr_noalloc.argtypes = [i, vp, vp, vp, vp, i, vp]
         h.palial_gpu_error_string.restype = ctypes.c_char_p
         _lib = h
     return _lib
