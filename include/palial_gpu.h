@@ -88,7 +88,9 @@ typedef struct palial_status {
     int ir_iters;           /* refinement iterations (solve_ir)                       */
     int gmres_iters;        /* total inner GMRES iterations (solve_ir)                */
     double backward_error;  /* final normwise backward error (solve_ir)               */
-    double kappa_est;       /* condition estimate used to choose the method           */
+    double kappa_est;       /* condition estimate used to choose the method (-1: none) */
+    double factor_seconds;  /* time of the factorization part (solve_ir)              */
+    double shift;           /* diagonal shift used by a low-precision Cholesky        */
     char message[160];
 } palial_status;
 
@@ -121,6 +123,27 @@ int palial_gpu_qr(const palial_desc *A, const palial_desc *S, const palial_opts 
 /* ---- same, on DEVICE-resident tile buffers (no host copies) ------------------------------ */
 int palial_gpu_factor_dev(int alg, double *dA, double *dS, int n, int nb, const palial_opts *opts,
                           palial_status *st, void *stream);
+
+/* ---- mixed precision + iterative refinement (no reference counterpart: north-star) ------
+ * Solve A X = B for nrhs <= 16 right-hand sides (dB, dX: n x nrhs column-major, device),
+ * A an FP64 tile-layout matrix on the device (not modified).  alg: PALIAL_ALG_CHOLESKY or
+ * PALIAL_ALG_LU (no pivoting).  opts->precision selects the trailing-update precision
+ * (PALIAL_PREC_BF16 / FP8 / BF16X3 on tcgen05 with FP32 accumulation, or FP64); diagonal
+ * tiles are factored in FP64, panels solved in FP32, residuals r = b - A x and corrections in
+ * FP64.  Iterates until the normwise backward error max_j |r_j|/(|A| |x_j| + |b_j|) (inf-
+ * norms) <= opts->ir_tol (default 1e-14 * n); GMRES-IR when plain refinement stagnates
+ * (opts->gmres: -1 never, 0 automatic, 1 always).  NB must be a multiple of 256.
+ * Returns PALIAL_ERR_NOT_CONVERGED (with the reached error in st) if the target is missed. */
+int palial_gpu_solve_ir(int alg, const double *dA, int n, int nb, const double *dB, double *dX,
+                        int nrhs, const palial_opts *opts, palial_status *st, void *stream);
+/* The low-precision factorization alone: dW (n*n floats, tile layout) receives the FP32
+ * factors (Cholesky: U in the upper tiles; LU: L\U). */
+int palial_gpu_mp_factor(int alg, const double *dA, float *dW, int n, int nb,
+                         const palial_opts *opts, palial_status *st, void *stream);
+/* One trailing update of step k on an FP32 tile matrix dW, as the mixed factorization does
+ * it: pack the step's panel(s) from dW in the given precision (1 bf16, 2 fp8, 3 bf16x3) and
+ * apply C -= A_op B_op^T with the tcgen05 kernel (Cholesky: upper tile pairs; LU: all). */
+int palial_gpu_mp_update_step(int alg, int precision, float *dW, int n, int nb, int k);
 
 /* ---- single-tile kernels on device pointers (reference tile-kernel ABI, for unit tests) ----
  * Each runs one tile task on one CTA of the persistent scheduler's kernels.

@@ -52,6 +52,7 @@ class Status(ctypes.Structure):
                 ("ntasks", ctypes.c_longlong), ("seconds", ctypes.c_double), ("total_seconds", ctypes.c_double),
                 ("tflops", ctypes.c_double), ("ir_iters", ctypes.c_int), ("gmres_iters", ctypes.c_int),
                 ("backward_error", ctypes.c_double), ("kappa_est", ctypes.c_double),
+                ("factor_seconds", ctypes.c_double), ("shift", ctypes.c_double),
                 ("message", ctypes.c_char * 160)]
 
     def as_dict(self) -> dict:
@@ -97,6 +98,9 @@ def lib() -> ctypes.CDLL:
         h.palial_gpu_tile_dtsmqr.argtypes = [i, vp, vp, vp, vp, i]
         h.palial_gpu_tile_dtsmqr_noalloc.argtypes = [i, vp, vp, vp, vp, i, vp]
         h.palial_gpu_error_string.restype = ctypes.c_char_p
+        h.palial_gpu_solve_ir.argtypes = [i, vp, i, i, vp, vp, i, ctypes.POINTER(Opts), ctypes.POINTER(Status), vp]
+        h.palial_gpu_mp_factor.argtypes = [i, vp, vp, i, i, ctypes.POINTER(Opts), ctypes.POINTER(Status), vp]
+        h.palial_gpu_mp_update_step.argtypes = [i, i, vp, i, i, i]
         _lib = h
     return _lib
 
@@ -162,6 +166,26 @@ def factor_dev(alg: str, d_a: int, d_s: int | None, n: int, nb: int, stream: int
     rc = lib().palial_gpu_factor_dev(ALG[alg], d_a, d_s or None, n, nb, ctypes.byref(make_opts(**kw)),
                                      ctypes.byref(st), stream or None)
     _check(rc, st, allow=(PALIAL_OK, 1) if allow_warn else (PALIAL_OK,))
+    return st
+
+
+def solve_ir(alg: str, d_a: int, n: int, nb: int, d_b: int, d_x: int, nrhs: int, stream: int = 0,
+             raise_on_error: bool = True, **kw) -> Status:
+    """Mixed-precision (or FP64) factorization + iterative refinement: A X = B on the device."""
+    st = Status()
+    rc = lib().palial_gpu_solve_ir(ALG[alg], d_a, n, nb, d_b, d_x, nrhs, ctypes.byref(make_opts(**kw)),
+                                   ctypes.byref(st), stream or None)
+    if raise_on_error:
+        _check(rc, st, allow=(PALIAL_OK, 1))
+    st.code = rc
+    return st
+
+
+def mp_factor(alg: str, d_a: int, d_w: int, n: int, nb: int, stream: int = 0, **kw) -> Status:
+    st = Status()
+    rc = lib().palial_gpu_mp_factor(ALG[alg], d_a, d_w, n, nb, ctypes.byref(make_opts(**kw)), ctypes.byref(st),
+                                    stream or None)
+    _check(rc, st, allow=(PALIAL_OK, 1))
     return st
 
 

@@ -1,0 +1,91 @@
+// host_state.hpp -- host-side state shared by the runtime translation units.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <cstdarg>
+#include <map>
+#include <memory>
+#include <tuple>
+#include <vector>
+
+#include "../../include/palial_gpu.h"
+#include "common.cuh"
+#include "dag.hpp"
+
+namespace palial {
+
+// grow-only device buffer
+struct DevBuf {
+    void *ptr = nullptr;
+    size_t bytes = 0;
+    cudaError_t ensure(size_t want) {
+        if (want <= bytes) return cudaSuccess;
+        if (ptr) cudaFree(ptr);
+        ptr = nullptr;
+        bytes = 0;
+        cudaError_t e = cudaMalloc(&ptr, want);
+        if (e == cudaSuccess) bytes = want;
+        return e;
+    }
+    void release() {
+        if (ptr) cudaFree(ptr);
+        ptr = nullptr;
+        bytes = 0;
+    }
+    template <class T>
+    T *as() const {
+        return static_cast<T *>(ptr);
+    }
+};
+
+// Device state of one persistent-scheduler instance (records, counters, status, ticket,
+// trace, scratch).  The main factorizations use one; the mixed-precision driver uses a
+// second one for its FP64 diagonal-tile factorizations.
+struct SchedCtx {
+    DevBuf tasks, counters, status, ticket, trace, scratch;
+    unsigned long long uploaded = 0;  // uid of the DAG whose records are on the device
+    void release() {
+        for (DevBuf *b : {&tasks, &counters, &status, &ticket, &trace, &scratch}) b->release();
+        uploaded = 0;
+    }
+};
+
+struct TraceState {
+    Dag dag;
+    std::vector<TraceRec> recs;
+    bool valid = false;
+};
+
+struct State {
+    bool init = false;
+    int device = -1;
+    int sms = 0;
+    int occupancy = 1;
+    SchedCtx main, diag;
+    DevBuf mat, smat, kbuf, probe;
+    std::map<std::tuple<int, int, int, int, int, int, unsigned>, std::shared_ptr<Dag>> dags;
+    unsigned long long next_uid = 1;
+    TraceState last_trace;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+};
+extern State g;
+
+int set_status(palial_status *st, int code, const char *fmt = nullptr, ...);
+int cuda_fail(palial_status *st, cudaError_t e, const char *what);
+int ensure_init(palial_status *st);
+int auto_block(int alg, int n, int nb);
+std::shared_ptr<Dag> get_dag(int alg, int n, int nb, int bs, int priority, int workers, unsigned seed);
+
+// Prepare a scheduler run (host: DAG upload, buffers) and return its launch parameters.
+int sched_prepare(SchedCtx &c, const std::shared_ptr<Dag> &dag, double *dA, double *dS, int workers, int trace,
+                  double timeout_s, SchedParams &p, palial_status *st);
+// Enqueue it (asynchronous): clear counters and ticket (and status if clear_status), launch.
+cudaError_t sched_enqueue(SchedCtx &c, const SchedParams &p, int nobj, int workers, bool clear_status, cudaStream_t s);
+
+#define PALIAL_CK(call, what)                                  \
+    do {                                                       \
+        cudaError_t _e = (call);                               \
+        if (_e != cudaSuccess) return cuda_fail(st, _e, what); \
+    } while (0)
+
+}  // namespace palial

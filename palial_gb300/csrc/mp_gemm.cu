@@ -1,0 +1,488 @@
+// mp_gemm.cu -- tcgen05 (5th-generation tensor core) trailing update of the mixed-precision
+// factorizations: C -= A_op * B_op^T on the FP32 trailing matrix, for every trailing tile of
+// one k step, with low-precision operands packed from the step's panel.
+//
+//   Cholesky: C(n,m) -= U(k,n)^T U(k,m)    A_op = B_op = packed panel row k
+//   LU:       C(m,n) -= L(m,k) U(k,n)      A_op = packed panel column k, B_op = panel row k
+//
+// Operands are K-major bf16 (or e4m3) matrices "rows x NB" (a packed panel: row r holds the
+// K = NB values that multiply trailing row/column r).  Each CTA computes one 128 x 256 output
+// block of one 512-aligned trailing tile:
+//   warp 0 lane 0  TMA producer: 128B-swizzled boxes of 128 (A) and 256 (B) rows x 128 bytes
+//                  of K into a 4-stage shared-memory ring (mbarrier complete_tx);
+//   warp 1 lane 0  MMA issuer: tcgen05.mma (M=128, N=256, K=16 bf16 / 32 fp8) into a TMEM
+//                  accumulator of 256 FP32 columns; tcgen05.commit frees ring slots;
+//   all 4 warps    epilogue: tcgen05.ld 32 lanes x 16 columns at a time, C -= scale * D with
+//                  coalesced FP32 loads/stores in the reference's tile layout.
+// Modes: BF16 (one MMA per K slice), FP8 e4m3 (per-tile scales applied in the epilogue) and
+// BF16X3 (operands split x = hi + lo in bf16; hi*hi + hi*lo + lo*hi accumulated in TMEM).
+// Every mbarrier wait is bounded; on expiry the CTA records an error, drains its own TMA
+// copies and frees its TMEM before returning.
+#include <cuda.h>
+#include <cuda_bf16.h>
+#include <cuda_fp8.h>
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "common.cuh"
+
+namespace palial {
+namespace mp {
+
+constexpr int BM = 128, BN = 256;      // CTA output block
+constexpr int KBYTES = 128;            // bytes of K per stage (one 128B swizzle row)
+constexpr int NTHR = 128;
+constexpr uint32_t TMEM_COLS = 256;
+constexpr uint32_t WAIT_LIMIT = 1u << 24;  // bounded spin (about a second with back-off)
+
+enum Mode { MODE_BF16 = 0, MODE_FP8 = 1, MODE_BF16X3 = 2 };
+
+template <int MODE>
+struct Cfg {
+    static constexpr int NOPS = (MODE == MODE_BF16X3) ? 2 : 1;   // hi (+ lo) operand copies
+    static constexpr int STAGES = (MODE == MODE_BF16X3) ? 2 : 4;
+    static constexpr int A_BYTES = BM * KBYTES;                  // 16 KB
+    static constexpr int B_BYTES = BN * KBYTES;                  // 32 KB
+    static constexpr int STAGE_BYTES = NOPS * (A_BYTES + B_BYTES);
+    static constexpr int SMEM = STAGES * STAGE_BYTES + 1024 /*align*/ + 256 /*barriers*/;
+    static constexpr int ELEM = (MODE == MODE_FP8) ? 1 : 2;     // bytes per element
+    static constexpr int KELEMS = KBYTES / ELEM;                 // elements of K per stage
+    // instruction descriptor: D=F32, A/B format, K-major A and B, N>>3, M>>4
+    static constexpr uint32_t IDESC = (1u << 4) | ((MODE == MODE_FP8 ? 0u : 1u) << 7) |
+                                      ((MODE == MODE_FP8 ? 0u : 1u) << 10) | ((uint32_t)(BN >> 3) << 17) |
+                                      ((uint32_t)(BM >> 4) << 24);
+};
+
+struct UpdateParams {
+    float *C;                 // FP32 tile-layout matrix, n x n
+    int n, nb;                // size, tile size (multiple of 256)
+    int k;                    // step: trailing tiles start at tile k+1
+    int ntr;                  // trailing tiles per dimension
+    int upper;                // 1: only tile pairs (ti <= tj) (Cholesky), 0: all (LU)
+    const float *scale_a;     // FP8: per trailing tile scale of A_op rows (nullptr: 1)
+    const float *scale_b;     // FP8: per trailing tile scale of B_op rows
+    int *status;              // error word (ST_CODE slot)
+};
+
+__device__ __forceinline__ uint32_t smem_u32(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void mbar_init(uint64_t *bar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count));
+}
+__device__ __forceinline__ void mbar_expect_tx(uint64_t *bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
+                 : "memory");
+}
+__device__ __forceinline__ bool mbar_try(uint64_t *bar, uint32_t parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(ok)
+        : "r"(smem_u32(bar)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+// Bounded wait: true when the phase of `parity` completed, false after WAIT_LIMIT tries.
+__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity) {
+    for (uint32_t i = 0; i < WAIT_LIMIT; i++) {
+        if (mbar_try(bar, parity)) return true;
+        if (i > 32) __nanosleep(64);
+    }
+    return false;
+}
+
+__device__ __forceinline__ void tma_load_2d(void *dst, const CUtensorMap *map, int x, int y, uint64_t *bar) {
+    asm volatile(
+        "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];" ::"r"(
+            smem_u32(dst)),
+        "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(smem_u32(bar))
+        : "memory");
+}
+
+// Shared-memory matrix descriptor: K-major, 128B swizzle, 8-row atoms 1024 B apart.
+__device__ __forceinline__ uint64_t smem_desc(const void *p) {
+    const uint32_t a = smem_u32(p);
+    uint64_t d = 0;
+    d |= (uint64_t)((a & 0x3FFFF) >> 4);   // start address
+    d |= (uint64_t)1 << 16;                // leading byte offset (unused for swizzled K-major)
+    d |= (uint64_t)(1024 >> 4) << 32;      // stride byte offset: 8 rows x 128 B
+    d |= (uint64_t)1 << 46;                // descriptor version (sm_100 family)
+    d |= (uint64_t)2 << 61;                // SWIZZLE_128B
+    return d;
+}
+
+template <int MODE>
+__device__ __forceinline__ void mma(uint32_t tmem_d, uint64_t a, uint64_t b, uint32_t accumulate) {
+    if (MODE == MODE_FP8) {
+        asm volatile(
+            "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+            " tcgen05.mma.cta_group::1.kind::f8f6f4 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem_d),
+            "l"(a), "l"(b), "r"(Cfg<MODE>::IDESC), "r"(accumulate));
+    } else {
+        asm volatile(
+            "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+            " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem_d),
+            "l"(a), "l"(b), "r"(Cfg<MODE>::IDESC), "r"(accumulate));
+    }
+}
+
+__device__ __forceinline__ void mma_commit(uint64_t *bar) {
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(bar))
+                 : "memory");
+}
+
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float *v) {
+    uint32_t r[16];
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+          "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+        : "r"(taddr));
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+    for (int i = 0; i < 16; i++) v[i] = __uint_as_float(r[i]);
+}
+
+__device__ __forceinline__ void decode_pair(int q, int ntr, int upper, int &ti, int &tj) {
+    if (!upper) {
+        ti = q % ntr;
+        tj = q / ntr;
+        return;
+    }
+    int j = (int)((sqrtf(8.0f * (float)q + 1.0f) - 1.0f) * 0.5f);
+    while (j * (j + 1) / 2 > q) j--;
+    while ((j + 1) * (j + 2) / 2 <= q) j++;
+    tj = j;
+    ti = q - j * (j + 1) / 2;
+}
+
+template <int MODE>
+__global__ void __launch_bounds__(NTHR, 1)
+    mp_update_kernel(const __grid_constant__ CUtensorMap ta, const __grid_constant__ CUtensorMap tb,
+                     const __grid_constant__ CUtensorMap ta_lo, const __grid_constant__ CUtensorMap tb_lo,
+                     UpdateParams p) {
+    using C = Cfg<MODE>;
+    extern __shared__ __align__(1024) uint8_t smem_raw[];
+    uint8_t *base = reinterpret_cast<uint8_t *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+    uint64_t *full = reinterpret_cast<uint64_t *>(base + C::STAGES * C::STAGE_BYTES);
+    uint64_t *empty = full + C::STAGES;
+    uint64_t *done = empty + C::STAGES;
+    uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(done + 1);
+    __shared__ int s_abort;
+
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int sub_m = p.nb / BM, sub_n = p.nb / BN;
+    const int q = blockIdx.x / (sub_m * sub_n), sub = blockIdx.x % (sub_m * sub_n);
+    int ti, tj;
+    decode_pair(q, p.ntr, p.upper, ti, tj);
+    const int mi = sub % sub_m, nj = sub / sub_m;
+    const int arow = ti * p.nb + mi * BM;   // first row of A_op
+    const int brow = tj * p.nb + nj * BN;   // first row of B_op
+    const int kstages = p.nb * C::ELEM / KBYTES;
+
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < C::STAGES; s++) {
+            mbar_init(&full[s], 1);
+            mbar_init(&empty[s], 1);
+        }
+        mbar_init(done, 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        s_abort = 0;
+    }
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
+                     "r"(TMEM_COLS));
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    const uint32_t tmem = *tmem_slot;
+
+    if (warp == 0 && lane == 0) {
+        // ---- TMA producer ----
+        int issued = 0;
+        for (int kb = 0; kb < kstages; kb++) {
+            const int s = kb % C::STAGES;
+            if (kb >= C::STAGES && !mbar_wait(&empty[s], ((kb / C::STAGES) - 1) & 1)) {
+                s_abort = 1;
+                break;
+            }
+            uint8_t *st = base + s * C::STAGE_BYTES;
+            mbar_expect_tx(&full[s], C::STAGE_BYTES);
+            const int kx = kb * C::KELEMS;
+            tma_load_2d(st, &ta, kx, arow, &full[s]);
+            tma_load_2d(st + C::A_BYTES, &tb, kx, brow, &full[s]);
+            if (C::NOPS == 2) {
+                tma_load_2d(st + C::A_BYTES + C::B_BYTES, &ta_lo, kx, arow, &full[s]);
+                tma_load_2d(st + 2 * C::A_BYTES + C::B_BYTES, &tb_lo, kx, brow, &full[s]);
+            }
+            issued = kb + 1;
+        }
+        if (s_abort) {
+            // drain: wait (bounded) for this CTA's own copies that may still be landing
+            for (int kb = issued - C::STAGES < 0 ? 0 : issued - C::STAGES; kb < issued; kb++)
+                mbar_wait(&full[kb % C::STAGES], (kb / C::STAGES) & 1);
+        }
+    } else if (warp == 1 && lane == 0) {
+        // ---- MMA issuer ----
+        bool ok = true;
+        for (int kb = 0; kb < kstages; kb++) {
+            const int s = kb % C::STAGES;
+            if (!mbar_wait(&full[s], (kb / C::STAGES) & 1)) {
+                ok = false;
+                s_abort = 1;
+                break;
+            }
+            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+            uint8_t *st = base + s * C::STAGE_BYTES;
+            const uint64_t da = smem_desc(st), db = smem_desc(st + C::A_BYTES);
+#pragma unroll
+            for (int kk = 0; kk < KBYTES / 32; kk++) {
+                const uint32_t acc = (kb | kk) ? 1u : 0u;
+                mma<MODE>(tmem, da + 2 * kk, db + 2 * kk, acc);  // +32 B per K slice
+                if (C::NOPS == 2) {
+                    const uint64_t dal = smem_desc(st + C::A_BYTES + C::B_BYTES);
+                    const uint64_t dbl = smem_desc(st + 2 * C::A_BYTES + C::B_BYTES);
+                    mma<MODE>(tmem, da + 2 * kk, dbl + 2 * kk, 1u);   // hi * lo
+                    mma<MODE>(tmem, dal + 2 * kk, db + 2 * kk, 1u);   // lo * hi
+                }
+            }
+            mma_commit(&empty[s]);
+        }
+        if (ok) mma_commit(done);
+    }
+    __syncwarp();
+    // ---- epilogue: all four warps ----
+    bool have = false;
+    if (!s_abort) have = mbar_wait(done, 0);
+    if (!have) {
+        if (threadIdx.x == 0 || lane == 0) atomicCAS(p.status + ST_CODE, 0, -4);
+    } else {
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        const int mt = p.n / p.nb;
+        const int tr = p.k + 1 + ti, tc = p.k + 1 + tj;
+        float *ct = p.C + (size_t)p.nb * p.nb * ((size_t)tr + (size_t)mt * tc) + (size_t)(mi * BM + warp * 32 + lane) +
+                    (size_t)(nj * BN) * p.nb;
+        float sc = 1.0f;
+        if (MODE == MODE_FP8 && p.scale_a) sc = p.scale_a[ti] * p.scale_b[tj];
+        for (int c0 = 0; c0 < BN; c0 += 16) {
+            float d[16];
+            tmem_ld16(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0, d);
+#pragma unroll
+            for (int c = 0; c < 16; c++) {
+                float *x = ct + (size_t)(c0 + c) * p.nb;
+                *x = fmaf(-sc, d[c], *x);
+            }
+        }
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TMEM_COLS));
+}
+
+// ---------------------------------------------------------------------------------------
+// Panel packing: K-major low-precision copies of the step's panel.
+// ---------------------------------------------------------------------------------------
+// Row panel k (Cholesky U(k, m) / LU U(k, n), m > k): packed row (m-k-1)*nb + j, col p =
+// tile (k, m) element (p, j): the tile's columns are already contiguous in p.
+// MODE 0: bf16; 2: bf16 hi + lo; 1: e4m3 with per-tile scale (max|x| / 448).
+__global__ void pack_rows_kernel(const float *W, int n, int nb, int k, int mode, __nv_bfloat16 *hi,
+                                 __nv_bfloat16 *lo, __nv_fp8_e4m3 *f8, float *scales) {
+    const int t = blockIdx.y;                   // trailing tile index
+    const int mt = n / nb;
+    const float *tile = W + (size_t)nb * nb * ((size_t)k + (size_t)mt * (k + 1 + t));
+    const size_t out0 = (size_t)t * nb * nb;
+    float inv = 1.0f;
+    if (mode == 1) {
+        __shared__ float red[32];
+        float mx = 0.f;
+        for (int e = threadIdx.x; e < nb * nb; e += blockDim.x) mx = fmaxf(mx, fabsf(tile[e]));
+        for (int o = 16; o; o >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+        if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = mx;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            float m = 0.f;
+            for (int i = 0; i < (int)(blockDim.x >> 5); i++) m = fmaxf(m, red[i]);
+            const float s = m > 0.f ? m / 448.0f : 1.0f;
+            red[0] = s;
+            scales[t] = s;
+        }
+        __syncthreads();
+        inv = 1.0f / red[0];
+    }
+    for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < nb * nb; e += gridDim.x * blockDim.x) {
+        const float x = tile[e];
+        if (mode == 1) {
+            f8[out0 + e] = __nv_fp8_e4m3(x * inv);
+        } else {
+            const __nv_bfloat16 h = __float2bfloat16_rn(x);
+            hi[out0 + e] = h;
+            if (mode == 2) lo[out0 + e] = __float2bfloat16_rn(x - __bfloat162float(h));
+        }
+    }
+}
+
+// Column panel k (LU L(m, k), m > k): packed row (m-k-1)*nb + i, col p = tile (m, k)
+// element (i, p): a transpose, through shared memory 32 x 32 at a time.
+__global__ void pack_cols_kernel(const float *W, int n, int nb, int k, int mode, __nv_bfloat16 *hi,
+                                 __nv_bfloat16 *lo, __nv_fp8_e4m3 *f8, const float *scales) {
+    __shared__ float s[32][33];
+    const int t = blockIdx.z;
+    const int mt = n / nb;
+    const float *tile = W + (size_t)nb * nb * ((size_t)(k + 1 + t) + (size_t)mt * k);
+    const int i0 = blockIdx.x * 32, p0 = blockIdx.y * 32;
+    for (int r = threadIdx.y; r < 32; r += blockDim.y) s[r][threadIdx.x] = tile[(size_t)(i0 + threadIdx.x) + (size_t)(p0 + r) * nb];
+    __syncthreads();
+    const float inv = (mode == 1) ? 1.0f / scales[t] : 1.0f;
+    for (int r = threadIdx.y; r < 32; r += blockDim.y) {
+        const float x = s[threadIdx.x][r];  // element (i0 + r, p0 + tx)
+        const size_t o = (size_t)t * nb * nb + (size_t)(i0 + r) * nb + p0 + threadIdx.x;
+        if (mode == 1) {
+            f8[o] = __nv_fp8_e4m3(x * inv);
+        } else {
+            const __nv_bfloat16 h = __float2bfloat16_rn(x);
+            hi[o] = h;
+            if (mode == 2) lo[o] = __float2bfloat16_rn(x - __bfloat162float(h));
+        }
+    }
+}
+
+// per-tile max-abs scales of the column panel (FP8 mode)
+__global__ void col_scales_kernel(const float *W, int n, int nb, int k, float *scales) {
+    __shared__ float red[32];
+    const int t = blockIdx.x;
+    const int mt = n / nb;
+    const float *tile = W + (size_t)nb * nb * ((size_t)(k + 1 + t) + (size_t)mt * k);
+    float mx = 0.f;
+    for (int e = threadIdx.x; e < nb * nb; e += blockDim.x) mx = fmaxf(mx, fabsf(tile[e]));
+    for (int o = 16; o; o >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = mx;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        float m = 0.f;
+        for (int i = 0; i < (int)(blockDim.x >> 5); i++) m = fmaxf(m, red[i]);
+        scales[t] = m > 0.f ? m / 448.0f : 1.0f;
+    }
+}
+
+}  // namespace mp
+
+// ---------------------------------------------------------------------------------------
+// Host side
+// ---------------------------------------------------------------------------------------
+namespace {
+using EncodeFn = CUresult (*)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *, const cuuint64_t *,
+                              const cuuint64_t *, const cuuint32_t *, const cuuint32_t *, CUtensorMapInterleave,
+                              CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+EncodeFn g_encode = nullptr;
+
+cudaError_t get_encode() {
+    if (g_encode) return cudaSuccess;
+    void *fn = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    cudaError_t e = cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q);
+    if (e != cudaSuccess || q != cudaDriverEntryPointSuccess || !fn) return cudaErrorNotSupported;
+    g_encode = reinterpret_cast<EncodeFn>(fn);
+    return cudaSuccess;
+}
+
+// K-major packed operand: rows x nb elements, box = box_rows x 128 bytes, 128B swizzle.
+cudaError_t make_map(CUtensorMap *m, const void *base, long long rows, int nb, int elem_bytes, int box_rows) {
+    cudaError_t e = get_encode();
+    if (e != cudaSuccess) return e;
+    const cuuint64_t dims[2] = {(cuuint64_t)nb, (cuuint64_t)rows};
+    const cuuint64_t strides[1] = {(cuuint64_t)nb * elem_bytes};
+    const cuuint32_t box[2] = {(cuuint32_t)(128 / elem_bytes), (cuuint32_t)box_rows};
+    const cuuint32_t estr[2] = {1, 1};
+    const CUresult r = g_encode(m, elem_bytes == 1 ? CU_TENSOR_MAP_DATA_TYPE_UINT8 : CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2,
+                                const_cast<void *>(base), dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                                CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                                CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    return r == CUDA_SUCCESS ? cudaSuccess : cudaErrorInvalidValue;
+}
+
+template <int MODE>
+cudaError_t launch_mode(const void *a_hi, const void *a_lo, const void *b_hi, const void *b_lo,
+                        const mp::UpdateParams &p, cudaStream_t s) {
+    using C = mp::Cfg<MODE>;
+    static bool configured = false;
+    if (!configured) {
+        cudaError_t e = cudaFuncSetAttribute(mp::mp_update_kernel<MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             C::SMEM);
+        if (e != cudaSuccess) return e;
+        configured = true;
+    }
+    const long long rows = (long long)p.ntr * p.nb;
+    const int eb = C::ELEM;
+    CUtensorMap ta, tb, tal, tbl;
+    cudaError_t e;
+    if ((e = make_map(&ta, a_hi, rows, p.nb, eb, mp::BM)) != cudaSuccess) return e;
+    if ((e = make_map(&tb, b_hi, rows, p.nb, eb, mp::BN)) != cudaSuccess) return e;
+    if (C::NOPS == 2) {
+        if ((e = make_map(&tal, a_lo, rows, p.nb, eb, mp::BM)) != cudaSuccess) return e;
+        if ((e = make_map(&tbl, b_lo, rows, p.nb, eb, mp::BN)) != cudaSuccess) return e;
+    } else {
+        tal = ta;
+        tbl = tb;
+    }
+    const long long pairs = p.upper ? (long long)p.ntr * (p.ntr + 1) / 2 : (long long)p.ntr * p.ntr;
+    const long long blocks = pairs * (p.nb / mp::BM) * (p.nb / mp::BN);
+    if (blocks <= 0) return cudaSuccess;
+    if (blocks > 0x7fffffffLL) return cudaErrorInvalidValue;
+    mp::mp_update_kernel<MODE><<<(unsigned)blocks, mp::NTHR, C::SMEM, s>>>(ta, tb, tal, tbl, p);
+    return cudaGetLastError();
+}
+}  // namespace
+
+// mode: 0 bf16, 1 fp8, 2 bf16x3.  a_*/b_*: packed operands (ntr*nb rows x nb), scales: per
+// trailing tile (fp8).  C: FP32 tile-layout matrix.
+cudaError_t mp_update(int mode, int upper, float *C, int n, int nb, int k, const void *a_hi, const void *a_lo,
+                      const void *b_hi, const void *b_lo, const float *scale_a, const float *scale_b, int *status,
+                      cudaStream_t s) {
+    if (nb % 256 || n % nb) return cudaErrorInvalidValue;
+    mp::UpdateParams p{};
+    p.C = C;
+    p.n = n;
+    p.nb = nb;
+    p.k = k;
+    p.ntr = n / nb - k - 1;
+    p.upper = upper;
+    p.scale_a = scale_a;
+    p.scale_b = scale_b;
+    p.status = status;
+    if (p.ntr <= 0) return cudaSuccess;
+    if (mode == mp::MODE_BF16) return launch_mode<mp::MODE_BF16>(a_hi, nullptr, b_hi, nullptr, p, s);
+    if (mode == mp::MODE_FP8) return launch_mode<mp::MODE_FP8>(a_hi, nullptr, b_hi, nullptr, p, s);
+    return launch_mode<mp::MODE_BF16X3>(a_hi, a_lo, b_hi, b_lo, p, s);
+}
+
+// Pack the row panel k (tiles (k, m), m > k) of the FP32 tile matrix W.
+cudaError_t mp_pack_rows(int mode, const float *W, int n, int nb, int k, void *hi, void *lo, float *scales,
+                         cudaStream_t s) {
+    const int ntr = n / nb - k - 1;
+    if (ntr <= 0) return cudaSuccess;
+    dim3 grid(mode == 1 ? 1 : 16, ntr);
+    mp::pack_rows_kernel<<<grid, 1024, 0, s>>>(W, n, nb, k, mode, static_cast<__nv_bfloat16 *>(hi),
+                                                static_cast<__nv_bfloat16 *>(lo), static_cast<__nv_fp8_e4m3 *>(hi),
+                                                scales);
+    return cudaGetLastError();
+}
+
+// Pack the column panel k (tiles (m, k), m > k), transposed to K-major.
+cudaError_t mp_pack_cols(int mode, const float *W, int n, int nb, int k, void *hi, void *lo, float *scales,
+                         cudaStream_t s) {
+    const int ntr = n / nb - k - 1;
+    if (ntr <= 0) return cudaSuccess;
+    if (mode == 1) {
+        mp::col_scales_kernel<<<ntr, 1024, 0, s>>>(W, n, nb, k, scales);
+    }
+    dim3 grid(nb / 32, nb / 32, ntr), block(32, 8);
+    mp::pack_cols_kernel<<<grid, block, 0, s>>>(W, n, nb, k, mode, static_cast<__nv_bfloat16 *>(hi),
+                                                 static_cast<__nv_bfloat16 *>(lo), static_cast<__nv_fp8_e4m3 *>(hi),
+                                                 scales);
+    return cudaGetLastError();
+}
+
+}  // namespace palial

@@ -20,6 +20,7 @@
 #include "../../include/palial_gpu.h"
 #include "common.cuh"
 #include "dag.hpp"
+#include "host_state.hpp"
 
 namespace palial {
 // sched_f64.cu
@@ -39,55 +40,11 @@ cudaError_t launch_tiled_mm(const double *A, const double *X, double *Y, int n, 
                             cudaStream_t s);
 cudaError_t launch_sumsq(const double *X, long long len, double *partial, int blocks, cudaStream_t s);
 cudaError_t launch_sub(const double *X, const double *Y, double *Z, long long len, cudaStream_t s);
-}  // namespace palial
+cudaError_t mps_configure();
 
-using namespace palial;
-
-namespace {
-
-// grow-only device buffer
-struct DevBuf {
-    void *ptr = nullptr;
-    size_t bytes = 0;
-    cudaError_t ensure(size_t want) {
-        if (want <= bytes) return cudaSuccess;
-        if (ptr) cudaFree(ptr);
-        ptr = nullptr;
-        bytes = 0;
-        cudaError_t e = cudaMalloc(&ptr, want);
-        if (e == cudaSuccess) bytes = want;
-        return e;
-    }
-    void release() {
-        if (ptr) cudaFree(ptr);
-        ptr = nullptr;
-        bytes = 0;
-    }
-    template <class T>
-    T *as() const { return static_cast<T *>(ptr); }
-};
-
-struct TraceState {
-    Dag dag;                       // the DAG of the last traced run (records in dispatch order)
-    std::vector<TraceRec> recs;    // by dispatch index
-    bool valid = false;
-};
-
-struct State {
-    bool init = false;
-    int device = -1;
-    int sms = 0;
-    int occupancy = 1;
-    DevBuf tasks, counters, status, ticket, trace, scratch, mat, smat, kbuf, probe;
-    std::map<std::tuple<int, int, int, int, int, int, unsigned>, std::shared_ptr<Dag>> dags;
-    unsigned long long uploaded = 0;    // uid of the DAG whose records are on the device
-    unsigned long long next_uid = 1;
-    TraceState last_trace;
-    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
-};
 State g;
 
-int set_status(palial_status *st, int code, const char *fmt = nullptr, ...) {
+int set_status(palial_status *st, int code, const char *fmt, ...) {
     if (st) {
         st->code = code;
         if (fmt) {
@@ -104,12 +61,6 @@ int cuda_fail(palial_status *st, cudaError_t e, const char *what) {
     if (st) st->cuda_error = (int)e;
     return set_status(st, PALIAL_ERR_CUDA, "%s: %s", what, cudaGetErrorString(e));
 }
-
-#define CK(call, what)                                    \
-    do {                                                  \
-        cudaError_t _e = (call);                          \
-        if (_e != cudaSuccess) return cuda_fail(st, _e, what); \
-    } while (0)
 
 int ensure_init(palial_status *st) {
     if (g.init) {
@@ -130,8 +81,7 @@ int auto_block(int alg, int n, int nb) {
     return std::max(64, bs);
 }
 
-std::shared_ptr<Dag> get_dag(int alg, int n, int nb, int bs, int priority, int workers, unsigned seed,
-                             palial_status *st) {
+std::shared_ptr<Dag> get_dag(int alg, int n, int nb, int bs, int priority, int workers, unsigned seed) {
     auto key = std::make_tuple(alg, n, nb, bs, priority, workers, seed);
     auto it = g.dags.find(key);
     if (it != g.dags.end()) return it->second;
@@ -140,11 +90,59 @@ std::shared_ptr<Dag> get_dag(int alg, int n, int nb, int bs, int priority, int w
     d->uid = g.next_uid++;
     if (g.dags.size() > 16) g.dags.clear();
     g.dags[key] = d;
-    (void)st;
     return d;
 }
 
-}  // namespace
+int sched_prepare(SchedCtx &c, const std::shared_ptr<Dag> &dag, double *dA, double *dS, int workers, int trace,
+                  double timeout_s, SchedParams &p, palial_status *st) {
+    const int ntasks = (int)dag->records.size();
+    void *old_tasks = c.tasks.ptr;
+    PALIAL_CK(c.tasks.ensure(sizeof(Task) * (size_t)std::max(1, ntasks)), "alloc tasks");
+    if (c.tasks.ptr != old_tasks) c.uploaded = 0;  // reallocated: contents gone
+    if (c.uploaded != dag->uid) {
+        c.uploaded = 0;
+        PALIAL_CK(cudaMemcpy(c.tasks.ptr, dag->records.data(), sizeof(Task) * ntasks, cudaMemcpyHostToDevice),
+                  "upload tasks");
+        c.uploaded = dag->uid;
+    }
+    // one spare counter past the objects: nothing ever signals it (used by the stall test)
+    PALIAL_CK(c.counters.ensure(sizeof(unsigned) * (size_t)(dag->nobj + 1)), "alloc counters");
+    PALIAL_CK(c.status.ensure(sizeof(int) * ST_NSLOTS + 64), "alloc status");
+    PALIAL_CK(c.ticket.ensure(64), "alloc ticket");
+    long long per_worker = 0;
+    const long long scr = sched_scratch_doubles(dag->alg, dag->n, dag->nb, dag->bs, workers, &per_worker);
+    PALIAL_CK(c.scratch.ensure(sizeof(double) * (size_t)std::max<long long>(1, scr)), "alloc scratch");
+    if (trace) PALIAL_CK(c.trace.ensure(sizeof(TraceRec) * (size_t)ntasks), "alloc trace");
+    p = SchedParams{};
+    p.tasks = c.tasks.as<Task>();
+    p.ntasks = ntasks;
+    p.ticket = c.ticket.as<unsigned>();
+    p.counters = c.counters.as<unsigned>();
+    p.status = c.status.as<int>();
+    p.trace = trace ? c.trace.as<TraceRec>() : nullptr;
+    p.A = dA;
+    p.S = dS;
+    p.scratch = c.scratch.as<double>();
+    p.scratch_per_worker = per_worker;
+    p.n = dag->n;
+    p.nb = dag->nb;
+    p.bs = dag->bs;
+    p.timeout_ns = (unsigned long long)((timeout_s > 0 ? timeout_s : 120.0) * 1e9);
+    return PALIAL_OK;
+}
+
+cudaError_t sched_enqueue(SchedCtx &c, const SchedParams &p, int nobj, int workers, bool clear_status, cudaStream_t s) {
+    cudaError_t e = cudaMemsetAsync(c.counters.ptr, 0, sizeof(unsigned) * (size_t)(nobj + 1), s);
+    if (e == cudaSuccess && clear_status) e = cudaMemsetAsync(c.status.ptr, 0, sizeof(int) * ST_NSLOTS, s);
+    if (e == cudaSuccess) e = cudaMemsetAsync(c.ticket.ptr, 0, 64, s);
+    if (e == cudaSuccess) e = sched_launch(p, workers, s);
+    return e;
+}
+}  // namespace palial
+
+using namespace palial;
+
+#define CK(call, what) PALIAL_CK(call, what)
 
 extern "C" {
 
@@ -181,6 +179,7 @@ int palial_gpu_init(int device) {
     g.device = device;
     g.sms = prop.multiProcessorCount;
     if (sched_configure() != cudaSuccess) return PALIAL_ERR_CUDA;
+    if (mps_configure() != cudaSuccess) return PALIAL_ERR_CUDA;
     g.occupancy = std::max(1, sched_occupancy());
     if (!g.ev0) cudaEventCreate(&g.ev0);
     if (!g.ev1) cudaEventCreate(&g.ev1);
@@ -190,11 +189,10 @@ int palial_gpu_init(int device) {
 
 int palial_gpu_finalize(void) {
     if (!g.init) return PALIAL_OK;
-    for (DevBuf *b : {&g.tasks, &g.counters, &g.status, &g.ticket, &g.trace, &g.scratch, &g.mat, &g.smat, &g.kbuf,
-                      &g.probe})
-        b->release();
+    g.main.release();
+    g.diag.release();
+    for (DevBuf *b : {&g.mat, &g.smat, &g.kbuf, &g.probe}) b->release();
     g.dags.clear();
-    g.uploaded = 0;
     return PALIAL_OK;
 }
 
@@ -223,29 +221,15 @@ int palial_gpu_factor_dev(int alg, double *dA, double *dS, int n, int nb, const 
     const int workers = sms * wps;
     std::shared_ptr<Dag> dag;
     try {
-        dag = get_dag(alg, n, nb, bs, o.priority, workers, o.shuffle_seed, st);
+        dag = get_dag(alg, n, nb, bs, o.priority, workers, o.shuffle_seed);
     } catch (const std::exception &ex) {
         return set_status(st, PALIAL_ERR_ARG, "%s", ex.what());
     }
     const int ntasks = (int)dag->records.size();
     cudaStream_t s = static_cast<cudaStream_t>(stream);
-    void *old_tasks = g.tasks.ptr;
-    CK(g.tasks.ensure(sizeof(Task) * (size_t)std::max(1, ntasks)), "alloc tasks");
-    if (g.tasks.ptr != old_tasks) g.uploaded = 0;  // reallocated: contents gone
-    if (g.uploaded != dag->uid) {
-        g.uploaded = 0;
-        CK(cudaMemcpy(g.tasks.ptr, dag->records.data(), sizeof(Task) * ntasks, cudaMemcpyHostToDevice), "upload tasks");
-        g.uploaded = dag->uid;
-    }
-    // one spare counter past the objects: nothing ever signals it (used by the stall test)
-    CK(g.counters.ensure(sizeof(unsigned) * (size_t)(dag->nobj + 1)), "alloc counters");
-    CK(g.status.ensure(sizeof(int) * ST_NSLOTS + 64), "alloc status");
-    CK(g.ticket.ensure(64), "alloc ticket");
-    long long per_worker = 0;
-    const long long scr = sched_scratch_doubles(alg, n, nb, dag->bs, workers, &per_worker);
-    CK(g.scratch.ensure(sizeof(double) * (size_t)std::max<long long>(1, scr)), "alloc scratch");
-    if (o.trace) CK(g.trace.ensure(sizeof(TraceRec) * (size_t)ntasks), "alloc trace");
-    CK(cudaMemsetAsync(g.counters.ptr, 0, sizeof(unsigned) * (dag->nobj + 1), s), "clear counters");
+    SchedParams p;
+    rc = sched_prepare(g.main, dag, dA, dS, workers, o.trace, o.timeout_s, p, st);
+    if (rc) return rc;
     // Fault injection for tests (opts.reserved[0] = r + 1): record r additionally waits on the
     // spare counter, which nothing signals, so its wait must end by deadline with
     // PALIAL_ERR_TIMEOUT.  The uploaded copy is patched and restored afterwards.
@@ -262,41 +246,21 @@ int palial_gpu_factor_dev(int alg, double *dA, double *dS, int n, int nb, const 
             t.wait_obj[2] = (uint32_t)dag->nobj;
             t.wait_cnt[2] = 1;
         }
-        CK(cudaMemcpy(g.tasks.as<Task>() + stall, &t, sizeof(Task), cudaMemcpyHostToDevice), "inject stall");
+        CK(cudaMemcpy(g.main.tasks.as<Task>() + stall, &t, sizeof(Task), cudaMemcpyHostToDevice), "inject stall");
     }
-    CK(cudaMemsetAsync(g.status.ptr, 0, sizeof(int) * ST_NSLOTS, s), "clear status");
-    CK(cudaMemsetAsync(g.ticket.ptr, 0, 64, s), "clear ticket");
-
-    SchedParams p{};
-    p.tasks = g.tasks.as<Task>();
-    p.ntasks = ntasks;
-    p.ticket = g.ticket.as<unsigned>();
-    p.counters = g.counters.as<unsigned>();
-    p.status = g.status.as<int>();
-    p.trace = o.trace ? g.trace.as<TraceRec>() : nullptr;
-    p.A = dA;
-    p.S = dS;
-    p.scratch = g.scratch.as<double>();
-    p.scratch_per_worker = per_worker;
-    p.n = n;
-    p.nb = nb;
-    p.bs = dag->bs;
-    const double to = o.timeout_s > 0 ? o.timeout_s : 120.0;
-    p.timeout_ns = (unsigned long long)(to * 1e9);
-
     const auto w0 = std::chrono::steady_clock::now();
     CK(cudaEventRecord(g.ev0, s), "event");
-    CK(sched_launch(p, workers, s), "launch scheduler");
+    CK(sched_enqueue(g.main, p, dag->nobj, workers, true, s), "launch scheduler");
     CK(cudaEventRecord(g.ev1, s), "event");
     CK(cudaEventSynchronize(g.ev1), "scheduler run");
     float ms = 0.f;
     cudaEventElapsedTime(&ms, g.ev0, g.ev1);
     int hs[ST_NSLOTS];
-    CK(cudaMemcpy(hs, g.status.ptr, sizeof hs, cudaMemcpyDeviceToHost), "read status");
+    CK(cudaMemcpy(hs, g.main.status.ptr, sizeof hs, cudaMemcpyDeviceToHost), "read status");
     unsigned tick = 0;
-    CK(cudaMemcpy(&tick, g.ticket.ptr, sizeof tick, cudaMemcpyDeviceToHost), "read ticket");
+    CK(cudaMemcpy(&tick, g.main.ticket.ptr, sizeof tick, cudaMemcpyDeviceToHost), "read ticket");
     if (stall >= 0 && stall < ntasks)
-        CK(cudaMemcpy(g.tasks.as<Task>() + stall, &saved, sizeof(Task), cudaMemcpyHostToDevice), "restore record");
+        CK(cudaMemcpy(g.main.tasks.as<Task>() + stall, &saved, sizeof(Task), cudaMemcpyHostToDevice), "restore record");
     const auto w1 = std::chrono::steady_clock::now();
     if (st) {
         st->ntasks = std::min<long long>(tick, ntasks);
@@ -311,7 +275,7 @@ int palial_gpu_factor_dev(int alg, double *dA, double *dS, int n, int nb, const 
     if (o.trace && hs[ST_CODE] == 0) {
         g.last_trace.dag = *dag;
         g.last_trace.recs.resize(ntasks);
-        CK(cudaMemcpy(g.last_trace.recs.data(), g.trace.ptr, sizeof(TraceRec) * ntasks, cudaMemcpyDeviceToHost),
+        CK(cudaMemcpy(g.last_trace.recs.data(), g.main.trace.ptr, sizeof(TraceRec) * ntasks, cudaMemcpyDeviceToHost),
            "read trace");
         g.last_trace.valid = true;
     }
@@ -375,13 +339,14 @@ static int tile_call(int type, int nb, int ld, double *p0, double *p1, double *p
     if (nb <= 0 || nb % 64 || ld < nb) return PALIAL_ERR_ARG;
     // scratch: 2 strips of nb x 64 (QR update kernels)
     const size_t need = sizeof(double) * ((size_t)2 * nb * 64);
-    CK(g.scratch.ensure(need), "alloc scratch");
-    CK(g.status.ensure(sizeof(int) * ST_NSLOTS + 64), "alloc status");
-    CK(cudaMemset(g.status.ptr, 0, sizeof(int) * ST_NSLOTS), "clear status");
-    CK(tile_task_launch(type, nb, ld, p0, p1, p2, p3, g.scratch.as<double>(), g.status.as<int>(), nullptr), "launch");
+    CK(g.main.scratch.ensure(need), "alloc scratch");
+    CK(g.main.status.ensure(sizeof(int) * ST_NSLOTS + 64), "alloc status");
+    CK(cudaMemset(g.main.status.ptr, 0, sizeof(int) * ST_NSLOTS), "clear status");
+    CK(tile_task_launch(type, nb, ld, p0, p1, p2, p3, g.main.scratch.as<double>(), g.main.status.as<int>(), nullptr),
+       "launch");
     CK(cudaDeviceSynchronize(), "tile kernel");
     int hs[ST_NSLOTS];
-    CK(cudaMemcpy(hs, g.status.ptr, sizeof hs, cudaMemcpyDeviceToHost), "status");
+    CK(cudaMemcpy(hs, g.main.status.ptr, sizeof hs, cudaMemcpyDeviceToHost), "status");
     if (hs[ST_CODE]) return hs[ST_CODE];
     if (hs[ST_ZEROPIV]) return PALIAL_WARN_ZERO_PIVOT;
     return PALIAL_OK;

@@ -1,0 +1,98 @@
+"""Mixed precision: the tcgen05 trailing update against a torch FP32 reference computed from
+the same quantized operands, and mixed-precision factorization + iterative refinement
+against numpy's FP64 solution (backward error gate 1e-14 * N, the target of the path)."""
+import numpy as np
+import pytest
+
+import palial_gb300 as P
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+torch = pytest.importorskip("torch")
+
+PREC = {1: "bf16", 2: "fp8", 3: "bf16x3"}
+
+
+def quant(x, prec, nb):
+    """Operand quantization of the kernel: x is (rows, nb*t) float32 panel, tiles along dim 1."""
+    if prec == 1:
+        return x.bfloat16().float()
+    if prec == 3:
+        hi = x.bfloat16().float()
+        return hi, (x - hi).bfloat16().float()
+    out = torch.empty_like(x)
+    for t in range(x.shape[1] // nb):
+        blk = x[:, t * nb:(t + 1) * nb]
+        s = blk.abs().max() / torch.tensor(448.0, dtype=torch.float32, device=x.device)
+        inv = torch.tensor(1.0, dtype=torch.float32, device=x.device) / s
+        out[:, t * nb:(t + 1) * nb] = (blk * inv).to(torch.float8_e4m3fn).float() * s
+    return out
+
+
+def prod(a, b, prec, nb):
+    """a: (nb x r1) operand whose columns are output rows, b: (nb x r2): returns a^T b."""
+    if prec == 3:
+        ah, al = quant(a, 3, nb)
+        bh, bl = quant(b, 3, nb)
+        return ah.T @ bh + ah.T @ bl + al.T @ bh
+    return quant(a, prec, nb).T @ quant(b, prec, nb)
+
+
+@pytest.mark.parametrize("prec", [1, 2, 3])
+@pytest.mark.parametrize("alg", [0, 1])
+def test_tcgen05_trailing_update(alg, prec):
+    n, nb, k = 1536, 512, 0
+    a = torch.from_numpy(O.gen_uniform(21 + alg, n).astype(np.float32)).cuda()
+    w = torch.from_numpy(O.to_tiles(a.cpu().numpy().astype(np.float64), nb).astype(np.float32)).cuda()
+    rc = P.lib().palial_gpu_mp_update_step(alg, prec, w.data_ptr(), n, nb, k)
+    torch.cuda.synchronize()
+    assert rc == 0
+    got = torch.from_numpy(O.from_tiles(w.cpu().numpy().astype(np.float64), n, nb)).cuda().float()
+    r0 = (k + 1) * nb
+    kk = slice(k * nb, (k + 1) * nb)
+    if alg == 0:
+        upd = prod(a[kk, r0:], a[kk, r0:], prec, nb)          # U(k,n)^T U(k,m)
+    else:
+        # L(m,k) U(k,n): the L panel enters as its transpose (columns = output rows)
+        upd = prod(a[r0:, kk].T.contiguous(), a[kk, r0:], prec, nb)
+    ref = a.clone()
+    ref[r0:, r0:] -= upd
+    if alg == 0:  # only tile pairs (n <= m) are updated
+        mt = n // nb
+        for ti in range(k + 1, mt):
+            for tj in range(k + 1, ti):
+                ref[ti * nb:(ti + 1) * nb, tj * nb:(tj + 1) * nb] = a[ti * nb:(ti + 1) * nb, tj * nb:(tj + 1) * nb]
+    err = float(torch.linalg.norm(got - ref) / torch.linalg.norm(upd))
+    assert err <= 1e-4, err
+    # the panel itself and the leading tiles are untouched
+    assert torch.equal(got[kk, :], a[kk, :]) and torch.equal(got[:, kk], a[:, kk])
+
+
+def dominant(seed, n):
+    a = np.full((n, n), 0.5)
+    u = (O.gen_uniform(seed, n, 1)[:, 0] + 1.0) * 0.5
+    a[np.diag_indices(n)] = 173.0 * u + 173.0
+    return a
+
+
+@pytest.mark.parametrize("prec", ["bf16", "bf16x3", "fp8", "fp64"])
+@pytest.mark.parametrize("alg", ["cholesky", "lu"])
+def test_solve_ir_reaches_fp64_backward_error(alg, prec):
+    n, nb, nrhs = 2048, 512, 16
+    a = O.gen_spd(0, n) if alg == "cholesky" else dominant(3, n)
+    b = O.gen_uniform(5, n, nrhs, stream=O.STREAM_RHS)
+    da = torch.from_numpy(O.to_tiles(a, nb)).cuda()
+    db = torch.from_numpy(np.asfortranarray(b).ravel(order="F")).cuda()
+    dx = torch.zeros_like(db)
+    st = P.solve_ir(alg, da.data_ptr(), n, nb, db.data_ptr(), dx.data_ptr(), nrhs, precision=prec,
+                    ir_max_iter=100, raise_on_error=False)
+    x = dx.cpu().numpy().reshape(nrhs, n).T
+    r = b - a @ x
+    eta = np.max(np.abs(r).max(0) / (np.abs(a).sum(1).max() * np.abs(x).max(0) + np.abs(b).max(0)))
+    xref = np.linalg.solve(a, b)
+    fwd = np.max(np.abs(x - xref).max(0) / np.abs(xref).max(0))
+    print(alg, prec, "iters", st.ir_iters, "eta(dev)", st.backward_error, "eta(host)", eta, "fwd", fwd,
+          "factor s", st.factor_seconds, "total s", st.seconds)
+    assert st.code in (0, 1), st.message
+    assert eta <= 1e-14 * n and st.backward_error <= 1e-14 * n
+    assert fwd <= 1e-10
