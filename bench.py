@@ -1,24 +1,32 @@
 """Benchmark: tiled Cholesky at N = 32768, NB = 512 on one GB300 (per GPU).
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+                    [--suite fp64|kappa]
 
-A step is one factorization of a device-resident N x N SPD matrix (B B^T + N I, B on a
-2^-7 grid in [-1, 1), seed 0; the reference's tile layout) through the library's
-device-pointer entry point, including the restore of the input from a pristine copy
-(8.6 GB device-to-device).  Inputs (8.6 GB) are far larger than L2 (129 MB), so no flush
-is needed.  value = algorithmic FP64 flops (N^3/3) per step / step time, whole job (sum
-over ranks; replicas: each rank factors its own matrix, no collective on the data path).
+A step is one solve A X = B (16 right-hand sides, uniform [-1, 1)) of a device-resident
+SPD matrix A = B B^T + N I (seed = rank; the reference's tile layout) by the mixed-precision
+path: BF16 trailing updates on tcgen05 with FP32 accumulation, FP64 diagonal tiles, FP32
+panels, FP64 residuals and refinement to the FP64-level normwise backward error
+(<= 1e-14 * N).  value = FP64-equivalent algorithmic flops (N^3/3) / time to solution
+(factorization + refinement), summed over ranks (replicas, no collective on the data path).
+Inputs (8.6 GB) are far larger than L2 (129 MB): no flush is needed.
 
 The JSON line also carries:
-  e2e           the same metric through the host-buffer C ABI entry point
-                (palial_gpu_cholesky on pinned host memory: H2D + factor + D2H per step);
-  roofline      the scheduler kernel's FP64 rate against the FP64 peak measured in this
-                run with cuBLAS DGEMM (no FP64 figure exists in MEASURED_PEAKS.json);
-  cpu_baseline  the oracle's OpenMP port of the reference (same task DAG, same OpenBLAS
-                calls) on this host's cores, on a bounded sample (N = 16384);
+  fp64_tiled    the plain FP64 tiled factorization (persistent scheduler, FP64 DFMA) of the
+                same matrix: its TFLOP/s and the mixed/FP64 speed-up;
+  e2e           the same solve through the host-buffer C ABI (palial_gpu_solve_ir_host on
+                pinned host memory: A and B copied in, X copied out, every step);
+  roofline      the tcgen05 trailing-update kernel (the mixed path's tensor-core kernel),
+                timed live on the largest step (k = 0): HBM-bound at K = NB = 512 with FP32
+                C, so bytes per launch / time against MEASURED_PEAKS.json's hbm_gbs;
+  cpu_baseline  the oracle's OpenMP port of the reference's Cholesky (same task DAG, same
+                OpenBLAS calls) on this host's cores, on a bounded sample (N = 16384);
   clocks        nvidia-smi samples taken during the timed region.
 `--impl reference` times the reference's CPU implementation (the oracle port, OpenMP, all
 host cores) on the same metric, one bounded sample (N = 16384) per step.
+`--suite fp64` prints one line per FP64 factorization of configs N in {16384, 32768} for
+Cholesky, LU and QR; `--suite kappa` one line per kappa in {1e2, 1e6, 1e10}, algorithm and
+precision at N = 32768 (A = U diag(s) V^T, 64 Householder reflectors each side).
 """
 from __future__ import annotations
 
@@ -178,6 +186,80 @@ def run_reference(args, rank: int, world: int) -> None:
     print(json.dumps(line), flush=True)
 
 
+def peaks() -> dict:
+    try:
+        return json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except (OSError, ValueError):
+        return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "source": "fallback"}
+
+
+def time_update_kernel(P, torch, n: int) -> dict:
+    """Live CUDA-event timing of one tcgen05 trailing update (step k = 0, BF16) on an FP32
+    tile matrix: flops and algorithmic bytes per launch (C read + write in FP32, packed
+    panel read once)."""
+    w = torch.randn(n * n, dtype=torch.float32, device="cuda")
+    for _ in range(2):
+        P.lib().palial_gpu_mp_update_step(0, 1, w.data_ptr(), n, NB, 0)
+    ts = []
+    for _ in range(3):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        P.lib().palial_gpu_mp_update_step(0, 1, w.data_ptr(), n, NB, 0)
+        e1.record()
+        torch.cuda.synchronize()
+        ts.append(e0.elapsed_time(e1) * 1e-3)
+    del w
+    torch.cuda.empty_cache()
+    r = n // NB - 1
+    pairs = r * (r + 1) // 2
+    flop = pairs * 2.0 * NB ** 3
+    byts = pairs * NB * NB * 8.0 + r * NB * NB * (4.0 + 2.0)   # C rmw + panel f32 read + bf16 write/read
+    t = min(ts)
+    return {"seconds": t, "flop": flop, "bytes": byts}
+
+
+def run_suite(args, P, torch) -> None:
+    import numpy as np
+    if args.suite == "fp64":
+        for alg in ("cholesky", "lu", "qr"):
+            for n in (16384, 32768):
+                d0 = torch.empty(n * n, dtype=torch.float64, device="cuda")
+                if alg == "cholesky":
+                    P.gen_spd(d0.data_ptr(), n, NB, 0)
+                else:
+                    P.gen_uniform(d0.data_ptr(), n, NB, 1)
+                s = torch.zeros_like(d0) if alg == "qr" else None
+                d = d0.clone()
+                st = P.factor_dev(alg, d.data_ptr(), s.data_ptr() if s is not None else None, n, NB)
+                probe = P.residual_probe(alg, d0.data_ptr(), d.data_ptr(), n, NB, 8)
+                print(json.dumps({"suite": "fp64", "alg": alg, "n": n, "nb": NB, "seconds": st.seconds,
+                                  "tflops": st.tflops, "residual_probe": probe,
+                                  "note": "TFLOP/s from N^3/3, 2N^3/3, 4N^3/3"}), flush=True)
+                del d, d0, s
+                torch.cuda.empty_cache()
+        return
+    n, nrhs = args.n, 16
+    b = torch.from_numpy(np.asfortranarray(
+        __import__("oracle.oracle", fromlist=["x"]).gen_uniform(5, n, nrhs, stream=2)).ravel(order="F")).cuda()
+    for alg in ("cholesky", "lu"):
+        for kappa in (1e2, 1e6, 1e10):
+            da = torch.empty(n * n, dtype=torch.float64, device="cuda")
+            P.gen_kappa(da.data_ptr(), n, NB, kappa, alg == "cholesky", seed=7)
+            for prec in ("bf16", "fp8", "bf16x3", "auto"):
+                dx = torch.zeros_like(b)
+                st = P.solve_ir(alg, da.data_ptr(), n, NB, b.data_ptr(), dx.data_ptr(), nrhs, precision=prec,
+                                ir_max_iter=30, raise_on_error=False)
+                print(json.dumps({"suite": "kappa", "alg": alg, "n": n, "kappa": kappa, "precision": prec,
+                                  "converged": st.code in (0, 1), "code": st.code, "ir_iters": st.ir_iters,
+                                  "gmres_iters": st.gmres_iters, "backward_error": st.backward_error,
+                                  "seconds": st.seconds, "factor_seconds": st.factor_seconds, "shift": st.shift,
+                                  "tflops_fp64_equiv": st.tflops,
+                                  "precision_used": P.PREC_NAME.get(int(st.kappa_est), prec)
+                                  if prec == "auto" else prec}), flush=True)
+            del da
+            torch.cuda.empty_cache()
+
+
 def main() -> None:
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -187,6 +269,9 @@ def main() -> None:
     ap.add_argument("--e2e-steps", type=int, default=2)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--n", type=int, default=N)
+    ap.add_argument("--precision", default="bf16")
+    ap.add_argument("--suite", default=None, choices=[None, "fp64", "kappa"])
+    ap.add_argument("--no-fp64", action="store_true")
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)
     rank, world, local = dist_info()
@@ -198,19 +283,24 @@ def main() -> None:
     import torch
 
     import palial_gb300 as P
+    from oracle import oracle as O
 
-    n = args.n
+    n, nrhs = args.n, 16
     torch.cuda.set_device(local)
     if world > 1:
         import torch.distributed as dist
         dist.init_process_group("nccl")
     P.init(local)
+    if args.suite:
+        if rank == 0:
+            run_suite(args, P, torch)
+        return
     stream = torch.cuda.current_stream()
-    peak = fp64_peak_tflops(torch)
-
     a0 = torch.empty(n * n, dtype=torch.float64, device="cuda")
-    a = torch.empty_like(a0)
     P.gen_spd(a0.data_ptr(), n, NB, seed=rank)
+    bh = np.asfortranarray(O.gen_uniform(5, n, nrhs, stream=O.STREAM_RHS))
+    b = torch.from_numpy(bh.ravel(order="F")).cuda()
+    x = torch.zeros_like(b)
     torch.cuda.synchronize()
 
     def barrier():
@@ -218,51 +308,71 @@ def main() -> None:
             torch.distributed.barrier()
         torch.cuda.synchronize()
 
-    def step() -> float:
-        a.copy_(a0)
-        st = P.factor_dev("cholesky", a.data_ptr(), None, n, NB, stream=stream.cuda_stream, allow_warn=False)
-        return st.seconds
+    def step() -> P.Status:
+        return P.solve_ir("cholesky", a0.data_ptr(), n, NB, b.data_ptr(), x.data_ptr(), nrhs,
+                          precision=args.precision, stream=stream.cuda_stream, raise_on_error=False)
 
     for _ in range(args.warmup):
         step()
-    kern = []
+    sts = []
     barrier()
+    launches0 = P.lib().palial_gpu_kernel_launches()
     with ClockSampler(local) as clk:
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e0.record(stream)
         for _ in range(args.steps):
-            kern.append(step())
+            sts.append(step())
         e1.record(stream)
         barrier()
     total = e0.elapsed_time(e1) * 1e-3
+    gpu_launches = P.lib().palial_gpu_kernel_launches() - launches0
     if world > 1:
         t = torch.tensor([total], device="cuda")
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
         total = float(t.item())
     per_step = total / args.steps
     value = world * flops(n) / per_step * 1e-12
-    resid = P.residual_probe("cholesky", a0.data_ptr(), a.data_ptr(), n, NB, 8)
+    converged = all(st.code in (0, 1) for st in sts)
+    eta = max(st.backward_error for st in sts)
+    launches = sts[-1].ir_iters  # informational
 
-    # e2e: host buffers through the C ABI (H2D + factor + D2H inside each timed step)
+    # plain FP64 tiled factorization of the same matrix (one timed run after the DAG is built)
+    fp64 = None
+    if not args.no_fp64:
+        a = torch.empty_like(a0)
+        a.copy_(a0)
+        P.factor_dev("cholesky", a.data_ptr(), None, n, NB, stream=stream.cuda_stream, allow_warn=False)
+        a.copy_(a0)
+        st64 = P.factor_dev("cholesky", a.data_ptr(), None, n, NB, stream=stream.cuda_stream, allow_warn=False)
+        fp64 = {"tflops": st64.tflops, "seconds": st64.seconds,
+                "residual_probe": P.residual_probe("cholesky", a0.data_ptr(), a.data_ptr(), n, NB, 8),
+                "speedup_mixed_over_fp64": (flops(n) / per_step * 1e-12) / st64.tflops}
+        del a
+        torch.cuda.empty_cache()
+
+    # roofline: live timing of the tcgen05 update kernel at its largest step
+    pk = peaks()
+    upd = time_update_kernel(P, torch, n)
+    gbs = upd["bytes"] / upd["seconds"] * 1e-9
+
+    # e2e: host buffers through the C ABI
     host = torch.empty(n * n, dtype=torch.float64, pin_memory=True)
+    host.copy_(a0.cpu())
     host_np = host.numpy()
-    a0_host = a0.cpu()
-    del a
-    torch.cuda.empty_cache()
+    xh = np.zeros((nrhs, n))
+    bhc = np.ascontiguousarray(bh.T)  # column-major n x nrhs == row-major nrhs x n
     e2e_times = []
     for i in range(1 + args.e2e_steps):
-        host.copy_(a0_host)
         barrier()
         t0 = time.perf_counter()
-        P.cholesky(host_np, n, NB)
+        P.solve_ir_host("cholesky", host_np, n, NB, bhc, xh, nrhs, precision=args.precision, raise_on_error=False)
         barrier()
         if i >= 1:
             e2e_times.append(time.perf_counter() - t0)
-    e2e_sec = sum(e2e_times) / max(1, len(e2e_times)) if e2e_times else float("nan")
+    e2e_sec = sum(e2e_times) / len(e2e_times) if e2e_times else float("nan")
     e2e_value = world * flops(n) / e2e_sec * 1e-12
-    del host, a0_host
+    del host
 
-    line = None
     if rank == 0:
         cpu = None
         if not args.no_cpu:
@@ -272,26 +382,29 @@ def main() -> None:
             cpu = {"value": v, "unit": "TFLOP/s", "cores": nthreads, "kind": "port",
                    "sample": f"one Cholesky N={CPU_N} NB={NB} ({sec:.1f} s): the oracle's OpenMP restatement of "
                              "reference src/cholesky.h over OpenBLAS on all host cores"}
-        kern_avg = sum(kern) / len(kern)
-        achieved = flops(n) / kern_avg * 1e-12
         line = {
             "metric": METRIC, "value": value, "unit": "TFLOP/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": per_step * 1e3, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": f"tiled Cholesky FP64 (plain path), N={n}, NB={NB}, scheduler block 256, "
-                                   "SPD B*B^T+N*I seed=rank, device-resident; inputs 8.6 GB >> L2 (no flush needed)",
-                       "n": n, "nb": NB, "precision": "fp64", "parallelism": f"replicas x{world}"},
-            "e2e": {"value": e2e_value, "unit": "TFLOP/s", "h2d_bytes_per_step": 8 * n * n,
-                    "d2h_bytes_per_step": 8 * n * n},
-            "roofline": {"bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
-                         "frac": achieved / peak, "traffic": None,
-                         "kernel": "sched_f64_kernel (persistent scheduler, 1 launch per step)",
-                         "peak_source": "FP64 cuBLAS DGEMM 8192^3 measured in this run (no FP64 peak in "
-                                        "MEASURED_PEAKS.json)"},
+            "vs_baseline": None, "dtype": "bf16", "data": "synthetic",
+            "config": {"workload": f"mixed-precision Cholesky + IR, N={n}, NB={NB}, 16 RHS, {args.precision} "
+                                   "trailing updates on tcgen05 (FP32 accumulate), FP64 diagonal tiles, FP64 "
+                                   "residuals; SPD B*B^T+N*I seed=rank, device-resident; inputs 8.6 GB >> L2 "
+                                   "(no flush needed)",
+                       "n": n, "nb": NB, "nrhs": nrhs, "precision": args.precision,
+                       "parallelism": f"replicas x{world}"},
+            "converged": converged, "backward_error": eta, "ir_iters": launches,
+            "fp64_tiled": fp64,
+            "e2e": {"value": e2e_value, "unit": "TFLOP/s", "h2d_bytes_per_step": 8 * n * n + 8 * n * nrhs,
+                    "d2h_bytes_per_step": 8 * n * nrhs},
+            "roofline": {"bound": "hbm", "achieved": gbs, "peak": pk.get("hbm_gbs", 6800.0), "unit": "GB/s",
+                         "frac": gbs / pk.get("hbm_gbs", 6800.0), "traffic": None,
+                         "kernel": "mp_update_kernel<bf16> (tcgen05, step k=0 of N=%d)" % n,
+                         "tensor_tflops": upd["flop"] / upd["seconds"] * 1e-12,
+                         "tensor_frac_of_bf16_peak": upd["flop"] / upd["seconds"] * 1e-12 / pk.get("bf16_tflops", 1900.0),
+                         "peak_source": "MEASURED_PEAKS.json (of measured)" if "source" not in pk else "fallback"},
             "cpu_baseline": cpu,
             "clocks": clk.summary(),
-            "gpu_launches": args.steps,
-            "residual_probe": resid,
+            "gpu_launches": gpu_launches,
         }
         print(json.dumps(line), flush=True)
     if world > 1:

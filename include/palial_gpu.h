@@ -45,6 +45,7 @@ extern "C" {
 #define PALIAL_PREC_BF16 1         /* trailing updates in BF16 on tcgen05, FP32 accumulate  */
 #define PALIAL_PREC_FP8 2          /* trailing updates in FP8 e4m3, per-tile scale          */
 #define PALIAL_PREC_BF16X3 3       /* trailing updates as 3 BF16 products (split operands)  */
+#define PALIAL_PREC_AUTO 4         /* solve_ir: precision ladder BF16 -> BF16x3 -> FP64      */
 
 /* ---- descriptor ------------------------------------------------------------------------ */
 /* Same field order, types and meaning as the reference's MATRIX_desc
@@ -100,6 +101,7 @@ void palial_opts_default(palial_opts *opts);
 int palial_gpu_init(int device);      /* select device, query SM count; idempotent     */
 int palial_gpu_finalize(void);        /* release cached device buffers                  */
 int palial_gpu_sm_count(void);
+long long palial_gpu_kernel_launches(void);  /* kernels launched by this library so far */
 const char *palial_gpu_error_string(int code);
 
 /* ---- whole factorizations on HOST buffers (drop-in for src/{cholesky,lu,qr}.h) ------------
@@ -136,6 +138,10 @@ int palial_gpu_factor_dev(int alg, double *dA, double *dS, int n, int nb, const 
  * Returns PALIAL_ERR_NOT_CONVERGED (with the reached error in st) if the target is missed. */
 int palial_gpu_solve_ir(int alg, const double *dA, int n, int nb, const double *dB, double *dX,
                         int nrhs, const palial_opts *opts, palial_status *st, void *stream);
+/* Same with host buffers: A in the reference's tile layout (descriptor), B and X n x nrhs
+ * column-major in host memory; includes the host<->device copies. */
+int palial_gpu_solve_ir_host(int alg, const palial_desc *A, const double *B, double *X, int nrhs,
+                             const palial_opts *opts, palial_status *st);
 /* The low-precision factorization alone: dW (n*n floats, tile layout) receives the FP32
  * factors (Cholesky: U in the upper tiles; LU: L\U). */
 int palial_gpu_mp_factor(int alg, const double *dA, float *dW, int n, int nb,
@@ -191,6 +197,12 @@ int palial_gpu_gen_refpattern(double *dA, int n, int nb, uint64_t seed, void *st
 /* Generate into a HOST tile buffer (generated on the device, then copied):
  * kind 0 = uniform, 1 = SPD B B^T + n I, 2 = reference pattern. */
 int palial_gpu_generate(int kind, uint64_t seed, const palial_desc *A);
+
+/* A = U diag(s) V^T with s_i = kappa^(-i/(n-1)) and U, V products of 64 Householder
+ * reflectors with random unit vectors (seeded; V = U when symmetric, then A is made exactly
+ * symmetric).  Tile layout, FP64, on the device.  Condition number kappa by construction. */
+int palial_gpu_gen_kappa(double *dA, int n, int nb, double kappa, int symmetric, uint64_t seed,
+                         void *stream);
 
 /* ---- checks on device buffers --------------------------------------------------------------- */
 /* Normwise relative residual of the factorization against the original matrix dA0 using

@@ -23,7 +23,8 @@ ERR = {
     -7: "device allocation failed", 1: "exact zero pivot skipped",
 }
 ALG = {"cholesky": 0, "lu": 1, "qr": 2}
-PREC = {"fp64": 0, "bf16": 1, "fp8": 2, "bf16x3": 3}
+PREC = {"fp64": 0, "bf16": 1, "fp8": 2, "bf16x3": 3, "auto": 4}
+PREC_NAME = {v: k for k, v in PREC.items()}
 
 
 class PalialError(RuntimeError):
@@ -98,9 +99,13 @@ def lib() -> ctypes.CDLL:
         h.palial_gpu_tile_dtsmqr.argtypes = [i, vp, vp, vp, vp, i]
         h.palial_gpu_tile_dtsmqr_noalloc.argtypes = [i, vp, vp, vp, vp, i, vp]
         h.palial_gpu_error_string.restype = ctypes.c_char_p
+        h.palial_gpu_kernel_launches.restype = ctypes.c_longlong
         h.palial_gpu_solve_ir.argtypes = [i, vp, i, i, vp, vp, i, ctypes.POINTER(Opts), ctypes.POINTER(Status), vp]
         h.palial_gpu_mp_factor.argtypes = [i, vp, vp, i, i, ctypes.POINTER(Opts), ctypes.POINTER(Status), vp]
         h.palial_gpu_mp_update_step.argtypes = [i, i, vp, i, i, i]
+        h.palial_gpu_gen_kappa.argtypes = [vp, i, i, d, i, ctypes.c_uint64, vp]
+        h.palial_gpu_solve_ir_host.argtypes = [i, ctypes.POINTER(Desc), vp, vp, i, ctypes.POINTER(Opts),
+                                               ctypes.POINTER(Status)]
         _lib = h
     return _lib
 
@@ -181,12 +186,28 @@ def solve_ir(alg: str, d_a: int, n: int, nb: int, d_b: int, d_x: int, nrhs: int,
     return st
 
 
+def solve_ir_host(alg: str, a_tiles: np.ndarray, n: int, nb: int, b: np.ndarray, x: np.ndarray, nrhs: int,
+                  raise_on_error: bool = True, **kw) -> Status:
+    """Host-buffer solve: a_tiles (tile layout), b and x (n x nrhs, column-major float64)."""
+    st = Status()
+    rc = lib().palial_gpu_solve_ir_host(ALG[alg], ctypes.byref(desc(a_tiles, n, nb)), b.ctypes.data, x.ctypes.data,
+                                        nrhs, ctypes.byref(make_opts(**kw)), ctypes.byref(st))
+    if raise_on_error:
+        _check(rc, st, allow=(PALIAL_OK, 1))
+    st.code = rc
+    return st
+
+
 def mp_factor(alg: str, d_a: int, d_w: int, n: int, nb: int, stream: int = 0, **kw) -> Status:
     st = Status()
     rc = lib().palial_gpu_mp_factor(ALG[alg], d_a, d_w, n, nb, ctypes.byref(make_opts(**kw)), ctypes.byref(st),
                                     stream or None)
     _check(rc, st, allow=(PALIAL_OK, 1))
     return st
+
+
+def gen_kappa(d_a: int, n: int, nb: int, kappa: float, symmetric: bool, seed: int = 0, stream: int = 0) -> None:
+    _check(lib().palial_gpu_gen_kappa(d_a, n, nb, float(kappa), int(symmetric), seed, stream or None), None)
 
 
 def gen_uniform(d_a: int, n: int, nb: int, seed: int, stream: int = 0) -> None:

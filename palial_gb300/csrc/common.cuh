@@ -72,6 +72,9 @@ struct SchedParams {
     unsigned long long timeout_ns;
 };
 
+// Host: count of kernel launches made by the library (every launch wrapper calls this).
+void note_launch();
+
 #ifdef __CUDACC__
 __device__ __forceinline__ unsigned long long globaltimer_ns() {
     unsigned long long t;

@@ -212,39 +212,47 @@ __global__ void sub_kernel(const double *X, const double *Y, double *Z, long lon
 // host wrappers
 // ---------------------------------------------------------------------------------------
 cudaError_t launch_gen_uniform(double *A, int n, int nb, uint64_t seed, cudaStream_t s) {
+    note_launch();
     gen_uniform_kernel<<<4096, 256, 0, s>>>(A, n, nb, stream_key(seed, STREAM_UNIFORM));
     return cudaGetLastError();
 }
 
 cudaError_t launch_gen_refpattern(double *A, int n, int nb, uint64_t seed, cudaStream_t s) {
+    note_launch();
     gen_refpattern_kernel<<<4096, 256, 0, s>>>(A, n, nb, stream_key(seed, STREAM_UNIFORM));
     return cudaGetLastError();
 }
 
 cudaError_t launch_gen_dense(double *X, long long rows, int cols, uint64_t seed, int stream, cudaStream_t s) {
+    note_launch();
     gen_uniform_dense_kernel<<<2048, 256, 0, s>>>(X, rows, cols, stream_key(seed, (uint64_t)stream));
     return cudaGetLastError();
 }
 
 cudaError_t launch_gen_spd(double *A, int n, int nb, uint64_t seed, int8_t *kbuf, cudaStream_t s) {
+    note_launch();
     gen_k8_kernel<<<4096, 256, 0, s>>>(kbuf, n, stream_key(seed, STREAM_SPD));
     dim3 grid((n + 127) / 128, (n + 127) / 128);  // n % 64 == 0 (checked by the caller)
+    note_launch();
     spd_from_k8_kernel<<<grid, 256, 0, s>>>(kbuf, A, n, nb);
     return cudaGetLastError();
 }
 
 cudaError_t launch_tiled_mm(const double *A, const double *X, double *Y, int n, int nb, int r, int mode, int trans,
                             cudaStream_t s) {
+    note_launch();
     tiled_mm_kernel<<<n / 64, 256, 0, s>>>(A, X, Y, n, nb, r, mode, trans);
     return cudaGetLastError();
 }
 
 cudaError_t launch_sumsq(const double *X, long long len, double *partial, int blocks, cudaStream_t s) {
+    note_launch();
     sumsq_kernel<<<blocks, 256, 0, s>>>(X, len, partial);
     return cudaGetLastError();
 }
 
 cudaError_t launch_sub(const double *X, const double *Y, double *Z, long long len, cudaStream_t s) {
+    note_launch();
     sub_kernel<<<1024, 256, 0, s>>>(X, Y, Z, len);
     return cudaGetLastError();
 }

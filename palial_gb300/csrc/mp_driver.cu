@@ -39,8 +39,6 @@ cudaError_t mps_f64_to_f32(const double *A, float *W, int n, int nb, double shif
 cudaError_t mps_tile_to_f64(const float *w, double *d, int nb, cudaStream_t s);
 cudaError_t mps_tile_to_f32(const double *d, float *w, int nb, int upper_only, cudaStream_t s);
 cudaError_t mps_panel_trsm(float *W, int n, int nb, int k, int kind, cudaStream_t s);
-cudaError_t mps_rhs_diag(const float *W, int n, int nb, int k, float *R, int kind, cudaStream_t s);
-cudaError_t mps_rhs_update(const float *W, int n, int nb, int k, float *R, int kind, cudaStream_t s);
 cudaError_t mps_residual(const double *A, int n, int nb, const double *X, const double *B, double *R, int nrhs,
                          cudaStream_t s);
 cudaError_t mps_norm_inf_matrix(const double *A, int n, int nb, double *out, cudaStream_t s);
@@ -49,6 +47,21 @@ cudaError_t mps_to_f32_rhs(const double *R, float *R32, long long n, int cols, c
 cudaError_t mps_add_correction(double *X, const float *D32, long long n, int cols, const double *scale,
                                cudaStream_t s);
 cudaError_t mps_mark_step(int *status, int k, cudaStream_t s);
+cudaError_t mps_invert_diag(const float *W, int n, int nb, float *Dinv, int kind, cudaStream_t s);
+cudaError_t mps_rhs_step(const float *W, const float *Dinv, int n, int nb, int k, float *R, float *S, int kind,
+                         cudaStream_t s);
+cudaError_t mps_multi_dot(const double *V, int count, const double *w, long long n, int nrhs, double *H,
+                          cudaStream_t s);
+cudaError_t mps_multi_axpy(const double *V, int count, const double *H, double *w, long long n, int nrhs, int assign,
+                           cudaStream_t s);
+cudaError_t mps_scale_cols(const double *w, double *out, long long n, int nrhs, const double *f, cudaStream_t s);
+cudaError_t mps_from_f32_rhs(double *X, const float *D32, long long n, int cols, const double *scale, cudaStream_t s);
+cudaError_t mps_rank1(double *X, int n, int nb, const double *a, const double *b, cudaStream_t s);
+cudaError_t mps_diag(double *X, int n, int nb, double kappa, cudaStream_t s);
+cudaError_t mps_matvec(const double *A, int n, int nb, const double *x, double *y, int trans, cudaStream_t s);
+cudaError_t mps_symmetrize(double *X, int n, int nb, cudaStream_t s);
+cudaError_t launch_gen_dense(double *X, long long rows, int cols, uint64_t seed, int stream, cudaStream_t s);
+cudaError_t launch_sumsq(const double *X, long long len, double *partial, int blocks, cudaStream_t s);
 }  // namespace palial
 
 using namespace palial;
@@ -56,7 +69,8 @@ using namespace palial;
 namespace {
 
 struct MpBufs {
-    DevBuf w, diag, pa_hi, pa_lo, pb_hi, pb_lo, scales, r, r32, x32, norms, work;
+    DevBuf w, diag, pa_hi, pa_lo, pb_hi, pb_lo, scales, r, r32, x32, norms, work, krylov, hbuf, gvec;
+    DevBuf dinv_u, dinv_l, stile;  // FP32 inverses of the diagonal factor tiles, solve scratch
 };
 MpBufs mb;
 
@@ -135,22 +149,207 @@ int mp_factor(int alg, int prec, float *W, int n, int nb, cudaStream_t s, palial
     return PALIAL_OK;
 }
 
-// d = M^-1 r for the FP32 factors in W; R32 (n x 64, zero padded) in/out.
-int mp_apply_inverse(int alg, const float *W, int n, int nb, float *R32, cudaStream_t s, palial_status *st) {
-    const int mt = n / nb;
-    const int fwd_kind = (alg == 0) ? 0 : 2;
-    for (int k = 0; k < mt; k++) {
-        PALIAL_CK(mps_rhs_diag(W, n, nb, k, R32, fwd_kind, s), "forward diag");
-        PALIAL_CK(mps_rhs_update(W, n, nb, k, R32, fwd_kind, s), "forward update");
-    }
-    for (int k = mt - 1; k >= 0; k--) {
-        PALIAL_CK(mps_rhs_diag(W, n, nb, k, R32, 1, s), "backward diag");
-        PALIAL_CK(mps_rhs_update(W, n, nb, k, R32, 1, s), "backward update");
+// Inverses of the diagonal factor tiles (FP32), used by the refinement solves: one parallel
+// launch per factor instead of a chain of single-CTA substitutions.
+int mp_prepare_solves(int alg, const float *W, int n, int nb, cudaStream_t s, palial_status *st) {
+    const size_t bytes = sizeof(float) * (size_t)n * nb;
+    PALIAL_CK(mb.dinv_u.ensure(bytes), "alloc inverses");
+    PALIAL_CK(mb.stile.ensure(sizeof(float) * (size_t)nb * 64), "alloc solve tile");
+    PALIAL_CK(mps_invert_diag(W, n, nb, mb.dinv_u.as<float>(), 1, s), "invert U tiles");
+    if (alg == 1) {
+        PALIAL_CK(mb.dinv_l.ensure(bytes), "alloc inverses");
+        PALIAL_CK(mps_invert_diag(W, n, nb, mb.dinv_l.as<float>(), 2, s), "invert L tiles");
     }
     return PALIAL_OK;
 }
 
+// d = M^-1 r for the FP32 factors in W; R32 (n x 64, zero padded) in/out.  Block forward and
+// backward substitution over tile rows: the diagonal step multiplies by the stored inverse,
+// the update step subtracts the solved tile row from the remaining ones.
+int mp_apply_inverse(int alg, const float *W, int n, int nb, float *R32, cudaStream_t s, palial_status *st) {
+    const int mt = n / nb;
+    float *S = mb.stile.as<float>();
+    const float *fwd_inv = (alg == 0) ? mb.dinv_u.as<float>() : mb.dinv_l.as<float>();
+    const int fwd_kind = (alg == 0) ? 0 : 2;
+    for (int k = 0; k < mt; k++) PALIAL_CK(mps_rhs_step(W, fwd_inv, n, nb, k, R32, S, fwd_kind, s), "forward");
+    for (int k = mt - 1; k >= 0; k--)
+        PALIAL_CK(mps_rhs_step(W, mb.dinv_u.as<float>(), n, nb, k, R32, S, 1, s), "backward");
+    return PALIAL_OK;
+}
+
+// z = M^-1 v for FP64 columns v (n x nrhs), through the FP32 factors (scaled per column).
+int precondition(int alg, const float *W, int n, int nb, const double *v, double *z, int nrhs, double *dscale,
+                 std::vector<double> &hscale, cudaStream_t s, palial_status *st) {
+    PALIAL_CK(mps_colmax(v, n, nrhs, dscale, s), "scale");
+    PALIAL_CK(cudaMemcpyAsync(hscale.data(), dscale, sizeof(double) * nrhs, cudaMemcpyDeviceToHost, s), "scale");
+    PALIAL_CK(cudaStreamSynchronize(s), "scale");
+    for (int j = 0; j < nrhs; j++)
+        if (hscale[j] == 0.0) hscale[j] = 1.0;
+    PALIAL_CK(cudaMemcpyAsync(dscale, hscale.data(), sizeof(double) * nrhs, cudaMemcpyHostToDevice, s), "scale");
+    PALIAL_CK(mps_to_f32_rhs(v, mb.r32.as<float>(), n, nrhs, dscale, s), "to f32");
+    int rc = mp_apply_inverse(alg, W, n, nb, mb.r32.as<float>(), s, st);
+    if (rc) return rc;
+    PALIAL_CK(mps_from_f32_rhs(z, mb.r32.as<float>(), n, nrhs, dscale, s), "from f32");
+    return PALIAL_OK;
+}
+
+// GMRES on M^-1 A d = M^-1 r (left preconditioned, FP64 vectors, one Krylov space per
+// right-hand side, classical Gram-Schmidt applied twice), restart length m, at most maxit
+// iterations; stops when every column's preconditioned residual drops by `rtol`.  d is
+// overwritten.  Returns PALIAL_OK and the iteration count in *iters.
+int gmres(int alg, const double *A, const float *W, int n, int nb, const double *r, double *d, int nrhs, int m,
+          int maxit, double rtol, cudaStream_t s, palial_status *st, int *iters) {
+    const size_t blk = (size_t)n * nrhs;
+    PALIAL_CK(mb.krylov.ensure(sizeof(double) * blk * (m + 3)), "alloc krylov");
+    PALIAL_CK(mb.hbuf.ensure(sizeof(double) * (size_t)(m + 2) * nrhs * 2), "alloc h");
+    double *V = mb.krylov.as<double>();
+    double *w = V + blk * (m + 1);  // work vectors after the basis
+    double *tv = w + blk;
+    double *dH = mb.hbuf.as<double>(), *dH2 = dH + (size_t)(m + 2) * nrhs;
+    double *dscale = mb.norms.as<double>() + 96;
+    std::vector<double> hs(nrhs), hh((size_t)(m + 2) * nrhs), hh2((size_t)(m + 2) * nrhs);
+    PALIAL_CK(cudaMemsetAsync(d, 0, sizeof(double) * blk, s), "d0");
+    int total = 0;
+    bool done = false;
+    while (!done && total < maxit) {
+        // z0 = M^-1 (r - A d)
+        if (total == 0) {
+            int rc = precondition(alg, W, n, nb, r, w, nrhs, dscale, hs, s, st);
+            if (rc) return rc;
+        } else {
+            PALIAL_CK(mps_residual(A, n, nb, d, r, V, nrhs, s), "inner residual");
+            int rc = precondition(alg, W, n, nb, V, w, nrhs, dscale, hs, s, st);
+            if (rc) return rc;
+        }
+        // beta = ||z0||, V0 = z0 / beta
+        PALIAL_CK(mps_multi_dot(w, 1, w, n, nrhs, dH, s), "beta");
+        PALIAL_CK(cudaMemcpyAsync(hh.data(), dH, sizeof(double) * nrhs, cudaMemcpyDeviceToHost, s), "beta");
+        PALIAL_CK(cudaStreamSynchronize(s), "beta");
+        std::vector<double> beta(nrhs);
+        for (int c = 0; c < nrhs; c++) beta[c] = std::sqrt(hh[c]) > 0 ? std::sqrt(hh[c]) : 1.0;
+        PALIAL_CK(cudaMemcpyAsync(dH, beta.data(), sizeof(double) * nrhs, cudaMemcpyHostToDevice, s), "beta");
+        PALIAL_CK(mps_scale_cols(w, V, n, nrhs, dH, s), "v0");
+        // Hessenberg, Givens rotations and rhs g per column (host)
+        std::vector<std::vector<double>> H(nrhs, std::vector<double>((size_t)(m + 1) * m, 0.0));
+        std::vector<std::vector<double>> cs(nrhs, std::vector<double>(m)), sn(nrhs, std::vector<double>(m));
+        std::vector<std::vector<double>> gv(nrhs, std::vector<double>(m + 1, 0.0));
+        for (int c = 0; c < nrhs; c++) gv[c][0] = beta[c];
+        int j = 0;
+        for (; j < m && total < maxit; j++, total++) {
+            // w = M^-1 A V_j
+            PALIAL_CK(mps_residual(A, n, nb, V + blk * j, nullptr, tv, nrhs, s), "A v");
+            int rc = precondition(alg, W, n, nb, tv, w, nrhs, dscale, hs, s, st);
+            if (rc) return rc;
+            // CGS twice: h = V^T w, w -= V h
+            PALIAL_CK(mps_multi_dot(V, j + 1, w, n, nrhs, dH, s), "cgs");
+            PALIAL_CK(mps_multi_axpy(V, j + 1, dH, w, n, nrhs, 0, s), "cgs");
+            PALIAL_CK(mps_multi_dot(V, j + 1, w, n, nrhs, dH2, s), "cgs2");
+            PALIAL_CK(mps_multi_axpy(V, j + 1, dH2, w, n, nrhs, 0, s), "cgs2");
+            PALIAL_CK(mps_multi_dot(w, 1, w, n, nrhs, dH2 + (size_t)(j + 1) * nrhs, s), "norm");
+            PALIAL_CK(cudaMemcpyAsync(hh.data(), dH, sizeof(double) * (j + 1) * nrhs, cudaMemcpyDeviceToHost, s), "h");
+            PALIAL_CK(cudaMemcpyAsync(hh2.data(), dH2, sizeof(double) * (j + 2) * nrhs, cudaMemcpyDeviceToHost, s), "h");
+            PALIAL_CK(cudaStreamSynchronize(s), "h");
+            std::vector<double> hnext(nrhs);
+            bool all_small = true;
+            for (int c = 0; c < nrhs; c++) {
+                double *Hc = H[c].data();
+                for (int l = 0; l <= j; l++) Hc[(size_t)l * m + j] = hh[(size_t)l * nrhs + c] + hh2[(size_t)l * nrhs + c];
+                const double hn = std::sqrt(std::max(0.0, hh2[(size_t)(j + 1) * nrhs + c]));
+                Hc[(size_t)(j + 1) * m + j] = hn;
+                hnext[c] = hn > 0 ? hn : 1.0;
+                for (int l = 0; l < j; l++) {  // previous rotations
+                    const double a = Hc[(size_t)l * m + j], b = Hc[(size_t)(l + 1) * m + j];
+                    Hc[(size_t)l * m + j] = cs[c][l] * a + sn[c][l] * b;
+                    Hc[(size_t)(l + 1) * m + j] = -sn[c][l] * a + cs[c][l] * b;
+                }
+                const double a = Hc[(size_t)j * m + j], b = Hc[(size_t)(j + 1) * m + j];
+                const double rr = std::hypot(a, b);
+                cs[c][j] = rr > 0 ? a / rr : 1.0;
+                sn[c][j] = rr > 0 ? b / rr : 0.0;
+                Hc[(size_t)j * m + j] = rr;
+                Hc[(size_t)(j + 1) * m + j] = 0.0;
+                gv[c][j + 1] = -sn[c][j] * gv[c][j];
+                gv[c][j] = cs[c][j] * gv[c][j];
+                if (std::fabs(gv[c][j + 1]) > rtol * beta[c]) all_small = false;
+            }
+            PALIAL_CK(cudaMemcpyAsync(dH2, hnext.data(), sizeof(double) * nrhs, cudaMemcpyHostToDevice, s), "hn");
+            PALIAL_CK(mps_scale_cols(w, V + blk * (j + 1), n, nrhs, dH2, s), "v next");
+            if (all_small) {
+                j++;
+                total++;
+                done = true;
+                break;
+            }
+        }
+        // y = R^-1 g per column, d += V y
+        const int kdim = j;
+        std::vector<double> ycoef((size_t)kdim * nrhs, 0.0);
+        for (int c = 0; c < nrhs; c++) {
+            const double *Hc = H[c].data();
+            for (int l = kdim - 1; l >= 0; l--) {
+                double v = gv[c][l];
+                for (int q = l + 1; q < kdim; q++) v -= Hc[(size_t)l * m + q] * ycoef[(size_t)q * nrhs + c];
+                ycoef[(size_t)l * nrhs + c] = Hc[(size_t)l * m + l] != 0 ? v / Hc[(size_t)l * m + l] : 0.0;
+            }
+        }
+        if (kdim > 0) {
+            PALIAL_CK(cudaMemcpyAsync(dH, ycoef.data(), sizeof(double) * kdim * nrhs, cudaMemcpyHostToDevice, s), "y");
+            // w = V y ; d += w
+            PALIAL_CK(mps_multi_axpy(V, kdim, dH, w, n, nrhs, 1, s), "V y");
+            std::vector<double> ones(nrhs, -1.0);
+            PALIAL_CK(cudaMemcpyAsync(dH2, ones.data(), sizeof(double) * nrhs, cudaMemcpyHostToDevice, s), "one");
+            PALIAL_CK(mps_multi_axpy(w, 1, dH2, d, n, nrhs, 0, s), "d += w");
+        }
+        PALIAL_CK(cudaStreamSynchronize(s), "gmres cycle");
+    }
+    if (iters) *iters = total;
+    return PALIAL_OK;
+}
+
 }  // namespace
+
+extern "C" int palial_gpu_gen_kappa(double *dA, int n, int nb, double kappa, int symmetric, uint64_t seed,
+                                    void *stream) {
+    palial_status *st = nullptr;
+    if (!dA || n <= 0 || nb <= 0 || n % nb || n % 64 || kappa < 1.0) return PALIAL_ERR_ARG;
+    int rc = ensure_init(nullptr);
+    if (rc) return rc;
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    const int nref = 64;
+    PALIAL_CK(mb.work.ensure(sizeof(double) * ((size_t)n * 2 * nref + (size_t)n + 1024)), "alloc");
+    double *vecs = mb.work.as<double>();               // n x 128 reflector vectors
+    double *y = vecs + (size_t)n * 2 * nref;            // n
+    double *part = y + n;                               // 512 partial sums
+    PALIAL_CK(launch_gen_dense(vecs, n, 2 * nref, seed, 3, s), "vectors");
+    std::vector<double> hp(512), norms(2 * nref);
+    for (int j = 0; j < 2 * nref; j++) {  // unit vectors: divide each by its 2-norm
+        PALIAL_CK(launch_sumsq(vecs + (size_t)j * n, n, part, 512, s), "norm");
+        PALIAL_CK(cudaMemcpyAsync(hp.data(), part, sizeof(double) * 512, cudaMemcpyDeviceToHost, s), "norm");
+        PALIAL_CK(cudaStreamSynchronize(s), "norm");
+        double t = 0;
+        for (double x : hp) t += x;
+        norms[j] = std::sqrt(t);
+    }
+    PALIAL_CK(cudaMemcpyAsync(part, norms.data(), sizeof(double) * 2 * nref, cudaMemcpyHostToDevice, s), "norms");
+    for (int j = 0; j < 2 * nref; j++)
+        PALIAL_CK(mps_scale_cols(vecs + (size_t)j * n, vecs + (size_t)j * n, n, 1, part + j, s), "normalize");
+    PALIAL_CK(mps_diag(dA, n, nb, kappa, s), "diag");
+    const double *U = vecs, *V = symmetric ? vecs : vecs + (size_t)n * nref;
+    // X = D V^T = D G_64 ... G_1 (right), then A = U X = H_1 ... H_64 X (left)
+    for (int j = nref - 1; j >= 0; j--) {
+        const double *g = V + (size_t)j * n;
+        PALIAL_CK(mps_matvec(dA, n, nb, g, y, 0, s), "X g");
+        PALIAL_CK(mps_rank1(dA, n, nb, y, g, s), "X -= 2 (Xg) g^T");
+    }
+    for (int j = nref - 1; j >= 0; j--) {
+        const double *h = U + (size_t)j * n;
+        PALIAL_CK(mps_matvec(dA, n, nb, h, y, 1, s), "X^T h");
+        PALIAL_CK(mps_rank1(dA, n, nb, h, y, s), "X -= 2 h (h^T X)");
+    }
+    if (symmetric) PALIAL_CK(mps_symmetrize(dA, n, nb, s), "symmetrize");
+    PALIAL_CK(cudaStreamSynchronize(s), "gen kappa");
+    return PALIAL_OK;
+}
 
 extern "C" int palial_gpu_mp_update_step(int alg, int precision, float *dW, int n, int nb, int k) {
     palial_status *st = nullptr;
@@ -206,8 +405,8 @@ extern "C" int palial_gpu_mp_factor(int alg, const double *dA, float *dW, int n,
     return set_status(st, zp ? PALIAL_WARN_ZERO_PIVOT : PALIAL_OK);
 }
 
-extern "C" int palial_gpu_solve_ir(int alg, const double *dA, int n, int nb, const double *dB, double *dX, int nrhs,
-                                   const palial_opts *opts, palial_status *st, void *stream) {
+static int solve_one(int alg, const double *dA, int n, int nb, const double *dB, double *dX, int nrhs,
+                     const palial_opts *opts, palial_status *st, void *stream) {
     palial_opts o;
     palial_opts_default(&o);
     if (opts) o = *opts;
@@ -259,6 +458,8 @@ extern "C" int palial_gpu_solve_ir(int alg, const double *dA, int n, int nb, con
         }
         if (rc) return set_status(st, rc, "mixed factorization failed (shift %.3e)", shift);
     }
+    rc = mp_prepare_solves(alg, W, n, nb, s, st);
+    if (rc) return rc;
     PALIAL_CK(cudaStreamSynchronize(s), "factorization");
     const double fsec = std::chrono::duration<double>(std::chrono::steady_clock::now() - f0).count();
     // ---- refinement -------------------------------------------------------------------------
@@ -271,28 +472,28 @@ extern "C" int palial_gpu_solve_ir(int alg, const double *dA, int n, int nb, con
     PALIAL_CK(cudaMemcpyAsync(mb.r.ptr, dB, sizeof(double) * (size_t)n * nrhs, cudaMemcpyDeviceToDevice, s), "r0");
     PALIAL_CK(cudaStreamSynchronize(s), "init");
     double eta = 1.0, eta_prev = 1e300;
-    int it = 0;
+    int it = 0, gmres_total = 0;
     bool converged = false;
+    bool use_gmres = (o.gmres == 1);
+    PALIAL_CK(mb.x32.ensure(sizeof(double) * (size_t)n * nrhs), "alloc d");
+    double *dcorr = mb.x32.as<double>();
     for (it = 1; it <= maxit; it++) {
-        // scale = max |r_j| (keeps the FP32 right-hand side well inside range)
-        PALIAL_CK(mps_colmax(mb.r.as<double>(), n, nrhs, nrm + 1, s), "scale");
-        PALIAL_CK(cudaMemcpyAsync(hscale.data(), nrm + 1, sizeof(double) * nrhs, cudaMemcpyDeviceToHost, s), "scale");
-        PALIAL_CK(cudaStreamSynchronize(s), "scale");
-        bool any = false;
-        for (int j = 0; j < nrhs; j++) {
-            if (hscale[j] == 0.0) hscale[j] = 1.0;
-            else any = true;
+        if (!use_gmres) {
+            // d = M^-1 r in FP32 (scaled per column), x += d
+            rc = precondition(alg, W, n, nb, mb.r.as<double>(), dcorr, nrhs, nrm + 1, hscale, s, st);
+            if (rc) return rc;
+        } else {
+            int inner = 0;
+            rc = gmres(alg, dA, W, n, nb, mb.r.as<double>(), dcorr, nrhs, 50, o.reserved[1] > 0 ? o.reserved[1] : 200,
+                       1e-4, s, st, &inner);
+            if (rc) return rc;
+            gmres_total += inner;
         }
-        if (!any) {
-            eta = 0.0;
-            converged = true;
-            break;
+        {
+            std::vector<double> ones(nrhs, -1.0);
+            PALIAL_CK(cudaMemcpyAsync(nrm + 80, ones.data(), sizeof(double) * nrhs, cudaMemcpyHostToDevice, s), "one");
+            PALIAL_CK(mps_multi_axpy(dcorr, 1, nrm + 80, dX, n, nrhs, 0, s), "x += d");
         }
-        PALIAL_CK(cudaMemcpyAsync(nrm + 1, hscale.data(), sizeof(double) * nrhs, cudaMemcpyHostToDevice, s), "scale");
-        PALIAL_CK(mps_to_f32_rhs(mb.r.as<double>(), mb.r32.as<float>(), n, nrhs, nrm + 1, s), "r to f32");
-        rc = mp_apply_inverse(alg, W, n, nb, mb.r32.as<float>(), s, st);
-        if (rc) return rc;
-        PALIAL_CK(mps_add_correction(dX, mb.r32.as<float>(), n, nrhs, nrm + 1, s), "x += d");
         PALIAL_CK(mps_residual(dA, n, nb, dX, dB, mb.r.as<double>(), nrhs, s), "residual");
         PALIAL_CK(mps_colmax(mb.r.as<double>(), n, nrhs, nrm + 17, s), "norm r");
         PALIAL_CK(mps_colmax(dX, n, nrhs, nrm + 33, s), "norm x");
@@ -306,8 +507,14 @@ extern "C" int palial_gpu_solve_ir(int alg, const double *dA, int n, int nb, con
             converged = true;
             break;
         }
-        if (it >= 3 && eta > 0.9 * eta_prev) break;  // stagnation: refinement cannot reach tol
-        eta_prev = eta;
+        if (!use_gmres && it >= 2 && eta > 0.5 * eta_prev && o.gmres >= 0) {
+            use_gmres = true;  // plain refinement contracts too slowly: switch to GMRES-IR
+        } else if (use_gmres && it >= 3 && eta > 0.9 * eta_prev) {
+            break;  // GMRES-IR stagnates as well
+        } else if (!use_gmres && o.gmres < 0 && it >= 3 && eta > 0.9 * eta_prev) {
+            break;
+        }
+        eta_prev = std::min(eta_prev, eta);
     }
     const double total = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
     if (st) {
@@ -319,11 +526,63 @@ extern "C" int palial_gpu_solve_ir(int alg, const double *dA, int n, int nb, con
         st->kappa_est = -1.0;
         st->factor_seconds = fsec;
         st->shift = shift;
-        st->gmres_iters = 0;
+        st->gmres_iters = gmres_total;
     }
     if (!converged)
         return set_status(st, PALIAL_ERR_NOT_CONVERGED, "refinement stopped at backward error %.3e after %d iterations",
                           eta, it);
     return set_status(st, zp ? PALIAL_WARN_ZERO_PIVOT : PALIAL_OK, "backward error %.3e in %d iterations (shift %.2e)",
                       eta, st ? st->ir_iters : it, shift);
+}
+
+// Precision ladder (PALIAL_PREC_AUTO): the cheapest update precision first; when refinement
+// misses the target, the factorization is redone one rung up (FP8 -> BF16 -> BF16x3 -> FP64).
+// The status reports the precision that converged (opts precision field of st->message) and
+// the total time of all attempts.
+extern "C" int palial_gpu_solve_ir(int alg, const double *dA, int n, int nb, const double *dB, double *dX, int nrhs,
+                                   const palial_opts *opts, palial_status *st, void *stream) {
+    palial_opts o;
+    palial_opts_default(&o);
+    if (opts) o = *opts;
+    if (o.precision != PALIAL_PREC_AUTO) return solve_one(alg, dA, n, nb, dB, dX, nrhs, &o, st, stream);
+    static const int ladder[] = {PALIAL_PREC_BF16, PALIAL_PREC_BF16X3, PALIAL_PREC_FP64};
+    const auto t0 = std::chrono::steady_clock::now();
+    int rc = PALIAL_ERR_NOT_CONVERGED;
+    int used = -1;
+    for (int prec : ladder) {
+        o.precision = prec;
+        rc = solve_one(alg, dA, n, nb, dB, dX, nrhs, &o, st, stream);
+        used = prec;
+        if (rc >= 0) break;
+        if (rc != PALIAL_ERR_NOT_CONVERGED && rc != PALIAL_ERR_NOT_SPD) break;
+    }
+    const double total = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    if (st) {
+        st->seconds = st->total_seconds = total;
+        st->tflops = algorithmic_flops(alg, n) / total * 1e-12;
+        st->kappa_est = (double)used;  // precision that produced the result (PALIAL_PREC_*)
+    }
+    return rc;
+}
+
+// Host-buffer variant (A: reference tile descriptor in host memory; B, X: n x nrhs host,
+// column-major): copies in, solves, copies X out.
+extern "C" int palial_gpu_solve_ir_host(int alg, const palial_desc *A, const double *B, double *X, int nrhs,
+                                        const palial_opts *opts, palial_status *st) {
+    if (st) memset(st, 0, sizeof *st);
+    if (!A || !A->matrix || !B || !X || nrhs < 1 || nrhs > 16) return set_status(st, PALIAL_ERR_ARG, "bad arguments");
+    const int n = A->matrix_size, nb = A->tile_size;
+    int rc = ensure_init(st);
+    if (rc) return rc;
+    const auto t0 = std::chrono::steady_clock::now();
+    const size_t bytes = sizeof(double) * (size_t)n * n, vb = sizeof(double) * (size_t)n * nrhs;
+    PALIAL_CK(g.smat.ensure(bytes), "alloc A");
+    PALIAL_CK(mb.work.ensure(std::max(mb.work.bytes, 2 * vb)), "alloc B/X");
+    double *dB = mb.work.as<double>(), *dX = dB + (size_t)n * nrhs;
+    PALIAL_CK(cudaMemcpy(g.smat.ptr, A->matrix, bytes, cudaMemcpyHostToDevice), "copy A");
+    PALIAL_CK(cudaMemcpy(dB, B, vb, cudaMemcpyHostToDevice), "copy B");
+    rc = palial_gpu_solve_ir(alg, g.smat.as<double>(), n, nb, dB, dX, nrhs, opts, st, nullptr);
+    PALIAL_CK(cudaMemcpy(X, dX, vb, cudaMemcpyDeviceToHost), "copy X");
+    if (st) st->total_seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    return rc;
 }

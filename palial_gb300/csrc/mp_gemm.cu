@@ -41,7 +41,9 @@ enum Mode { MODE_BF16 = 0, MODE_FP8 = 1, MODE_BF16X3 = 2 };
 template <int MODE>
 struct Cfg {
     static constexpr int NOPS = (MODE == MODE_BF16X3) ? 2 : 1;   // hi (+ lo) operand copies
-    static constexpr int STAGES = (MODE == MODE_BF16X3) ? 2 : 4;
+    // 2 stages: K = NB = 512 is only 8 (bf16) or 4 (fp8) stages, and 2 CTAs then share an SM
+    // (2 x 256 TMEM columns), so one CTA's epilogue overlaps the other's main loop.
+    static constexpr int STAGES = 2;
     static constexpr int A_BYTES = BM * KBYTES;                  // 16 KB
     static constexpr int B_BYTES = BN * KBYTES;                  // 32 KB
     static constexpr int STAGE_BYTES = NOPS * (A_BYTES + B_BYTES);
@@ -254,26 +256,41 @@ __global__ void __launch_bounds__(NTHR, 1)
         if (ok) mma_commit(done);
     }
     __syncwarp();
-    // ---- epilogue: all four warps ----
+    // ---- epilogue: all four warps; thread = accumulator row, 64 columns per pass ----
+    // The old C values of a pass are loaded as 64 independent loads before they are needed
+    // (the first pass before the MMA has finished), so each pass costs one memory round trip.
+    const int mt = p.n / p.nb;
+    const int tr = p.k + 1 + ti, tc = p.k + 1 + tj;
+    float *ct = p.C + (size_t)p.nb * p.nb * ((size_t)tr + (size_t)mt * tc) + (size_t)(mi * BM + warp * 32 + lane) +
+                (size_t)(nj * BN) * p.nb;
+    float cold[64];
+#pragma unroll
+    for (int c = 0; c < 64; c++) cold[c] = __ldcs(ct + (size_t)c * p.nb);
     bool have = false;
     if (!s_abort) have = mbar_wait(done, 0);
     if (!have) {
-        if (threadIdx.x == 0 || lane == 0) atomicCAS(p.status + ST_CODE, 0, -4);
+        if (lane == 0) atomicCAS(p.status + ST_CODE, 0, -4);
     } else {
         asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-        const int mt = p.n / p.nb;
-        const int tr = p.k + 1 + ti, tc = p.k + 1 + tj;
-        float *ct = p.C + (size_t)p.nb * p.nb * ((size_t)tr + (size_t)mt * tc) + (size_t)(mi * BM + warp * 32 + lane) +
-                    (size_t)(nj * BN) * p.nb;
         float sc = 1.0f;
         if (MODE == MODE_FP8 && p.scale_a) sc = p.scale_a[ti] * p.scale_b[tj];
-        for (int c0 = 0; c0 < BN; c0 += 16) {
-            float d[16];
-            tmem_ld16(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0, d);
+        const uint32_t trow = tmem + ((uint32_t)(warp * 32) << 16);
+        for (int c0 = 0; c0 < BN; c0 += 64) {
+            float d[64];
+            tmem_ld16(trow + (uint32_t)c0, d);
+            tmem_ld16(trow + (uint32_t)(c0 + 16), d + 16);
+            tmem_ld16(trow + (uint32_t)(c0 + 32), d + 32);
+            tmem_ld16(trow + (uint32_t)(c0 + 48), d + 48);
+            float nxt[64];
+            if (c0 + 64 < BN) {
 #pragma unroll
-            for (int c = 0; c < 16; c++) {
-                float *x = ct + (size_t)(c0 + c) * p.nb;
-                *x = fmaf(-sc, d[c], *x);
+                for (int c = 0; c < 64; c++) nxt[c] = __ldcs(ct + (size_t)(c0 + 64 + c) * p.nb);
+            }
+#pragma unroll
+            for (int c = 0; c < 64; c++) __stcs(ct + (size_t)(c0 + c) * p.nb, fmaf(-sc, d[c], cold[c]));
+            if (c0 + 64 < BN) {
+#pragma unroll
+                for (int c = 0; c < 64; c++) cold[c] = nxt[c];
             }
         }
     }
@@ -431,6 +448,7 @@ cudaError_t launch_mode(const void *a_hi, const void *a_lo, const void *b_hi, co
     const long long blocks = pairs * (p.nb / mp::BM) * (p.nb / mp::BN);
     if (blocks <= 0) return cudaSuccess;
     if (blocks > 0x7fffffffLL) return cudaErrorInvalidValue;
+    note_launch();
     mp::mp_update_kernel<MODE><<<(unsigned)blocks, mp::NTHR, C::SMEM, s>>>(ta, tb, tal, tbl, p);
     return cudaGetLastError();
 }
@@ -464,6 +482,7 @@ cudaError_t mp_pack_rows(int mode, const float *W, int n, int nb, int k, void *h
     const int ntr = n / nb - k - 1;
     if (ntr <= 0) return cudaSuccess;
     dim3 grid(mode == 1 ? 1 : 16, ntr);
+    note_launch();
     mp::pack_rows_kernel<<<grid, 1024, 0, s>>>(W, n, nb, k, mode, static_cast<__nv_bfloat16 *>(hi),
                                                 static_cast<__nv_bfloat16 *>(lo), static_cast<__nv_fp8_e4m3 *>(hi),
                                                 scales);
@@ -476,9 +495,11 @@ cudaError_t mp_pack_cols(int mode, const float *W, int n, int nb, int k, void *h
     const int ntr = n / nb - k - 1;
     if (ntr <= 0) return cudaSuccess;
     if (mode == 1) {
+        note_launch();
         mp::col_scales_kernel<<<ntr, 1024, 0, s>>>(W, n, nb, k, scales);
     }
     dim3 grid(nb / 32, nb / 32, ntr), block(32, 8);
+    note_launch();
     mp::pack_cols_kernel<<<grid, block, 0, s>>>(W, n, nb, k, mode, static_cast<__nv_bfloat16 *>(hi),
                                                  static_cast<__nv_bfloat16 *>(lo), static_cast<__nv_fp8_e4m3 *>(hi),
                                                  scales);

@@ -109,30 +109,59 @@ __global__ void __launch_bounds__(NT, 1) panel_trsm_kernel(float *W, int n, int 
     else strip_run(m, T, nb, W + tile_off(n, nb, t, k) + s * 64, nb, nb);
 }
 
-// ---- blocked triangular solves of the refinement right-hand sides (R: n x 64, ld n) ---------
-// diag step: one CTA solves tile row k of R with the diagonal tile; kind as below.
-//   0: U^T y = r (forward, Cholesky)   1: U z = y (backward)   2: L y = r (forward, unit)
-__global__ void __launch_bounds__(NT, 1) rhs_diag_kernel(const float *W, int n, int nb, int k, float *R, int kind) {
+// ---- diagonal-tile inverses for the refinement solves --------------------------------------
+// Dinv tile k (nb x nb, column-major) = T_kk^-1 with T the upper factor (kind 1) or the unit
+// lower factor (kind 2) of the diagonal tile; one CTA per 64-column strip of the identity.
+__global__ void __launch_bounds__(NT, 1) invert_diag_kernel(const float *W, int n, int nb, float *Dinv, int kind) {
     extern __shared__ __align__(16) float smem[];
     const Smem m = smem_parts(smem);
+    const int k = blockIdx.y, s = blockIdx.x;
+    float *X = Dinv + (size_t)k * nb * nb + (size_t)s * 64 * nb;   // strip of columns s*64..
+    for (int e = threadIdx.x; e < nb * 64; e += NT) {
+        const int r = e % nb, c = e / nb;
+        X[r + (size_t)c * nb] = (r == s * 64 + c) ? 1.f : 0.f;
+    }
+    __syncthreads();
     const float *T = W + tile_off(n, nb, k, k);
-    float *B = R + (size_t)k * nb;
-    if (kind == 0) strip_lut(m, T, nb, const_cast<float *>(B), n, nb);
-    else if (kind == 1) strip_un(m, T, nb, B, n, nb);
-    else strip_llu(m, T, nb, B, n, nb);
+    if (kind == 1) strip_un(m, T, nb, X, nb, nb);
+    else strip_llu(m, T, nb, X, nb, nb);
 }
 
-// update step: for every other tile row t (blockIdx.x) in the active range:
-//   kind 0: R_t -= U(k,t)^T R_k  (t > k)     kind 1: R_t -= U(t,k) R_k (t < k)
-//   kind 2: R_t -= L(t,k) R_k    (t > k)
-__global__ void __launch_bounds__(NT, 1) rhs_update_kernel(const float *W, int n, int nb, int k, float *R, int kind) {
+// S = op(Dinv_k) R_k for one 64-row block per CTA (op = transpose when trans), then the
+// solution tile row is written back over R_k by the update kernel.
+__global__ void __launch_bounds__(NT, 1) rhs_apply_kernel(const float *Dinv, int n, int nb, int k, const float *R,
+                                                           float *S, int trans) {
     extern __shared__ __align__(16) float smem[];
     const Smem m = smem_parts(smem);
-    const int t = (kind == 1) ? (int)blockIdx.x : k + 1 + (int)blockIdx.x;
+    const int rb = blockIdx.x * 64;
+    const float *D = Dinv + (size_t)k * nb * nb;
     const float *Rk = R + (size_t)k * nb;
-    float *Rt = R + (size_t)t * nb;
-    if (kind == 0) cta_gemm<true, false>(nb, 64, nb, -1.f, W + tile_off(n, nb, k, t), nb, Rk, n, Rt, n, m.g);
-    else cta_gemm<false, false>(nb, 64, nb, -1.f, W + tile_off(n, nb, t, k), nb, Rk, n, Rt, n, m.g);
+    float *out = S + rb;
+    for (int e = threadIdx.x; e < 64 * 64; e += NT) out[(e & 63) + (size_t)(e >> 6) * nb] = 0.f;
+    __syncthreads();
+    if (trans) cta_gemm<true, false>(64, 64, nb, 1.f, D + (size_t)rb * nb, nb, Rk, n, out, nb, m.g);
+    else cta_gemm<false, false>(64, 64, nb, 1.f, D + rb, nb, Rk, n, out, nb, m.g);
+}
+
+// R_t -= op(W tile) S for one 64-row block of tile row t per CTA (blockIdx.y = row block);
+// blockIdx.x == count writes S back into R_k instead.
+//   kind 0: R_t -= U(k,t)^T S (t > k);  kind 1: R_t -= U(t,k) S (t < k);  kind 2: R_t -= L(t,k) S
+__global__ void __launch_bounds__(NT, 1) rhs_update2_kernel(const float *W, int n, int nb, int k, float *R,
+                                                             const float *S, int kind, int count) {
+    extern __shared__ __align__(16) float smem[];
+    const Smem m = smem_parts(smem);
+    const int rb = blockIdx.y * 64;
+    if ((int)blockIdx.x == count) {
+        float *Rk = R + (size_t)k * nb + rb;
+        for (int e = threadIdx.x; e < 64 * 64; e += NT) Rk[(e & 63) + (size_t)(e >> 6) * n] = S[rb + (e & 63) + (size_t)(e >> 6) * nb];
+        return;
+    }
+    const int t = (kind == 1) ? (int)blockIdx.x : k + 1 + (int)blockIdx.x;
+    float *Rt = R + (size_t)t * nb + rb;
+    if (kind == 0)
+        cta_gemm<true, false>(64, 64, nb, -1.f, W + tile_off(n, nb, k, t) + (size_t)rb * nb, nb, S, nb, Rt, n, m.g);
+    else
+        cta_gemm<false, false>(64, 64, nb, -1.f, W + tile_off(n, nb, t, k) + rb, nb, S, nb, Rt, n, m.g);
 }
 
 // ---- FP64 residual R = B - A X (A: FP64 tile layout; X, B, R: n x nrhs, ld n; nrhs <= 16) ---
@@ -166,7 +195,7 @@ __global__ void __launch_bounds__(256) residual_kernel(const double *A, int n, i
         const int c = grp * 4 + j;
         if (c < nrhs) {
             const size_t o = (size_t)(i0 + row) + (size_t)c * n;
-            R[o] = B[o] - acc[j];
+            R[o] = B ? B[o] - acc[j] : acc[j];
         }
     }
 }
@@ -219,6 +248,106 @@ __global__ void add_correction_kernel(double *X, const float *D32, long long n, 
         X[e] += scale[e / n] * (double)D32[e];
 }
 
+// ---- GMRES building blocks (n x nrhs column-major blocks, one Krylov space per column) ----
+// H[l*nrhs + c] += <V_l[:,c], w[:,c]> for l < count (V_l at V + l*n*nrhs)
+__global__ void multi_dot_kernel(const double *V, int count, const double *w, long long n, int nrhs, double *H) {
+    const int l = blockIdx.y;
+    const double *v = V + (size_t)l * n * nrhs;
+    double acc[16];
+#pragma unroll
+    for (int c = 0; c < 16; c++) acc[c] = 0.0;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+        for (int c = 0; c < nrhs; c++) acc[c] = fma(v[(size_t)c * n + i], w[(size_t)c * n + i], acc[c]);
+    for (int c = 0; c < nrhs; c++) {
+        double x = acc[c];
+        for (int o = 16; o; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
+        if ((threadIdx.x & 31) == 0) atomicAdd(H + (size_t)l * nrhs + c, x);
+    }
+}
+// w[:,c] -= sum_l H[l*nrhs + c] V_l[:,c]   (or w = sum_l H V_l when assign)
+__global__ void multi_axpy_kernel(const double *V, int count, const double *H, double *w, long long n, int nrhs,
+                                  int assign) {
+    const long long total = n * nrhs;
+    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < total; e += (long long)gridDim.x * blockDim.x) {
+        const int c = (int)(e / n);
+        double s = 0.0;
+        for (int l = 0; l < count; l++) s = fma(H[(size_t)l * nrhs + c], V[(size_t)l * n * nrhs + e], s);
+        w[e] = assign ? s : w[e] - s;
+    }
+}
+// out = w / f[c] (f > 0) or copy with scaling; X = scale_c * D32 (assign)
+__global__ void scale_cols_kernel(const double *w, double *out, long long n, int nrhs, const double *f) {
+    const long long total = n * nrhs;
+    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < total; e += (long long)gridDim.x * blockDim.x)
+        out[e] = w[e] / f[e / n];
+}
+__global__ void from_f32_rhs_kernel(double *X, const float *D32, long long n, int cols, const double *scale) {
+    const long long total = n * cols;
+    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < total; e += (long long)gridDim.x * blockDim.x)
+        X[e] = scale[e / n] * (double)D32[e];
+}
+
+// ---- Householder reflector application on a tile-layout FP64 matrix -----------------------
+// X(i,j) -= 2 * a_i * b_j  (rank-1 update)
+__global__ void rank1_kernel(double *X, int n, int nb, const double *a, const double *b) {
+    const long long total = (long long)n * n;
+    const int mt = n / nb;
+    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < total; e += (long long)gridDim.x * blockDim.x) {
+        const long long t = e / ((long long)nb * nb);
+        const int in = (int)(e - t * (long long)nb * nb);
+        const long long i = (t % mt) * nb + in % nb, j = (t / mt) * nb + in / nb;
+        X[e] -= 2.0 * a[i] * b[j];
+    }
+}
+// diagonal tile matrix with s_i = kappa^(-i/(n-1))
+__global__ void diag_kernel(double *X, int n, int nb, double kappa) {
+    const long long total = (long long)n * n;
+    const int mt = n / nb;
+    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < total; e += (long long)gridDim.x * blockDim.x) {
+        const long long t = e / ((long long)nb * nb);
+        const int in = (int)(e - t * (long long)nb * nb);
+        const long long i = (t % mt) * nb + in % nb, j = (t / mt) * nb + in / nb;
+        X[e] = (i == j) ? pow(kappa, -(double)i / (double)(n > 1 ? n - 1 : 1)) : 0.0;
+    }
+}
+// y = A^T x for one vector (tile layout): one warp per output, lanes walk a tile column
+// (contiguous).  y = A x: one thread per output row, a warp reads 32 consecutive rows of a
+// column (contiguous) per step.
+__global__ void matvec_t_kernel(const double *A, int n, int nb, const double *x, double *y) {
+    const int mt = n / nb;
+    const long long col = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (col >= n) return;
+    double s = 0.0;
+    for (int j = lane; j < n; j += 32)
+        s = fma(A[(size_t)nb * nb * ((size_t)(j / nb) + (size_t)mt * (col / nb)) + (size_t)(j % nb) + (size_t)(col % nb) * nb],
+                x[j], s);
+    for (int o = 16; o; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    if (lane == 0) y[col] = s;
+}
+__global__ void matvec_n_kernel(const double *A, int n, int nb, const double *x, double *y) {
+    const int mt = n / nb;
+    const long long row = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (row >= n) return;
+    const double *base = A + (size_t)nb * nb * (size_t)(row / nb) + (size_t)(row % nb);
+    double s = 0.0;
+    for (int j = 0; j < n; j++) s = fma(base[(size_t)nb * nb * (size_t)mt * (j / nb) + (size_t)(j % nb) * nb], x[j], s);
+    y[row] = s;
+}
+
+// lower triangle := upper triangle (exact symmetry of a generated SPD matrix)
+__global__ void symmetrize_kernel(double *X, int n, int nb) {
+    const long long total = (long long)n * n;
+    const int mt = n / nb;
+    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < total; e += (long long)gridDim.x * blockDim.x) {
+        const long long t = e / ((long long)nb * nb);
+        const int in = (int)(e - t * (long long)nb * nb);
+        const long long i = (t % mt) * nb + in % nb, j = (t / mt) * nb + in / nb;
+        if (i > j)
+            X[e] = X[(size_t)nb * nb * ((size_t)(j / nb) + (size_t)mt * (i / nb)) + (size_t)(j % nb) + (size_t)(i % nb) * nb];
+    }
+}
+
 // record the step of a diagonal-tile factorization until the first error
 __global__ void mark_step_kernel(int *st, int k) {
     if (st[ST_CODE] == 0) st[6] = k;
@@ -232,49 +361,65 @@ __global__ void mark_step_kernel(int *st, int k) {
 cudaError_t mps_configure() {
     cudaError_t e = cudaFuncSetAttribute(mps::panel_trsm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, mps::SMEM_BYTES);
     if (e != cudaSuccess) return e;
-    e = cudaFuncSetAttribute(mps::rhs_diag_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, mps::SMEM_BYTES);
+    e = cudaFuncSetAttribute(mps::invert_diag_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, mps::SMEM_BYTES);
     if (e != cudaSuccess) return e;
-    return cudaFuncSetAttribute(mps::rhs_update_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, mps::SMEM_BYTES);
+    e = cudaFuncSetAttribute(mps::rhs_apply_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, mps::SMEM_BYTES);
+    if (e != cudaSuccess) return e;
+    e = cudaFuncSetAttribute(mps::rhs_update2_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, mps::SMEM_BYTES);
+    return e;
 }
 
 cudaError_t mps_f64_to_f32(const double *A, float *W, int n, int nb, double shift, cudaStream_t s) {
+    note_launch();
     mps::f64_to_f32_kernel<<<4096, 256, 0, s>>>(A, W, (long long)n * n, shift, n, nb);
     return cudaGetLastError();
 }
 cudaError_t mps_tile_to_f64(const float *w, double *d, int nb, cudaStream_t s) {
+    note_launch();
     mps::tile_f32_to_f64_kernel<<<256, 256, 0, s>>>(w, d, nb * nb);
     return cudaGetLastError();
 }
 cudaError_t mps_tile_to_f32(const double *d, float *w, int nb, int upper_only, cudaStream_t s) {
+    note_launch();
     mps::tile_f64_to_f32_kernel<<<256, 256, 0, s>>>(d, w, nb, upper_only);
+    return cudaGetLastError();
+}
+cudaError_t mps_invert_diag(const float *W, int n, int nb, float *Dinv, int kind, cudaStream_t s) {
+    dim3 grid(nb / 64, n / nb);
+    note_launch();
+    mps::invert_diag_kernel<<<grid, mps::NT, mps::SMEM_BYTES, s>>>(W, n, nb, Dinv, kind);
+    return cudaGetLastError();
+}
+cudaError_t mps_rhs_step(const float *W, const float *Dinv, int n, int nb, int k, float *R, float *S, int kind,
+                         cudaStream_t s) {
+    // kind 0: Cholesky forward (U^T), 1: backward (U), 2: LU forward (unit L)
+    const int mt = n / nb;
+    note_launch();
+    mps::rhs_apply_kernel<<<nb / 64, mps::NT, mps::SMEM_BYTES, s>>>(Dinv, n, nb, k, R, S, kind == 0 ? 1 : 0);
+    const int cnt = (kind == 1) ? k : mt - k - 1;
+    dim3 grid(cnt + 1, nb / 64);
+    note_launch();
+    mps::rhs_update2_kernel<<<grid, mps::NT, mps::SMEM_BYTES, s>>>(W, n, nb, k, R, S, kind, cnt);
     return cudaGetLastError();
 }
 cudaError_t mps_panel_trsm(float *W, int n, int nb, int k, int kind, cudaStream_t s) {
     const int ntr = n / nb - k - 1;
     if (ntr <= 0) return cudaSuccess;
     dim3 grid(nb / 64, ntr);
+    note_launch();
     mps::panel_trsm_kernel<<<grid, mps::NT, mps::SMEM_BYTES, s>>>(W, n, nb, k, kind);
-    return cudaGetLastError();
-}
-cudaError_t mps_rhs_diag(const float *W, int n, int nb, int k, float *R, int kind, cudaStream_t s) {
-    mps::rhs_diag_kernel<<<1, mps::NT, mps::SMEM_BYTES, s>>>(W, n, nb, k, R, kind);
-    return cudaGetLastError();
-}
-cudaError_t mps_rhs_update(const float *W, int n, int nb, int k, float *R, int kind, cudaStream_t s) {
-    const int mt = n / nb;
-    const int cnt = (kind == 1) ? k : mt - k - 1;
-    if (cnt <= 0) return cudaSuccess;
-    mps::rhs_update_kernel<<<cnt, mps::NT, mps::SMEM_BYTES, s>>>(W, n, nb, k, R, kind);
     return cudaGetLastError();
 }
 cudaError_t mps_residual(const double *A, int n, int nb, const double *X, const double *B, double *R, int nrhs,
                          cudaStream_t s) {
+    note_launch();
     mps::residual_kernel<<<n / 64, 256, 0, s>>>(A, n, nb, X, B, R, nrhs);
     return cudaGetLastError();
 }
 cudaError_t mps_norm_inf_matrix(const double *A, int n, int nb, double *out, cudaStream_t s) {
     cudaError_t e = cudaMemsetAsync(out, 0, sizeof(double), s);
     if (e != cudaSuccess) return e;
+    note_launch();
     mps::rowsum_kernel<<<n / 64, 256, 0, s>>>(A, n, nb, out);
     return cudaGetLastError();
 }
@@ -282,19 +427,76 @@ cudaError_t mps_colmax(const double *X, long long n, int cols, double *out, cuda
     cudaError_t e = cudaMemsetAsync(out, 0, sizeof(double) * cols, s);
     if (e != cudaSuccess) return e;
     dim3 grid(64, cols);
+    note_launch();
     mps::colmax_kernel<<<grid, 256, 0, s>>>(X, n, cols, out);
     return cudaGetLastError();
 }
 cudaError_t mps_to_f32_rhs(const double *R, float *R32, long long n, int cols, const double *scale, cudaStream_t s) {
+    note_launch();
     mps::to_f32_rhs_kernel<<<2048, 256, 0, s>>>(R, R32, n, cols, scale);
     return cudaGetLastError();
 }
 cudaError_t mps_mark_step(int *status, int k, cudaStream_t s) {
+    note_launch();
     mps::mark_step_kernel<<<1, 1, 0, s>>>(status, k);
     return cudaGetLastError();
 }
+cudaError_t mps_multi_dot(const double *V, int count, const double *w, long long n, int nrhs, double *H,
+                          cudaStream_t s) {
+    cudaError_t e = cudaMemsetAsync(H, 0, sizeof(double) * count * nrhs, s);
+    if (e != cudaSuccess || count <= 0) return e;
+    dim3 grid(128, count);
+    note_launch();
+    mps::multi_dot_kernel<<<grid, 256, 0, s>>>(V, count, w, n, nrhs, H);
+    return cudaGetLastError();
+}
+cudaError_t mps_multi_axpy(const double *V, int count, const double *H, double *w, long long n, int nrhs, int assign,
+                           cudaStream_t s) {
+    note_launch();
+    mps::multi_axpy_kernel<<<2048, 256, 0, s>>>(V, count, H, w, n, nrhs, assign);
+    return cudaGetLastError();
+}
+cudaError_t mps_scale_cols(const double *w, double *out, long long n, int nrhs, const double *f, cudaStream_t s) {
+    note_launch();
+    mps::scale_cols_kernel<<<2048, 256, 0, s>>>(w, out, n, nrhs, f);
+    return cudaGetLastError();
+}
+cudaError_t mps_from_f32_rhs(double *X, const float *D32, long long n, int cols, const double *scale, cudaStream_t s) {
+    note_launch();
+    mps::from_f32_rhs_kernel<<<2048, 256, 0, s>>>(X, D32, n, cols, scale);
+    return cudaGetLastError();
+}
+cudaError_t mps_rank1(double *X, int n, int nb, const double *a, const double *b, cudaStream_t s) {
+    note_launch();
+    mps::rank1_kernel<<<4096, 256, 0, s>>>(X, n, nb, a, b);
+    return cudaGetLastError();
+}
+cudaError_t mps_diag(double *X, int n, int nb, double kappa, cudaStream_t s) {
+    note_launch();
+    mps::diag_kernel<<<4096, 256, 0, s>>>(X, n, nb, kappa);
+    return cudaGetLastError();
+}
+cudaError_t mps_matvec(const double *A, int n, int nb, const double *x, double *y, int trans, cudaStream_t s) {
+    if (trans) {
+        const long long threads = (long long)n * 32;
+        note_launch();
+        mps::matvec_t_kernel<<<(unsigned)((threads + 255) / 256), 256, 0, s>>>(A, n, nb, x, y);
+    } else {
+        note_launch();
+        mps::matvec_n_kernel<<<(n + 127) / 128, 128, 0, s>>>(A, n, nb, x, y);
+    }
+    return cudaGetLastError();
+}
+
+cudaError_t mps_symmetrize(double *X, int n, int nb, cudaStream_t s) {
+    note_launch();
+    mps::symmetrize_kernel<<<4096, 256, 0, s>>>(X, n, nb);
+    return cudaGetLastError();
+}
+
 cudaError_t mps_add_correction(double *X, const float *D32, long long n, int cols, const double *scale,
                                cudaStream_t s) {
+    note_launch();
     mps::add_correction_kernel<<<2048, 256, 0, s>>>(X, D32, n, cols, scale);
     return cudaGetLastError();
 }

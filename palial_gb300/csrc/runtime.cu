@@ -43,6 +43,8 @@ cudaError_t launch_sub(const double *X, const double *Y, double *Z, long long le
 cudaError_t mps_configure();
 
 State g;
+static long long g_launches = 0;
+void note_launch() { g_launches++; }
 
 int set_status(palial_status *st, int code, const char *fmt, ...) {
     if (st) {
@@ -197,6 +199,8 @@ int palial_gpu_finalize(void) {
 }
 
 int palial_gpu_sm_count(void) { return g.init ? g.sms : 0; }
+
+long long palial_gpu_kernel_launches(void) { return palial::g_launches; }
 
 int palial_gpu_factor_dev(int alg, double *dA, double *dS, int n, int nb, const palial_opts *opts,
                           palial_status *st, void *stream) {

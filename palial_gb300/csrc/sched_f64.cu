@@ -640,6 +640,7 @@ cudaError_t sched_configure() {
 
 cudaError_t tile_task_launch(int type, int nb, int ld, double *p0, double *p1, double *p2, double *p3, double *scratch,
                              int *status, cudaStream_t s) {
+    note_launch();
     tile_task_kernel<<<1, NT, SCHED_SMEM_BYTES, s>>>(type, nb, ld, p0, p1, p2, p3, scratch, status);
     return cudaGetLastError();
 }
@@ -651,6 +652,7 @@ int sched_occupancy() {
 }
 
 cudaError_t sched_launch(const SchedParams &p, int grid, cudaStream_t s) {
+    note_launch();
     sched_f64_kernel<<<grid, NT, SCHED_SMEM_BYTES, s>>>(p);
     return cudaGetLastError();
 }

@@ -96,3 +96,33 @@ def test_solve_ir_reaches_fp64_backward_error(alg, prec):
     assert st.code in (0, 1), st.message
     assert eta <= 1e-14 * n and st.backward_error <= 1e-14 * n
     assert fwd <= 1e-10
+
+
+@pytest.mark.parametrize("kappa", [1e2, 1e6, 1e10])
+@pytest.mark.parametrize("alg", ["cholesky", "lu"])
+def test_kappa_sweep_small(alg, kappa):
+    """A = U diag(s) V^T with kappa(A) = kappa (64 Householder reflectors each side).  BF16
+    updates + IR, switching to GMRES-IR when plain refinement stagnates.  kappa <= 1e6 must
+    reach the FP64-level target; kappa = 1e10 is reported (pass or 'did not converge')."""
+    n, nb, nrhs = 2048, 512, 16
+    da = torch.empty(n * n, dtype=torch.float64, device="cuda")
+    P.gen_kappa(da.data_ptr(), n, nb, kappa, alg == "cholesky", seed=7)
+    torch.cuda.synchronize()
+    a = O.from_tiles(da.cpu().numpy(), n, nb)
+    s = np.linalg.svd(a, compute_uv=False)
+    assert abs(s[0] / s[-1] / kappa - 1) < 1e-3 * max(1.0, kappa / 1e6)
+    if alg == "cholesky":
+        assert np.array_equal(a, a.T)
+    b = O.gen_uniform(5, n, nrhs, stream=O.STREAM_RHS)
+    db = torch.from_numpy(np.asfortranarray(b).ravel(order="F")).cuda()
+    dx = torch.zeros_like(db)
+    st = P.solve_ir(alg, da.data_ptr(), n, nb, db.data_ptr(), dx.data_ptr(), nrhs, precision="auto",
+                    ir_max_iter=30, raise_on_error=False)
+    x = dx.cpu().numpy().reshape(nrhs, n).T
+    xref = np.linalg.solve(a, b)
+    fwd = np.max(np.abs(x - xref).max(0) / np.abs(xref).max(0))
+    print(f"{alg} kappa={kappa:.0e} code={st.code} prec={P.PREC_NAME.get(int(st.kappa_est))} iters={st.ir_iters} "
+          f"gmres={st.gmres_iters} eta={st.backward_error:.3e} fwd={fwd:.3e} shift={st.shift:.2e} t={st.seconds:.3f}s")
+    if kappa <= 1e6:
+        assert st.code in (0, 1), st.message
+        assert st.backward_error <= 1e-14 * n
