@@ -218,8 +218,42 @@ def time_update_kernel(P, torch, n: int) -> dict:
     return {"seconds": t, "flop": flop, "bytes": byts}
 
 
+def run_batched(args, P, torch) -> None:
+    """configs[3]: 2000 matrices, N log-uniform in [32, 2048) (seed 2), half SPD Cholesky, half
+    uniform LU, FP64, one persistent launch replayed from a CUDA graph; block size per size
+    class chosen by the autotuner."""
+    import numpy as np
+    from palial_gb300 import batched as B
+    ns, algs = B.batch_sizes(args.batch, 2)
+    t0 = time.perf_counter()
+    choice, timings = B.autotune(torch, ns, algs)
+    tune_s = time.perf_counter() - t0
+    b = B.Batch(torch, ns, algs, choice, seed=2)
+    b.run(graph=True)
+    times = []
+    for _ in range(max(3, args.steps)):
+        b.reset()
+        st, comp = b.run(graph=True, completion=True)
+        times.append(st.seconds)
+    t = float(np.median(times))
+    per_class = {}
+    for c in sorted(set(B.size_class(int(n)) for n in ns)):
+        sel = np.array([B.size_class(int(n)) == c for n in ns])
+        per_class[B.class_label(c)] = {"count": int(sel.sum()), "block": int(choice[c]),
+                                       "p50_ms": float(np.percentile(comp[sel], 50) * 1e3),
+                                       "p99_ms": float(np.percentile(comp[sel], 99) * 1e3)}
+    print(json.dumps({"suite": "batched", "matrices": int(len(ns)), "precision": "fp64",
+                      "matrices_per_s": len(ns) / t, "batch_seconds": t, "tflops": b.flops / t * 1e-12,
+                      "launches_per_batch": 1, "cuda_graph": True, "autotune_seconds": tune_s,
+                      "autotune": {f"{B.class_label(c)} bs={bs}": v for (c, bs), v in timings.items()},
+                      "per_size_class": per_class}), flush=True)
+
+
 def run_suite(args, P, torch) -> None:
     import numpy as np
+    if args.suite == "batched":
+        run_batched(args, P, torch)
+        return
     if args.suite == "fp64":
         for alg in ("cholesky", "lu", "qr"):
             for n in (16384, 32768):
@@ -270,7 +304,8 @@ def main() -> None:
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--n", type=int, default=N)
     ap.add_argument("--precision", default="bf16")
-    ap.add_argument("--suite", default=None, choices=[None, "fp64", "kappa"])
+    ap.add_argument("--suite", default=None, choices=[None, "fp64", "kappa", "batched"])
+    ap.add_argument("--batch", type=int, default=2000)
     ap.add_argument("--no-fp64", action="store_true")
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)

@@ -184,6 +184,22 @@ int palial_gpu_tile_dtsmqr_noalloc(int nb, double *dA1, double *dA2, const doubl
  * (LU), 2 = left lower no-trans unit (LU).  kind for dgemm: 0 = C -= A^T B (Cholesky),
  * 1 = C -= A B (LU). */
 
+/* ---- batched factorizations (no reference counterpart: north-star) ------------------------
+ * Factor `count` independent matrices (alg 0 Cholesky / 1 LU per matrix) in ONE persistent
+ * launch: the DAGs of all matrices are merged into one dispatch list ordered by critical path.
+ * Matrix i: device tile-layout buffer dA[i] of size ns[i] (multiple of nbs[i]), scheduled in
+ * blocks of bss[i] (multiple of 64, divides nbs[i]).  Matrices whose true size is not a multiple
+ * of 64 are embedded with identity (LU) or n*I (Cholesky) padding, which keeps the leading
+ * factor exact (palial_gpu_gen_batch_matrix makes such inputs).  completion_s (optional, count
+ * doubles) receives each matrix's completion time from the start of the launch (device trace).
+ * opts->reserved[2] = 1 replays the launch from a CUDA graph (captured on first use for the
+ * same DAG and matrix table). */
+int palial_gpu_batched(int count, const int *algs, const int *ns, const int *nbs, const int *bss,
+                       double *const *dA, const palial_opts *opts, palial_status *st,
+                       double *completion_s, void *stream);
+int palial_gpu_gen_batch_matrix(double *dA, int kind, int n_true, int n_pad, int nb, uint64_t seed,
+                                void *stream);
+
 /* ---- generators (counter-based; the same bytes as the CPU oracle's generators) ------------ */
 /* uniform [-1,1): entry (i,j) from splitmix64 of seed/stream and i + j*rows.  Tile layout. */
 int palial_gpu_gen_uniform(double *dA, int n, int nb, uint64_t seed, void *stream);
@@ -241,6 +257,10 @@ long long palial_dag_info(int alg, int n, int nb, int block, int priority, int n
  * dispatch with `nworkers` workers and random durations (seed).  Returns 0 if valid. */
 int palial_dag_validate(int alg, int n, int nb, int block, int priority, int nworkers,
                         unsigned int seed, char *msg, int msglen);
+
+/* Same validation for a merged batch DAG (and that no record crosses matrices). */
+int palial_dag_batch_validate(int count, const int *algs, const int *ns, const int *nbs, const int *bss,
+                              int nworkers, unsigned int seed, char *msg, int msglen);
 
 #ifdef __cplusplus
 }

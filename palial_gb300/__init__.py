@@ -104,6 +104,14 @@ def lib() -> ctypes.CDLL:
         h.palial_gpu_mp_factor.argtypes = [i, vp, vp, i, i, ctypes.POINTER(Opts), ctypes.POINTER(Status), vp]
         h.palial_gpu_mp_update_step.argtypes = [i, i, vp, i, i, i]
         h.palial_gpu_gen_kappa.argtypes = [vp, i, i, d, i, ctypes.c_uint64, vp]
+        h.palial_gpu_batched.argtypes = [i, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int),
+                                         ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int),
+                                         ctypes.POINTER(ctypes.c_void_p), ctypes.POINTER(Opts), ctypes.POINTER(Status),
+                                         ctypes.POINTER(ctypes.c_double), vp]
+        h.palial_gpu_gen_batch_matrix.argtypes = [vp, i, i, i, i, ctypes.c_uint64, vp]
+        h.palial_dag_batch_validate.argtypes = [i, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int),
+                                                ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int), i,
+                                                ctypes.c_uint, ctypes.c_char_p, i]
         h.palial_gpu_solve_ir_host.argtypes = [i, ctypes.POINTER(Desc), vp, vp, i, ctypes.POINTER(Opts),
                                                ctypes.POINTER(Status)]
         _lib = h

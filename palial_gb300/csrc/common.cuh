@@ -43,8 +43,15 @@ struct alignas(16) Task {
     uint32_t wait_obj[3];
     uint32_t wait_cnt[3];
     uint32_t sig_obj[2];
+    uint32_t mat;      // matrix of a batched run (index into SchedParams::mats)
 };
 static_assert(sizeof(Task) == 48, "Task record layout");
+
+// One matrix of a batched run: its own tile-layout buffer, sizes and counter range.
+struct MatInfo {
+    double *A;
+    int n, nb, bs;
+};
 
 struct TraceRec {
     unsigned long long t0, t1;  // %globaltimer ns
@@ -70,6 +77,7 @@ struct SchedParams {
     long long scratch_per_worker;  // doubles
     int n, nb, bs;              // matrix size, tile size, block size
     unsigned long long timeout_ns;
+    const MatInfo *mats;        // batched run: per-matrix buffers and sizes (else nullptr)
 };
 
 // Host: count of kernel launches made by the library (every launch wrapper calls this).

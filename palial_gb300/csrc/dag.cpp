@@ -141,6 +141,26 @@ Dag build_dag(int alg, int n, int nb, int bs, const double *costs) {
     return d;
 }
 
+Dag build_batch_dag(const std::vector<BatchSpec> &specs, const double *costs) {
+    Dag all;
+    all.alg = -1;
+    all.nobj = 0;
+    for (size_t i = 0; i < specs.size(); i++) {
+        const BatchSpec &b = specs[i];
+        Dag d = build_dag(b.alg, b.n, b.nb, b.bs, costs);
+        const uint32_t base = (uint32_t)all.nobj;
+        for (LogicalTask t : d.logical) {
+            t.mat = (uint32_t)i;
+            for (int w = 0; w < t.nwait; w++) t.wait_obj[w] += base;
+            for (int s2 = 0; s2 < t.nsig; s2++) t.sig_obj[s2] += base;
+            all.logical.push_back(t);
+        }
+        all.nobj += d.nobj;
+        all.critical_path = std::max(all.critical_path, d.critical_path);
+    }
+    return all;
+}
+
 namespace {
 Task make_record(const LogicalTask &t, int part) {
     Task r{};
@@ -158,6 +178,7 @@ Task make_record(const LogicalTask &t, int part) {
     }
     r.sig_obj[0] = t.sig_obj[0];
     r.sig_obj[1] = t.sig_obj[1];
+    r.mat = t.mat;
     return r;
 }
 
@@ -286,11 +307,23 @@ void order_dag(Dag &d, int priority, int nworkers, unsigned shuffle_seed) {
     std::mt19937_64 rng(shuffle_seed);
     std::uniform_real_distribution<double> jitter(0.5, 1.5);
     std::vector<double> pr(part_logical.size()), du(part_logical.size());
+    // Batches: shortest matrix first (total work of its tasks), critical path within a matrix.
+    // The makespan is set by the total work and the largest matrices' critical paths, so the
+    // small matrices can finish early at almost no cost.
+    std::vector<double> mat_work;
+    const bool batch = (d.alg < 0);
+    if (batch) {
+        for (const auto &t : d.logical) {
+            if (t.mat >= mat_work.size()) mat_work.resize(t.mat + 1, 0.0);
+            mat_work[t.mat] += t.cost * t.nparts;
+        }
+    }
     for (size_t p = 0; p < part_logical.size(); p++) {
         const LogicalTask &t = d.logical[part_logical[p]];
         const double j = shuffle_seed ? jitter(rng) : 1.0;
         du[p] = t.cost * j;
         pr[p] = (priority == 1) ? -(double)p : t.bl * (shuffle_seed ? jitter(rng) : 1.0);
+        if (batch && priority != 1) pr[p] -= 1e6 * mat_work[t.mat];
     }
     Sim s = simulate(d, part_logical, std::max(1, nworkers), [&](uint32_t p) { return du[p]; },
                      [&](uint32_t p) { return pr[p]; });

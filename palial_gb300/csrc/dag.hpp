@@ -14,6 +14,7 @@
 namespace palial {
 
 struct LogicalTask {
+    uint32_t mat;      // matrix index (batched DAGs)
     uint8_t type;
     uint8_t nparts;
     uint16_t k, m, n;
@@ -41,6 +42,13 @@ double task_cost(int type, int bs, int nb, int part, const double *costs);
 
 // Build the program-order DAG.  bs = block size (divides nb) for Cholesky/LU; QR uses nb.
 Dag build_dag(int alg, int n, int nb, int bs, const double *costs = nullptr);
+
+// One matrix of a batch: algorithm (0 Cholesky, 1 LU), padded size, tile size, block size.
+struct BatchSpec {
+    int alg, n, nb, bs;
+};
+// Merge the DAGs of independent matrices (object ranges offset per matrix) into one.
+Dag build_batch_dag(const std::vector<BatchSpec> &specs, const double *costs = nullptr);
 
 // Dispatch order.  priority 0: critical-path list scheduling simulated with `nworkers`
 // workers; 1: program order; 2: same as 0 with the caller's costs.  shuffle_seed != 0

@@ -84,7 +84,7 @@ __global__ void gen_k8_kernel(int8_t *K, int n, uint64_t key) {
 
 // A(i,j) = (K K^T)(i,j) * 2^-14 + n*[i==j], 128x128 output tile per CTA (256 threads, 8x8
 // each), K chunk of 64 bytes staged in shared memory as packed int32 words.
-__global__ void __launch_bounds__(256) spd_from_k8_kernel(const int8_t *K, double *A, int n, int nb) {
+__global__ void __launch_bounds__(256) spd_from_k8_kernel(const int8_t *K, double *A, int n, int nb, double diag) {
     __shared__ int As[16][128 + 4];
     __shared__ int Bs[16][128 + 4];
     const int i0 = blockIdx.y * 128, j0 = blockIdx.x * 128;
@@ -126,11 +126,34 @@ __global__ void __launch_bounds__(256) spd_from_k8_kernel(const int8_t *K, doubl
             const int i = i0 + ty + 16 * a, j = j0 + tx + 16 * b;
             if (i >= n || j >= n) continue;
             double v = (double)acc[a][b] * 0x1.0p-14;
-            if (i == j) v += (double)n;
+            if (i == j) v += diag;
             const size_t off = (size_t)nb * nb * ((size_t)(i / nb) + (size_t)mt * (j / nb)) + (size_t)(i % nb) +
                                (size_t)(j % nb) * nb;
             A[off] = v;
         }
+}
+
+// One matrix of a batch, n_true x n_true embedded in an n_pad x n_pad tile-layout buffer:
+//   kind 0 (LU): uniform [-1, 1) from index i + j*n_true, identity padding;
+//   kind 1 (Cholesky): A = K K^T / 2^14 + n_true I, K int8 (index i + p*n_true), computed
+//   exactly per element, padding n_true * I (block diagonal: the leading factor is exact).
+__global__ void gen_batch_uniform_kernel(double *A, int nt, int np, int nb, uint64_t key) {
+    const long long total = (long long)np * np;
+    const int mt = np / nb;
+    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < total; e += (long long)gridDim.x * blockDim.x) {
+        const long long t = e / ((long long)nb * nb);
+        const int in = (int)(e - t * (long long)nb * nb);
+        const long long i = (t % mt) * nb + in % nb, j = (t / mt) * nb + in / nb;
+        A[e] = (i < nt && j < nt) ? uniform_pm1(mix64(key + (uint64_t)(i + j * nt))) : (i == j ? 1.0 : 0.0);
+    }
+}
+// K of a batched SPD matrix: np x np row-major int8, zero outside the leading nt x nt block
+__global__ void gen_batch_k8_kernel(int8_t *K, int nt, int np, uint64_t key) {
+    const long long total = (long long)np * np;
+    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < total; e += (long long)gridDim.x * blockDim.x) {
+        const long long i = e / np, p = e - i * np;
+        K[e] = (i < nt && p < nt) ? (int8_t)((int)(mix64(key + (uint64_t)(i + p * nt)) >> 56) - 128) : (int8_t)0;
+    }
 }
 
 // ---------------------------------------------------------------------------------------
@@ -234,7 +257,22 @@ cudaError_t launch_gen_spd(double *A, int n, int nb, uint64_t seed, int8_t *kbuf
     gen_k8_kernel<<<4096, 256, 0, s>>>(kbuf, n, stream_key(seed, STREAM_SPD));
     dim3 grid((n + 127) / 128, (n + 127) / 128);  // n % 64 == 0 (checked by the caller)
     note_launch();
-    spd_from_k8_kernel<<<grid, 256, 0, s>>>(kbuf, A, n, nb);
+    spd_from_k8_kernel<<<grid, 256, 0, s>>>(kbuf, A, n, nb, (double)n);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_gen_batch(double *A, int kind, int nt, int np, int nb, uint64_t seed, int8_t *kbuf,
+                             cudaStream_t s) {
+    if (kind == 0) {
+        note_launch();
+        gen_batch_uniform_kernel<<<1024, 256, 0, s>>>(A, nt, np, nb, stream_key(seed, STREAM_UNIFORM));
+        return cudaGetLastError();
+    }
+    note_launch();
+    gen_batch_k8_kernel<<<1024, 256, 0, s>>>(kbuf, nt, np, stream_key(seed, STREAM_SPD));
+    dim3 grid((np + 127) / 128, (np + 127) / 128);
+    note_launch();
+    spd_from_k8_kernel<<<grid, 256, 0, s>>>(kbuf, A, np, nb, (double)nt);
     return cudaGetLastError();
 }
 

@@ -4,6 +4,7 @@
 
 #include <cstdarg>
 #include <map>
+#include <string>
 #include <memory>
 #include <tuple>
 #include <vector>
@@ -61,7 +62,13 @@ struct State {
     int device = -1;
     int sms = 0;
     int occupancy = 1;
-    SchedCtx main, diag;
+    SchedCtx main, diag, batch;
+    DevBuf batch_mats;
+    std::map<std::string, std::shared_ptr<Dag>> batch_dags;
+    cudaGraphExec_t batch_graph = nullptr;
+    unsigned long long batch_graph_uid = 0;
+    const void *batch_graph_mats = nullptr;
+    const void *batch_graph_trace = nullptr;
     DevBuf mat, smat, kbuf, probe;
     std::map<std::tuple<int, int, int, int, int, int, unsigned>, std::shared_ptr<Dag>> dags;
     unsigned long long next_uid = 1;

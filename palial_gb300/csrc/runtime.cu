@@ -36,6 +36,8 @@ cudaError_t launch_gen_uniform(double *A, int n, int nb, uint64_t seed, cudaStre
 cudaError_t launch_gen_refpattern(double *A, int n, int nb, uint64_t seed, cudaStream_t s);
 cudaError_t launch_gen_dense(double *X, long long rows, int cols, uint64_t seed, int stream, cudaStream_t s);
 cudaError_t launch_gen_spd(double *A, int n, int nb, uint64_t seed, int8_t *kbuf, cudaStream_t s);
+cudaError_t launch_gen_batch(double *A, int kind, int nt, int np, int nb, uint64_t seed, int8_t *kbuf,
+                             cudaStream_t s);
 cudaError_t launch_tiled_mm(const double *A, const double *X, double *Y, int n, int nb, int r, int mode, int trans,
                             cudaStream_t s);
 cudaError_t launch_sumsq(const double *X, long long len, double *partial, int blocks, cudaStream_t s);
@@ -193,6 +195,11 @@ int palial_gpu_finalize(void) {
     if (!g.init) return PALIAL_OK;
     g.main.release();
     g.diag.release();
+    g.batch.release();
+    g.batch_mats.release();
+    g.batch_dags.clear();
+    if (g.batch_graph) cudaGraphExecDestroy(g.batch_graph);
+    g.batch_graph = nullptr;
     for (DevBuf *b : {&g.mat, &g.smat, &g.kbuf, &g.probe}) b->release();
     g.dags.clear();
     return PALIAL_OK;
@@ -495,6 +502,124 @@ int palial_gpu_residual_host(int alg, const double *a0_host, const palial_desc *
     return rc;
 }
 
+// ---- batched factorizations ---------------------------------------------------------------
+int palial_gpu_gen_batch_matrix(double *dA, int kind, int n_true, int n_pad, int nb, uint64_t seed, void *stream) {
+    palial_status *st = nullptr;
+    int rc = ensure_init(nullptr);
+    if (rc) return rc;
+    if (!dA || n_true <= 0 || n_pad < n_true || nb <= 0 || n_pad % nb || n_pad % 64 || (kind != 0 && kind != 1))
+        return PALIAL_ERR_ARG;
+    CK(g.kbuf.ensure((size_t)n_pad * n_pad), "alloc K");
+    CK(launch_gen_batch(dA, kind, n_true, n_pad, nb, seed, g.kbuf.as<int8_t>(), static_cast<cudaStream_t>(stream)),
+       "gen batch");
+    return PALIAL_OK;
+}
+
+int palial_gpu_batched(int count, const int *algs, const int *ns, const int *nbs, const int *bss, double *const *dA,
+                       const palial_opts *opts, palial_status *st, double *completion_s, void *stream) {
+    palial_opts o;
+    palial_opts_default(&o);
+    if (opts) o = *opts;
+    if (st) memset(st, 0, sizeof *st);
+    if (count <= 0 || !algs || !ns || !nbs || !bss || !dA) return set_status(st, PALIAL_ERR_ARG, "empty batch");
+    int rc = ensure_init(st);
+    if (rc) return rc;
+    std::vector<BatchSpec> specs(count);
+    std::string key = std::to_string(o.priority) + ":";
+    double flops = 0;
+    for (int i = 0; i < count; i++) {
+        const int a = algs[i], n = ns[i], nb = nbs[i], bs = bss[i];
+        if ((a != 0 && a != 1) || n <= 0 || nb <= 0 || n % nb || nb % bs || bs % 64 || !dA[i])
+            return set_status(st, PALIAL_ERR_ARG, "matrix %d: alg %d n %d nb %d bs %d", i, a, n, nb, bs);
+        specs[i] = BatchSpec{a, n, nb, bs};
+        key += std::to_string(a) + "," + std::to_string(n) + "," + std::to_string(nb) + "," + std::to_string(bs) + ";";
+        flops += algorithmic_flops(a, n);
+    }
+    std::shared_ptr<Dag> dag;
+    auto it = g.batch_dags.find(key);
+    if (it != g.batch_dags.end()) {
+        dag = it->second;
+    } else {
+        try {
+            dag = std::make_shared<Dag>(build_batch_dag(specs));
+            order_dag(*dag, o.priority, g.sms, 0);
+        } catch (const std::exception &ex) {
+            return set_status(st, PALIAL_ERR_ARG, "%s", ex.what());
+        }
+        dag->uid = g.next_uid++;
+        if (g.batch_dags.size() > 8) g.batch_dags.clear();
+        g.batch_dags[key] = dag;
+    }
+    std::vector<MatInfo> mats(count);
+    for (int i = 0; i < count; i++) mats[i] = MatInfo{dA[i], ns[i], nbs[i], bss[i]};
+    CK(g.batch_mats.ensure(sizeof(MatInfo) * count), "alloc matrix table");
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    CK(cudaMemcpyAsync(g.batch_mats.ptr, mats.data(), sizeof(MatInfo) * count, cudaMemcpyHostToDevice, s), "upload");
+    const bool want_trace = o.trace || completion_s;
+    SchedParams p;
+    rc = sched_prepare(g.batch, dag, nullptr, nullptr, g.sms, want_trace, o.timeout_s, p, st);
+    if (rc) return rc;
+    p.mats = g.batch_mats.as<MatInfo>();
+    const bool use_graph = o.reserved[2] == 1;
+    CK(cudaEventRecord(g.ev0, s), "event");
+    if (use_graph) {
+        // one CUDA graph per (DAG, matrix table): counter/ticket/status clears + the launch
+        const void *gkey = want_trace ? (const void *)g.batch.trace.ptr : nullptr;
+        if (!g.batch_graph || g.batch_graph_uid != dag->uid || g.batch_graph_mats != g.batch_mats.ptr ||
+            g.batch_graph_trace != gkey) {
+            if (g.batch_graph) cudaGraphExecDestroy(g.batch_graph);
+            g.batch_graph = nullptr;
+            cudaStream_t cs;
+            CK(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking), "stream");
+            cudaGraph_t graph;
+            CK(cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal), "capture");
+            cudaError_t e = sched_enqueue(g.batch, p, dag->nobj, g.sms, true, cs);
+            cudaError_t e2 = cudaStreamEndCapture(cs, &graph);
+            cudaStreamDestroy(cs);
+            CK(e, "capture enqueue");
+            CK(e2, "end capture");
+            CK(cudaGraphInstantiate(&g.batch_graph, graph, 0), "instantiate");
+            cudaGraphDestroy(graph);
+            g.batch_graph_uid = dag->uid;
+            g.batch_graph_mats = g.batch_mats.ptr;
+            g.batch_graph_trace = gkey;
+        }
+        CK(cudaGraphLaunch(g.batch_graph, s), "graph launch");
+        note_launch();
+    } else {
+        CK(sched_enqueue(g.batch, p, dag->nobj, g.sms, true, s), "launch");
+    }
+    CK(cudaEventRecord(g.ev1, s), "event");
+    CK(cudaEventSynchronize(g.ev1), "batched run");
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, g.ev0, g.ev1);
+    int hs[ST_NSLOTS];
+    CK(cudaMemcpy(hs, g.batch.status.ptr, sizeof hs, cudaMemcpyDeviceToHost), "status");
+    if (st) {
+        st->seconds = ms * 1e-3;
+        st->tflops = flops / std::max(1e-12, st->seconds) * 1e-12;
+        st->ntasks = (long long)dag->records.size();
+    }
+    if (want_trace && hs[ST_CODE] == 0) {
+        std::vector<TraceRec> recs(dag->records.size());
+        CK(cudaMemcpy(recs.data(), g.batch.trace.ptr, sizeof(TraceRec) * recs.size(), cudaMemcpyDeviceToHost), "trace");
+        unsigned long long t0 = ~0ull;
+        for (const auto &r : recs) t0 = std::min(t0, r.t0);
+        if (completion_s) {
+            for (int i = 0; i < count; i++) completion_s[i] = 0;
+            for (size_t r = 0; r < recs.size(); r++) {
+                const uint32_t m = dag->records[r].mat;
+                completion_s[m] = std::max(completion_s[m], (double)(recs[r].t1 - t0) * 1e-9);
+            }
+        }
+    }
+    if (hs[ST_CODE] == PALIAL_ERR_NOT_SPD)
+        return set_status(st, PALIAL_ERR_NOT_SPD, "non-positive pivot in a batched Cholesky");
+    if (hs[ST_CODE] != 0) return set_status(st, hs[ST_CODE], "device error %d", hs[ST_CODE]);
+    if (hs[ST_ZEROPIV]) return set_status(st, PALIAL_WARN_ZERO_PIVOT, "exact zero pivot skipped");
+    return set_status(st, PALIAL_OK);
+}
+
 // ---- trace ----------------------------------------------------------------------------------
 long long palial_gpu_trace_count(void) {
     return g.last_trace.valid ? (long long)g.last_trace.dag.logical.size() : 0;
@@ -560,6 +685,38 @@ int palial_dag_validate(int alg, int n, int nb, int block, int priority, int nwo
         Dag d = build_dag(alg, n, nb, bs);
         order_dag(d, priority, nworkers, seed);
         const std::string r = validate_dag(d, nworkers, seed);
+        if (msg && msglen > 0) snprintf(msg, msglen, "%s", r.c_str());
+        return r.empty() ? 0 : 1;
+    } catch (const std::exception &ex) {
+        if (msg && msglen > 0) snprintf(msg, msglen, "%s", ex.what());
+        return -1;
+    }
+}
+
+int palial_dag_batch_validate(int count, const int *algs, const int *ns, const int *nbs, const int *bss, int nworkers,
+                              unsigned int seed, char *msg, int msglen) {
+    try {
+        std::vector<BatchSpec> specs(count);
+        for (int i = 0; i < count; i++) specs[i] = BatchSpec{algs[i], ns[i], nbs[i], bss[i]};
+        Dag d = build_batch_dag(specs);
+        order_dag(d, 0, nworkers, seed);
+        std::string r = validate_dag(d, nworkers, seed);
+        // every record of matrix i touches only matrix i's objects
+        std::vector<uint32_t> lo(count, ~0u), hi(count, 0);
+        uint32_t base = 0;
+        for (int i = 0; i < count; i++) {
+            const int mb = ns[i] / bss[i];
+            lo[i] = base;
+            hi[i] = base + (uint32_t)(mb * mb);
+            base = hi[i];
+        }
+        for (size_t q = 0; q < d.records.size() && r.empty(); q++) {
+            const Task &t = d.records[q];
+            for (int w = 0; w < t.nwait; w++)
+                if (t.wait_obj[w] < lo[t.mat] || t.wait_obj[w] >= hi[t.mat]) r = "record waits on another matrix";
+            for (int s2 = 0; s2 < t.nsig; s2++)
+                if (t.sig_obj[s2] < lo[t.mat] || t.sig_obj[s2] >= hi[t.mat]) r = "record signals another matrix";
+        }
         if (msg && msglen > 0) snprintf(msg, msglen, "%s", r.c_str());
         return r.empty() ? 0 : 1;
     } catch (const std::exception &ex) {

@@ -412,8 +412,16 @@ __device__ void record_error(const SchedParams &p, int code, int task, int m, in
 }
 
 __device__ void run_task(const SchedParams &p, const Worker &w, const Task &t, int tid, double *wscr) {
-    const int n = p.n, nb = p.nb, bs = p.bs, ld = nb;
+    int n = p.n, nb = p.nb, bs = p.bs;
     double *A = p.A;
+    if (p.mats) {
+        const MatInfo mi = p.mats[t.mat];
+        A = mi.A;
+        n = mi.n;
+        nb = mi.nb;
+        bs = mi.bs;
+    }
+    const int ld = nb;
     switch (t.type) {
         case T_POTRF: {
             double *D = block_ptr(A, n, nb, bs, t.k, t.k);

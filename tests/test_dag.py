@@ -1,6 +1,8 @@
 """Host logic of the device scheduler: task counts, dependence validity, emulation with
 random durations, and the C ABI exports.  No GPU needed (no compute calls)."""
 import re
+
+import numpy as np
 import os
 
 import pytest
@@ -63,3 +65,27 @@ def test_critical_path_order_beats_program_order_in_model():
 def test_bad_sizes_rejected():
     with pytest.raises(P.PalialError):
         P.dag_info("cholesky", 1000, 512)
+
+
+def test_batch_sizes_log_uniform_and_split():
+    from palial_gb300 import batched as B
+    ns, algs = B.batch_sizes(2000, 2)
+    assert ns.min() >= 32 and ns.max() < 2048
+    # log-uniform: about 1/6 of the mass in each octave pair of [32, 2048)
+    counts = np.bincount([B.size_class(int(n)) for n in ns], minlength=6)
+    assert all(abs(c / 2000 - 1 / 6) < 0.05 for c in counts)
+    assert (algs == np.arange(2000) % 2).all()
+    ns2, _ = B.batch_sizes(2000, 2)
+    assert (ns == ns2).all()
+
+
+def test_batch_dag_validates_and_isolates_matrices():
+    import ctypes
+    from palial_gb300 import batched as B
+    ns, algs = B.batch_sizes(60, 3)
+    bs = [64 if n < 256 else 128 for n in ns]
+    npad = [B.padded(int(n), b) for n, b in zip(ns, bs)]
+    arr = lambda x: (ctypes.c_int * len(x))(*[int(v) for v in x])  # noqa: E731
+    buf = ctypes.create_string_buffer(256)
+    rc = P.lib().palial_dag_batch_validate(60, arr(algs), arr(npad), arr(bs), arr(bs), 152, 5, buf, 256)
+    assert rc == 0, buf.value
