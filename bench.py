@@ -249,8 +249,78 @@ def run_batched(args, P, torch) -> None:
                       "per_size_class": per_class}), flush=True)
 
 
+def run_costmodel(args, P, torch) -> None:
+    """configs[4]: train the task-cost MLP on device traces of FP64 Cholesky / LU / QR sweeps,
+    report its prediction error on held-out runs, then factor N=49152 FP64 Cholesky with (a)
+    the learned block size + learned critical-path priorities and (b) the fallback (exhaustive
+    autotuner on a proxy size + static flop-model priorities), and report both makespans."""
+    import numpy as np
+    from palial_gb300.costmodel import CostModel, exhaustive_block, trace_records
+    # N must be a multiple of NB (reference palial_src/main.c:101-105): 12288 takes all five
+    # NB values of the sweep, 8192 and 16384 the powers of two.
+    sweep = []
+    for alg in ("cholesky", "lu", "qr"):
+        for n in (8192, 12288, 16384):
+            for nb in (256, 384, 512, 768, 1024):
+                if n % nb or (alg == "qr" and n > 12288):
+                    continue
+                bs = nb if alg == "qr" else 0
+                sweep.append((alg, n, nb, bs))
+    xs, ys, tags = [], [], []
+    t0 = time.perf_counter()
+    for alg, n, nb, bs in sweep:
+        x, y = trace_records(torch, alg, n, nb, bs)
+        xs.append(x)
+        ys.append(y)
+        tags.append(np.full(len(y), len(tags)))
+    trace_s = time.perf_counter() - t0
+    X, Y, T = np.concatenate(xs), np.concatenate(ys), np.concatenate(tags)
+    rng = np.random.default_rng(0)
+    held = set(rng.choice(len(sweep), 3, replace=False).tolist())   # whole runs held out
+    test = np.isin(T, list(held))
+    train_idx = np.flatnonzero(~test)
+    if len(train_idx) > 200000:
+        train_idx = rng.choice(train_idx, 200000, replace=False)
+    m = CostModel(seed=0)
+    t1 = time.perf_counter()
+    loss = m.train(X[train_idx], Y[train_idx], epochs=30, batch=1024, lr=2e-3)
+    train_s = time.perf_counter() - t1
+    pred = m.predict(X[test])
+    rel = np.abs(np.exp(pred - Y[test]) - 1.0)
+    nbig, nb, cands = 49152, 512, (128, 256, 512)
+    workers = P.lib().palial_gpu_sm_count()
+    learned_bs, predicted = m.choose_block(0, nbig, nb, cands, workers)
+    fb_bs, fb_times = exhaustive_block(torch, "cholesky", 16384, nb, cands)
+    a0 = torch.empty(nbig * nbig, dtype=torch.float64, device="cuda")
+    P.gen_spd(a0.data_ptr(), nbig, nb, 0)
+    a = torch.empty_like(a0)
+    m.register(0, nbig, nb, learned_bs, workers)
+    a.copy_(a0)
+    st_l = P.factor_dev("cholesky", a.data_ptr(), None, nbig, nb, block=learned_bs, priority=2)
+    res_l = P.residual_probe("cholesky", a0.data_ptr(), a.data_ptr(), nbig, nb, 4)
+    learned_bits = a.clone() if learned_bs == fb_bs else None
+    a.copy_(a0)
+    st_f = P.factor_dev("cholesky", a.data_ptr(), None, nbig, nb, block=fb_bs, priority=0)
+    res_f = P.residual_probe("cholesky", a0.data_ptr(), a.data_ptr(), nbig, nb, 4)
+    same_bits = bool(torch.equal(learned_bits, a)) if learned_bits is not None else None
+    print(json.dumps({"suite": "costmodel", "records_total": int(len(Y)), "records_train": int(len(train_idx)),
+                      "records_heldout": int(test.sum()), "trace_seconds": trace_s, "train_seconds": train_s,
+                      "train_loss_log_us": loss, "heldout_median_rel_error": float(np.median(rel)),
+                      "heldout_p90_rel_error": float(np.percentile(rel, 90)),
+                      "n": nbig, "nb": nb, "candidates": list(cands),
+                      "learned": {"block": learned_bs, "predicted_makespan_s": predicted,
+                                  "measured_makespan_s": st_l.seconds, "residual_probe": res_l},
+                      "fallback": {"block": fb_bs, "proxy_times_s_n16384": fb_times,
+                                   "measured_makespan_s": st_f.seconds, "residual_probe": res_f},
+                      "gain_fallback_over_learned": st_f.seconds / st_l.seconds,
+                      "factors_bitwise_identical_across_schedules": same_bits}), flush=True)
+
+
 def run_suite(args, P, torch) -> None:
     import numpy as np
+    if args.suite == "costmodel":
+        run_costmodel(args, P, torch)
+        return
     if args.suite == "batched":
         run_batched(args, P, torch)
         return
@@ -304,7 +374,7 @@ def main() -> None:
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--n", type=int, default=N)
     ap.add_argument("--precision", default="bf16")
-    ap.add_argument("--suite", default=None, choices=[None, "fp64", "kappa", "batched"])
+    ap.add_argument("--suite", default=None, choices=[None, "fp64", "kappa", "batched", "costmodel"])
     ap.add_argument("--batch", type=int, default=2000)
     ap.add_argument("--no-fp64", action="store_true")
     args = ap.parse_args()

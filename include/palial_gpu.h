@@ -258,6 +258,28 @@ long long palial_dag_info(int alg, int n, int nb, int block, int priority, int n
 int palial_dag_validate(int alg, int n, int nb, int block, int priority, int nworkers,
                         unsigned int seed, char *msg, int msglen);
 
+/* ---- learned task-cost model (no reference counterpart: north-star) ------------------------
+ * An MLP (nin -> hidden -> hidden -> 1, ReLU, FP32) trained on the device by this library's
+ * own forward / backward / Adam kernels.  Inputs are task features (palial_dag_features_count()
+ * floats per task); the target is log(task time in microseconds). */
+int palial_mlp_init(int nin, int hidden, uint64_t seed);
+long long palial_mlp_param_count(void);
+int palial_mlp_get_params(float *out);
+int palial_mlp_set_params(const float *in);
+int palial_mlp_grad(const float *X, const float *y, int n, float *grads_out, float *loss_out);
+int palial_mlp_train(const float *X, const float *y, int n, int epochs, int batch, float lr, uint64_t seed,
+                     float *final_loss);
+int palial_mlp_predict(const float *X, int n, float *out);
+int palial_dag_features_count(void);
+/* Training data from the last traced factorization: features and log(us) per task record. */
+long long palial_gpu_trace_features(float *X, float *y, long long cap);
+/* Planning: features of every logical task of the DAG (alg, n, nb, block). */
+long long palial_dag_logical_features(int alg, int n, int nb, int block, int nworkers, float *X, long long cap);
+/* Register per-logical-task costs (seconds) for a DAG shape; opts.priority = 2 (and
+ * palial_dag_info with priority 2) then orders by the critical path of these costs.
+ * cost_s = NULL removes them. */
+int palial_gpu_set_task_costs(int alg, int n, int nb, int block, const double *cost_s, long long count);
+
 /* Same validation for a merged batch DAG (and that no record crosses matrices). */
 int palial_dag_batch_validate(int count, const int *algs, const int *ns, const int *nbs, const int *bss,
                               int nworkers, unsigned int seed, char *msg, int msglen);

@@ -127,8 +127,14 @@ Dag build_dag(int alg, int n, int nb, int bs, const double *costs) {
             }
         }
     }
-    // bottom levels: reverse program order; M[x] = max bl of later tasks waiting on x
+    recompute_bottom_levels(d);
+    return d;
+}
+
+void recompute_bottom_levels(Dag &d) {
+    // reverse program order; M[x] = max bl of later tasks waiting on / updating x
     std::vector<double> M(d.nobj, 0.0);
+    d.critical_path = 0.0;
     for (size_t i = d.logical.size(); i-- > 0;) {
         LogicalTask &t = d.logical[i];
         double succ = 0.0;
@@ -138,7 +144,35 @@ Dag build_dag(int alg, int n, int nb, int bs, const double *costs) {
         for (int s = 0; s < t.nsig; s++) M[t.sig_obj[s]] = std::max(M[t.sig_obj[s]], t.bl);
     }
     for (const auto &t : d.logical) d.critical_path = std::max(d.critical_path, t.bl);
-    return d;
+}
+
+double nominal_task_flops(int type, int bs, int nb, int part) { return nominal_flops(type, bs, nb, part); }
+
+std::vector<int> step_widths(const Dag &d) {
+    std::vector<int> w;
+    for (const auto &t : d.logical) {
+        if (t.k >= w.size()) w.resize(t.k + 1, 0);
+        w[t.k] += t.nparts;
+    }
+    return w;
+}
+
+void task_features(const Dag &d, const LogicalTask &t, int part, int nworkers, int precision,
+                   const std::vector<int> &step_width, float *f) {
+    for (int i = 0; i < kFeatures; i++) f[i] = 0.f;
+    f[t.type < 12 ? t.type : 11] = 1.f;
+    const int bs = d.bs > 0 ? d.bs : 64, nb = d.nb > 0 ? d.nb : bs;
+    const double mb = std::max(1, d.n / bs);
+    f[12] = (float)(std::log2((double)bs) / 10.0);
+    f[13] = (float)(std::log2((double)nb) / 10.0);
+    f[14] = (float)(t.k / mb);
+    f[15] = (float)((mb - t.k) / mb);
+    f[16] = (float)((double)part / std::max(1, (int)t.nparts));
+    const int w = t.k < step_width.size() ? step_width[t.k] : 1;
+    f[17] = (float)(std::log2((double)std::max(1, w)) / 20.0);
+    f[18] = (float)(std::log2(std::max(1.0, nominal_flops(t.type, bs, nb, part))) / 40.0);
+    f[19] = (float)(std::log2((double)std::max(1, nworkers)) / 10.0);
+    f[20] = (float)(precision / 3.0);
 }
 
 Dag build_batch_dag(const std::vector<BatchSpec> &specs, const double *costs) {

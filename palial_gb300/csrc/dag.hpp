@@ -65,4 +65,16 @@ std::vector<std::string> reference_names(const Dag &d);
 
 double algorithmic_flops(int alg, double n);
 
+// Bottom levels (critical path to the end) from the current per-task costs.
+void recompute_bottom_levels(Dag &d);
+
+// Features of the cost model for one task part (kFeatures floats): task type one-hot, block
+// and tile size, k-step progress, part position, parallel width of the step, nominal flops,
+// workers, precision.  The same function serves training (trace records) and planning.
+constexpr int kFeatures = 21;
+void task_features(const Dag &d, const LogicalTask &t, int part, int nworkers, int precision,
+                   const std::vector<int> &step_width, float *f);
+std::vector<int> step_widths(const Dag &d);
+double nominal_task_flops(int type, int bs, int nb, int part);
+
 }  // namespace palial

@@ -73,6 +73,9 @@ struct State {
     std::map<std::tuple<int, int, int, int, int, int, unsigned>, std::shared_ptr<Dag>> dags;
     unsigned long long next_uid = 1;
     TraceState last_trace;
+    int last_trace_workers = 0;
+    // learned per-task costs (seconds, per logical task) keyed by "alg,n,nb,bs"
+    std::map<std::string, std::vector<double>> task_costs;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
 };
 extern State g;

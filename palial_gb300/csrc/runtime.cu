@@ -85,12 +85,26 @@ int auto_block(int alg, int n, int nb) {
     return std::max(64, bs);
 }
 
+static std::string cost_key(int alg, int n, int nb, int bs) {
+    return std::to_string(alg) + "," + std::to_string(n) + "," + std::to_string(nb) + "," + std::to_string(bs);
+}
+
+// priority 2: critical-path order from the learned per-task costs registered with
+// palial_gpu_set_task_costs (falls back to the flop model when none are registered).
+static void apply_learned_costs(Dag &d) {
+    auto it = g.task_costs.find(cost_key(d.alg, d.n, d.nb, d.bs));
+    if (it == g.task_costs.end() || it->second.size() != d.logical.size()) return;
+    for (size_t i = 0; i < d.logical.size(); i++) d.logical[i].cost = it->second[i];
+    recompute_bottom_levels(d);
+}
+
 std::shared_ptr<Dag> get_dag(int alg, int n, int nb, int bs, int priority, int workers, unsigned seed) {
     auto key = std::make_tuple(alg, n, nb, bs, priority, workers, seed);
     auto it = g.dags.find(key);
     if (it != g.dags.end()) return it->second;
     auto d = std::make_shared<Dag>(build_dag(alg, n, nb, bs));
-    order_dag(*d, priority, workers, seed);
+    if (priority == 2) apply_learned_costs(*d);
+    order_dag(*d, priority == 2 ? 0 : priority, workers, seed);
     d->uid = g.next_uid++;
     if (g.dags.size() > 16) g.dags.clear();
     g.dags[key] = d;
@@ -285,6 +299,7 @@ int palial_gpu_factor_dev(int alg, double *dA, double *dS, int n, int nb, const 
     }
     if (o.trace && hs[ST_CODE] == 0) {
         g.last_trace.dag = *dag;
+        g.last_trace_workers = workers;
         g.last_trace.recs.resize(ntasks);
         CK(cudaMemcpy(g.last_trace.recs.data(), g.main.trace.ptr, sizeof(TraceRec) * ntasks, cudaMemcpyDeviceToHost),
            "read trace");
@@ -660,12 +675,63 @@ int palial_gpu_trace_dump(const char *path, const char *csv_path) {
 }
 
 // ---- DAG (host only) ------------------------------------------------------------------------
+// ---- learned cost model plumbing ----------------------------------------------------------
+// Features and log-durations (log of microseconds) of every task record of the last traced
+// factorization; returns the number of records (or the count needed when cap is too small).
+long long palial_gpu_trace_features(float *X, float *y, long long cap) {
+    if (!g.last_trace.valid) return -1;
+    const Dag &d = g.last_trace.dag;
+    const long long nrec = (long long)d.records.size();
+    if (!X || !y || cap < nrec) return nrec;
+    const auto widths = step_widths(d);
+    for (long long r = 0; r < nrec; r++) {
+        const LogicalTask &t = d.logical[d.rec_logical[r]];
+        task_features(d, t, d.records[r].part, g.last_trace_workers, 0, widths, X + r * kFeatures);
+        const double us = std::max(1.0, (double)(g.last_trace.recs[r].t1 - g.last_trace.recs[r].t0) * 1e-3);
+        y[r] = (float)std::log(us);
+    }
+    return nrec;
+}
+
+// Features of every logical task (part 0) of a DAG, for planning with the model.
+long long palial_dag_logical_features(int alg, int n, int nb, int block, int nworkers, float *X, long long cap) {
+    try {
+        const int bs = block > 0 ? block : auto_block(alg, n, nb);
+        Dag d = build_dag(alg, n, nb, bs);
+        const long long nl = (long long)d.logical.size();
+        if (!X || cap < nl) return nl;
+        const auto widths = step_widths(d);
+        for (long long i = 0; i < nl; i++) task_features(d, d.logical[i], 0, nworkers, 0, widths, X + i * kFeatures);
+        return nl;
+    } catch (const std::exception &) {
+        return -1;
+    }
+}
+
+int palial_gpu_set_task_costs(int alg, int n, int nb, int block, const double *cost_s, long long count) {
+    const int bs = block > 0 ? block : auto_block(alg, n, nb);
+    if (!cost_s || count <= 0) {
+        g.task_costs.erase(cost_key(alg, n, nb, bs));
+    } else {
+        g.task_costs[cost_key(alg, n, nb, bs)] = std::vector<double>(cost_s, cost_s + count);
+    }
+    // invalidate cached learned-priority DAGs of this shape
+    for (auto it = g.dags.begin(); it != g.dags.end();) {
+        if (std::get<4>(it->first) == 2) it = g.dags.erase(it);
+        else ++it;
+    }
+    return PALIAL_OK;
+}
+
+int palial_dag_features_count(void) { return kFeatures; }
+
 long long palial_dag_info(int alg, int n, int nb, int block, int priority, int nworkers, long long *type_counts,
                           double *critical_path_s, double *makespan_s) {
     try {
         const int bs = block > 0 ? block : auto_block(alg, n, nb);
         Dag d = build_dag(alg, n, nb, bs);
-        order_dag(d, priority, nworkers, 0);
+        if (priority == 2) apply_learned_costs(d);
+        order_dag(d, priority == 2 ? 0 : priority, nworkers, 0);
         if (type_counts) {
             for (int i = 0; i < 16; i++) type_counts[i] = 0;
             for (const auto &t : d.logical) type_counts[t.type]++;
