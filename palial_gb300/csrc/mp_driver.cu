@@ -183,8 +183,10 @@ int precondition(int alg, const float *W, int n, int nb, const double *v, double
     PALIAL_CK(mps_colmax(v, n, nrhs, dscale, s), "scale");
     PALIAL_CK(cudaMemcpyAsync(hscale.data(), dscale, sizeof(double) * nrhs, cudaMemcpyDeviceToHost, s), "scale");
     PALIAL_CK(cudaStreamSynchronize(s), "scale");
-    for (int j = 0; j < nrhs; j++)
+    for (int j = 0; j < nrhs; j++) {
+        if (!std::isfinite(hscale[j])) return set_status(st, PALIAL_ERR_NOT_CONVERGED, "non-finite residual");
         if (hscale[j] == 0.0) hscale[j] = 1.0;
+    }
     PALIAL_CK(cudaMemcpyAsync(dscale, hscale.data(), sizeof(double) * nrhs, cudaMemcpyHostToDevice, s), "scale");
     PALIAL_CK(mps_to_f32_rhs(v, mb.r32.as<float>(), n, nrhs, dscale, s), "to f32");
     int rc = mp_apply_inverse(alg, W, n, nb, mb.r32.as<float>(), s, st);
@@ -488,6 +490,10 @@ static int solve_one(int alg, const double *dA, int n, int nb, const double *dB,
                        1e-4, s, st, &inner);
             if (rc) return rc;
             gmres_total += inner;
+            if (o.reserved[3] > 0 && gmres_total >= o.reserved[3]) {
+                it++;
+                break;  // GMRES budget of this attempt spent (precision ladder moves up)
+            }
         }
         {
             std::vector<double> ones(nrhs, -1.0);
@@ -501,8 +507,15 @@ static int solve_one(int alg, const double *dA, int n, int nb, const double *dB,
         PALIAL_CK(cudaMemcpyAsync(hx.data(), nrm + 33, sizeof(double) * nrhs, cudaMemcpyDeviceToHost, s), "norm x");
         PALIAL_CK(cudaStreamSynchronize(s), "iteration");
         eta = 0.0;
-        for (int j = 0; j < nrhs; j++) eta = std::max(eta, hr[j] / (anorm * hx[j] + hb[j]));
-        if (!std::isfinite(eta)) break;
+        bool finite = true;
+        for (int j = 0; j < nrhs; j++) {
+            finite = finite && std::isfinite(hr[j]) && std::isfinite(hx[j]);
+            eta = std::max(eta, hr[j] / (anorm * hx[j] + hb[j]));
+        }
+        if (!finite || !std::isfinite(eta)) {
+            eta = INFINITY;
+            break;
+        }
         if (eta <= tol) {
             converged = true;
             break;
@@ -551,7 +564,14 @@ extern "C" int palial_gpu_solve_ir(int alg, const double *dA, int n, int nb, con
     int used = -1;
     for (int prec : ladder) {
         o.precision = prec;
-        rc = solve_one(alg, dA, n, nb, dB, dX, nrhs, &o, st, stream);
+        // lower rungs get a bounded effort: at most 10 outer iterations and 100 GMRES steps
+        palial_opts oo = o;
+        if (prec != PALIAL_PREC_FP64) {
+            if (oo.ir_max_iter <= 0 || oo.ir_max_iter > 10) oo.ir_max_iter = 10;
+            oo.reserved[1] = 50;
+            oo.reserved[3] = 100;
+        }
+        rc = solve_one(alg, dA, n, nb, dB, dX, nrhs, &oo, st, stream);
         used = prec;
         if (rc >= 0) break;
         if (rc != PALIAL_ERR_NOT_CONVERGED && rc != PALIAL_ERR_NOT_SPD) break;

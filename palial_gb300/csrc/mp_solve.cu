@@ -223,13 +223,17 @@ __global__ void rowsum_kernel(const double *A, int n, int nb, double *out_max) {
     }
 }
 
-// per-column max |x| of dense n x cols (FP64), atomicMax on the bit patterns (values >= 0)
+// per-column max |x| of dense n x cols (FP64), atomicMax on the bit patterns (values >= 0).
+// NaN propagates (a NaN anywhere makes the column's maximum NaN: its bit pattern as an
+// unsigned integer exceeds every finite double), so a non-finite solution can never look
+// like a zero residual.
+__device__ __forceinline__ double nanmax(double a, double b) { return (a > b || a != a) ? a : b; }
 __global__ void colmax_kernel(const double *X, long long n, int cols, double *out) {
     const int c = blockIdx.y;
     double mx = 0.0;
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
-        mx = fmax(mx, fabs(X[(size_t)i + (size_t)c * n]));
-    for (int o = 16; o; o >>= 1) mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+        mx = nanmax(mx, fabs(X[(size_t)i + (size_t)c * n]));
+    for (int o = 16; o; o >>= 1) mx = nanmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
     if ((threadIdx.x & 31) == 0)
         atomicMax(reinterpret_cast<unsigned long long *>(out + c), (unsigned long long)__double_as_longlong(mx));
 }

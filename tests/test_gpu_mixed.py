@@ -126,3 +126,20 @@ def test_kappa_sweep_small(alg, kappa):
     if kappa <= 1e6:
         assert st.code in (0, 1), st.message
         assert st.backward_error <= 1e-14 * n
+
+
+def test_non_finite_factor_is_not_reported_as_converged():
+    """An exact zero leading pivot: the no-pivot LU skips it (as the reference does) and the
+    factor is singular; refinement must end with an error, never with a false success."""
+    n, nb, nrhs = 1024, 256, 4
+    a = dominant(3, n)
+    a[0, :] = 0.0
+    a[:, 0] = 0.0
+    b = O.gen_uniform(5, n, nrhs, stream=O.STREAM_RHS)
+    da = torch.from_numpy(O.to_tiles(a, nb)).cuda()
+    db = torch.from_numpy(np.asfortranarray(b).ravel(order="F")).cuda()
+    dx = torch.zeros_like(db)
+    for prec in ("bf16", "fp8", "fp64"):
+        st = P.solve_ir("lu", da.data_ptr(), n, nb, db.data_ptr(), dx.data_ptr(), nrhs, precision=prec,
+                        ir_max_iter=5, raise_on_error=False)
+        assert st.code < 0, (prec, st.code, st.backward_error)
