@@ -326,7 +326,7 @@ def run_suite(args, P, torch) -> None:
         return
     if args.suite == "fp64":
         for alg in ("cholesky", "lu", "qr"):
-            for n in (16384, 32768):
+            for n in ((4096, 16384, 32768) if alg == "cholesky" else (16384, 32768)):
                 d0 = torch.empty(n * n, dtype=torch.float64, device="cuda")
                 if alg == "cholesky":
                     P.gen_spd(d0.data_ptr(), n, NB, 0)
