@@ -238,6 +238,9 @@ int palial_gpu_residual_host(int alg, const double *a0_host, const palial_desc *
  * start/end ns, SM id and dispatch index is written to `csv_path` if not NULL. */
 int palial_gpu_trace_dump(const char *path, const char *csv_path);
 long long palial_gpu_trace_count(void);
+/* Host only: the task names of a DAG in creation order, newline separated (the same names the
+ * trace prints).  Returns the bytes needed including the terminating zero, -1 on bad sizes. */
+long long palial_dag_names(int alg, int n, int nb, int block, char *buf, long long buflen);
 
 /* ---- GPU clock reporting (replaces the reference's palial_power CPU frequency control) ----- */
 typedef struct palial_clock_report {

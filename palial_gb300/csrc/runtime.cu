@@ -725,6 +725,24 @@ int palial_gpu_set_task_costs(int alg, int n, int nb, int block, const double *c
 
 int palial_dag_features_count(void) { return kFeatures; }
 
+// The reference-rule task names of a DAG (creation order), newline separated.  Returns the
+// number of bytes needed (including the terminating zero).
+long long palial_dag_names(int alg, int n, int nb, int block, char *buf, long long buflen) {
+    try {
+        const int bs = block > 0 ? block : auto_block(alg, n, nb);
+        Dag d = build_dag(alg, n, nb, bs);
+        std::string all;
+        for (const auto &s : reference_names(d)) {
+            all += s;
+            all += '\n';
+        }
+        if (buf && buflen > (long long)all.size()) memcpy(buf, all.c_str(), all.size() + 1);
+        return (long long)all.size() + 1;
+    } catch (const std::exception &) {
+        return -1;
+    }
+}
+
 long long palial_dag_info(int alg, int n, int nb, int block, int priority, int nworkers, long long *type_counts,
                           double *critical_path_s, double *makespan_s) {
     try {

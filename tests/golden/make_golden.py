@@ -10,7 +10,10 @@ checksums and outputs as small .npz files:
   of the seeded generators (SPD B B^T + N I with seed 0; uniform [-1, 1) with seed 1; the
   reference's own diagonally dominant pattern 0.5 + diag in [173, 346) from seed 3);
 * ``sha256.json``: SHA-256 of reference outputs at N = 1024, NB = 256 (bit-exact check of
-  the restatement wherever the same OpenBLAS build is loaded).
+  the restatement wherever the same OpenBLAS build is loaded);
+* ``trace_names_cholesky_8192_512.txt``: the task names, in creation order, of the
+  reference's own published trace of Cholesky N = 8192, NB = 512
+  (exp/data/tasks_times_8192_512_31_ondemand, first column).
 
 Usage: ``python tests/golden/make_golden.py`` (needs the reference checkout).
 """
@@ -27,6 +30,8 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, os.path.dirname(os.path.dirname(HERE)))
 
 from oracle import build_oracle, oracle as O  # noqa: E402
+
+REF = build_oracle.REF_DEFAULT
 
 
 def sha(a: np.ndarray) -> str:
@@ -100,6 +105,10 @@ def main() -> None:
                     st[i, j] = np.triu(st[i, j].T).T  # tile stored column-major: [col][row]
             big[alg]["s_upper"] = sha(st)
     meta["sha256_1024_256"] = big
+    published = os.path.join(REF, "exp", "data", "tasks_times_8192_512_31_ondemand")
+    with open(published) as src, open(os.path.join(HERE, "trace_names_cholesky_8192_512.txt"), "w") as dst:
+        for line in src:
+            dst.write(line.split(",")[0].strip() + "\n")
     with open(os.path.join(HERE, "sha256.json"), "w") as f:
         json.dump(meta, f, indent=1, sort_keys=True)
     print("wrote fixtures for", blas)

@@ -89,3 +89,33 @@ def test_batch_dag_validates_and_isolates_matrices():
     buf = ctypes.create_string_buffer(256)
     rc = P.lib().palial_dag_batch_validate(60, arr(algs), arr(npad), arr(bs), arr(bs), 152, 5, buf, 256)
     assert rc == 0, buf.value
+
+
+def _names(alg, n, nb, block):
+    import ctypes
+    lib = P.lib()
+    lib.palial_dag_names.restype = ctypes.c_longlong
+    lib.palial_dag_names.argtypes = [ctypes.c_int] * 4 + [ctypes.c_char_p, ctypes.c_longlong]
+    need = lib.palial_dag_names({"cholesky": 0, "lu": 1, "qr": 2}[alg], n, nb, block, None, 0)
+    buf = ctypes.create_string_buffer(need)
+    lib.palial_dag_names({"cholesky": 0, "lu": 1, "qr": 2}[alg], n, nb, block, buf, need)
+    return buf.value.decode().split()
+
+
+def test_task_names_equal_reference_published_trace():
+    """The reference's own trace of Cholesky N=8192 NB=512 (exp/data, first column): same
+    names, same creation order, stale loop variables included (potrf11615 ...)."""
+    gold = open(os.path.join(ROOT, "tests", "golden", "trace_names_cholesky_8192_512.txt")).read().split()
+    assert _names("cholesky", 8192, 512, 512) == gold
+    assert "potrf11615" in gold
+
+
+def test_task_names_lu_qr_follow_loop_rule():
+    """Names from the reference's loops (src/lu.h:14-144, src/qr.h:18-158): k, m, n are
+    function-scope ints, so a name takes whatever value the last finished loop left."""
+    lu = _names("lu", 2048, 512, 512)
+    assert lu[:9] == ["getrf000", "trsm010", "trsm020", "trsm030", "trsm041", "gemm011", "gemm021",
+                      "gemm031", "trsm042"]
+    assert lu[16] == "getrf144" and len(lu) == 4 + 6 + 6 + 14
+    qr = _names("qr", 1024, 512, 512)
+    assert qr == ["geqrt000", "ormqr001", "tsqrt012", "tsmqr011", "geqrt122"]

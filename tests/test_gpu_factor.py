@@ -184,3 +184,21 @@ def test_dependency_timeout_is_reported_not_hung():
     got, _, _ = gpu_factor("cholesky", a, nb)  # still works afterwards
     ref, _ = oracle_factor("cholesky", a, nb)
     assert rel(got, ref) <= 1e-12
+
+
+def test_trace_names_equal_reference_published_trace(tmp_path):
+    """Device trace of Cholesky N=8192 NB=512 (block = tile): one `name, ms` line per task in
+    the reference's creation order, the same names as its own published trace
+    (exp/data/tasks_times_8192_512_31_ondemand), every duration positive and finite."""
+    import torch
+    n, nb = 8192, 512
+    a = torch.empty(n * n, dtype=torch.float64, device="cuda")
+    P.gen_spd(a.data_ptr(), n, nb, 0)
+    P.factor_dev("cholesky", a.data_ptr(), None, n, nb, block=nb, trace=True)
+    out = tmp_path / "trace.txt"
+    P.trace_dump(str(out))
+    lines = out.read_text().splitlines()
+    gold = open(os.path.join(GOLD, "trace_names_cholesky_8192_512.txt")).read().split()
+    assert [ln.split(",")[0] for ln in lines] == gold
+    ms = np.array([float(ln.split(",")[1]) for ln in lines])
+    assert np.all(np.isfinite(ms)) and np.all(ms > 0)
