@@ -14,6 +14,13 @@
  * size, trace, ...) and `palial_entry_status` (time, TFLOP/s, error details) can be set/read
  * by the caller around the calls.
  *
+ * Trace hooks: the reference's tasks call the weak hooks palial_set_task_name,
+ * palial_set_task_cpu_node and palial_get_task_time (reference include/common.h:9-11) that a
+ * tracing library may define.  When palial_entry_opts.trace is set, the wrappers replay the
+ * device trace of the call into whichever of those hooks are linked: every name in creation
+ * order, then per task the SM id as `cpu`, the GPU ordinal as `node`, and the task's start and
+ * end wall times.
+ *
  * MATRIX_desc must be defined before inclusion: by the reference's include/descriptor.h or
  * by palial_descriptor.h (identical layout).
  */
@@ -21,14 +28,39 @@
 #define PALIAL_ENTRY_H
 
 #include <stdio.h>
+#include <sys/time.h>
 
 #include "palial_gpu.h"
 
 palial_opts palial_entry_opts;
 palial_status palial_entry_status;
 
+void __attribute__((weak)) palial_set_task_name(const char *name);
+void __attribute__((weak)) palial_set_task_cpu_node(int cpu, int node, char *name);
+void __attribute__((weak)) palial_get_task_time(struct timeval start, struct timeval end, char *name);
+
+static void palial_entry_task_time(long long start_us, long long end_us, char *name)
+{
+    struct timeval a, b;
+    a.tv_sec = (time_t)(start_us / 1000000);
+    a.tv_usec = (suseconds_t)(start_us % 1000000);
+    b.tv_sec = (time_t)(end_us / 1000000);
+    b.tv_usec = (suseconds_t)(end_us % 1000000);
+    palial_get_task_time(a, b, name);
+}
+
+static void palial_entry_hooks(int rc)
+{
+    if (rc < 0 || !palial_entry_opts.trace) return;
+    if (!palial_set_task_name && !palial_set_task_cpu_node && !palial_get_task_time) return;
+    palial_gpu_trace_hooks(palial_set_task_name ? palial_set_task_name : NULL,
+                           palial_set_task_cpu_node ? palial_set_task_cpu_node : NULL,
+                           palial_get_task_time ? palial_entry_task_time : NULL);
+}
+
 static void palial_entry_report(const char *what, int rc)
 {
+    palial_entry_hooks(rc);
     if (rc < 0)
         fprintf(stderr, "palial: %s failed: %s (%s)\n", what, palial_gpu_error_string(rc),
                 palial_entry_status.message);

@@ -238,6 +238,13 @@ int palial_gpu_residual_host(int alg, const double *a0_host, const palial_desc *
  * start/end ns, SM id and dispatch index is written to `csv_path` if not NULL. */
 int palial_gpu_trace_dump(const char *path, const char *csv_path);
 long long palial_gpu_trace_count(void);
+/* Replay the last trace into the reference's trace hooks (reference include/common.h:9-11):
+ * set_name(name) for every task in creation order, then per task in start order
+ * cpu_node(SM id, device ordinal, name) and task_time(start_us, end_us, name), wall-clock
+ * microseconds since the epoch.  NULL hooks are skipped.  palial_entry.h calls this with the
+ * weak palial_set_task_name / palial_set_task_cpu_node / palial_get_task_time. */
+int palial_gpu_trace_hooks(void (*set_name)(const char *), void (*cpu_node)(int, int, char *),
+                           void (*task_time)(long long, long long, char *));
 /* Host only: the task names of a DAG in creation order, newline separated (the same names the
  * trace prints).  Returns the bytes needed including the terminating zero, -1 on bad sizes. */
 long long palial_dag_names(int alg, int n, int nb, int block, char *buf, long long buflen);
@@ -248,7 +255,14 @@ typedef struct palial_clock_report {
     double sm_mhz_device;                         /* clock64 / globaltimer during the run */
     int throttle_reasons;                         /* NVML bit mask, -1 if unavailable     */
 } palial_clock_report;
+/* Clocks around the last traced factorization (NVML samples just before and during the
+ * launch, device clock64/globaltimer ratio of its tasks); without a traced run, the current
+ * NVML values.  NVML is loaded at run time and only queried, never used to set anything. */
 int palial_gpu_clock_report(palial_clock_report *out);
+/* The current SM clock, its maximum (MHz) and the NVML clock-event reason mask (bit 0x4
+ * software power cap, 0x8 hardware slowdown, 0x20 software thermal, 0x40 hardware thermal).
+ * PALIAL_ERR_NO_DEVICE (values -1) when NVML is not available. */
+int palial_gpu_clock_sample(double *sm_mhz, double *sm_max_mhz, long long *reasons);
 
 /* ---- DAG builder (host only; exported for tests) -------------------------------------------- */
 /* Build the task list the scheduler would run; returns the number of tasks, fills counts per

@@ -74,11 +74,18 @@ struct State {
     unsigned long long next_uid = 1;
     TraceState last_trace;
     int last_trace_workers = 0;
+    long long last_trace_host_ns = 0;  // host CLOCK_REALTIME just before the traced launch
+    // NVML clock samples around the last traced factorization (-1: not available)
+    double clk_start = -1, clk_end = -1, clk_max = -1;
+    long long clk_reasons = -1;
     // learned per-task costs (seconds, per logical task) keyed by "alg,n,nb,bs"
     std::map<std::string, std::vector<double>> task_costs;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
 };
 extern State g;
+
+// Read-only NVML query of the library's device (false and -1 values without NVML).
+bool nvml_sample(double *sm_mhz, double *sm_max_mhz, long long *reasons);
 
 int set_status(palial_status *st, int code, const char *fmt = nullptr, ...);
 int cuda_fail(palial_status *st, cudaError_t e, const char *what);

@@ -11,6 +11,7 @@
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
+#include <ctime>
 #include <map>
 #include <memory>
 #include <string>
@@ -273,10 +274,27 @@ int palial_gpu_factor_dev(int alg, double *dA, double *dS, int n, int nb, const 
         }
         CK(cudaMemcpy(g.main.tasks.as<Task>() + stall, &t, sizeof(Task), cudaMemcpyHostToDevice), "inject stall");
     }
+    double clk0 = -1, clk_max = -1;
+    long long reasons = -1;
+    if (o.trace) {
+        nvml_sample(&clk0, &clk_max, &reasons);
+        timespec ts;
+        clock_gettime(CLOCK_REALTIME, &ts);
+        g.last_trace_host_ns = (long long)ts.tv_sec * 1000000000ll + ts.tv_nsec;
+    }
     const auto w0 = std::chrono::steady_clock::now();
     CK(cudaEventRecord(g.ev0, s), "event");
     CK(sched_enqueue(g.main, p, dag->nobj, workers, true, s), "launch scheduler");
     CK(cudaEventRecord(g.ev1, s), "event");
+    if (o.trace) {
+        // sample while the scheduler runs (the launch is asynchronous)
+        double c1, m1;
+        nvml_sample(&c1, &m1, &reasons);
+        g.clk_start = clk0;
+        g.clk_end = c1;
+        g.clk_max = m1;
+        g.clk_reasons = reasons;
+    }
     CK(cudaEventSynchronize(g.ev1), "scheduler run");
     float ms = 0.f;
     cudaEventElapsedTime(&ms, g.ev0, g.ev1);
@@ -821,6 +839,60 @@ int palial_gpu_clock_report(palial_clock_report *out) {
             ns += (double)(r.t1 - r.t0);
         }
         if (ns > 0) out->sm_mhz_device = cyc / ns * 1e3;
+        out->sm_mhz_start = g.clk_start;
+        out->sm_mhz_end = g.clk_end;
+        out->sm_mhz_max = g.clk_max;
+        out->throttle_reasons = (int)g.clk_reasons;
+    } else {
+        // no traced run yet: the current clocks
+        long long r;
+        nvml_sample(&out->sm_mhz_end, &out->sm_mhz_max, &r);
+        out->throttle_reasons = (int)r;
+    }
+    return PALIAL_OK;
+}
+
+// Replays the last trace into the reference's hook interface (include/common.h:9-11 of the
+// reference): every task name in creation order (set_task_name, called by the reference at
+// task creation), then per task in start order the executing SM and GPU ordinal
+// (set_task_cpu_node: cpu -> SM id, node -> device) and the start/end wall times in
+// microseconds since the epoch (get_task_time; the host clock at launch plus the device
+// %globaltimer offsets).  A NULL hook is skipped.
+int palial_gpu_trace_hooks(void (*set_name)(const char *), void (*cpu_node)(int, int, char *),
+                           void (*task_time)(long long, long long, char *)) {
+    if (!g.last_trace.valid) return PALIAL_ERR_ARG;
+    const Dag &d = g.last_trace.dag;
+    const auto names = reference_names(d);
+    const size_t nl = d.logical.size();
+    std::vector<unsigned long long> t0(nl, ~0ull), t1(nl, 0);
+    std::vector<unsigned> sm(nl, 0);
+    unsigned long long tmin = ~0ull;
+    for (size_t r = 0; r < d.records.size(); r++) {
+        const TraceRec &x = g.last_trace.recs[r];
+        const uint32_t l = d.rec_logical[r];
+        if (x.t0 < t0[l]) {
+            t0[l] = x.t0;
+            sm[l] = x.smid;
+        }
+        t1[l] = std::max(t1[l], x.t1);
+        tmin = std::min(tmin, x.t0);
+    }
+    std::vector<std::vector<char>> buf(nl);
+    for (size_t l = 0; l < nl; l++) {
+        buf[l].assign(names[l].begin(), names[l].end());
+        buf[l].push_back(0);
+        if (set_name) set_name(buf[l].data());
+    }
+    std::vector<size_t> order(nl);
+    for (size_t l = 0; l < nl; l++) order[l] = l;
+    std::stable_sort(order.begin(), order.end(), [&](size_t a, size_t b) { return t0[a] < t0[b]; });
+    for (size_t l : order) {
+        if (cpu_node) cpu_node((int)sm[l], g.device, buf[l].data());
+        if (task_time) {
+            const long long s = (g.last_trace_host_ns + (long long)(t0[l] - tmin)) / 1000;
+            const long long e = (g.last_trace_host_ns + (long long)(t1[l] - tmin)) / 1000;
+            task_time(s, e, buf[l].data());
+        }
     }
     return PALIAL_OK;
 }

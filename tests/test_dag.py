@@ -18,8 +18,11 @@ def test_library_exports_every_declared_symbol():
         if hdr.endswith(".h"):
             src = open(os.path.join(ROOT, "include", hdr)).read()
             src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
-            # prototypes only (header-defined helpers of palial_entry.h are not exports)
-            names |= set(re.findall(r"\b(palial_\w+)\s*\([^;{)]*\)\s*;", src))
+            # prototypes only: a return type before the name, ';' after the parameter list
+            # (header-defined helpers of palial_entry.h, calls inside them and the caller's weak
+            # trace hooks are not exports)
+            names |= set(re.findall(r"^[ \t]*(?:\w+[ \t\*]+)+(palial_\w+)\s*\((?:[^;{()]|\([^()]*\))*\)\s*;", src,
+                                    flags=re.M))
     assert names
     lib = P.lib()
     missing = [n for n in sorted(names) if not hasattr(lib, n)]
