@@ -151,6 +151,21 @@ int palial_gpu_mp_factor(int alg, const double *dA, float *dW, int n, int nb,
  * apply C -= A_op B_op^T with the tcgen05 kernel (Cholesky: upper tile pairs; LU: all). */
 int palial_gpu_mp_update_step(int alg, int precision, float *dW, int n, int nb, int k);
 
+/* ---- linear solve and least squares through the tile QR (no reference counterpart) -------
+ * A: rows x cols FP64 tile matrix on the device (rows >= cols, both multiples of nb, nb a
+ * multiple of 64; tile (m,n) at element nb*nb*(m + (rows/nb)*n)), not modified.
+ * B: rows x nrhs column-major (ld = rows), 1 <= nrhs <= nb.  X: cols x nrhs column-major
+ * (ld = cols) receives the solution of A X = B (square) or the least-squares solution
+ * min ||A X - B||_2 (tall).  resid (optional, nrhs doubles) receives ||A x_j - b_j||_2 for
+ * the tall case (0 for square).  One persistent launch runs the flat-tree tile QR of [A | B]
+ * (Q^T applied to B by the same UNMQR/TSMQR tasks as the reference's src/qr.h:57-188 applies
+ * to the trailing tiles) followed by the blocked back-substitution with R. */
+int palial_gpu_qr_solve(int rows, int cols, int nb, const double *dA, const double *dB, double *dX, int nrhs,
+                        double *dResid, const palial_opts *opts, palial_status *st, void *stream);
+/* Same with host buffers (A in tile layout, B and X column-major, resid optional). */
+int palial_gpu_qr_solve_host(int rows, int cols, int nb, const double *A, const double *B, double *X, int nrhs,
+                             double *resid, const palial_opts *opts, palial_status *st);
+
 /* ---- single-tile kernels on device pointers (reference tile-kernel ABI, for unit tests) ----
  * Each runs one tile task on one CTA of the persistent scheduler's kernels.
  * Replace reference src/srclu/dgetrf.h:11 PALIAL_dgetrf, src/srcqr/dgeqrt.h:9 PALIAL_dgeqrt,
@@ -181,7 +196,7 @@ int palial_gpu_tile_dtsmqr(int nb, double *dA1, double *dA2, const double *dV, c
 int palial_gpu_tile_dtsmqr_noalloc(int nb, double *dA1, double *dA2, const double *dV,
                                    const double *dT, int lda, void *stream);
 /* kind for dtrsm: 0 = left upper trans non-unit (Cholesky), 1 = right upper no-trans non-unit
- * (LU), 2 = left lower no-trans unit (LU).  kind for dgemm: 0 = C -= A^T B (Cholesky),
+ * (LU), 2 = left lower no-trans unit (LU), 3 = left upper no-trans non-unit (QR solve).  kind for dgemm: 0 = C -= A^T B (Cholesky),
  * 1 = C -= A B (LU). */
 
 /* ---- batched factorizations (no reference counterpart: north-star) ------------------------
@@ -269,6 +284,11 @@ int palial_gpu_clock_sample(double *sm_mhz, double *sm_max_mhz, long long *reaso
  * task type (array of 16) and the critical-path length estimate (seconds, model costs). */
 long long palial_dag_info(int alg, int n, int nb, int block, int priority, int nworkers,
                           long long *type_counts, double *critical_path_s, double *makespan_s);
+/* Host only: build, order and validate the QR solve DAG (rows x cols, nrhs right-hand
+ * sides); returns its number of task records, or -1 with the reason in msg.  type_counts
+ * (optional, 16 entries) receives the logical task count per type. */
+long long palial_dag_qr_solve_validate(int rows, int cols, int nb, int nrhs, int nworkers, unsigned int seed,
+                                       long long *type_counts, char *msg, int msglen);
 /* Validate a built DAG on the host: every wait is satisfiable by earlier tasks in dispatch
  * order, updates to each object are totally ordered, no read/write race; then emulate the
  * dispatch with `nworkers` workers and random durations (seed).  Returns 0 if valid. */

@@ -93,16 +93,17 @@ def run_reference(alg: str, a_tiles: np.ndarray, n: int, nb: int,
 # Tile layout (include/tile_address.h:9-17)
 # --------------------------------------------------------------------------------------
 def to_tiles(a: np.ndarray, nb: int) -> np.ndarray:
-    """Full N x N matrix (indexed a[i, j]) -> flat tile-layout buffer."""
-    n = a.shape[0]
-    mt = n // nb
-    return np.ascontiguousarray(a.reshape(mt, nb, mt, nb).transpose(2, 0, 3, 1)).ravel()
+    """Full M x N matrix (indexed a[i, j]) -> flat tile-layout buffer: tile (m, n) at element
+    nb*nb*(m + (M/nb)*n), column-major inside (reference include/tile_address.h:9-17)."""
+    mt, nt = a.shape[0] // nb, a.shape[1] // nb
+    return np.ascontiguousarray(a.reshape(mt, nb, nt, nb).transpose(2, 0, 3, 1)).ravel()
 
 
-def from_tiles(t: np.ndarray, n: int, nb: int) -> np.ndarray:
-    """Flat tile-layout buffer -> full N x N matrix indexed [i, j]."""
-    mt = n // nb
-    return np.ascontiguousarray(t.reshape(mt, mt, nb, nb).transpose(1, 3, 0, 2).reshape(n, n))
+def from_tiles(t: np.ndarray, n: int, nb: int, cols: int | None = None) -> np.ndarray:
+    """Flat tile-layout buffer -> full n x cols (default n x n) matrix indexed [i, j]."""
+    cols = n if cols is None else cols
+    mt, nt = n // nb, cols // nb
+    return np.ascontiguousarray(t.reshape(nt, mt, nb, nb).transpose(1, 3, 0, 2).reshape(n, cols))
 
 
 # --------------------------------------------------------------------------------------
@@ -193,13 +194,13 @@ def qr_apply_qt(f: np.ndarray, s: np.ndarray, nb: int, c: np.ndarray) -> np.ndar
     """Apply Q^T of the flat-tree tile QR (factors f, T factors s, both full matrices) to c.
 
     Follows the transform order of src/qr.h:15-192: for each k, the GEQRT block reflector
-    of tile row k, then the TS block reflectors coupling tile rows k and m > k.
+    of tile row k, then the TS block reflectors coupling tile rows k and m > k.  f may be tall
+    (rows x cols factors of the same algorithm on a rectangular tile grid).
     """
-    n = f.shape[0]
-    mt = n // nb
+    mt, nt = f.shape[0] // nb, f.shape[1] // nb
     c = c.copy()
     blk = lambda i: slice(i * nb, (i + 1) * nb)  # noqa: E731
-    for k in range(mt):
+    for k in range(nt):
         v = np.tril(f[blk(k), blk(k)], -1) + np.eye(nb)
         t = np.triu(s[blk(k), blk(k)])
         c[blk(k)] -= v @ (t.T @ (v.T @ c[blk(k)]))
@@ -210,6 +211,23 @@ def qr_apply_qt(f: np.ndarray, s: np.ndarray, nb: int, c: np.ndarray) -> np.ndar
             c[blk(k)] -= w
             c[blk(m)] -= v2 @ w
     return c
+
+
+def r_upper(f: np.ndarray, nb: int) -> np.ndarray:
+    """R of the tile QR: the upper triangle of the top cols x cols tile block of the factors."""
+    cols = f.shape[1]
+    return np.triu(f[:cols, :cols])
+
+
+def qr_solve(f: np.ndarray, s: np.ndarray, nb: int, b: np.ndarray) -> tuple[np.ndarray, np.ndarray]:
+    """Solve / least squares with the tile QR factors: y = Q^T b, x = R^-1 y(0:cols); returns
+    (x, ||y(cols:rows)||_2 per column)."""
+    import scipy.linalg as sl
+
+    cols = f.shape[1]
+    y = qr_apply_qt(f, s, nb, b.reshape(f.shape[0], -1))
+    x = sl.solve_triangular(r_upper(f, nb), y[:cols], lower=False)
+    return x, np.linalg.norm(y[cols:], axis=0)
 
 
 def qr_checks(a: np.ndarray, f: np.ndarray, s: np.ndarray, nb: int) -> tuple[float, float]:

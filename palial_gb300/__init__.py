@@ -114,6 +114,13 @@ def lib() -> ctypes.CDLL:
                                                 ctypes.c_uint, ctypes.c_char_p, i]
         h.palial_gpu_solve_ir_host.argtypes = [i, ctypes.POINTER(Desc), vp, vp, i, ctypes.POINTER(Opts),
                                                ctypes.POINTER(Status)]
+        h.palial_gpu_qr_solve.argtypes = [i, i, i, vp, vp, vp, i, vp, ctypes.POINTER(Opts), ctypes.POINTER(Status),
+                                          vp]
+        h.palial_gpu_qr_solve_host.argtypes = [i, i, i, vp, vp, vp, i, vp, ctypes.POINTER(Opts),
+                                               ctypes.POINTER(Status)]
+        h.palial_dag_qr_solve_validate.restype = ctypes.c_longlong
+        h.palial_dag_qr_solve_validate.argtypes = [i, i, i, i, i, ctypes.c_uint, ctypes.POINTER(ctypes.c_longlong),
+                                                   ctypes.c_char_p, i]
         _lib = h
     return _lib
 
@@ -204,6 +211,40 @@ def solve_ir_host(alg: str, a_tiles: np.ndarray, n: int, nb: int, b: np.ndarray,
         _check(rc, st, allow=(PALIAL_OK, 1))
     st.code = rc
     return st
+
+
+def qr_solve(d_a: int, rows: int, cols: int, nb: int, d_b: int, d_x: int, nrhs: int, d_resid: int | None = None,
+             stream: int = 0, **kw) -> Status:
+    """A X = B (rows == cols) or least squares min ||A X - B||_2 (rows > cols) through the tile
+    QR, on device buffers: A tile layout (rows x cols), B rows x nrhs and X cols x nrhs
+    column-major, d_resid (optional) nrhs residual 2-norms."""
+    st = Status()
+    rc = lib().palial_gpu_qr_solve(rows, cols, nb, d_a, d_b, d_x, nrhs, d_resid or None,
+                                   ctypes.byref(make_opts(**kw)), ctypes.byref(st), stream or None)
+    _check(rc, st)
+    return st
+
+
+def qr_solve_host(a_tiles: np.ndarray, rows: int, cols: int, nb: int, b: np.ndarray, **kw):
+    """Host-buffer QR solve: returns (X cols x nrhs, residual norms, status)."""
+    b = np.asfortranarray(b.reshape(rows, -1), dtype=np.float64)
+    nrhs = b.shape[1]
+    x = np.zeros((cols, nrhs), dtype=np.float64, order="F")
+    resid = np.zeros(nrhs)
+    st = Status()
+    rc = lib().palial_gpu_qr_solve_host(rows, cols, nb, np.ascontiguousarray(a_tiles).ctypes.data, b.ctypes.data,
+                                        x.ctypes.data, nrhs, resid.ctypes.data, ctypes.byref(make_opts(**kw)),
+                                        ctypes.byref(st))
+    _check(rc, st)
+    return x, resid, st
+
+
+def qr_solve_dag(rows: int, cols: int, nb: int, nrhs: int, nworkers: int = 152, seed: int = 0) -> dict:
+    """Host only: build and validate the QR solve DAG; records and logical task counts per type."""
+    counts = (ctypes.c_longlong * 16)()
+    msg = ctypes.create_string_buffer(256)
+    nrec = lib().palial_dag_qr_solve_validate(rows, cols, nb, nrhs, nworkers, seed, counts, msg, 256)
+    return {"records": nrec, "type_counts": list(counts), "message": msg.value.decode()}
 
 
 def mp_factor(alg: str, d_a: int, d_w: int, n: int, nb: int, stream: int = 0, **kw) -> Status:

@@ -29,6 +29,8 @@ enum TaskType : uint8_t {
     T_UNMQR,       // tile (k,n) <- (I - V T V^T)^T tile(k,n); part = column strip
     T_TSQRT,       // tiles (k,k) upper + (m,k) -> S(m,k)
     T_TSMQR,       // tiles (k,n), (m,n) with V = A(m,k), T = S(m,k); part = column strip
+    // QR solve back-substitution
+    T_TRSM_LUN,    // block (k,n) <- R(k,k)^-1 block(k,n) (R upper, non-unit); part = column strip
     T_NUM_TYPES
 };
 

@@ -30,6 +30,7 @@ double nominal_flops(int type, int bs, int nb, int part) {
         case T_UNMQR: return 3.0 * q * q * w;
         case T_TSQRT: return 3.0 * q * q * q;
         case T_TSMQR: return 5.0 * q * q * w;
+        case T_TRSM_LUN: return b * b * w;
         default: return 0.0;
     }
 }
@@ -71,7 +72,7 @@ struct Builder {
 
 double task_cost(int type, int bs, int nb, int part, const double *costs) {
     const double f = nominal_flops(type, bs, nb, part);
-    if (costs && costs[type] > 0.0) return costs[type] * f;
+    if (costs && type < T_TRSM_LUN && costs[type] > 0.0) return costs[type] * f;
     return f / kWorkerFlops;
 }
 
@@ -131,6 +132,41 @@ Dag build_dag(int alg, int n, int nb, int bs, const double *costs) {
     return d;
 }
 
+Dag build_qr_solve_dag(int rows, int cols, int nb, int nrhs) {
+    Dag d;
+    d.alg = 3;
+    d.n = rows;
+    d.cols = cols;
+    d.nrhs = nrhs;
+    d.nb = nb;
+    d.bs = nb;
+    if (nb <= 0 || nb % 64 || rows % nb || cols % nb || cols <= 0 || rows < cols || nrhs < 1 || nrhs > nb)
+        throw std::runtime_error("dag: bad QR solve sizes");
+    const int mt = rows / nb, nt = cols / nb;
+    const int parts = nb / 64, rparts = (nrhs + 63) / 64;
+    if (mt > 65535 || parts > 255) throw std::runtime_error("dag: QR solve too large");
+    auto obj = [mt](int i, int j) { return (uint32_t)(i + j * mt); };
+    Builder b(d, mt * (nt + 1));
+    for (int k = 0; k < nt; k++) {
+        b.emit(T_GEQRT, k, k, k, 1, {}, {obj(k, k)}, nullptr);
+        for (int j = k + 1; j < nt; j++) b.emit(T_UNMQR, k, 0, j, parts, {obj(k, k)}, {obj(k, j)}, nullptr);
+        b.emit(T_UNMQR, k, 0, nt, rparts, {obj(k, k)}, {obj(k, nt)}, nullptr);
+        for (int m = k + 1; m < mt; m++) {
+            b.emit(T_TSQRT, k, m, 0, 1, {}, {obj(k, k), obj(m, k)}, nullptr);
+            for (int j = k + 1; j < nt; j++)
+                b.emit(T_TSMQR, k, m, j, parts, {obj(m, k)}, {obj(k, j), obj(m, j)}, nullptr);
+            b.emit(T_TSMQR, k, m, nt, rparts, {obj(m, k)}, {obj(k, nt), obj(m, nt)}, nullptr);
+        }
+    }
+    // R X = Y: the last tile row first; every solved block updates the rows above it
+    for (int k = nt - 1; k >= 0; k--) {
+        b.emit(T_TRSM_LUN, k, k, nt, rparts, {obj(k, k)}, {obj(k, nt)}, nullptr);
+        for (int i = 0; i < k; i++) b.emit(T_GEMM_NN, k, i, nt, rparts, {obj(i, k), obj(k, nt)}, {obj(i, nt)}, nullptr);
+    }
+    recompute_bottom_levels(d);
+    return d;
+}
+
 void recompute_bottom_levels(Dag &d) {
     // reverse program order; M[x] = max bl of later tasks waiting on / updating x
     std::vector<double> M(d.nobj, 0.0);
@@ -160,7 +196,7 @@ std::vector<int> step_widths(const Dag &d) {
 void task_features(const Dag &d, const LogicalTask &t, int part, int nworkers, int precision,
                    const std::vector<int> &step_width, float *f) {
     for (int i = 0; i < kFeatures; i++) f[i] = 0.f;
-    f[t.type < 12 ? t.type : 11] = 1.f;
+    f[t.type == T_TRSM_LUN ? (int)T_TRSM_LUT : (t.type < 12 ? t.type : 11)] = 1.f;
     const int bs = d.bs > 0 ? d.bs : 64, nb = d.nb > 0 ? d.nb : bs;
     const double mb = std::max(1, d.n / bs);
     f[12] = (float)(std::log2((double)bs) / 10.0);
@@ -426,6 +462,14 @@ std::vector<std::string> reference_names(const Dag &d) {
         return std::string(b);
     };
     int k = 0, m = 0, n = 0;  // zero-initialised, as the reference's loop variables read as
+    if (d.alg < 0 || d.alg > 2) {
+        // no reference counterpart (batched, QR solve): type + the task's own coordinates
+        static const char *tn[] = {"potrf", "trsm", "syrk", "gemm", "getrf", "trsm", "trsm",
+                                   "gemm",  "geqrt", "ormqr", "tsqrt", "tsmqr", "trsm"};
+        for (const LogicalTask &t : d.logical)
+            names.push_back(nm(t.type < T_NUM_TYPES ? tn[t.type] : "task", t.k, t.m, t.n));
+        return names;
+    }
     if (d.alg == 0) {
         for (k = 0; k < mt; k++) {
             names.push_back(nm("potrf", k, m, n));

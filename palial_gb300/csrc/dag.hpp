@@ -26,7 +26,8 @@ struct LogicalTask {
 };
 
 struct Dag {
-    int alg = 0, n = 0, nb = 0, bs = 0;
+    int alg = 0, n = 0, nb = 0, bs = 0;  // alg 3 = QR solve: n = rows
+    int cols = 0, nrhs = 0;              // QR solve only
     int nobj = 0;
     unsigned long long uid = 0;         // unique per built DAG (device upload cache key)
     std::vector<LogicalTask> logical;   // program order
@@ -42,6 +43,13 @@ double task_cost(int type, int bs, int nb, int part, const double *costs);
 
 // Build the program-order DAG.  bs = block size (divides nb) for Cholesky/LU; QR uses nb.
 Dag build_dag(int alg, int n, int nb, int bs, const double *costs = nullptr);
+
+// QR solve / least squares (alg 3): the flat-tree tile QR of a rows x cols tile matrix
+// (rows >= cols, both multiples of nb) extended by one tile column holding nrhs <= nb
+// right-hand sides (tile column cols/nb of the rows x (cols + nb) tile layout), so the
+// UNMQR/TSMQR tasks apply Q^T to them inside the same launch; then the blocked
+// back-substitution R X = (Q^T B)(0:cols) with left-upper TRSM and GEMM tasks.
+Dag build_qr_solve_dag(int rows, int cols, int nb, int nrhs);
 
 // One matrix of a batch: algorithm (0 Cholesky, 1 LU), padded size, tile size, block size.
 struct BatchSpec {

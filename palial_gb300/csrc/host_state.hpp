@@ -84,6 +84,9 @@ struct State {
 };
 extern State g;
 
+// Free the QR solve's cached device buffers and DAG (palial_gpu_finalize).
+void qr_solve_release();
+
 // Read-only NVML query of the library's device (false and -1 values without NVML).
 bool nvml_sample(double *sm_mhz, double *sm_max_mhz, long long *reasons);
 

@@ -216,6 +216,7 @@ int palial_gpu_finalize(void) {
     if (g.batch_graph) cudaGraphExecDestroy(g.batch_graph);
     g.batch_graph = nullptr;
     for (DevBuf *b : {&g.mat, &g.smat, &g.kbuf, &g.probe}) b->release();
+    qr_solve_release();
     g.dags.clear();
     return PALIAL_OK;
 }
@@ -399,7 +400,7 @@ static int tile_call(int type, int nb, int ld, double *p0, double *p1, double *p
 int palial_gpu_tile_dpotrf(int nb, double *dA, int lda) { return tile_call(T_POTRF, nb, lda, dA, 0, 0, 0); }
 int palial_gpu_tile_dgetrf(int nb, double *dA, int lda) { return tile_call(T_GETRF, nb, lda, dA, 0, 0, 0); }
 int palial_gpu_tile_dtrsm(int kind, int nb, const double *dT, double *dB, int lda) {
-    const int ty = kind == 0 ? T_TRSM_LUT : kind == 1 ? T_TRSM_RUN : kind == 2 ? T_TRSM_LLU : -1;
+    const int ty = kind == 0 ? T_TRSM_LUT : kind == 1 ? T_TRSM_RUN : kind == 2 ? T_TRSM_LLU : kind == 3 ? T_TRSM_LUN : -1;
     if (ty < 0) return PALIAL_ERR_ARG;
     return tile_call(ty, nb, lda, const_cast<double *>(dT), dB, 0, 0);
 }
@@ -678,7 +679,7 @@ int palial_gpu_trace_dump(const char *path, const char *csv_path) {
         FILE *c = fopen(csv_path, "w");
         if (!c) return PALIAL_ERR_ARG;
         static const char *tn[] = {"potrf", "trsm", "syrk", "gemm", "getrf", "trsm", "trsm", "gemm",
-                                   "geqrt", "ormqr", "tsqrt", "tsmqr"};
+                                   "geqrt", "ormqr", "tsqrt", "tsmqr", "trsm"};
         fprintf(c, "dispatch,logical,name,type,k,m,n,part,nparts,t0_ns,t1_ns,smid,clk\n");
         for (size_t r = 0; r < d.records.size(); r++) {
             const TraceRec &x = g.last_trace.recs[r];
@@ -789,6 +790,24 @@ int palial_dag_validate(int alg, int n, int nb, int block, int priority, int nwo
         const std::string r = validate_dag(d, nworkers, seed);
         if (msg && msglen > 0) snprintf(msg, msglen, "%s", r.c_str());
         return r.empty() ? 0 : 1;
+    } catch (const std::exception &ex) {
+        if (msg && msglen > 0) snprintf(msg, msglen, "%s", ex.what());
+        return -1;
+    }
+}
+
+long long palial_dag_qr_solve_validate(int rows, int cols, int nb, int nrhs, int nworkers, unsigned int seed,
+                                       long long *type_counts, char *msg, int msglen) {
+    try {
+        Dag d = build_qr_solve_dag(rows, cols, nb, nrhs);
+        order_dag(d, 0, nworkers, seed);
+        if (type_counts) {
+            for (int i = 0; i < 16; i++) type_counts[i] = 0;
+            for (const auto &t : d.logical) type_counts[t.type]++;
+        }
+        const std::string r = validate_dag(d, nworkers, seed);
+        if (msg && msglen > 0) snprintf(msg, msglen, "%s", r.c_str());
+        return r.empty() ? (long long)d.records.size() : -1;
     } catch (const std::exception &ex) {
         if (msg && msglen > 0) snprintf(msg, msglen, "%s", ex.what());
         return -1;

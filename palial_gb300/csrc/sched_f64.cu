@@ -57,6 +57,7 @@ __device__ __forceinline__ Worker make_worker(double *smem) {
 //   KIND 0: U^T X = B (U upper, non-unit)   -- Cholesky TRSM (left, upper, trans)
 //   KIND 1: X U = B   (U upper, non-unit)   -- LU TRSM (right, upper, no-trans)
 //   KIND 2: L X = B   (L unit lower)        -- LU TRSM (left, lower, unit)
+//   KIND 3: U X = B   (U upper, non-unit)   -- QR solve back-substitution (left, upper)
 // ---------------------------------------------------------------------------------------
 template <int KIND>
 __device__ void solve64(const Worker &w, double *B, int ld) {
@@ -66,8 +67,17 @@ __device__ void solve64(const Worker &w, double *B, int ld) {
         w.Bs[c][r] = ldg(B + r + (size_t)c * ld);
     }
     __syncthreads();
-    for (int p = 0; p < 64; p++) {
-        if (KIND == 0) {
+    for (int pp = 0; pp < 64; pp++) {
+        const int p = (KIND == 3) ? 63 - pp : pp;
+        if (KIND == 3) {
+            // unknown row p (last first): X(p,c) = B(p,c) / U(p,p); rows i < p: B(i,c) -= U(i,p) X(p,c)
+            if (threadIdx.x < 64) w.Bs[threadIdx.x][p] = w.Bs[threadIdx.x][p] / w.Ds[p][p];
+            __syncthreads();
+            for (int e = threadIdx.x; e < 64 * 64; e += NT) {
+                const int i = e & 63, c = e >> 6;
+                if (i < p) w.Bs[c][i] = fma(-w.Ds[p][i], w.Bs[c][p], w.Bs[c][i]);
+            }
+        } else if (KIND == 0) {
             if (threadIdx.x < 64) w.Bs[threadIdx.x][p] = w.Bs[threadIdx.x][p] / w.Ds[p][p];
             __syncthreads();
             // rows i > p of every column c: B(i,c) -= U(p,i) X(p,c)
@@ -191,6 +201,16 @@ __device__ void trsm_run(const Worker &w, const double *U, double *B, int n, int
                                    w.gsm);
         load_diag64(w.Ds, U + cb + (size_t)cb * ld, ld);
         solve64<1>(w, B + (size_t)cb * ld, ld);
+    }
+}
+// X = U^-1 B (U upper, B n x 64): row blocks bottom-up.
+__device__ void trsm_lun(const Worker &w, const double *U, double *B, int n, int ld) {
+    for (int rb = n - 64; rb >= 0; rb -= 64) {
+        if (rb + 64 < n)
+            cta_gemm<false, false>(64, 64, n - rb - 64, -1.0, U + rb + (size_t)(rb + 64) * ld, ld, B + rb + 64, ld, 1.0,
+                                   B + rb, ld, w.gsm);
+        load_diag64(w.Ds, U + rb + (size_t)rb * ld, ld);
+        solve64<3>(w, B + rb, ld);
     }
 }
 // X = L^-1 B (L unit lower, B n x 64): row blocks top-down.
@@ -482,6 +502,12 @@ __device__ void run_task(const SchedParams &p, const Worker &w, const Task &t, i
                                    w.gsm);
             break;
         }
+        case T_TRSM_LUN: {
+            const double *U = block_ptr(A, n, nb, bs, t.k, t.k);
+            double *B = block_ptr(A, n, nb, bs, t.k, t.n) + (size_t)t.part * 64 * ld;
+            trsm_lun(w, U, B, bs, ld);
+            break;
+        }
         case T_GEQRT: {
             geqrt(w, tile_ptr(A, n, nb, t.k, t.k), nb, ld, tile_ptr(p.S, n, nb, t.k, t.k), ld);
             break;
@@ -601,6 +627,9 @@ __global__ void __launch_bounds__(NT, 1) tile_task_kernel(int type, int nb, int 
         case T_TRSM_LLU:
             for (int q = 0; q < parts; q++) trsm_llu(w, p0, p1 + (size_t)q * 64 * ld, nb, ld);
             break;
+        case T_TRSM_LUN:
+            for (int q = 0; q < parts; q++) trsm_lun(w, p0, p1 + (size_t)q * 64 * ld, nb, ld);
+            break;
         case T_SYRK:
             for (int q = 0; q < parts; q++) {
                 const int c0 = q * 64;
@@ -669,7 +698,7 @@ cudaError_t sched_launch(const SchedParams &p, int grid, cudaStream_t s) {
 long long sched_scratch_doubles(int alg, int n, int nb, int bs, int workers, long long *per_worker) {
     (void)n;
     (void)bs;
-    const long long pw = (alg == 2) ? 2LL * nb * 64 : 0;
+    const long long pw = (alg == 2 || alg == 3) ? 2LL * nb * 64 : 0;
     if (per_worker) *per_worker = pw;
     return pw * workers;
 }
