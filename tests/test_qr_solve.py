@@ -5,7 +5,7 @@ and against numpy's least squares (tall: no reference counterpart).
 
 Tolerances: normwise ||X - X_ref|| / ||X_ref|| <= 1e-10 (uniform random A, kappa ~ 1e3-1e4
 at these sizes, so 1e-10 leaves two orders of magnitude over kappa * u); residual norms of
-least squares <= 1e-10 relative; backward error ||A X - B|| / (||A|| ||X|| + ||B||) <= 1e-14."""
+least squares <= 1e-10 relative; backward error ||A X - B|| / (||A|| ||X|| + ||B||) <= 1e-13 (N = 8192)."""
 import numpy as np
 import pytest
 
@@ -141,7 +141,7 @@ def test_gpu_qr_solve_host_and_large_backward_error():
     A = da.view(mt, mt, nb, nb).permute(1, 3, 0, 2).reshape(n, n)
     X = dx.view(nrhs, n).t()
     res = torch.linalg.norm(A @ X - b) / (torch.linalg.norm(A) * torch.linalg.norm(X) + torch.linalg.norm(b))
-    assert float(res) < 1e-14
+    assert float(res) < 1e-13
     # host-buffer entry point gives the same X bit for bit (same DAG, same kernels)
     xh, _, _ = P.qr_solve_host(da.cpu().numpy(), n, n, nb, b.cpu().numpy())
     assert np.array_equal(xh, X.cpu().numpy())
