@@ -218,35 +218,37 @@ def time_update_kernel(P, torch, n: int) -> dict:
     return {"seconds": t, "flop": flop, "bytes": byts}
 
 
-def run_batched(args, P, torch) -> None:
+def run_batched(args, P, torch, rank: int = 0, world: int = 1) -> None:
     """configs[3]: 2000 matrices, N log-uniform in [32, 2048) (seed 2), half SPD Cholesky, half
     uniform LU, FP64, one persistent launch replayed from a CUDA graph; block size per size
-    class chosen by the autotuner."""
-    import numpy as np
+    class chosen by the autotuner.  With N > 1 ranks every rank factors its share of a
+    size-balanced partition (no collective on the data path; total work fixed: strong
+    scaling); the batch time is the max over ranks."""
     from palial_gb300 import batched as B
+    rep = B.synthetic(args.batch, seed=2, rank=rank, world=world, autotune=True, reps=max(3, args.steps))
+    t = rep["seconds"]
+    if world > 1:
+        import torch.distributed as dist
+        tt = torch.tensor([t], dtype=torch.float64, device="cuda")
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        t = float(tt.item())
+    if rank != 0:
+        return
     ns, algs = B.batch_sizes(args.batch, 2)
-    t0 = time.perf_counter()
-    choice, timings = B.autotune(torch, ns, algs)
-    tune_s = time.perf_counter() - t0
-    b = B.Batch(torch, ns, algs, choice, seed=2)
-    b.run(graph=True)
-    times = []
-    for _ in range(max(3, args.steps)):
-        b.reset()
-        st, comp = b.run(graph=True, completion=True)
-        times.append(st.seconds)
-    t = float(np.median(times))
+    total_flops = float(sum(n ** 3 / 3.0 if a == 0 else 2.0 * n ** 3 / 3.0 for n, a in zip(ns, algs)))
     per_class = {}
-    for c in sorted(set(B.size_class(int(n)) for n in ns)):
-        sel = np.array([B.size_class(int(n)) == c for n in ns])
-        per_class[B.class_label(c)] = {"count": int(sel.sum()), "block": int(choice[c]),
-                                       "p50_ms": float(np.percentile(comp[sel], 50) * 1e3),
-                                       "p99_ms": float(np.percentile(comp[sel], 99) * 1e3)}
-    print(json.dumps({"suite": "batched", "matrices": int(len(ns)), "precision": "fp64",
-                      "matrices_per_s": len(ns) / t, "batch_seconds": t, "tflops": b.flops / t * 1e-12,
-                      "launches_per_batch": 1, "cuda_graph": True, "autotune_seconds": tune_s,
-                      "autotune": {f"{B.class_label(c)} bs={bs}": v for (c, bs), v in timings.items()},
-                      "per_size_class": per_class}), flush=True)
+    for c in range(6):
+        if rep["count_of_class"][c]:
+            per_class[B.class_label(c)] = {"count": rep["count_of_class"][c], "block": rep["bs_of_class"][c],
+                                           "p50_ms": rep["p50_ms"][c], "p99_ms": rep["p99_ms"][c]}
+    print(json.dumps({"suite": "batched", "matrices": int(len(ns)), "precision": "fp64", "n_gpus": world,
+                      "scaling": "strong", "matrices_per_s": len(ns) / t, "batch_seconds": t,
+                      "tflops": total_flops / t * 1e-12, "launches_per_batch_per_rank": 1, "cuda_graph": True,
+                      "autotune_seconds": rep["autotune_seconds"],
+                      "autotune": {f"{B.class_label(c)} bs={bs}": rep["autotune_s"][c * 3 + j]
+                                   for c in range(6) for j, bs in enumerate(B.CANDIDATE_BS)
+                                   if rep["autotune_s"][c * 3 + j] >= 0},
+                      "per_size_class_rank0": per_class}), flush=True)
 
 
 def run_costmodel(args, P, torch) -> None:
@@ -396,6 +398,9 @@ def main() -> None:
         import torch.distributed as dist
         dist.init_process_group("nccl")
     P.init(local)
+    if args.suite == "batched":
+        run_batched(args, P, torch, rank, world)
+        return
     if args.suite:
         if rank == 0:
             run_suite(args, P, torch)

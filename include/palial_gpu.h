@@ -215,6 +215,37 @@ int palial_gpu_batched(int count, const int *algs, const int *ns, const int *nbs
 int palial_gpu_gen_batch_matrix(double *dA, int kind, int n_true, int n_pad, int nb, uint64_t seed,
                                 void *stream);
 
+/* ---- the synthetic uneven batch, its autotuner and its rank partition -----------------------
+ * Batch of `count` matrices: N_i = floor(32 * 64^u_i), u_i uniform in [0,1) (splitmix64 of
+ * seed, stream 6, index i), capped at 2047; alg_i = i % 2 (0 Cholesky on B B^T + N I, 1 LU on
+ * uniform [-1,1)).  Size classes [32,64) [64,128) [128,256) [256,512) [512,1024) [1024,2048). */
+typedef struct palial_batch_report {
+    int count;                /* matrices run by this rank                                   */
+    int bs_of_class[6];       /* block size used per size class                              */
+    int count_of_class[6];
+    double seconds;           /* median device time of one batched launch                   */
+    double matrices_per_s;
+    double tflops;            /* algorithmic flops / seconds                                 */
+    double p50_ms[6], p99_ms[6]; /* completion time from the launch, per size class        */
+    double autotune_seconds;
+    double autotune_s[18];    /* autotuner times [class][candidate 64,128,256], -1 = not run */
+} palial_batch_report;
+/* Host only: the sizes and algorithms of the synthetic batch. */
+int palial_gpu_batch_sizes(int count, uint64_t seed, int *ns, int *algs);
+/* Host only: size-balanced partition over `world` ranks (longest-processing-time first on the
+ * flop counts, deterministic): rank_of[i] = the rank that factors matrix i.  No collective is
+ * needed: every rank computes the same partition and factors its own matrices. */
+int palial_gpu_batch_partition(int count, const int *ns, const int *algs, int world, int *rank_of);
+/* Per size class, time the class's matrices alone with each candidate block size (64, 128,
+ * 256 where it fits the class) in a batched launch and keep the fastest. */
+int palial_gpu_batch_autotune(int count, const int *ns, const int *algs, uint64_t seed, int reps, int *bs_of_class,
+                              double *timings, palial_status *st);
+/* Generate this rank's share of the synthetic batch on the device, optionally autotune the
+ * block size per class (else bs_of_class, NULL = 64 below N = 512 and 128 above), run one
+ * warm-up and `reps` timed batched launches (CUDA graph replay), and fill the report. */
+int palial_gpu_batch_synthetic(int count, uint64_t seed, int rank, int world, int autotune, const int *bs_of_class,
+                               int reps, const palial_opts *opts, palial_status *st, palial_batch_report *rep);
+
 /* ---- generators (counter-based; the same bytes as the CPU oracle's generators) ------------ */
 /* uniform [-1,1): entry (i,j) from splitmix64 of seed/stream and i + j*rows.  Tile layout. */
 int palial_gpu_gen_uniform(double *dA, int n, int nb, uint64_t seed, void *stream);

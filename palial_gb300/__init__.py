@@ -121,6 +121,11 @@ def lib() -> ctypes.CDLL:
         h.palial_dag_qr_solve_validate.restype = ctypes.c_longlong
         h.palial_dag_qr_solve_validate.argtypes = [i, i, i, i, i, ctypes.c_uint, ctypes.POINTER(ctypes.c_longlong),
                                                    ctypes.c_char_p, i]
+        h.palial_gpu_batch_sizes.argtypes = [i, ctypes.c_uint64, vp, vp]
+        h.palial_gpu_batch_partition.argtypes = [i, vp, vp, i, vp]
+        h.palial_gpu_batch_autotune.argtypes = [i, vp, vp, ctypes.c_uint64, i, vp, vp, ctypes.POINTER(Status)]
+        h.palial_gpu_batch_synthetic.argtypes = [i, ctypes.c_uint64, i, i, i, vp, i, ctypes.POINTER(Opts),
+                                                 ctypes.POINTER(Status), vp]
         _lib = h
     return _lib
 

@@ -23,27 +23,40 @@ from . import PalialError, Status, lib, make_opts
 CLASS_EDGES = (32, 64, 128, 256, 512, 1024, 2048)
 CANDIDATE_BS = (64, 128, 256)
 
-_M1, _M2, _M3, _K1 = (np.uint64(0x9E3779B97F4A7C15), np.uint64(0xBF58476D1CE4E5B9),
-                      np.uint64(0x94D049BB133111EB), np.uint64(0xD1B54A32D192ED03))
+
+class BatchReport(ctypes.Structure):
+    _fields_ = [("count", ctypes.c_int), ("bs_of_class", ctypes.c_int * 6), ("count_of_class", ctypes.c_int * 6),
+                ("seconds", ctypes.c_double), ("matrices_per_s", ctypes.c_double), ("tflops", ctypes.c_double),
+                ("p50_ms", ctypes.c_double * 6), ("p99_ms", ctypes.c_double * 6),
+                ("autotune_seconds", ctypes.c_double), ("autotune_s", ctypes.c_double * 18)]
 
 
-def _mix(z):
-    with np.errstate(over="ignore"):
-        z = z + _M1
-        z = (z ^ (z >> np.uint64(30))) * _M2
-        z = (z ^ (z >> np.uint64(27))) * _M3
-        return z ^ (z >> np.uint64(31))
+def _ints(a) -> ctypes.Array:
+    a = [int(x) for x in a]
+    return (ctypes.c_int * max(1, len(a)))(*a)
 
 
 def batch_sizes(count: int = 2000, seed: int = 2) -> tuple[np.ndarray, np.ndarray]:
-    """(N_i, alg_i): N log-uniform in [32, 2048), alg 0 (Cholesky, SPD) for even i, 1 (LU)."""
-    with np.errstate(over="ignore"):
-        key = _mix(np.array([np.uint64(seed) * _K1 + np.uint64(6)], dtype=np.uint64))[0]
-        r = _mix(key + np.arange(count, dtype=np.uint64))
-    u = (r >> np.uint64(11)).astype(np.float64) * 2.0 ** -53
-    ns = np.minimum(np.floor(32.0 * 64.0 ** u).astype(np.int64), 2047)
-    algs = (np.arange(count) % 2).astype(np.int64)
-    return ns, algs
+    """(N_i, alg_i) of the synthetic batch (the library's generator): N log-uniform in
+    [32, 2048), alg 0 (Cholesky, SPD) for even i, 1 (LU) for odd i."""
+    ns = (ctypes.c_int * max(1, count))()
+    algs = (ctypes.c_int * max(1, count))()
+    _check_rc(lib().palial_gpu_batch_sizes(count, ctypes.c_uint64(seed), ns, algs))
+    return np.array(ns[:count], dtype=np.int64), np.array(algs[:count], dtype=np.int64)
+
+
+def partition(ns, algs, world: int) -> np.ndarray:
+    """Size-balanced owner rank of every matrix (the library's LPT partition; identical on
+    every rank, so sharding a batch needs no collective)."""
+    count = len(ns)
+    out = (ctypes.c_int * max(1, count))()
+    _check_rc(lib().palial_gpu_batch_partition(count, _ints(ns), _ints(algs), world, out))
+    return np.array(out[:count], dtype=np.int64)
+
+
+def _check_rc(rc: int) -> None:
+    if rc:
+        raise PalialError(rc, "batch call failed")
 
 
 def size_class(n: int) -> int:
@@ -64,9 +77,11 @@ def padded(n: int, bs: int) -> int:
 class Batch:
     """Device buffers of one batch (torch provides the memory) and its launch arguments."""
 
-    def __init__(self, torch, ns, algs, bs_of_class: dict, seed: int = 2, index_base: int = 0):
+    def __init__(self, torch, ns, algs, bs_of_class: dict, seed: int = 2, index_base: int = 0, indices=None):
         self.torch = torch
         self.ns = np.asarray(ns, dtype=np.int64)
+        # batch index of every matrix (its generator seed): index_base + i unless given
+        self.indices = (np.arange(len(self.ns)) + index_base) if indices is None else np.asarray(indices)
         self.algs = np.asarray(algs, dtype=np.int64)
         self.count = len(self.ns)
         self.bs = np.array([bs_of_class[size_class(int(n))] for n in self.ns], dtype=np.int32)
@@ -79,8 +94,8 @@ class Batch:
         self.offs = offs
         for i in range(self.count):
             rc = lib().palial_gpu_gen_batch_matrix(self.ptrs[i], 1 if self.algs[i] == 0 else 0, int(self.ns[i]),
-                                                   int(self.np_[i]), int(self.bs[i]), seed * 100000 + index_base + i,
-                                                   None)
+                                                   int(self.np_[i]), int(self.bs[i]),
+                                                   seed * 100000 + int(self.indices[i]), None)
             if rc:
                 raise PalialError(rc, f"generating matrix {i}")
         torch.cuda.synchronize()
@@ -120,30 +135,39 @@ class Batch:
 
 
 def autotune(torch, ns, algs, candidates=CANDIDATE_BS, reps: int = 2, seed: int = 2) -> tuple[dict, dict]:
-    """Per size class, time the class's matrices alone with each candidate block size (one
-    launch per repetition after a warm-up) and keep the fastest.  Returns (choice, timings)."""
+    """Per size class, the fastest candidate block size (the library's autotuner: each class's
+    matrices alone in a batched launch per candidate).  Returns (choice, timings) with
+    choice[class] = block size and timings[(class, bs)] = seconds.  `torch` and `candidates`
+    are accepted for the older signature; the candidates are 64, 128, 256."""
+    del torch, candidates
     ns = np.asarray(ns)
     algs = np.asarray(algs)
-    classes = sorted({size_class(int(n)) for n in ns})
-    choice, timings = {}, {}
-    for c in classes:
-        idx = [i for i in range(len(ns)) if size_class(int(ns[i])) == c]
-        best = None
-        for bs in candidates:
-            if bs > max(64, CLASS_EDGES[c + 1]):
-                continue
-            b = Batch(torch, ns[idx], algs[idx], {c: bs}, seed=seed, index_base=idx[0])
-            times = []
-            for r in range(reps + 1):
-                b.reset()
-                st, _ = b.run(graph=True)
-                if r > 0:
-                    times.append(st.seconds)
-            t = min(times)
-            timings[(c, bs)] = t
-            if best is None or t < best[1]:
-                best = (bs, t)
-            del b
-            torch.cuda.empty_cache()
-        choice[c] = best[0]
+    cls = (ctypes.c_int * 6)()
+    tim = (ctypes.c_double * 18)()
+    st = Status()
+    rc = lib().palial_gpu_batch_autotune(len(ns), _ints(ns), _ints(algs), ctypes.c_uint64(seed), reps, cls, tim,
+                                         ctypes.byref(st))
+    if rc:
+        raise PalialError(rc, st.message.decode(errors="replace"))
+    present = sorted({size_class(int(n)) for n in ns})
+    choice = {c: int(cls[c]) for c in present}
+    timings = {(c, bs): float(tim[c * 3 + j]) for c in present for j, bs in enumerate(CANDIDATE_BS)
+               if tim[c * 3 + j] >= 0}
     return choice, timings
+
+
+def synthetic(count: int = 2000, seed: int = 2, rank: int = 0, world: int = 1, autotune: bool = True,
+              bs_of_class=None, reps: int = 3) -> dict:
+    """Run this rank's share of the synthetic batch entirely inside the library; returns the
+    report as a dict."""
+    rep = BatchReport()
+    st = Status()
+    cls = (ctypes.c_int * 6)(*bs_of_class) if bs_of_class is not None else None
+    rc = lib().palial_gpu_batch_synthetic(count, ctypes.c_uint64(seed), rank, world, int(autotune), cls, reps,
+                                          ctypes.byref(make_opts()), ctypes.byref(st), ctypes.byref(rep))
+    if rc:
+        raise PalialError(rc, st.message.decode(errors="replace"))
+    out = {f: getattr(rep, f) for f, _ in BatchReport._fields_}
+    for f in ("bs_of_class", "count_of_class", "p50_ms", "p99_ms", "autotune_s"):
+        out[f] = list(out[f])
+    return out

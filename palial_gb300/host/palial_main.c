@@ -14,16 +14,30 @@
  *
  * Long options:
  *   --gen ref|spd|uniform   input: the reference's pattern (default), B B^T + N I, U[-1,1)
- *   --seed S                generator seed (default 0)
+ *   --seed S                generator seed (default 0; 2 for --batch)
  *   --block BS              scheduler block size (divides NB, multiple of 64)
  *   --priority 0|1          critical-path list order (default) or program order
  *   --trace FILE            write the per-task trace in the reference's "name, ms" format
  *   --trace-csv FILE        side-car CSV with start/end ns and SM id per task record
  *   --check                 report the normwise residual (random probes, on the GPU)
+ *   --clocks                add the GPU clock report (NVML samples, device clock estimate)
  *   --quiet                 no JSON line
+ * Solve mode (A X = B with K seeded uniform right-hand sides instead of the bare factorization):
+ *   --rhs K                 K right-hand sides (Cholesky/LU: 1..16, QR: 1..NB)
+ *   --precision P           fp64 | bf16 | fp8 | bf16x3 | auto: trailing-update precision of the
+ *                           Cholesky/LU factorization, refined to FP64 accuracy (QR: fp64 only);
+ *                           any precision other than fp64 implies --rhs 1 when --rhs is absent
+ *   --ir-tol T, --ir-max N  refinement target backward error and iteration cap
+ *   --gmres -1|0|1          GMRES-IR never / automatic / always
+ * Batch mode (no -a/-m/-b needed):
+ *   --batch COUNT           the synthetic uneven batch: COUNT matrices, N log-uniform in
+ *                           [32, 2048), half Cholesky half LU, one persistent launch
+ *   --autotune              choose the block size per size class by timing (batch mode)
  */
 #define _GNU_SOURCE
 #include <getopt.h>
+#include <math.h>
+#include <stdint.h>
 #include <stdio.h>
 #include <stdlib.h>
 #include <string.h>
@@ -41,21 +55,87 @@ static int parse_gen(const char *s)
     return 2;
 }
 
+static int parse_precision(const char *s)
+{
+    static const char *names[] = {"fp64", "bf16", "fp8", "bf16x3", "auto"};
+    for (int i = 0; i < 5; i++)
+        if (!strcmp(s, names[i])) return i;
+    return -1;
+}
+
+static const char *precision_name(int p)
+{
+    static const char *names[] = {"fp64", "bf16", "fp8", "bf16x3", "auto"};
+    return p >= 0 && p < 5 ? names[p] : "?";
+}
+
+/* uniform [-1, 1) right-hand sides from splitmix64 (seed, index) */
+static uint64_t splitmix(uint64_t z)
+{
+    z += 0x9E3779B97F4A7C15ull;
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    return z ^ (z >> 31);
+}
+
+static void print_clocks(void)
+{
+    palial_clock_report c;
+    if (palial_gpu_clock_report(&c) == PALIAL_OK)
+        printf(", \"clocks\": {\"sm_mhz_start\": %.0f, \"sm_mhz_end\": %.0f, \"sm_mhz_max\": %.0f, "
+               "\"sm_mhz_device\": %.0f, \"reasons\": %d}",
+               c.sm_mhz_start, c.sm_mhz_end, c.sm_mhz_max, c.sm_mhz_device, c.throttle_reasons);
+}
+
+static int run_batch(int count, unsigned long long seed, int autotune, int quiet)
+{
+    palial_batch_report rep;
+    palial_status st;
+    int rc = palial_gpu_batch_synthetic(count, seed, 0, 1, autotune, NULL, 3, &palial_entry_opts, &st, &rep);
+    if (rc) {
+        fprintf(stderr, "palial: batch failed: %s (%s)\n", palial_gpu_error_string(rc), st.message);
+        return 1;
+    }
+    if (!quiet) {
+        printf("{\"batch\": %d, \"seed\": %llu, \"autotune\": %d, \"seconds\": %.6f, \"matrices_per_s\": %.1f, "
+               "\"tflops\": %.4f, \"classes\": [",
+               rep.count, seed, autotune, rep.seconds, rep.matrices_per_s, rep.tflops);
+        static const int edges[7] = {32, 64, 128, 256, 512, 1024, 2048};
+        int first = 1;
+        for (int c = 0; c < 6; c++) {
+            if (!rep.count_of_class[c]) continue;
+            printf("%s{\"n\": [%d, %d], \"count\": %d, \"block\": %d, \"p50_ms\": %.3f, \"p99_ms\": %.3f}",
+                   first ? "" : ", ", edges[c], edges[c + 1], rep.count_of_class[c], rep.bs_of_class[c],
+                   rep.p50_ms[c], rep.p99_ms[c]);
+            first = 0;
+        }
+        printf("]}\n");
+    }
+    return 0;
+}
+
 int main(int argc, char *argv[])
 {
     char algorithm[16] = "";
-    int gen = 2, check = 0, quiet = 0;
+    int gen = 2, check = 0, quiet = 0, nrhs = 0, batch = 0, autotune = 0, clocks = 0, seed_given = 0;
     unsigned long long seed = 0;
     const char *trace = NULL, *trace_csv = NULL;
     palial_opts_default(&palial_entry_opts);
-    enum { O_GEN = 1000, O_SEED, O_BLOCK, O_PRIO, O_TRACE, O_TRACECSV, O_CHECK, O_QUIET };
+    enum {
+        O_GEN = 1000, O_SEED, O_BLOCK, O_PRIO, O_TRACE, O_TRACECSV, O_CHECK, O_QUIET, O_PREC, O_RHS, O_IRTOL,
+        O_IRMAX, O_GMRES, O_BATCH, O_AUTOTUNE, O_CLOCKS
+    };
     struct option long_options[] = {
         {"Algorithm", required_argument, NULL, 'a'}, {"Matrix size", required_argument, NULL, 'm'},
         {"Tile size", required_argument, NULL, 'b'}, {"gen", required_argument, NULL, O_GEN},
         {"seed", required_argument, NULL, O_SEED},   {"block", required_argument, NULL, O_BLOCK},
         {"priority", required_argument, NULL, O_PRIO}, {"trace", required_argument, NULL, O_TRACE},
         {"trace-csv", required_argument, NULL, O_TRACECSV}, {"check", no_argument, NULL, O_CHECK},
-        {"quiet", no_argument, NULL, O_QUIET},       {NULL, no_argument, NULL, 0}};
+        {"quiet", no_argument, NULL, O_QUIET},       {"precision", required_argument, NULL, O_PREC},
+        {"rhs", required_argument, NULL, O_RHS},     {"ir-tol", required_argument, NULL, O_IRTOL},
+        {"ir-max", required_argument, NULL, O_IRMAX}, {"gmres", required_argument, NULL, O_GMRES},
+        {"batch", required_argument, NULL, O_BATCH}, {"autotune", no_argument, NULL, O_AUTOTUNE},
+        {"clocks", no_argument, NULL, O_CLOCKS},     {NULL, no_argument, NULL, 0}};
     if (argc < 2) {
         printf("Missing arguments.\n");
         printf("Aborting...\n");
@@ -69,18 +149,38 @@ int main(int argc, char *argv[])
             case 'b': BSIZE = atoi(optarg); break;
             case 'h': printf("HELP\n"); return 0;
             case O_GEN: gen = parse_gen(optarg); break;
-            case O_SEED: seed = strtoull(optarg, NULL, 10); break;
+            case O_SEED: seed = strtoull(optarg, NULL, 10); seed_given = 1; break;
             case O_BLOCK: palial_entry_opts.block = atoi(optarg); break;
             case O_PRIO: palial_entry_opts.priority = atoi(optarg); break;
             case O_TRACE: trace = optarg; palial_entry_opts.trace = 1; break;
             case O_TRACECSV: trace_csv = optarg; palial_entry_opts.trace = 1; break;
             case O_CHECK: check = 1; break;
             case O_QUIET: quiet = 1; break;
+            case O_PREC:
+                palial_entry_opts.precision = parse_precision(optarg);
+                if (palial_entry_opts.precision < 0) {
+                    printf("Invalid arguments.\n");
+                    printf("Aborting...\n");
+                    return 0;
+                }
+                break;
+            case O_RHS: nrhs = atoi(optarg); break;
+            case O_IRTOL: palial_entry_opts.ir_tol = atof(optarg); break;
+            case O_IRMAX: palial_entry_opts.ir_max_iter = atoi(optarg); break;
+            case O_GMRES: palial_entry_opts.gmres = atoi(optarg); break;
+            case O_BATCH: batch = atoi(optarg); break;
+            case O_AUTOTUNE: autotune = 1; break;
+            case O_CLOCKS: clocks = 1; palial_entry_opts.trace = 1; break;
             default:
                 printf("Invalid arguments.\n");
                 printf("Aborting...\n");
                 return 0;
         }
+    }
+    if (batch > 0) {
+        const int rc = run_batch(batch, seed_given ? seed : 2, autotune, quiet);
+        palial_gpu_finalize();
+        return rc;
     }
     if (BSIZE <= 0 || MSIZE <= 0 || MSIZE % BSIZE != 0) {
         printf("Tile size does not divide the matrix size. Aborting...\n");
@@ -88,6 +188,13 @@ int main(int argc, char *argv[])
     }
     if (strcmp(algorithm, "cholesky") && strcmp(algorithm, "lu") && strcmp(algorithm, "qr")) {
         /* the reference silently does nothing for an unknown algorithm */
+        return 0;
+    }
+    const int alg = !strcmp(algorithm, "cholesky") ? 0 : !strcmp(algorithm, "lu") ? 1 : 2;
+    if (palial_entry_opts.precision != PALIAL_PREC_FP64 && nrhs <= 0) nrhs = 1;
+    if (nrhs > 0 && ((alg != 2 && nrhs > 16) || (alg == 2 && (nrhs > BSIZE || palial_entry_opts.precision)))) {
+        printf("Invalid arguments.\n");
+        printf("Aborting...\n");
         return 0;
     }
     const size_t bytes = (size_t)MSIZE * MSIZE * sizeof(double);
@@ -103,6 +210,40 @@ int main(int argc, char *argv[])
         fprintf(stderr, "palial: input generation failed: %s\n", palial_gpu_error_string(rc));
         free(ptr);
         return 1;
+    }
+    if (nrhs > 0) {
+        /* solve mode: A X = B, X refined to FP64 accuracy (Cholesky/LU) or by the tile QR */
+        double *B = (double *)malloc(sizeof(double) * (size_t)MSIZE * nrhs);
+        double *X = (double *)calloc((size_t)MSIZE * nrhs, sizeof(double));
+        if (!B || !X) {
+            printf("Problem allocating contiguous memory.\n");
+            return EXIT_FAILURE;
+        }
+        const uint64_t key = splitmix(seed * 0xD1B54A32D192ED03ull + 2ull);
+        for (size_t i = 0; i < (size_t)MSIZE * nrhs; i++)
+            B[i] = (double)(splitmix(key + i) >> 11) * 0x1.0p-52 - 1.0;
+        palial_status st;
+        if (alg == 2)
+            rc = palial_gpu_qr_solve_host(MSIZE, MSIZE, BSIZE, ptr, B, X, nrhs, NULL, &palial_entry_opts, &st);
+        else
+            rc = palial_gpu_solve_ir_host(alg, (const palial_desc *)&A, B, X, nrhs, &palial_entry_opts, &st);
+        if (rc < 0) fprintf(stderr, "palial: solve failed: %s (%s)\n", palial_gpu_error_string(rc), st.message);
+        if (!quiet) {
+            printf("{\"algorithm\": \"%s\", \"mode\": \"solve\", \"n\": %d, \"nb\": %d, \"nrhs\": %d, "
+                   "\"precision\": \"%s\", \"code\": %d, \"seconds\": %.6f, \"total_seconds\": %.6f, "
+                   "\"tflops\": %.4f, \"ir_iters\": %d, \"gmres_iters\": %d, \"backward_error\": %.3e, "
+                   "\"factor_seconds\": %.6f, \"tasks\": %lld",
+                   algorithm, MSIZE, BSIZE, nrhs, precision_name(palial_entry_opts.precision), rc, st.seconds,
+                   st.total_seconds, st.tflops, st.ir_iters, st.gmres_iters, st.backward_error, st.factor_seconds,
+                   st.ntasks);
+            if (clocks) print_clocks();
+            printf("}\n");
+        }
+        free(B);
+        free(X);
+        free(ptr);
+        palial_gpu_finalize();
+        return rc < 0 ? 1 : 0;
     }
     double *orig = NULL;
     if (check) {
@@ -125,17 +266,17 @@ int main(int argc, char *argv[])
     }
     const palial_status st = palial_entry_status;
     double resid = -1.0;
-    if (check && orig && st.code >= 0) {
-        const int alg = !strcmp(algorithm, "cholesky") ? 0 : !strcmp(algorithm, "lu") ? 1 : 2;
-        palial_gpu_residual_host(alg, orig, (const palial_desc *)&A, 8, 7, &resid);
-    }
+    if (check && orig && st.code >= 0) palial_gpu_residual_host(alg, orig, (const palial_desc *)&A, 8, 7, &resid);
     if (trace && st.code >= 0) palial_gpu_trace_dump(trace, trace_csv);
     else if (trace_csv && st.code >= 0) palial_gpu_trace_dump("/dev/null", trace_csv);
-    if (!quiet)
+    if (!quiet) {
         printf("{\"algorithm\": \"%s\", \"n\": %d, \"nb\": %d, \"block\": %d, \"code\": %d, \"seconds\": %.6f, "
-               "\"total_seconds\": %.6f, \"tflops\": %.4f, \"tasks\": %lld, \"residual_probe\": %.3e}\n",
+               "\"total_seconds\": %.6f, \"tflops\": %.4f, \"tasks\": %lld, \"residual_probe\": %.3e",
                algorithm, MSIZE, BSIZE, palial_entry_opts.block, st.code, st.seconds, st.total_seconds, st.tflops,
                st.ntasks, resid);
+        if (clocks) print_clocks();
+        printf("}\n");
+    }
     free(orig);
     free(S.matrix);
     free(ptr);

@@ -41,3 +41,24 @@ def test_graph_replay_bitwise_equal():
         st, _ = b.run(graph=True)
         assert torch.equal(b.buf, direct)
     assert st.seconds > 0
+
+
+def test_library_synthetic_batch_split_over_two_ranks():
+    """The library's synthetic batch driver: the two ranks' shares cover the batch, and every
+    share runs and reports per-class completion times."""
+    reps = [B.synthetic(64, seed=5, rank=r, world=2, autotune=False, reps=1) for r in range(2)]
+    assert sum(r["count"] for r in reps) == 64
+    for r in reps:
+        assert r["seconds"] > 0 and r["matrices_per_s"] > 0
+        assert sum(r["count_of_class"]) == r["count"]
+        for c in range(6):
+            if r["count_of_class"][c]:
+                assert 0 < r["p50_ms"][c] <= r["p99_ms"][c] <= r["seconds"] * 1e3 * 1.01
+
+
+def test_library_autotune_picks_a_candidate():
+    ns, algs = B.batch_sizes(40, 6)
+    choice, timings = B.autotune(torch, ns, algs, reps=1, seed=6)
+    for c, bs in choice.items():
+        assert bs in B.CANDIDATE_BS and bs <= max(64, B.CLASS_EDGES[c + 1])
+        assert timings[(c, bs)] == min(t for (cc, _), t in timings.items() if cc == c)
