@@ -1,0 +1,288 @@
+// mp_diag.cu -- FP32 factorization of one diagonal tile of the mixed-precision path, in one
+// CTA, in place on the FP32 working copy.
+//
+// The mixed-precision factorization keeps its working copy in FP32 and its trailing updates in
+// BF16/FP8, so the diagonal tiles need FP32 accuracy, not FP64; and FP32 runs 64 times faster
+// per SM than FP64 on this part.  The tile (nb x nb, column-major, ld = nb, nb a multiple of
+// 64 up to 1024) is factored right-looking in 64-column steps:
+//   1. the 64 x 64 diagonal block in shared memory (Cholesky: U^T U, upper; LU: no pivoting
+//      with the reference's pivot rule, src/srclu/dgetrf_no_pivot.h:11-57: scale by the
+//      reciprocal when |pivot| > FLT_MIN, divide otherwise, skip an exact zero);
+//   2. the panel(s) by substitution, one thread per column (or row), the 64 unknowns in
+//      registers: Cholesky U12 = U11^-T A12; LU U12 = L11^-1 A12 and L21 = A21 U11^-1;
+//   3. the trailing block by a register-tiled (8 x 8 per thread) product from panel chunks
+//      staged in shared memory: Cholesky A22 -= U12^T U12 (upper triangle only), LU
+//      A22 -= L21 U12.
+// Errors go to the status words of the factorization: a non-positive Cholesky pivot records
+// PALIAL_ERR_NOT_SPD with the step and column; an exact zero LU pivot sets the zero-pivot
+// flag.  A CTA that finds an error already recorded does nothing.
+#include <cuda_runtime.h>
+
+#include <cfloat>
+
+#include "common.cuh"
+
+namespace palial {
+namespace mpd {
+
+constexpr int NT = 512;   // threads
+constexpr int DP = 65;    // padded leading dimension of the 64 x 64 block in shared memory
+constexpr int MT = 8;     // micro-tile edge
+
+__host__ __device__ constexpr int chunk_k(int nb) { return nb <= 512 ? 32 : 16; }
+// shared memory (floats): Ds[64][65] + two staged chunks of chunk_k x (nb - 64)
+__host__ __device__ constexpr int smem_floats(int nb) { return 64 * DP + 2 * chunk_k(nb) * (nb - 64) + 64; }
+
+// ---- 64 x 64 diagonal block in shared memory ---------------------------------------------
+// Ds[c][r] = A(r, c).  Returns the first failing column (Cholesky) or -1.
+__device__ int chol64(float (*Ds)[DP], int *sflag) {
+    for (int p = 0; p < 64; p++) {
+        const float d = Ds[p][p];
+        if (!(d > 0.f)) {
+            // every thread reads the same pivot: the decision is uniform
+            return p;
+        }
+        const float r = sqrtf(d);
+        for (int q = p + 1 + threadIdx.x; q < 64; q += NT) Ds[q][p] = Ds[q][p] / r;
+        __syncthreads();
+        if (threadIdx.x == 0) Ds[p][p] = r;
+        const int w = 63 - p;  // trailing (i, q), p < i <= q
+        for (int e = threadIdx.x; e < w * w; e += NT) {
+            const int i = p + 1 + e % w, q = p + 1 + e / w;
+            if (i <= q) Ds[q][i] = fmaf(-Ds[i][p], Ds[q][p], Ds[q][i]);
+        }
+        __syncthreads();
+    }
+    (void)sflag;
+    return -1;
+}
+
+// No-pivot LU of the block; returns 1 if an exact zero pivot was skipped.
+__device__ int getrf64(float (*Ds)[DP]) {
+    int zero = 0;
+    for (int p = 0; p < 64; p++) {
+        const float piv = Ds[p][p];
+        if (piv != 0.f) {
+            const bool recip = fabsf(piv) > FLT_MIN;
+            const float rp = 1.f / piv;
+            for (int i = p + 1 + threadIdx.x; i < 64; i += NT) Ds[p][i] = recip ? Ds[p][i] * rp : Ds[p][i] / piv;
+        } else {
+            zero = 1;
+        }
+        __syncthreads();
+        const int w = 63 - p;
+        for (int e = threadIdx.x; e < w * w; e += NT) {
+            const int i = p + 1 + e % w, q = p + 1 + e / w;
+            Ds[q][i] = fmaf(-Ds[p][i], Ds[q][p], Ds[q][i]);
+        }
+        __syncthreads();
+    }
+    return zero;
+}
+
+// ---- panels by substitution ----------------------------------------------------------------
+// One vector of 64 entries (b[i * stride], i < 64), solved in place against the block in Ds,
+// in two halves of 32 unknowns kept in registers:
+//   KIND 0: U^T x = b (U upper, non-unit): coefficient of x_p in row u is U(p,u) = Ds[u][p]
+//   KIND 1: L x = b (L unit lower):           coefficient L(u,p) = Ds[p][u]
+//   KIND 2: x U = b (row vector, U upper):    coefficient U(p,u) = Ds[u][p], the reference's
+//           pivot rule on the division (reciprocal when |u_uu| > FLT_MIN, zero skipped)
+template <int KIND>
+__device__ __forceinline__ float coef(const float (*Ds)[DP], int u, int p) {
+    return KIND == 1 ? Ds[p][u] : Ds[u][p];
+}
+template <int KIND>
+__device__ __forceinline__ float finish(const float (*Ds)[DP], int u, float s) {
+    if (KIND == 1) return s;
+    const float d = Ds[u][u];
+    if (KIND == 0) return s / d;
+    return d == 0.f ? s : (fabsf(d) > FLT_MIN ? s * (1.f / d) : s / d);
+}
+template <int KIND>
+__device__ void solve_vec(const float (*Ds)[DP], float *b, size_t stride) {
+#pragma unroll 1
+    for (int h = 0; h < 64; h += 32) {
+        float x[32];
+#pragma unroll
+        for (int i = 0; i < 32; i++) x[i] = b[(size_t)(h + i) * stride];
+        if (h) {
+            // contributions of the solved first half
+#pragma unroll 4
+            for (int p = 0; p < 32; p++) {
+                const float xp = b[(size_t)p * stride];
+#pragma unroll
+                for (int i = 0; i < 32; i++) x[i] = fmaf(-coef<KIND>(Ds, 32 + i, p), xp, x[i]);
+            }
+        }
+#pragma unroll
+        for (int i = 0; i < 32; i++) {
+            float acc = x[i];
+#pragma unroll
+            for (int p = 0; p < i; p++) acc = fmaf(-coef<KIND>(Ds, h + i, h + p), x[p], acc);
+            x[i] = finish<KIND>(Ds, h + i, acc);
+        }
+#pragma unroll
+        for (int i = 0; i < 32; i++) b[(size_t)(h + i) * stride] = x[i];
+    }
+}
+
+// ---- trailing update -----------------------------------------------------------------------
+// C (m x m at C, ld) -= A^T B where A, B are KC x m chunks As[kk][i], Bs[kk][j] in shared
+// memory, accumulated over all 64 rows of the panel in chunks staged by `stage`.
+// UPPER: only micro-tiles with bj >= bi, and inside diagonal micro-tiles only i <= j.
+template <bool UPPER, class Stage>
+__device__ void trailing(float *C, int ld, int m, int kc, float *As, float *Bs, Stage stage) {
+    const int mb = m / MT;
+    const int tiles = UPPER ? mb * (mb + 1) / 2 : mb * mb;  // UPPER: micro-tiles with bj >= bi
+    for (int base = 0; base < tiles; base += NT) {
+        const int u = base + threadIdx.x;
+        int bi = 0, bj = 0;
+        if (UPPER) {
+            int rem = u;
+            while (bi < mb && rem >= mb - bi) {
+                rem -= mb - bi;
+                bi++;
+            }
+            bj = bi + rem;
+        } else {
+            bi = u / mb;
+            bj = u % mb;
+        }
+        const bool active = u < tiles;
+        float acc[MT][MT];
+#pragma unroll
+        for (int i = 0; i < MT; i++)
+#pragma unroll
+            for (int j = 0; j < MT; j++) acc[i][j] = 0.f;
+        for (int k0 = 0; k0 < 64; k0 += kc) {
+            __syncthreads();
+            stage(k0);
+            __syncthreads();
+            if (active) {
+                for (int kk = 0; kk < kc; kk++) {
+                    const float4 a0 = *reinterpret_cast<const float4 *>(As + (size_t)kk * m + bi * MT);
+                    const float4 a1 = *reinterpret_cast<const float4 *>(As + (size_t)kk * m + bi * MT + 4);
+                    const float4 b0 = *reinterpret_cast<const float4 *>(Bs + (size_t)kk * m + bj * MT);
+                    const float4 b1 = *reinterpret_cast<const float4 *>(Bs + (size_t)kk * m + bj * MT + 4);
+                    const float a[MT] = {a0.x, a0.y, a0.z, a0.w, a1.x, a1.y, a1.z, a1.w};
+                    const float b[MT] = {b0.x, b0.y, b0.z, b0.w, b1.x, b1.y, b1.z, b1.w};
+#pragma unroll
+                    for (int i = 0; i < MT; i++)
+#pragma unroll
+                        for (int j = 0; j < MT; j++) acc[i][j] = fmaf(a[i], b[j], acc[i][j]);
+                }
+            }
+        }
+        if (active) {
+#pragma unroll
+            for (int j = 0; j < MT; j++)
+#pragma unroll
+                for (int i = 0; i < MT; i++) {
+                    const int r = bi * MT + i, c = bj * MT + j;
+                    if (!UPPER || r <= c) {
+                        float *x = C + r + (size_t)c * ld;
+                        *x -= acc[i][j];
+                    }
+                }
+        }
+    }
+}
+
+// status: int[8] of the factorization (ST_CODE, ..., [6] = step)
+template <int ALG>
+__global__ void __launch_bounds__(NT, 1) diag_factor_kernel(float *T, int nb, int k, int *status) {
+    extern __shared__ __align__(16) float smem[];
+    float (*Ds)[DP] = reinterpret_cast<float (*)[DP]>(smem);
+    const int kc = chunk_k(nb);
+    float *As = smem + 64 * DP;
+    float *Bs = As + (size_t)kc * (nb - 64);
+    if (ld_volatile(status + ST_CODE) != 0) return;
+    if (threadIdx.x == 0) status[6] = k;  // current step (error reports of later kernels)
+    int zero = 0;
+    for (int j0 = 0; j0 < nb; j0 += 64) {
+        float *D = T + j0 + (size_t)j0 * nb;
+        for (int e = threadIdx.x; e < 4096; e += NT) Ds[e >> 6][e & 63] = D[(e & 63) + (size_t)(e >> 6) * nb];
+        __syncthreads();
+        if (ALG == 0) {
+            const int bad = chol64(Ds, nullptr);
+            if (bad >= 0) {
+                if (threadIdx.x == 0 && atomicCAS(status + ST_CODE, 0, -3 /*PALIAL_ERR_NOT_SPD*/) == 0) {
+                    status[ST_COL] = j0 + bad;
+                    status[ST_M] = status[ST_N] = k;
+                    status[6] = k;
+                    __threadfence();
+                }
+                return;
+            }
+        } else {
+            zero |= getrf64(Ds);
+        }
+        for (int e = threadIdx.x; e < 4096; e += NT) {
+            const int r = e & 63, c = e >> 6;
+            if (ALG == 1 || r <= c) D[r + (size_t)c * nb] = Ds[c][r];
+        }
+        const int m = nb - j0 - 64;
+        if (m == 0) break;
+        __syncthreads();
+        // panels
+        float *A12 = T + j0 + (size_t)(j0 + 64) * nb;  // 64 x m, columns at stride nb
+        for (int c = threadIdx.x; c < m; c += NT) {
+            if (ALG == 0) solve_vec<0>(Ds, A12 + (size_t)c * nb, 1);
+            else solve_vec<1>(Ds, A12 + (size_t)c * nb, 1);
+        }
+        if (ALG == 1) {
+            float *A21 = T + (j0 + 64) + (size_t)j0 * nb;  // m x 64, rows contiguous
+            for (int r = threadIdx.x; r < m; r += NT) solve_vec<2>(Ds, A21 + r, nb);
+        }
+        __syncthreads();
+        float *C = T + (j0 + 64) + (size_t)(j0 + 64) * nb;
+        if (ALG == 0) {
+            // As[kk][i] = U12(k0 + kk, i): contiguous in kk in global memory
+            auto stage = [&](int k0) {
+                for (int e = threadIdx.x; e < kc * m; e += NT) {
+                    const int kk = e % kc, i = e / kc;
+                    As[(size_t)kk * m + i] = A12[(k0 + kk) + (size_t)i * nb];
+                }
+            };
+            trailing<true>(C, nb, m, kc, As, As, stage);
+        } else {
+            const float *A21 = T + (j0 + 64) + (size_t)j0 * nb;
+            auto stage = [&](int k0) {
+                for (int e = threadIdx.x; e < kc * m; e += NT) {
+                    const int i = e % m, kk = e / m;  // L21(i, k0+kk): contiguous in i
+                    As[(size_t)kk * m + i] = A21[i + (size_t)(k0 + kk) * nb];
+                }
+                for (int e = threadIdx.x; e < kc * m; e += NT) {
+                    const int kk = e % kc, j = e / kc;  // U12(k0+kk, j): contiguous in kk
+                    Bs[(size_t)kk * m + j] = A12[(k0 + kk) + (size_t)j * nb];
+                }
+            };
+            trailing<false>(C, nb, m, kc, As, Bs, stage);
+        }
+        __syncthreads();
+    }
+    if (ALG == 1 && zero && threadIdx.x == 0) atomicOr(status + ST_ZEROPIV, 1);
+}
+
+}  // namespace mpd
+
+cudaError_t mpd_configure() {
+    const int bytes = mpd::smem_floats(1024) * 4;
+    cudaError_t e = cudaFuncSetAttribute(mpd::diag_factor_kernel<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    if (e != cudaSuccess) return e;
+    return cudaFuncSetAttribute(mpd::diag_factor_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+}
+
+// Factor diagonal tile k of the FP32 tile matrix W (n x n, tile nb) in place.
+cudaError_t mpd_factor_tile(int alg, float *W, int n, int nb, int k, int *status, cudaStream_t s) {
+    if (nb % 64 || nb > 1024) return cudaErrorInvalidValue;
+    const int mt = n / nb;
+    float *T = W + (size_t)nb * nb * ((size_t)k + (size_t)mt * k);
+    const int bytes = mpd::smem_floats(nb) * 4;
+    note_launch();
+    if (alg == 0) mpd::diag_factor_kernel<0><<<1, mpd::NT, bytes, s>>>(T, nb, k, status);
+    else mpd::diag_factor_kernel<1><<<1, mpd::NT, bytes, s>>>(T, nb, k, status);
+    return cudaGetLastError();
+}
+
+}  // namespace palial

@@ -2,9 +2,9 @@
 //
 // Factorization (right-looking, one k step at a time on one stream), on an FP32 working
 // copy W of A in the reference's tile layout:
-//   1. the diagonal tile W(k,k) is factored in FP64 by the persistent FP64 scheduler
-//      (64-wide blocks, many CTAs): POTRF for Cholesky, the reference's no-pivot GETRF for LU;
-//   2. the panel is solved in FP32 (substitution against the FP64-computed diagonal factor);
+//   1. the diagonal tile W(k,k) is factored in FP32 by one CTA (mp_diag.cu): POTRF for
+//      Cholesky, no-pivot GETRF with the reference's pivot rule for LU;
+//   2. the panel is solved in FP32 (substitution against the diagonal factor);
 //   3. the panel is packed into K-major low-precision operands (BF16, FP8 e4m3 with per-tile
 //      scales, or BF16 hi + lo) and the whole trailing matrix is updated by the tcgen05
 //      kernel with FP32 accumulation.
@@ -47,6 +47,7 @@ cudaError_t mps_to_f32_rhs(const double *R, float *R32, long long n, int cols, c
 cudaError_t mps_add_correction(double *X, const float *D32, long long n, int cols, const double *scale,
                                cudaStream_t s);
 cudaError_t mps_mark_step(int *status, int k, cudaStream_t s);
+cudaError_t mpd_factor_tile(int alg, float *W, int n, int nb, int k, int *status, cudaStream_t s);
 cudaError_t mps_invert_diag(const float *W, int n, int nb, float *Dinv, int kind, cudaStream_t s);
 cudaError_t mps_rhs_step(const float *W, const float *Dinv, int n, int nb, int k, float *R, float *S, int kind,
                          cudaStream_t s);
@@ -90,7 +91,6 @@ int mp_factor(int alg, int prec, float *W, int n, int nb, cudaStream_t s, palial
     const int mode = prec == PALIAL_PREC_FP8 ? 1 : prec == PALIAL_PREC_BF16X3 ? 2 : 0;
     const size_t elem = (mode == 1) ? 1 : 2;
     const size_t panel = (size_t)std::max(1, mt - 1) * nb * nb * elem;
-    PALIAL_CK(mb.diag.ensure(sizeof(double) * (size_t)nb * nb), "alloc diag");
     PALIAL_CK(mb.pa_hi.ensure(panel), "alloc panel");
     PALIAL_CK(mb.pb_hi.ensure(panel), "alloc panel");
     if (mode == 2) {
@@ -98,25 +98,12 @@ int mp_factor(int alg, int prec, float *W, int n, int nb, cudaStream_t s, palial
         PALIAL_CK(mb.pb_lo.ensure(panel), "alloc panel");
     }
     PALIAL_CK(mb.scales.ensure(sizeof(float) * 2 * (size_t)std::max(1, mt)), "alloc scales");
-    // FP64 diagonal-tile factorization on the persistent scheduler (64-wide blocks)
-    const int bsd = 64;
-    std::shared_ptr<Dag> ddag;
-    try {
-        ddag = get_dag(alg, nb, nb, bsd, 0, g.sms, 0);
-    } catch (const std::exception &ex) {
-        return set_status(st, PALIAL_ERR_ARG, "%s", ex.what());
-    }
-    SchedParams dp;
-    int rc = sched_prepare(g.diag, ddag, mb.diag.as<double>(), nullptr, g.sms, 0, 120.0, dp, st);
-    if (rc) return rc;
+    PALIAL_CK(g.diag.status.ensure(sizeof(int) * ST_NSLOTS + 64), "alloc status");
     PALIAL_CK(cudaMemsetAsync(g.diag.status.ptr, 0, sizeof(int) * ST_NSLOTS, s), "clear status");
     float *sa = mb.scales.as<float>(), *sb = sa + mt;
     for (int k = 0; k < mt; k++) {
-        float *wkk = W + (size_t)nb * nb * ((size_t)k + (size_t)mt * k);
-        PALIAL_CK(mps_tile_to_f64(wkk, mb.diag.as<double>(), nb, s), "diag to f64");
-        PALIAL_CK(mps_mark_step(g.diag.status.as<int>(), k, s), "mark");
-        PALIAL_CK(sched_enqueue(g.diag, dp, ddag->nobj, g.sms, false, s), "diag factor");
-        PALIAL_CK(mps_tile_to_f32(mb.diag.as<double>(), wkk, nb, alg == 0 ? 1 : 0, s), "diag to f32");
+        // the diagonal tile in FP32, one CTA (mp_diag.cu)
+        PALIAL_CK(mpd_factor_tile(alg, W, n, nb, k, g.diag.status.as<int>(), s), "diag factor");
         if (k == mt - 1) break;
         if (alg == 0) {
             PALIAL_CK(mps_panel_trsm(W, n, nb, k, 0, s), "panel trsm");

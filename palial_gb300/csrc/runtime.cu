@@ -44,6 +44,7 @@ cudaError_t launch_tiled_mm(const double *A, const double *X, double *Y, int n, 
 cudaError_t launch_sumsq(const double *X, long long len, double *partial, int blocks, cudaStream_t s);
 cudaError_t launch_sub(const double *X, const double *Y, double *Z, long long len, cudaStream_t s);
 cudaError_t mps_configure();
+cudaError_t mpd_configure();
 
 State g;
 static long long g_launches = 0;
@@ -199,6 +200,7 @@ int palial_gpu_init(int device) {
     g.sms = prop.multiProcessorCount;
     if (sched_configure() != cudaSuccess) return PALIAL_ERR_CUDA;
     if (mps_configure() != cudaSuccess) return PALIAL_ERR_CUDA;
+    if (mpd_configure() != cudaSuccess) return PALIAL_ERR_CUDA;
     g.occupancy = std::max(1, sched_occupancy());
     if (!g.ev0) cudaEventCreate(&g.ev0);
     if (!g.ev1) cudaEventCreate(&g.ev1);

@@ -143,3 +143,39 @@ def test_non_finite_factor_is_not_reported_as_converged():
         st = P.solve_ir("lu", da.data_ptr(), n, nb, db.data_ptr(), dx.data_ptr(), nrhs, precision=prec,
                         ir_max_iter=5, raise_on_error=False)
         assert st.code < 0, (prec, st.code, st.backward_error)
+
+
+@pytest.mark.parametrize("nb", [256, 512, 768, 1024])
+@pytest.mark.parametrize("alg", ["cholesky", "lu"])
+def test_fp32_diagonal_tile_factor(alg, nb):
+    """A one-tile matrix: the mixed factorization is exactly the FP32 diagonal-tile kernel.
+    Factors against numpy's FP64 ones (FP32 accuracy: normwise 2e-6 on these well-conditioned
+    inputs); for Cholesky the strictly lower triangle must stay untouched."""
+    n = nb
+    a = O.gen_spd(0, n) if alg == "cholesky" else dominant(3, n)
+    da = torch.from_numpy(O.to_tiles(a, nb)).cuda()
+    dw = torch.zeros(n * n, dtype=torch.float32, device="cuda")
+    st = P.mp_factor(alg, da.data_ptr(), dw.data_ptr(), n, nb, precision="bf16")
+    assert st.code == 0
+    w = O.from_tiles(dw.double().cpu().numpy(), n, nb)
+    if alg == "cholesky":
+        u = np.linalg.cholesky(a).T
+        assert np.linalg.norm(np.triu(w) - u) / np.linalg.norm(u) < 2e-6
+        assert np.array_equal(np.tril(w, -1), np.tril(a.astype(np.float32).astype(np.float64), -1))
+    else:
+        import scipy.linalg as sl
+        p, l, u = sl.lu(a)
+        assert np.array_equal(p, np.eye(n))  # diagonally dominant: partial pivoting keeps the order
+        assert np.linalg.norm(np.triu(w) - u) / np.linalg.norm(u) < 2e-6
+        assert np.linalg.norm(np.tril(w, -1) - np.tril(l, -1)) / np.linalg.norm(np.tril(l, -1)) < 2e-6
+
+
+def test_fp32_diagonal_tile_reports_breakdown():
+    """An indefinite diagonal tile: the kernel reports the failing column, not NaN factors."""
+    n, nb = 512, 512
+    a = O.gen_spd(0, n)
+    a[300, 300] = -1.0
+    da = torch.from_numpy(O.to_tiles(a, nb)).cuda()
+    dw = torch.zeros(n * n, dtype=torch.float32, device="cuda")
+    with pytest.raises(P.PalialError):
+        P.mp_factor("cholesky", da.data_ptr(), dw.data_ptr(), n, nb, precision="bf16")
