@@ -5,7 +5,7 @@
 
 A step is one solve A X = B (16 right-hand sides, uniform [-1, 1)) of a device-resident
 SPD matrix A = B B^T + N I (seed = rank; the reference's tile layout) by the mixed-precision
-path: BF16 trailing updates on tcgen05 with FP32 accumulation, FP64 diagonal tiles, FP32
+path: BF16 trailing updates on tcgen05 with FP32 accumulation, FP32 diagonal tiles and
 panels, FP64 residuals and refinement to the FP64-level normwise backward error
 (<= 1e-14 * N).  value = FP64-equivalent algorithmic flops (N^3/3) / time to solution
 (factorization + refinement), summed over ranks (replicas, no collective on the data path).
@@ -430,8 +430,10 @@ def main() -> None:
     with ClockSampler(local) as clk:
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e0.record(stream)
+        torch.cuda.nvtx.range_push("timed_steps")  # profilers can select this region by name
         for _ in range(args.steps):
             sts.append(step())
+        torch.cuda.nvtx.range_pop()
         e1.record(stream)
         barrier()
     total = e0.elapsed_time(e1) * 1e-3
@@ -497,8 +499,8 @@ def main() -> None:
             "warmup": args.warmup, "ms_per_step": per_step * 1e3, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "bf16", "data": "synthetic",
             "config": {"workload": f"mixed-precision Cholesky + IR, N={n}, NB={NB}, 16 RHS, {args.precision} "
-                                   "trailing updates on tcgen05 (FP32 accumulate), FP64 diagonal tiles, FP64 "
-                                   "residuals; SPD B*B^T+N*I seed=rank, device-resident; inputs 8.6 GB >> L2 "
+                                   "trailing updates on tcgen05 (FP32 accumulate), FP32 diagonal tiles and "
+                                   "panels, FP64 residuals; SPD B*B^T+N*I seed=rank, device-resident; inputs 8.6 GB >> L2 "
                                    "(no flush needed)",
                        "n": n, "nb": NB, "nrhs": nrhs, "precision": args.precision,
                        "parallelism": f"replicas x{world}"},
