@@ -25,55 +25,76 @@
 namespace palial {
 namespace mpd {
 
-constexpr int NT = 512;   // threads
+constexpr int NT = 512;   // threads (chol64/getrf64 map 8 threads per column of the 64 x 64 block)
 constexpr int DP = 65;    // padded leading dimension of the 64 x 64 block in shared memory
 constexpr int MT = 8;     // micro-tile edge
+constexpr int PP = 65;    // pitch of the staged panel columns
 
 __host__ __device__ constexpr int chunk_k(int nb) { return nb <= 512 ? 32 : 16; }
 // shared memory (floats): Ds[64][65] + two staged chunks of chunk_k x (nb - 64)
 __host__ __device__ constexpr int smem_floats(int nb) { return 64 * DP + 2 * chunk_k(nb) * (nb - 64) + 64; }
 
 // ---- 64 x 64 diagonal block in shared memory ---------------------------------------------
-// Ds[c][r] = A(r, c).  Returns the first failing column (Cholesky) or -1.
-__device__ int chol64(float (*Ds)[DP], int *sflag) {
+// Ds[c][r] = A(r, c).  Thread t owns column q = t / 8 and rows i = t % 8 + 8 j (j < 8) of the
+// block for the trailing updates, so the pivot loop has no index arithmetic.
+// Returns the first failing column (Cholesky) or -1.
+__device__ __forceinline__ int chol64(float (*Ds)[DP]) {
+    const int q = threadIdx.x >> 3, i0 = threadIdx.x & 7;
     for (int p = 0; p < 64; p++) {
         const float d = Ds[p][p];
-        if (!(d > 0.f)) {
-            // every thread reads the same pivot: the decision is uniform
-            return p;
-        }
+        if (!(d > 0.f)) return p;  // every thread reads the same pivot: a uniform decision
         const float r = sqrtf(d);
-        for (int q = p + 1 + threadIdx.x; q < 64; q += NT) Ds[q][p] = Ds[q][p] / r;
+        if (threadIdx.x < 64 && threadIdx.x > p) Ds[threadIdx.x][p] = Ds[threadIdx.x][p] / r;  // U(p, q)
         __syncthreads();
         if (threadIdx.x == 0) Ds[p][p] = r;
-        const int w = 63 - p;  // trailing (i, q), p < i <= q
-        for (int e = threadIdx.x; e < w * w; e += NT) {
-            const int i = p + 1 + e % w, q = p + 1 + e / w;
-            if (i <= q) Ds[q][i] = fmaf(-Ds[i][p], Ds[q][p], Ds[q][i]);
+        if (q > p) {
+            // all 16 loads before the 8 stores: one shared-memory round trip per pivot
+            const float uq = Ds[q][p];
+            float lv[8], cv[8];
+#pragma unroll
+            for (int j = 0; j < 8; j++) {
+                lv[j] = Ds[i0 + 8 * j][p];
+                cv[j] = Ds[q][i0 + 8 * j];
+            }
+#pragma unroll
+            for (int j = 0; j < 8; j++) {
+                const int i = i0 + 8 * j;
+                if (i > p && i <= q) Ds[q][i] = fmaf(-lv[j], uq, cv[j]);  // A(i,q) -= U(p,i) U(p,q)
+            }
         }
         __syncthreads();
     }
-    (void)sflag;
     return -1;
 }
 
 // No-pivot LU of the block; returns 1 if an exact zero pivot was skipped.
-__device__ int getrf64(float (*Ds)[DP]) {
+__device__ __forceinline__ int getrf64(float (*Ds)[DP]) {
+    const int q = threadIdx.x >> 3, i0 = threadIdx.x & 7;
     int zero = 0;
     for (int p = 0; p < 64; p++) {
         const float piv = Ds[p][p];
         if (piv != 0.f) {
-            const bool recip = fabsf(piv) > FLT_MIN;
-            const float rp = 1.f / piv;
-            for (int i = p + 1 + threadIdx.x; i < 64; i += NT) Ds[p][i] = recip ? Ds[p][i] * rp : Ds[p][i] / piv;
+            if (threadIdx.x < 64 && threadIdx.x > p) {
+                const float x = Ds[p][threadIdx.x];  // L(i, p) = A(i, p) / piv
+                Ds[p][threadIdx.x] = fabsf(piv) > FLT_MIN ? x * (1.f / piv) : x / piv;
+            }
         } else {
             zero = 1;
         }
         __syncthreads();
-        const int w = 63 - p;
-        for (int e = threadIdx.x; e < w * w; e += NT) {
-            const int i = p + 1 + e % w, q = p + 1 + e / w;
-            Ds[q][i] = fmaf(-Ds[p][i], Ds[q][p], Ds[q][i]);
+        if (q > p) {
+            const float up = Ds[q][p];  // U(p, q)
+            float lv[8], cv[8];
+#pragma unroll
+            for (int j = 0; j < 8; j++) {
+                lv[j] = Ds[p][i0 + 8 * j];
+                cv[j] = Ds[q][i0 + 8 * j];
+            }
+#pragma unroll
+            for (int j = 0; j < 8; j++) {
+                const int i = i0 + 8 * j;
+                if (i > p) Ds[q][i] = fmaf(-lv[j], up, cv[j]);  // A(i,q) -= L(i,p) U(p,q)
+            }
         }
         __syncthreads();
     }
@@ -98,32 +119,41 @@ __device__ __forceinline__ float finish(const float (*Ds)[DP], int u, float s) {
     if (KIND == 0) return s / d;
     return d == 0.f ? s : (fabsf(d) > FLT_MIN ? s * (1.f / d) : s / d);
 }
+// Right-looking: once unknown p is final, every later unknown is updated at once (independent
+// FMAs).  Two halves of 32 unknowns in registers (the first half is read back from v for the
+// second half's right-hand side).  v[i * stride] holds the vector.
 template <int KIND>
-__device__ void solve_vec(const float (*Ds)[DP], float *b, size_t stride) {
-#pragma unroll 1
-    for (int h = 0; h < 64; h += 32) {
+__device__ __noinline__ void solve_vec(const float (*Ds)[DP], float *v, size_t stride) {
+    {
         float x[32];
 #pragma unroll
-        for (int i = 0; i < 32; i++) x[i] = b[(size_t)(h + i) * stride];
-        if (h) {
-            // contributions of the solved first half
-#pragma unroll 4
-            for (int p = 0; p < 32; p++) {
-                const float xp = b[(size_t)p * stride];
+        for (int i = 0; i < 32; i++) x[i] = v[(size_t)i * stride];
 #pragma unroll
-                for (int i = 0; i < 32; i++) x[i] = fmaf(-coef<KIND>(Ds, 32 + i, p), xp, x[i]);
-            }
+        for (int p = 0; p < 32; p++) {
+            x[p] = finish<KIND>(Ds, p, x[p]);
+#pragma unroll
+            for (int i = p + 1; i < 32; i++) x[i] = fmaf(-coef<KIND>(Ds, i, p), x[p], x[i]);
         }
 #pragma unroll
-        for (int i = 0; i < 32; i++) {
-            float acc = x[i];
-#pragma unroll
-            for (int p = 0; p < i; p++) acc = fmaf(-coef<KIND>(Ds, h + i, h + p), x[p], acc);
-            x[i] = finish<KIND>(Ds, h + i, acc);
-        }
-#pragma unroll
-        for (int i = 0; i < 32; i++) b[(size_t)(h + i) * stride] = x[i];
+        for (int i = 0; i < 32; i++) v[(size_t)i * stride] = x[i];
     }
+    float y[32];
+#pragma unroll
+    for (int i = 0; i < 32; i++) y[i] = v[(size_t)(32 + i) * stride];
+#pragma unroll 4
+    for (int p = 0; p < 32; p++) {
+        const float xp = v[(size_t)p * stride];
+#pragma unroll
+        for (int i = 0; i < 32; i++) y[i] = fmaf(-coef<KIND>(Ds, 32 + i, p), xp, y[i]);
+    }
+#pragma unroll
+    for (int p = 0; p < 32; p++) {
+        y[p] = finish<KIND>(Ds, 32 + p, y[p]);
+#pragma unroll
+        for (int i = p + 1; i < 32; i++) y[i] = fmaf(-coef<KIND>(Ds, 32 + i, 32 + p), y[p], y[i]);
+    }
+#pragma unroll
+    for (int i = 0; i < 32; i++) v[(size_t)(32 + i) * stride] = y[i];
 }
 
 // ---- trailing update -----------------------------------------------------------------------
@@ -131,22 +161,24 @@ __device__ void solve_vec(const float (*Ds)[DP], float *b, size_t stride) {
 // memory, accumulated over all 64 rows of the panel in chunks staged by `stage`.
 // UPPER: only micro-tiles with bj >= bi, and inside diagonal micro-tiles only i <= j.
 template <bool UPPER, class Stage>
-__device__ void trailing(float *C, int ld, int m, int kc, float *As, float *Bs, Stage stage) {
+__device__ __forceinline__ void trailing(float *C, int ld, int m, int kc, float *As, float *Bs, Stage stage) {
     const int mb = m / MT;
     const int tiles = UPPER ? mb * (mb + 1) / 2 : mb * mb;  // UPPER: micro-tiles with bj >= bi
     for (int base = 0; base < tiles; base += NT) {
         const int u = base + threadIdx.x;
+        // consecutive threads take consecutive row blocks bi of one column block bj, so a warp's
+        // accesses to a column of C are contiguous
         int bi = 0, bj = 0;
         if (UPPER) {
-            int rem = u;
-            while (bi < mb && rem >= mb - bi) {
-                rem -= mb - bi;
-                bi++;
+            int rem = u;  // column block bj holds bj + 1 micro-tiles (bi <= bj)
+            while (bj < mb && rem > bj) {
+                rem -= bj + 1;
+                bj++;
             }
-            bj = bi + rem;
+            bi = rem;
         } else {
-            bi = u / mb;
-            bj = u % mb;
+            bi = u % mb;
+            bj = u / mb;
         }
         const bool active = u < tiles;
         float acc[MT][MT];
@@ -174,16 +206,27 @@ __device__ void trailing(float *C, int ld, int m, int kc, float *As, float *Bs, 
             }
         }
         if (active) {
+            // C micro-tile: per column two float4 (rows bi*8 .. bi*8+7), all loads before the
+            // stores; inside a diagonal micro-tile of the upper update the strictly lower entries
+            // are written back unchanged
+            float4 cv[MT][2];
 #pragma unroll
-            for (int j = 0; j < MT; j++)
+            for (int j = 0; j < MT; j++) {
+                const float *cc = C + bi * MT + (size_t)(bj * MT + j) * ld;
+                cv[j][0] = *reinterpret_cast<const float4 *>(cc);
+                cv[j][1] = *reinterpret_cast<const float4 *>(cc + 4);
+            }
 #pragma unroll
-                for (int i = 0; i < MT; i++) {
-                    const int r = bi * MT + i, c = bj * MT + j;
-                    if (!UPPER || r <= c) {
-                        float *x = C + r + (size_t)c * ld;
-                        *x -= acc[i][j];
-                    }
-                }
+            for (int j = 0; j < MT; j++) {
+                float o[MT] = {cv[j][0].x, cv[j][0].y, cv[j][0].z, cv[j][0].w,
+                               cv[j][1].x, cv[j][1].y, cv[j][1].z, cv[j][1].w};
+#pragma unroll
+                for (int i = 0; i < MT; i++)
+                    if (!UPPER || bi < bj || i <= j) o[i] -= acc[i][j];
+                float *cc = C + bi * MT + (size_t)(bj * MT + j) * ld;
+                *reinterpret_cast<float4 *>(cc) = make_float4(o[0], o[1], o[2], o[3]);
+                *reinterpret_cast<float4 *>(cc + 4) = make_float4(o[4], o[5], o[6], o[7]);
+            }
         }
     }
 }
@@ -204,7 +247,7 @@ __global__ void __launch_bounds__(NT, 1) diag_factor_kernel(float *T, int nb, in
         for (int e = threadIdx.x; e < 4096; e += NT) Ds[e >> 6][e & 63] = D[(e & 63) + (size_t)(e >> 6) * nb];
         __syncthreads();
         if (ALG == 0) {
-            const int bad = chol64(Ds, nullptr);
+            const int bad = chol64(Ds);
             if (bad >= 0) {
                 if (threadIdx.x == 0 && atomicCAS(status + ST_CODE, 0, -3 /*PALIAL_ERR_NOT_SPD*/) == 0) {
                     status[ST_COL] = j0 + bad;
@@ -226,9 +269,25 @@ __global__ void __launch_bounds__(NT, 1) diag_factor_kernel(float *T, int nb, in
         __syncthreads();
         // panels
         float *A12 = T + j0 + (size_t)(j0 + 64) * nb;  // 64 x m, columns at stride nb
-        for (int c = threadIdx.x; c < m; c += NT) {
-            if (ALG == 0) solve_vec<0>(Ds, A12 + (size_t)c * nb, 1);
-            else solve_vec<1>(Ds, A12 + (size_t)c * nb, 1);
+        // column panel: staged through shared memory (coalesced loads and stores; a thread
+        // solves one column, Ps[c][i] with an odd pitch so the threads' columns do not share banks)
+        {
+            float *Ps = As;  // the trailing update's chunk space is free here
+            const int cwmax = (2 * kc * (nb - 64)) / PP;
+            for (int c0 = 0; c0 < m; c0 += cwmax) {
+                const int cw = min(cwmax, m - c0);
+                for (int e = threadIdx.x; e < cw * 64; e += NT)
+                    Ps[(e >> 6) * PP + (e & 63)] = A12[(e & 63) + (size_t)(c0 + (e >> 6)) * nb];
+                __syncthreads();
+                for (int c = threadIdx.x; c < cw; c += NT) {
+                    if (ALG == 0) solve_vec<0>(Ds, Ps + c * PP, 1);
+                    else solve_vec<1>(Ds, Ps + c * PP, 1);
+                }
+                __syncthreads();
+                for (int e = threadIdx.x; e < cw * 64; e += NT)
+                    A12[(e & 63) + (size_t)(c0 + (e >> 6)) * nb] = Ps[(e >> 6) * PP + (e & 63)];
+                __syncthreads();
+            }
         }
         if (ALG == 1) {
             float *A21 = T + (j0 + 64) + (size_t)j0 * nb;  // m x 64, rows contiguous
@@ -237,11 +296,17 @@ __global__ void __launch_bounds__(NT, 1) diag_factor_kernel(float *T, int nb, in
         __syncthreads();
         float *C = T + (j0 + 64) + (size_t)(j0 + 64) * nb;
         if (ALG == 0) {
-            // As[kk][i] = U12(k0 + kk, i): contiguous in kk in global memory
+            // As[kk][i] = U12(k0 + kk, i), contiguous in kk in global memory: each thread loads
+            // 4 consecutive kk of one column (float4) and a warp covers 32 consecutive columns,
+            // so the shared stores of a warp hit 32 different banks
             auto stage = [&](int k0) {
-                for (int e = threadIdx.x; e < kc * m; e += NT) {
-                    const int kk = e % kc, i = e / kc;
-                    As[(size_t)kk * m + i] = A12[(k0 + kk) + (size_t)i * nb];
+                for (int e = threadIdx.x; e < (kc / 4) * m; e += NT) {
+                    const int i = e % m, kq = 4 * (e / m);
+                    const float4 v = *reinterpret_cast<const float4 *>(A12 + (k0 + kq) + (size_t)i * nb);
+                    As[(size_t)(kq + 0) * m + i] = v.x;
+                    As[(size_t)(kq + 1) * m + i] = v.y;
+                    As[(size_t)(kq + 2) * m + i] = v.z;
+                    As[(size_t)(kq + 3) * m + i] = v.w;
                 }
             };
             trailing<true>(C, nb, m, kc, As, As, stage);
@@ -252,9 +317,13 @@ __global__ void __launch_bounds__(NT, 1) diag_factor_kernel(float *T, int nb, in
                     const int i = e % m, kk = e / m;  // L21(i, k0+kk): contiguous in i
                     As[(size_t)kk * m + i] = A21[i + (size_t)(k0 + kk) * nb];
                 }
-                for (int e = threadIdx.x; e < kc * m; e += NT) {
-                    const int kk = e % kc, j = e / kc;  // U12(k0+kk, j): contiguous in kk
-                    Bs[(size_t)kk * m + j] = A12[(k0 + kk) + (size_t)j * nb];
+                for (int e = threadIdx.x; e < (kc / 4) * m; e += NT) {
+                    const int j = e % m, kq = 4 * (e / m);  // U12(k0+kq.., j): float4 along kk
+                    const float4 v = *reinterpret_cast<const float4 *>(A12 + (k0 + kq) + (size_t)j * nb);
+                    Bs[(size_t)(kq + 0) * m + j] = v.x;
+                    Bs[(size_t)(kq + 1) * m + j] = v.y;
+                    Bs[(size_t)(kq + 2) * m + j] = v.z;
+                    Bs[(size_t)(kq + 3) * m + j] = v.w;
                 }
             };
             trailing<false>(C, nb, m, kc, As, Bs, stage);

@@ -40,7 +40,7 @@ cudaError_t mps_tile_to_f64(const float *w, double *d, int nb, cudaStream_t s);
 cudaError_t mps_tile_to_f32(const double *d, float *w, int nb, int upper_only, cudaStream_t s);
 cudaError_t mps_panel_trsm(float *W, int n, int nb, int k, int kind, cudaStream_t s);
 cudaError_t mps_residual(const double *A, int n, int nb, const double *X, const double *B, double *R, int nrhs,
-                         cudaStream_t s);
+                         double *amax, cudaStream_t s);
 cudaError_t mps_norm_inf_matrix(const double *A, int n, int nb, double *out, cudaStream_t s);
 cudaError_t mps_colmax(const double *X, long long n, int cols, double *out, cudaStream_t s);
 cudaError_t mps_to_f32_rhs(const double *R, float *R32, long long n, int cols, const double *scale, cudaStream_t s);
@@ -150,7 +150,7 @@ int mp_prepare_solves(int alg, const float *W, int n, int nb, cudaStream_t s, pa
     return PALIAL_OK;
 }
 
-// d = M^-1 r for the FP32 factors in W; R32 (n x 64, zero padded) in/out.  Block forward and
+// d = M^-1 r for the FP32 factors in W; R32 (n x 16, zero padded) in/out.  Block forward and
 // backward substitution over tile rows: the diagonal step multiplies by the stored inverse,
 // the update step subtracts the solved tile row from the remaining ones.
 int mp_apply_inverse(int alg, const float *W, int n, int nb, float *R32, cudaStream_t s, palial_status *st) {
@@ -206,7 +206,7 @@ int gmres(int alg, const double *A, const float *W, int n, int nb, const double 
             int rc = precondition(alg, W, n, nb, r, w, nrhs, dscale, hs, s, st);
             if (rc) return rc;
         } else {
-            PALIAL_CK(mps_residual(A, n, nb, d, r, V, nrhs, s), "inner residual");
+            PALIAL_CK(mps_residual(A, n, nb, d, r, V, nrhs, nullptr, s), "inner residual");
             int rc = precondition(alg, W, n, nb, V, w, nrhs, dscale, hs, s, st);
             if (rc) return rc;
         }
@@ -226,7 +226,7 @@ int gmres(int alg, const double *A, const float *W, int n, int nb, const double 
         int j = 0;
         for (; j < m && total < maxit; j++, total++) {
             // w = M^-1 A V_j
-            PALIAL_CK(mps_residual(A, n, nb, V + blk * j, nullptr, tv, nrhs, s), "A v");
+            PALIAL_CK(mps_residual(A, n, nb, V + blk * j, nullptr, tv, nrhs, nullptr, s), "A v");
             int rc = precondition(alg, W, n, nb, tv, w, nrhs, dscale, hs, s, st);
             if (rc) return rc;
             // CGS twice: h = V^T w, w -= V h
@@ -415,10 +415,9 @@ static int solve_one(int alg, const double *dA, int n, int nb, const double *dB,
     float *W = mb.w.as<float>();
     double *nrm = mb.norms.as<double>();  // [0] ||A||, [1..16] scale, [17..32] |r|, [33..48] |x|, [49..64] |b|
     // ||A||_inf and max |a_ii| (for the shift)
-    PALIAL_CK(mps_norm_inf_matrix(dA, n, nb, nrm, s), "norm A");
-    double anorm = 0;
-    PALIAL_CK(cudaMemcpyAsync(&anorm, nrm, sizeof(double), cudaMemcpyDeviceToHost, s), "norm");
-    PALIAL_CK(cudaStreamSynchronize(s), "norm");
+    // ||A||_inf comes with the first residual (same pass over A); a shifted retry of a
+    // broken-down factorization computes it on its own
+    double anorm = -1.0;
     const int prec = o.precision;
     // ---- factorization (FP64 path: plain FP64 scheduler, then the same FP32 solves) -------
     int zp = 0;
@@ -442,6 +441,12 @@ static int solve_one(int alg, const double *dA, int n, int nb, const double *dB,
             PALIAL_CK(mps_f64_to_f32(dA, W, n, nb, shift, s), "convert");
             rc = mp_factor(alg, prec, W, n, nb, s, st, &zp);
             if (rc != PALIAL_ERR_NOT_SPD || alg != 0) break;
+            if (anorm < 0) {
+                PALIAL_CK(cudaMemsetAsync(nrm, 0, sizeof(double), s), "norm A");
+                PALIAL_CK(mps_norm_inf_matrix(dA, n, nb, nrm, s), "norm A");
+                PALIAL_CK(cudaMemcpyAsync(&anorm, nrm, sizeof(double), cudaMemcpyDeviceToHost, s), "norm");
+                PALIAL_CK(cudaStreamSynchronize(s), "norm");
+            }
             // Higham-Pranesh style shift: a small multiple of u_f * ||A||
             shift = (shift == 0.0) ? 4.0 * unit_roundoff(prec) * anorm / std::sqrt((double)n) : shift * 4.0;
         }
@@ -487,7 +492,10 @@ static int solve_one(int alg, const double *dA, int n, int nb, const double *dB,
             PALIAL_CK(cudaMemcpyAsync(nrm + 80, ones.data(), sizeof(double) * nrhs, cudaMemcpyHostToDevice, s), "one");
             PALIAL_CK(mps_multi_axpy(dcorr, 1, nrm + 80, dX, n, nrhs, 0, s), "x += d");
         }
-        PALIAL_CK(mps_residual(dA, n, nb, dX, dB, mb.r.as<double>(), nrhs, s), "residual");
+        const bool need_norm = anorm < 0;
+        if (need_norm) PALIAL_CK(cudaMemsetAsync(nrm, 0, sizeof(double), s), "norm A");
+        PALIAL_CK(mps_residual(dA, n, nb, dX, dB, mb.r.as<double>(), nrhs, need_norm ? nrm : nullptr, s), "residual");
+        if (need_norm) PALIAL_CK(cudaMemcpyAsync(&anorm, nrm, sizeof(double), cudaMemcpyDeviceToHost, s), "norm A");
         PALIAL_CK(mps_colmax(mb.r.as<double>(), n, nrhs, nrm + 17, s), "norm r");
         PALIAL_CK(mps_colmax(dX, n, nrhs, nrm + 33, s), "norm x");
         PALIAL_CK(cudaMemcpyAsync(hr.data(), nrm + 17, sizeof(double) * nrhs, cudaMemcpyDeviceToHost, s), "norm r");

@@ -62,44 +62,44 @@ __device__ __forceinline__ Smem smem_parts(float *s) {
 }
 
 // X = U^-T B, B = nb x 64 strip (ld), U upper nb x nb (ld_u)
-__device__ void strip_lut(const Smem &m, const float *U, int ldu, float *B, int ldb, int nb) {
+__device__ __forceinline__ void strip_lut(const Smem &m, const float *U, int ldu, float *B, int ldb, int nb) {
     for (int rb = 0; rb < nb; rb += 64) {
         if (rb > 0) cta_gemm<true, false>(64, 64, rb, -1.f, U + (size_t)rb * ldu, ldu, B, ldb, B + rb, ldb, m.g);
         load_diag64(m.Ds, U + rb + (size_t)rb * ldu, ldu);
-        solve64<0>(m.Ds, m.Bs, B + rb, ldb);
+        solve64<0>(m.Ds, B + rb, ldb);
     }
 }
 // X = U^-1 B (backward), B = nb x 64 strip
-__device__ void strip_un(const Smem &m, const float *U, int ldu, float *B, int ldb, int nb) {
+__device__ __forceinline__ void strip_un(const Smem &m, const float *U, int ldu, float *B, int ldb, int nb) {
     for (int rb = nb - 64; rb >= 0; rb -= 64) {
         if (rb + 64 < nb)
             cta_gemm<false, false>(64, 64, nb - rb - 64, -1.f, U + rb + (size_t)(rb + 64) * ldu, ldu, B + rb + 64, ldb,
                                    B + rb, ldb, m.g);
         load_diag64(m.Ds, U + rb + (size_t)rb * ldu, ldu);
-        solve64<3>(m.Ds, m.Bs, B + rb, ldb);
+        solve64<3>(m.Ds, B + rb, ldb);
     }
 }
 // X = L^-1 B (unit lower), B = nb x 64 strip
-__device__ void strip_llu(const Smem &m, const float *L, int ldl, float *B, int ldb, int nb) {
+__device__ __forceinline__ void strip_llu(const Smem &m, const float *L, int ldl, float *B, int ldb, int nb) {
     for (int rb = 0; rb < nb; rb += 64) {
         if (rb > 0) cta_gemm<false, false>(64, 64, rb, -1.f, L + rb, ldl, B, ldb, B + rb, ldb, m.g);
         load_diag64(m.Ds, L + rb + (size_t)rb * ldl, ldl);
-        solve64<2>(m.Ds, m.Bs, B + rb, ldb);
+        solve64<2>(m.Ds, B + rb, ldb);
     }
 }
 // X = B U^-1, B = 64 x nb row strip
-__device__ void strip_run(const Smem &m, const float *U, int ldu, float *B, int ldb, int nb) {
+__device__ __forceinline__ void strip_run(const Smem &m, const float *U, int ldu, float *B, int ldb, int nb) {
     for (int cb = 0; cb < nb; cb += 64) {
         if (cb > 0)
             cta_gemm<false, false>(64, 64, cb, -1.f, B, ldb, U + (size_t)cb * ldu, ldu, B + (size_t)cb * ldb, ldb, m.g);
         load_diag64(m.Ds, U + cb + (size_t)cb * ldu, ldu);
-        solve64<1>(m.Ds, m.Bs, B + (size_t)cb * ldb, ldb);
+        solve64<1>(m.Ds, B + (size_t)cb * ldb, ldb);
     }
 }
 
 // kind 0: Cholesky row panel U(k,m) <- U_kk^-T U(k,m);  1: LU row panel U(k,n) <- L_kk^-1 .;
 // 2: LU column panel L(m,k) <- L(m,k) U_kk^-1.  grid (nb/64, trailing tiles).
-__global__ void __launch_bounds__(NT, 1) panel_trsm_kernel(float *W, int n, int nb, int k, int kind) {
+__global__ void __launch_bounds__(NT, 2) panel_trsm_kernel(float *W, int n, int nb, int k, int kind) {
     extern __shared__ __align__(16) float smem[];
     const Smem m = smem_parts(smem);
     const int t = k + 1 + blockIdx.y, s = blockIdx.x;
@@ -137,10 +137,10 @@ __global__ void __launch_bounds__(NT, 1) rhs_apply_kernel(const float *Dinv, int
     const float *D = Dinv + (size_t)k * nb * nb;
     const float *Rk = R + (size_t)k * nb;
     float *out = S + rb;
-    for (int e = threadIdx.x; e < 64 * 64; e += NT) out[(e & 63) + (size_t)(e >> 6) * nb] = 0.f;
+    for (int e = threadIdx.x; e < 64 * RW; e += NT) out[(e & 63) + (size_t)(e >> 6) * nb] = 0.f;
     __syncthreads();
-    if (trans) cta_gemm<true, false>(64, 64, nb, 1.f, D + (size_t)rb * nb, nb, Rk, n, out, nb, m.g);
-    else cta_gemm<false, false>(64, 64, nb, 1.f, D + rb, nb, Rk, n, out, nb, m.g);
+    if (trans) cta_gemm_rw<true>(64, nb, 1.f, D + (size_t)rb * nb, nb, Rk, n, out, nb, m.g);
+    else cta_gemm_rw<false>(64, nb, 1.f, D + rb, nb, Rk, n, out, nb, m.g);
 }
 
 // R_t -= op(W tile) S for one 64-row block of tile row t per CTA (blockIdx.y = row block);
@@ -153,49 +153,74 @@ __global__ void __launch_bounds__(NT, 1) rhs_update2_kernel(const float *W, int 
     const int rb = blockIdx.y * 64;
     if ((int)blockIdx.x == count) {
         float *Rk = R + (size_t)k * nb + rb;
-        for (int e = threadIdx.x; e < 64 * 64; e += NT) Rk[(e & 63) + (size_t)(e >> 6) * n] = S[rb + (e & 63) + (size_t)(e >> 6) * nb];
+        for (int e = threadIdx.x; e < 64 * RW; e += NT) Rk[(e & 63) + (size_t)(e >> 6) * n] = S[rb + (e & 63) + (size_t)(e >> 6) * nb];
         return;
     }
     const int t = (kind == 1) ? (int)blockIdx.x : k + 1 + (int)blockIdx.x;
     float *Rt = R + (size_t)t * nb + rb;
     if (kind == 0)
-        cta_gemm<true, false>(64, 64, nb, -1.f, W + tile_off(n, nb, k, t) + (size_t)rb * nb, nb, S, nb, Rt, n, m.g);
+        cta_gemm_rw<true>(64, nb, -1.f, W + tile_off(n, nb, k, t) + (size_t)rb * nb, nb, S, nb, Rt, n, m.g);
     else
-        cta_gemm<false, false>(64, 64, nb, -1.f, W + tile_off(n, nb, t, k) + rb, nb, S, nb, Rt, n, m.g);
+        cta_gemm_rw<false>(64, nb, -1.f, W + tile_off(n, nb, t, k) + rb, nb, S, nb, Rt, n, m.g);
 }
 
 // ---- FP64 residual R = B - A X (A: FP64 tile layout; X, B, R: n x nrhs, ld n; nrhs <= 16) ---
+// One CTA per 32-row block (n/32 CTAs, several resident per SM, so the last wave is short);
+// thread (row = t % 32, group g = t / 32) accumulates right-hand sides 2g and 2g + 1 over all
+// columns, A staged 64 columns at a time.  The FP64 pipe is the bound (16 right-hand sides:
+// 4 flop per byte of A).  With amax != nullptr the same pass also returns ||A||_inf (the row
+// sums of |a_ij| in FP32 partials, combined in FP64; atomicMax on the bit pattern, amax
+// zeroed by the caller).
 __global__ void __launch_bounds__(256) residual_kernel(const double *A, int n, int nb, const double *X,
-                                                       const double *B, double *R, int nrhs) {
-    __shared__ double As[64][65];
+                                                       const double *B, double *R, int nrhs, double *amax) {
+    __shared__ double As[64][33];
     __shared__ double Xs[64][17];
-    const int i0 = blockIdx.x * 64;
-    const int row = threadIdx.x & 63, grp = threadIdx.x >> 6;   // 4 groups x 4 right-hand sides
-    double acc[4] = {0.0, 0.0, 0.0, 0.0};
+    __shared__ float part[8][33];
+    const int i0 = blockIdx.x * 32;
+    const int row = threadIdx.x & 31, grp = threadIdx.x >> 5;
+    double acc0 = 0.0, acc1 = 0.0;
+    float asum = 0.f;
     const int mt = n / nb;
+    const double *tilerow = A + (size_t)nb * nb * (size_t)(i0 / nb) + (size_t)(i0 % nb);
     for (int p0 = 0; p0 < n; p0 += 64) {
-        const double *blk = A + (size_t)nb * nb * ((size_t)(i0 / nb) + (size_t)mt * (p0 / nb)) + (size_t)(i0 % nb) +
-                            (size_t)(p0 % nb) * nb;
-        for (int e = threadIdx.x; e < 4096; e += 256) As[e >> 6][e & 63] = blk[(e & 63) + (size_t)(e >> 6) * nb];
+        const double *blk = tilerow + (size_t)nb * nb * (size_t)mt * (p0 / nb) + (size_t)(p0 % nb) * nb;
+        for (int e = threadIdx.x; e < 2048; e += 256) As[e >> 5][e & 31] = blk[(e & 31) + (size_t)(e >> 5) * nb];
         for (int e = threadIdx.x; e < 64 * 16; e += 256) {
             const int r = e & 63, c = e >> 6;
             Xs[r][c] = (c < nrhs) ? X[(size_t)(p0 + r) + (size_t)c * n] : 0.0;
         }
         __syncthreads();
-#pragma unroll 4
+        if (amax) {
+#pragma unroll
+            for (int p = grp; p < 64; p += 8) asum += fabsf((float)As[p][row]);
+        }
+#pragma unroll 8
         for (int p = 0; p < 64; p++) {
             const double a = As[p][row];
-#pragma unroll
-            for (int j = 0; j < 4; j++) acc[j] = fma(a, Xs[p][grp * 4 + j], acc[j]);
+            acc0 = fma(a, Xs[p][2 * grp], acc0);
+            acc1 = fma(a, Xs[p][2 * grp + 1], acc1);
         }
         __syncthreads();
     }
+    const double accs[2] = {acc0, acc1};
 #pragma unroll
-    for (int j = 0; j < 4; j++) {
-        const int c = grp * 4 + j;
+    for (int j = 0; j < 2; j++) {
+        const int c = 2 * grp + j;
         if (c < nrhs) {
             const size_t o = (size_t)(i0 + row) + (size_t)c * n;
-            R[o] = B ? B[o] - acc[j] : acc[j];
+            R[o] = B ? B[o] - accs[j] : accs[j];
+        }
+    }
+    if (amax) {
+        part[grp][row] = asum;
+        __syncthreads();
+        if (threadIdx.x < 32) {
+            double t = 0.0;
+#pragma unroll
+            for (int g = 0; g < 8; g++) t += (double)part[g][row];
+            for (int o = 16; o; o >>= 1) t = fmax(t, __shfl_xor_sync(0xffffffffu, t, o));
+            if (threadIdx.x == 0)
+                atomicMax(reinterpret_cast<unsigned long long *>(amax), (unsigned long long)__double_as_longlong(t));
         }
     }
 }
@@ -238,9 +263,9 @@ __global__ void colmax_kernel(const double *X, long long n, int cols, double *ou
         atomicMax(reinterpret_cast<unsigned long long *>(out + c), (unsigned long long)__double_as_longlong(mx));
 }
 
-// R32 (n x 64, zero padded) = float(R64 / scale_c) ; X64 += scale_c * D32
+// R32 (n x RW, zero padded) = float(R64 / scale_c) ; X64 += scale_c * D32
 __global__ void to_f32_rhs_kernel(const double *R, float *R32, long long n, int cols, const double *scale) {
-    const long long total = n * 64;
+    const long long total = n * RW;
     for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < total; e += (long long)gridDim.x * blockDim.x) {
         const int c = (int)(e / n);
         R32[e] = (c < cols) ? (float)(R[e] / scale[c]) : 0.f;
@@ -415,9 +440,9 @@ cudaError_t mps_panel_trsm(float *W, int n, int nb, int k, int kind, cudaStream_
     return cudaGetLastError();
 }
 cudaError_t mps_residual(const double *A, int n, int nb, const double *X, const double *B, double *R, int nrhs,
-                         cudaStream_t s) {
+                         double *amax, cudaStream_t s) {
     note_launch();
-    mps::residual_kernel<<<n / 64, 256, 0, s>>>(A, n, nb, X, B, R, nrhs);
+    mps::residual_kernel<<<n / 32, 256, 0, s>>>(A, n, nb, X, B, R, nrhs, amax);
     return cudaGetLastError();
 }
 cudaError_t mps_norm_inf_matrix(const double *A, int n, int nb, double *out, cudaStream_t s) {

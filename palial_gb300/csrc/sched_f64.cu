@@ -160,10 +160,28 @@ __device__ int getrf_nopiv(const Worker &w, double *A, int n, int ld) {
             }
             __syncthreads();
             const int rows = n - col - 1, cols = j0 + 63 - col;
-            for (int e = threadIdx.x; e < rows * cols; e += NT) {
-                const int r = col + 1 + e % rows, c = col + 1 + e / rows;
-                double *x = A + r + (size_t)c * ld;
-                *x = fma(-ldg(ccol + r), ldg(A + col + (size_t)c * ld), ldg(x));
+            // rank-1 update of the panel, 4 elements per thread per pass with all loads issued
+            // before the stores (a load after a possibly aliasing store waits a round trip)
+            for (int e0 = threadIdx.x; e0 < rows * cols; e0 += 4 * NT) {
+                double l[4], u[4], x[4];
+#pragma unroll
+                for (int q = 0; q < 4; q++) {
+                    const int e = e0 + q * NT;
+                    if (e < rows * cols) {
+                        const int r = col + 1 + e % rows, c = col + 1 + e / rows;
+                        l[q] = ldg(ccol + r);
+                        u[q] = ldg(A + col + (size_t)c * ld);
+                        x[q] = ldg(A + r + (size_t)c * ld);
+                    }
+                }
+#pragma unroll
+                for (int q = 0; q < 4; q++) {
+                    const int e = e0 + q * NT;
+                    if (e < rows * cols) {
+                        const int r = col + 1 + e % rows, c = col + 1 + e / rows;
+                        A[r + (size_t)c * ld] = fma(-l[q], u[q], x[q]);
+                    }
+                }
             }
             __syncthreads();
         }
@@ -305,6 +323,57 @@ __device__ double larfg(const Worker &w, double *alpha_p, double *x, int m) {
     return tau;
 }
 
+// Apply one Householder reflector to column cj, one warp: s = head + <v, cj(r0:nb)>, where
+// v = ci(r0:nb) and head = the column's entry on the reflector's unit position (*hj, which is
+// updated too), then cj(r0:nb) += (-tau s) v.  The lane's slice of cj and v stays in registers
+// between the dot product and the update (up to 16 entries per lane, nb - r0 <= 512; longer
+// columns are handled in passes with batched loads), so no load waits behind a store.  The
+// summation order is the plain lane-strided one either way.
+__device__ __forceinline__ void reflect_col(const double *ci, double *cj, double *hj, int r0, int nb, double tau,
+                                            int lane) {
+    constexpr int U = 16;
+    double s = (lane == 0) ? ldg(hj) : 0.0;
+    if (nb - r0 <= 32 * U) {
+        double vi[U], vj[U];
+#pragma unroll
+        for (int u = 0; u < U; u++) {
+            const int r = r0 + lane + 32 * u;
+            vi[u] = r < nb ? ldg(ci + r) : 0.0;
+            vj[u] = r < nb ? ldg(cj + r) : 0.0;
+        }
+#pragma unroll
+        for (int u = 0; u < U; u++)
+            if (r0 + lane + 32 * u < nb) s = fma(vi[u], vj[u], s);
+        for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+        const double f = -tau * s;
+        if (lane == 0) *hj = ldg(hj) + f;
+#pragma unroll
+        for (int u = 0; u < U; u++) {
+            const int r = r0 + lane + 32 * u;
+            if (r < nb) cj[r] = fma(f, vi[u], vj[u]);
+        }
+        return;
+    }
+    for (int r = r0 + lane; r < nb; r += 32) s = fma(ldg(ci + r), ldg(cj + r), s);
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    const double f = -tau * s;
+    if (lane == 0) *hj = ldg(hj) + f;
+    for (int b = r0 + lane; b < nb; b += 32 * U) {
+        double vi[U], vj[U];
+#pragma unroll
+        for (int u = 0; u < U; u++) {
+            const int r = b + 32 * u;
+            vi[u] = r < nb ? ldg(ci + r) : 0.0;
+            vj[u] = r < nb ? ldg(cj + r) : 0.0;
+        }
+#pragma unroll
+        for (int u = 0; u < U; u++) {
+            const int r = b + 32 * u;
+            if (r < nb) cj[r] = fma(f, vi[u], vj[u]);
+        }
+    }
+}
+
 // T (upper, nb x nb, ld) of the forward column-wise compact WY form: T(i,i) = tau_i,
 // T(0:i,i) = -tau_i T(0:i,0:i) z, z_j = <v_j, v_i> for j < i (LAPACK dlarft 'F','C').
 // dot(j, i) is supplied by the caller as a functor evaluated by one warp.
@@ -343,12 +412,7 @@ __device__ void geqrt(const Worker &w, double *A, int nb, int ld, double *Tm, in
         if (ti != 0.0) {
             for (int j = i + 1 + warp; j < nb; j += NT / 32) {
                 double *cj = A + (size_t)j * ld;
-                double s = (lane == 0) ? ldg(cj + i) : 0.0;
-                for (int r = i + 1 + lane; r < nb; r += 32) s = fma(ldg(ci + r), ldg(cj + r), s);
-                for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
-                const double f = -ti * s;
-                if (lane == 0) cj[i] = ldg(cj + i) + f;
-                for (int r = i + 1 + lane; r < nb; r += 32) cj[r] = fma(f, ldg(ci + r), ldg(cj + r));
+                reflect_col(ci, cj, cj + i, i + 1, nb, ti, lane);
             }
         }
         __syncthreads();
@@ -372,16 +436,8 @@ __device__ void tsqrt(const Worker &w, double *A1, double *A2, int nb, int ld, d
         const double ti = larfg(w, A1 + i + (size_t)i * ld, vi, nb);
         if (threadIdx.x == 0) tau[i] = ti;
         if (ti != 0.0) {
-            for (int j = i + 1 + warp; j < nb; j += NT / 32) {
-                double *a1 = A1 + i + (size_t)j * ld;
-                double *cj = A2 + (size_t)j * ld;
-                double s = (lane == 0) ? ldg(a1) : 0.0;
-                for (int r = lane; r < nb; r += 32) s = fma(ldg(vi + r), ldg(cj + r), s);
-                for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
-                const double f = -ti * s;
-                if (lane == 0) *a1 = ldg(a1) + f;
-                for (int r = lane; r < nb; r += 32) cj[r] = fma(f, ldg(vi + r), ldg(cj + r));
-            }
+            for (int j = i + 1 + warp; j < nb; j += NT / 32)
+                reflect_col(vi, A2 + (size_t)j * ld, A1 + i + (size_t)j * ld, 0, nb, ti, lane);
         }
         __syncthreads();
     }

@@ -45,11 +45,13 @@ __device__ __forceinline__ void stage(float (*Xs)[SP], const float *X, int ld, i
 
 // C[M x N] += alpha * op(A) op(B) (beta = 1), dims multiples of 64 / 32.  Ends synced.
 template <bool TA, bool TB>
-__device__ void cta_gemm(int M, int N, int K, float alpha, const float *A, int lda, const float *B, int ldb, float *C,
+__device__ __forceinline__ void cta_gemm(int M, int N, int K, float alpha, const float *A, int lda, const float *B, int ldb, float *C,
                          int ldc, float *smem) {
     float (*As)[SP] = reinterpret_cast<float (*)[SP]>(smem);
     float (*Bs)[SP] = reinterpret_cast<float (*)[SP]>(smem + KC * SP);
-    const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
+    // thread: rows 4*tr .. 4*tr+3 (tr = t % 16, so a warp's 16 row groups are contiguous in a
+    // column of C) and columns 4*tc .. 4*tc+3 (tc = t / 16)
+    const int tr = threadIdx.x & 15, tc = threadIdx.x >> 4;
     for (int i0 = 0; i0 < M; i0 += BM)
         for (int j0 = 0; j0 < N; j0 += BM) {
             float acc[4][4] = {};
@@ -59,8 +61,8 @@ __device__ void cta_gemm(int M, int N, int K, float alpha, const float *A, int l
                 __syncthreads();
 #pragma unroll 8
                 for (int p = 0; p < KC; p++) {
-                    const float4 a = *reinterpret_cast<const float4 *>(&As[p][ty * 4]);
-                    const float4 b = *reinterpret_cast<const float4 *>(&Bs[p][tx * 4]);
+                    const float4 a = *reinterpret_cast<const float4 *>(&As[p][tr * 4]);
+                    const float4 b = *reinterpret_cast<const float4 *>(&Bs[p][tc * 4]);
                     const float av[4] = {a.x, a.y, a.z, a.w}, bv[4] = {b.x, b.y, b.z, b.w};
 #pragma unroll
                     for (int x = 0; x < 4; x++)
@@ -69,54 +71,113 @@ __device__ void cta_gemm(int M, int N, int K, float alpha, const float *A, int l
                 }
                 __syncthreads();
             }
+            // all loads of the output block first (see tile_f64.cuh, cta_gemm); one float4 per
+            // column (ldc and the row offsets are multiples of 4)
+            float4 cv[4];
 #pragma unroll
             for (int y = 0; y < 4; y++)
+                cv[y] = __ldcg(reinterpret_cast<const float4 *>(C + (size_t)(i0 + tr * 4) + (size_t)(j0 + tc * 4 + y) * ldc));
 #pragma unroll
-                for (int x = 0; x < 4; x++) {
-                    float *c = C + (size_t)(i0 + ty * 4 + x) + (size_t)(j0 + tx * 4 + y) * ldc;
-                    *c = fmaf(alpha, acc[x][y], ldg(c));
-                }
+            for (int y = 0; y < 4; y++)
+                *reinterpret_cast<float4 *>(C + (size_t)(i0 + tr * 4) + (size_t)(j0 + tc * 4 + y) * ldc) =
+                    make_float4(fmaf(alpha, acc[0][y], cv[y].x), fmaf(alpha, acc[1][y], cv[y].y),
+                                fmaf(alpha, acc[2][y], cv[y].z), fmaf(alpha, acc[3][y], cv[y].w));
         }
     __syncthreads();
 }
 
-__device__ inline void load_diag64(float (*Ds)[DP], const float *A, int ld) {
+// C[M x 16] += alpha * op(A) B with B K x 16 (element (p, j) at B[p + j*ldb], 16-byte aligned
+// columns): the refinement solves' right-hand-side blocks (at most 16 right-hand sides).
+// Thread t computes row t/4 and columns 4*(t%4)..+3 of each 64-row block.  Ends synced.
+constexpr int RW = 16;       // right-hand-side width of the refinement solves
+constexpr int RP = RW + 4;   // pitch of the staged B chunk
+template <bool TA>
+__device__ __forceinline__ void cta_gemm_rw(int M, int K, float alpha, const float *A, int lda, const float *B, int ldb, float *C,
+                            int ldc, float *smem) {
+    float (*As)[SP] = reinterpret_cast<float (*)[SP]>(smem);
+    float (*Bs)[RP] = reinterpret_cast<float (*)[RP]>(smem + KC * SP);
+    const int tx = threadIdx.x & 3, ty = threadIdx.x >> 2;
+    for (int i0 = 0; i0 < M; i0 += BM) {
+        float acc[4] = {0.f, 0.f, 0.f, 0.f};
+        for (int p0 = 0; p0 < K; p0 += KC) {
+            stage<TA>(As, A, lda, i0, p0);
+            if (threadIdx.x < KC * RW / 4) {
+                const int j = threadIdx.x / (KC / 4), p = (threadIdx.x % (KC / 4)) * 4;
+                const float4 v = __ldcg(reinterpret_cast<const float4 *>(B + (size_t)(p0 + p) + (size_t)j * ldb));
+                Bs[p][j] = v.x;
+                Bs[p + 1][j] = v.y;
+                Bs[p + 2][j] = v.z;
+                Bs[p + 3][j] = v.w;
+            }
+            __syncthreads();
+#pragma unroll 8
+            for (int p = 0; p < KC; p++) {
+                const float a = As[p][ty];
+                const float4 b = *reinterpret_cast<const float4 *>(&Bs[p][tx * 4]);
+                acc[0] = fmaf(a, b.x, acc[0]);
+                acc[1] = fmaf(a, b.y, acc[1]);
+                acc[2] = fmaf(a, b.z, acc[2]);
+                acc[3] = fmaf(a, b.w, acc[3]);
+            }
+            __syncthreads();
+        }
+        float cv[4];
+#pragma unroll
+        for (int y = 0; y < 4; y++) cv[y] = ldg(C + (size_t)(i0 + ty) + (size_t)(tx * 4 + y) * ldc);
+#pragma unroll
+        for (int y = 0; y < 4; y++) C[(size_t)(i0 + ty) + (size_t)(tx * 4 + y) * ldc] = fmaf(alpha, acc[y], cv[y]);
+    }
+    __syncthreads();
+}
+
+__device__ __forceinline__ void load_diag64(float (*Ds)[DP], const float *A, int ld) {
     for (int e = threadIdx.x; e < 4096; e += NT) Ds[e >> 6][e & 63] = ldg(A + (e & 63) + (size_t)(e >> 6) * ld);
     __syncthreads();
 }
 
 // 64 x 64 substitution, triangle in Ds (Ds[c][r] = T(r,c)), right-hand sides B (global, ld):
 //   KIND 0: U^T X = B;  KIND 1: X U = B;  KIND 2: L X = B (unit lower);  KIND 3: U X = B.
+// Threads 0..63 each solve one right-hand side (a column of B; a row for KIND 1) with its 64
+// unknowns in registers, in two halves of 32 (no barrier inside the solve).  Ends synced.
 template <int KIND>
-__device__ void solve64(float (*Ds)[DP], float (*Bs)[DP], float *B, int ld) {
-    for (int e = threadIdx.x; e < 4096; e += NT) Bs[e >> 6][e & 63] = ldg(B + (e & 63) + (size_t)(e >> 6) * ld);
-    __syncthreads();
-    for (int q = 0; q < 64; q++) {
-        const int p = (KIND == 3) ? 63 - q : q;
-        if (KIND == 0 || KIND == 3) {
-            if (threadIdx.x < 64) Bs[threadIdx.x][p] = Bs[threadIdx.x][p] / Ds[p][p];
-            __syncthreads();
-            for (int e = threadIdx.x; e < 4096; e += NT) {
-                const int i = e & 63, c = e >> 6;
-                if (KIND == 0 && i > p) Bs[c][i] = fmaf(-Ds[i][p], Bs[c][p], Bs[c][i]);   // U(p,i)
-                if (KIND == 3 && i < p) Bs[c][i] = fmaf(-Ds[p][i], Bs[c][p], Bs[c][i]);   // U(i,p)
+__device__ __forceinline__ int sub_row(int j) { return KIND == 3 ? 63 - j : j; }  // solve order
+template <int KIND>
+__device__ __forceinline__ float sub_coef(const float (*Ds)[DP], int u, int p) {
+    // coefficient of unknown p in the equation of unknown u
+    return (KIND == 0 || KIND == 1) ? Ds[u][p] : Ds[p][u];
+}
+template <int KIND>
+__device__ __forceinline__ void solve64(float (*Ds)[DP], float *B, int ld) {
+    if (threadIdx.x < 64) {
+        const size_t vstride = (KIND == 1) ? 1 : (size_t)ld;   // between right-hand sides
+        const size_t estride = (KIND == 1) ? (size_t)ld : 1;   // between entries of one
+        float *b = B + (size_t)threadIdx.x * vstride;
+#pragma unroll 1
+        for (int h = 0; h < 64; h += 32) {
+            float x[32];
+#pragma unroll
+            for (int i = 0; i < 32; i++) x[i] = ldg(b + (size_t)sub_row<KIND>(h + i) * estride);
+            if (h) {
+#pragma unroll 4
+                for (int pj = 0; pj < 32; pj++) {
+                    const int pu = sub_row<KIND>(pj);
+                    const float xp = b[(size_t)pu * estride];
+#pragma unroll
+                    for (int i = 0; i < 32; i++) x[i] = fmaf(-sub_coef<KIND>(Ds, sub_row<KIND>(h + i), pu), xp, x[i]);
+                }
             }
-        } else if (KIND == 1) {
-            if (threadIdx.x < 64) Bs[p][threadIdx.x] = Bs[p][threadIdx.x] / Ds[p][p];
-            __syncthreads();
-            for (int e = threadIdx.x; e < 4096; e += NT) {
-                const int r = e & 63, c = e >> 6;
-                if (c > p) Bs[c][r] = fmaf(-Bs[p][r], Ds[c][p], Bs[c][r]);
+#pragma unroll
+            for (int i = 0; i < 32; i++) {
+                const int u = sub_row<KIND>(h + i);
+                float acc = x[i];
+#pragma unroll
+                for (int pi = 0; pi < i; pi++) acc = fmaf(-sub_coef<KIND>(Ds, u, sub_row<KIND>(h + pi)), x[pi], acc);
+                x[i] = (KIND == 2) ? acc : acc / Ds[u][u];
             }
-        } else {
-            for (int e = threadIdx.x; e < 4096; e += NT) {
-                const int i = e & 63, c = e >> 6;
-                if (i > p) Bs[c][i] = fmaf(-Ds[p][i], Bs[c][p], Bs[c][i]);
-            }
+#pragma unroll
+            for (int i = 0; i < 32; i++) b[(size_t)sub_row<KIND>(h + i) * estride] = x[i];
         }
-        __syncthreads();
     }
-    for (int e = threadIdx.x; e < 4096; e += NT) B[(e & 63) + (size_t)(e >> 6) * ld] = Bs[e >> 6][e & 63];
     __syncthreads();
 }
 

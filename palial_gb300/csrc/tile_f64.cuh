@@ -131,6 +131,19 @@ __device__ void cta_gemm(int M, int N, int K, double alpha, const double *A, int
                 }
                 __syncthreads();
             }
+            // all loads of the output block before any store: a load issued after a store the
+            // compiler cannot prove disjoint would wait for a full memory round trip each time
+            double cv[4][4];
+#pragma unroll
+            for (int b = 0; b < 4; b++) {
+                const int j = j0 + tx * 4 + b;
+#pragma unroll
+                for (int a = 0; a < 4; a++) {
+                    const int i = i0 + ty * 4 + a;
+                    const bool skip = (CUP && i > j + coff) || beta == 0.0;
+                    cv[a][b] = skip ? 0.0 : ldg(C + (size_t)i + (size_t)j * ldc);
+                }
+            }
 #pragma unroll
             for (int b = 0; b < 4; b++) {
                 const int j = j0 + tx * 4 + b;
@@ -138,9 +151,8 @@ __device__ void cta_gemm(int M, int N, int K, double alpha, const double *A, int
                 for (int a = 0; a < 4; a++) {
                     const int i = i0 + ty * 4 + a;
                     if (CUP && i > j + coff) continue;
-                    double *cp = C + (size_t)i + (size_t)j * ldc;
                     const double v = alpha * acc[a][b];
-                    *cp = (beta == 0.0) ? v : fma(beta, ldg(cp), v);
+                    C[(size_t)i + (size_t)j * ldc] = (beta == 0.0) ? v : fma(beta, cv[a][b], v);
                 }
             }
         }
@@ -151,11 +163,26 @@ __device__ void cta_gemm(int M, int N, int K, double alpha, const double *A, int
 // Y[M x N] = alpha * X + beta * Y  (column-major, any M, N).  Ends with __syncthreads().
 __device__ inline void cta_axpby(int M, int N, double alpha, const double *X, int ldx, double beta,
                                  double *Y, int ldy) {
-    for (int e = threadIdx.x; e < M * N; e += NT) {
-        const int i = e % M, j = e / M;
-        double *y = Y + (size_t)i + (size_t)j * ldy;
-        const double x = ldg(X + (size_t)i + (size_t)j * ldx);
-        *y = (beta == 0.0) ? alpha * x : fma(alpha, x, beta * ldg(y));
+    // 4 elements per thread per pass, loads before stores
+    for (int e0 = threadIdx.x; e0 < M * N; e0 += 4 * NT) {
+        double xv[4], yv[4];
+#pragma unroll
+        for (int q = 0; q < 4; q++) {
+            const int e = e0 + q * NT;
+            if (e < M * N) {
+                const int i = e % M, j = e / M;
+                xv[q] = ldg(X + (size_t)i + (size_t)j * ldx);
+                yv[q] = beta == 0.0 ? 0.0 : ldg(Y + (size_t)i + (size_t)j * ldy);
+            }
+        }
+#pragma unroll
+        for (int q = 0; q < 4; q++) {
+            const int e = e0 + q * NT;
+            if (e < M * N) {
+                const int i = e % M, j = e / M;
+                Y[(size_t)i + (size_t)j * ldy] = (beta == 0.0) ? alpha * xv[q] : fma(alpha, xv[q], beta * yv[q]);
+            }
+        }
     }
     __syncthreads();
 }
