@@ -35,31 +35,123 @@ __host__ __device__ constexpr int chunk_k(int nb) { return nb <= 512 ? 32 : 16; 
 __host__ __device__ constexpr int smem_floats(int nb) { return 64 * DP + 2 * chunk_k(nb) * (nb - 64) + 64; }
 
 // ---- 64 x 64 diagonal block in shared memory ---------------------------------------------
-// Ds[c][r] = A(r, c).  Thread t owns column q = t / 8 and rows i = t % 8 + 8 j (j < 8) of the
-// block for the trailing updates, so the pivot loop has no index arithmetic.
-// Returns the first failing column (Cholesky) or -1.
-__device__ __forceinline__ int chol64(float (*Ds)[DP]) {
+// Ds[c][r] = A(r, c).  Blocked by 16: the 16 x 16 diagonal block is factored by warp 0 in
+// registers (lane l < 16 holds its column; pivots and factor rows broadcast by shuffles), then
+// the 16-row panel(s) by substitution and the rank-16 update of the rest of the block by all
+// threads (thread t: column q = t / 8, rows i = t % 8 + 8 j).
+constexpr unsigned FULL = 0xffffffffu;
+
+// Cholesky of the 16 x 16 block at (c0, c0) by lanes 0..15 of warp 0 in shared memory (lane l
+// updates column c0 + l; warp-level syncs only).  Returns the first failing pivot or -1
+// (warp-uniform).
+__device__ __forceinline__ int chol16_warp(float (*Ds)[DP], int c0) {
+    const int l = threadIdx.x & 31;
+    float *col = &Ds[c0 + (l & 15)][c0];
+    for (int p = 0; p < 16; p++) {
+        const float d = Ds[c0 + p][c0 + p];
+        if (!(d > 0.f)) return p;
+        const float ri = rsqrtf(d);
+        if (l > p && l < 16) col[p] *= ri;  // U(p, l)
+        __syncwarp();
+        if (l == p) col[p] = d * ri;
+        if (l > p && l < 16) {
+            const float u = col[p];
+            float rv[16], cv[16];
+#pragma unroll
+            for (int i = 0; i < 16; i++) {
+                rv[i] = Ds[c0 + i][c0 + p];  // U(p, i)
+                cv[i] = col[i];
+            }
+#pragma unroll
+            for (int i = 0; i < 16; i++)
+                if (i > p && i <= l) col[i] = fmaf(-rv[i], u, cv[i]);
+        }
+        __syncwarp();
+    }
+    return -1;
+}
+
+// No-pivot LU of the 16 x 16 block at (c0, c0) by lanes 0..15 of warp 0 in shared memory,
+// with the reference's pivot rule; returns 1 if an exact zero pivot was skipped.
+__device__ __forceinline__ int getrf16_warp(float (*Ds)[DP], int c0) {
+    const int l = threadIdx.x & 31;
+    float *col = &Ds[c0 + (l & 15)][c0];
+    float *pcol = nullptr;
+    int zero = 0;
+    for (int p = 0; p < 16; p++) {
+        pcol = &Ds[c0 + p][c0];
+        const float piv = pcol[p];
+        if (piv != 0.f) {
+            // L(i, p) = A(i, p) / piv, lane i scales row i of column p
+            if (l > p && l < 16) pcol[l] = fabsf(piv) > FLT_MIN ? pcol[l] * (1.f / piv) : pcol[l] / piv;
+        } else {
+            zero = 1;
+        }
+        __syncwarp();
+        if (l > p && l < 16) {
+            const float u = col[p];  // U(p, l)
+            float lv[16], cv[16];
+#pragma unroll
+            for (int i = 0; i < 16; i++) {
+                lv[i] = pcol[i];  // L(i, p)
+                cv[i] = col[i];
+            }
+#pragma unroll
+            for (int i = 0; i < 16; i++)
+                if (i > p) col[i] = fmaf(-lv[i], u, cv[i]);
+        }
+        __syncwarp();
+    }
+    return zero;
+}
+
+// Returns the first failing column (Cholesky) or -1.  sflag: one shared int.
+__device__ __forceinline__ int chol64(float (*Ds)[DP], int *sflag) {
     const int q = threadIdx.x >> 3, i0 = threadIdx.x & 7;
-    for (int p = 0; p < 64; p++) {
-        const float d = Ds[p][p];
-        if (!(d > 0.f)) return p;  // every thread reads the same pivot: a uniform decision
-        const float r = sqrtf(d);
-        if (threadIdx.x < 64 && threadIdx.x > p) Ds[threadIdx.x][p] = Ds[threadIdx.x][p] / r;  // U(p, q)
+    for (int c0 = 0; c0 < 64; c0 += 16) {
+        if (threadIdx.x < 32) {
+            const int bad = chol16_warp(Ds, c0);
+            if (threadIdx.x == 0) *sflag = bad;
+        }
         __syncthreads();
-        if (threadIdx.x == 0) Ds[p][p] = r;
-        if (q > p) {
-            // all 16 loads before the 8 stores: one shared-memory round trip per pivot
-            const float uq = Ds[q][p];
-            float lv[8], cv[8];
+        const int bad = *sflag;
+        if (bad >= 0) return c0 + bad;
+        const int c1 = c0 + 16;
+        if (c1 == 64) break;
+        // row panel U(c0:c1, c1:64) = U11^-T A(c0:c1, c1:64), one column per thread
+        if (threadIdx.x < 64 - c1) {
+            const int col = c1 + threadIdx.x;
+            float x[16];
+#pragma unroll
+            for (int i = 0; i < 16; i++) x[i] = Ds[col][c0 + i];
+#pragma unroll
+            for (int p = 0; p < 16; p++) {
+                x[p] = x[p] / Ds[c0 + p][c0 + p];
+#pragma unroll
+                for (int i = p + 1; i < 16; i++) x[i] = fmaf(-Ds[c0 + i][c0 + p], x[p], x[i]);  // U(p,i)
+            }
+#pragma unroll
+            for (int i = 0; i < 16; i++) Ds[col][c0 + i] = x[i];
+        }
+        __syncthreads();
+        // A(i, q) -= U(c0:c1, i)^T U(c0:c1, q), c1 <= i <= q
+        if (q >= c1) {
+            float uq[16];
+#pragma unroll
+            for (int k = 0; k < 16; k++) uq[k] = Ds[q][c0 + k];
+            float out[8];
 #pragma unroll
             for (int j = 0; j < 8; j++) {
-                lv[j] = Ds[i0 + 8 * j][p];
-                cv[j] = Ds[q][i0 + 8 * j];
+                const int i = i0 + 8 * j;
+                float a = Ds[q][i];
+#pragma unroll
+                for (int k = 0; k < 16; k++) a = fmaf(-Ds[i][c0 + k], uq[k], a);
+                out[j] = a;
             }
 #pragma unroll
             for (int j = 0; j < 8; j++) {
                 const int i = i0 + 8 * j;
-                if (i > p && i <= q) Ds[q][i] = fmaf(-lv[j], uq, cv[j]);  // A(i,q) -= U(p,i) U(p,q)
+                if (i >= c1 && i <= q) Ds[q][i] = out[j];
             }
         }
         __syncthreads();
@@ -68,32 +160,65 @@ __device__ __forceinline__ int chol64(float (*Ds)[DP]) {
 }
 
 // No-pivot LU of the block; returns 1 if an exact zero pivot was skipped.
-__device__ __forceinline__ int getrf64(float (*Ds)[DP]) {
+__device__ __forceinline__ int getrf64(float (*Ds)[DP], int *sflag) {
     const int q = threadIdx.x >> 3, i0 = threadIdx.x & 7;
     int zero = 0;
-    for (int p = 0; p < 64; p++) {
-        const float piv = Ds[p][p];
-        if (piv != 0.f) {
-            if (threadIdx.x < 64 && threadIdx.x > p) {
-                const float x = Ds[p][threadIdx.x];  // L(i, p) = A(i, p) / piv
-                Ds[p][threadIdx.x] = fabsf(piv) > FLT_MIN ? x * (1.f / piv) : x / piv;
-            }
-        } else {
-            zero = 1;
+    for (int c0 = 0; c0 < 64; c0 += 16) {
+        if (threadIdx.x < 32) {
+            const int z = getrf16_warp(Ds, c0);
+            if (threadIdx.x == 0) *sflag = z;
         }
         __syncthreads();
-        if (q > p) {
-            const float up = Ds[q][p];  // U(p, q)
-            float lv[8], cv[8];
+        zero |= *sflag;
+        const int c1 = c0 + 16;
+        if (c1 == 64) break;
+        if (threadIdx.x < 64 - c1) {
+            // row panel U(c0:c1, col) = L11^-1 A(c0:c1, col) (unit lower)
+            const int col = c1 + threadIdx.x;
+            float x[16];
+#pragma unroll
+            for (int i = 0; i < 16; i++) x[i] = Ds[col][c0 + i];
+#pragma unroll
+            for (int p = 0; p < 16; p++)
+#pragma unroll
+                for (int i = p + 1; i < 16; i++) x[i] = fmaf(-Ds[c0 + p][c0 + i], x[p], x[i]);  // L(i,p)
+#pragma unroll
+            for (int i = 0; i < 16; i++) Ds[col][c0 + i] = x[i];
+        } else if (threadIdx.x >= 64 && threadIdx.x < 128 - c1) {
+            // column panel L(row, c0:c1) = A(row, c0:c1) U11^-1, the reference's pivot rule
+            const int row = c1 + threadIdx.x - 64;
+            float x[16];
+#pragma unroll
+            for (int k = 0; k < 16; k++) x[k] = Ds[c0 + k][row];
+#pragma unroll
+            for (int p = 0; p < 16; p++) {
+                const float u = Ds[c0 + p][c0 + p];
+                if (u != 0.f) x[p] = fabsf(u) > FLT_MIN ? x[p] * (1.f / u) : x[p] / u;
+#pragma unroll
+                for (int k = p + 1; k < 16; k++) x[k] = fmaf(-x[p], Ds[c0 + k][c0 + p], x[k]);  // U(p,k)
+            }
+#pragma unroll
+            for (int k = 0; k < 16; k++) Ds[c0 + k][row] = x[k];
+        }
+        __syncthreads();
+        // A(i, q) -= L(i, c0:c1) U(c0:c1, q), i, q >= c1
+        if (q >= c1) {
+            float uq[16];
+#pragma unroll
+            for (int k = 0; k < 16; k++) uq[k] = Ds[q][c0 + k];
+            float out[8];
 #pragma unroll
             for (int j = 0; j < 8; j++) {
-                lv[j] = Ds[p][i0 + 8 * j];
-                cv[j] = Ds[q][i0 + 8 * j];
+                const int i = i0 + 8 * j;
+                float a = Ds[q][i];
+#pragma unroll
+                for (int k = 0; k < 16; k++) a = fmaf(-Ds[c0 + k][i], uq[k], a);
+                out[j] = a;
             }
 #pragma unroll
             for (int j = 0; j < 8; j++) {
                 const int i = i0 + 8 * j;
-                if (i > p) Ds[q][i] = fmaf(-lv[j], up, cv[j]);  // A(i,q) -= L(i,p) U(p,q)
+                if (i >= c1) Ds[q][i] = out[j];
             }
         }
         __syncthreads();
@@ -239,6 +364,7 @@ __global__ void __launch_bounds__(NT, 1) diag_factor_kernel(float *T, int nb, in
     const int kc = chunk_k(nb);
     float *As = smem + 64 * DP;
     float *Bs = As + (size_t)kc * (nb - 64);
+    int *sflag = reinterpret_cast<int *>(Bs + (size_t)kc * (nb - 64));
     if (ld_volatile(status + ST_CODE) != 0) return;
     if (threadIdx.x == 0) status[6] = k;  // current step (error reports of later kernels)
     int zero = 0;
@@ -247,7 +373,7 @@ __global__ void __launch_bounds__(NT, 1) diag_factor_kernel(float *T, int nb, in
         for (int e = threadIdx.x; e < 4096; e += NT) Ds[e >> 6][e & 63] = D[(e & 63) + (size_t)(e >> 6) * nb];
         __syncthreads();
         if (ALG == 0) {
-            const int bad = chol64(Ds);
+            const int bad = chol64(Ds, sflag);
             if (bad >= 0) {
                 if (threadIdx.x == 0 && atomicCAS(status + ST_CODE, 0, -3 /*PALIAL_ERR_NOT_SPD*/) == 0) {
                     status[ST_COL] = j0 + bad;
@@ -258,7 +384,7 @@ __global__ void __launch_bounds__(NT, 1) diag_factor_kernel(float *T, int nb, in
                 return;
             }
         } else {
-            zero |= getrf64(Ds);
+            zero |= getrf64(Ds, sflag);
         }
         for (int e = threadIdx.x; e < 4096; e += NT) {
             const int r = e & 63, c = e >> 6;
