@@ -135,13 +135,22 @@ int palial_gpu_factor_dev(int alg, double *dA, double *dS, int n, int nb, const 
  * FP64.  Iterates until the normwise backward error max_j |r_j|/(|A| |x_j| + |b_j|) (inf-
  * norms) <= opts->ir_tol (default 1e-14 * n); GMRES-IR when plain refinement stagnates
  * (opts->gmres: -1 never, 0 automatic, 1 always).  NB must be a multiple of 256.
- * Returns PALIAL_ERR_NOT_CONVERGED (with the reached error in st) if the target is missed. */
+ * Returns PALIAL_ERR_NOT_CONVERGED (with the reached error in st) if the target is missed.
+ * The refinement steers with a compensated-FP32 residual (operands split into 48-bit FP32
+ * pairs, error-free products and sums, FP64 accumulation every 64 terms) and confirms
+ * convergence with an FP64 residual, so the reported backward error is an FP64 one;
+ * opts->reserved[4] = 1 computes every residual in FP64. */
 int palial_gpu_solve_ir(int alg, const double *dA, int n, int nb, const double *dB, double *dX,
                         int nrhs, const palial_opts *opts, palial_status *st, void *stream);
 /* Same with host buffers: A in the reference's tile layout (descriptor), B and X n x nrhs
  * column-major in host memory; includes the host<->device copies. */
 int palial_gpu_solve_ir_host(int alg, const palial_desc *A, const double *B, double *X, int nrhs,
                              const palial_opts *opts, palial_status *st);
+/* R = B - A X (B may be NULL: R = A X) on device buffers, A an FP64 tile matrix, X, B, R
+ * n x nrhs column-major (nrhs <= 16): mode 0 in FP64, mode 1 with the compensated FP32
+ * arithmetic the refinement steers with. */
+int palial_gpu_residual(const double *dA, int n, int nb, const double *dX, const double *dB, double *dR, int nrhs,
+                        int mode, void *stream);
 /* The low-precision factorization alone: dW (n*n floats, tile layout) receives the FP32
  * factors (Cholesky: U in the upper tiles; LU: L\U). */
 int palial_gpu_mp_factor(int alg, const double *dA, float *dW, int n, int nb,

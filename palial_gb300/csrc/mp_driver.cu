@@ -35,7 +35,10 @@ cudaError_t mp_pack_rows(int mode, const float *W, int n, int nb, int k, void *h
                          cudaStream_t s);
 cudaError_t mp_pack_cols(int mode, const float *W, int n, int nb, int k, void *hi, void *lo, float *scales,
                          cudaStream_t s);
-cudaError_t mps_f64_to_f32(const double *A, float *W, int n, int nb, double shift, cudaStream_t s);
+cudaError_t mps_f64_to_f32(const double *A, float *W, int n, int nb, double shift, cudaStream_t s,
+                           double *amax = nullptr);
+cudaError_t mps_residual_df(const double *A, int n, int nb, const double *X, const double *colmax, const double *B,
+                            double *R, int nrhs, int sigma, float2 *Xs, int *tau, double *amax, cudaStream_t s);
 cudaError_t mps_tile_to_f64(const float *w, double *d, int nb, cudaStream_t s);
 cudaError_t mps_tile_to_f32(const double *d, float *w, int nb, int upper_only, cudaStream_t s);
 cudaError_t mps_panel_trsm(float *W, int n, int nb, int k, int kind, cudaStream_t s);
@@ -71,6 +74,7 @@ namespace {
 
 struct MpBufs {
     DevBuf w, diag, pa_hi, pa_lo, pb_hi, pb_lo, scales, r, r32, x32, norms, work, krylov, hbuf, gvec;
+    DevBuf xsplit;  // compensated residual: X as FP32 pairs (n x 16 float2) + 16 scale exponents
     DevBuf dinv_u, dinv_l, stile;  // FP32 inverses of the diagonal factor tiles, solve scratch
 };
 MpBufs mb;
@@ -437,8 +441,9 @@ static int solve_one(int alg, const double *dA, int n, int nb, const double *dB,
         }
         PALIAL_CK(mps_f64_to_f32(g.mat.as<double>(), W, n, nb, 0.0, s), "factor to f32");
     } else {
+        PALIAL_CK(cudaMemsetAsync(nrm + 120, 0, sizeof(double), s), "max |a|");
         for (int attempt = 0; attempt < 4; attempt++) {
-            PALIAL_CK(mps_f64_to_f32(dA, W, n, nb, shift, s), "convert");
+            PALIAL_CK(mps_f64_to_f32(dA, W, n, nb, shift, s, attempt == 0 ? nrm + 120 : nullptr), "convert");
             rc = mp_factor(alg, prec, W, n, nb, s, st, &zp);
             if (rc != PALIAL_ERR_NOT_SPD || alg != 0) break;
             if (anorm < 0) {
@@ -454,7 +459,20 @@ static int solve_one(int alg, const double *dA, int n, int nb, const double *dB,
     }
     rc = mp_prepare_solves(alg, W, n, nb, s, st);
     if (rc) return rc;
+    // The refinement steers with a compensated-FP32 residual (48-bit operands, error-free
+    // products and sums, FP64 chunk accumulation; about 5x faster than the FP64 pipe) and
+    // confirms convergence with the FP64 residual, so the reported error is an FP64 one.
+    // opts.reserved[4] = 1 keeps every residual in FP64.
+    double amax = 0.0;
+    if (prec != PALIAL_PREC_FP64) PALIAL_CK(cudaMemcpyAsync(&amax, nrm + 120, sizeof(double), cudaMemcpyDeviceToHost, s), "max |a|");
     PALIAL_CK(cudaStreamSynchronize(s), "factorization");
+    const bool use_df = prec != PALIAL_PREC_FP64 && o.reserved[4] != 1 && std::isfinite(amax) && amax > 0.0;
+    int sigma = 0;
+    if (use_df) {
+        std::frexp(amax, &sigma);
+        PALIAL_CK(mb.xsplit.ensure(sizeof(float2) * (size_t)n * 16 + 64), "alloc split x");
+    }
+    bool fp64_phase = false;
     const double fsec = std::chrono::duration<double>(std::chrono::steady_clock::now() - f0).count();
     // ---- refinement -------------------------------------------------------------------------
     const double tol = o.ir_tol > 0 ? o.ir_tol : 1e-14 * n;
@@ -492,12 +510,20 @@ static int solve_one(int alg, const double *dA, int n, int nb, const double *dB,
             PALIAL_CK(cudaMemcpyAsync(nrm + 80, ones.data(), sizeof(double) * nrhs, cudaMemcpyHostToDevice, s), "one");
             PALIAL_CK(mps_multi_axpy(dcorr, 1, nrm + 80, dX, n, nrhs, 0, s), "x += d");
         }
+        PALIAL_CK(mps_colmax(dX, n, nrhs, nrm + 33, s), "norm x");
         const bool need_norm = anorm < 0;
         if (need_norm) PALIAL_CK(cudaMemsetAsync(nrm, 0, sizeof(double), s), "norm A");
-        PALIAL_CK(mps_residual(dA, n, nb, dX, dB, mb.r.as<double>(), nrhs, need_norm ? nrm : nullptr, s), "residual");
+        const bool used_df = use_df && !fp64_phase;
+        if (used_df) {
+            float2 *xs = mb.xsplit.as<float2>();
+            PALIAL_CK(mps_residual_df(dA, n, nb, dX, nrm + 33, dB, mb.r.as<double>(), nrhs, sigma, xs,
+                                      reinterpret_cast<int *>(xs + (size_t)n * 16), need_norm ? nrm : nullptr, s),
+                      "residual (compensated FP32)");
+        } else {
+            PALIAL_CK(mps_residual(dA, n, nb, dX, dB, mb.r.as<double>(), nrhs, need_norm ? nrm : nullptr, s), "residual");
+        }
         if (need_norm) PALIAL_CK(cudaMemcpyAsync(&anorm, nrm, sizeof(double), cudaMemcpyDeviceToHost, s), "norm A");
         PALIAL_CK(mps_colmax(mb.r.as<double>(), n, nrhs, nrm + 17, s), "norm r");
-        PALIAL_CK(mps_colmax(dX, n, nrhs, nrm + 33, s), "norm x");
         PALIAL_CK(cudaMemcpyAsync(hr.data(), nrm + 17, sizeof(double) * nrhs, cudaMemcpyDeviceToHost, s), "norm r");
         PALIAL_CK(cudaMemcpyAsync(hx.data(), nrm + 33, sizeof(double) * nrhs, cudaMemcpyDeviceToHost, s), "norm x");
         PALIAL_CK(cudaStreamSynchronize(s), "iteration");
@@ -510,6 +536,23 @@ static int solve_one(int alg, const double *dA, int n, int nb, const double *dB,
         if (!finite || !std::isfinite(eta)) {
             eta = INFINITY;
             break;
+        }
+        if (eta <= tol && used_df) {
+            // confirm with the FP64 residual; if the compensated residual's floor misled, go on in FP64
+            PALIAL_CK(mps_residual(dA, n, nb, dX, dB, mb.r.as<double>(), nrhs, nullptr, s), "residual");
+            PALIAL_CK(mps_colmax(mb.r.as<double>(), n, nrhs, nrm + 17, s), "norm r");
+            PALIAL_CK(cudaMemcpyAsync(hr.data(), nrm + 17, sizeof(double) * nrhs, cudaMemcpyDeviceToHost, s), "norm r");
+            PALIAL_CK(cudaStreamSynchronize(s), "confirmation");
+            eta = 0.0;
+            for (int j = 0; j < nrhs; j++) {
+                finite = finite && std::isfinite(hr[j]);
+                eta = std::max(eta, hr[j] / (anorm * hx[j] + hb[j]));
+            }
+            if (!finite || !std::isfinite(eta)) {
+                eta = INFINITY;
+                break;
+            }
+            fp64_phase = true;
         }
         if (eta <= tol) {
             converged = true;
@@ -578,6 +621,40 @@ extern "C" int palial_gpu_solve_ir(int alg, const double *dA, int n, int nb, con
         st->kappa_est = (double)used;  // precision that produced the result (PALIAL_PREC_*)
     }
     return rc;
+}
+
+// R = B - A X on device buffers (B may be NULL: R = A X), FP64 (mode 0) or compensated FP32
+// (mode 1, the refinement's steering residual); nrhs <= 16.
+extern "C" int palial_gpu_residual(const double *dA, int n, int nb, const double *dX, const double *dB, double *dR,
+                                   int nrhs, int mode, void *stream) {
+    if (!dA || !dX || !dR || n <= 0 || nb <= 0 || n % nb || n % 64 || nrhs < 1 || nrhs > 16 || (mode != 0 && mode != 1))
+        return PALIAL_ERR_ARG;
+    palial_status st0;
+    palial_status *st = &st0;
+    int rc = ensure_init(st);
+    if (rc) return rc;
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    if (mode == 0) {
+        PALIAL_CK(mps_residual(dA, n, nb, dX, dB, dR, nrhs, nullptr, s), "residual");
+        return PALIAL_OK;
+    }
+    PALIAL_CK(mb.norms.ensure(sizeof(double) * 128), "alloc norms");
+    PALIAL_CK(mb.xsplit.ensure(sizeof(float2) * (size_t)n * 16 + 64), "alloc split x");
+    double *nrm = mb.norms.as<double>();
+    PALIAL_CK(cudaMemsetAsync(nrm + 120, 0, sizeof(double), s), "max |a|");
+    PALIAL_CK(mb.w.ensure(sizeof(float) * (size_t)n * n), "alloc W");
+    PALIAL_CK(mps_f64_to_f32(dA, mb.w.as<float>(), n, nb, 0.0, s, nrm + 120), "max |a|");
+    double amax = 0;
+    PALIAL_CK(cudaMemcpyAsync(&amax, nrm + 120, sizeof(double), cudaMemcpyDeviceToHost, s), "max |a|");
+    PALIAL_CK(cudaStreamSynchronize(s), "max |a|");
+    int sigma = 0;
+    std::frexp(amax, &sigma);
+    PALIAL_CK(mps_colmax(dX, n, nrhs, nrm + 33, s), "norm x");
+    float2 *xs = mb.xsplit.as<float2>();
+    PALIAL_CK(mps_residual_df(dA, n, nb, dX, nrm + 33, dB, dR, nrhs, sigma, xs, reinterpret_cast<int *>(xs + (size_t)n * 16),
+                              nullptr, s),
+              "residual");
+    return PALIAL_OK;
 }
 
 // Host-buffer variant (A: reference tile descriptor in host memory; B, X: n x nrhs host,

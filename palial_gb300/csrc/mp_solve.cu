@@ -21,16 +21,152 @@ __device__ __forceinline__ size_t tile_off(int n, int nb, int tm, int tn) {
 }
 
 // ---- conversions --------------------------------------------------------------------------
-__global__ void f64_to_f32_kernel(const double *a, float *w, long long len, double shift_diag, int n, int nb) {
+// W = float(A (+ shift on the diagonal)); amax (optional, zeroed by the caller) receives
+// max |a_ij| of the unshifted A (atomicMax on the bit pattern, NaN propagating).
+__global__ void f64_to_f32_kernel(const double *a, float *w, long long len, double shift_diag, int n, int nb,
+                                  double *amax) {
     const int mt = n / nb;
+    double mx = 0.0;
     for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < len; e += (long long)gridDim.x * blockDim.x) {
         double v = a[e];
+        const double av = fabs(v);
+        mx = (av > mx || av != av) ? av : mx;
         if (shift_diag != 0.0) {
             const long long t = e / ((long long)nb * nb);
             const int in = (int)(e - t * (long long)nb * nb);
             if ((t % mt) == (t / mt) && (in % nb) == (in / nb)) v += shift_diag;
         }
         w[e] = (float)v;
+    }
+    if (amax) {
+        for (int o = 16; o; o >>= 1) {
+            const double y = __shfl_xor_sync(0xffffffffu, mx, o);
+            mx = (y > mx || y != y) ? y : mx;
+        }
+        if ((threadIdx.x & 31) == 0)
+            atomicMax(reinterpret_cast<unsigned long long *>(amax), (unsigned long long)__double_as_longlong(mx));
+    }
+}
+
+// ---- compensated FP32 residual -------------------------------------------------------------
+// Operands as pairs of FP32 numbers: v * 2^-sc = hi + lo with hi the top 24 bits of the
+// significand and lo the next 29 rounded to 24 (48 bits in all), taken from the bit pattern
+// with integer operations (no FP64 arithmetic).  Values below 2^-100 relative to the scale
+// flush gradually (their contribution is below 2^-124 of the largest entry).  Inf/NaN -> NaN.
+__device__ __forceinline__ float pow2f(int k) {  // 2^k for k >= -126 (else 0)
+    return k < -126 ? 0.f : __int_as_float((k + 127) << 23);
+}
+__device__ __forceinline__ float2 split_df(double v, int sc) {
+    const unsigned long long bits = (unsigned long long)__double_as_longlong(v);
+    const int E = (int)((bits >> 52) & 0x7FF);
+    if (E == 0x7FF) return make_float2(__int_as_float(0x7fc00000), 0.f);
+    const unsigned long long M = (bits & ((1ull << 52) - 1)) | (E ? (1ull << 52) : 0ull);
+    const int e2 = (E ? E : 1) - 1075 - sc;  // v * 2^-sc = M * 2^e2
+    float hi = __fmul_rn(__uint2float_rn((unsigned)(M >> 29)), pow2f(e2 + 29));
+    float lo = __fmul_rn(__uint2float_rn((unsigned)(M & ((1ull << 29) - 1))), pow2f(e2));
+    if (bits >> 63) {
+        hi = -hi;
+        lo = -lo;
+    }
+    return make_float2(hi, lo);
+}
+
+// Xs (n x 16 float2, rhs-minor: Xs[r * 16 + c]) = split(X(r, c) * 2^-tau_c), tau_c the
+// exponent of the column's max |x| (colmax from mps_colmax), zero beyond nrhs.
+__global__ void split_x_kernel(const double *X, long long n, int nrhs, const double *colmax, float2 *Xs, int *tau) {
+    const long long total = n * 16;
+    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < total; e += (long long)gridDim.x * blockDim.x) {
+        const int c = (int)(e & 15);
+        const long long r = e >> 4;
+        int t = 0;
+        if (c < nrhs) frexp(colmax[c], &t);
+        Xs[e] = (c < nrhs) ? split_df(X[(size_t)r + (size_t)c * n], t) : make_float2(0.f, 0.f);
+        if (r == 0) tau[c] = t;
+    }
+}
+
+// R = B - A X with A and X as FP32 pairs: per product the exact FP32 product of the high parts
+// (fma), the cross terms into its error, and a TwoSum accumulation (Knuth) of the pair; every
+// 64 products the pair is added to an FP64 accumulator.  Same layout as residual_kernel (one
+// CTA per 32-row block, thread = row x 2 right-hand sides).  amax as there (row sums of |a|).
+__global__ void __launch_bounds__(256) residual_df_kernel(const double *A, int n, int nb, const float2 *Xs,
+                                                          const int *tau, int sigma, const double *B, double *R,
+                                                          int nrhs, double *amax) {
+    __shared__ float2 As[64][33];
+    __shared__ float4 Xp[64][8];  // (hi, lo) of right-hand sides 2g, 2g+1
+    __shared__ float part[8][33];
+    const int i0 = blockIdx.x * 32;
+    const int row = threadIdx.x & 31, grp = threadIdx.x >> 5;
+    double acc0 = 0.0, acc1 = 0.0;
+    float asum = 0.f;
+    const int mt = n / nb;
+    const double *tilerow = A + (size_t)nb * nb * (size_t)(i0 / nb) + (size_t)(i0 % nb);
+    for (int p0 = 0; p0 < n; p0 += 64) {
+        const double *blk = tilerow + (size_t)nb * nb * (size_t)mt * (p0 / nb) + (size_t)(p0 % nb) * nb;
+        for (int e = threadIdx.x; e < 2048; e += 256) {
+            const double v = blk[(e & 31) + (size_t)(e >> 5) * nb];
+            As[e >> 5][e & 31] = split_df(v, sigma);
+        }
+        for (int e = threadIdx.x; e < 64 * 8; e += 256) {
+            const float2 a = Xs[(size_t)(p0 + (e >> 3)) * 16 + 2 * (e & 7)];
+            const float2 b = Xs[(size_t)(p0 + (e >> 3)) * 16 + 2 * (e & 7) + 1];
+            Xp[e >> 3][e & 7] = make_float4(a.x, a.y, b.x, b.y);
+        }
+        __syncthreads();
+        if (amax) {
+#pragma unroll
+            for (int p = grp; p < 64; p += 8) {
+                const float2 a = As[p][row];
+                asum += fabsf(a.x + a.y);
+            }
+        }
+        float s0 = 0.f, c0 = 0.f, s1 = 0.f, c1 = 0.f;
+#pragma unroll 4
+        for (int p = 0; p < 64; p++) {
+            const float2 a = As[p][row];
+            const float4 x = Xp[p][grp];
+            // explicit _rn intrinsics: no FMA contraction may touch the error-free steps
+            {
+                const float pr = __fmul_rn(a.x, x.x);
+                const float t = fmaf(a.x, x.y, fmaf(a.y, x.x, fmaf(a.x, x.x, -pr)));
+                const float sn = __fadd_rn(s0, pr), bp = __fsub_rn(sn, s0);
+                c0 = __fadd_rn(c0, __fadd_rn(__fadd_rn(__fsub_rn(s0, __fsub_rn(sn, bp)), __fsub_rn(pr, bp)), t));
+                s0 = sn;
+            }
+            {
+                const float pr = __fmul_rn(a.x, x.z);
+                const float t = fmaf(a.x, x.w, fmaf(a.y, x.z, fmaf(a.x, x.z, -pr)));
+                const float sn = __fadd_rn(s1, pr), bp = __fsub_rn(sn, s1);
+                c1 = __fadd_rn(c1, __fadd_rn(__fadd_rn(__fsub_rn(s1, __fsub_rn(sn, bp)), __fsub_rn(pr, bp)), t));
+                s1 = sn;
+            }
+        }
+        acc0 += (double)s0 + (double)c0;
+        acc1 += (double)s1 + (double)c1;
+        __syncthreads();
+    }
+    const double accs[2] = {acc0, acc1};
+#pragma unroll
+    for (int j = 0; j < 2; j++) {
+        const int c = 2 * grp + j;
+        if (c < nrhs) {
+            const size_t o = (size_t)(i0 + row) + (size_t)c * n;
+            const double ax = ldexp(accs[j], sigma + tau[c]);
+            R[o] = B ? B[o] - ax : ax;
+        }
+    }
+    if (amax) {
+        part[grp][row] = asum;
+        __syncthreads();
+        if (threadIdx.x < 32) {
+            double t = 0.0;
+#pragma unroll
+            for (int g = 0; g < 8; g++) t += (double)part[g][row];
+            t = ldexp(t, sigma);
+            for (int o = 16; o; o >>= 1) t = fmax(t, __shfl_xor_sync(0xffffffffu, t, o));
+            if (threadIdx.x == 0)
+                atomicMax(reinterpret_cast<unsigned long long *>(amax), (unsigned long long)__double_as_longlong(t));
+        }
     }
 }
 
@@ -398,9 +534,21 @@ cudaError_t mps_configure() {
     return e;
 }
 
-cudaError_t mps_f64_to_f32(const double *A, float *W, int n, int nb, double shift, cudaStream_t s) {
+cudaError_t mps_f64_to_f32(const double *A, float *W, int n, int nb, double shift, cudaStream_t s, double *amax) {
     note_launch();
-    mps::f64_to_f32_kernel<<<4096, 256, 0, s>>>(A, W, (long long)n * n, shift, n, nb);
+    mps::f64_to_f32_kernel<<<4096, 256, 0, s>>>(A, W, (long long)n * n, shift, n, nb, amax);
+    return cudaGetLastError();
+}
+// R = B - A X in compensated FP32 (see residual_df_kernel); sigma: |a_ij| < 2^sigma for all
+// entries.  Xs (n x 16 float2) and tau (16 ints) are scratch; colmax = per-column max |x|.
+cudaError_t mps_residual_df(const double *A, int n, int nb, const double *X, const double *colmax, const double *B,
+                            double *R, int nrhs, int sigma, float2 *Xs, int *tau, double *amax, cudaStream_t s) {
+    note_launch();
+    mps::split_x_kernel<<<1024, 256, 0, s>>>(X, n, nrhs, colmax, Xs, tau);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    note_launch();
+    mps::residual_df_kernel<<<n / 32, 256, 0, s>>>(A, n, nb, Xs, tau, sigma, B, R, nrhs, amax);
     return cudaGetLastError();
 }
 cudaError_t mps_tile_to_f64(const float *w, double *d, int nb, cudaStream_t s) {

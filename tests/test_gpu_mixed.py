@@ -179,3 +179,55 @@ def test_fp32_diagonal_tile_reports_breakdown():
     dw = torch.zeros(n * n, dtype=torch.float32, device="cuda")
     with pytest.raises(P.PalialError):
         P.mp_factor("cholesky", da.data_ptr(), dw.data_ptr(), n, nb, precision="bf16")
+
+
+@pytest.mark.parametrize("kind", ["spd", "kappa"])
+def test_compensated_residual_matches_fp64(kind):
+    """The refinement's steering residual (compensated FP32, 48-bit operands) against a torch
+    FP64 product: normwise error <= 1e-12 of |A||x| scale; the FP64 mode against torch <= 1e-14."""
+    import ctypes
+    n, nb, nrhs = 4096, 512, 16
+    da = torch.empty(n * n, dtype=torch.float64, device="cuda")
+    if kind == "spd":
+        P.gen_spd(da.data_ptr(), n, nb, 0)
+    else:
+        P.gen_kappa(da.data_ptr(), n, nb, 1e8, False, seed=3)
+    x = torch.rand(nrhs, n, dtype=torch.float64, device="cuda", generator=torch.Generator("cuda").manual_seed(1)) - 0.5
+    x[3] *= 1e-9  # a column of very different scale
+    b = torch.rand(nrhs, n, dtype=torch.float64, device="cuda", generator=torch.Generator("cuda").manual_seed(2))
+    mt = n // nb
+    A = da.view(mt, mt, nb, nb).permute(1, 3, 0, 2).reshape(n, n)
+    ref = b.t() - A @ x.t()
+    scale = (A.abs() @ x.t().abs()).max(dim=0).values + b.t().abs().max(dim=0).values
+    lib = P.lib()
+    lib.palial_gpu_residual.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p,
+                                        ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_void_p]
+    for mode, bound in ((0, 1e-14), (1, 1e-12)):
+        r = torch.zeros(nrhs, n, dtype=torch.float64, device="cuda")
+        assert lib.palial_gpu_residual(da.data_ptr(), n, nb, x.data_ptr(), b.data_ptr(), r.data_ptr(), nrhs, mode,
+                                       None) == 0
+        torch.cuda.synchronize()
+        err = ((r.t() - ref).abs().max(dim=0).values / scale).max().item()
+        assert err <= bound, (mode, err)
+
+
+def test_refinement_with_compensated_residual_reports_fp64_error():
+    """Steering with the compensated residual and confirming in FP64 gives the same solution
+    quality as FP64 residuals throughout (backward errors of both at the FP64 target)."""
+    n, nb, nrhs = 4096, 512, 8
+    a = O.gen_spd(0, n)
+    b = O.gen_uniform(5, n, nrhs, stream=O.STREAM_RHS)
+    da = torch.from_numpy(O.to_tiles(a, nb)).cuda()
+    db = torch.from_numpy(np.asfortranarray(b).ravel(order="F")).cuda()
+    xs = []
+    for r4 in (0, 1):
+        dx = torch.zeros_like(db)
+        o = P.make_opts(precision="bf16")
+        o.reserved[4] = r4
+        import ctypes
+        st = P.Status()
+        rc = P.lib().palial_gpu_solve_ir(0, da.data_ptr(), n, nb, db.data_ptr(), dx.data_ptr(), nrhs, ctypes.byref(o),
+                                         ctypes.byref(st), None)
+        assert rc == 0 and st.backward_error <= 1e-14 * n, (r4, rc, st.backward_error)
+        xs.append(dx.cpu().numpy())
+    assert np.linalg.norm(xs[0] - xs[1]) / np.linalg.norm(xs[1]) < 1e-11
