@@ -137,9 +137,10 @@ int palial_gpu_factor_dev(int alg, double *dA, double *dS, int n, int nb, const 
  * (opts->gmres: -1 never, 0 automatic, 1 always).  NB must be a multiple of 256.
  * Returns PALIAL_ERR_NOT_CONVERGED (with the reached error in st) if the target is missed.
  * The refinement steers with a compensated-FP32 residual (operands split into 48-bit FP32
- * pairs, error-free products and sums, FP64 accumulation every 64 terms) and confirms
- * convergence with an FP64 residual, so the reported backward error is an FP64 one;
- * opts->reserved[4] = 1 computes every residual in FP64. */
+ * pairs, error-free products and sums, FP64 accumulation every 64 terms; its error is below
+ * 1e-12 of the backward error's scale).  When the tolerance is below 1e-11 (or
+ * opts->reserved[4] = 2) convergence is confirmed with an FP64 residual; opts->reserved[4] =
+ * 1 computes every residual in FP64. */
 int palial_gpu_solve_ir(int alg, const double *dA, int n, int nb, const double *dB, double *dX,
                         int nrhs, const palial_opts *opts, palial_status *st, void *stream);
 /* Same with host buffers: A in the reference's tile layout (descriptor), B and X n x nrhs

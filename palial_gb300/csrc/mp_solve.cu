@@ -26,11 +26,13 @@ __device__ __forceinline__ size_t tile_off(int n, int nb, int tm, int tn) {
 __global__ void f64_to_f32_kernel(const double *a, float *w, long long len, double shift_diag, int n, int nb,
                                   double *amax) {
     const int mt = n / nb;
-    double mx = 0.0;
+    // max |a| on the bit patterns (integer compares; for non-negative doubles the unsigned
+    // order is the value order, and a NaN's pattern exceeds every finite one)
+    unsigned long long mx = 0;
     for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < len; e += (long long)gridDim.x * blockDim.x) {
         double v = a[e];
-        const double av = fabs(v);
-        mx = (av > mx || av != av) ? av : mx;
+        const unsigned long long ab = (unsigned long long)__double_as_longlong(v) & 0x7FFFFFFFFFFFFFFFull;
+        mx = ab > mx ? ab : mx;
         if (shift_diag != 0.0) {
             const long long t = e / ((long long)nb * nb);
             const int in = (int)(e - t * (long long)nb * nb);
@@ -40,11 +42,10 @@ __global__ void f64_to_f32_kernel(const double *a, float *w, long long len, doub
     }
     if (amax) {
         for (int o = 16; o; o >>= 1) {
-            const double y = __shfl_xor_sync(0xffffffffu, mx, o);
-            mx = (y > mx || y != y) ? y : mx;
+            const unsigned long long y = __shfl_xor_sync(0xffffffffu, mx, o);
+            mx = y > mx ? y : mx;
         }
-        if ((threadIdx.x & 31) == 0)
-            atomicMax(reinterpret_cast<unsigned long long *>(amax), (unsigned long long)__double_as_longlong(mx));
+        if ((threadIdx.x & 31) == 0) atomicMax(reinterpret_cast<unsigned long long *>(amax), mx);
     }
 }
 
