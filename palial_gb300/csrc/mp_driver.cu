@@ -50,6 +50,8 @@ cudaError_t mps_to_f32_rhs(const double *R, float *R32, long long n, int cols, c
 cudaError_t mps_add_correction(double *X, const float *D32, long long n, int cols, const double *scale,
                                cudaStream_t s);
 cudaError_t mps_mark_step(int *status, int k, cudaStream_t s);
+cudaError_t mpr_solve(const float *W, const float *Dinv, int n, int nb, int kind, float *R, float *Y, int *status,
+                      cudaStream_t s);
 cudaError_t mpd_factor_tile(int alg, float *W, int n, int nb, int k, int *status, cudaStream_t s);
 cudaError_t mps_invert_diag(const float *W, int n, int nb, float *Dinv, int kind, cudaStream_t s);
 cudaError_t mps_rhs_step(const float *W, const float *Dinv, int n, int nb, int k, float *R, float *S, int kind,
@@ -74,6 +76,7 @@ namespace {
 
 struct MpBufs {
     DevBuf w, diag, pa_hi, pa_lo, pb_hi, pb_lo, scales, r, r32, x32, norms, work, krylov, hbuf, gvec;
+    DevBuf y32;     // output of the forward triangular solve (n x 16)
     DevBuf xsplit;  // compensated residual: X as FP32 pairs (n x 16 float2) + 16 scale exponents
     DevBuf dinv_u, dinv_l, stile;  // FP32 inverses of the diagonal factor tiles, solve scratch
 };
@@ -158,13 +161,13 @@ int mp_prepare_solves(int alg, const float *W, int n, int nb, cudaStream_t s, pa
 // backward substitution over tile rows: the diagonal step multiplies by the stored inverse,
 // the update step subtracts the solved tile row from the remaining ones.
 int mp_apply_inverse(int alg, const float *W, int n, int nb, float *R32, cudaStream_t s, palial_status *st) {
-    const int mt = n / nb;
-    float *S = mb.stile.as<float>();
+    // forward into Y, backward back into R32: one persistent launch per direction (mp_rhs.cu)
+    PALIAL_CK(mb.y32.ensure(sizeof(float) * (size_t)n * 16), "alloc solve output");
+    float *Y = mb.y32.as<float>();
     const float *fwd_inv = (alg == 0) ? mb.dinv_u.as<float>() : mb.dinv_l.as<float>();
-    const int fwd_kind = (alg == 0) ? 0 : 2;
-    for (int k = 0; k < mt; k++) PALIAL_CK(mps_rhs_step(W, fwd_inv, n, nb, k, R32, S, fwd_kind, s), "forward");
-    for (int k = mt - 1; k >= 0; k--)
-        PALIAL_CK(mps_rhs_step(W, mb.dinv_u.as<float>(), n, nb, k, R32, S, 1, s), "backward");
+    int *status = g.diag.status.as<int>();
+    PALIAL_CK(mpr_solve(W, fwd_inv, n, nb, alg == 0 ? 0 : 2, R32, Y, status, s), "forward solve");
+    PALIAL_CK(mpr_solve(W, mb.dinv_u.as<float>(), n, nb, 1, Y, R32, status, s), "backward solve");
     return PALIAL_OK;
 }
 
@@ -474,6 +477,9 @@ static int solve_one(int alg, const double *dA, int n, int nb, const double *dB,
     }
     bool fp64_phase = false;
     constexpr double kDfConfirmBelow = 1e-11;
+    // status words of the refinement's solve launches (a timed-out wait is reported there)
+    PALIAL_CK(g.diag.status.ensure(sizeof(int) * ST_NSLOTS + 64), "alloc status");
+    PALIAL_CK(cudaMemsetAsync(g.diag.status.ptr, 0, sizeof(int) * ST_NSLOTS, s), "clear status");
     const double fsec = std::chrono::duration<double>(std::chrono::steady_clock::now() - f0).count();
     // ---- refinement -------------------------------------------------------------------------
     const double tol = o.ir_tol > 0 ? o.ir_tol : 1e-14 * n;
@@ -569,6 +575,11 @@ static int solve_one(int alg, const double *dA, int n, int nb, const double *dB,
             break;
         }
         eta_prev = std::min(eta_prev, eta);
+    }
+    {
+        int code = 0;
+        PALIAL_CK(cudaMemcpy(&code, g.diag.status.ptr, sizeof code, cudaMemcpyDeviceToHost), "solve status");
+        if (code) return set_status(st, code, "refinement solve: device error %d", code);
     }
     const double total = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
     if (st) {

@@ -1,0 +1,234 @@
+// mp_rhs.cu -- the refinement's blocked triangular solves with the FP32 factors, one
+// persistent launch per direction.
+//
+// Solve T Y = R (16 right-hand sides, R and Y n x 16 FP32, ld n) by tile rows of the factor:
+//   APPLY(k, b):     Y_k[b] = op(D_k^-1)[b rows] R_k      (D_k^-1 the stored inverse of the
+//                                                           diagonal factor tile, 64-row block b)
+//   UPDATE(k, t, b): R_t[b] -= op(W_kt)[b rows] Y_k       (t after k in the solve order)
+// with, per kind: 0 = Cholesky forward U^T y = r (op = transpose, W_kt = U(k,t), t > k);
+// 1 = backward U x = y (op = none, W_kt = U(t,k), t < k, k descending); 2 = LU forward
+// L y = r (unit L, op = none, W_kt = L(t,k), t > k).
+// Tasks run in one launch of persistent CTAs that take records in a fixed order (right-looking:
+// step k's applies, then its updates) with an atomic ticket and wait on completion
+// counters: per tile t the updates applied to it (APPLY waits for all of them), per 64-row
+// block the updates applied to it (updates into one block run in k order: deterministic
+// results), per tile k its applies (UPDATE(k, ..) waits for all of Y_k).  Every wait refers to
+// earlier records, so the dispatch cannot deadlock; every wait has a deadline and reports
+// PALIAL_ERR_TIMEOUT in the status words instead of hanging.
+#include <cuda_runtime.h>
+
+#include <map>
+#include <tuple>
+#include <vector>
+
+#include "host_state.hpp"
+#include "tile_f32.cuh"
+
+namespace palial {
+namespace mpr {
+using namespace f32;
+
+struct alignas(16) RhsTask {
+    int type;  // 0 apply, 1 update
+    int k, t, b;
+    int wobj[2], wcnt[2];
+    int sobj[2];
+    int nwait, nsig;
+};
+
+struct RhsParams {
+    const RhsTask *tasks;
+    int ntasks;
+    unsigned *ticket, *counters;
+    int *status;
+    const float *W, *Dinv;
+    float *R, *Y;
+    int n, nb, kind;
+    unsigned long long timeout_ns;
+};
+
+constexpr int SMEM_BYTES = GEMM_SMEM_FLOATS * 4;
+
+__device__ __forceinline__ size_t tile_off(int n, int nb, int tm, int tn) {
+    return (size_t)nb * nb * ((size_t)tm + (size_t)(n / nb) * tn);
+}
+
+__global__ void __launch_bounds__(NT, 2) rhs_solve_kernel(RhsParams p) {
+    extern __shared__ __align__(16) float smem[];
+    __shared__ int s_task, s_abort;
+    const int n = p.n, nb = p.nb;
+    for (;;) {
+        if (threadIdx.x == 0) {
+            int tk = p.ntasks;
+            if (ld_volatile(p.status + ST_CODE) == 0) tk = (int)atomicAdd(p.ticket, 1u);
+            s_task = tk;
+            s_abort = 0;
+        }
+        __syncthreads();
+        const int id = s_task;
+        if (id >= p.ntasks) break;
+        const RhsTask t = p.tasks[id];
+        if (threadIdx.x == 0) {
+            const unsigned long long start = globaltimer_ns();
+            for (int i = 0; i < t.nwait && !s_abort; i++) {
+                const unsigned *c = p.counters + t.wobj[i];
+                while (ld_acquire(c) < (unsigned)t.wcnt[i]) {
+                    if (ld_volatile(p.status + ST_CODE) != 0) { s_abort = 1; break; }
+                    if (globaltimer_ns() - start > p.timeout_ns) {
+                        if (atomicCAS(p.status + ST_CODE, 0, -4 /*PALIAL_ERR_TIMEOUT*/) == 0) {
+                            p.status[ST_TASK] = id;
+                            p.status[ST_COL] = t.wobj[i];
+                        }
+                        s_abort = 1;
+                        break;
+                    }
+                    __nanosleep(128);
+                }
+            }
+        }
+        __syncthreads();
+        if (s_abort) break;
+        const int rb = t.b * 64;
+        if (t.type == 0) {
+            // Y_k[rb] = op(D_k^-1)[rb rows] R_k
+            const float *D = p.Dinv + (size_t)t.k * nb * nb;
+            float *out = p.Y + (size_t)t.k * nb + rb;
+            for (int e = threadIdx.x; e < 64 * RW; e += NT) out[(e & 63) + (size_t)(e >> 6) * n] = 0.f;
+            __syncthreads();
+            if (p.kind == 0) cta_gemm_rw<true>(64, nb, 1.f, D + (size_t)rb * nb, nb, p.R + (size_t)t.k * nb, n, out, n, smem);
+            else cta_gemm_rw<false>(64, nb, 1.f, D + rb, nb, p.R + (size_t)t.k * nb, n, out, n, smem);
+        } else {
+            // R_t[rb] -= op(W_kt)[rb rows] Y_k
+            float *Rt = p.R + (size_t)t.t * nb + rb;
+            const float *Yk = p.Y + (size_t)t.k * nb;
+            if (p.kind == 0)
+                cta_gemm_rw<true>(64, nb, -1.f, p.W + tile_off(n, nb, t.k, t.t) + (size_t)rb * nb, nb, Yk, n, Rt, n, smem);
+            else
+                cta_gemm_rw<false>(64, nb, -1.f, p.W + tile_off(n, nb, t.t, t.k) + rb, nb, Yk, n, Rt, n, smem);
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            __threadfence();
+            for (int i = 0; i < t.nsig; i++) atomicAdd(p.counters + t.sobj[i], 1u);
+        }
+    }
+}
+
+// Task list of one direction, right-looking: step k's applies, then its updates of every
+// later tile (the next tile first: it is on the critical path).  Updates into one 64-row block
+// come from different steps, so the per-block chains never fill the dispatch window.
+// Objects: [0, mt) updates into tile t; [mt, 2 mt) applies of tile k; [2 mt, 2 mt + mt * nbl)
+// updates into 64-row block (t, b).
+std::vector<RhsTask> build_tasks(int mt, int nbl, int kind) {
+    std::vector<RhsTask> v;
+    const auto order = [&](int i) { return kind == 1 ? mt - 1 - i : i; };  // solve order
+    std::vector<int> upd_tile(mt, 0), upd_blk((size_t)mt * nbl, 0);
+    for (int ik = 0; ik < mt; ik++) {
+        const int k = order(ik);
+        for (int b = 0; b < nbl; b++) {
+            RhsTask r{};
+            r.type = 0;
+            r.k = k;
+            r.t = k;
+            r.b = b;
+            if (upd_tile[k] > 0) {
+                r.wobj[0] = k;
+                r.wcnt[0] = upd_tile[k];
+                r.nwait = 1;
+            }
+            r.sobj[0] = mt + k;
+            r.nsig = 1;
+            v.push_back(r);
+        }
+        for (int it = ik + 1; it < mt; it++) {
+            const int t = order(it);
+            for (int b = 0; b < nbl; b++) {
+                RhsTask r{};
+                r.type = 1;
+                r.k = k;
+                r.t = t;
+                r.b = b;
+                const int blk = 2 * mt + t * nbl + b;
+                r.wobj[0] = mt + k;
+                r.wcnt[0] = nbl;  // Y_k complete
+                r.nwait = 1;
+                if (upd_blk[(size_t)t * nbl + b] > 0) {  // the previous step's update of this block
+                    r.wobj[1] = blk;
+                    r.wcnt[1] = upd_blk[(size_t)t * nbl + b];
+                    r.nwait = 2;
+                }
+                r.sobj[0] = t;
+                r.sobj[1] = blk;
+                r.nsig = 2;
+                upd_blk[(size_t)t * nbl + b]++;
+                upd_tile[t]++;
+                v.push_back(r);
+            }
+        }
+    }
+    return v;
+}
+
+struct Cached {
+    DevBuf tasks;
+    int ntasks = 0;
+};
+std::map<std::tuple<int, int, int>, Cached> g_cache;
+DevBuf g_counters, g_ticket;
+
+}  // namespace mpr
+
+cudaError_t mpr_configure() {
+    return cudaFuncSetAttribute(mpr::rhs_solve_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, mpr::SMEM_BYTES);
+}
+
+void mpr_release() {
+    for (auto &kv : mpr::g_cache) kv.second.tasks.release();
+    mpr::g_cache.clear();
+    mpr::g_counters.release();
+    mpr::g_ticket.release();
+}
+
+// One direction of the blocked triangular solve: R (input, overwritten) -> Y (output), on
+// stream s.  status: the factorization's status words (a timed-out wait is reported there).
+cudaError_t mpr_solve(const float *W, const float *Dinv, int n, int nb, int kind, float *R, float *Y, int *status,
+                      cudaStream_t s) {
+    const int mt = n / nb, nbl = nb / 64;
+    auto key = std::make_tuple(mt, nbl, kind);
+    auto it = mpr::g_cache.find(key);
+    if (it == mpr::g_cache.end()) {
+        const auto tasks = mpr::build_tasks(mt, nbl, kind);
+        mpr::Cached c;
+        cudaError_t e = c.tasks.ensure(sizeof(mpr::RhsTask) * tasks.size());
+        if (e != cudaSuccess) return e;
+        e = cudaMemcpy(c.tasks.ptr, tasks.data(), sizeof(mpr::RhsTask) * tasks.size(), cudaMemcpyHostToDevice);
+        if (e != cudaSuccess) return e;
+        c.ntasks = (int)tasks.size();
+        it = mpr::g_cache.emplace(key, c).first;
+    }
+    const int nobj = 2 * mt + mt * nbl;
+    cudaError_t e = mpr::g_counters.ensure(sizeof(unsigned) * (size_t)nobj);
+    if (e == cudaSuccess) e = mpr::g_ticket.ensure(64);
+    if (e == cudaSuccess) e = cudaMemsetAsync(mpr::g_counters.ptr, 0, sizeof(unsigned) * (size_t)nobj, s);
+    if (e == cudaSuccess) e = cudaMemsetAsync(mpr::g_ticket.ptr, 0, 64, s);
+    if (e != cudaSuccess) return e;
+    mpr::RhsParams p;
+    p.tasks = it->second.tasks.as<mpr::RhsTask>();
+    p.ntasks = it->second.ntasks;
+    p.ticket = mpr::g_ticket.as<unsigned>();
+    p.counters = mpr::g_counters.as<unsigned>();
+    p.status = status;
+    p.W = W;
+    p.Dinv = Dinv;
+    p.R = R;
+    p.Y = Y;
+    p.n = n;
+    p.nb = nb;
+    p.kind = kind;
+    p.timeout_ns = 30ull * 1000000000ull;
+    note_launch();
+    mpr::rhs_solve_kernel<<<g.sms * 2, f32::NT, mpr::SMEM_BYTES, s>>>(p);
+    return cudaGetLastError();
+}
+
+}  // namespace palial

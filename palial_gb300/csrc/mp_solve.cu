@@ -88,26 +88,31 @@ __global__ void split_x_kernel(const double *X, long long n, int nrhs, const dou
 
 // R = B - A X with A and X as FP32 pairs: per product the exact FP32 product of the high parts
 // (fma), the cross terms into its error, and a TwoSum accumulation (Knuth) of the pair; every
-// 64 products the pair is added to an FP64 accumulator.  Same layout as residual_kernel (one
-// CTA per 32-row block, thread = row x 2 right-hand sides).  amax as there (row sums of |a|).
+// 64 products the pair is added to an FP64 accumulator.  One CTA per 64-row block; thread =
+// row x 4 right-hand sides (t % 64, t / 64).  amax as in residual_kernel (row sums of |a|).
+__device__ __forceinline__ void df_acc(float ah, float al, float xh, float xl, float &s, float &c) {
+    // explicit _rn intrinsics: no FMA contraction may touch the error-free steps
+    const float pr = __fmul_rn(ah, xh);
+    const float t = fmaf(ah, xl, fmaf(al, xh, fmaf(ah, xh, -pr)));
+    const float sn = __fadd_rn(s, pr), bp = __fsub_rn(sn, s);
+    c = __fadd_rn(c, __fadd_rn(__fadd_rn(__fsub_rn(s, __fsub_rn(sn, bp)), __fsub_rn(pr, bp)), t));
+    s = sn;
+}
 __global__ void __launch_bounds__(256) residual_df_kernel(const double *A, int n, int nb, const float2 *Xs,
                                                           const int *tau, int sigma, const double *B, double *R,
                                                           int nrhs, double *amax) {
-    __shared__ float2 As[64][33];
-    __shared__ float4 Xp[64][8];  // (hi, lo) of right-hand sides 2g, 2g+1
-    __shared__ float part[8][33];
-    const int i0 = blockIdx.x * 32;
-    const int row = threadIdx.x & 31, grp = threadIdx.x >> 5;
-    double acc0 = 0.0, acc1 = 0.0;
+    __shared__ float2 As[64][65];
+    __shared__ float4 Xp[64][8];  // (hi, lo) of right-hand sides 2j, 2j+1
+    __shared__ float part[4][65];
+    const int i0 = blockIdx.x * 64;
+    const int row = threadIdx.x & 63, grp = threadIdx.x >> 6;  // right-hand sides 4 grp .. 4 grp + 3
+    double acc[4] = {0.0, 0.0, 0.0, 0.0};
     float asum = 0.f;
     const int mt = n / nb;
     const double *tilerow = A + (size_t)nb * nb * (size_t)(i0 / nb) + (size_t)(i0 % nb);
     for (int p0 = 0; p0 < n; p0 += 64) {
         const double *blk = tilerow + (size_t)nb * nb * (size_t)mt * (p0 / nb) + (size_t)(p0 % nb) * nb;
-        for (int e = threadIdx.x; e < 2048; e += 256) {
-            const double v = blk[(e & 31) + (size_t)(e >> 5) * nb];
-            As[e >> 5][e & 31] = split_df(v, sigma);
-        }
+        for (int e = threadIdx.x; e < 4096; e += 256) As[e >> 6][e & 63] = split_df(blk[(e & 63) + (size_t)(e >> 6) * nb], sigma);
         for (int e = threadIdx.x; e < 64 * 8; e += 256) {
             const float2 a = Xs[(size_t)(p0 + (e >> 3)) * 16 + 2 * (e & 7)];
             const float2 b = Xs[(size_t)(p0 + (e >> 3)) * 16 + 2 * (e & 7) + 1];
@@ -116,56 +121,42 @@ __global__ void __launch_bounds__(256) residual_df_kernel(const double *A, int n
         __syncthreads();
         if (amax) {
 #pragma unroll
-            for (int p = grp; p < 64; p += 8) {
+            for (int p = grp; p < 64; p += 4) {
                 const float2 a = As[p][row];
                 asum += fabsf(a.x + a.y);
             }
         }
-        float s0 = 0.f, c0 = 0.f, s1 = 0.f, c1 = 0.f;
+        float s[4] = {0.f, 0.f, 0.f, 0.f}, c[4] = {0.f, 0.f, 0.f, 0.f};
 #pragma unroll 4
         for (int p = 0; p < 64; p++) {
             const float2 a = As[p][row];
-            const float4 x = Xp[p][grp];
-            // explicit _rn intrinsics: no FMA contraction may touch the error-free steps
-            {
-                const float pr = __fmul_rn(a.x, x.x);
-                const float t = fmaf(a.x, x.y, fmaf(a.y, x.x, fmaf(a.x, x.x, -pr)));
-                const float sn = __fadd_rn(s0, pr), bp = __fsub_rn(sn, s0);
-                c0 = __fadd_rn(c0, __fadd_rn(__fadd_rn(__fsub_rn(s0, __fsub_rn(sn, bp)), __fsub_rn(pr, bp)), t));
-                s0 = sn;
-            }
-            {
-                const float pr = __fmul_rn(a.x, x.z);
-                const float t = fmaf(a.x, x.w, fmaf(a.y, x.z, fmaf(a.x, x.z, -pr)));
-                const float sn = __fadd_rn(s1, pr), bp = __fsub_rn(sn, s1);
-                c1 = __fadd_rn(c1, __fadd_rn(__fadd_rn(__fsub_rn(s1, __fsub_rn(sn, bp)), __fsub_rn(pr, bp)), t));
-                s1 = sn;
-            }
+            const float4 x01 = Xp[p][2 * grp], x23 = Xp[p][2 * grp + 1];
+            df_acc(a.x, a.y, x01.x, x01.y, s[0], c[0]);
+            df_acc(a.x, a.y, x01.z, x01.w, s[1], c[1]);
+            df_acc(a.x, a.y, x23.x, x23.y, s[2], c[2]);
+            df_acc(a.x, a.y, x23.z, x23.w, s[3], c[3]);
         }
-        acc0 += (double)s0 + (double)c0;
-        acc1 += (double)s1 + (double)c1;
+#pragma unroll
+        for (int j = 0; j < 4; j++) acc[j] += (double)s[j] + (double)c[j];
         __syncthreads();
     }
-    const double accs[2] = {acc0, acc1};
 #pragma unroll
-    for (int j = 0; j < 2; j++) {
-        const int c = 2 * grp + j;
-        if (c < nrhs) {
-            const size_t o = (size_t)(i0 + row) + (size_t)c * n;
-            const double ax = ldexp(accs[j], sigma + tau[c]);
+    for (int j = 0; j < 4; j++) {
+        const int cc = 4 * grp + j;
+        if (cc < nrhs) {
+            const size_t o = (size_t)(i0 + row) + (size_t)cc * n;
+            const double ax = ldexp(acc[j], sigma + tau[cc]);
             R[o] = B ? B[o] - ax : ax;
         }
     }
     if (amax) {
         part[grp][row] = asum;
         __syncthreads();
-        if (threadIdx.x < 32) {
-            double t = 0.0;
-#pragma unroll
-            for (int g = 0; g < 8; g++) t += (double)part[g][row];
+        if (threadIdx.x < 64) {
+            double t = (double)part[0][row] + (double)part[1][row] + (double)part[2][row] + (double)part[3][row];
             t = ldexp(t, sigma);
             for (int o = 16; o; o >>= 1) t = fmax(t, __shfl_xor_sync(0xffffffffu, t, o));
-            if (threadIdx.x == 0)
+            if ((threadIdx.x & 31) == 0)
                 atomicMax(reinterpret_cast<unsigned long long *>(amax), (unsigned long long)__double_as_longlong(t));
         }
     }
@@ -549,7 +540,7 @@ cudaError_t mps_residual_df(const double *A, int n, int nb, const double *X, con
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
     note_launch();
-    mps::residual_df_kernel<<<n / 32, 256, 0, s>>>(A, n, nb, Xs, tau, sigma, B, R, nrhs, amax);
+    mps::residual_df_kernel<<<n / 64, 256, 0, s>>>(A, n, nb, Xs, tau, sigma, B, R, nrhs, amax);
     return cudaGetLastError();
 }
 cudaError_t mps_tile_to_f64(const float *w, double *d, int nb, cudaStream_t s) {

@@ -45,6 +45,8 @@ cudaError_t launch_sumsq(const double *X, long long len, double *partial, int bl
 cudaError_t launch_sub(const double *X, const double *Y, double *Z, long long len, cudaStream_t s);
 cudaError_t mps_configure();
 cudaError_t mpd_configure();
+cudaError_t mpr_configure();
+void mpr_release();
 
 State g;
 static long long g_launches = 0;
@@ -201,6 +203,7 @@ int palial_gpu_init(int device) {
     if (sched_configure() != cudaSuccess) return PALIAL_ERR_CUDA;
     if (mps_configure() != cudaSuccess) return PALIAL_ERR_CUDA;
     if (mpd_configure() != cudaSuccess) return PALIAL_ERR_CUDA;
+    if (mpr_configure() != cudaSuccess) return PALIAL_ERR_CUDA;
     g.occupancy = std::max(1, sched_occupancy());
     if (!g.ev0) cudaEventCreate(&g.ev0);
     if (!g.ev1) cudaEventCreate(&g.ev1);
@@ -219,6 +222,7 @@ int palial_gpu_finalize(void) {
     g.batch_graph = nullptr;
     for (DevBuf *b : {&g.mat, &g.smat, &g.kbuf, &g.probe}) b->release();
     qr_solve_release();
+    mpr_release();
     g.dags.clear();
     return PALIAL_OK;
 }
