@@ -43,6 +43,42 @@ __device__ __forceinline__ void stage(float (*Xs)[SP], const float *X, int ld, i
     }
 }
 
+// The same staging split in two halves, so the next chunk's global loads can be in flight
+// while the current chunk is computed: stage_load reads into registers, stage_store writes them.
+template <bool TX>
+__device__ __forceinline__ void stage_load(float4 (&v)[2], const float *X, int ld, int i0, int p0) {
+    const int t = threadIdx.x;
+#pragma unroll
+    for (int q = 0; q < 2; q++) {
+        const int e = t + q * NT;
+        if (!TX) {
+            const int p = e >> 4, i = (e & 15) * 4;
+            v[q] = __ldcg(reinterpret_cast<const float4 *>(X + (size_t)(i0 + i) + (size_t)(p0 + p) * ld));
+        } else {
+            const int i = e >> 3, p = (e & 7) * 4;
+            v[q] = __ldcg(reinterpret_cast<const float4 *>(X + (size_t)(p0 + p) + (size_t)(i0 + i) * ld));
+        }
+    }
+}
+template <bool TX>
+__device__ __forceinline__ void stage_store(float (*Xs)[SP], const float4 (&v)[2]) {
+    const int t = threadIdx.x;
+#pragma unroll
+    for (int q = 0; q < 2; q++) {
+        const int e = t + q * NT;
+        if (!TX) {
+            const int p = e >> 4, i = (e & 15) * 4;
+            *reinterpret_cast<float4 *>(&Xs[p][i]) = v[q];
+        } else {
+            const int i = e >> 3, p = (e & 7) * 4;
+            Xs[p][i] = v[q].x;
+            Xs[p + 1][i] = v[q].y;
+            Xs[p + 2][i] = v[q].z;
+            Xs[p + 3][i] = v[q].w;
+        }
+    }
+}
+
 // C[M x N] += alpha * op(A) op(B) (beta = 1), dims multiples of 64 / 32.  Ends synced.
 template <bool TA, bool TB>
 __device__ __forceinline__ void cta_gemm(int M, int N, int K, float alpha, const float *A, int lda, const float *B, int ldb, float *C,
@@ -55,10 +91,19 @@ __device__ __forceinline__ void cta_gemm(int M, int N, int K, float alpha, const
     for (int i0 = 0; i0 < M; i0 += BM)
         for (int j0 = 0; j0 < N; j0 += BM) {
             float acc[4][4] = {};
+            float4 ra[2], rb[2];  // the next chunk, in flight during the current one's compute
+            if (K > 0) {
+                stage_load<TA>(ra, A, lda, i0, 0);
+                stage_load<!TB>(rb, B, ldb, j0, 0);
+            }
             for (int p0 = 0; p0 < K; p0 += KC) {
-                stage<TA>(As, A, lda, i0, p0);
-                stage<!TB>(Bs, B, ldb, j0, p0);
+                stage_store<TA>(As, ra);
+                stage_store<!TB>(Bs, rb);
                 __syncthreads();
+                if (p0 + KC < K) {
+                    stage_load<TA>(ra, A, lda, i0, p0 + KC);
+                    stage_load<!TB>(rb, B, ldb, j0, p0 + KC);
+                }
 #pragma unroll 8
                 for (int p = 0; p < KC; p++) {
                     const float4 a = *reinterpret_cast<const float4 *>(&As[p][tr * 4]);
@@ -99,17 +144,26 @@ __device__ __forceinline__ void cta_gemm_rw(int M, int K, float alpha, const flo
     const int tx = threadIdx.x & 3, ty = threadIdx.x >> 2;
     for (int i0 = 0; i0 < M; i0 += BM) {
         float acc[4] = {0.f, 0.f, 0.f, 0.f};
+        float4 ra[2], rbv = make_float4(0.f, 0.f, 0.f, 0.f);  // the next chunk, in flight
+        const int bj = threadIdx.x / (KC / 4), bp = (threadIdx.x % (KC / 4)) * 4;
+        const bool bthr = threadIdx.x < KC * RW / 4;
+        if (K > 0) {
+            stage_load<TA>(ra, A, lda, i0, 0);
+            if (bthr) rbv = __ldcg(reinterpret_cast<const float4 *>(B + (size_t)bp + (size_t)bj * ldb));
+        }
         for (int p0 = 0; p0 < K; p0 += KC) {
-            stage<TA>(As, A, lda, i0, p0);
-            if (threadIdx.x < KC * RW / 4) {
-                const int j = threadIdx.x / (KC / 4), p = (threadIdx.x % (KC / 4)) * 4;
-                const float4 v = __ldcg(reinterpret_cast<const float4 *>(B + (size_t)(p0 + p) + (size_t)j * ldb));
-                Bs[p][j] = v.x;
-                Bs[p + 1][j] = v.y;
-                Bs[p + 2][j] = v.z;
-                Bs[p + 3][j] = v.w;
+            stage_store<TA>(As, ra);
+            if (bthr) {
+                Bs[bp][bj] = rbv.x;
+                Bs[bp + 1][bj] = rbv.y;
+                Bs[bp + 2][bj] = rbv.z;
+                Bs[bp + 3][bj] = rbv.w;
             }
             __syncthreads();
+            if (p0 + KC < K) {
+                stage_load<TA>(ra, A, lda, i0, p0 + KC);
+                if (bthr) rbv = __ldcg(reinterpret_cast<const float4 *>(B + (size_t)(p0 + KC + bp) + (size_t)bj * ldb));
+            }
 #pragma unroll 8
             for (int p = 0; p < KC; p++) {
                 const float a = As[p][ty];
