@@ -189,6 +189,24 @@ int precondition(int alg, const float *W, int n, int nb, const double *v, double
     return PALIAL_OK;
 }
 
+// A X products of the refinement (B - A X, or A X with B = NULL): the compensated-FP32
+// residual when the current solve uses it (GMRES's inner products need far less than FP64),
+// else FP64.
+struct ResidCtx {
+    bool df = false;
+    int sigma = 0;
+} g_rctx;
+static cudaError_t apply_A(const double *A, int n, int nb, const double *X, const double *B, double *R, int nrhs,
+                           cudaStream_t s) {
+    if (!g_rctx.df) return mps_residual(A, n, nb, X, B, R, nrhs, nullptr, s);
+    double *cm = mb.norms.as<double>() + 128;
+    cudaError_t e = mps_colmax(X, n, nrhs, cm, s);
+    if (e != cudaSuccess) return e;
+    float2 *xs = mb.xsplit.as<float2>();
+    return mps_residual_df(A, n, nb, X, cm, B, R, nrhs, g_rctx.sigma, xs, reinterpret_cast<int *>(xs + (size_t)n * 16),
+                           nullptr, s);
+}
+
 // GMRES on M^-1 A d = M^-1 r (left preconditioned, FP64 vectors, one Krylov space per
 // right-hand side, classical Gram-Schmidt applied twice), restart length m, at most maxit
 // iterations; stops when every column's preconditioned residual drops by `rtol`.  d is
@@ -213,7 +231,7 @@ int gmres(int alg, const double *A, const float *W, int n, int nb, const double 
             int rc = precondition(alg, W, n, nb, r, w, nrhs, dscale, hs, s, st);
             if (rc) return rc;
         } else {
-            PALIAL_CK(mps_residual(A, n, nb, d, r, V, nrhs, nullptr, s), "inner residual");
+            PALIAL_CK(apply_A(A, n, nb, d, r, V, nrhs, s), "inner residual");
             int rc = precondition(alg, W, n, nb, V, w, nrhs, dscale, hs, s, st);
             if (rc) return rc;
         }
@@ -233,7 +251,7 @@ int gmres(int alg, const double *A, const float *W, int n, int nb, const double 
         int j = 0;
         for (; j < m && total < maxit; j++, total++) {
             // w = M^-1 A V_j
-            PALIAL_CK(mps_residual(A, n, nb, V + blk * j, nullptr, tv, nrhs, nullptr, s), "A v");
+            PALIAL_CK(apply_A(A, n, nb, V + blk * j, nullptr, tv, nrhs, s), "A v");
             int rc = precondition(alg, W, n, nb, tv, w, nrhs, dscale, hs, s, st);
             if (rc) return rc;
             // CGS twice: h = V^T w, w -= V h
@@ -418,7 +436,7 @@ static int solve_one(int alg, const double *dA, int n, int nb, const double *dB,
     PALIAL_CK(mb.w.ensure(sizeof(float) * nn), "alloc W");
     PALIAL_CK(mb.r.ensure(sizeof(double) * (size_t)n * nrhs), "alloc r");
     PALIAL_CK(mb.r32.ensure(sizeof(float) * (size_t)n * 64), "alloc r32");
-    PALIAL_CK(mb.norms.ensure(sizeof(double) * 128), "alloc norms");
+    PALIAL_CK(mb.norms.ensure(sizeof(double) * 256), "alloc norms");
     float *W = mb.w.as<float>();
     double *nrm = mb.norms.as<double>();  // [0] ||A||, [1..16] scale, [17..32] |r|, [33..48] |x|, [49..64] |b|
     // ||A||_inf and max |a_ii| (for the shift)
@@ -477,6 +495,8 @@ static int solve_one(int alg, const double *dA, int n, int nb, const double *dB,
     }
     bool fp64_phase = false;
     constexpr double kDfConfirmBelow = 1e-11;
+    g_rctx.df = use_df;
+    g_rctx.sigma = sigma;
     // status words of the refinement's solve launches (a timed-out wait is reported there)
     PALIAL_CK(g.diag.status.ensure(sizeof(int) * ST_NSLOTS + 64), "alloc status");
     PALIAL_CK(cudaMemsetAsync(g.diag.status.ptr, 0, sizeof(int) * ST_NSLOTS, s), "clear status");
@@ -567,6 +587,9 @@ static int solve_one(int alg, const double *dA, int n, int nb, const double *dB,
             converged = true;
             break;
         }
+        if (o.reserved[5] == 1 && it >= 2 && eta > 0.1 * eta_prev) {
+            break;  // a lower rung of the precision ladder that contracts slowly: move up
+        }
         if (!use_gmres && it >= 2 && eta > 0.5 * eta_prev && o.gmres >= 0) {
             use_gmres = true;  // plain refinement contracts too slowly: switch to GMRES-IR
         } else if (use_gmres && it >= 3 && eta > 0.9 * eta_prev) {
@@ -616,9 +639,15 @@ extern "C" int palial_gpu_solve_ir(int alg, const double *dA, int n, int nb, con
     int used = -1;
     for (int prec : ladder) {
         o.precision = prec;
-        // lower rungs get a bounded effort: at most 10 outer iterations and 100 GMRES steps
+        // lower rungs get a bounded effort: BF16 plain refinement that must contract 10x per
+        // step, BF16x3 at most 10 outer iterations and 100 GMRES steps
         palial_opts oo = o;
-        if (prec != PALIAL_PREC_FP64) {
+        if (prec == PALIAL_PREC_BF16) {
+            // plain refinement only; leave as soon as it contracts by less than 10x per step
+            if (oo.ir_max_iter <= 0 || oo.ir_max_iter > 10) oo.ir_max_iter = 10;
+            oo.gmres = -1;
+            oo.reserved[5] = 1;
+        } else if (prec != PALIAL_PREC_FP64) {
             if (oo.ir_max_iter <= 0 || oo.ir_max_iter > 10) oo.ir_max_iter = 10;
             oo.reserved[1] = 50;
             oo.reserved[3] = 100;
