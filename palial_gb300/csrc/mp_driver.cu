@@ -30,7 +30,7 @@
 namespace palial {
 cudaError_t mp_update(int mode, int upper, float *C, int n, int nb, int k, const void *a_hi, const void *a_lo,
                       const void *b_hi, const void *b_lo, const float *scale_a, const float *scale_b, int *status,
-                      cudaStream_t s);
+                      cudaStream_t s, int part = 0);
 cudaError_t mp_pack_rows(int mode, const float *W, int n, int nb, int k, void *hi, void *lo, float *scales,
                          cudaStream_t s);
 cudaError_t mp_pack_cols(int mode, const float *W, int n, int nb, int k, void *hi, void *lo, float *scales,
@@ -93,41 +93,81 @@ double unit_roundoff(int prec) {
 
 // Low-precision factorization of W (FP32 tile layout, in place).  Returns PALIAL_OK,
 // PALIAL_ERR_NOT_SPD (Cholesky breakdown) or an error.
+// Lookahead: step k's critical chain (diagonal tile, panel, pack, the update of the next
+// step's tiles) runs on a high-priority stream; the rest of step k's trailing update runs on a
+// low-priority stream, overlapping step k+1's diagonal tile and panel.  The next step's first
+// update waits for it (both write the rows below).  Packed panels alternate between two
+// buffers so step k+1's pack never overwrites what step k's rest still reads.
+struct Lookahead {
+    cudaStream_t hi = nullptr, lo = nullptr;
+    cudaEvent_t start = nullptr, packed = nullptr, rest = nullptr, join = nullptr;
+} g_la;
+
+static cudaError_t lookahead_init() {
+    if (g_la.hi) return cudaSuccess;
+    int least = 0, greatest = 0;
+    cudaError_t e = cudaDeviceGetStreamPriorityRange(&least, &greatest);
+    if (e == cudaSuccess) e = cudaStreamCreateWithPriority(&g_la.hi, cudaStreamNonBlocking, greatest);
+    if (e == cudaSuccess) e = cudaStreamCreateWithPriority(&g_la.lo, cudaStreamNonBlocking, least);
+    for (cudaEvent_t *ev : {&g_la.start, &g_la.packed, &g_la.rest, &g_la.join})
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(ev, cudaEventDisableTiming);
+    return e;
+}
+
 int mp_factor(int alg, int prec, float *W, int n, int nb, cudaStream_t s, palial_status *st, int *zero_piv) {
     const int mt = n / nb;
     const int mode = prec == PALIAL_PREC_FP8 ? 1 : prec == PALIAL_PREC_BF16X3 ? 2 : 0;
     const size_t elem = (mode == 1) ? 1 : 2;
     const size_t panel = (size_t)std::max(1, mt - 1) * nb * nb * elem;
-    PALIAL_CK(mb.pa_hi.ensure(panel), "alloc panel");
-    PALIAL_CK(mb.pb_hi.ensure(panel), "alloc panel");
+    PALIAL_CK(mb.pa_hi.ensure(2 * panel), "alloc panel");
+    PALIAL_CK(mb.pb_hi.ensure(2 * panel), "alloc panel");
     if (mode == 2) {
-        PALIAL_CK(mb.pa_lo.ensure(panel), "alloc panel");
-        PALIAL_CK(mb.pb_lo.ensure(panel), "alloc panel");
+        PALIAL_CK(mb.pa_lo.ensure(2 * panel), "alloc panel");
+        PALIAL_CK(mb.pb_lo.ensure(2 * panel), "alloc panel");
     }
-    PALIAL_CK(mb.scales.ensure(sizeof(float) * 2 * (size_t)std::max(1, mt)), "alloc scales");
+    PALIAL_CK(mb.scales.ensure(sizeof(float) * 4 * (size_t)std::max(1, mt)), "alloc scales");
     PALIAL_CK(g.diag.status.ensure(sizeof(int) * ST_NSLOTS + 64), "alloc status");
+    PALIAL_CK(lookahead_init(), "lookahead streams");
     PALIAL_CK(cudaMemsetAsync(g.diag.status.ptr, 0, sizeof(int) * ST_NSLOTS, s), "clear status");
-    float *sa = mb.scales.as<float>(), *sb = sa + mt;
+    PALIAL_CK(cudaEventRecord(g_la.start, s), "event");
+    cudaStream_t hi = g_la.hi, lo = g_la.lo;
+    PALIAL_CK(cudaStreamWaitEvent(hi, g_la.start, 0), "event");
+    PALIAL_CK(cudaStreamWaitEvent(lo, g_la.start, 0), "event");
+    int *status = g.diag.status.as<int>();
+    auto buf = [&](const DevBuf &b, int par) { return static_cast<void *>(static_cast<uint8_t *>(b.ptr) + par * panel); };
+    bool have_rest = false;
     for (int k = 0; k < mt; k++) {
         // the diagonal tile in FP32, one CTA (mp_diag.cu)
-        PALIAL_CK(mpd_factor_tile(alg, W, n, nb, k, g.diag.status.as<int>(), s), "diag factor");
+        PALIAL_CK(mpd_factor_tile(alg, W, n, nb, k, status, hi), "diag factor");
         if (k == mt - 1) break;
+        const int par = k & 1;
+        float *sa = mb.scales.as<float>() + 2 * mt * par, *sb = sa + mt;
+        void *ah = buf(mb.pa_hi, par), *al = mode == 2 ? buf(mb.pa_lo, par) : nullptr;
+        void *bh = buf(mb.pb_hi, par), *bl = mode == 2 ? buf(mb.pb_lo, par) : nullptr;
         if (alg == 0) {
-            PALIAL_CK(mps_panel_trsm(W, n, nb, k, 0, s), "panel trsm");
-            PALIAL_CK(mp_pack_rows(mode, W, n, nb, k, mb.pa_hi.ptr, mb.pa_lo.ptr, sa, s), "pack");
-            PALIAL_CK(mp_update(mode, 1, W, n, nb, k, mb.pa_hi.ptr, mb.pa_lo.ptr, mb.pa_hi.ptr, mb.pa_lo.ptr, sa, sa,
-                                g.diag.status.as<int>(), s),
-                      "update");
+            PALIAL_CK(mps_panel_trsm(W, n, nb, k, 0, hi), "panel trsm");
+            PALIAL_CK(mp_pack_rows(mode, W, n, nb, k, ah, al, sa, hi), "pack");
+            bh = ah;
+            bl = al;
+            sb = sa;
         } else {
-            PALIAL_CK(mps_panel_trsm(W, n, nb, k, 1, s), "row panel trsm");
-            PALIAL_CK(mps_panel_trsm(W, n, nb, k, 2, s), "column panel trsm");
-            PALIAL_CK(mp_pack_cols(mode, W, n, nb, k, mb.pa_hi.ptr, mb.pa_lo.ptr, sa, s), "pack L");
-            PALIAL_CK(mp_pack_rows(mode, W, n, nb, k, mb.pb_hi.ptr, mb.pb_lo.ptr, sb, s), "pack U");
-            PALIAL_CK(mp_update(mode, 0, W, n, nb, k, mb.pa_hi.ptr, mb.pa_lo.ptr, mb.pb_hi.ptr, mb.pb_lo.ptr, sa, sb,
-                                g.diag.status.as<int>(), s),
-                      "update");
+            PALIAL_CK(mps_panel_trsm(W, n, nb, k, 1, hi), "row panel trsm");
+            PALIAL_CK(mps_panel_trsm(W, n, nb, k, 2, hi), "column panel trsm");
+            PALIAL_CK(mp_pack_cols(mode, W, n, nb, k, ah, al, sa, hi), "pack L");
+            PALIAL_CK(mp_pack_rows(mode, W, n, nb, k, bh, bl, sb, hi), "pack U");
         }
+        PALIAL_CK(cudaEventRecord(g_la.packed, hi), "event");
+        if (have_rest) PALIAL_CK(cudaStreamWaitEvent(hi, g_la.rest, 0), "event");
+        PALIAL_CK(mp_update(mode, alg == 0 ? 1 : 0, W, n, nb, k, ah, al, bh, bl, sa, sb, status, hi, 1), "update (next)");
+        PALIAL_CK(cudaStreamWaitEvent(lo, g_la.packed, 0), "event");
+        PALIAL_CK(mp_update(mode, alg == 0 ? 1 : 0, W, n, nb, k, ah, al, bh, bl, sa, sb, status, lo, 2), "update (rest)");
+        PALIAL_CK(cudaEventRecord(g_la.rest, lo), "event");
+        have_rest = true;
     }
+    PALIAL_CK(cudaEventRecord(g_la.join, lo), "event");
+    PALIAL_CK(cudaStreamWaitEvent(hi, g_la.join, 0), "event");
+    PALIAL_CK(cudaEventRecord(g_la.join, hi), "event");
+    PALIAL_CK(cudaStreamWaitEvent(s, g_la.join, 0), "event");
     int hs[ST_NSLOTS];
     PALIAL_CK(cudaMemcpyAsync(hs, g.diag.status.ptr, sizeof hs, cudaMemcpyDeviceToHost, s), "status");
     PALIAL_CK(cudaStreamSynchronize(s), "factorization");

@@ -62,6 +62,8 @@ struct UpdateParams {
     int k;                    // step: trailing tiles start at tile k+1
     int ntr;                  // trailing tiles per dimension
     int upper;                // 1: only tile pairs (ti <= tj) (Cholesky), 0: all (LU)
+    int part;                 // 0: every pair; 1: the next step's tiles (row 0; LU also column
+                              // 0); 2: all other pairs (lookahead split)
     const float *scale_a;     // FP8: per trailing tile scale of A_op rows (nullptr: 1)
     const float *scale_b;     // FP8: per trailing tile scale of B_op rows
     int *status;              // error word (ST_CODE slot)
@@ -146,6 +148,27 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float *v) {
     for (int i = 0; i < 16; i++) v[i] = __uint_as_float(r[i]);
 }
 
+__device__ __forceinline__ void decode_pair(int q, int ntr, int upper, int &ti, int &tj);
+// Pair q of the launch's part (see UpdateParams::part).
+__device__ __forceinline__ void decode_part(int q, int ntr, int upper, int part, int &ti, int &tj) {
+    if (part == 1) {
+        if (upper || q < ntr) {
+            ti = 0;
+            tj = q;
+        } else {
+            ti = q - ntr + 1;
+            tj = 0;
+        }
+        return;
+    }
+    if (part == 2) {
+        decode_pair(q, ntr - 1, upper, ti, tj);
+        ti++;
+        tj++;
+        return;
+    }
+    decode_pair(q, ntr, upper, ti, tj);
+}
 __device__ __forceinline__ void decode_pair(int q, int ntr, int upper, int &ti, int &tj) {
     if (!upper) {
         ti = q % ntr;
@@ -177,7 +200,7 @@ __global__ void __launch_bounds__(NTHR, 1)
     const int sub_m = p.nb / BM, sub_n = p.nb / BN;
     const int q = blockIdx.x / (sub_m * sub_n), sub = blockIdx.x % (sub_m * sub_n);
     int ti, tj;
-    decode_pair(q, p.ntr, p.upper, ti, tj);
+    decode_part(q, p.ntr, p.upper, p.part, ti, tj);
     const int mi = sub % sub_m, nj = sub / sub_m;
     const int arow = ti * p.nb + mi * BM;   // first row of A_op
     const int brow = tj * p.nb + nj * BN;   // first row of B_op
@@ -444,7 +467,10 @@ cudaError_t launch_mode(const void *a_hi, const void *a_lo, const void *b_hi, co
         tal = ta;
         tbl = tb;
     }
-    const long long pairs = p.upper ? (long long)p.ntr * (p.ntr + 1) / 2 : (long long)p.ntr * p.ntr;
+    const long long nt = p.ntr, ns = nt - 1;
+    const long long pairs = p.part == 1 ? (p.upper ? nt : 2 * nt - 1)
+                            : p.part == 2 ? (p.upper ? ns * (ns + 1) / 2 : ns * ns)
+                                          : (p.upper ? nt * (nt + 1) / 2 : nt * nt);
     const long long blocks = pairs * (p.nb / mp::BM) * (p.nb / mp::BN);
     if (blocks <= 0) return cudaSuccess;
     if (blocks > 0x7fffffffLL) return cudaErrorInvalidValue;
@@ -458,7 +484,7 @@ cudaError_t launch_mode(const void *a_hi, const void *a_lo, const void *b_hi, co
 // trailing tile (fp8).  C: FP32 tile-layout matrix.
 cudaError_t mp_update(int mode, int upper, float *C, int n, int nb, int k, const void *a_hi, const void *a_lo,
                       const void *b_hi, const void *b_lo, const float *scale_a, const float *scale_b, int *status,
-                      cudaStream_t s) {
+                      cudaStream_t s, int part) {
     if (nb % 256 || n % nb) return cudaErrorInvalidValue;
     mp::UpdateParams p{};
     p.C = C;
@@ -470,6 +496,7 @@ cudaError_t mp_update(int mode, int upper, float *C, int n, int nb, int k, const
     p.scale_a = scale_a;
     p.scale_b = scale_b;
     p.status = status;
+    p.part = part;
     if (p.ntr <= 0) return cudaSuccess;
     if (mode == mp::MODE_BF16) return launch_mode<mp::MODE_BF16>(a_hi, nullptr, b_hi, nullptr, p, s);
     if (mode == mp::MODE_FP8) return launch_mode<mp::MODE_FP8>(a_hi, nullptr, b_hi, nullptr, p, s);
