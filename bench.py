@@ -539,7 +539,12 @@ def main() -> None:
             "e2e": {"value": e2e_value, "unit": "TFLOP/s", "h2d_bytes_per_step": 8 * n * n + 8 * n * nrhs,
                     "d2h_bytes_per_step": 8 * n * nrhs},
             "roofline": {"bound": "hbm", "achieved": gbs, "peak": pk.get("hbm_gbs", 6800.0), "unit": "GB/s",
-                         "frac": gbs / pk.get("hbm_gbs", 6800.0), "traffic": None,
+                         "frac": gbs / pk.get("hbm_gbs", 6800.0),
+                         # DRAM read + write of one launch: ncu (dram__bytes_read.sum +
+                         # dram__bytes_write.sum) on the same kernel at N=8192, k=0 (120 tile pairs,
+                         # 199.0 MB, profiles/mp_update_and_residual_n8192.md), scaled by tile pairs
+                         "traffic": 199.0e6 / 120 * ((n // NB - 1) * (n // NB) // 2),
+                         "traffic_note": "scaled from an ncu capture at N=8192 step 0 by tile pairs",
                          "kernel": "mp_update_kernel<bf16> (tcgen05, step k=0 of N=%d)" % n,
                          "tensor_tflops": upd["flop"] / upd["seconds"] * 1e-12,
                          "tensor_frac_of_bf16_peak": upd["flop"] / upd["seconds"] * 1e-12 / pk.get("bf16_tflops", 1900.0),

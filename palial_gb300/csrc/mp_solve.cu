@@ -88,8 +88,9 @@ __global__ void split_x_kernel(const double *X, long long n, int nrhs, const dou
 
 // R = B - A X with A and X as FP32 pairs: per product the exact FP32 product of the high parts
 // (fma), the cross terms into its error, and a TwoSum accumulation (Knuth) of the pair; every
-// 64 products the pair is added to an FP64 accumulator.  One CTA per 64-row block; thread =
-// row x 4 right-hand sides (t % 64, t / 64).  amax as in residual_kernel (row sums of |a|).
+// 64 products the pair is added to an FP64 accumulator.  One CTA of 128 threads per 32-row
+// block (n/32 CTAs: many resident per SM, a short last wave); thread = row x 4 right-hand
+// sides (t % 32, t / 32).  amax as in residual_kernel (row sums of |a|).
 __device__ __forceinline__ void df_acc(float ah, float al, float xh, float xl, float &s, float &c) {
     // explicit _rn intrinsics: no FMA contraction may touch the error-free steps
     const float pr = __fmul_rn(ah, xh);
@@ -98,22 +99,22 @@ __device__ __forceinline__ void df_acc(float ah, float al, float xh, float xl, f
     c = __fadd_rn(c, __fadd_rn(__fadd_rn(__fsub_rn(s, __fsub_rn(sn, bp)), __fsub_rn(pr, bp)), t));
     s = sn;
 }
-__global__ void __launch_bounds__(256) residual_df_kernel(const double *A, int n, int nb, const float2 *Xs,
+__global__ void __launch_bounds__(128) residual_df_kernel(const double *A, int n, int nb, const float2 *Xs,
                                                           const int *tau, int sigma, const double *B, double *R,
                                                           int nrhs, double *amax) {
-    __shared__ float2 As[64][65];
+    __shared__ float2 As[64][33];
     __shared__ float4 Xp[64][8];  // (hi, lo) of right-hand sides 2j, 2j+1
-    __shared__ float part[4][65];
-    const int i0 = blockIdx.x * 64;
-    const int row = threadIdx.x & 63, grp = threadIdx.x >> 6;  // right-hand sides 4 grp .. 4 grp + 3
+    __shared__ float part[4][33];
+    const int i0 = blockIdx.x * 32;
+    const int row = threadIdx.x & 31, grp = threadIdx.x >> 5;  // right-hand sides 4 grp .. 4 grp + 3
     double acc[4] = {0.0, 0.0, 0.0, 0.0};
     float asum = 0.f;
     const int mt = n / nb;
     const double *tilerow = A + (size_t)nb * nb * (size_t)(i0 / nb) + (size_t)(i0 % nb);
     for (int p0 = 0; p0 < n; p0 += 64) {
         const double *blk = tilerow + (size_t)nb * nb * (size_t)mt * (p0 / nb) + (size_t)(p0 % nb) * nb;
-        for (int e = threadIdx.x; e < 4096; e += 256) As[e >> 6][e & 63] = split_df(blk[(e & 63) + (size_t)(e >> 6) * nb], sigma);
-        for (int e = threadIdx.x; e < 64 * 8; e += 256) {
+        for (int e = threadIdx.x; e < 2048; e += 128) As[e >> 5][e & 31] = split_df(blk[(e & 31) + (size_t)(e >> 5) * nb], sigma);
+        for (int e = threadIdx.x; e < 64 * 8; e += 128) {
             const float2 a = Xs[(size_t)(p0 + (e >> 3)) * 16 + 2 * (e & 7)];
             const float2 b = Xs[(size_t)(p0 + (e >> 3)) * 16 + 2 * (e & 7) + 1];
             Xp[e >> 3][e & 7] = make_float4(a.x, a.y, b.x, b.y);
@@ -152,11 +153,11 @@ __global__ void __launch_bounds__(256) residual_df_kernel(const double *A, int n
     if (amax) {
         part[grp][row] = asum;
         __syncthreads();
-        if (threadIdx.x < 64) {
+        if (threadIdx.x < 32) {
             double t = (double)part[0][row] + (double)part[1][row] + (double)part[2][row] + (double)part[3][row];
             t = ldexp(t, sigma);
             for (int o = 16; o; o >>= 1) t = fmax(t, __shfl_xor_sync(0xffffffffu, t, o));
-            if ((threadIdx.x & 31) == 0)
+            if (threadIdx.x == 0)
                 atomicMax(reinterpret_cast<unsigned long long *>(amax), (unsigned long long)__double_as_longlong(t));
         }
     }
@@ -540,7 +541,7 @@ cudaError_t mps_residual_df(const double *A, int n, int nb, const double *X, con
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
     note_launch();
-    mps::residual_df_kernel<<<n / 64, 256, 0, s>>>(A, n, nb, Xs, tau, sigma, B, R, nrhs, amax);
+    mps::residual_df_kernel<<<n / 32, 128, 0, s>>>(A, n, nb, Xs, tau, sigma, B, R, nrhs, amax);
     return cudaGetLastError();
 }
 cudaError_t mps_tile_to_f64(const float *w, double *d, int nb, cudaStream_t s) {
