@@ -5,9 +5,11 @@
 
 A step is one solve A X = B (16 right-hand sides, uniform [-1, 1)) of a device-resident
 SPD matrix A = B B^T + N I (seed = rank; the reference's tile layout) by the mixed-precision
-path: BF16 trailing updates on tcgen05 with FP32 accumulation, FP32 diagonal tiles and
-panels, FP64 residuals and refinement to the FP64-level normwise backward error
-(<= 1e-14 * N).  value = FP64-equivalent algorithmic flops (N^3/3) / time to solution
+path: BF16x3 trailing updates on tcgen05 (operands split into BF16 hi + lo, three products,
+FP32 accumulation; --precision bf16 / fp8 select one product), FP32 diagonal tiles and
+panels, compensated-FP32 refinement residuals (FP64 accumulation) and refinement to the
+FP64-level normwise backward error (<= 1e-14 * N), checked after the timed region with the
+FP64 residual.  value = FP64-equivalent algorithmic flops (N^3/3) / time to solution
 (factorization + refinement), summed over ranks (replicas, no collective on the data path).
 Inputs (8.6 GB) are far larger than L2 (129 MB): no flush is needed.
 
@@ -221,18 +223,19 @@ def peaks() -> dict:
         return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "source": "fallback"}
 
 
-def time_update_kernel(P, torch, n: int) -> dict:
-    """Live CUDA-event timing of one tcgen05 trailing update (step k = 0, BF16) on an FP32
-    tile matrix: flops and algorithmic bytes per launch (C read + write in FP32, packed
-    panel read once)."""
+def time_update_kernel(P, torch, n: int, precision: str = "bf16") -> dict:
+    """Live CUDA-event timing of one tcgen05 trailing update (step k = 0, the bench's update
+    precision) on an FP32 tile matrix, pack included: tensor flops and algorithmic bytes per
+    launch (C read + write in FP32, panel read once in FP32, packed operands written and read)."""
+    code = {"bf16": 1, "fp8": 2, "bf16x3": 3}.get(precision, 1)
     w = torch.randn(n * n, dtype=torch.float32, device="cuda")
     for _ in range(2):
-        P.lib().palial_gpu_mp_update_step(0, 1, w.data_ptr(), n, NB, 0)
+        P.lib().palial_gpu_mp_update_step(0, code, w.data_ptr(), n, NB, 0)
     ts = []
     for _ in range(3):
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e0.record()
-        P.lib().palial_gpu_mp_update_step(0, 1, w.data_ptr(), n, NB, 0)
+        P.lib().palial_gpu_mp_update_step(0, code, w.data_ptr(), n, NB, 0)
         e1.record()
         torch.cuda.synchronize()
         ts.append(e0.elapsed_time(e1) * 1e-3)
@@ -240,8 +243,10 @@ def time_update_kernel(P, torch, n: int) -> dict:
     torch.cuda.empty_cache()
     r = n // NB - 1
     pairs = r * (r + 1) // 2
-    flop = pairs * 2.0 * NB ** 3
-    byts = pairs * NB * NB * 8.0 + r * NB * NB * (4.0 + 2.0)   # C rmw + panel f32 read + bf16 write/read
+    products = 3 if code == 3 else 1
+    packed = {1: 2.0, 2: 1.0, 3: 4.0}[code]  # bytes per element of the packed panel(s)
+    flop = pairs * 2.0 * NB ** 3 * products
+    byts = pairs * NB * NB * 8.0 + r * NB * NB * (4.0 + 2.0 * packed)
     t = min(ts)
     return {"seconds": t, "flop": flop, "bytes": byts}
 
@@ -403,7 +408,7 @@ def main() -> None:
     ap.add_argument("--e2e-steps", type=int, default=2)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--n", type=int, default=N)
-    ap.add_argument("--precision", default="bf16")
+    ap.add_argument("--precision", default="bf16x3")
     ap.add_argument("--suite", default=None, choices=[None, "fp64", "kappa", "batched", "costmodel"])
     ap.add_argument("--batch", type=int, default=2000)
     ap.add_argument("--no-fp64", action="store_true")
@@ -493,7 +498,7 @@ def main() -> None:
 
     # roofline: live timing of the tcgen05 update kernel at its largest step
     pk = peaks()
-    upd = time_update_kernel(P, torch, n)
+    upd = time_update_kernel(P, torch, n, args.precision)
     gbs = upd["bytes"] / upd["seconds"] * 1e-9
 
     # e2e: host buffers through the C ABI
@@ -529,7 +534,7 @@ def main() -> None:
             "vs_baseline": None, "dtype": "bf16", "data": "synthetic",
             "config": {"workload": f"mixed-precision Cholesky + IR, N={n}, NB={NB}, 16 RHS, {args.precision} "
                                    "trailing updates on tcgen05 (FP32 accumulate), FP32 diagonal tiles and "
-                                   "panels, FP64 residuals; SPD B*B^T+N*I seed=rank, device-resident; inputs 8.6 GB >> L2 "
+                                   "panels, compensated-FP32 refinement residuals, FP64-checked backward error; SPD B*B^T+N*I seed=rank, device-resident; inputs 8.6 GB >> L2 "
                                    "(no flush needed)",
                        "n": n, "nb": NB, "nrhs": nrhs, "precision": args.precision,
                        "parallelism": f"replicas x{world}"},
@@ -545,7 +550,7 @@ def main() -> None:
                          # 199.0 MB, profiles/mp_update_and_residual_n8192.md), scaled by tile pairs
                          "traffic": 199.0e6 / 120 * ((n // NB - 1) * (n // NB) // 2),
                          "traffic_note": "scaled from an ncu capture at N=8192 step 0 by tile pairs",
-                         "kernel": "mp_update_kernel<bf16> (tcgen05, step k=0 of N=%d)" % n,
+                         "kernel": "mp_update_kernel<%s> (tcgen05, step k=0 of N=%d, pack included)" % (args.precision, n),
                          "tensor_tflops": upd["flop"] / upd["seconds"] * 1e-12,
                          "tensor_frac_of_bf16_peak": upd["flop"] / upd["seconds"] * 1e-12 / pk.get("bf16_tflops", 1900.0),
                          "peak_source": "MEASURED_PEAKS.json (of measured)" if "source" not in pk else "fallback"},
