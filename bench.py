@@ -380,21 +380,26 @@ def run_suite(args, P, torch) -> None:
     n, nrhs = args.n, 16
     b = torch.from_numpy(np.asfortranarray(
         __import__("oracle.oracle", fromlist=["x"]).gen_uniform(5, n, nrhs, stream=2)).ravel(order="F")).cuda()
+    import ctypes
     for alg in ("cholesky", "lu"):
         for kappa in (1e2, 1e6, 1e10):
             da = torch.empty(n * n, dtype=torch.float64, device="cuda")
             P.gen_kappa(da.data_ptr(), n, NB, kappa, alg == "cholesky", seed=7)
-            for prec in ("bf16", "fp8", "bf16x3", "auto"):
+            precs = ("bf16", "fp8", "bf16x3", "auto") + (("bf16x3-rbt",) if alg == "lu" else ())
+            for prec in precs:
                 dx = torch.zeros_like(b)
-                st = P.solve_ir(alg, da.data_ptr(), n, NB, b.data_ptr(), dx.data_ptr(), nrhs, precision=prec,
-                                ir_max_iter=30, raise_on_error=False)
+                o = P.make_opts(precision=prec.split("-")[0], ir_max_iter=30)
+                o.reserved[6] = 1 if prec.endswith("-rbt") else 0  # LU of the random-butterfly transform
+                st = P.Status()
+                st.code = P.lib().palial_gpu_solve_ir(P.ALG[alg], da.data_ptr(), n, NB, b.data_ptr(), dx.data_ptr(),
+                                                      nrhs, ctypes.byref(o), ctypes.byref(st), None)
                 print(json.dumps({"suite": "kappa", "alg": alg, "n": n, "kappa": kappa, "precision": prec,
                                   "converged": st.code in (0, 1), "code": st.code, "ir_iters": st.ir_iters,
                                   "gmres_iters": st.gmres_iters, "backward_error": st.backward_error,
                                   "seconds": st.seconds, "factor_seconds": st.factor_seconds, "shift": st.shift,
                                   "tflops_fp64_equiv": st.tflops,
-                                  "precision_used": P.PREC_NAME.get(int(st.kappa_est), prec)
-                                  if prec == "auto" else prec}), flush=True)
+                                  "precision_used": (P.PREC_NAME.get(int(st.kappa_est), prec)
+                                                     if prec == "auto" else prec)}), flush=True)
             del da
             torch.cuda.empty_cache()
 

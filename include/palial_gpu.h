@@ -140,7 +140,12 @@ int palial_gpu_factor_dev(int alg, double *dA, double *dS, int n, int nb, const 
  * pairs, error-free products and sums, FP64 accumulation every 64 terms; its error is below
  * 1e-12 of the backward error's scale).  When the tolerance is below 1e-11 (or
  * opts->reserved[4] = 2) convergence is confirmed with an FP64 residual; opts->reserved[4] =
- * 1 computes every residual in FP64. */
+ * 1 computes every residual in FP64.
+ * Opt-in stabilised LU (alg = PALIAL_ALG_LU, mixed precisions): opts->reserved[6] = 1 factors
+ * the random-butterfly transform U^T A V (depth-2 recursive butterflies, Parker 1995) without
+ * pivoting instead of A, refines against A (seed: opts->reserved[7], 0 = 1).  The AUTO ladder
+ * for LU tries BF16, BF16x3, BF16x3 on the butterfly transform, then FP64; status.kappa_est
+ * reports the rung that produced the result (PALIAL_PREC_*, + 100 for the butterfly rung). */
 int palial_gpu_solve_ir(int alg, const double *dA, int n, int nb, const double *dB, double *dX,
                         int nrhs, const palial_opts *opts, palial_status *st, void *stream);
 /* Same with host buffers: A in the reference's tile layout (descriptor), B and X n x nrhs
@@ -175,6 +180,27 @@ int palial_gpu_qr_solve(int rows, int cols, int nb, const double *dA, const doub
 /* Same with host buffers (A in tile layout, B and X column-major, resid optional). */
 int palial_gpu_qr_solve_host(int rows, int cols, int nb, const double *A, const double *B, double *X, int nrhs,
                              double *resid, const palial_opts *opts, palial_status *st);
+
+/* ---- layout bridges, any N, tiled-matrix files (no reference counterpart) ------------------
+ * The reference requires N % NB == 0 and the tile layout (palial_src/main.c:101-105,
+ * include/tile_address.h:9-17).  These convert LAPACK column-major matrices (device) to and
+ * from the tile layout, padding to npad = the next multiple of nb: the padding is zero except
+ * its diagonal (pad_diag; 1 for LU, the matrix' diagonal scale for Cholesky), so the leading
+ * n x n block of the padded matrix' factors is the factor of the original. */
+int palial_gpu_padded_size(int n, int nb);
+int palial_gpu_colmajor_to_tiles(const double *dC, long long ldc, int n, double *dT, int npad, int nb,
+                                 double pad_diag, void *stream);
+int palial_gpu_tiles_to_colmajor(const double *dT, int npad, int nb, double *dC, long long ldc, int n, void *stream);
+/* A X = B for a column-major A of any n (device buffers, lda/ldb/ldx leading dimensions):
+ * padded internally, solved by palial_gpu_solve_ir (opts as there), X = the first n rows. */
+int palial_gpu_solve_colmajor(int alg, int n, const double *dA, long long lda, const double *dB, long long ldb,
+                              double *dX, long long ldx, int nrhs, int nb, const palial_opts *opts, palial_status *st,
+                              void *stream);
+/* Tiled-matrix file (host): 8-byte magic "PALTILE1", int64 n, int64 nb, int64 flags (0), then
+ * the n*n doubles of the tile layout in memory order, little-endian.  palial_tiles_read fills
+ * n and nb and, when dst is not NULL, reads the n*n doubles into it. */
+int palial_tiles_write(const char *path, const palial_desc *A);
+int palial_tiles_read(const char *path, int *n_out, int *nb_out, double *dst);
 
 /* ---- single-tile kernels on device pointers (reference tile-kernel ABI, for unit tests) ----
  * Each runs one tile task on one CTA of the persistent scheduler's kernels.

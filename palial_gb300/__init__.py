@@ -25,6 +25,7 @@ ERR = {
 ALG = {"cholesky": 0, "lu": 1, "qr": 2}
 PREC = {"fp64": 0, "bf16": 1, "fp8": 2, "bf16x3": 3, "auto": 4}
 PREC_NAME = {v: k for k, v in PREC.items()}
+PREC_NAME[100 + PREC["bf16x3"]] = "bf16x3-rbt"  # AUTO ladder rung: BF16x3 on the butterfly transform
 
 
 class PalialError(RuntimeError):
@@ -126,6 +127,14 @@ def lib() -> ctypes.CDLL:
         h.palial_gpu_batch_autotune.argtypes = [i, vp, vp, ctypes.c_uint64, i, vp, vp, ctypes.POINTER(Status)]
         h.palial_gpu_batch_synthetic.argtypes = [i, ctypes.c_uint64, i, i, i, vp, i, ctypes.POINTER(Opts),
                                                  ctypes.POINTER(Status), vp]
+        h.palial_gpu_colmajor_to_tiles.argtypes = [vp, ctypes.c_longlong, i, vp, i, i, d, vp]
+        h.palial_gpu_tiles_to_colmajor.argtypes = [vp, i, i, vp, ctypes.c_longlong, i, vp]
+        h.palial_gpu_solve_colmajor.argtypes = [i, i, vp, ctypes.c_longlong, vp, ctypes.c_longlong, vp,
+                                                ctypes.c_longlong, i, i, ctypes.POINTER(Opts), ctypes.POINTER(Status),
+                                                vp]
+        h.palial_tiles_write.argtypes = [ctypes.c_char_p, ctypes.POINTER(Desc)]
+        h.palial_tiles_read.argtypes = [ctypes.c_char_p, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int),
+                                        vp]
         _lib = h
     return _lib
 
@@ -242,6 +251,33 @@ def qr_solve_host(a_tiles: np.ndarray, rows: int, cols: int, nb: int, b: np.ndar
                                         ctypes.byref(st))
     _check(rc, st)
     return x, resid, st
+
+
+def tiles_write(path: str, a_tiles: np.ndarray, n: int, nb: int) -> None:
+    """Write a tile-layout matrix in the library's tiled-matrix file format."""
+    a = np.ascontiguousarray(a_tiles, dtype=np.float64)
+    _check(lib().palial_tiles_write(path.encode(), ctypes.byref(desc(a, n, nb))), None)
+
+
+def tiles_read(path: str) -> tuple[np.ndarray, int, int]:
+    """Read a tiled-matrix file: (tile-layout buffer, n, nb)."""
+    n, nb = ctypes.c_int(), ctypes.c_int()
+    _check(lib().palial_tiles_read(path.encode(), ctypes.byref(n), ctypes.byref(nb), None), None)
+    out = np.empty(n.value * n.value, dtype=np.float64)
+    _check(lib().palial_tiles_read(path.encode(), ctypes.byref(n), ctypes.byref(nb), out.ctypes.data), None)
+    return out, n.value, nb.value
+
+
+def solve_colmajor(alg: str, n: int, d_a: int, lda: int, d_b: int, ldb: int, d_x: int, ldx: int, nrhs: int,
+                   nb: int = 512, stream: int = 0, raise_on_error: bool = True, **kw) -> Status:
+    """A X = B for a column-major device A of any n (padded to a multiple of nb internally)."""
+    st = Status()
+    rc = lib().palial_gpu_solve_colmajor(ALG[alg], n, d_a, lda, d_b, ldb, d_x, ldx, nrhs, nb,
+                                         ctypes.byref(make_opts(**kw)), ctypes.byref(st), stream or None)
+    if raise_on_error:
+        _check(rc, st, allow=(PALIAL_OK, 1))
+    st.code = rc
+    return st
 
 
 def qr_solve_dag(rows: int, cols: int, nb: int, nrhs: int, nworkers: int = 152, seed: int = 0) -> dict:

@@ -86,6 +86,10 @@ extern State g;
 
 // Free the QR solve's cached device buffers and DAG (palial_gpu_finalize).
 void qr_solve_release();
+// Free the layout bridges' padded buffers (palial_gpu_finalize).
+void layout_release();
+// Free the random butterflies (palial_gpu_finalize).
+void rbt_release();
 
 // Read-only NVML query of the library's device (false and -1 values without NVML).
 bool nvml_sample(double *sm_mhz, double *sm_max_mhz, long long *reasons);

@@ -52,6 +52,9 @@ cudaError_t mps_add_correction(double *X, const float *D32, long long n, int col
 cudaError_t mps_mark_step(int *status, int k, cudaStream_t s);
 cudaError_t mpr_solve(const float *W, const float *Dinv, int n, int nb, int kind, float *R, float *Y, int *status,
                       cudaStream_t s);
+cudaError_t rbt_prepare(int n, uint64_t seed);
+cudaError_t rbt_transform_matrix(const double *A, float *W, int n, int nb, double *amax, cudaStream_t s);
+cudaError_t rbt_transform_vectors(float *X, int n, int cols, int which, cudaStream_t s);
 cudaError_t mpd_factor_tile(int alg, float *W, int n, int nb, int k, int *status, cudaStream_t s);
 cudaError_t mps_invert_diag(const float *W, int n, int nb, float *Dinv, int kind, cudaStream_t s);
 cudaError_t mps_rhs_step(const float *W, const float *Dinv, int n, int nb, int k, float *R, float *S, int kind,
@@ -197,6 +200,14 @@ int mp_prepare_solves(int alg, const float *W, int n, int nb, cudaStream_t s, pa
     return PALIAL_OK;
 }
 
+// State of the current solve shared by the refinement helpers: which residual steers, and
+// whether the factors are those of the random-butterfly transform.
+struct ResidCtx {
+    bool df = false;
+    int sigma = 0;
+    bool rbt = false;  // the factors are those of U^T A V (random butterflies, LU)
+} g_rctx;
+
 // d = M^-1 r for the FP32 factors in W; R32 (n x 16, zero padded) in/out.  Block forward and
 // backward substitution over tile rows: the diagonal step multiplies by the stored inverse,
 // the update step subtracts the solved tile row from the remaining ones.
@@ -223,8 +234,10 @@ int precondition(int alg, const float *W, int n, int nb, const double *v, double
     }
     PALIAL_CK(cudaMemcpyAsync(dscale, hscale.data(), sizeof(double) * nrhs, cudaMemcpyHostToDevice, s), "scale");
     PALIAL_CK(mps_to_f32_rhs(v, mb.r32.as<float>(), n, nrhs, dscale, s), "to f32");
+    if (g_rctx.rbt) PALIAL_CK(rbt_transform_vectors(mb.r32.as<float>(), n, 16, 0, s), "U^T r");
     int rc = mp_apply_inverse(alg, W, n, nb, mb.r32.as<float>(), s, st);
     if (rc) return rc;
+    if (g_rctx.rbt) PALIAL_CK(rbt_transform_vectors(mb.r32.as<float>(), n, 16, 1, s), "V y");
     PALIAL_CK(mps_from_f32_rhs(z, mb.r32.as<float>(), n, nrhs, dscale, s), "from f32");
     return PALIAL_OK;
 }
@@ -232,10 +245,6 @@ int precondition(int alg, const float *W, int n, int nb, const double *v, double
 // A X products of the refinement (B - A X, or A X with B = NULL): the compensated-FP32
 // residual when the current solve uses it (GMRES's inner products need far less than FP64),
 // else FP64.
-struct ResidCtx {
-    bool df = false;
-    int sigma = 0;
-} g_rctx;
 static cudaError_t apply_A(const double *A, int n, int nb, const double *X, const double *B, double *R, int nrhs,
                            cudaStream_t s) {
     if (!g_rctx.df) return mps_residual(A, n, nb, X, B, R, nrhs, nullptr, s);
@@ -489,6 +498,7 @@ static int solve_one(int alg, const double *dA, int n, int nb, const double *dB,
     double shift = 0.0;
     const auto f0 = std::chrono::steady_clock::now();
     if (prec == PALIAL_PREC_FP64) {
+        g_rctx.rbt = false;
         PALIAL_CK(g.mat.ensure(sizeof(double) * nn), "alloc copy");
         PALIAL_CK(cudaMemcpyAsync(g.mat.ptr, dA, sizeof(double) * nn, cudaMemcpyDeviceToDevice, s), "copy");
         palial_opts fo = o;
@@ -503,8 +513,15 @@ static int solve_one(int alg, const double *dA, int n, int nb, const double *dB,
         PALIAL_CK(mps_f64_to_f32(g.mat.as<double>(), W, n, nb, 0.0, s), "factor to f32");
     } else {
         PALIAL_CK(cudaMemsetAsync(nrm + 120, 0, sizeof(double), s), "max |a|");
+        // opts.reserved[6] = 1: LU of the random-butterfly transform U^T A V (rbt.cu)
+        const bool rbt = alg == 1 && o.reserved[6] == 1;
+        g_rctx.rbt = rbt;
+        if (rbt) PALIAL_CK(rbt_prepare(n, o.reserved[7] ? (uint64_t)o.reserved[7] : 1ull), "butterflies");
         for (int attempt = 0; attempt < 4; attempt++) {
-            PALIAL_CK(mps_f64_to_f32(dA, W, n, nb, shift, s, attempt == 0 ? nrm + 120 : nullptr), "convert");
+            if (rbt)
+                PALIAL_CK(rbt_transform_matrix(dA, W, n, nb, attempt == 0 ? nrm + 120 : nullptr, s), "butterfly transform");
+            else
+                PALIAL_CK(mps_f64_to_f32(dA, W, n, nb, shift, s, attempt == 0 ? nrm + 120 : nullptr), "convert");
             rc = mp_factor(alg, prec, W, n, nb, s, st, &zp);
             if (rc != PALIAL_ERR_NOT_SPD || alg != 0) break;
             if (anorm < 0) {
@@ -673,12 +690,17 @@ extern "C" int palial_gpu_solve_ir(int alg, const double *dA, int n, int nb, con
     palial_opts_default(&o);
     if (opts) o = *opts;
     if (o.precision != PALIAL_PREC_AUTO) return solve_one(alg, dA, n, nb, dB, dX, nrhs, &o, st, stream);
-    static const int ladder[] = {PALIAL_PREC_BF16, PALIAL_PREC_BF16X3, PALIAL_PREC_FP64};
+    // LU adds a BF16x3 rung on the random-butterfly transform before the FP64 factorization
+    static const int ladder_chol[] = {PALIAL_PREC_BF16, PALIAL_PREC_BF16X3, PALIAL_PREC_FP64, -1};
+    static const int ladder_lu[] = {PALIAL_PREC_BF16, PALIAL_PREC_BF16X3, 100 + PALIAL_PREC_BF16X3, PALIAL_PREC_FP64};
+    const int *ladder = alg == 1 ? ladder_lu : ladder_chol;
     const auto t0 = std::chrono::steady_clock::now();
     int rc = PALIAL_ERR_NOT_CONVERGED;
     int used = -1;
-    for (int prec : ladder) {
+    for (int li = 0; li < 4 && ladder[li] >= 0; li++) {
+        const int prec = ladder[li] % 100;
         o.precision = prec;
+        o.reserved[6] = ladder[li] >= 100 ? 1 : opts ? opts->reserved[6] : 0;
         // lower rungs get a bounded effort: BF16 plain refinement that must contract 10x per
         // step, BF16x3 at most 10 outer iterations and 100 GMRES steps
         palial_opts oo = o;
@@ -693,7 +715,7 @@ extern "C" int palial_gpu_solve_ir(int alg, const double *dA, int n, int nb, con
             oo.reserved[3] = 100;
         }
         rc = solve_one(alg, dA, n, nb, dB, dX, nrhs, &oo, st, stream);
-        used = prec;
+        used = ladder[li];  // 100 + p: precision p on the random-butterfly transform
         if (rc >= 0) break;
         if (rc != PALIAL_ERR_NOT_CONVERGED && rc != PALIAL_ERR_NOT_SPD) break;
     }

@@ -223,6 +223,8 @@ int palial_gpu_finalize(void) {
     for (DevBuf *b : {&g.mat, &g.smat, &g.kbuf, &g.probe}) b->release();
     qr_solve_release();
     mpr_release();
+    layout_release();
+    rbt_release();
     g.dags.clear();
     return PALIAL_OK;
 }

@@ -231,3 +231,64 @@ def test_refinement_with_compensated_residual_reports_fp64_error():
         assert rc == 0 and st.backward_error <= 1e-14 * n, (r4, rc, st.backward_error)
         xs.append(dx.cpu().numpy())
     assert np.linalg.norm(xs[0] - xs[1]) / np.linalg.norm(xs[1]) < 1e-11
+
+
+def _solve_lu(da, n, nb, db, nrhs, precision, rbt, maxit=30):
+    import ctypes
+    dx = torch.zeros_like(db)
+    o = P.make_opts(precision=precision, ir_max_iter=maxit)
+    o.reserved[6] = 1 if rbt else 0
+    st = P.Status()
+    rc = P.lib().palial_gpu_solve_ir(1, da.data_ptr(), n, nb, db.data_ptr(), dx.data_ptr(), nrhs, ctypes.byref(o),
+                                     ctypes.byref(st), None)
+    return rc, st, dx
+
+
+def _block_antidiagonal(n):
+    """[[0, B], [C, 0]] with B, C = I + 0.5 G / sqrt(n/2) (G uniform in [-1, 1)): well
+    conditioned, but its leading entry is zero, so LU without pivoting breaks down at its
+    first pivot."""
+    h = n // 2
+    g = O.gen_uniform(21, n)
+    a = np.zeros((n, n))
+    a[:h, h:] = np.eye(h) + 0.5 * g[:h, :h] / np.sqrt(h)
+    a[h:, :h] = np.eye(h) + 0.5 * g[h:, h:] / np.sqrt(h)
+    return a
+
+
+@pytest.mark.parametrize("precision", ["bf16", "bf16x3"])
+def test_random_butterfly_lu_matches_numpy(precision):
+    """LU of U^T A V (depth-2 random butterflies) as the preconditioner, refinement against A.
+    On a block anti-diagonal matrix the no-pivot LU of A itself breaks down (zero pivot); the
+    butterflies mix row i with rows i + n/4, i + n/2, i + 3n/4, and the transformed matrix
+    factors with growth near 1, so refinement reaches the FP64 target."""
+    n, nb, nrhs = 2048, 256, 4
+    a = _block_antidiagonal(n)
+    b = O.gen_uniform(12, n, nrhs)
+    da = torch.from_numpy(O.to_tiles(a, nb)).cuda()
+    db = torch.from_numpy(np.asfortranarray(b).ravel(order="F")).cuda()
+    rc_plain, _, _ = _solve_lu(da, n, nb, db, nrhs, precision, False)
+    assert rc_plain != 0
+    rc, st, dx = _solve_lu(da, n, nb, db, nrhs, precision, True)
+    assert rc == 0, (rc, st.backward_error, st.ir_iters)
+    x = dx.cpu().numpy().reshape(nrhs, n).T
+    # forward error within kappa (2.3) times the backward-error target 1e-14 n
+    assert np.linalg.norm(x - np.linalg.solve(a, b)) / np.linalg.norm(x) < 1e-10
+    assert st.backward_error <= 1e-14 * n
+
+
+def test_random_butterfly_on_dense_matrix_agrees():
+    """On a dense A = U diag(s) V^T (orthogonal factors, kappa 1e2) both the plain no-pivot LU
+    and the butterfly transform's LU precondition refinement to the FP64 target, and the two
+    solutions agree: the transform changes the preconditioner, not the answer."""
+    n, nb, nrhs = 4096, 512, 4
+    da = torch.empty(n * n, dtype=torch.float64, device="cuda")
+    P.gen_kappa(da.data_ptr(), n, nb, 1e2, False, seed=7)
+    b = O.gen_uniform(5, n, nrhs, stream=O.STREAM_RHS)
+    db = torch.from_numpy(np.asfortranarray(b).ravel(order="F")).cuda()
+    rc_plain, st_plain, x_plain = _solve_lu(da, n, nb, db, nrhs, "bf16x3", False)
+    rc, st, x_rbt = _solve_lu(da, n, nb, db, nrhs, "bf16x3", True)
+    assert rc_plain == 0 and rc == 0, (rc_plain, rc)
+    assert st.backward_error <= 1e-14 * n
+    # both within kappa * (backward-error target 1e-14 n) of the exact solution
+    assert (torch.linalg.vector_norm(x_rbt - x_plain) / torch.linalg.vector_norm(x_plain)).item() < 2 * 1e2 * 1e-14 * n
