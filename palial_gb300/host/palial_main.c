@@ -29,6 +29,12 @@
  *                           any precision other than fp64 implies --rhs 1 when --rhs is absent
  *   --ir-tol T, --ir-max N  refinement target backward error and iteration cap
  *   --gmres -1|0|1          GMRES-IR never / automatic / always
+ *   --butterfly SEED        LU: factor the random-butterfly transform U^T A V (depth 2, seeded;
+ *                           SEED 0 = default) as the refinement's preconditioner; no pivoting
+ * Tiled-matrix files ("PALTILE1": magic, int64 n, nb, flags, then the tile layout):
+ *   --load FILE             the input matrix from FILE (-m/-b optional; must match when given)
+ *   --save FILE             write the input matrix to FILE before the run
+ *   --save-result FILE      write the factored matrix to FILE (factorization mode)
  * Batch mode (no -a/-m/-b needed):
  *   --batch COUNT           the synthetic uneven batch: COUNT matrices, N log-uniform in
  *                           [32, 2048), half Cholesky half LU, one persistent launch
@@ -119,11 +125,11 @@ int main(int argc, char *argv[])
     char algorithm[16] = "";
     int gen = 2, check = 0, quiet = 0, nrhs = 0, batch = 0, autotune = 0, clocks = 0, seed_given = 0;
     unsigned long long seed = 0;
-    const char *trace = NULL, *trace_csv = NULL;
+    const char *trace = NULL, *trace_csv = NULL, *load = NULL, *save = NULL, *save_result = NULL;
     palial_opts_default(&palial_entry_opts);
     enum {
         O_GEN = 1000, O_SEED, O_BLOCK, O_PRIO, O_TRACE, O_TRACECSV, O_CHECK, O_QUIET, O_PREC, O_RHS, O_IRTOL,
-        O_IRMAX, O_GMRES, O_BATCH, O_AUTOTUNE, O_CLOCKS
+        O_IRMAX, O_GMRES, O_BATCH, O_AUTOTUNE, O_CLOCKS, O_BUTTERFLY, O_LOAD, O_SAVE, O_SAVERES
     };
     struct option long_options[] = {
         {"Algorithm", required_argument, NULL, 'a'}, {"Matrix size", required_argument, NULL, 'm'},
@@ -135,7 +141,9 @@ int main(int argc, char *argv[])
         {"rhs", required_argument, NULL, O_RHS},     {"ir-tol", required_argument, NULL, O_IRTOL},
         {"ir-max", required_argument, NULL, O_IRMAX}, {"gmres", required_argument, NULL, O_GMRES},
         {"batch", required_argument, NULL, O_BATCH}, {"autotune", no_argument, NULL, O_AUTOTUNE},
-        {"clocks", no_argument, NULL, O_CLOCKS},     {NULL, no_argument, NULL, 0}};
+        {"clocks", no_argument, NULL, O_CLOCKS},     {"butterfly", required_argument, NULL, O_BUTTERFLY},
+        {"load", required_argument, NULL, O_LOAD},   {"save", required_argument, NULL, O_SAVE},
+        {"save-result", required_argument, NULL, O_SAVERES}, {NULL, no_argument, NULL, 0}};
     if (argc < 2) {
         printf("Missing arguments.\n");
         printf("Aborting...\n");
@@ -171,6 +179,13 @@ int main(int argc, char *argv[])
             case O_BATCH: batch = atoi(optarg); break;
             case O_AUTOTUNE: autotune = 1; break;
             case O_CLOCKS: clocks = 1; palial_entry_opts.trace = 1; break;
+            case O_BUTTERFLY:
+                palial_entry_opts.reserved[6] = 1;
+                palial_entry_opts.reserved[7] = (int)strtoul(optarg, NULL, 10);
+                break;
+            case O_LOAD: load = optarg; break;
+            case O_SAVE: save = optarg; break;
+            case O_SAVERES: save_result = optarg; break;
             default:
                 printf("Invalid arguments.\n");
                 printf("Aborting...\n");
@@ -182,6 +197,17 @@ int main(int argc, char *argv[])
         palial_gpu_finalize();
         return rc;
     }
+    if (load) {
+        int fn = 0, fnb = 0;
+        if (palial_tiles_read(load, &fn, &fnb, NULL) != PALIAL_OK || (MSIZE && MSIZE != fn) ||
+            (BSIZE && BSIZE != fnb)) {
+            printf("Invalid arguments.\n");
+            printf("Aborting...\n");
+            return 0;
+        }
+        MSIZE = fn;
+        BSIZE = fnb;
+    }
     if (BSIZE <= 0 || MSIZE <= 0 || MSIZE % BSIZE != 0) {
         printf("Tile size does not divide the matrix size. Aborting...\n");
         return 0;
@@ -192,7 +218,8 @@ int main(int argc, char *argv[])
     }
     const int alg = !strcmp(algorithm, "cholesky") ? 0 : !strcmp(algorithm, "lu") ? 1 : 2;
     if (palial_entry_opts.precision != PALIAL_PREC_FP64 && nrhs <= 0) nrhs = 1;
-    if (nrhs > 0 && ((alg != 2 && nrhs > 16) || (alg == 2 && (nrhs > BSIZE || palial_entry_opts.precision)))) {
+    if ((nrhs > 0 && ((alg != 2 && nrhs > 16) || (alg == 2 && (nrhs > BSIZE || palial_entry_opts.precision)))) ||
+        (palial_entry_opts.reserved[6] && (alg != 1 || nrhs <= 0))) {
         printf("Invalid arguments.\n");
         printf("Aborting...\n");
         return 0;
@@ -205,9 +232,14 @@ int main(int argc, char *argv[])
     }
     MATRIX_desc A = palial_matrix_desc_init(BSIZE, (long)MSIZE * MSIZE, (long)BSIZE * BSIZE, MSIZE);
     A.matrix = ptr;
-    int rc = palial_gpu_generate(gen, seed, (const palial_desc *)&A);
+    int rc = load ? palial_tiles_read(load, NULL, NULL, ptr) : palial_gpu_generate(gen, seed, (const palial_desc *)&A);
     if (rc) {
-        fprintf(stderr, "palial: input generation failed: %s\n", palial_gpu_error_string(rc));
+        fprintf(stderr, "palial: input %s failed: %s\n", load ? "file" : "generation", palial_gpu_error_string(rc));
+        free(ptr);
+        return 1;
+    }
+    if (save && palial_tiles_write(save, (const palial_desc *)&A) != PALIAL_OK) {
+        fprintf(stderr, "palial: cannot write %s\n", save);
         free(ptr);
         return 1;
     }
@@ -267,6 +299,8 @@ int main(int argc, char *argv[])
     const palial_status st = palial_entry_status;
     double resid = -1.0;
     if (check && orig && st.code >= 0) palial_gpu_residual_host(alg, orig, (const palial_desc *)&A, 8, 7, &resid);
+    if (save_result && st.code >= 0 && palial_tiles_write(save_result, (const palial_desc *)&A) != PALIAL_OK)
+        fprintf(stderr, "palial: cannot write %s\n", save_result);
     if (trace && st.code >= 0) palial_gpu_trace_dump(trace, trace_csv);
     else if (trace_csv && st.code >= 0) palial_gpu_trace_dump("/dev/null", trace_csv);
     if (!quiet) {

@@ -4,6 +4,7 @@ import json
 import os
 import subprocess
 
+import numpy as np
 import pytest
 
 import palial_gb300 as P
@@ -88,3 +89,54 @@ def test_trace_file(tmp_path):
     assert rc == 0 and out == ""
     lines = f.read_text().splitlines()
     assert len(lines) == 4 + 6 + 6 + 4 and lines[0].startswith("potrf000, ")
+
+
+def test_load_rejects_bad_or_mismatched_files(tmp_path):
+    f = tmp_path / "a.palt"
+    assert run("-a", "lu", "--load", str(f))[1].startswith("Invalid arguments.")  # missing file
+    n, nb = 256, 128
+    P.tiles_write(str(f), np.zeros(n * n), n, nb)
+    assert run("-a", "lu", "-m", "512", "--load", str(f))[1].startswith("Invalid arguments.")
+    assert run("-a", "lu", "-b", "64", "--load", str(f))[1].startswith("Invalid arguments.")
+
+
+def test_butterfly_needs_lu_solve():
+    assert run("-a", "cholesky", "-m", "1024", "-b", "256", "--rhs", "1", "--butterfly", "3")[1].startswith("Invalid")
+    assert run("-a", "lu", "-m", "1024", "-b", "256", "--butterfly", "3")[1].startswith("Invalid")
+
+
+@pytest.mark.gpu
+def test_save_load_roundtrip(tmp_path):
+    """The generated input saved, loaded back and factored gives the same factors (bit for bit:
+    the schedule-independent FP64 path), and the saved factors read back as a tile matrix."""
+    src, f1, f2 = tmp_path / "in.palt", tmp_path / "f1.palt", tmp_path / "f2.palt"
+    rc, out = run("-a", "lu", "-m", "1024", "-b", "256", "--gen", "uniform", "--seed", "4", "--save", str(src),
+                  "--save-result", str(f1))
+    assert rc == 0 and _json(out)["code"] == 0
+    rc, out = run("-a", "lu", "--load", str(src), "--save-result", str(f2))
+    j = _json(out)
+    assert rc == 0 and j["code"] == 0 and (j["n"], j["nb"]) == (1024, 256)
+    a, n, nb = P.tiles_read(str(f1))
+    b, _, _ = P.tiles_read(str(f2))
+    assert (n, nb) == (1024, 256) and np.array_equal(a, b)
+    orig, _, _ = P.tiles_read(str(src))
+    assert not np.array_equal(orig, a)
+
+
+@pytest.mark.gpu
+def test_butterfly_solve_mode(tmp_path):
+    """A block anti-diagonal matrix written as a tile file: the plain no-pivot LU fails at its
+    zero pivot, the butterfly-preconditioned solve reaches the FP64 target."""
+    from oracle import oracle as O
+    n, nb, h = 1024, 256, 512
+    g = O.gen_uniform(21, n)
+    a = np.zeros((n, n))
+    a[:h, h:] = np.eye(h) + 0.5 * g[:h, :h] / np.sqrt(h)
+    a[h:, :h] = np.eye(h) + 0.5 * g[h:, h:] / np.sqrt(h)
+    f = tmp_path / "a.palt"
+    P.tiles_write(str(f), O.to_tiles(a, nb), n, nb)
+    rc, out = run("--load", str(f), "-a", "lu", "--precision", "bf16x3", "--rhs", "2")
+    assert rc == 1 and _json(out)["code"] < 0
+    rc, out = run("--load", str(f), "-a", "lu", "--precision", "bf16x3", "--rhs", "2", "--butterfly", "5")
+    j = _json(out)
+    assert rc == 0 and j["code"] in (0, 1) and j["backward_error"] <= 1e-14 * n
