@@ -131,8 +131,8 @@ int palial_gpu_factor_dev(int alg, double *dA, double *dS, int n, int nb, const 
  * A an FP64 tile-layout matrix on the device (not modified).  alg: PALIAL_ALG_CHOLESKY or
  * PALIAL_ALG_LU (no pivoting).  opts->precision selects the trailing-update precision
  * (PALIAL_PREC_BF16 / FP8 / BF16X3 on tcgen05 with FP32 accumulation, or FP64); diagonal
- * tiles are factored in FP64, panels solved in FP32, residuals r = b - A x and corrections in
- * FP64.  Iterates until the normwise backward error max_j |r_j|/(|A| |x_j| + |b_j|) (inf-
+ * tiles are factored and panels solved in FP32, residuals r = b - A x and corrections in
+ * FP64 storage.  Iterates until the normwise backward error max_j |r_j|/(|A| |x_j| + |b_j|) (inf-
  * norms) <= opts->ir_tol (default 1e-14 * n); GMRES-IR when plain refinement stagnates
  * (opts->gmres: -1 never, 0 automatic, 1 always).  NB must be a multiple of 256.
  * Returns PALIAL_ERR_NOT_CONVERGED (with the reached error in st) if the target is missed.
@@ -140,7 +140,11 @@ int palial_gpu_factor_dev(int alg, double *dA, double *dS, int n, int nb, const 
  * pairs, error-free products and sums, FP64 accumulation every 64 terms; its error is below
  * 1e-12 of the backward error's scale).  When the tolerance is below 1e-11 (or
  * opts->reserved[4] = 2) convergence is confirmed with an FP64 residual; opts->reserved[4] =
- * 1 computes every residual in FP64.
+ * 1 computes every residual in FP64.  Once a correction d is small (2^-17 ||d|| <= tol/4 ||x||
+ * per column) the next residual is r - A d with FP32 products (one HBM-bound pass over A);
+ * their error bounds are summed and convergence requires backward error + bound <= tol (else
+ * the residual is recomputed in full).  opts->reserved[4] = 3 computes every residual in
+ * full instead.  The status message counts the update-form residuals.
  * Opt-in stabilised LU (alg = PALIAL_ALG_LU, mixed precisions): opts->reserved[6] = 1 factors
  * the random-butterfly transform U^T A V (depth-2 recursive butterflies, Parker 1995) without
  * pivoting instead of A, refines against A (seed: opts->reserved[7], 0 = 1).  The AUTO ladder
@@ -154,7 +158,8 @@ int palial_gpu_solve_ir_host(int alg, const palial_desc *A, const double *B, dou
                              const palial_opts *opts, palial_status *st);
 /* R = B - A X (B may be NULL: R = A X) on device buffers, A an FP64 tile matrix, X, B, R
  * n x nrhs column-major (nrhs <= 16): mode 0 in FP64, mode 1 with the compensated FP32
- * arithmetic the refinement steers with. */
+ * arithmetic the refinement steers with; mode 2 (B must be NULL) is the refinement's update
+ * form R <- R - A X with FP32 products (|error| <= 2^-17 |A| |X| per entry). */
 int palial_gpu_residual(const double *dA, int n, int nb, const double *dX, const double *dB, double *dR, int nrhs,
                         int mode, void *stream);
 /* The low-precision factorization alone: dW (n*n floats, tile layout) receives the FP32

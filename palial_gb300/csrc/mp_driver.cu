@@ -39,6 +39,8 @@ cudaError_t mps_f64_to_f32(const double *A, float *W, int n, int nb, double shif
                            double *amax = nullptr);
 cudaError_t mps_residual_df(const double *A, int n, int nb, const double *X, const double *colmax, const double *B,
                             double *R, int nrhs, int sigma, float2 *Xs, int *tau, double *amax, cudaStream_t s);
+cudaError_t mps_residual_update(const double *A, int n, int nb, const double *D, const double *colmax, double *R,
+                                int nrhs, int sigma, float *Ds, int *tau, cudaStream_t s);
 cudaError_t mps_tile_to_f64(const float *w, double *d, int nb, cudaStream_t s);
 cudaError_t mps_tile_to_f32(const double *d, float *w, int nb, int upper_only, cudaStream_t s);
 cudaError_t mps_panel_trsm(float *W, int n, int nb, int k, int kind, cudaStream_t s);
@@ -561,7 +563,8 @@ static int solve_one(int alg, const double *dA, int n, int nb, const double *dB,
     // ---- refinement -------------------------------------------------------------------------
     const double tol = o.ir_tol > 0 ? o.ir_tol : 1e-14 * n;
     const int maxit = o.ir_max_iter > 0 ? o.ir_max_iter : 50;
-    std::vector<double> hb(nrhs), hr(nrhs), hx(nrhs), hscale(nrhs);
+    std::vector<double> hb(nrhs), hr(nrhs), hx(nrhs), hd(nrhs), hscale(nrhs), drift(nrhs, 0.0);
+    int resid_updates = 0;
     PALIAL_CK(mps_colmax(dB, n, nrhs, nrm + 49, s), "norm b");
     PALIAL_CK(cudaMemcpyAsync(hb.data(), nrm + 49, sizeof(double) * nrhs, cudaMemcpyDeviceToHost, s), "norm b");
     PALIAL_CK(cudaMemsetAsync(dX, 0, sizeof(double) * (size_t)n * nrhs, s), "x0");
@@ -598,13 +601,46 @@ static int solve_one(int alg, const double *dA, int n, int nb, const double *dB,
         const bool need_norm = anorm < 0;
         if (need_norm) PALIAL_CK(cudaMemsetAsync(nrm, 0, sizeof(double), s), "norm A");
         const bool used_df = use_df && !fp64_phase;
-        if (used_df) {
+        // Update form r <- r - A d for a small correction: FP32 products, error <= 2^-17 |A| |d|
+        // per entry, so at most 2^-17 ||d_j|| / ||x_j|| on column j's backward error; one
+        // HBM-bound pass over A instead of the issue-bound compensated residual.  drift[j]
+        // sums these bounds since the last full residual and convergence needs eta_j +
+        // drift_j <= tol.  Used while a step adds at most tol / 4; the first residual (d = x)
+        // is always full; opts.reserved[4] = 3 disables the form.
+        bool update_form = false;
+        if (used_df && !need_norm && o.reserved[4] != 3) {
+            PALIAL_CK(mps_colmax(dcorr, n, nrhs, nrm + 176, s), "norm d");
+            PALIAL_CK(cudaMemcpyAsync(hd.data(), nrm + 176, sizeof(double) * nrhs, cudaMemcpyDeviceToHost, s), "norm d");
+            PALIAL_CK(cudaMemcpyAsync(hx.data(), nrm + 33, sizeof(double) * nrhs, cudaMemcpyDeviceToHost, s), "norm x");
+            PALIAL_CK(cudaStreamSynchronize(s), "norm d");
+            update_form = true;
+            for (int j = 0; j < nrhs; j++) {
+                const double step = std::ldexp(hd[j], -17) / hx[j];
+                update_form = update_form && std::isfinite(step) && step <= tol / 4.0;
+            }
+        }
+        const auto full_residual = [&](double *anorm_out) -> int {
+            if (used_df) {
+                float2 *xs = mb.xsplit.as<float2>();
+                PALIAL_CK(mps_residual_df(dA, n, nb, dX, nrm + 33, dB, mb.r.as<double>(), nrhs, sigma, xs,
+                                          reinterpret_cast<int *>(xs + (size_t)n * 16), anorm_out, s),
+                          "residual (compensated FP32)");
+            } else {
+                PALIAL_CK(mps_residual(dA, n, nb, dX, dB, mb.r.as<double>(), nrhs, anorm_out, s), "residual");
+            }
+            std::fill(drift.begin(), drift.end(), 0.0);
+            return PALIAL_OK;
+        };
+        if (update_form) {
             float2 *xs = mb.xsplit.as<float2>();
-            PALIAL_CK(mps_residual_df(dA, n, nb, dX, nrm + 33, dB, mb.r.as<double>(), nrhs, sigma, xs,
-                                      reinterpret_cast<int *>(xs + (size_t)n * 16), need_norm ? nrm : nullptr, s),
-                      "residual (compensated FP32)");
+            PALIAL_CK(mps_residual_update(dA, n, nb, dcorr, nrm + 176, mb.r.as<double>(), nrhs, sigma,
+                                          reinterpret_cast<float *>(xs), reinterpret_cast<int *>(xs + (size_t)n * 16), s),
+                      "residual (update form)");
+            resid_updates++;
+            for (int j = 0; j < nrhs; j++) drift[j] += std::ldexp(hd[j], -17) / hx[j];
         } else {
-            PALIAL_CK(mps_residual(dA, n, nb, dX, dB, mb.r.as<double>(), nrhs, need_norm ? nrm : nullptr, s), "residual");
+            rc = full_residual(need_norm ? nrm : nullptr);
+            if (rc) return rc;
         }
         if (need_norm) PALIAL_CK(cudaMemcpyAsync(&anorm, nrm, sizeof(double), cudaMemcpyDeviceToHost, s), "norm A");
         PALIAL_CK(mps_colmax(mb.r.as<double>(), n, nrhs, nrm + 17, s), "norm r");
@@ -612,14 +648,34 @@ static int solve_one(int alg, const double *dA, int n, int nb, const double *dB,
         PALIAL_CK(cudaMemcpyAsync(hx.data(), nrm + 33, sizeof(double) * nrhs, cudaMemcpyDeviceToHost, s), "norm x");
         PALIAL_CK(cudaStreamSynchronize(s), "iteration");
         eta = 0.0;
+        double eta_bound = 0.0;
         bool finite = true;
         for (int j = 0; j < nrhs; j++) {
             finite = finite && std::isfinite(hr[j]) && std::isfinite(hx[j]);
-            eta = std::max(eta, hr[j] / (anorm * hx[j] + hb[j]));
+            const double ej = hr[j] / (anorm * hx[j] + hb[j]);
+            eta = std::max(eta, ej);
+            eta_bound = std::max(eta_bound, ej + drift[j]);
         }
         if (!finite || !std::isfinite(eta)) {
             eta = INFINITY;
             break;
+        }
+        if (eta <= tol && eta_bound > tol) {
+            // the update form's drift leaves the decision open: recompute the residual in full
+            rc = full_residual(nullptr);
+            if (rc) return rc;
+            PALIAL_CK(mps_colmax(mb.r.as<double>(), n, nrhs, nrm + 17, s), "norm r");
+            PALIAL_CK(cudaMemcpyAsync(hr.data(), nrm + 17, sizeof(double) * nrhs, cudaMemcpyDeviceToHost, s), "norm r");
+            PALIAL_CK(cudaStreamSynchronize(s), "full residual");
+            eta = 0.0;
+            for (int j = 0; j < nrhs; j++) {
+                finite = finite && std::isfinite(hr[j]);
+                eta = std::max(eta, hr[j] / (anorm * hx[j] + hb[j]));
+            }
+            if (!finite || !std::isfinite(eta)) {
+                eta = INFINITY;
+                break;
+            }
         }
         // The compensated residual's error is below 1e-12 of the backward error's scale
         // (tested); a tolerance 10x above that needs no FP64 confirmation.
@@ -676,8 +732,9 @@ static int solve_one(int alg, const double *dA, int n, int nb, const double *dB,
     if (!converged)
         return set_status(st, PALIAL_ERR_NOT_CONVERGED, "refinement stopped at backward error %.3e after %d iterations",
                           eta, it);
-    return set_status(st, zp ? PALIAL_WARN_ZERO_PIVOT : PALIAL_OK, "backward error %.3e in %d iterations (shift %.2e)",
-                      eta, st ? st->ir_iters : it, shift);
+    return set_status(st, zp ? PALIAL_WARN_ZERO_PIVOT : PALIAL_OK,
+                      "backward error %.3e in %d iterations (shift %.2e, %d update-form residuals)", eta,
+                      st ? st->ir_iters : it, shift, resid_updates);
 }
 
 // Precision ladder (PALIAL_PREC_AUTO): the cheapest update precision first; when refinement
@@ -732,8 +789,9 @@ extern "C" int palial_gpu_solve_ir(int alg, const double *dA, int n, int nb, con
 // (mode 1, the refinement's steering residual); nrhs <= 16.
 extern "C" int palial_gpu_residual(const double *dA, int n, int nb, const double *dX, const double *dB, double *dR,
                                    int nrhs, int mode, void *stream) {
-    if (!dA || !dX || !dR || n <= 0 || nb <= 0 || n % nb || n % 64 || nrhs < 1 || nrhs > 16 || (mode != 0 && mode != 1))
+    if (!dA || !dX || !dR || n <= 0 || nb <= 0 || n % nb || n % 64 || nrhs < 1 || nrhs > 16 || mode < 0 || mode > 2)
         return PALIAL_ERR_ARG;
+    if (mode == 2 && dB) return PALIAL_ERR_ARG;  // update form: R <- R - A X in place
     palial_status st0;
     palial_status *st = &st0;
     int rc = ensure_init(st);
@@ -756,6 +814,12 @@ extern "C" int palial_gpu_residual(const double *dA, int n, int nb, const double
     std::frexp(amax, &sigma);
     PALIAL_CK(mps_colmax(dX, n, nrhs, nrm + 33, s), "norm x");
     float2 *xs = mb.xsplit.as<float2>();
+    if (mode == 2) {
+        PALIAL_CK(mps_residual_update(dA, n, nb, dX, nrm + 33, dR, nrhs, sigma, reinterpret_cast<float *>(xs),
+                                      reinterpret_cast<int *>(xs + (size_t)n * 16), s),
+                  "residual (update form)");
+        return PALIAL_OK;
+    }
     PALIAL_CK(mps_residual_df(dA, n, nb, dX, nrm + 33, dB, dR, nrhs, sigma, xs, reinterpret_cast<int *>(xs + (size_t)n * 16),
                               nullptr, s),
               "residual");

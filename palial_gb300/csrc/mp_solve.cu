@@ -163,6 +163,125 @@ __global__ void __launch_bounds__(128) residual_df_kernel(const double *A, int n
     }
 }
 
+// ---- update-form residual R <- R - A D for a small correction D ---------------------------
+// After x += d with ||d|| << ||x||, the residual of the new x is r - A d, and A d needs only
+// a modest relative accuracy: its error enters the backward error scaled by ||d|| / ||x||.
+// Plain FP32 products then suffice and the kernel is bound by reading A once from HBM
+// (8 bytes per element) instead of by the compensated residual's ~12 FP32 operations per
+// product.  Error bound: A's entries and D rounded to FP32 (2^-24 each), every lane sums 64
+// products with FMAs (64 roundings of at most 2^-24 of the running sum) before folding them
+// into a float-float accumulator (TwoSum, error ~2^-44), so per entry
+// |computed - exact| <= 67 * 2^-24 * sum_p |a_ip| |d_p| < 2^-17 * sum_p |a_ip| |d_p|
+// (the caller weighs 2^-17 ||A|| ||d|| against its tolerance before choosing this form).
+
+// float(v * 2^-sc) rounded to 24 significant bits (half-way cases away from zero), integer
+// operations only (no FP64 pipe): adding half an FP32 ulp to the pattern lets a carry out of
+// the significand step the exponent.  Results below 2^-126 after scaling flush to zero (|v|
+// < 2^sc, so their weight is below 2^-126 of the largest entry); Inf/NaN give NaN.
+__device__ __forceinline__ float f64_round_f32(unsigned long long bits, int sc) {
+    const bool special = ((bits >> 52) & 0x7FF) == 0x7FF;
+    bits += 1ull << 28;
+    const int E = (int)((bits >> 52) & 0x7FF);
+    const int e32 = E - 1023 - sc + 127;
+    unsigned f = ((unsigned)(bits >> 32) & 0x80000000u) | ((unsigned)(bits >> 29) & 0x7FFFFFu) | ((unsigned)e32 << 23);
+    f = e32 <= 0 ? (f & 0x80000000u) : f;
+    f = special ? 0x7fc00000u : f;
+    return __uint_as_float(f);
+}
+
+// Ds (n x 16 floats, rhs-minor: Ds[r * 16 + c]) = float(D(r, c) * 2^-tau_c), tau_c the exponent
+// of the column's max |d| (colmax); zero beyond nrhs.
+__global__ void d_to_f32_kernel(const double *D, long long n, int nrhs, const double *colmax, float *Ds, int *tau) {
+    const long long total = n * 16;
+    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < total; e += (long long)gridDim.x * blockDim.x) {
+        const int c = (int)(e & 15);
+        const long long r = e >> 4;
+        int t = 0;
+        if (c < nrhs) frexp(colmax[c], &t);
+        float v = 0.f;
+        if (c < nrhs) {
+            const float2 h = split_df(D[(size_t)r + (size_t)c * n], t);
+            v = __fadd_rn(h.x, h.y);
+        }
+        Ds[e] = v;
+        if (r == 0) tau[c] = t;
+    }
+}
+
+__device__ __forceinline__ void two_sum_acc(float v, float &H, float &L) {
+    const float sn = __fadd_rn(H, v), bp = __fsub_rn(sn, H);
+    L = __fadd_rn(L, __fadd_rn(__fsub_rn(H, __fsub_rn(sn, bp)), __fsub_rn(v, bp)));
+    H = sn;
+}
+
+// One CTA of 4 warps per 32-row block: lane = row, warp w takes columns p0 + w + 4 j
+// (j < 16) of every 64-column chunk, all 16 right-hand sides per lane; the chunk of D is staged
+// in shared memory (read as broadcasts).  Partial sums of warps 1..3 are combined by warp 0 in
+// a fixed order (deterministic).
+__global__ void __launch_bounds__(128) residual_update_kernel(const double *__restrict__ A, int n, int nb,
+                                                              const float *__restrict__ Ds, const int *__restrict__ tau,
+                                                              int sigma, double *__restrict__ R, int nrhs) {
+    __shared__ float4 Dsh[64][4];
+    __shared__ double part[3][16][32];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const int i0 = blockIdx.x * 32;
+    const int mt = n / nb;
+    const unsigned long long *tilerow =
+        reinterpret_cast<const unsigned long long *>(A) + (size_t)nb * nb * (size_t)(i0 / nb) + (size_t)(i0 % nb) + lane;
+    float s[16], H[16], L[16];
+#pragma unroll
+    for (int c = 0; c < 16; c++) s[c] = H[c] = L[c] = 0.f;
+    int chunks = 0;
+    for (int p0 = 0; p0 < n; p0 += 64) {
+        const unsigned long long *blk = tilerow + (size_t)nb * nb * (size_t)mt * (p0 / nb) + (size_t)(p0 % nb) * nb;
+        unsigned long long av[16];
+#pragma unroll
+        for (int j = 0; j < 16; j++) av[j] = __ldcs(blk + (size_t)(w + 4 * j) * nb);  // read once: streaming
+        __syncthreads();  // the previous chunk's D is consumed
+        for (int e = threadIdx.x; e < 256; e += 128)
+            Dsh[e >> 2][e & 3] = __ldg(reinterpret_cast<const float4 *>(Ds + (size_t)p0 * 16) + e);
+        __syncthreads();
+#pragma unroll
+        for (int j = 0; j < 16; j++) {
+            const float a = f64_round_f32(av[j], sigma);
+            const int p = w + 4 * j;
+#pragma unroll
+            for (int q = 0; q < 4; q++) {
+                const float4 d = Dsh[p][q];
+                s[4 * q + 0] = fmaf(a, d.x, s[4 * q + 0]);
+                s[4 * q + 1] = fmaf(a, d.y, s[4 * q + 1]);
+                s[4 * q + 2] = fmaf(a, d.z, s[4 * q + 2]);
+                s[4 * q + 3] = fmaf(a, d.w, s[4 * q + 3]);
+            }
+        }
+        if (++chunks == 4) {  // 64 products per lane and right-hand side
+#pragma unroll
+            for (int c = 0; c < 16; c++) {
+                two_sum_acc(s[c], H[c], L[c]);
+                s[c] = 0.f;
+            }
+            chunks = 0;
+        }
+    }
+#pragma unroll
+    for (int c = 0; c < 16; c++) two_sum_acc(s[c], H[c], L[c]);
+    if (w > 0) {
+#pragma unroll
+        for (int c = 0; c < 16; c++) part[w - 1][c][lane] = (double)H[c] + (double)L[c];
+    }
+    __syncthreads();
+    if (w == 0) {
+#pragma unroll
+        for (int c = 0; c < 16; c++) {
+            if (c < nrhs) {
+                const double v = (double)H[c] + (double)L[c] + part[0][c][lane] + part[1][c][lane] + part[2][c][lane];
+                const size_t o = (size_t)(i0 + lane) + (size_t)c * n;
+                R[o] -= ldexp(v, sigma + tau[c]);
+            }
+        }
+    }
+}
+
 __global__ void tile_f32_to_f64_kernel(const float *w, double *d, int count) {
     for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < count; e += gridDim.x * blockDim.x) d[e] = (double)w[e];
 }
@@ -542,6 +661,18 @@ cudaError_t mps_residual_df(const double *A, int n, int nb, const double *X, con
     if (e != cudaSuccess) return e;
     note_launch();
     mps::residual_df_kernel<<<n / 32, 128, 0, s>>>(A, n, nb, Xs, tau, sigma, B, R, nrhs, amax);
+    return cudaGetLastError();
+}
+// R <- R - A D (update-form residual, see residual_update_kernel); colmax = per-column max
+// |d|; Ds (n x 16 floats) and tau (16 ints) are scratch.
+cudaError_t mps_residual_update(const double *A, int n, int nb, const double *D, const double *colmax, double *R,
+                                int nrhs, int sigma, float *Ds, int *tau, cudaStream_t s) {
+    note_launch();
+    mps::d_to_f32_kernel<<<1024, 256, 0, s>>>(D, n, nrhs, colmax, Ds, tau);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    note_launch();
+    mps::residual_update_kernel<<<n / 32, 128, 0, s>>>(A, n, nb, Ds, tau, sigma, R, nrhs);
     return cudaGetLastError();
 }
 cudaError_t mps_tile_to_f64(const float *w, double *d, int nb, cudaStream_t s) {

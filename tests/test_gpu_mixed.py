@@ -211,6 +211,69 @@ def test_compensated_residual_matches_fp64(kind):
         assert err <= bound, (mode, err)
 
 
+@pytest.mark.parametrize("nrhs", [16, 5])
+def test_update_form_residual_error_bound(nrhs):
+    """R <- R - A D with FP32 products (the refinement's update form) against torch FP64:
+    entrywise |error| <= 2^-17 (|A| |D|)_i, columns of very different scale, a zero column
+    leaves R exactly unchanged."""
+    import ctypes
+    n, nb = 4096, 512
+    da = torch.empty(n * n, dtype=torch.float64, device="cuda")
+    P.gen_kappa(da.data_ptr(), n, nb, 1e4, False, seed=5)
+    g = torch.Generator("cuda").manual_seed(7)
+    d = torch.rand(nrhs, n, dtype=torch.float64, device="cuda", generator=g) - 0.5
+    d[1] *= 1e-12
+    d[2] = 0.0
+    r0 = torch.rand(nrhs, n, dtype=torch.float64, device="cuda", generator=g)
+    mt = n // nb
+    A = da.view(mt, mt, nb, nb).permute(1, 3, 0, 2).reshape(n, n)
+    ref = r0.t() - A @ d.t()
+    bound = (A.abs() @ d.t().abs()) * 2.0 ** -17 + 1e-15 * ref.abs()
+    r = r0.clone()
+    lib = P.lib()
+    lib.palial_gpu_residual.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p,
+                                        ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_void_p]
+    assert lib.palial_gpu_residual(da.data_ptr(), n, nb, d.data_ptr(), None, r.data_ptr(), nrhs, 2, None) == 0
+    torch.cuda.synchronize()
+    err = (r.t() - ref).abs()
+    assert bool((err <= bound).all()), (err / bound.clamp_min(1e-300)).max().item()
+    assert torch.equal(r[2], r0[2])
+    # the bound is not vacuous: the FP32 products do differ from FP64
+    assert err[:, 0].max().item() > 0
+
+
+def test_refinement_update_form_residual():
+    """BF16x3 at N = 8192: the second residual takes the update form (the message counts it),
+    and the solution's FP64 backward error meets the target as with full residuals only."""
+    n, nb, nrhs = 8192, 512, 16
+    a = O.gen_spd(0, n)
+    b = O.gen_uniform(5, n, nrhs, stream=O.STREAM_RHS)
+    da = torch.from_numpy(O.to_tiles(a, nb)).cuda()
+    db = torch.from_numpy(np.asfortranarray(b).ravel(order="F")).cuda()
+    at = torch.from_numpy(a).cuda()
+    bt = torch.from_numpy(b).cuda()
+    res = {}
+    for r4 in (0, 3):
+        dx = torch.zeros_like(db)
+        o = P.make_opts(precision="bf16x3")
+        o.reserved[4] = r4
+        import ctypes
+        st = P.Status()
+        rc = P.lib().palial_gpu_solve_ir(0, da.data_ptr(), n, nb, db.data_ptr(), dx.data_ptr(), nrhs, ctypes.byref(o),
+                                         ctypes.byref(st), None)
+        assert rc == 0, st.message
+        x = dx.view(nrhs, n).t()
+        r = bt - at @ x
+        eta = (r.abs().max(0).values / (at.abs().sum(1).max() * x.abs().max(0).values + bt.abs().max(0).values)).max()
+        assert eta.item() <= 1e-14 * n
+        msg = st.message.decode(errors="replace")
+        res[r4] = (st.ir_iters, msg, x.clone())
+    import re
+    count = {k: int(re.search(r"(\d+) update-form", v[1]).group(1)) for k, v in res.items()}
+    assert count[0] >= 1 and count[3] == 0, res
+    assert res[0][0] == res[3][0]
+
+
 def test_refinement_with_compensated_residual_reports_fp64_error():
     """Steering with the compensated residual and confirming in FP64 gives the same solution
     quality as FP64 residuals throughout (backward errors of both at the FP64 target)."""
