@@ -36,7 +36,7 @@ cudaError_t mp_pack_rows(int mode, const float *W, int n, int nb, int k, void *h
 cudaError_t mp_pack_cols(int mode, const float *W, int n, int nb, int k, void *hi, void *lo, float *scales,
                          cudaStream_t s);
 cudaError_t mps_f64_to_f32(const double *A, float *W, int n, int nb, double shift, cudaStream_t s,
-                           double *amax = nullptr);
+                           double *amax = nullptr, bool upper_only = false);
 cudaError_t mps_residual_df(const double *A, int n, int nb, const double *X, const double *colmax, const double *B,
                             double *R, int nrhs, int sigma, float2 *Xs, int *tau, double *amax, cudaStream_t s);
 cudaError_t mps_residual_update(const double *A, int n, int nb, const double *D, const double *colmax, double *R,
@@ -107,6 +107,20 @@ struct Lookahead {
     cudaStream_t hi = nullptr, lo = nullptr;
     cudaEvent_t start = nullptr, packed = nullptr, rest = nullptr, join = nullptr;
 } g_la;
+
+// Host-buffer solves copy the tiles a Cholesky factorization reads (upper triangle) first
+// and the rest on `copy` behind them; `full` marks the whole matrix resident.  g_full_ready
+// is that event while such a solve runs (null otherwise): every reader of the full FP64
+// matrix waits for it.
+struct SplitCopy {
+    cudaStream_t copy = nullptr;
+    cudaEvent_t upper = nullptr, full = nullptr;
+} g_sc;
+cudaEvent_t g_full_ready = nullptr;
+
+static cudaError_t wait_full_matrix(cudaStream_t s) {
+    return g_full_ready ? cudaStreamWaitEvent(s, g_full_ready, 0) : cudaSuccess;
+}
 
 static cudaError_t lookahead_init() {
     if (g_la.hi) return cudaSuccess;
@@ -501,6 +515,7 @@ static int solve_one(int alg, const double *dA, int n, int nb, const double *dB,
     const auto f0 = std::chrono::steady_clock::now();
     if (prec == PALIAL_PREC_FP64) {
         g_rctx.rbt = false;
+        PALIAL_CK(wait_full_matrix(s), "matrix copy");
         PALIAL_CK(g.mat.ensure(sizeof(double) * nn), "alloc copy");
         PALIAL_CK(cudaMemcpyAsync(g.mat.ptr, dA, sizeof(double) * nn, cudaMemcpyDeviceToDevice, s), "copy");
         palial_opts fo = o;
@@ -512,7 +527,7 @@ static int solve_one(int alg, const double *dA, int n, int nb, const double *dB,
             }
             return rc;
         }
-        PALIAL_CK(mps_f64_to_f32(g.mat.as<double>(), W, n, nb, 0.0, s), "factor to f32");
+        PALIAL_CK(mps_f64_to_f32(g.mat.as<double>(), W, n, nb, 0.0, s, nullptr, alg == 0), "factor to f32");
     } else {
         PALIAL_CK(cudaMemsetAsync(nrm + 120, 0, sizeof(double), s), "max |a|");
         // opts.reserved[6] = 1: LU of the random-butterfly transform U^T A V (rbt.cu)
@@ -523,10 +538,12 @@ static int solve_one(int alg, const double *dA, int n, int nb, const double *dB,
             if (rbt)
                 PALIAL_CK(rbt_transform_matrix(dA, W, n, nb, attempt == 0 ? nrm + 120 : nullptr, s), "butterfly transform");
             else
-                PALIAL_CK(mps_f64_to_f32(dA, W, n, nb, shift, s, attempt == 0 ? nrm + 120 : nullptr), "convert");
+                PALIAL_CK(mps_f64_to_f32(dA, W, n, nb, shift, s, attempt == 0 ? nrm + 120 : nullptr, alg == 0),
+                          "convert");
             rc = mp_factor(alg, prec, W, n, nb, s, st, &zp);
             if (rc != PALIAL_ERR_NOT_SPD || alg != 0) break;
             if (anorm < 0) {
+                PALIAL_CK(wait_full_matrix(s), "matrix copy");
                 PALIAL_CK(cudaMemsetAsync(nrm, 0, sizeof(double), s), "norm A");
                 PALIAL_CK(mps_norm_inf_matrix(dA, n, nb, nrm, s), "norm A");
                 PALIAL_CK(cudaMemcpyAsync(&anorm, nrm, sizeof(double), cudaMemcpyDeviceToHost, s), "norm");
@@ -565,6 +582,7 @@ static int solve_one(int alg, const double *dA, int n, int nb, const double *dB,
     const int maxit = o.ir_max_iter > 0 ? o.ir_max_iter : 50;
     std::vector<double> hb(nrhs), hr(nrhs), hx(nrhs), hd(nrhs), hscale(nrhs), drift(nrhs, 0.0);
     int resid_updates = 0;
+    PALIAL_CK(wait_full_matrix(s), "matrix copy");  // the residuals read all of A
     PALIAL_CK(mps_colmax(dB, n, nrhs, nrm + 49, s), "norm b");
     PALIAL_CK(cudaMemcpyAsync(hb.data(), nrm + 49, sizeof(double) * nrhs, cudaMemcpyDeviceToHost, s), "norm b");
     PALIAL_CK(cudaMemsetAsync(dX, 0, sizeof(double) * (size_t)n * nrhs, s), "x0");
@@ -840,9 +858,38 @@ extern "C" int palial_gpu_solve_ir_host(int alg, const palial_desc *A, const dou
     PALIAL_CK(g.smat.ensure(bytes), "alloc A");
     PALIAL_CK(mb.work.ensure(std::max(mb.work.bytes, 2 * vb)), "alloc B/X");
     double *dB = mb.work.as<double>(), *dX = dB + (size_t)n * nrhs;
-    PALIAL_CK(cudaMemcpy(g.smat.ptr, A->matrix, bytes, cudaMemcpyHostToDevice), "copy A");
-    PALIAL_CK(cudaMemcpy(dB, B, vb, cudaMemcpyHostToDevice), "copy B");
-    rc = palial_gpu_solve_ir(alg, g.smat.as<double>(), n, nb, dB, dX, nrhs, opts, st, nullptr);
+    PALIAL_CK(cudaMemcpyAsync(dB, B, vb, cudaMemcpyHostToDevice, nullptr), "copy B");
+    const int mt = nb > 0 ? n / nb : 0;
+    const size_t te = (size_t)nb * nb;
+    double *dA = g.smat.as<double>();
+    const double *hA = static_cast<const double *>(A->matrix);
+    if (alg == 0 && mt > 1 && n % nb == 0) {
+        // Cholesky reads only the upper triangle: tile column j's tiles 0..j are contiguous and
+        // go first; the factorization starts when they are in while the lower triangle follows
+        // on the copy stream (the host link is the bottleneck, so the two phases never share it)
+        if (!g_sc.copy) {
+            PALIAL_CK(cudaStreamCreateWithFlags(&g_sc.copy, cudaStreamNonBlocking), "copy stream");
+            PALIAL_CK(cudaEventCreateWithFlags(&g_sc.upper, cudaEventDisableTiming), "copy event");
+            PALIAL_CK(cudaEventCreateWithFlags(&g_sc.full, cudaEventDisableTiming), "copy event");
+        }
+        for (int j = 0; j < mt; j++)
+            PALIAL_CK(cudaMemcpyAsync(dA + te * mt * j, hA + te * mt * j, sizeof(double) * te * (j + 1),
+                                      cudaMemcpyHostToDevice, nullptr),
+                      "copy A (upper)");
+        PALIAL_CK(cudaEventRecord(g_sc.upper, nullptr), "copy A");
+        PALIAL_CK(cudaStreamWaitEvent(g_sc.copy, g_sc.upper, 0), "copy A");
+        for (int j = 0; j + 1 < mt; j++)
+            PALIAL_CK(cudaMemcpyAsync(dA + te * (mt * j + j + 1), hA + te * (mt * j + j + 1),
+                                      sizeof(double) * te * (mt - 1 - j), cudaMemcpyHostToDevice, g_sc.copy),
+                      "copy A (lower)");
+        PALIAL_CK(cudaEventRecord(g_sc.full, g_sc.copy), "copy A");
+        g_full_ready = g_sc.full;
+    } else {
+        PALIAL_CK(cudaMemcpyAsync(dA, hA, bytes, cudaMemcpyHostToDevice, nullptr), "copy A");
+    }
+    rc = palial_gpu_solve_ir(alg, dA, n, nb, dB, dX, nrhs, opts, st, nullptr);
+    g_full_ready = nullptr;
+    if (g_sc.full) PALIAL_CK(cudaStreamWaitEvent(nullptr, g_sc.full, 0), "copy A");  // error paths too
     PALIAL_CK(cudaMemcpy(X, dX, vb, cudaMemcpyDeviceToHost), "copy X");
     if (st) st->total_seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
     return rc;

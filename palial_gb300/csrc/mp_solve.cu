@@ -22,23 +22,38 @@ __device__ __forceinline__ size_t tile_off(int n, int nb, int tm, int tn) {
 
 // ---- conversions --------------------------------------------------------------------------
 // W = float(A (+ shift on the diagonal)); amax (optional, zeroed by the caller) receives
-// max |a_ij| of the unshifted A (atomicMax on the bit pattern, NaN propagating).
-__global__ void f64_to_f32_kernel(const double *a, float *w, long long len, double shift_diag, int n, int nb,
-                                  double *amax) {
+// max |a_ij| of the unshifted A (atomicMax on the bit pattern, NaN propagating).  Work items
+// are 8192-element chunks of tiles; upper_only skips the tiles below the diagonal (Cholesky
+// reads only the upper triangle, which a caller may have copied in first).
+constexpr int kConvChunk = 8192;
+__global__ void f64_to_f32_kernel(const double *__restrict__ a, float *__restrict__ w, int n, int nb,
+                                  double shift_diag, int upper_only, double *amax) {
     const int mt = n / nb;
+    const int te = nb * nb;
+    const int chunks = (te + kConvChunk - 1) / kConvChunk;
+    const long long items = (long long)mt * mt * chunks;
     // max |a| on the bit patterns (integer compares; for non-negative doubles the unsigned
     // order is the value order, and a NaN's pattern exceeds every finite one)
     unsigned long long mx = 0;
-    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < len; e += (long long)gridDim.x * blockDim.x) {
-        double v = a[e];
-        const unsigned long long ab = (unsigned long long)__double_as_longlong(v) & 0x7FFFFFFFFFFFFFFFull;
-        mx = ab > mx ? ab : mx;
-        if (shift_diag != 0.0) {
-            const long long t = e / ((long long)nb * nb);
-            const int in = (int)(e - t * (long long)nb * nb);
-            if ((t % mt) == (t / mt) && (in % nb) == (in / nb)) v += shift_diag;
+    for (long long it = blockIdx.x; it < items; it += gridDim.x) {
+        const int t = (int)(it / chunks), ch = (int)(it - (long long)t * chunks);
+        const int tr = t % mt, tc = t / mt;
+        if (upper_only && tr > tc) continue;  // uniform per CTA
+        const size_t base = (size_t)t * te;
+        const int end = min(te, (ch + 1) * kConvChunk);
+        const bool diag = shift_diag != 0.0 && tr == tc;
+        for (int i = ch * kConvChunk + 2 * threadIdx.x; i < end; i += 2 * blockDim.x) {
+            double2 v = *reinterpret_cast<const double2 *>(a + base + i);  // te even: 16-byte aligned
+            const unsigned long long b0 = (unsigned long long)__double_as_longlong(v.x) & 0x7FFFFFFFFFFFFFFFull;
+            const unsigned long long b1 = (unsigned long long)__double_as_longlong(v.y) & 0x7FFFFFFFFFFFFFFFull;
+            mx = b0 > mx ? b0 : mx;
+            mx = b1 > mx ? b1 : mx;
+            if (diag) {
+                if (i % (nb + 1) == 0) v.x += shift_diag;
+                if ((i + 1) % (nb + 1) == 0) v.y += shift_diag;
+            }
+            *reinterpret_cast<float2 *>(w + base + i) = make_float2((float)v.x, (float)v.y);
         }
-        w[e] = (float)v;
     }
     if (amax) {
         for (int o = 16; o; o >>= 1) {
@@ -646,9 +661,12 @@ cudaError_t mps_configure() {
     return e;
 }
 
-cudaError_t mps_f64_to_f32(const double *A, float *W, int n, int nb, double shift, cudaStream_t s, double *amax) {
+cudaError_t mps_f64_to_f32(const double *A, float *W, int n, int nb, double shift, cudaStream_t s, double *amax,
+                           bool upper_only) {
+    const long long items = (long long)(n / nb) * (n / nb) * ((nb * nb + mps::kConvChunk - 1) / mps::kConvChunk);
     note_launch();
-    mps::f64_to_f32_kernel<<<4096, 256, 0, s>>>(A, W, (long long)n * n, shift, n, nb, amax);
+    mps::f64_to_f32_kernel<<<(int)std::min<long long>(items, 2048), 256, 0, s>>>(
+        A, W, n, nb, shift, upper_only ? 1 : 0, amax);
     return cudaGetLastError();
 }
 // R = B - A X in compensated FP32 (see residual_df_kernel); sigma: |a_ij| < 2^sigma for all
