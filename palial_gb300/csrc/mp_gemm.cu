@@ -41,9 +41,11 @@ enum Mode { MODE_BF16 = 0, MODE_FP8 = 1, MODE_BF16X3 = 2 };
 template <int MODE>
 struct Cfg {
     static constexpr int NOPS = (MODE == MODE_BF16X3) ? 2 : 1;   // hi (+ lo) operand copies
-    // 2 stages: K = NB = 512 is only 8 (bf16) or 4 (fp8) stages, and 2 CTAs then share an SM
-    // (2 x 256 TMEM columns), so one CTA's epilogue overlaps the other's main loop.
-    static constexpr int STAGES = 2;
+    // K = NB = 512 is only 8 (bf16) or 4 (fp8) stages.  2 CTAs share an SM (2 x 256 TMEM
+    // columns, 2 x 128 threads x 256 registers), so one CTA's epilogue overlaps the other's
+    // loads and MMAs: bf16 and fp8 keep a 2-stage ring (96 KB); BF16x3's stage holds four
+    // operand boxes (96 KB), so it runs one stage per CTA to fit two CTAs in shared memory.
+    static constexpr int STAGES = (MODE == MODE_BF16X3) ? 1 : 2;
     static constexpr int A_BYTES = BM * KBYTES;                  // 16 KB
     static constexpr int B_BYTES = BN * KBYTES;                  // 32 KB
     static constexpr int STAGE_BYTES = NOPS * (A_BYTES + B_BYTES);
