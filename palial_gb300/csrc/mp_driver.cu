@@ -43,7 +43,8 @@ cudaError_t mps_residual_update(const double *A, int n, int nb, const double *D,
                                 int nrhs, int sigma, float *Ds, int *tau, cudaStream_t s);
 cudaError_t mps_tile_to_f64(const float *w, double *d, int nb, cudaStream_t s);
 cudaError_t mps_tile_to_f32(const double *d, float *w, int nb, int upper_only, cudaStream_t s);
-cudaError_t mps_panel_trsm(float *W, int n, int nb, int k, int kind, cudaStream_t s);
+cudaError_t mps_panel_trsm(float *W, int n, int nb, int k, int kind, const float *binv, cudaStream_t s);
+cudaError_t mps_block_inverse(const float *W, int n, int nb, int k, int factors, float *binv, cudaStream_t s);
 cudaError_t mps_residual(const double *A, int n, int nb, const double *X, const double *B, double *R, int nrhs,
                          double *amax, cudaStream_t s);
 cudaError_t mps_norm_inf_matrix(const double *A, int n, int nb, double *out, cudaStream_t s);
@@ -73,6 +74,7 @@ cudaError_t mps_matvec(const double *A, int n, int nb, const double *x, double *
 cudaError_t mps_symmetrize(double *X, int n, int nb, cudaStream_t s);
 cudaError_t launch_gen_dense(double *X, long long rows, int cols, uint64_t seed, int stream, cudaStream_t s);
 cudaError_t launch_sumsq(const double *X, long long len, double *partial, int blocks, cudaStream_t s);
+void mp_release();
 }  // namespace palial
 
 using namespace palial;
@@ -83,6 +85,7 @@ struct MpBufs {
     DevBuf w, diag, pa_hi, pa_lo, pb_hi, pb_lo, scales, r, r32, x32, norms, work, krylov, hbuf, gvec;
     DevBuf y32;     // output of the forward triangular solve (n x 16)
     DevBuf xsplit;  // compensated residual: X as FP32 pairs (n x 16 float2) + 16 scale exponents
+    DevBuf binv;    // inverses of the current diagonal tile's 64 x 64 diagonal blocks (panel solves)
     DevBuf dinv_u, dinv_l, stile;  // FP32 inverses of the diagonal factor tiles, solve scratch
 };
 MpBufs mb;
@@ -145,6 +148,7 @@ int mp_factor(int alg, int prec, float *W, int n, int nb, cudaStream_t s, palial
         PALIAL_CK(mb.pb_lo.ensure(2 * panel), "alloc panel");
     }
     PALIAL_CK(mb.scales.ensure(sizeof(float) * 4 * (size_t)std::max(1, mt)), "alloc scales");
+    PALIAL_CK(mb.binv.ensure(sizeof(float) * 2 * (size_t)nb * 64), "alloc block inverses");
     PALIAL_CK(g.diag.status.ensure(sizeof(int) * ST_NSLOTS + 64), "alloc status");
     PALIAL_CK(lookahead_init(), "lookahead streams");
     PALIAL_CK(cudaMemsetAsync(g.diag.status.ptr, 0, sizeof(int) * ST_NSLOTS, s), "clear status");
@@ -163,15 +167,17 @@ int mp_factor(int alg, int prec, float *W, int n, int nb, cudaStream_t s, palial
         float *sa = mb.scales.as<float>() + 2 * mt * par, *sb = sa + mt;
         void *ah = buf(mb.pa_hi, par), *al = mode == 2 ? buf(mb.pa_lo, par) : nullptr;
         void *bh = buf(mb.pb_hi, par), *bl = mode == 2 ? buf(mb.pb_lo, par) : nullptr;
+        float *binv = mb.binv.as<float>();
+        PALIAL_CK(mps_block_inverse(W, n, nb, k, alg == 0 ? 1 : 2, binv, hi), "diagonal block inverses");
         if (alg == 0) {
-            PALIAL_CK(mps_panel_trsm(W, n, nb, k, 0, hi), "panel trsm");
+            PALIAL_CK(mps_panel_trsm(W, n, nb, k, 0, binv, hi), "panel trsm");
             PALIAL_CK(mp_pack_rows(mode, W, n, nb, k, ah, al, sa, hi), "pack");
             bh = ah;
             bl = al;
             sb = sa;
         } else {
-            PALIAL_CK(mps_panel_trsm(W, n, nb, k, 1, hi), "row panel trsm");
-            PALIAL_CK(mps_panel_trsm(W, n, nb, k, 2, hi), "column panel trsm");
+            PALIAL_CK(mps_panel_trsm(W, n, nb, k, 1, binv, hi), "row panel trsm");
+            PALIAL_CK(mps_panel_trsm(W, n, nb, k, 2, binv, hi), "column panel trsm");
             PALIAL_CK(mp_pack_cols(mode, W, n, nb, k, ah, al, sa, hi), "pack L");
             PALIAL_CK(mp_pack_rows(mode, W, n, nb, k, bh, bl, sb, hi), "pack U");
         }
@@ -386,6 +392,14 @@ int gmres(int alg, const double *A, const float *W, int n, int nb, const double 
 }
 
 }  // namespace
+
+// Frees the mixed-precision path's device buffers (palial_gpu_finalize).
+void palial::mp_release() {
+    for (DevBuf *b : {&mb.w, &mb.diag, &mb.pa_hi, &mb.pa_lo, &mb.pb_hi, &mb.pb_lo, &mb.scales, &mb.r, &mb.r32,
+                      &mb.x32, &mb.norms, &mb.work, &mb.krylov, &mb.hbuf, &mb.gvec, &mb.y32, &mb.xsplit, &mb.binv,
+                      &mb.dinv_u, &mb.dinv_l, &mb.stile})
+        b->release();
+}
 
 extern "C" int palial_gpu_gen_kappa(double *dA, int n, int nb, double kappa, int symmetric, uint64_t seed,
                                     void *stream) {

@@ -324,12 +324,108 @@ __device__ __forceinline__ Smem smem_parts(float *s) {
     return m;
 }
 
-// X = U^-T B, B = nb x 64 strip (ld), U upper nb x nb (ld_u)
-__device__ __forceinline__ void strip_lut(const Smem &m, const float *U, int ldu, float *B, int ldb, int nb) {
+// ---- inverses of the 64 x 64 diagonal blocks of a factored diagonal tile -------------------
+// binv[(which * (nb/64) + b) * 4096 ..]: the column-major 64 x 64 inverse of diagonal block b of
+// tile (k, k): which 0 = of the upper factor U_bb (Cholesky and LU), 1 = of the unit lower
+// factor L_bb (LU).  One CTA of 64 threads per block and factor; thread c computes column c,
+// its 64 unknowns in registers, eliminating right-looking (the FMAs of one step are
+// independent; the coefficients are shared-memory broadcasts).  The panel solves then apply
+// each diagonal block as a 64 x 64 product instead of a 64-step substitution.
+__global__ void __launch_bounds__(64) block_inverse_kernel(const float *W, int n, int nb, int k, float *binv) {
+    __shared__ __align__(16) float Ts[64][64];  // Ts[c][r] = block(r, c)
+    const int b = blockIdx.x, which = blockIdx.y;
+    const float *T = W + tile_off(n, nb, k, k) + (size_t)b * 64 * ((size_t)nb + 1);
+    for (int e = threadIdx.x; e < 4096; e += 64) Ts[e >> 6][e & 63] = T[(e & 63) + (size_t)(e >> 6) * nb];
+    __syncthreads();
+    const int c = threadIdx.x;
+    float x[64];
+#pragma unroll
+    for (int i = 0; i < 64; i++) x[i] = (i == c) ? 1.f : 0.f;
+    if (which == 0) {
+        // U x = e_c, backward: x_p /= u_pp, then x_i -= u_ip x_p for i < p
+#pragma unroll
+        for (int p = 63; p >= 0; p--) {
+            x[p] = x[p] / Ts[p][p];
+#pragma unroll
+            for (int i0 = 0; i0 < p; i0 += 4) {
+                const float4 u = *reinterpret_cast<const float4 *>(&Ts[p][i0]);
+                const float uv[4] = {u.x, u.y, u.z, u.w};
+#pragma unroll
+                for (int j = 0; j < 4; j++)
+                    if (i0 + j < p) x[i0 + j] = fmaf(-uv[j], x[p], x[i0 + j]);
+            }
+        }
+    } else {
+        // L x = e_c (unit lower), forward: x_i -= l_ip x_p for i > p
+#pragma unroll
+        for (int p = 0; p < 63; p++) {
+#pragma unroll
+            for (int i0 = (p + 1) & ~3; i0 < 64; i0 += 4) {
+                const float4 l = *reinterpret_cast<const float4 *>(&Ts[p][i0]);
+                const float lv[4] = {l.x, l.y, l.z, l.w};
+#pragma unroll
+                for (int j = 0; j < 4; j++)
+                    if (i0 + j > p) x[i0 + j] = fmaf(-lv[j], x[p], x[i0 + j]);
+            }
+        }
+    }
+    float *out = binv + ((size_t)which * (nb / 64) + b) * 4096 + (size_t)c * 64;
+#pragma unroll
+    for (int i = 0; i < 64; i += 4) *reinterpret_cast<float4 *>(out + i) = make_float4(x[i], x[i + 1], x[i + 2], x[i + 3]);
+}
+
+// The 64 x 64 block B (at B, ld) in place: OP 0: X^T B; 1: X B; 2: B X, with X a column-major
+// 64 x 64 inverse block.  Staged through shared memory (m.Ds[c][r] = X(r, c), m.Bs[c][r] =
+// B(r, c)); thread: rows 4 tr .. 4 tr + 3, columns 4 tc .. 4 tc + 3.  Ends synced.
+template <int OP>
+__device__ __forceinline__ void apply_inv64(const Smem &m, const float *X, float *B, int ldb) {
+    for (int e = threadIdx.x; e < 4096; e += NT) {
+        m.Ds[e >> 6][e & 63] = ldg(X + e);
+        m.Bs[e >> 6][e & 63] = B[(e & 63) + (size_t)(e >> 6) * ldb];
+    }
+    __syncthreads();
+    const int tr = threadIdx.x & 15, tc = threadIdx.x >> 4;
+    float acc[4][4] = {};
+#pragma unroll 8
+    for (int p = 0; p < 64; p++) {
+        float a[4], bv[4];
+#pragma unroll
+        for (int x = 0; x < 4; x++) {
+            const int r = 4 * tr + x;
+            a[x] = OP == 0 ? m.Ds[r][p] : OP == 1 ? m.Ds[p][r] : m.Bs[p][r];
+        }
+#pragma unroll
+        for (int y = 0; y < 4; y++) {
+            const int c = 4 * tc + y;
+            bv[y] = OP == 2 ? m.Ds[c][p] : m.Bs[c][p];
+        }
+#pragma unroll
+        for (int x = 0; x < 4; x++)
+#pragma unroll
+            for (int y = 0; y < 4; y++) acc[x][y] = fmaf(a[x], bv[y], acc[x][y]);
+    }
+#pragma unroll
+    for (int y = 0; y < 4; y++)
+        *reinterpret_cast<float4 *>(B + (size_t)(4 * tr) + (size_t)(4 * tc + y) * ldb) =
+            make_float4(acc[0][y], acc[1][y], acc[2][y], acc[3][y]);
+    __syncthreads();
+}
+
+// X = U^-T B, B = nb x 64 strip (ld), U upper nb x nb (ld_u); uinv: inverses of U's 64 x 64
+// diagonal blocks
+__device__ __forceinline__ void strip_lut(const Smem &m, const float *U, int ldu, float *B, int ldb, int nb,
+                                          const float *uinv) {
     for (int rb = 0; rb < nb; rb += 64) {
         if (rb > 0) cta_gemm<true, false>(64, 64, rb, -1.f, U + (size_t)rb * ldu, ldu, B, ldb, B + rb, ldb, m.g);
-        load_diag64(m.Ds, U + rb + (size_t)rb * ldu, ldu);
-        solve64<0>(m.Ds, B + rb, ldb);
+        apply_inv64<0>(m, uinv + (size_t)(rb / 64) * 4096, B + rb, ldb);
+    }
+}
+// X = L^-1 B (unit lower) with L's diagonal-block inverses linv
+__device__ __forceinline__ void strip_llu_inv(const Smem &m, const float *L, int ldl, float *B, int ldb, int nb,
+                                              const float *linv) {
+    for (int rb = 0; rb < nb; rb += 64) {
+        if (rb > 0) cta_gemm<false, false>(64, 64, rb, -1.f, L + rb, ldl, B, ldb, B + rb, ldb, m.g);
+        apply_inv64<1>(m, linv + (size_t)(rb / 64) * 4096, B + rb, ldb);
     }
 }
 // X = U^-1 B (backward), B = nb x 64 strip
@@ -350,26 +446,29 @@ __device__ __forceinline__ void strip_llu(const Smem &m, const float *L, int ldl
         solve64<2>(m.Ds, B + rb, ldb);
     }
 }
-// X = B U^-1, B = 64 x nb row strip
-__device__ __forceinline__ void strip_run(const Smem &m, const float *U, int ldu, float *B, int ldb, int nb) {
+// X = B U^-1, B = 64 x nb row strip, with U's diagonal-block inverses uinv
+__device__ __forceinline__ void strip_run(const Smem &m, const float *U, int ldu, float *B, int ldb, int nb,
+                                          const float *uinv) {
     for (int cb = 0; cb < nb; cb += 64) {
         if (cb > 0)
             cta_gemm<false, false>(64, 64, cb, -1.f, B, ldb, U + (size_t)cb * ldu, ldu, B + (size_t)cb * ldb, ldb, m.g);
-        load_diag64(m.Ds, U + cb + (size_t)cb * ldu, ldu);
-        solve64<1>(m.Ds, B + (size_t)cb * ldb, ldb);
+        apply_inv64<2>(m, uinv + (size_t)(cb / 64) * 4096, B + (size_t)cb * ldb, ldb);
     }
 }
 
 // kind 0: Cholesky row panel U(k,m) <- U_kk^-T U(k,m);  1: LU row panel U(k,n) <- L_kk^-1 .;
-// 2: LU column panel L(m,k) <- L(m,k) U_kk^-1.  grid (nb/64, trailing tiles).
-__global__ void __launch_bounds__(NT, 2) panel_trsm_kernel(float *W, int n, int nb, int k, int kind) {
+// 2: LU column panel L(m,k) <- L(m,k) U_kk^-1.  grid (nb/64, trailing tiles).  binv: the
+// diagonal-block inverses of tile k (block_inverse_kernel).
+__global__ void __launch_bounds__(NT, 2) panel_trsm_kernel(float *W, int n, int nb, int k, int kind,
+                                                          const float *binv) {
     extern __shared__ __align__(16) float smem[];
     const Smem m = smem_parts(smem);
     const int t = k + 1 + blockIdx.y, s = blockIdx.x;
     const float *T = W + tile_off(n, nb, k, k);
-    if (kind == 0) strip_lut(m, T, nb, W + tile_off(n, nb, k, t) + (size_t)s * 64 * nb, nb, nb);
-    else if (kind == 1) strip_llu(m, T, nb, W + tile_off(n, nb, k, t) + (size_t)s * 64 * nb, nb, nb);
-    else strip_run(m, T, nb, W + tile_off(n, nb, t, k) + s * 64, nb, nb);
+    if (kind == 0) strip_lut(m, T, nb, W + tile_off(n, nb, k, t) + (size_t)s * 64 * nb, nb, nb, binv);
+    else if (kind == 1)
+        strip_llu_inv(m, T, nb, W + tile_off(n, nb, k, t) + (size_t)s * 64 * nb, nb, nb, binv + (size_t)(nb / 64) * 4096);
+    else strip_run(m, T, nb, W + tile_off(n, nb, t, k) + s * 64, nb, nb, binv);
 }
 
 // ---- diagonal-tile inverses for the refinement solves --------------------------------------
@@ -721,12 +820,19 @@ cudaError_t mps_rhs_step(const float *W, const float *Dinv, int n, int nb, int k
     mps::rhs_update2_kernel<<<grid, mps::NT, mps::SMEM_BYTES, s>>>(W, n, nb, k, R, S, kind, cnt);
     return cudaGetLastError();
 }
-cudaError_t mps_panel_trsm(float *W, int n, int nb, int k, int kind, cudaStream_t s) {
+// binv (2 nb x 64 floats): inverses of the 64 x 64 diagonal blocks of tile k's upper factor,
+// and for LU (factors = 2) of its unit lower factor
+cudaError_t mps_block_inverse(const float *W, int n, int nb, int k, int factors, float *binv, cudaStream_t s) {
+    note_launch();
+    mps::block_inverse_kernel<<<dim3(nb / 64, factors), 64, 0, s>>>(W, n, nb, k, binv);
+    return cudaGetLastError();
+}
+cudaError_t mps_panel_trsm(float *W, int n, int nb, int k, int kind, const float *binv, cudaStream_t s) {
     const int ntr = n / nb - k - 1;
     if (ntr <= 0) return cudaSuccess;
     dim3 grid(nb / 64, ntr);
     note_launch();
-    mps::panel_trsm_kernel<<<grid, mps::NT, mps::SMEM_BYTES, s>>>(W, n, nb, k, kind);
+    mps::panel_trsm_kernel<<<grid, mps::NT, mps::SMEM_BYTES, s>>>(W, n, nb, k, kind, binv);
     return cudaGetLastError();
 }
 cudaError_t mps_residual(const double *A, int n, int nb, const double *X, const double *B, double *R, int nrhs,

@@ -47,6 +47,7 @@ cudaError_t mps_configure();
 cudaError_t mpd_configure();
 cudaError_t mpr_configure();
 void mpr_release();
+void mp_release();
 
 State g;
 static long long g_launches = 0;
@@ -223,6 +224,7 @@ int palial_gpu_finalize(void) {
     for (DevBuf *b : {&g.mat, &g.smat, &g.kbuf, &g.probe}) b->release();
     qr_solve_release();
     mpr_release();
+    mp_release();
     layout_release();
     rbt_release();
     g.dags.clear();
