@@ -358,7 +358,7 @@ __device__ __forceinline__ void trailing(float *C, int ld, int m, int kc, float 
 
 // status: int[8] of the factorization (ST_CODE, ..., [6] = step)
 template <int ALG>
-__global__ void __launch_bounds__(NT, 1) diag_factor_kernel(float *T, int nb, int k, int *status) {
+__global__ void __launch_bounds__(NT, 1) diag_factor_kernel(float *T, int nb, int ld, int k, int col0, int *status) {
     extern __shared__ __align__(16) float smem[];
     float (*Ds)[DP] = reinterpret_cast<float (*)[DP]>(smem);
     const int kc = chunk_k(nb);
@@ -369,14 +369,14 @@ __global__ void __launch_bounds__(NT, 1) diag_factor_kernel(float *T, int nb, in
     if (threadIdx.x == 0) status[6] = k;  // current step (error reports of later kernels)
     int zero = 0;
     for (int j0 = 0; j0 < nb; j0 += 64) {
-        float *D = T + j0 + (size_t)j0 * nb;
-        for (int e = threadIdx.x; e < 4096; e += NT) Ds[e >> 6][e & 63] = D[(e & 63) + (size_t)(e >> 6) * nb];
+        float *D = T + j0 + (size_t)j0 * ld;
+        for (int e = threadIdx.x; e < 4096; e += NT) Ds[e >> 6][e & 63] = D[(e & 63) + (size_t)(e >> 6) * ld];
         __syncthreads();
         if (ALG == 0) {
             const int bad = chol64(Ds, sflag);
             if (bad >= 0) {
                 if (threadIdx.x == 0 && atomicCAS(status + ST_CODE, 0, -3 /*PALIAL_ERR_NOT_SPD*/) == 0) {
-                    status[ST_COL] = j0 + bad;
+                    status[ST_COL] = col0 + j0 + bad;
                     status[ST_M] = status[ST_N] = k;
                     status[6] = k;
                     __threadfence();
@@ -388,13 +388,13 @@ __global__ void __launch_bounds__(NT, 1) diag_factor_kernel(float *T, int nb, in
         }
         for (int e = threadIdx.x; e < 4096; e += NT) {
             const int r = e & 63, c = e >> 6;
-            if (ALG == 1 || r <= c) D[r + (size_t)c * nb] = Ds[c][r];
+            if (ALG == 1 || r <= c) D[r + (size_t)c * ld] = Ds[c][r];
         }
         const int m = nb - j0 - 64;
         if (m == 0) break;
         __syncthreads();
         // panels
-        float *A12 = T + j0 + (size_t)(j0 + 64) * nb;  // 64 x m, columns at stride nb
+        float *A12 = T + j0 + (size_t)(j0 + 64) * ld;  // 64 x m, columns at stride ld
         // column panel: staged through shared memory (coalesced loads and stores; a thread
         // solves one column, Ps[c][i] with an odd pitch so the threads' columns do not share banks)
         {
@@ -403,7 +403,7 @@ __global__ void __launch_bounds__(NT, 1) diag_factor_kernel(float *T, int nb, in
             for (int c0 = 0; c0 < m; c0 += cwmax) {
                 const int cw = min(cwmax, m - c0);
                 for (int e = threadIdx.x; e < cw * 64; e += NT)
-                    Ps[(e >> 6) * PP + (e & 63)] = A12[(e & 63) + (size_t)(c0 + (e >> 6)) * nb];
+                    Ps[(e >> 6) * PP + (e & 63)] = A12[(e & 63) + (size_t)(c0 + (e >> 6)) * ld];
                 __syncthreads();
                 for (int c = threadIdx.x; c < cw; c += NT) {
                     if (ALG == 0) solve_vec<0>(Ds, Ps + c * PP, 1);
@@ -411,16 +411,16 @@ __global__ void __launch_bounds__(NT, 1) diag_factor_kernel(float *T, int nb, in
                 }
                 __syncthreads();
                 for (int e = threadIdx.x; e < cw * 64; e += NT)
-                    A12[(e & 63) + (size_t)(c0 + (e >> 6)) * nb] = Ps[(e >> 6) * PP + (e & 63)];
+                    A12[(e & 63) + (size_t)(c0 + (e >> 6)) * ld] = Ps[(e >> 6) * PP + (e & 63)];
                 __syncthreads();
             }
         }
         if (ALG == 1) {
-            float *A21 = T + (j0 + 64) + (size_t)j0 * nb;  // m x 64, rows contiguous
-            for (int r = threadIdx.x; r < m; r += NT) solve_vec<2>(Ds, A21 + r, nb);
+            float *A21 = T + (j0 + 64) + (size_t)j0 * ld;  // m x 64, rows contiguous
+            for (int r = threadIdx.x; r < m; r += NT) solve_vec<2>(Ds, A21 + r, ld);
         }
         __syncthreads();
-        float *C = T + (j0 + 64) + (size_t)(j0 + 64) * nb;
+        float *C = T + (j0 + 64) + (size_t)(j0 + 64) * ld;
         if (ALG == 0) {
             // As[kk][i] = U12(k0 + kk, i), contiguous in kk in global memory: each thread loads
             // 4 consecutive kk of one column (float4) and a warp covers 32 consecutive columns,
@@ -428,31 +428,31 @@ __global__ void __launch_bounds__(NT, 1) diag_factor_kernel(float *T, int nb, in
             auto stage = [&](int k0) {
                 for (int e = threadIdx.x; e < (kc / 4) * m; e += NT) {
                     const int i = e % m, kq = 4 * (e / m);
-                    const float4 v = *reinterpret_cast<const float4 *>(A12 + (k0 + kq) + (size_t)i * nb);
+                    const float4 v = *reinterpret_cast<const float4 *>(A12 + (k0 + kq) + (size_t)i * ld);
                     As[(size_t)(kq + 0) * m + i] = v.x;
                     As[(size_t)(kq + 1) * m + i] = v.y;
                     As[(size_t)(kq + 2) * m + i] = v.z;
                     As[(size_t)(kq + 3) * m + i] = v.w;
                 }
             };
-            trailing<true>(C, nb, m, kc, As, As, stage);
+            trailing<true>(C, ld, m, kc, As, As, stage);
         } else {
-            const float *A21 = T + (j0 + 64) + (size_t)j0 * nb;
+            const float *A21 = T + (j0 + 64) + (size_t)j0 * ld;
             auto stage = [&](int k0) {
                 for (int e = threadIdx.x; e < kc * m; e += NT) {
                     const int i = e % m, kk = e / m;  // L21(i, k0+kk): contiguous in i
-                    As[(size_t)kk * m + i] = A21[i + (size_t)(k0 + kk) * nb];
+                    As[(size_t)kk * m + i] = A21[i + (size_t)(k0 + kk) * ld];
                 }
                 for (int e = threadIdx.x; e < (kc / 4) * m; e += NT) {
                     const int j = e % m, kq = 4 * (e / m);  // U12(k0+kq.., j): float4 along kk
-                    const float4 v = *reinterpret_cast<const float4 *>(A12 + (k0 + kq) + (size_t)j * nb);
+                    const float4 v = *reinterpret_cast<const float4 *>(A12 + (k0 + kq) + (size_t)j * ld);
                     Bs[(size_t)(kq + 0) * m + j] = v.x;
                     Bs[(size_t)(kq + 1) * m + j] = v.y;
                     Bs[(size_t)(kq + 2) * m + j] = v.z;
                     Bs[(size_t)(kq + 3) * m + j] = v.w;
                 }
             };
-            trailing<false>(C, nb, m, kc, As, Bs, stage);
+            trailing<false>(C, ld, m, kc, As, Bs, stage);
         }
         __syncthreads();
     }
@@ -468,15 +468,38 @@ cudaError_t mpd_configure() {
     return cudaFuncSetAttribute(mpd::diag_factor_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
 }
 
-// Factor diagonal tile k of the FP32 tile matrix W (n x n, tile nb) in place.
-cudaError_t mpd_factor_tile(int alg, float *W, int n, int nb, int k, int *status, cudaStream_t s) {
+cudaError_t mps_block_inverse(const float *W, int n, int nb, int k, int factors, float *binv, cudaStream_t s,
+                              int blocks);
+cudaError_t mps_half_panel(float *T, int h, int ld, const float *binv, cudaStream_t s);
+cudaError_t mps_half_update(float *T, int h, int ld, cudaStream_t s);
+
+// Factor diagonal tile k of the FP32 tile matrix W (n x n, tile nb) in place.  Cholesky tiles of
+// NB >= 512 go two-level: A11 (h = NB/2) in one CTA, A12 <- U11^-T A12 and the upper part of
+// A22 -= A12^T A12 on many CTAs, then A22 in one CTA (the one-CTA kernel's time grows about
+// 3.5x per doubling of the size, the multi-CTA steps are short).  binv: scratch for the
+// inverses of U11's 64 x 64 diagonal blocks (nb x 64 floats).
+cudaError_t mpd_factor_tile(int alg, float *W, int n, int nb, int k, int *status, float *binv, cudaStream_t s) {
     if (nb % 64 || nb > 1024) return cudaErrorInvalidValue;
     const int mt = n / nb;
     float *T = W + (size_t)nb * nb * ((size_t)k + (size_t)mt * k);
+    if (alg == 0 && nb >= 512 && nb % 128 == 0 && binv) {
+        const int h = nb / 2;
+        const int bytes = mpd::smem_floats(h) * 4;
+        note_launch();
+        mpd::diag_factor_kernel<0><<<1, mpd::NT, bytes, s>>>(T, h, nb, k, 0, status);
+        cudaError_t e = cudaGetLastError();
+        if (e == cudaSuccess) e = mps_block_inverse(W, n, nb, k, 1, binv, s, h / 64);
+        if (e == cudaSuccess) e = mps_half_panel(T, h, nb, binv, s);
+        if (e == cudaSuccess) e = mps_half_update(T, h, nb, s);
+        if (e != cudaSuccess) return e;
+        note_launch();
+        mpd::diag_factor_kernel<0><<<1, mpd::NT, bytes, s>>>(T + (size_t)h * (nb + 1), h, nb, k, h, status);
+        return cudaGetLastError();
+    }
     const int bytes = mpd::smem_floats(nb) * 4;
     note_launch();
-    if (alg == 0) mpd::diag_factor_kernel<0><<<1, mpd::NT, bytes, s>>>(T, nb, k, status);
-    else mpd::diag_factor_kernel<1><<<1, mpd::NT, bytes, s>>>(T, nb, k, status);
+    if (alg == 0) mpd::diag_factor_kernel<0><<<1, mpd::NT, bytes, s>>>(T, nb, nb, k, 0, status);
+    else mpd::diag_factor_kernel<1><<<1, mpd::NT, bytes, s>>>(T, nb, nb, k, 0, status);
     return cudaGetLastError();
 }
 

@@ -44,7 +44,8 @@ cudaError_t mps_residual_update(const double *A, int n, int nb, const double *D,
 cudaError_t mps_tile_to_f64(const float *w, double *d, int nb, cudaStream_t s);
 cudaError_t mps_tile_to_f32(const double *d, float *w, int nb, int upper_only, cudaStream_t s);
 cudaError_t mps_panel_trsm(float *W, int n, int nb, int k, int kind, const float *binv, cudaStream_t s);
-cudaError_t mps_block_inverse(const float *W, int n, int nb, int k, int factors, float *binv, cudaStream_t s);
+cudaError_t mps_block_inverse(const float *W, int n, int nb, int k, int factors, float *binv, cudaStream_t s,
+                              int blocks = 0);
 cudaError_t mps_residual(const double *A, int n, int nb, const double *X, const double *B, double *R, int nrhs,
                          double *amax, cudaStream_t s);
 cudaError_t mps_norm_inf_matrix(const double *A, int n, int nb, double *out, cudaStream_t s);
@@ -58,7 +59,7 @@ cudaError_t mpr_solve(const float *W, const float *Dinv, int n, int nb, int kind
 cudaError_t rbt_prepare(int n, uint64_t seed);
 cudaError_t rbt_transform_matrix(const double *A, float *W, int n, int nb, double *amax, cudaStream_t s);
 cudaError_t rbt_transform_vectors(float *X, int n, int cols, int which, cudaStream_t s);
-cudaError_t mpd_factor_tile(int alg, float *W, int n, int nb, int k, int *status, cudaStream_t s);
+cudaError_t mpd_factor_tile(int alg, float *W, int n, int nb, int k, int *status, float *binv, cudaStream_t s);
 cudaError_t mps_invert_diag(const float *W, int n, int nb, float *Dinv, int kind, cudaStream_t s);
 cudaError_t mps_rhs_step(const float *W, const float *Dinv, int n, int nb, int k, float *R, float *S, int kind,
                          cudaStream_t s);
@@ -161,7 +162,7 @@ int mp_factor(int alg, int prec, float *W, int n, int nb, cudaStream_t s, palial
     bool have_rest = false;
     for (int k = 0; k < mt; k++) {
         // the diagonal tile in FP32, one CTA (mp_diag.cu)
-        PALIAL_CK(mpd_factor_tile(alg, W, n, nb, k, status, hi), "diag factor");
+        PALIAL_CK(mpd_factor_tile(alg, W, n, nb, k, status, mb.binv.as<float>(), hi), "diag factor");
         if (k == mt - 1) break;
         const int par = k & 1;
         float *sa = mb.scales.as<float>() + 2 * mt * par, *sb = sa + mt;

@@ -471,6 +471,37 @@ __global__ void __launch_bounds__(NT, 2) panel_trsm_kernel(float *W, int n, int 
     else strip_run(m, T, nb, W + tile_off(n, nb, t, k) + s * 64, nb, nb, binv);
 }
 
+// ---- two-level Cholesky of a diagonal tile (NB >= 512) ---------------------------------------
+// The tile is factored as 2 x 2 blocks of h = NB/2: one-CTA factorization of A11, then these
+// two multi-CTA steps, then one-CTA factorization of A22 (mp_diag.cu).
+// A12 (h x h at T + h ld) <- U11^-T A12, U11 the factored leading block (binv: inverses of its
+// 64 x 64 diagonal blocks); one CTA per 64-column strip.
+__global__ void __launch_bounds__(NT, 2) half_panel_kernel(float *T, int h, int ld, const float *binv) {
+    extern __shared__ __align__(16) float smem[];
+    const Smem m = smem_parts(smem);
+    strip_lut(m, T, ld, T + (size_t)h * ld + (size_t)blockIdx.x * 64 * ld, ld, h, binv);
+}
+// A22 -= A12^T A12 on the 64 x 64 blocks (bi, bj), bi <= bj, of the trailing h x h block (one
+// CTA each); inside diagonal blocks the strictly lower entries stay unchanged.
+__global__ void __launch_bounds__(NT, 2) half_update_kernel(float *T, int h, int ld) {
+    extern __shared__ __align__(16) float smem[];
+    int q = blockIdx.x, bj = 0;
+    while (q > bj) {
+        q -= bj + 1;
+        bj++;
+    }
+    const int bi = q;
+    const float *A12 = T + (size_t)h * ld;
+    float *C = T + (size_t)(h + bi * 64) + (size_t)(h + bj * 64) * ld;
+    const Smem m = smem_parts(smem);
+    if (bi == bj)
+        cta_gemm<true, false, true>(64, 64, h, -1.f, A12 + (size_t)bi * 64 * ld, ld, A12 + (size_t)bj * 64 * ld, ld, C,
+                                    ld, m.g);
+    else
+        cta_gemm<true, false>(64, 64, h, -1.f, A12 + (size_t)bi * 64 * ld, ld, A12 + (size_t)bj * 64 * ld, ld, C, ld,
+                              m.g);
+}
+
 // ---- diagonal-tile inverses for the refinement solves --------------------------------------
 // Dinv tile k (nb x nb, column-major) = T_kk^-1 with T the upper factor (kind 1) or the unit
 // lower factor (kind 2) of the diagonal tile; one CTA per 64-column strip of the identity.
@@ -757,7 +788,10 @@ cudaError_t mps_configure() {
     e = cudaFuncSetAttribute(mps::rhs_apply_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, mps::SMEM_BYTES);
     if (e != cudaSuccess) return e;
     e = cudaFuncSetAttribute(mps::rhs_update2_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, mps::SMEM_BYTES);
-    return e;
+    if (e != cudaSuccess) return e;
+    e = cudaFuncSetAttribute(mps::half_panel_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, mps::SMEM_BYTES);
+    if (e != cudaSuccess) return e;
+    return cudaFuncSetAttribute(mps::half_update_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, mps::SMEM_BYTES);
 }
 
 cudaError_t mps_f64_to_f32(const double *A, float *W, int n, int nb, double shift, cudaStream_t s, double *amax,
@@ -822,9 +856,22 @@ cudaError_t mps_rhs_step(const float *W, const float *Dinv, int n, int nb, int k
 }
 // binv (2 nb x 64 floats): inverses of the 64 x 64 diagonal blocks of tile k's upper factor,
 // and for LU (factors = 2) of its unit lower factor
-cudaError_t mps_block_inverse(const float *W, int n, int nb, int k, int factors, float *binv, cudaStream_t s) {
+// (blocks: how many leading 64 x 64 diagonal blocks, 0 = all nb / 64)
+cudaError_t mps_block_inverse(const float *W, int n, int nb, int k, int factors, float *binv, cudaStream_t s,
+                              int blocks) {
     note_launch();
-    mps::block_inverse_kernel<<<dim3(nb / 64, factors), 64, 0, s>>>(W, n, nb, k, binv);
+    mps::block_inverse_kernel<<<dim3(blocks > 0 ? blocks : nb / 64, factors), 64, 0, s>>>(W, n, nb, k, binv);
+    return cudaGetLastError();
+}
+cudaError_t mps_half_panel(float *T, int h, int ld, const float *binv, cudaStream_t s) {
+    note_launch();
+    mps::half_panel_kernel<<<h / 64, mps::NT, mps::SMEM_BYTES, s>>>(T, h, ld, binv);
+    return cudaGetLastError();
+}
+cudaError_t mps_half_update(float *T, int h, int ld, cudaStream_t s) {
+    const int nbl = h / 64;
+    note_launch();
+    mps::half_update_kernel<<<nbl * (nbl + 1) / 2, mps::NT, mps::SMEM_BYTES, s>>>(T, h, ld);
     return cudaGetLastError();
 }
 cudaError_t mps_panel_trsm(float *W, int n, int nb, int k, int kind, const float *binv, cudaStream_t s) {

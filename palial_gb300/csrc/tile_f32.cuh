@@ -79,8 +79,9 @@ __device__ __forceinline__ void stage_store(float (*Xs)[SP], const float4 (&v)[2
     }
 }
 
-// C[M x N] += alpha * op(A) op(B) (beta = 1), dims multiples of 64 / 32.  Ends synced.
-template <bool TA, bool TB>
+// C[M x N] += alpha * op(A) op(B) (beta = 1), dims multiples of 64 / 32.  KEEP_LOWER leaves
+// the entries below C's diagonal unchanged (an upper-triangle update).  Ends synced.
+template <bool TA, bool TB, bool KEEP_LOWER = false>
 __device__ __forceinline__ void cta_gemm(int M, int N, int K, float alpha, const float *A, int lda, const float *B, int ldb, float *C,
                          int ldc, float *smem) {
     float (*As)[SP] = reinterpret_cast<float (*)[SP]>(smem);
@@ -123,10 +124,18 @@ __device__ __forceinline__ void cta_gemm(int M, int N, int K, float alpha, const
             for (int y = 0; y < 4; y++)
                 cv[y] = __ldcg(reinterpret_cast<const float4 *>(C + (size_t)(i0 + tr * 4) + (size_t)(j0 + tc * 4 + y) * ldc));
 #pragma unroll
-            for (int y = 0; y < 4; y++)
-                *reinterpret_cast<float4 *>(C + (size_t)(i0 + tr * 4) + (size_t)(j0 + tc * 4 + y) * ldc) =
-                    make_float4(fmaf(alpha, acc[0][y], cv[y].x), fmaf(alpha, acc[1][y], cv[y].y),
-                                fmaf(alpha, acc[2][y], cv[y].z), fmaf(alpha, acc[3][y], cv[y].w));
+            for (int y = 0; y < 4; y++) {
+                float4 o = make_float4(fmaf(alpha, acc[0][y], cv[y].x), fmaf(alpha, acc[1][y], cv[y].y),
+                                       fmaf(alpha, acc[2][y], cv[y].z), fmaf(alpha, acc[3][y], cv[y].w));
+                if (KEEP_LOWER) {
+                    const int r = i0 + tr * 4, c = j0 + tc * 4 + y;
+                    if (r + 0 > c) o.x = cv[y].x;
+                    if (r + 1 > c) o.y = cv[y].y;
+                    if (r + 2 > c) o.z = cv[y].z;
+                    if (r + 3 > c) o.w = cv[y].w;
+                }
+                *reinterpret_cast<float4 *>(C + (size_t)(i0 + tr * 4) + (size_t)(j0 + tc * 4 + y) * ldc) = o;
+            }
         }
     __syncthreads();
 }
