@@ -84,6 +84,14 @@ static uint64_t splitmix(uint64_t z)
     return z ^ (z >> 31);
 }
 
+/* a JSON number, or null when it is not finite (JSON has no inf / nan) */
+static void json_num(const char *key, double v, const char *fmt)
+{
+    printf(", \"%s\": ", key);
+    if (isfinite(v)) printf(fmt, v);
+    else printf("null");
+}
+
 static void print_clocks(void)
 {
     palial_clock_report c;
@@ -262,12 +270,14 @@ int main(int argc, char *argv[])
         if (rc < 0) fprintf(stderr, "palial: solve failed: %s (%s)\n", palial_gpu_error_string(rc), st.message);
         if (!quiet) {
             printf("{\"algorithm\": \"%s\", \"mode\": \"solve\", \"n\": %d, \"nb\": %d, \"nrhs\": %d, "
-                   "\"precision\": \"%s\", \"code\": %d, \"seconds\": %.6f, \"total_seconds\": %.6f, "
-                   "\"tflops\": %.4f, \"ir_iters\": %d, \"gmres_iters\": %d, \"backward_error\": %.3e, "
-                   "\"factor_seconds\": %.6f, \"tasks\": %lld",
-                   algorithm, MSIZE, BSIZE, nrhs, precision_name(palial_entry_opts.precision), rc, st.seconds,
-                   st.total_seconds, st.tflops, st.ir_iters, st.gmres_iters, st.backward_error, st.factor_seconds,
-                   st.ntasks);
+                   "\"precision\": \"%s\", \"code\": %d, \"ir_iters\": %d, \"gmres_iters\": %d, \"tasks\": %lld",
+                   algorithm, MSIZE, BSIZE, nrhs, precision_name(palial_entry_opts.precision), rc, st.ir_iters,
+                   st.gmres_iters, st.ntasks);
+            json_num("seconds", st.seconds, "%.6f");
+            json_num("total_seconds", st.total_seconds, "%.6f");
+            json_num("tflops", st.tflops, "%.4f");
+            json_num("backward_error", st.backward_error, "%.3e");
+            json_num("factor_seconds", st.factor_seconds, "%.6f");
             if (clocks) print_clocks();
             printf("}\n");
         }
@@ -304,10 +314,12 @@ int main(int argc, char *argv[])
     if (trace && st.code >= 0) palial_gpu_trace_dump(trace, trace_csv);
     else if (trace_csv && st.code >= 0) palial_gpu_trace_dump("/dev/null", trace_csv);
     if (!quiet) {
-        printf("{\"algorithm\": \"%s\", \"n\": %d, \"nb\": %d, \"block\": %d, \"code\": %d, \"seconds\": %.6f, "
-               "\"total_seconds\": %.6f, \"tflops\": %.4f, \"tasks\": %lld, \"residual_probe\": %.3e",
-               algorithm, MSIZE, BSIZE, palial_entry_opts.block, st.code, st.seconds, st.total_seconds, st.tflops,
-               st.ntasks, resid);
+        printf("{\"algorithm\": \"%s\", \"n\": %d, \"nb\": %d, \"block\": %d, \"code\": %d, \"tasks\": %lld",
+               algorithm, MSIZE, BSIZE, palial_entry_opts.block, st.code, st.ntasks);
+        json_num("seconds", st.seconds, "%.6f");
+        json_num("total_seconds", st.total_seconds, "%.6f");
+        json_num("tflops", st.tflops, "%.4f");
+        json_num("residual_probe", resid, "%.3e");
         if (clocks) print_clocks();
         printf("}\n");
     }
