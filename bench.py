@@ -1,15 +1,15 @@
 """Benchmark: tiled Cholesky at N = 32768, NB = 512 on one GB300 (per GPU).
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-                    [--suite fp64|kappa]
+                    [--suite fp64|kappa|batched|costmodel|kernels]
 
 A step is one solve A X = B (16 right-hand sides, uniform [-1, 1)) of a device-resident
 SPD matrix A = B B^T + N I (seed = rank; the reference's tile layout) by the mixed-precision
 path: BF16x3 trailing updates on tcgen05 (operands split into BF16 hi + lo, three products,
 FP32 accumulation; --precision bf16 / fp8 select one product), FP32 diagonal tiles and
-panels, compensated-FP32 refinement residuals (FP64 accumulation) and refinement to the
-FP64-level normwise backward error (<= 1e-14 * N), checked after the timed region with the
-FP64 residual.  value = FP64-equivalent algorithmic flops (N^3/3) / time to solution
+panels, compensated-FP32 refinement residuals (FP64 accumulation; once the correction is
+small, the update form r - A d with FP32 products) and refinement to the FP64-level normwise
+backward error (<= 1e-14 * N), checked after the timed region with the FP64 residual.  value = FP64-equivalent algorithmic flops (N^3/3) / time to solution
 (factorization + refinement), summed over ranks (replicas, no collective on the data path).
 Inputs (8.6 GB) are far larger than L2 (129 MB): no flush is needed.
 
@@ -19,8 +19,9 @@ The JSON line also carries:
   e2e           the same solve through the host-buffer C ABI (palial_gpu_solve_ir_host on
                 pinned host memory: A and B copied in, X copied out, every step);
   roofline      the tcgen05 trailing-update kernel (the mixed path's tensor-core kernel),
-                timed live on the largest step (k = 0): HBM-bound at K = NB = 512 with FP32
-                C, so bytes per launch / time against MEASURED_PEAKS.json's hbm_gbs;
+                timed live on the largest step (k = 0); bound chosen by its arithmetic
+                intensity against the measured ridge (BF16x3: tensor), achieved / measured
+                peak from MEASURED_PEAKS.json, the HBM rate beside it;
   cpu_baseline  the oracle's OpenMP port of the reference's Cholesky (same task DAG, same
                 OpenBLAS calls) on this host's cores, on a bounded sample (N = 16384);
   clocks        nvidia-smi samples taken during the timed region.
@@ -28,7 +29,8 @@ The JSON line also carries:
 host cores) on the same metric, one bounded sample (N = 16384) per step.
 `--suite fp64` prints one line per FP64 factorization of configs N in {16384, 32768} for
 Cholesky, LU and QR; `--suite kappa` one line per kappa in {1e2, 1e6, 1e10}, algorithm and
-precision at N = 32768 (A = U diag(s) V^T, 64 Householder reflectors each side).
+precision at N = 32768 (A = U diag(s) V^T, 64 Householder reflectors each side);
+`--suite kernels [--n N]` times the dominant kernels alone (the small case ncu captures run).
 """
 from __future__ import annotations
 
@@ -351,8 +353,58 @@ def run_costmodel(args, P, torch) -> None:
                       "factors_bitwise_identical_across_schedules": same_bits}), flush=True)
 
 
+def run_kernels(args, P, torch) -> None:
+    """The path's dominant kernels alone at N = --n (small captures for ncu): the tcgen05
+    trailing update of step 0 (pack included), the compensated-FP32 residual and the
+    update-form residual with 16 right-hand sides, and the two-level FP32 factorization of one
+    NB x NB diagonal tile; CUDA-event times (best of 3 after 2 warm-ups) per call."""
+    import ctypes
+    n = args.n
+    upd = time_update_kernel(P, torch, n, args.precision)
+    a = torch.empty(n * n, dtype=torch.float64, device="cuda")
+    P.gen_spd(a.data_ptr(), n, NB, 0)
+    g = torch.Generator("cuda").manual_seed(1)
+    x = torch.rand(16, n, dtype=torch.float64, device="cuda", generator=g) - 0.5
+    b = torch.rand(16, n, dtype=torch.float64, device="cuda", generator=g)
+    r = torch.empty_like(b)
+    lib = P.lib()
+    lib.palial_gpu_residual.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_void_p,
+                                        ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_void_p]
+
+    def best(fn):
+        for _ in range(2):
+            fn()
+        ts = []
+        for _ in range(3):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            fn()
+            e1.record()
+            torch.cuda.synchronize()
+            ts.append(e0.elapsed_time(e1) * 1e-3)
+        return min(ts)
+
+    t_df = best(lambda: lib.palial_gpu_residual(a.data_ptr(), n, NB, x.data_ptr(), b.data_ptr(), r.data_ptr(), 16,
+                                                1, None))
+    t_up = best(lambda: lib.palial_gpu_residual(a.data_ptr(), n, NB, x.data_ptr(), None, r.data_ptr(), 16, 2,
+                                                None))
+    t1 = torch.empty(NB * NB, dtype=torch.float64, device="cuda")
+    P.gen_spd(t1.data_ptr(), NB, NB, 0)
+    w1 = torch.empty(NB * NB, dtype=torch.float32, device="cuda")
+    t_diag = best(lambda: P.mp_factor("cholesky", t1.data_ptr(), w1.data_ptr(), NB, NB, precision=args.precision))
+    print(json.dumps({"suite": "kernels", "n": n, "nb": NB, "precision": args.precision,
+                      "update_step0_s": upd["seconds"], "update_tflops": upd["flop"] / upd["seconds"] * 1e-12,
+                      "update_gbs": upd["bytes"] / upd["seconds"] * 1e-9,
+                      "residual_compensated_call_s": t_df, "residual_update_form_call_s": t_up,
+                      "residual_update_form_gbs": 8.0 * n * n / t_up * 1e-9,
+                      "diag_tile_call_s": t_diag}), flush=True)
+
+
 def run_suite(args, P, torch) -> None:
     import numpy as np
+    if args.suite == "kernels":
+        run_kernels(args, P, torch)
+        return
     if args.suite == "costmodel":
         run_costmodel(args, P, torch)
         return
@@ -414,7 +466,7 @@ def main() -> None:
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--n", type=int, default=N)
     ap.add_argument("--precision", default="bf16x3")
-    ap.add_argument("--suite", default=None, choices=[None, "fp64", "kappa", "batched", "costmodel"])
+    ap.add_argument("--suite", default=None, choices=[None, "fp64", "kappa", "batched", "costmodel", "kernels"])
     ap.add_argument("--batch", type=int, default=2000)
     ap.add_argument("--no-fp64", action="store_true")
     args = ap.parse_args()

@@ -370,7 +370,11 @@ __global__ void __launch_bounds__(NT, 1) diag_factor_kernel(float *T, int nb, in
     int zero = 0;
     for (int j0 = 0; j0 < nb; j0 += 64) {
         float *D = T + j0 + (size_t)j0 * ld;
-        for (int e = threadIdx.x; e < 4096; e += NT) Ds[e >> 6][e & 63] = D[(e & 63) + (size_t)(e >> 6) * ld];
+#pragma unroll
+        for (int j = 0; j < 4096 / NT; j++) {
+            const int e = threadIdx.x + NT * j;
+            Ds[e >> 6][e & 63] = D[(e & 63) + (size_t)(e >> 6) * ld];
+        }
         __syncthreads();
         if (ALG == 0) {
             const int bad = chol64(Ds, sflag);

@@ -331,12 +331,18 @@ __device__ __forceinline__ Smem smem_parts(float *s) {
 // its 64 unknowns in registers, eliminating right-looking (the FMAs of one step are
 // independent; the coefficients are shared-memory broadcasts).  The panel solves then apply
 // each diagonal block as a 64 x 64 product instead of a 64-step substitution.
-__global__ void __launch_bounds__(64) block_inverse_kernel(const float *W, int n, int nb, int k, float *binv) {
+__global__ void __launch_bounds__(256) block_inverse_kernel(const float *W, int n, int nb, int k, float *binv) {
     __shared__ __align__(16) float Ts[64][64];  // Ts[c][r] = block(r, c)
     const int b = blockIdx.x, which = blockIdx.y;
     const float *T = W + tile_off(n, nb, k, k) + (size_t)b * 64 * ((size_t)nb + 1);
-    for (int e = threadIdx.x; e < 4096; e += 64) Ts[e >> 6][e & 63] = T[(e & 63) + (size_t)(e >> 6) * nb];
+    // 256 threads load (16 independent loads each, all in flight), 64 of them solve
+#pragma unroll
+    for (int j = 0; j < 16; j++) {
+        const int e = threadIdx.x + 256 * j;
+        Ts[e >> 6][e & 63] = T[(e & 63) + (size_t)(e >> 6) * nb];
+    }
     __syncthreads();
+    if (threadIdx.x >= 64) return;
     const int c = threadIdx.x;
     float x[64];
 #pragma unroll
@@ -379,7 +385,10 @@ __global__ void __launch_bounds__(64) block_inverse_kernel(const float *W, int n
 // B(r, c)); thread: rows 4 tr .. 4 tr + 3, columns 4 tc .. 4 tc + 3.  Ends synced.
 template <int OP>
 __device__ __forceinline__ void apply_inv64(const Smem &m, const float *X, float *B, int ldb) {
-    for (int e = threadIdx.x; e < 4096; e += NT) {
+    static_assert(4096 % NT == 0, "whole staging rounds");
+#pragma unroll
+    for (int j = 0; j < 4096 / NT; j++) {
+        const int e = threadIdx.x + NT * j;
         m.Ds[e >> 6][e & 63] = ldg(X + e);
         m.Bs[e >> 6][e & 63] = B[(e & 63) + (size_t)(e >> 6) * ldb];
     }
@@ -860,7 +869,7 @@ cudaError_t mps_rhs_step(const float *W, const float *Dinv, int n, int nb, int k
 cudaError_t mps_block_inverse(const float *W, int n, int nb, int k, int factors, float *binv, cudaStream_t s,
                               int blocks) {
     note_launch();
-    mps::block_inverse_kernel<<<dim3(blocks > 0 ? blocks : nb / 64, factors), 64, 0, s>>>(W, n, nb, k, binv);
+    mps::block_inverse_kernel<<<dim3(blocks > 0 ? blocks : nb / 64, factors), 256, 0, s>>>(W, n, nb, k, binv);
     return cudaGetLastError();
 }
 cudaError_t mps_half_panel(float *T, int h, int ld, const float *binv, cudaStream_t s) {

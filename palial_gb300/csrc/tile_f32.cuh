@@ -194,7 +194,11 @@ __device__ __forceinline__ void cta_gemm_rw(int M, int K, float alpha, const flo
 }
 
 __device__ __forceinline__ void load_diag64(float (*Ds)[DP], const float *A, int ld) {
-    for (int e = threadIdx.x; e < 4096; e += NT) Ds[e >> 6][e & 63] = ldg(A + (e & 63) + (size_t)(e >> 6) * ld);
+#pragma unroll
+    for (int j = 0; j < 4096 / NT; j++) {
+        const int e = threadIdx.x + NT * j;
+        Ds[e >> 6][e & 63] = ldg(A + (e & 63) + (size_t)(e >> 6) * ld);
+    }
     __syncthreads();
 }
 
