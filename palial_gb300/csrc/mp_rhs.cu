@@ -47,13 +47,13 @@ struct RhsParams {
     unsigned long long timeout_ns;
 };
 
-constexpr int SMEM_BYTES = GEMM_SMEM_FLOATS * 4;
+constexpr int SMEM_BYTES = RW2_SMEM_FLOATS * 4;
 
 __device__ __forceinline__ size_t tile_off(int n, int nb, int tm, int tn) {
     return (size_t)nb * nb * ((size_t)tm + (size_t)(n / nb) * tn);
 }
 
-__global__ void __launch_bounds__(NT, 2) rhs_solve_kernel(RhsParams p) {
+__global__ void __launch_bounds__(NT, 1) rhs_solve_kernel(RhsParams p) {
     extern __shared__ __align__(16) float smem[];
     __shared__ int s_task, s_abort;
     const int n = p.n, nb = p.nb;
@@ -95,16 +95,16 @@ __global__ void __launch_bounds__(NT, 2) rhs_solve_kernel(RhsParams p) {
             float *out = p.Y + (size_t)t.k * nb + rb;
             for (int e = threadIdx.x; e < 64 * RW; e += NT) out[(e & 63) + (size_t)(e >> 6) * n] = 0.f;
             __syncthreads();
-            if (p.kind == 0) cta_gemm_rw<true>(64, nb, 1.f, D + (size_t)rb * nb, nb, p.R + (size_t)t.k * nb, n, out, n, smem);
-            else cta_gemm_rw<false>(64, nb, 1.f, D + rb, nb, p.R + (size_t)t.k * nb, n, out, n, smem);
+            if (p.kind == 0) cta_gemm_rw128<true>(nb, 1.f, D + (size_t)rb * nb, nb, p.R + (size_t)t.k * nb, n, out, n, smem);
+            else cta_gemm_rw128<false>(nb, 1.f, D + rb, nb, p.R + (size_t)t.k * nb, n, out, n, smem);
         } else {
             // R_t[rb] -= op(W_kt)[rb rows] Y_k
             float *Rt = p.R + (size_t)t.t * nb + rb;
             const float *Yk = p.Y + (size_t)t.k * nb;
             if (p.kind == 0)
-                cta_gemm_rw<true>(64, nb, -1.f, p.W + tile_off(n, nb, t.k, t.t) + (size_t)rb * nb, nb, Yk, n, Rt, n, smem);
+                cta_gemm_rw128<true>(nb, -1.f, p.W + tile_off(n, nb, t.k, t.t) + (size_t)rb * nb, nb, Yk, n, Rt, n, smem);
             else
-                cta_gemm_rw<false>(64, nb, -1.f, p.W + tile_off(n, nb, t.t, t.k) + rb, nb, Yk, n, Rt, n, smem);
+                cta_gemm_rw128<false>(nb, -1.f, p.W + tile_off(n, nb, t.t, t.k) + rb, nb, Yk, n, Rt, n, smem);
         }
         __syncthreads();
         if (threadIdx.x == 0) {
@@ -227,7 +227,7 @@ cudaError_t mpr_solve(const float *W, const float *Dinv, int n, int nb, int kind
     p.kind = kind;
     p.timeout_ns = 30ull * 1000000000ull;
     note_launch();
-    mpr::rhs_solve_kernel<<<g.sms * 2, f32::NT, mpr::SMEM_BYTES, s>>>(p);
+    mpr::rhs_solve_kernel<<<g.sms, f32::NT, mpr::SMEM_BYTES, s>>>(p);  // one per SM (255 registers)
     return cudaGetLastError();
 }
 

@@ -193,6 +193,87 @@ __device__ __forceinline__ void cta_gemm_rw(int M, int K, float alpha, const flo
     __syncthreads();
 }
 
+// C[64 x 16] += alpha * op(A) B as cta_gemm_rw for M = 64, with K staged in chunks of 128 (K a
+// multiple of 128): each chunk's loads (a 32 KB slice of A, 8 KB of B) are one round trip, in
+// flight while the previous chunk is computed, so a K = 512 product costs four memory round
+// trips instead of sixteen.  Shared layouts: op(A) = A^T is stored row-major by output row
+// (Ar[i][p], float4 stores), op(A) = A column-major by K (Ac[p][i]); B as Bs[p][j].
+constexpr int KC2 = 128;
+constexpr int AP2 = KC2 + 4;  // pitch of Ar (float4-aligned, rows 4 banks apart)
+constexpr int RW2_SMEM_FLOATS = (64 * AP2 > KC2 * SP ? 64 * AP2 : KC2 * SP) + KC2 * RP;
+template <bool TA>
+__device__ __forceinline__ void cta_gemm_rw128(int K, float alpha, const float *A, int lda, const float *B, int ldb,
+                                               float *C, int ldc, float *smem) {
+    float (*Ar)[AP2] = reinterpret_cast<float (*)[AP2]>(smem);
+    float (*Ac)[SP] = reinterpret_cast<float (*)[SP]>(smem);
+    float (*Bs)[RP] = reinterpret_cast<float (*)[RP]>(smem + (64 * AP2 > KC2 * SP ? 64 * AP2 : KC2 * SP));
+    const int t = threadIdx.x, tx = t & 3, ty = t >> 2;
+    static_assert(NT == 256, "thread mapping");
+    float4 ra[8], rb[2];
+    auto load = [&](int p0) {
+#pragma unroll
+        for (int q = 0; q < 8; q++) {
+            const int e = t + NT * q;
+            if (TA) {
+                const int i = e >> 5, p = (e & 31) * 4;
+                ra[q] = __ldcg(reinterpret_cast<const float4 *>(A + (size_t)(p0 + p) + (size_t)i * lda));
+            } else {
+                const int p = e >> 4, i = (e & 15) * 4;
+                ra[q] = __ldcg(reinterpret_cast<const float4 *>(A + (size_t)i + (size_t)(p0 + p) * lda));
+            }
+        }
+#pragma unroll
+        for (int q = 0; q < 2; q++) {
+            // a warp spans the 16 right-hand sides (B is small and in L2): conflict-free stores
+            const int e = t + NT * q;
+            const int j = e & 15, p = (e >> 4) * 4;
+            rb[q] = __ldcg(reinterpret_cast<const float4 *>(B + (size_t)(p0 + p) + (size_t)j * ldb));
+        }
+    };
+    float acc[4] = {0.f, 0.f, 0.f, 0.f};
+    if (K > 0) load(0);
+    for (int p0 = 0; p0 < K; p0 += KC2) {
+#pragma unroll
+        for (int q = 0; q < 8; q++) {
+            const int e = t + NT * q;
+            if (TA) {
+                const int i = e >> 5, p = (e & 31) * 4;
+                *reinterpret_cast<float4 *>(&Ar[i][p]) = ra[q];
+            } else {
+                const int p = e >> 4, i = (e & 15) * 4;
+                *reinterpret_cast<float4 *>(&Ac[p][i]) = ra[q];
+            }
+        }
+#pragma unroll
+        for (int q = 0; q < 2; q++) {
+            const int e = t + NT * q;
+            const int j = e & 15, p = (e >> 4) * 4;
+            Bs[p][j] = rb[q].x;
+            Bs[p + 1][j] = rb[q].y;
+            Bs[p + 2][j] = rb[q].z;
+            Bs[p + 3][j] = rb[q].w;
+        }
+        __syncthreads();
+        if (p0 + KC2 < K) load(p0 + KC2);
+#pragma unroll 8
+        for (int p = 0; p < KC2; p++) {
+            const float a = TA ? Ar[ty][p] : Ac[p][ty];
+            const float4 b = *reinterpret_cast<const float4 *>(&Bs[p][tx * 4]);
+            acc[0] = fmaf(a, b.x, acc[0]);
+            acc[1] = fmaf(a, b.y, acc[1]);
+            acc[2] = fmaf(a, b.z, acc[2]);
+            acc[3] = fmaf(a, b.w, acc[3]);
+        }
+        __syncthreads();
+    }
+    float cv[4];
+#pragma unroll
+    for (int y = 0; y < 4; y++) cv[y] = ldg(C + (size_t)ty + (size_t)(tx * 4 + y) * ldc);
+#pragma unroll
+    for (int y = 0; y < 4; y++) C[(size_t)ty + (size_t)(tx * 4 + y) * ldc] = fmaf(alpha, acc[y], cv[y]);
+    __syncthreads();
+}
+
 __device__ __forceinline__ void load_diag64(float (*Ds)[DP], const float *A, int ld) {
 #pragma unroll
     for (int j = 0; j < 4096 / NT; j++) {
