@@ -598,7 +598,7 @@ def main() -> None:
             "vs_baseline": None, "dtype": "bf16", "data": "synthetic",
             "config": {"workload": f"mixed-precision Cholesky + IR, N={n}, NB={NB}, 16 RHS, {args.precision} "
                                    "trailing updates on tcgen05 (FP32 accumulate), FP32 diagonal tiles and "
-                                   "panels, compensated-FP32 refinement residuals, FP64-checked backward error; SPD B*B^T+N*I seed=rank, device-resident; inputs 8.6 GB >> L2 "
+                                   "panels, compensated-FP32 and update-form refinement residuals, FP64-checked backward error; SPD B*B^T+N*I seed=rank, device-resident; inputs 8.6 GB >> L2 "
                                    "(no flush needed)",
                        "n": n, "nb": NB, "nrhs": nrhs, "precision": args.precision,
                        "parallelism": f"replicas x{world}"},
@@ -611,11 +611,11 @@ def main() -> None:
                          "frac": achieved / peak,
                          "hbm_gbs": gbs, "hbm_frac": gbs / pk.get("hbm_gbs", 6800.0),
                          # DRAM read + write of one launch: ncu (dram__bytes_read.sum +
-                         # dram__bytes_write.sum) on the same kernel at N=8192, k=0 (120 tile pairs,
-                         # 199.0 MB, profiles/mp_update_and_residual_n8192.md), scaled by tile pairs
-                         "traffic": 199.0e6 / 120 * ((n // NB - 1) * (n // NB) // 2),
-                         "traffic_note": "ncu capture of the BF16 variant at N=8192 step 0 (the FP32 C "
-                                         "tiles dominate and are the same for every variant), scaled by tile pairs",
+                         # dram__bytes_write.sum) on the BF16x3 update at N=8192, k=0 (120 tile
+                         # pairs, 141.7 + 67.0 MB, profiles/mixed_kernels_n8192.md), scaled by tile pairs
+                         "traffic": 208.7e6 / 120 * ((n // NB - 1) * (n // NB) // 2),
+                         "traffic_note": "ncu capture of the BF16x3 update at N=8192 step 0 (bench.py --suite "
+                                         "kernels --n 8192), scaled by tile pairs",
                          "kernel": "mp_update_kernel<%s> (tcgen05, step k=0 of N=%d, pack included)" % (args.precision, n),
                          "tensor_tflops": upd["flop"] / upd["seconds"] * 1e-12,
                          "tensor_frac_of_bf16_peak": upd["flop"] / upd["seconds"] * 1e-12 / pk.get("bf16_tflops", 1900.0),
