@@ -114,17 +114,18 @@ __global__ void __launch_bounds__(NT, 1) rhs_solve_kernel(RhsParams p) {
     }
 }
 
-// Task list of one direction, right-looking: step k's applies, then its updates of every
-// later tile (the next tile first: it is on the critical path).  Updates into one 64-row block
-// come from different steps, so the per-block chains never fill the dispatch window.
+// Task list of one direction, right-looking with a lookahead of one tile: step k's updates of
+// the next tile come first, then that tile's applies (the critical path: they need only those
+// updates and the earlier steps'), then step k's updates of the remaining tiles.  Updates into
+// one 64-row block run in k order (deterministic sums).  Every wait refers to earlier records,
+// so the in-order dispatch cannot deadlock.
 // Objects: [0, mt) updates into tile t; [mt, 2 mt) applies of tile k; [2 mt, 2 mt + mt * nbl)
 // updates into 64-row block (t, b).
 std::vector<RhsTask> build_tasks(int mt, int nbl, int kind) {
     std::vector<RhsTask> v;
     const auto order = [&](int i) { return kind == 1 ? mt - 1 - i : i; };  // solve order
     std::vector<int> upd_tile(mt, 0), upd_blk((size_t)mt * nbl, 0);
-    for (int ik = 0; ik < mt; ik++) {
-        const int k = order(ik);
+    const auto add_applies = [&](int k) {
         for (int b = 0; b < nbl; b++) {
             RhsTask r{};
             r.type = 0;
@@ -140,31 +141,39 @@ std::vector<RhsTask> build_tasks(int mt, int nbl, int kind) {
             r.nsig = 1;
             v.push_back(r);
         }
-        for (int it = ik + 1; it < mt; it++) {
-            const int t = order(it);
-            for (int b = 0; b < nbl; b++) {
-                RhsTask r{};
-                r.type = 1;
-                r.k = k;
-                r.t = t;
-                r.b = b;
-                const int blk = 2 * mt + t * nbl + b;
-                r.wobj[0] = mt + k;
-                r.wcnt[0] = nbl;  // Y_k complete
-                r.nwait = 1;
-                if (upd_blk[(size_t)t * nbl + b] > 0) {  // the previous step's update of this block
-                    r.wobj[1] = blk;
-                    r.wcnt[1] = upd_blk[(size_t)t * nbl + b];
-                    r.nwait = 2;
-                }
-                r.sobj[0] = t;
-                r.sobj[1] = blk;
-                r.nsig = 2;
-                upd_blk[(size_t)t * nbl + b]++;
-                upd_tile[t]++;
-                v.push_back(r);
+    };
+    const auto add_updates = [&](int k, int t) {
+        for (int b = 0; b < nbl; b++) {
+            RhsTask r{};
+            r.type = 1;
+            r.k = k;
+            r.t = t;
+            r.b = b;
+            const int blk = 2 * mt + t * nbl + b;
+            r.wobj[0] = mt + k;
+            r.wcnt[0] = nbl;  // Y_k complete
+            r.nwait = 1;
+            if (upd_blk[(size_t)t * nbl + b] > 0) {  // the previous step's update of this block
+                r.wobj[1] = blk;
+                r.wcnt[1] = upd_blk[(size_t)t * nbl + b];
+                r.nwait = 2;
             }
+            r.sobj[0] = t;
+            r.sobj[1] = blk;
+            r.nsig = 2;
+            upd_blk[(size_t)t * nbl + b]++;
+            upd_tile[t]++;
+            v.push_back(r);
         }
+    };
+    add_applies(order(0));
+    for (int ik = 0; ik < mt; ik++) {
+        const int k = order(ik);
+        if (ik + 1 < mt) {
+            add_updates(k, order(ik + 1));
+            add_applies(order(ik + 1));
+        }
+        for (int it = ik + 2; it < mt; it++) add_updates(k, order(it));
     }
     return v;
 }
