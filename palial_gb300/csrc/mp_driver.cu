@@ -30,13 +30,13 @@
 namespace palial {
 cudaError_t mp_update(int mode, int upper, float *C, int n, int nb, int k, const void *a_hi, const void *a_lo,
                       const void *b_hi, const void *b_lo, const float *scale_a, const float *scale_b, int *status,
-                      cudaStream_t s, int part = 0);
+                      cudaStream_t s, int part = 0, int r0 = 0, int r1 = 0);
 cudaError_t mp_pack_rows(int mode, const float *W, int n, int nb, int k, void *hi, void *lo, float *scales,
                          cudaStream_t s);
 cudaError_t mp_pack_cols(int mode, const float *W, int n, int nb, int k, void *hi, void *lo, float *scales,
                          cudaStream_t s);
 cudaError_t mps_f64_to_f32(const double *A, float *W, int n, int nb, double shift, cudaStream_t s,
-                           double *amax = nullptr, bool upper_only = false);
+                           double *amax = nullptr, bool upper_only = false, int r0 = 0, int r1 = -1);
 cudaError_t mps_residual_df(const double *A, int n, int nb, const double *X, const double *colmax, const double *B,
                             double *R, int nrhs, int sigma, float2 *Xs, int *tau, double *amax, cudaStream_t s);
 cudaError_t mps_residual_update(const double *A, int n, int nb, const double *D, const double *colmax, double *R,
@@ -126,6 +126,20 @@ static cudaError_t wait_full_matrix(cudaStream_t s) {
     return g_full_ready ? cudaStreamWaitEvent(s, g_full_ready, 0) : cudaSuccess;
 }
 
+// Row-group arrival (host-buffer mixed Cholesky): the upper triangle arrives in groups of tile
+// rows [gs[g], ge[g]) (FP32 working copy converted per group, event ready[g]); group 0 holds
+// rows 0 and 1.  The factorization starts on group 0 and treats group g as present from step
+// kg[g] <= gs[g] - 2 on: until then the trailing updates skip its rows; at step kg[g] (before
+// that step's rest update, on the same stream) the skipped steps 0..kg[g]-1 are applied to it
+// in step order, from packed panels kept for every step, so each tile receives the same updates
+// in the same order as without deferral.  One-shot: mp_factor clears `on`.
+struct RowArrival {
+    bool on = false;
+    int ngroups = 0;
+    int gs[64], ge[64], kg[64];
+    cudaEvent_t ready[64] = {};
+} g_arrival;
+
 static cudaError_t lookahead_init() {
     if (g_la.hi) return cudaSuccess;
     int least = 0, greatest = 0;
@@ -142,13 +156,17 @@ int mp_factor(int alg, int prec, float *W, int n, int nb, cudaStream_t s, palial
     const int mode = prec == PALIAL_PREC_FP8 ? 1 : prec == PALIAL_PREC_BF16X3 ? 2 : 0;
     const size_t elem = (mode == 1) ? 1 : 2;
     const size_t panel = (size_t)std::max(1, mt - 1) * nb * nb * elem;
-    PALIAL_CK(mb.pa_hi.ensure(2 * panel), "alloc panel");
+    const bool arrive = g_arrival.on && alg == 0 && mt > 2;
+    g_arrival.on = false;
+    // packed panels: two alternating slots, or one per step when row groups arrive late
+    const int slots = arrive ? mt - 1 : 2;
+    PALIAL_CK(mb.pa_hi.ensure(slots * panel), "alloc panel");
     PALIAL_CK(mb.pb_hi.ensure(2 * panel), "alloc panel");
     if (mode == 2) {
-        PALIAL_CK(mb.pa_lo.ensure(2 * panel), "alloc panel");
+        PALIAL_CK(mb.pa_lo.ensure(slots * panel), "alloc panel");
         PALIAL_CK(mb.pb_lo.ensure(2 * panel), "alloc panel");
     }
-    PALIAL_CK(mb.scales.ensure(sizeof(float) * 4 * (size_t)std::max(1, mt)), "alloc scales");
+    PALIAL_CK(mb.scales.ensure(sizeof(float) * (size_t)std::max(4, slots * 2) * (size_t)std::max(1, mt)), "alloc scales");
     PALIAL_CK(mb.binv.ensure(sizeof(float) * 2 * (size_t)nb * 64), "alloc block inverses");
     PALIAL_CK(g.diag.status.ensure(sizeof(int) * ST_NSLOTS + 64), "alloc status");
     PALIAL_CK(lookahead_init(), "lookahead streams");
@@ -159,15 +177,21 @@ int mp_factor(int alg, int prec, float *W, int n, int nb, cudaStream_t s, palial
     PALIAL_CK(cudaStreamWaitEvent(lo, g_la.start, 0), "event");
     int *status = g.diag.status.as<int>();
     auto buf = [&](const DevBuf &b, int par) { return static_cast<void *>(static_cast<uint8_t *>(b.ptr) + par * panel); };
+    if (arrive) {
+        PALIAL_CK(cudaStreamWaitEvent(hi, g_arrival.ready[0], 0), "rows");
+        PALIAL_CK(cudaStreamWaitEvent(lo, g_arrival.ready[0], 0), "rows");
+    }
+    int present = arrive ? g_arrival.ge[0] : mt;  // tile rows the trailing updates cover
+    int next_group = 1;
     bool have_rest = false;
     for (int k = 0; k < mt; k++) {
         // the diagonal tile in FP32, one CTA (mp_diag.cu)
         PALIAL_CK(mpd_factor_tile(alg, W, n, nb, k, status, mb.binv.as<float>(), hi), "diag factor");
         if (k == mt - 1) break;
-        const int par = k & 1;
+        const int par = arrive ? k : (k & 1);
         float *sa = mb.scales.as<float>() + 2 * mt * par, *sb = sa + mt;
         void *ah = buf(mb.pa_hi, par), *al = mode == 2 ? buf(mb.pa_lo, par) : nullptr;
-        void *bh = buf(mb.pb_hi, par), *bl = mode == 2 ? buf(mb.pb_lo, par) : nullptr;
+        void *bh = buf(mb.pb_hi, k & 1), *bl = mode == 2 ? buf(mb.pb_lo, k & 1) : nullptr;
         float *binv = mb.binv.as<float>();
         PALIAL_CK(mps_block_inverse(W, n, nb, k, alg == 0 ? 1 : 2, binv, hi), "diagonal block inverses");
         if (alg == 0) {
@@ -186,7 +210,29 @@ int mp_factor(int alg, int prec, float *W, int n, int nb, cudaStream_t s, palial
         if (have_rest) PALIAL_CK(cudaStreamWaitEvent(hi, g_la.rest, 0), "event");
         PALIAL_CK(mp_update(mode, alg == 0 ? 1 : 0, W, n, nb, k, ah, al, bh, bl, sa, sb, status, hi, 1), "update (next)");
         PALIAL_CK(cudaStreamWaitEvent(lo, g_la.packed, 0), "event");
-        PALIAL_CK(mp_update(mode, alg == 0 ? 1 : 0, W, n, nb, k, ah, al, bh, bl, sa, sb, status, lo, 2), "update (rest)");
+        if (!arrive) {
+            PALIAL_CK(mp_update(mode, alg == 0 ? 1 : 0, W, n, nb, k, ah, al, bh, bl, sa, sb, status, lo, 2),
+                      "update (rest)");
+        } else {
+            // row groups due at this step: their skipped steps 0..k-1, in order, then the rest
+            // update of step k over every present row
+            while (next_group < g_arrival.ngroups && g_arrival.kg[next_group] <= k) {
+                const int g0 = g_arrival.gs[next_group], g1 = g_arrival.ge[next_group];
+                PALIAL_CK(cudaStreamWaitEvent(lo, g_arrival.ready[next_group], 0), "rows");
+                for (int sk = 0; sk < k; sk++) {
+                    float *ss = mb.scales.as<float>() + 2 * mt * sk;
+                    void *sh = buf(mb.pa_hi, sk), *sl = mode == 2 ? buf(mb.pa_lo, sk) : nullptr;
+                    PALIAL_CK(mp_update(mode, 1, W, n, nb, sk, sh, sl, sh, sl, ss, ss, status, lo, 3, g0 - sk - 1,
+                                        g1 - sk - 1),
+                              "update (arrived rows)");
+                }
+                present = g1;
+                next_group++;
+            }
+            if (present - k - 1 > 1)
+                PALIAL_CK(mp_update(mode, 1, W, n, nb, k, ah, al, bh, bl, sa, sb, status, lo, 3, 1, present - k - 1),
+                          "update (rest)");
+        }
         PALIAL_CK(cudaEventRecord(g_la.rest, lo), "event");
         have_rest = true;
     }
@@ -544,7 +590,10 @@ static int solve_one(int alg, const double *dA, int n, int nb, const double *dB,
         }
         PALIAL_CK(mps_f64_to_f32(g.mat.as<double>(), W, n, nb, 0.0, s, nullptr, alg == 0), "factor to f32");
     } else {
-        PALIAL_CK(cudaMemsetAsync(nrm + 120, 0, sizeof(double), s), "max |a|");
+        // host-buffer Cholesky with row-group arrival: the copy pipeline converts the upper
+        // triangle group by group (and accumulates max |a_ij|) while the factorization runs
+        const bool arrived_conv = g_arrival.on && alg == 0;
+        if (!arrived_conv) PALIAL_CK(cudaMemsetAsync(nrm + 120, 0, sizeof(double), s), "max |a|");
         // opts.reserved[6] = 1: LU of the random-butterfly transform U^T A V (rbt.cu)
         const bool rbt = alg == 1 && o.reserved[6] == 1;
         g_rctx.rbt = rbt;
@@ -552,7 +601,7 @@ static int solve_one(int alg, const double *dA, int n, int nb, const double *dB,
         for (int attempt = 0; attempt < 4; attempt++) {
             if (rbt)
                 PALIAL_CK(rbt_transform_matrix(dA, W, n, nb, attempt == 0 ? nrm + 120 : nullptr, s), "butterfly transform");
-            else
+            else if (!(arrived_conv && attempt == 0))
                 PALIAL_CK(mps_f64_to_f32(dA, W, n, nb, shift, s, attempt == 0 ? nrm + 120 : nullptr, alg == 0),
                           "convert");
             rc = mp_factor(alg, prec, W, n, nb, s, st, &zp);
@@ -878,10 +927,64 @@ extern "C" int palial_gpu_solve_ir_host(int alg, const palial_desc *A, const dou
     const size_t te = (size_t)nb * nb;
     double *dA = g.smat.as<double>();
     const double *hA = static_cast<const double *>(A->matrix);
-    if (alg == 0 && mt > 1 && n % nb == 0) {
-        // Cholesky reads only the upper triangle: tile column j's tiles 0..j are contiguous and
-        // go first; the factorization starts when they are in while the lower triangle follows
-        // on the copy stream (the host link is the bottleneck, so the two phases never share it)
+    palial_opts oo;
+    palial_opts_default(&oo);
+    if (opts) oo = *opts;
+    const bool mixed = oo.precision != PALIAL_PREC_FP64;
+    if (alg == 0 && mt > 2 && n % nb == 0 && nb % 256 == 0 && mixed && oo.reserved[4] != 1) {
+        // Cholesky reads only the upper triangle.  Mixed precision: it arrives in groups of tile
+        // rows (row r's tiles (r, j >= r): one strided copy), each converted to the FP32 working
+        // copy on the copy stream, and the factorization starts on the first group (RowArrival);
+        // the lower triangle (for the residuals) follows.  The host link is the bottleneck, so
+        // the copies run back to back on one stream.
+        if (!g_sc.copy) {
+            PALIAL_CK(cudaStreamCreateWithFlags(&g_sc.copy, cudaStreamNonBlocking), "copy stream");
+            PALIAL_CK(cudaEventCreateWithFlags(&g_sc.upper, cudaEventDisableTiming), "copy event");
+            PALIAL_CK(cudaEventCreateWithFlags(&g_sc.full, cudaEventDisableTiming), "copy event");
+        }
+        PALIAL_CK(mb.w.ensure(sizeof(float) * (size_t)n * n), "alloc W");
+        PALIAL_CK(mb.norms.ensure(sizeof(double) * 256), "alloc norms");
+        double *amax = mb.norms.as<double>() + 120;
+        PALIAL_CK(cudaMemsetAsync(amax, 0, sizeof(double), g_sc.copy), "max |a|");
+        // groups: rows {0,1}, single rows 2..7, then 2, 2, 4, 4, 8, 8, ... rows (a row must be
+        // present two steps before the front reaches it); group g counts as present
+        // from the step the front is expected to reach after its copy (host link ~200 GB/s,
+        // about 1.1 ms per step at NB = 512, scaled by (NB/512)^2), at most gs - 2
+        RowArrival &ar = g_arrival;
+        ar.ngroups = 0;
+        double bytes = 0.0;
+        const double step_s = 1.1e-3 * (double)nb * nb / (512.0 * 512.0) * std::max(1.0, (double)mt / 64.0);
+        for (int r = 0; r < mt && ar.ngroups < 64;) {
+            const int g = ar.ngroups;
+            const int size = g == 0 ? 2 : r < 8 ? 1 : 2 << ((g - 7) / 2);
+            const int r1 = std::min(mt, g == 63 ? mt : r + size);
+            if (!ar.ready[g]) PALIAL_CK(cudaEventCreateWithFlags(&ar.ready[g], cudaEventDisableTiming), "copy event");
+            for (int rr = r; rr < r1; rr++)
+                PALIAL_CK(cudaMemcpy2DAsync(dA + te * ((size_t)rr + (size_t)mt * rr), sizeof(double) * te * mt,
+                                            hA + te * ((size_t)rr + (size_t)mt * rr), sizeof(double) * te * mt,
+                                            sizeof(double) * te, (size_t)(mt - rr), cudaMemcpyHostToDevice, g_sc.copy),
+                          "copy A (row)");
+            PALIAL_CK(mps_f64_to_f32(dA, mb.w.as<float>(), n, nb, 0.0, g_sc.copy, amax, true, r, r1), "convert rows");
+            PALIAL_CK(cudaEventRecord(ar.ready[g], g_sc.copy), "copy event");
+            for (int rr = r; rr < r1; rr++) bytes += 8.0 * (double)te * (double)(mt - rr);
+            ar.gs[g] = r;
+            ar.ge[g] = r1;
+            const int due = (int)std::ceil(bytes / 200e9 / step_s);
+            ar.kg[g] = g == 0 ? 0 : std::max(ar.kg[g - 1], std::min(r - 2, due));
+            ar.ngroups++;
+            r = r1;
+        }
+        ar.on = true;
+        PALIAL_CK(cudaEventRecord(g_sc.upper, g_sc.copy), "copy A");
+        for (int j = 0; j + 1 < mt; j++)
+            PALIAL_CK(cudaMemcpyAsync(dA + te * (mt * j + j + 1), hA + te * (mt * j + j + 1),
+                                      sizeof(double) * te * (mt - 1 - j), cudaMemcpyHostToDevice, g_sc.copy),
+                      "copy A (lower)");
+        PALIAL_CK(cudaEventRecord(g_sc.full, g_sc.copy), "copy A");
+        g_full_ready = g_sc.full;
+    } else if (alg == 0 && mt > 1 && n % nb == 0) {
+        // FP64 Cholesky: the upper triangle (tile column j's tiles 0..j are contiguous) first,
+        // the rest on the copy stream behind it
         if (!g_sc.copy) {
             PALIAL_CK(cudaStreamCreateWithFlags(&g_sc.copy, cudaStreamNonBlocking), "copy stream");
             PALIAL_CK(cudaEventCreateWithFlags(&g_sc.upper, cudaEventDisableTiming), "copy event");
@@ -903,6 +1006,7 @@ extern "C" int palial_gpu_solve_ir_host(int alg, const palial_desc *A, const dou
         PALIAL_CK(cudaMemcpyAsync(dA, hA, bytes, cudaMemcpyHostToDevice, nullptr), "copy A");
     }
     rc = palial_gpu_solve_ir(alg, dA, n, nb, dB, dX, nrhs, opts, st, nullptr);
+    g_arrival.on = false;
     g_full_ready = nullptr;
     if (g_sc.full) PALIAL_CK(cudaStreamWaitEvent(nullptr, g_sc.full, 0), "copy A");  // error paths too
     PALIAL_CK(cudaMemcpy(X, dX, vb, cudaMemcpyDeviceToHost), "copy X");

@@ -65,7 +65,9 @@ struct UpdateParams {
     int ntr;                  // trailing tiles per dimension
     int upper;                // 1: only tile pairs (ti <= tj) (Cholesky), 0: all (LU)
     int part;                 // 0: every pair; 1: the next step's tiles (row 0; LU also column
-                              // 0); 2: all other pairs (lookahead split)
+                              // 0); 2: all other pairs (lookahead split); 3 (upper only): the
+                              // pairs of trailing rows r0 <= ti < r1, row by row
+    int r0, r1;               // part 3 row range (trailing-relative)
     const float *scale_a;     // FP8: per trailing tile scale of A_op rows (nullptr: 1)
     const float *scale_b;     // FP8: per trailing tile scale of B_op rows
     int *status;              // error word (ST_CODE slot)
@@ -152,7 +154,16 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float *v) {
 
 __device__ __forceinline__ void decode_pair(int q, int ntr, int upper, int &ti, int &tj);
 // Pair q of the launch's part (see UpdateParams::part).
-__device__ __forceinline__ void decode_part(int q, int ntr, int upper, int part, int &ti, int &tj) {
+__device__ __forceinline__ void decode_part(int q, int ntr, int upper, int part, int &ti, int &tj, int r0) {
+    if (part == 3) {  // row ti holds ntr - ti pairs (tj >= ti)
+        ti = r0;
+        while (q >= ntr - ti) {
+            q -= ntr - ti;
+            ti++;
+        }
+        tj = ti + q;
+        return;
+    }
     if (part == 1) {
         if (upper || q < ntr) {
             ti = 0;
@@ -202,7 +213,7 @@ __global__ void __launch_bounds__(NTHR, 1)
     const int sub_m = p.nb / BM, sub_n = p.nb / BN;
     const int q = blockIdx.x / (sub_m * sub_n), sub = blockIdx.x % (sub_m * sub_n);
     int ti, tj;
-    decode_part(q, p.ntr, p.upper, p.part, ti, tj);
+    decode_part(q, p.ntr, p.upper, p.part, ti, tj, p.r0);
     const int mi = sub % sub_m, nj = sub / sub_m;
     const int arow = ti * p.nb + mi * BM;   // first row of A_op
     const int brow = tj * p.nb + nj * BN;   // first row of B_op
@@ -470,9 +481,14 @@ cudaError_t launch_mode(const void *a_hi, const void *a_lo, const void *b_hi, co
         tbl = tb;
     }
     const long long nt = p.ntr, ns = nt - 1;
-    const long long pairs = p.part == 1 ? (p.upper ? nt : 2 * nt - 1)
-                            : p.part == 2 ? (p.upper ? ns * (ns + 1) / 2 : ns * ns)
-                                          : (p.upper ? nt * (nt + 1) / 2 : nt * nt);
+    long long pairs = p.part == 1 ? (p.upper ? nt : 2 * nt - 1)
+                      : p.part == 2 ? (p.upper ? ns * (ns + 1) / 2 : ns * ns)
+                                    : (p.upper ? nt * (nt + 1) / 2 : nt * nt);
+    if (p.part == 3) {
+        if (!p.upper || p.r0 < 0 || p.r1 > p.ntr) return cudaErrorInvalidValue;
+        pairs = 0;
+        for (int r = p.r0; r < p.r1; r++) pairs += nt - r;
+    }
     const long long blocks = pairs * (p.nb / mp::BM) * (p.nb / mp::BN);
     if (blocks <= 0) return cudaSuccess;
     if (blocks > 0x7fffffffLL) return cudaErrorInvalidValue;
@@ -486,7 +502,7 @@ cudaError_t launch_mode(const void *a_hi, const void *a_lo, const void *b_hi, co
 // trailing tile (fp8).  C: FP32 tile-layout matrix.
 cudaError_t mp_update(int mode, int upper, float *C, int n, int nb, int k, const void *a_hi, const void *a_lo,
                       const void *b_hi, const void *b_lo, const float *scale_a, const float *scale_b, int *status,
-                      cudaStream_t s, int part) {
+                      cudaStream_t s, int part, int r0, int r1) {
     if (nb % 256 || n % nb) return cudaErrorInvalidValue;
     mp::UpdateParams p{};
     p.C = C;
@@ -499,6 +515,8 @@ cudaError_t mp_update(int mode, int upper, float *C, int n, int nb, int k, const
     p.scale_b = scale_b;
     p.status = status;
     p.part = part;
+    p.r0 = r0;
+    p.r1 = r1;
     if (p.ntr <= 0) return cudaSuccess;
     if (mode == mp::MODE_BF16) return launch_mode<mp::MODE_BF16>(a_hi, nullptr, b_hi, nullptr, p, s);
     if (mode == mp::MODE_FP8) return launch_mode<mp::MODE_FP8>(a_hi, nullptr, b_hi, nullptr, p, s);

@@ -27,7 +27,7 @@ __device__ __forceinline__ size_t tile_off(int n, int nb, int tm, int tn) {
 // reads only the upper triangle, which a caller may have copied in first).
 constexpr int kConvChunk = 8192;
 __global__ void f64_to_f32_kernel(const double *__restrict__ a, float *__restrict__ w, int n, int nb,
-                                  double shift_diag, int upper_only, double *amax) {
+                                  double shift_diag, int upper_only, int r0, int r1, double *amax) {
     const int mt = n / nb;
     const int te = nb * nb;
     const int chunks = (te + kConvChunk - 1) / kConvChunk;
@@ -38,7 +38,7 @@ __global__ void f64_to_f32_kernel(const double *__restrict__ a, float *__restric
     for (long long it = blockIdx.x; it < items; it += gridDim.x) {
         const int t = (int)(it / chunks), ch = (int)(it - (long long)t * chunks);
         const int tr = t % mt, tc = t / mt;
-        if (upper_only && tr > tc) continue;  // uniform per CTA
+        if ((upper_only && tr > tc) || tr < r0 || tr >= r1) continue;  // uniform per CTA
         const size_t base = (size_t)t * te;
         const int end = min(te, (ch + 1) * kConvChunk);
         const bool diag = shift_diag != 0.0 && tr == tc;
@@ -803,12 +803,13 @@ cudaError_t mps_configure() {
     return cudaFuncSetAttribute(mps::half_update_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, mps::SMEM_BYTES);
 }
 
+// (tile rows [r0, r1) only; r1 < 0: all)
 cudaError_t mps_f64_to_f32(const double *A, float *W, int n, int nb, double shift, cudaStream_t s, double *amax,
-                           bool upper_only) {
+                           bool upper_only, int r0, int r1) {
     const long long items = (long long)(n / nb) * (n / nb) * ((nb * nb + mps::kConvChunk - 1) / mps::kConvChunk);
     note_launch();
     mps::f64_to_f32_kernel<<<(int)std::min<long long>(items, 2048), 256, 0, s>>>(
-        A, W, n, nb, shift, upper_only ? 1 : 0, amax);
+        A, W, n, nb, shift, upper_only ? 1 : 0, r0, r1 < 0 ? n / nb : r1, amax);
     return cudaGetLastError();
 }
 // R = B - A X in compensated FP32 (see residual_df_kernel); sigma: |a_ij| < 2^sigma for all
