@@ -128,15 +128,18 @@ static cudaError_t wait_full_matrix(cudaStream_t s) {
 
 // Row-group arrival (host-buffer mixed Cholesky): the upper triangle arrives in groups of tile
 // rows [gs[g], ge[g]) (FP32 working copy converted per group, event ready[g]); group 0 holds
-// rows 0 and 1.  The factorization starts on group 0 and treats group g as present from step
-// kg[g] <= gs[g] - 2 on: until then the trailing updates skip its rows; at step kg[g] (before
-// that step's rest update, on the same stream) the skipped steps 0..kg[g]-1 are applied to it
-// in step order, from packed panels kept for every step, so each tile receives the same updates
-// in the same order as without deferral.  One-shot: mp_factor clears `on`.
+// rows 0 and 1.  The factorization starts on group 0; the rest updates skip groups that have
+// not joined.  From the step its data is due, a group catches up on the rest-update stream
+// (the skipped steps in order, from packed panels kept for every step) within each step's
+// estimated slack (the critical chain's time minus that step's rest update), and joins once
+// caught up; at step kg[g] = gs[g] - 2 it must join (the rest update of that step covers its
+// first row), so whatever is left is applied then.  Every tile receives the same updates in the
+// same order as without deferral (bit-identical factors).  One-shot: mp_factor clears `on`.
 struct RowArrival {
     bool on = false;
     int ngroups = 0;
     int gs[64], ge[64], kg[64];
+    int due[64];  // step by which the group's data is expected (host link rate)
     cudaEvent_t ready[64] = {};
 } g_arrival;
 
@@ -183,6 +186,12 @@ int mp_factor(int alg, int prec, float *W, int n, int nb, cudaStream_t s, palial
     }
     int present = arrive ? g_arrival.ge[0] : mt;  // tile rows the trailing updates cover
     int next_group = 1;
+    int applied[64] = {};  // per group: steps 0..applied-1 applied
+    bool waited[64] = {};
+    // the critical chain's time per step in tile-pair updates of the trailing update (about
+    // 0.8 ms per step, a BF16x3 pair update about 0.8 us at NB = 512, BF16 / FP8 a third; a
+    // pair costs NB^3, the chain about NB^2)
+    const long long chain_pairs = (mode == 2 ? 1000 : 3000) * 512 / nb;
     bool have_rest = false;
     for (int k = 0; k < mt; k++) {
         // the diagonal tile in FP32, one CTA (mp_diag.cu)
@@ -214,24 +223,54 @@ int mp_factor(int alg, int prec, float *W, int n, int nb, cudaStream_t s, palial
             PALIAL_CK(mp_update(mode, alg == 0 ? 1 : 0, W, n, nb, k, ah, al, bh, bl, sa, sb, status, lo, 2),
                       "update (rest)");
         } else {
-            // row groups due at this step: their skipped steps 0..k-1, in order, then the rest
-            // update of step k over every present row
-            while (next_group < g_arrival.ngroups && g_arrival.kg[next_group] <= k) {
-                const int g0 = g_arrival.gs[next_group], g1 = g_arrival.ge[next_group];
-                PALIAL_CK(cudaStreamWaitEvent(lo, g_arrival.ready[next_group], 0), "rows");
-                for (int sk = 0; sk < k; sk++) {
-                    float *ss = mb.scales.as<float>() + 2 * mt * sk;
-                    void *sh = buf(mb.pa_hi, sk), *sl = mode == 2 ? buf(mb.pa_lo, sk) : nullptr;
-                    PALIAL_CK(mp_update(mode, 1, W, n, nb, sk, sh, sl, sh, sl, ss, ss, status, lo, 3, g0 - sk - 1,
-                                        g1 - sk - 1),
-                              "update (arrived rows)");
+            RowArrival &ar = g_arrival;
+            // step sk's update of group gi's rows (on lo, in step order)
+            const auto apply = [&](int gi, int sk) -> int {
+                if (!waited[gi]) {
+                    PALIAL_CK(cudaStreamWaitEvent(lo, ar.ready[gi], 0), "rows");
+                    waited[gi] = true;
                 }
-                present = g1;
+                float *ss = mb.scales.as<float>() + 2 * mt * sk;
+                void *sh = buf(mb.pa_hi, sk), *sl = mode == 2 ? buf(mb.pa_lo, sk) : nullptr;
+                PALIAL_CK(mp_update(mode, 1, W, n, nb, sk, sh, sl, sh, sl, ss, ss, status, lo, 3, ar.gs[gi] - sk - 1,
+                                    ar.ge[gi] - sk - 1),
+                          "update (arrived rows)");
+                applied[gi] = sk + 1;
+                return PALIAL_OK;
+            };
+            const auto pairs_of = [&](int r0, int r1) {  // tile pairs (r, j >= r) of rows [r0, r1)
+                long long c = 0;
+                for (int r = r0; r < r1; r++) c += mt - r;
+                return c;
+            };
+            // a group whose data is due and that is caught up through step k-1 joins; a group at
+            // its deadline gets the rest of its skipped steps first
+            while (next_group < ar.ngroups &&
+                   ((ar.due[next_group] <= k && applied[next_group] >= k) || ar.kg[next_group] <= k)) {
+                for (int sk = applied[next_group]; sk < k; sk++) {
+                    const int rc2 = apply(next_group, sk);
+                    if (rc2) return rc2;
+                }
+                if (!waited[next_group]) {
+                    PALIAL_CK(cudaStreamWaitEvent(lo, ar.ready[next_group], 0), "rows");
+                    waited[next_group] = true;
+                }
+                present = ar.ge[next_group];
                 next_group++;
             }
             if (present - k - 1 > 1)
                 PALIAL_CK(mp_update(mode, 1, W, n, nb, k, ah, al, bh, bl, sa, sb, status, lo, 3, 1, present - k - 1),
                           "update (rest)");
+            // catch-up of the next groups within this step's slack (in tile-pair updates)
+            long long budget = std::max(chain_pairs / 5, chain_pairs - pairs_of(k + 2, present));
+            for (int gi = next_group; gi < ar.ngroups && budget > 0 && ar.due[gi] <= k; gi++) {
+                const long long cost = pairs_of(ar.gs[gi], ar.ge[gi]);
+                while (budget > 0 && applied[gi] <= k) {
+                    const int rc2 = apply(gi, applied[gi]);
+                    if (rc2) return rc2;
+                    budget -= cost;
+                }
+            }
         }
         PALIAL_CK(cudaEventRecord(g_la.rest, lo), "event");
         have_rest = true;
@@ -947,9 +986,9 @@ extern "C" int palial_gpu_solve_ir_host(int alg, const palial_desc *A, const dou
         double *amax = mb.norms.as<double>() + 120;
         PALIAL_CK(cudaMemsetAsync(amax, 0, sizeof(double), g_sc.copy), "max |a|");
         // groups: rows {0,1}, single rows 2..7, then 2, 2, 4, 4, 8, 8, ... rows (a row must be
-        // present two steps before the front reaches it); group g counts as present
-        // from the step the front is expected to reach after its copy (host link ~200 GB/s,
-        // about 1.1 ms per step at NB = 512, scaled by (NB/512)^2), at most gs - 2
+        // present two steps before the front reaches it); group g's data is expected by the step
+        // the front reaches after its copy (host link ~200 GB/s, about 1.1 ms per step at
+        // NB = 512, scaled by (NB/512)^2), and it must join by step gs - 2
         RowArrival &ar = g_arrival;
         ar.ngroups = 0;
         double bytes = 0.0;
@@ -969,8 +1008,8 @@ extern "C" int palial_gpu_solve_ir_host(int alg, const palial_desc *A, const dou
             for (int rr = r; rr < r1; rr++) bytes += 8.0 * (double)te * (double)(mt - rr);
             ar.gs[g] = r;
             ar.ge[g] = r1;
-            const int due = (int)std::ceil(bytes / 200e9 / step_s);
-            ar.kg[g] = g == 0 ? 0 : std::max(ar.kg[g - 1], std::min(r - 2, due));
+            ar.due[g] = (int)std::ceil(bytes / 200e9 / step_s);
+            ar.kg[g] = g == 0 ? 0 : std::max(0, r - 2);
             ar.ngroups++;
             r = r1;
         }
