@@ -474,30 +474,34 @@ cudaError_t mpd_configure() {
 
 cudaError_t mps_block_inverse(const float *W, int n, int nb, int k, int factors, float *binv, cudaStream_t s,
                               int blocks);
-cudaError_t mps_half_panel(float *T, int h, int ld, const float *binv, cudaStream_t s);
-cudaError_t mps_half_update(float *T, int h, int ld, cudaStream_t s);
+cudaError_t mps_half_panel(float *T, int h, int ld, const float *binv, int alg, cudaStream_t s);
+cudaError_t mps_half_update(float *T, int h, int ld, int alg, cudaStream_t s);
 
-// Factor diagonal tile k of the FP32 tile matrix W (n x n, tile nb) in place.  Cholesky tiles of
-// NB >= 512 go two-level: A11 (h = NB/2) in one CTA, A12 <- U11^-T A12 and the upper part of
-// A22 -= A12^T A12 on many CTAs, then A22 in one CTA (the one-CTA kernel's time grows about
-// 3.5x per doubling of the size, the multi-CTA steps are short).  binv: scratch for the
-// inverses of U11's 64 x 64 diagonal blocks (nb x 64 floats).
+// Factor diagonal tile k of the FP32 tile matrix W (n x n, tile nb) in place.  Tiles of
+// NB >= 512 go two-level: A11 (h = NB/2) in one CTA; on many CTAs the off-diagonal blocks
+// (Cholesky A12 <- U11^-T A12; LU U12 <- L11^-1 A12 and L21 <- A21 U11^-1) and the update of
+// A22 (Cholesky its upper part -= A12^T A12, LU -= L21 U12); then A22 in one CTA (the one-CTA
+// kernel's time grows about 3.5x per doubling of the size, the multi-CTA steps are short).
+// binv: scratch for the inverses of A11's 64 x 64 diagonal factor blocks (2 nb x 64 floats).
 cudaError_t mpd_factor_tile(int alg, float *W, int n, int nb, int k, int *status, float *binv, cudaStream_t s) {
     if (nb % 64 || nb > 1024) return cudaErrorInvalidValue;
     const int mt = n / nb;
     float *T = W + (size_t)nb * nb * ((size_t)k + (size_t)mt * k);
-    if (alg == 0 && nb >= 512 && nb % 128 == 0 && binv) {
+    if (nb >= 512 && nb % 128 == 0 && binv) {
         const int h = nb / 2;
         const int bytes = mpd::smem_floats(h) * 4;
+        cudaError_t e;
         note_launch();
-        mpd::diag_factor_kernel<0><<<1, mpd::NT, bytes, s>>>(T, h, nb, k, 0, status);
-        cudaError_t e = cudaGetLastError();
-        if (e == cudaSuccess) e = mps_block_inverse(W, n, nb, k, 1, binv, s, h / 64);
-        if (e == cudaSuccess) e = mps_half_panel(T, h, nb, binv, s);
-        if (e == cudaSuccess) e = mps_half_update(T, h, nb, s);
+        if (alg == 0) mpd::diag_factor_kernel<0><<<1, mpd::NT, bytes, s>>>(T, h, nb, k, 0, status);
+        else mpd::diag_factor_kernel<1><<<1, mpd::NT, bytes, s>>>(T, h, nb, k, 0, status);
+        e = cudaGetLastError();
+        if (e == cudaSuccess) e = mps_block_inverse(W, n, nb, k, alg == 0 ? 1 : 2, binv, s, h / 64);
+        if (e == cudaSuccess) e = mps_half_panel(T, h, nb, binv, alg, s);
+        if (e == cudaSuccess) e = mps_half_update(T, h, nb, alg, s);
         if (e != cudaSuccess) return e;
         note_launch();
-        mpd::diag_factor_kernel<0><<<1, mpd::NT, bytes, s>>>(T + (size_t)h * (nb + 1), h, nb, k, h, status);
+        if (alg == 0) mpd::diag_factor_kernel<0><<<1, mpd::NT, bytes, s>>>(T + (size_t)h * (nb + 1), h, nb, k, h, status);
+        else mpd::diag_factor_kernel<1><<<1, mpd::NT, bytes, s>>>(T + (size_t)h * (nb + 1), h, nb, k, h, status);
         return cudaGetLastError();
     }
     const int bytes = mpd::smem_floats(nb) * 4;

@@ -42,6 +42,7 @@ __global__ void f64_to_f32_kernel(const double *__restrict__ a, float *__restric
         const size_t base = (size_t)t * te;
         const int end = min(te, (ch + 1) * kConvChunk);
         const bool diag = shift_diag != 0.0 && tr == tc;
+#pragma unroll 4
         for (int i = ch * kConvChunk + 2 * threadIdx.x; i < end; i += 2 * blockDim.x) {
             double2 v = *reinterpret_cast<const double2 *>(a + base + i);  // te even: 16-byte aligned
             const unsigned long long b0 = (unsigned long long)__double_as_longlong(v.x) & 0x7FFFFFFFFFFFFFFFull;
@@ -480,20 +481,33 @@ __global__ void __launch_bounds__(NT, 2) panel_trsm_kernel(float *W, int n, int 
     else strip_run(m, T, nb, W + tile_off(n, nb, t, k) + s * 64, nb, nb, binv);
 }
 
-// ---- two-level Cholesky of a diagonal tile (NB >= 512) ---------------------------------------
+// ---- two-level factorization of a diagonal tile (NB >= 512) ---------------------------------
 // The tile is factored as 2 x 2 blocks of h = NB/2: one-CTA factorization of A11, then these
 // two multi-CTA steps, then one-CTA factorization of A22 (mp_diag.cu).
-// A12 (h x h at T + h ld) <- U11^-T A12, U11 the factored leading block (binv: inverses of its
-// 64 x 64 diagonal blocks); one CTA per 64-column strip.
-__global__ void __launch_bounds__(NT, 2) half_panel_kernel(float *T, int h, int ld, const float *binv) {
+// Cholesky (alg 0): A12 (h x h at T + h ld) <- U11^-T A12, one CTA per 64-column strip.
+// LU (alg 1): blockIdx.y = 0: U12 <- L11^-1 A12 (64-column strips), 1: L21 <- A21 U11^-1
+// (64-row strips).  binv: inverses of the 64 x 64 diagonal blocks of U11 (and, for LU, of
+// L11 at binv + (ld / 64) * 4096).
+__global__ void __launch_bounds__(NT, 2) half_panel_kernel(float *T, int h, int ld, const float *binv, int alg) {
     extern __shared__ __align__(16) float smem[];
     const Smem m = smem_parts(smem);
-    strip_lut(m, T, ld, T + (size_t)h * ld + (size_t)blockIdx.x * 64 * ld, ld, h, binv);
+    if (alg == 0) strip_lut(m, T, ld, T + (size_t)h * ld + (size_t)blockIdx.x * 64 * ld, ld, h, binv);
+    else if (blockIdx.y == 0)
+        strip_llu_inv(m, T, ld, T + (size_t)h * ld + (size_t)blockIdx.x * 64 * ld, ld, h, binv + (size_t)(ld / 64) * 4096);
+    else strip_run(m, T, ld, T + h + (size_t)blockIdx.x * 64, ld, h, binv);
 }
-// A22 -= A12^T A12 on the 64 x 64 blocks (bi, bj), bi <= bj, of the trailing h x h block (one
-// CTA each); inside diagonal blocks the strictly lower entries stay unchanged.
-__global__ void __launch_bounds__(NT, 2) half_update_kernel(float *T, int h, int ld) {
+// Cholesky: A22 -= A12^T A12 on the 64 x 64 blocks (bi, bj), bi <= bj, of the trailing h x h
+// block (one CTA each; inside diagonal blocks the strictly lower entries stay unchanged).
+// LU: A22 -= L21 U12 on every 64 x 64 block.
+__global__ void __launch_bounds__(NT, 2) half_update_kernel(float *T, int h, int ld, int alg) {
     extern __shared__ __align__(16) float smem[];
+    const Smem m = smem_parts(smem);
+    if (alg == 1) {
+        const int nbl = h / 64, bi = blockIdx.x % nbl, bj = blockIdx.x / nbl;
+        cta_gemm<false, false>(64, 64, h, -1.f, T + h + (size_t)bi * 64, ld, T + (size_t)(h + bj * 64) * ld, ld,
+                               T + (size_t)(h + bi * 64) + (size_t)(h + bj * 64) * ld, ld, m.g);
+        return;
+    }
     int q = blockIdx.x, bj = 0;
     while (q > bj) {
         q -= bj + 1;
@@ -502,7 +516,6 @@ __global__ void __launch_bounds__(NT, 2) half_update_kernel(float *T, int h, int
     const int bi = q;
     const float *A12 = T + (size_t)h * ld;
     float *C = T + (size_t)(h + bi * 64) + (size_t)(h + bj * 64) * ld;
-    const Smem m = smem_parts(smem);
     if (bi == bj)
         cta_gemm<true, false, true>(64, 64, h, -1.f, A12 + (size_t)bi * 64 * ld, ld, A12 + (size_t)bj * 64 * ld, ld, C,
                                     ld, m.g);
@@ -873,15 +886,16 @@ cudaError_t mps_block_inverse(const float *W, int n, int nb, int k, int factors,
     mps::block_inverse_kernel<<<dim3(blocks > 0 ? blocks : nb / 64, factors), 256, 0, s>>>(W, n, nb, k, binv);
     return cudaGetLastError();
 }
-cudaError_t mps_half_panel(float *T, int h, int ld, const float *binv, cudaStream_t s) {
+cudaError_t mps_half_panel(float *T, int h, int ld, const float *binv, int alg, cudaStream_t s) {
     note_launch();
-    mps::half_panel_kernel<<<h / 64, mps::NT, mps::SMEM_BYTES, s>>>(T, h, ld, binv);
+    mps::half_panel_kernel<<<dim3(h / 64, alg == 0 ? 1 : 2), mps::NT, mps::SMEM_BYTES, s>>>(T, h, ld, binv, alg);
     return cudaGetLastError();
 }
-cudaError_t mps_half_update(float *T, int h, int ld, cudaStream_t s) {
+cudaError_t mps_half_update(float *T, int h, int ld, int alg, cudaStream_t s) {
     const int nbl = h / 64;
     note_launch();
-    mps::half_update_kernel<<<nbl * (nbl + 1) / 2, mps::NT, mps::SMEM_BYTES, s>>>(T, h, ld);
+    mps::half_update_kernel<<<alg == 0 ? nbl * (nbl + 1) / 2 : nbl * nbl, mps::NT, mps::SMEM_BYTES, s>>>(T, h, ld,
+                                                                                                        alg);
     return cudaGetLastError();
 }
 cudaError_t mps_panel_trsm(float *W, int n, int nb, int k, int kind, const float *binv, cudaStream_t s) {
