@@ -51,8 +51,6 @@ cudaError_t mps_residual(const double *A, int n, int nb, const double *X, const 
 cudaError_t mps_norm_inf_matrix(const double *A, int n, int nb, double *out, cudaStream_t s);
 cudaError_t mps_colmax(const double *X, long long n, int cols, double *out, cudaStream_t s);
 cudaError_t mps_to_f32_rhs(const double *R, float *R32, long long n, int cols, const double *scale, cudaStream_t s);
-cudaError_t mps_add_correction(double *X, const float *D32, long long n, int cols, const double *scale,
-                               cudaStream_t s);
 cudaError_t mps_mark_step(int *status, int k, cudaStream_t s);
 cudaError_t mpr_solve(const float *W, const float *Dinv, int n, int nb, int kind, float *R, float *Y, int *status,
                       cudaStream_t s);
@@ -61,8 +59,6 @@ cudaError_t rbt_transform_matrix(const double *A, float *W, int n, int nb, doubl
 cudaError_t rbt_transform_vectors(float *X, int n, int cols, int which, cudaStream_t s);
 cudaError_t mpd_factor_tile(int alg, float *W, int n, int nb, int k, int *status, float *binv, cudaStream_t s);
 cudaError_t mps_invert_diag(const float *W, int n, int nb, float *Dinv, int kind, cudaStream_t s);
-cudaError_t mps_rhs_step(const float *W, const float *Dinv, int n, int nb, int k, float *R, float *S, int kind,
-                         cudaStream_t s);
 cudaError_t mps_multi_dot(const double *V, int count, const double *w, long long n, int nrhs, double *H,
                           cudaStream_t s);
 cudaError_t mps_multi_axpy(const double *V, int count, const double *H, double *w, long long n, int nrhs, int assign,

@@ -542,42 +542,6 @@ __global__ void __launch_bounds__(NT, 1) invert_diag_kernel(const float *W, int 
     else strip_llu(m, T, nb, X, nb, nb);
 }
 
-// S = op(Dinv_k) R_k for one 64-row block per CTA (op = transpose when trans), then the
-// solution tile row is written back over R_k by the update kernel.
-__global__ void __launch_bounds__(NT, 1) rhs_apply_kernel(const float *Dinv, int n, int nb, int k, const float *R,
-                                                           float *S, int trans) {
-    extern __shared__ __align__(16) float smem[];
-    const Smem m = smem_parts(smem);
-    const int rb = blockIdx.x * 64;
-    const float *D = Dinv + (size_t)k * nb * nb;
-    const float *Rk = R + (size_t)k * nb;
-    float *out = S + rb;
-    for (int e = threadIdx.x; e < 64 * RW; e += NT) out[(e & 63) + (size_t)(e >> 6) * nb] = 0.f;
-    __syncthreads();
-    if (trans) cta_gemm_rw<true>(64, nb, 1.f, D + (size_t)rb * nb, nb, Rk, n, out, nb, m.g);
-    else cta_gemm_rw<false>(64, nb, 1.f, D + rb, nb, Rk, n, out, nb, m.g);
-}
-
-// R_t -= op(W tile) S for one 64-row block of tile row t per CTA (blockIdx.y = row block);
-// blockIdx.x == count writes S back into R_k instead.
-//   kind 0: R_t -= U(k,t)^T S (t > k);  kind 1: R_t -= U(t,k) S (t < k);  kind 2: R_t -= L(t,k) S
-__global__ void __launch_bounds__(NT, 1) rhs_update2_kernel(const float *W, int n, int nb, int k, float *R,
-                                                             const float *S, int kind, int count) {
-    extern __shared__ __align__(16) float smem[];
-    const Smem m = smem_parts(smem);
-    const int rb = blockIdx.y * 64;
-    if ((int)blockIdx.x == count) {
-        float *Rk = R + (size_t)k * nb + rb;
-        for (int e = threadIdx.x; e < 64 * RW; e += NT) Rk[(e & 63) + (size_t)(e >> 6) * n] = S[rb + (e & 63) + (size_t)(e >> 6) * nb];
-        return;
-    }
-    const int t = (kind == 1) ? (int)blockIdx.x : k + 1 + (int)blockIdx.x;
-    float *Rt = R + (size_t)t * nb + rb;
-    if (kind == 0)
-        cta_gemm_rw<true>(64, nb, -1.f, W + tile_off(n, nb, k, t) + (size_t)rb * nb, nb, S, nb, Rt, n, m.g);
-    else
-        cta_gemm_rw<false>(64, nb, -1.f, W + tile_off(n, nb, t, k) + rb, nb, S, nb, Rt, n, m.g);
-}
 
 // ---- FP64 residual R = B - A X (A: FP64 tile layout; X, B, R: n x nrhs, ld n; nrhs <= 16) ---
 // One CTA per 32-row block (n/32 CTAs, several resident per SM, so the last wave is short);
@@ -678,7 +642,8 @@ __global__ void colmax_kernel(const double *X, long long n, int cols, double *ou
         atomicMax(reinterpret_cast<unsigned long long *>(out + c), (unsigned long long)__double_as_longlong(mx));
 }
 
-// R32 (n x RW, zero padded) = float(R64 / scale_c) ; X64 += scale_c * D32
+
+// R32 (n x RW, zero padded) = float(R64 / scale_c)
 __global__ void to_f32_rhs_kernel(const double *R, float *R32, long long n, int cols, const double *scale) {
     const long long total = n * RW;
     for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < total; e += (long long)gridDim.x * blockDim.x) {
@@ -686,12 +651,6 @@ __global__ void to_f32_rhs_kernel(const double *R, float *R32, long long n, int 
         R32[e] = (c < cols) ? (float)(R[e] / scale[c]) : 0.f;
     }
 }
-__global__ void add_correction_kernel(double *X, const float *D32, long long n, int cols, const double *scale) {
-    const long long total = n * cols;
-    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < total; e += (long long)gridDim.x * blockDim.x)
-        X[e] += scale[e / n] * (double)D32[e];
-}
-
 // ---- GMRES building blocks (n x nrhs column-major blocks, one Krylov space per column) ----
 // H[l*nrhs + c] += <V_l[:,c], w[:,c]> for l < count (V_l at V + l*n*nrhs)
 __global__ void multi_dot_kernel(const double *V, int count, const double *w, long long n, int nrhs, double *H) {
@@ -807,10 +766,6 @@ cudaError_t mps_configure() {
     if (e != cudaSuccess) return e;
     e = cudaFuncSetAttribute(mps::invert_diag_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, mps::SMEM_BYTES);
     if (e != cudaSuccess) return e;
-    e = cudaFuncSetAttribute(mps::rhs_apply_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, mps::SMEM_BYTES);
-    if (e != cudaSuccess) return e;
-    e = cudaFuncSetAttribute(mps::rhs_update2_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, mps::SMEM_BYTES);
-    if (e != cudaSuccess) return e;
     e = cudaFuncSetAttribute(mps::half_panel_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, mps::SMEM_BYTES);
     if (e != cudaSuccess) return e;
     return cudaFuncSetAttribute(mps::half_update_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, mps::SMEM_BYTES);
@@ -863,18 +818,6 @@ cudaError_t mps_invert_diag(const float *W, int n, int nb, float *Dinv, int kind
     dim3 grid(nb / 64, n / nb);
     note_launch();
     mps::invert_diag_kernel<<<grid, mps::NT, mps::SMEM_BYTES, s>>>(W, n, nb, Dinv, kind);
-    return cudaGetLastError();
-}
-cudaError_t mps_rhs_step(const float *W, const float *Dinv, int n, int nb, int k, float *R, float *S, int kind,
-                         cudaStream_t s) {
-    // kind 0: Cholesky forward (U^T), 1: backward (U), 2: LU forward (unit L)
-    const int mt = n / nb;
-    note_launch();
-    mps::rhs_apply_kernel<<<nb / 64, mps::NT, mps::SMEM_BYTES, s>>>(Dinv, n, nb, k, R, S, kind == 0 ? 1 : 0);
-    const int cnt = (kind == 1) ? k : mt - k - 1;
-    dim3 grid(cnt + 1, nb / 64);
-    note_launch();
-    mps::rhs_update2_kernel<<<grid, mps::NT, mps::SMEM_BYTES, s>>>(W, n, nb, k, R, S, kind, cnt);
     return cudaGetLastError();
 }
 // binv (2 nb x 64 floats): inverses of the 64 x 64 diagonal blocks of tile k's upper factor,
@@ -990,11 +933,5 @@ cudaError_t mps_symmetrize(double *X, int n, int nb, cudaStream_t s) {
     return cudaGetLastError();
 }
 
-cudaError_t mps_add_correction(double *X, const float *D32, long long n, int cols, const double *scale,
-                               cudaStream_t s) {
-    note_launch();
-    mps::add_correction_kernel<<<2048, 256, 0, s>>>(X, D32, n, cols, scale);
-    return cudaGetLastError();
-}
 
 }  // namespace palial
