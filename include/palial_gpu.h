@@ -393,6 +393,17 @@ int palial_gpu_set_task_costs(int alg, int n, int nb, int block, const double *c
 int palial_dag_batch_validate(int count, const int *algs, const int *ns, const int *nbs, const int *bss,
                               int nworkers, unsigned int seed, char *msg, int msglen);
 
+/* ---- introspection of host-side schedules (host only, no GPU needed) ---------------------
+ * palial_gpu_row_groups: the tile-row groups in which palial_gpu_solve_ir_host sends the upper
+ * triangle of a mixed-precision Cholesky (gs/ge: rows [gs, ge); due: step by which the group's
+ * data is expected; kg: step by which it joins the trailing updates); arrays of at least 64;
+ * returns the number of groups or a negative error.
+ * palial_gpu_check_solve_tasks: 0 when the refinement's triangular-solve task list for mt tile
+ * rows, nbl 64-row blocks per tile and direction kind (0 U^T, 1 U, 2 unit L) is deadlock-free
+ * under in-order dispatch and its counters are consistent; else 1 + the first bad record. */
+int palial_gpu_row_groups(int n, int nb, int *gs, int *ge, int *due, int *kg, int max_groups);
+int palial_gpu_check_solve_tasks(int mt, int nbl, int kind);
+
 #ifdef __cplusplus
 }
 #endif

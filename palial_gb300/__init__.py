@@ -133,6 +133,9 @@ def lib() -> ctypes.CDLL:
                                                 ctypes.c_longlong, i, i, ctypes.POINTER(Opts), ctypes.POINTER(Status),
                                                 vp]
         h.palial_tiles_write.argtypes = [ctypes.c_char_p, ctypes.POINTER(Desc)]
+        h.palial_gpu_row_groups.argtypes = [i, i, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int),
+                                            ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int), i]
+        h.palial_gpu_check_solve_tasks.argtypes = [i, i, i]
         h.palial_tiles_read.argtypes = [ctypes.c_char_p, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int),
                                         vp]
         _lib = h
@@ -335,3 +338,17 @@ def dag_validate(alg: str, n: int, nb: int, block: int = 0, priority: int = 0, n
     buf = ctypes.create_string_buffer(256)
     rc = lib().palial_dag_validate(ALG[alg], n, nb, block, priority, nworkers, seed, buf, 256)
     return "" if rc == 0 else (buf.value.decode() or f"rc={rc}")
+
+
+def row_groups(n: int, nb: int) -> list[tuple[int, int, int, int]]:
+    """The tile-row groups (first row, end row, due step, join step) in which the host-buffer
+    mixed-precision Cholesky sends the upper triangle (host logic, no GPU)."""
+    arrs = [(ctypes.c_int * 64)() for _ in range(4)]
+    ng = lib().palial_gpu_row_groups(n, nb, *arrs, 64)
+    _check(0 if ng > 0 else ng, None)
+    return [(arrs[0][g], arrs[1][g], arrs[2][g], arrs[3][g]) for g in range(ng)]
+
+
+def check_solve_tasks(mt: int, nbl: int, kind: int) -> int:
+    """0 when the refinement's triangular-solve task list is deadlock-free (host logic)."""
+    return lib().palial_gpu_check_solve_tasks(mt, nbl, kind)

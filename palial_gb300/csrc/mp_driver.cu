@@ -139,6 +139,31 @@ struct RowArrival {
     cudaEvent_t ready[64] = {};
 } g_arrival;
 
+// The row groups of an n x n tile matrix (tile nb) for RowArrival: rows {0, 1}, single rows
+// 2..7, then 2, 2, 4, 4, 8, 8, ... rows (the first rows are needed first; a row must be present
+// two steps before the front reaches it).  due: the step by which the group's data is expected
+// (host link ~200 GB/s, about 1.1 ms per step at NB = 512, scaled by (NB/512)^2); kg: the step by
+// which it must join (gs - 2).  At most 64 groups.
+static void row_groups(int n, int nb, int &ngroups, int *gs, int *ge, int *due, int *kg) {
+    const int mt = n / nb;
+    const double te = (double)nb * nb;
+    const double step_s = 1.1e-3 * te / (512.0 * 512.0) * std::max(1.0, (double)mt / 64.0);
+    double bytes = 0.0;
+    ngroups = 0;
+    for (int r = 0; r < mt && ngroups < 64;) {
+        const int g = ngroups;
+        const int size = g == 0 ? 2 : r < 8 ? 1 : 2 << ((g - 7) / 2);
+        const int r1 = std::min(mt, g == 63 ? mt : r + size);
+        for (int rr = r; rr < r1; rr++) bytes += 8.0 * te * (double)(mt - rr);
+        gs[g] = r;
+        ge[g] = r1;
+        due[g] = (int)std::ceil(bytes / 200e9 / step_s);
+        kg[g] = g == 0 ? 0 : std::max(0, r - 2);
+        ngroups++;
+        r = r1;
+    }
+}
+
 static cudaError_t lookahead_init() {
     if (g_la.hi) return cudaSuccess;
     int least = 0, greatest = 0;
@@ -981,33 +1006,18 @@ extern "C" int palial_gpu_solve_ir_host(int alg, const palial_desc *A, const dou
         PALIAL_CK(mb.norms.ensure(sizeof(double) * 256), "alloc norms");
         double *amax = mb.norms.as<double>() + 120;
         PALIAL_CK(cudaMemsetAsync(amax, 0, sizeof(double), g_sc.copy), "max |a|");
-        // groups: rows {0,1}, single rows 2..7, then 2, 2, 4, 4, 8, 8, ... rows (a row must be
-        // present two steps before the front reaches it); group g's data is expected by the step
-        // the front reaches after its copy (host link ~200 GB/s, about 1.1 ms per step at
-        // NB = 512, scaled by (NB/512)^2), and it must join by step gs - 2
         RowArrival &ar = g_arrival;
-        ar.ngroups = 0;
-        double bytes = 0.0;
-        const double step_s = 1.1e-3 * (double)nb * nb / (512.0 * 512.0) * std::max(1.0, (double)mt / 64.0);
-        for (int r = 0; r < mt && ar.ngroups < 64;) {
-            const int g = ar.ngroups;
-            const int size = g == 0 ? 2 : r < 8 ? 1 : 2 << ((g - 7) / 2);
-            const int r1 = std::min(mt, g == 63 ? mt : r + size);
+        row_groups(n, nb, ar.ngroups, ar.gs, ar.ge, ar.due, ar.kg);
+        for (int g = 0; g < ar.ngroups; g++) {
             if (!ar.ready[g]) PALIAL_CK(cudaEventCreateWithFlags(&ar.ready[g], cudaEventDisableTiming), "copy event");
-            for (int rr = r; rr < r1; rr++)
+            for (int rr = ar.gs[g]; rr < ar.ge[g]; rr++)
                 PALIAL_CK(cudaMemcpy2DAsync(dA + te * ((size_t)rr + (size_t)mt * rr), sizeof(double) * te * mt,
                                             hA + te * ((size_t)rr + (size_t)mt * rr), sizeof(double) * te * mt,
                                             sizeof(double) * te, (size_t)(mt - rr), cudaMemcpyHostToDevice, g_sc.copy),
                           "copy A (row)");
-            PALIAL_CK(mps_f64_to_f32(dA, mb.w.as<float>(), n, nb, 0.0, g_sc.copy, amax, true, r, r1), "convert rows");
+            PALIAL_CK(mps_f64_to_f32(dA, mb.w.as<float>(), n, nb, 0.0, g_sc.copy, amax, true, ar.gs[g], ar.ge[g]),
+                      "convert rows");
             PALIAL_CK(cudaEventRecord(ar.ready[g], g_sc.copy), "copy event");
-            for (int rr = r; rr < r1; rr++) bytes += 8.0 * (double)te * (double)(mt - rr);
-            ar.gs[g] = r;
-            ar.ge[g] = r1;
-            ar.due[g] = (int)std::ceil(bytes / 200e9 / step_s);
-            ar.kg[g] = g == 0 ? 0 : std::max(0, r - 2);
-            ar.ngroups++;
-            r = r1;
         }
         ar.on = true;
         PALIAL_CK(cudaEventRecord(g_sc.upper, g_sc.copy), "copy A");
@@ -1047,4 +1057,12 @@ extern "C" int palial_gpu_solve_ir_host(int alg, const palial_desc *A, const dou
     PALIAL_CK(cudaMemcpy(X, dX, vb, cudaMemcpyDeviceToHost), "copy X");
     if (st) st->total_seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
     return rc;
+}
+
+// ---- introspection of the host-side schedules (host only, no GPU) -----------------------------
+extern "C" int palial_gpu_row_groups(int n, int nb, int *gs, int *ge, int *due, int *kg, int max_groups) {
+    if (n <= 0 || nb <= 0 || n % nb || !gs || !ge || !due || !kg || max_groups < 64) return PALIAL_ERR_ARG;
+    int ng = 0;
+    row_groups(n, nb, ng, gs, ge, due, kg);
+    return ng;
 }

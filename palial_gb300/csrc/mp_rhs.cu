@@ -241,3 +241,20 @@ cudaError_t mpr_solve(const float *W, const float *Dinv, int n, int nb, int kind
 }
 
 }  // namespace palial
+
+// Checks the task list of one solve direction: every wait must be met by signals of earlier
+// records (in-order dispatch cannot deadlock) and every object receives exactly the signals
+// its waiters count.  Returns 0, or 1 + the index of the first bad record.  Host only.
+extern "C" int palial_gpu_check_solve_tasks(int mt, int nbl, int kind) {
+    if (mt <= 0 || nbl <= 0 || kind < 0 || kind > 2) return -1;
+    const auto v = palial::mpr::build_tasks(mt, nbl, kind);
+    std::vector<int> sig((size_t)(2 * mt + mt * nbl), 0);
+    for (size_t i = 0; i < v.size(); i++) {
+        const auto &t = v[i];
+        for (int w = 0; w < t.nwait; w++)
+            if (t.wobj[w] < 0 || t.wobj[w] >= (int)sig.size() || sig[t.wobj[w]] < t.wcnt[w]) return (int)i + 1;
+        for (int q = 0; q < t.nsig; q++) sig[t.sobj[q]]++;
+    }
+    const size_t expect = (size_t)mt * nbl + (size_t)mt * (mt - 1) / 2 * nbl;
+    return v.size() == expect ? 0 : (int)v.size() + 1;
+}
