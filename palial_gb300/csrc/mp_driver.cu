@@ -970,8 +970,8 @@ extern "C" int palial_gpu_residual(const double *dA, int n, int nb, const double
 
 // Host-buffer variant (A: reference tile descriptor in host memory; B, X: n x nrhs host,
 // column-major): copies in, solves, copies X out.
-extern "C" int palial_gpu_solve_ir_host(int alg, const palial_desc *A, const double *B, double *X, int nrhs,
-                                        const palial_opts *opts, palial_status *st) {
+static int solve_ir_host_impl(int alg, const palial_desc *A, const double *B, double *X, int nrhs,
+                              const palial_opts *opts, palial_status *st) {
     if (st) memset(st, 0, sizeof *st);
     if (!A || !A->matrix || !B || !X || nrhs < 1 || nrhs > 16) return set_status(st, PALIAL_ERR_ARG, "bad arguments");
     const int n = A->matrix_size, nb = A->tile_size;
@@ -1056,6 +1056,18 @@ extern "C" int palial_gpu_solve_ir_host(int alg, const palial_desc *A, const dou
     if (g_sc.full) PALIAL_CK(cudaStreamWaitEvent(nullptr, g_sc.full, 0), "copy A");  // error paths too
     PALIAL_CK(cudaMemcpy(X, dX, vb, cudaMemcpyDeviceToHost), "copy X");
     if (st) st->total_seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    return rc;
+}
+
+// Whatever path returns, no copy of the caller's host buffers is left in flight (the caller may
+// free them as soon as the call returns).
+extern "C" int palial_gpu_solve_ir_host(int alg, const palial_desc *A, const double *B, double *X, int nrhs,
+                                        const palial_opts *opts, palial_status *st) {
+    const int rc = solve_ir_host_impl(alg, A, B, X, nrhs, opts, st);
+    g_arrival.on = false;
+    g_full_ready = nullptr;
+    if (g_sc.copy) cudaStreamSynchronize(g_sc.copy);
+    cudaStreamSynchronize(nullptr);
     return rc;
 }
 
