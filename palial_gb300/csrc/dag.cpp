@@ -167,6 +167,41 @@ Dag build_qr_solve_dag(int rows, int cols, int nb, int nrhs) {
     return d;
 }
 
+Dag build_trsolve_dag(int n, int nb, int nrhs, int alg) {
+    Dag d;
+    d.alg = 4;
+    d.n = n;
+    d.cols = n;
+    d.nrhs = nrhs;
+    d.nb = nb;
+    d.bs = nb;
+    if (nb <= 0 || nb % 64 || n % nb || nrhs < 1 || nrhs > nb || (alg != 0 && alg != 1))
+        throw std::runtime_error("dag: bad triangular solve sizes");
+    const int mt = n / nb, rparts = (nrhs + 63) / 64;
+    if (mt > 65535) throw std::runtime_error("dag: triangular solve too large");
+    auto obj = [mt](int i, int j) { return (uint32_t)(i + j * mt); };
+    Builder b(d, mt * (mt + 1));
+    // forward: Cholesky U^T Y = B, LU L Y = B (unit); each solved block updates the rows below
+    for (int k = 0; k < mt; k++) {
+        if (alg == 0) {
+            b.emit(T_TRSM_LUT, k, mt, 0, rparts, {obj(k, k)}, {obj(k, mt)}, nullptr);
+            for (int i = k + 1; i < mt; i++)
+                b.emit(T_GEMM_TN, k, mt, i, rparts, {obj(k, i), obj(k, mt)}, {obj(i, mt)}, nullptr);
+        } else {
+            b.emit(T_TRSM_LLU, k, 0, mt, rparts, {obj(k, k)}, {obj(k, mt)}, nullptr);
+            for (int i = k + 1; i < mt; i++)
+                b.emit(T_GEMM_NN, k, i, mt, rparts, {obj(i, k), obj(k, mt)}, {obj(i, mt)}, nullptr);
+        }
+    }
+    // backward: U X = Y, the last tile row first; each solved block updates the rows above
+    for (int k = mt - 1; k >= 0; k--) {
+        b.emit(T_TRSM_LUN, k, k, mt, rparts, {obj(k, k)}, {obj(k, mt)}, nullptr);
+        for (int i = 0; i < k; i++) b.emit(T_GEMM_NN, k, i, mt, rparts, {obj(i, k), obj(k, mt)}, {obj(i, mt)}, nullptr);
+    }
+    recompute_bottom_levels(d);
+    return d;
+}
+
 void recompute_bottom_levels(Dag &d) {
     // reverse program order; M[x] = max bl of later tasks waiting on / updating x
     std::vector<double> M(d.nobj, 0.0);

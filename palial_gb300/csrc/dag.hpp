@@ -50,6 +50,10 @@ Dag build_dag(int alg, int n, int nb, int bs, const double *costs = nullptr);
 // UNMQR/TSMQR tasks apply Q^T to them inside the same launch; then the blocked
 // back-substitution R X = (Q^T B)(0:cols) with left-upper TRSM and GEMM tasks.
 Dag build_qr_solve_dag(int rows, int cols, int nb, int nrhs);
+// A X = B with the FP64 factors of a Cholesky (alg 0, U^T U) or no-pivot LU (alg 1) in the first
+// n / nb tile columns of an n x (n + nb) tile matrix whose last tile column holds B (nrhs <= nb
+// columns): forward substitution tasks (TRSM + GEMM on the extra column), then backward.
+Dag build_trsolve_dag(int n, int nb, int nrhs, int alg);
 
 // One matrix of a batch: algorithm (0 Cholesky, 1 LU), padded size, tile size, block size.
 struct BatchSpec {

@@ -86,6 +86,9 @@ extern State g;
 
 // Free the QR solve's cached device buffers and DAG (palial_gpu_finalize).
 void qr_solve_release();
+// z = F^-1 v in FP64 for Cholesky / LU factors F in an n x (n + nb) tile matrix (qr_solve.cu).
+int fp64_trsolve(int alg, double *W, int n, int nb, const double *v, double *z, int nrhs, cudaStream_t s,
+                 palial_status *st);
 // Free the layout bridges' padded buffers (palial_gpu_finalize).
 void layout_release();
 // Free the random butterflies (palial_gpu_finalize).

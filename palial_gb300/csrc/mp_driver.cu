@@ -334,7 +334,8 @@ int mp_prepare_solves(int alg, const float *W, int n, int nb, cudaStream_t s, pa
 struct ResidCtx {
     bool df = false;
     int sigma = 0;
-    bool rbt = false;  // the factors are those of U^T A V (random butterflies, LU)
+    bool rbt = false;         // the factors are those of U^T A V (random butterflies, LU)
+    double *f64 = nullptr;    // FP64 factors (n x (n + nb) tile matrix): FP64 triangular solves
 } g_rctx;
 
 // d = M^-1 r for the FP32 factors in W; R32 (n x 16, zero padded) in/out.  Block forward and
@@ -354,6 +355,7 @@ int mp_apply_inverse(int alg, const float *W, int n, int nb, float *R32, cudaStr
 // z = M^-1 v for FP64 columns v (n x nrhs), through the FP32 factors (scaled per column).
 int precondition(int alg, const float *W, int n, int nb, const double *v, double *z, int nrhs, double *dscale,
                  std::vector<double> &hscale, cudaStream_t s, palial_status *st) {
+    if (g_rctx.f64) return fp64_trsolve(alg, g_rctx.f64, n, nb, v, z, nrhs, s, st);
     PALIAL_CK(mps_colmax(v, n, nrhs, dscale, s), "scale");
     PALIAL_CK(cudaMemcpyAsync(hscale.data(), dscale, sizeof(double) * nrhs, cudaMemcpyDeviceToHost, s), "scale");
     PALIAL_CK(cudaStreamSynchronize(s), "scale");
@@ -637,7 +639,8 @@ static int solve_one(int alg, const double *dA, int n, int nb, const double *dB,
     if (prec == PALIAL_PREC_FP64) {
         g_rctx.rbt = false;
         PALIAL_CK(wait_full_matrix(s), "matrix copy");
-        PALIAL_CK(g.mat.ensure(sizeof(double) * nn), "alloc copy");
+        // the factors plus one tile column of right-hand-side workspace (FP64 triangular solves)
+        PALIAL_CK(g.mat.ensure(sizeof(double) * (nn + (size_t)n * nb)), "alloc copy");
         PALIAL_CK(cudaMemcpyAsync(g.mat.ptr, dA, sizeof(double) * nn, cudaMemcpyDeviceToDevice, s), "copy");
         palial_opts fo = o;
         palial_status fs;
@@ -648,8 +651,9 @@ static int solve_one(int alg, const double *dA, int n, int nb, const double *dB,
             }
             return rc;
         }
-        PALIAL_CK(mps_f64_to_f32(g.mat.as<double>(), W, n, nb, 0.0, s, nullptr, alg == 0), "factor to f32");
+        g_rctx.f64 = g.mat.as<double>();
     } else {
+        g_rctx.f64 = nullptr;
         // host-buffer Cholesky with row-group arrival: the copy pipeline converts the upper
         // triangle group by group (and accumulates max |a_ij|) while the factorization runs
         const bool arrived_conv = g_arrival.on && alg == 0;
@@ -678,8 +682,10 @@ static int solve_one(int alg, const double *dA, int n, int nb, const double *dB,
         }
         if (rc) return set_status(st, rc, "mixed factorization failed (shift %.3e)", shift);
     }
-    rc = mp_prepare_solves(alg, W, n, nb, s, st);
-    if (rc) return rc;
+    if (!g_rctx.f64) {  // FP32 inverses of the diagonal factor tiles for the FP32 solves
+        rc = mp_prepare_solves(alg, W, n, nb, s, st);
+        if (rc) return rc;
+    }
     // The refinement steers with a compensated-FP32 residual (48-bit operands, error-free
     // products and sums, FP64 chunk accumulation; about 5x faster than the FP64 pipe) and
     // confirms convergence with the FP64 residual, so the reported error is an FP64 one.

@@ -64,6 +64,8 @@ __global__ void ls_resid_kernel(const double *__restrict__ W, double *__restrict
 DevBuf qs_work, qs_s;
 std::shared_ptr<Dag> qs_dag;
 int qs_key[6] = {0, 0, 0, 0, -1, 0};
+std::shared_ptr<Dag> ts_dag;  // FP64 triangular solves (build_trsolve_dag)
+int ts_key[4] = {0, 0, 0, -1};
 
 int grid_for(long long elems) {
     const long long b = (elems + 255) / 256;
@@ -77,6 +79,49 @@ void qr_solve_release() {
     qs_s.release();
     qs_dag.reset();
     qs_key[4] = -1;
+    ts_dag.reset();
+    ts_key[3] = -1;
+}
+
+// z = F^-1 v in FP64 with F the Cholesky (alg 0) or no-pivot LU (alg 1) factors held in the
+// first n / nb tile columns of W, an n x (n + nb) tile matrix whose last tile column is the
+// right-hand-side workspace; v, z n x nrhs column-major (nrhs <= nb).  One persistent
+// scheduler launch: forward then backward substitution tasks (build_trsolve_dag).
+int fp64_trsolve(int alg, double *W, int n, int nb, const double *v, double *z, int nrhs, cudaStream_t s,
+                 palial_status *st) {
+    const int workers = g.sms;
+    const int key[4] = {n, nb, nrhs, alg};
+    if (!ts_dag || memcmp(key, ts_key, sizeof key) != 0) {
+        try {
+            auto d = std::make_shared<Dag>(build_trsolve_dag(n, nb, nrhs, alg));
+            order_dag(*d, 0, workers, 0);
+            d->uid = g.next_uid++;
+            ts_dag = d;
+            memcpy(ts_key, key, sizeof key);
+        } catch (const std::exception &ex) {
+            return set_status(st, PALIAL_ERR_ARG, "%s", ex.what());
+        }
+    }
+    const std::shared_ptr<Dag> dag = ts_dag;
+    SchedParams p;
+    palial_opts o;
+    palial_opts_default(&o);
+    int rc = sched_prepare(g.main, dag, W, nullptr, workers, 0, o.timeout_s, p, st);
+    if (rc) return rc;
+    const int width = ((nrhs + 63) / 64) * 64;
+    double *rhs = W + (size_t)n * n;
+    note_launch();
+    rhs_to_tiles_kernel<<<grid_for((long long)n * width), 256, 0, s>>>(v, rhs, n, nrhs, nb, width);
+    PALIAL_CK(cudaGetLastError(), "pack right-hand sides");
+    PALIAL_CK(sched_enqueue(g.main, p, dag->nobj, workers, true, s), "launch scheduler");
+    note_launch();
+    tiles_to_x_kernel<<<grid_for((long long)n * nrhs), 256, 0, s>>>(rhs, z, n, nrhs, nb);
+    PALIAL_CK(cudaGetLastError(), "unpack solution");
+    int code = 0;
+    PALIAL_CK(cudaMemcpyAsync(&code, g.main.status.ptr, sizeof code, cudaMemcpyDeviceToHost, s), "status");
+    PALIAL_CK(cudaStreamSynchronize(s), "triangular solve");
+    if (code) return set_status(st, code, "FP64 triangular solve: device error %d", code);
+    return PALIAL_OK;
 }
 
 }  // namespace palial

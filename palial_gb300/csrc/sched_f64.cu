@@ -754,7 +754,7 @@ cudaError_t sched_launch(const SchedParams &p, int grid, cudaStream_t s) {
 long long sched_scratch_doubles(int alg, int n, int nb, int bs, int workers, long long *per_worker) {
     (void)n;
     (void)bs;
-    const long long pw = (alg == 2 || alg == 3) ? 2LL * nb * 64 : 0;
+    const long long pw = (alg == 2 || alg == 3 || alg == 4) ? 2LL * nb * 64 : 0;
     if (per_worker) *per_worker = pw;
     return pw * workers;
 }
