@@ -356,11 +356,12 @@ def test_random_butterfly_on_dense_matrix_agrees():
     assert (torch.linalg.vector_norm(x_rbt - x_plain) / torch.linalg.vector_norm(x_plain)).item() < 2 * 1e2 * 1e-14 * n
 
 
-@pytest.mark.parametrize("alg", ["cholesky", "lu"])
-def test_host_solve_matches_device_solve(alg):
-    """The host-buffer entry point (Cholesky: upper-triangle tiles copied first, the
-    factorization overlapping the copy of the rest) returns exactly the device-resident
-    solve's X."""
+@pytest.mark.parametrize("alg,prec", [("cholesky", "bf16x3"), ("cholesky", "bf16"), ("cholesky", "fp8"),
+                                      ("cholesky", "fp64"), ("lu", "bf16x3")])
+def test_host_solve_matches_device_solve(alg, prec):
+    """The host-buffer entry point (mixed Cholesky: the upper triangle arrives in row groups
+    and the factorization starts on the first ones, catching up skipped updates in step order;
+    FP64 Cholesky: upper triangle first) returns exactly the device-resident solve's X."""
     n, nb, nrhs = 4096, 512, 8
     a = O.gen_spd(0, n) if alg == "cholesky" else dominant(3, n)
     b = O.gen_uniform(5, n, nrhs, stream=O.STREAM_RHS)
@@ -369,10 +370,10 @@ def test_host_solve_matches_device_solve(alg):
     da = torch.from_numpy(at).cuda()
     db = torch.from_numpy(bf.ravel(order="F")).cuda()
     dx = torch.zeros_like(db)
-    st = P.solve_ir(alg, da.data_ptr(), n, nb, db.data_ptr(), dx.data_ptr(), nrhs, precision="bf16x3")
+    st = P.solve_ir(alg, da.data_ptr(), n, nb, db.data_ptr(), dx.data_ptr(), nrhs, precision=prec)
     assert st.code == 0
     host_a = torch.from_numpy(at).pin_memory()
     xh = np.zeros((nrhs, n))
-    sth = P.solve_ir_host(alg, host_a.numpy(), n, nb, np.ascontiguousarray(b.T), xh, nrhs, precision="bf16x3")
+    sth = P.solve_ir_host(alg, host_a.numpy(), n, nb, np.ascontiguousarray(b.T), xh, nrhs, precision=prec)
     assert sth.code == 0 and sth.ir_iters == st.ir_iters
     assert np.array_equal(xh, dx.cpu().numpy().reshape(nrhs, n))
