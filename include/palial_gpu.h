@@ -132,7 +132,8 @@ int palial_gpu_factor_dev(int alg, double *dA, double *dS, int n, int nb, const 
  * PALIAL_ALG_LU (no pivoting).  opts->precision selects the trailing-update precision
  * (PALIAL_PREC_BF16 / FP8 / BF16X3 on tcgen05 with FP32 accumulation, or FP64); diagonal
  * tiles are factored and panels solved in FP32, residuals r = b - A x and corrections in
- * FP64 storage.  Iterates until the normwise backward error max_j |r_j|/(|A| |x_j| + |b_j|) (inf-
+ * FP64 storage.  With PALIAL_PREC_FP64 the factorization runs on the FP64 tile scheduler and
+ * the refinement solves with the FP64 factors (one step to the target in practice).  Iterates until the normwise backward error max_j |r_j|/(|A| |x_j| + |b_j|) (inf-
  * norms) <= opts->ir_tol (default 1e-14 * n); GMRES-IR when plain refinement stagnates
  * (opts->gmres: -1 never, 0 automatic, 1 always).  NB must be a multiple of 256.
  * Returns PALIAL_ERR_NOT_CONVERGED (with the reached error in st) if the target is missed.
