@@ -254,7 +254,7 @@ def time_update_kernel(P, torch, n: int, precision: str = "bf16") -> dict:
 
 
 def run_batched(args, P, torch, rank: int = 0, world: int = 1) -> None:
-    """configs[3]: 2000 matrices, N log-uniform in [32, 2048) (seed 2), half SPD Cholesky, half
+    """The batched workload: 2000 matrices, N log-uniform in [32, 2048) (seed 2), half SPD Cholesky, half
     uniform LU, FP64, one persistent launch replayed from a CUDA graph; block size per size
     class chosen by the autotuner.  With N > 1 ranks every rank factors its share of a
     size-balanced partition (no collective on the data path; total work fixed: strong
@@ -287,7 +287,7 @@ def run_batched(args, P, torch, rank: int = 0, world: int = 1) -> None:
 
 
 def run_costmodel(args, P, torch) -> None:
-    """configs[4]: train the task-cost MLP on device traces of FP64 Cholesky / LU / QR sweeps,
+    """The learned cost model: train the task-cost MLP on device traces of FP64 Cholesky / LU / QR sweeps,
     report its prediction error on held-out runs, then factor N=49152 FP64 Cholesky with (a)
     the learned block size + learned critical-path priorities and (b) the fallback (exhaustive
     autotuner on a proxy size + static flop-model priorities), and report both makespans."""

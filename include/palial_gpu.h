@@ -126,7 +126,7 @@ int palial_gpu_qr(const palial_desc *A, const palial_desc *S, const palial_opts 
 int palial_gpu_factor_dev(int alg, double *dA, double *dS, int n, int nb, const palial_opts *opts,
                           palial_status *st, void *stream);
 
-/* ---- mixed precision + iterative refinement (no reference counterpart: north-star) ------
+/* ---- mixed precision + iterative refinement (no reference counterpart) ------
  * Solve A X = B for nrhs <= 16 right-hand sides (dB, dX: n x nrhs column-major, device),
  * A an FP64 tile-layout matrix on the device (not modified).  alg: PALIAL_ALG_CHOLESKY or
  * PALIAL_ALG_LU (no pivoting).  opts->precision selects the trailing-update precision
@@ -241,7 +241,7 @@ int palial_gpu_tile_dtsmqr_noalloc(int nb, double *dA1, double *dA2, const doubl
  * (LU), 2 = left lower no-trans unit (LU), 3 = left upper no-trans non-unit (QR solve).  kind for dgemm: 0 = C -= A^T B (Cholesky),
  * 1 = C -= A B (LU). */
 
-/* ---- batched factorizations (no reference counterpart: north-star) ------------------------
+/* ---- batched factorizations (no reference counterpart) ------------------------
  * Factor `count` independent matrices (alg 0 Cholesky / 1 LU per matrix) in ONE persistent
  * launch: the DAGs of all matrices are merged into one dispatch list ordered by critical path.
  * Matrix i: device tile-layout buffer dA[i] of size ns[i] (multiple of nbs[i]), scheduled in
@@ -368,7 +368,7 @@ long long palial_dag_qr_solve_validate(int rows, int cols, int nb, int nrhs, int
 int palial_dag_validate(int alg, int n, int nb, int block, int priority, int nworkers,
                         unsigned int seed, char *msg, int msglen);
 
-/* ---- learned task-cost model (no reference counterpart: north-star) ------------------------
+/* ---- learned task-cost model (no reference counterpart) ------------------------
  * An MLP (nin -> hidden -> hidden -> 1, ReLU, FP32) trained on the device by this library's
  * own forward / backward / Adam kernels.  Inputs are task features (palial_dag_features_count()
  * floats per task); the target is log(task time in microseconds). */

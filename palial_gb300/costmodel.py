@@ -2,7 +2,7 @@
 the GPU by the library's own kernels, and its two uses -- per-task costs for the critical-path
 dispatch order (opts.priority = 2) and the choice of the block size by predicted makespan.
 
-The fallback it is judged against: an exhaustive autotuner (every candidate block size timed
+The fallback it is compared with: an exhaustive autotuner (every candidate block size timed
 on a proxy size) with the static flop-model critical-path priorities.
 """
 from __future__ import annotations
