@@ -43,7 +43,8 @@ cudaError_t mps_residual_update(const double *A, int n, int nb, const double *D,
                                 int nrhs, int sigma, float *Ds, int *tau, cudaStream_t s);
 cudaError_t mps_tile_to_f64(const float *w, double *d, int nb, cudaStream_t s);
 cudaError_t mps_tile_to_f32(const double *d, float *w, int nb, int upper_only, cudaStream_t s);
-cudaError_t mps_panel_trsm(float *W, int n, int nb, int k, int kind, const float *binv, cudaStream_t s);
+cudaError_t mps_panel_trsm(float *W, int n, int nb, int k, int kind, const float *binv, cudaStream_t s,
+                           void *ph = nullptr, void *pl = nullptr);
 cudaError_t mps_block_inverse(const float *W, int n, int nb, int k, int factors, float *binv, cudaStream_t s,
                               int blocks = 0);
 cudaError_t mps_residual(const double *A, int n, int nb, const double *X, const double *B, double *R, int nrhs,
@@ -224,17 +225,21 @@ int mp_factor(int alg, int prec, float *W, int n, int nb, cudaStream_t s, palial
         void *bh = buf(mb.pb_hi, k & 1), *bl = mode == 2 ? buf(mb.pb_lo, k & 1) : nullptr;
         float *binv = mb.binv.as<float>();
         PALIAL_CK(mps_block_inverse(W, n, nb, k, alg == 0 ? 1 : 2, binv, hi), "diagonal block inverses");
+        // BF16 / BF16x3: the row-panel solve writes the packed operand with its results; FP8
+        // needs per-tile scales first, so it packs in a separate pass
+        const bool fused = mode != 1;
         if (alg == 0) {
-            PALIAL_CK(mps_panel_trsm(W, n, nb, k, 0, binv, hi), "panel trsm");
-            PALIAL_CK(mp_pack_rows(mode, W, n, nb, k, ah, al, sa, hi), "pack");
+            PALIAL_CK(mps_panel_trsm(W, n, nb, k, 0, binv, hi, fused ? ah : nullptr, fused ? al : nullptr), "panel trsm");
+            if (!fused) PALIAL_CK(mp_pack_rows(mode, W, n, nb, k, ah, al, sa, hi), "pack");
             bh = ah;
             bl = al;
             sb = sa;
         } else {
-            PALIAL_CK(mps_panel_trsm(W, n, nb, k, 1, binv, hi), "row panel trsm");
+            PALIAL_CK(mps_panel_trsm(W, n, nb, k, 1, binv, hi, fused ? bh : nullptr, fused ? bl : nullptr),
+                      "row panel trsm");
             PALIAL_CK(mps_panel_trsm(W, n, nb, k, 2, binv, hi), "column panel trsm");
             PALIAL_CK(mp_pack_cols(mode, W, n, nb, k, ah, al, sa, hi), "pack L");
-            PALIAL_CK(mp_pack_rows(mode, W, n, nb, k, bh, bl, sb, hi), "pack U");
+            if (!fused) PALIAL_CK(mp_pack_rows(mode, W, n, nb, k, bh, bl, sb, hi), "pack U");
         }
         PALIAL_CK(cudaEventRecord(g_la.packed, hi), "event");
         if (have_rest) PALIAL_CK(cudaStreamWaitEvent(hi, g_la.rest, 0), "event");

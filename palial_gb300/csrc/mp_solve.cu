@@ -2,6 +2,7 @@
 // refinement: precision conversions, panel triangular solves (FP32 SIMT), blocked triangular
 // solves of the refinement corrections with the low-precision factors, the FP64 residual
 // r = b - A x on the FP64 tile-layout matrix, and the norms of the backward error.
+#include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
 #include <cstdint>
@@ -385,7 +386,8 @@ __global__ void __launch_bounds__(256) block_inverse_kernel(const float *W, int 
 // 64 x 64 inverse block.  Staged through shared memory (m.Ds[c][r] = X(r, c), m.Bs[c][r] =
 // B(r, c)); thread: rows 4 tr .. 4 tr + 3, columns 4 tc .. 4 tc + 3.  Ends synced.
 template <int OP>
-__device__ __forceinline__ void apply_inv64(const Smem &m, const float *X, float *B, int ldb) {
+__device__ __forceinline__ void apply_inv64(const Smem &m, const float *X, float *B, int ldb,
+                                            __nv_bfloat16 *ph = nullptr, __nv_bfloat16 *pl = nullptr) {
     static_assert(4096 % NT == 0, "whole staging rounds");
 #pragma unroll
     for (int j = 0; j < 4096 / NT; j++) {
@@ -415,27 +417,39 @@ __device__ __forceinline__ void apply_inv64(const Smem &m, const float *X, float
             for (int y = 0; y < 4; y++) acc[x][y] = fmaf(a[x], bv[y], acc[x][y]);
     }
 #pragma unroll
-    for (int y = 0; y < 4; y++)
-        *reinterpret_cast<float4 *>(B + (size_t)(4 * tr) + (size_t)(4 * tc + y) * ldb) =
-            make_float4(acc[0][y], acc[1][y], acc[2][y], acc[3][y]);
+    for (int y = 0; y < 4; y++) {
+        const size_t o = (size_t)(4 * tr) + (size_t)(4 * tc + y) * ldb;
+        *reinterpret_cast<float4 *>(B + o) = make_float4(acc[0][y], acc[1][y], acc[2][y], acc[3][y]);
+        if (ph) {  // the packed BF16 operand (and the BF16x3 remainder) of the same elements
+#pragma unroll
+            for (int x = 0; x < 4; x++) {
+                const __nv_bfloat16 h = __float2bfloat16_rn(acc[x][y]);
+                ph[o + x] = h;
+                if (pl) pl[o + x] = __float2bfloat16_rn(acc[x][y] - __bfloat162float(h));
+            }
+        }
+    }
     __syncthreads();
 }
 
 // X = U^-T B, B = nb x 64 strip (ld), U upper nb x nb (ld_u); uinv: inverses of U's 64 x 64
 // diagonal blocks
+// (ph, pl: optional packed BF16 copy of the strip, same layout, written with the results)
 __device__ __forceinline__ void strip_lut(const Smem &m, const float *U, int ldu, float *B, int ldb, int nb,
-                                          const float *uinv) {
+                                          const float *uinv, __nv_bfloat16 *ph = nullptr,
+                                          __nv_bfloat16 *pl = nullptr) {
     for (int rb = 0; rb < nb; rb += 64) {
         if (rb > 0) cta_gemm<true, false>(64, 64, rb, -1.f, U + (size_t)rb * ldu, ldu, B, ldb, B + rb, ldb, m.g);
-        apply_inv64<0>(m, uinv + (size_t)(rb / 64) * 4096, B + rb, ldb);
+        apply_inv64<0>(m, uinv + (size_t)(rb / 64) * 4096, B + rb, ldb, ph ? ph + rb : nullptr, pl ? pl + rb : nullptr);
     }
 }
 // X = L^-1 B (unit lower) with L's diagonal-block inverses linv
 __device__ __forceinline__ void strip_llu_inv(const Smem &m, const float *L, int ldl, float *B, int ldb, int nb,
-                                              const float *linv) {
+                                              const float *linv, __nv_bfloat16 *ph = nullptr,
+                                              __nv_bfloat16 *pl = nullptr) {
     for (int rb = 0; rb < nb; rb += 64) {
         if (rb > 0) cta_gemm<false, false>(64, 64, rb, -1.f, L + rb, ldl, B, ldb, B + rb, ldb, m.g);
-        apply_inv64<1>(m, linv + (size_t)(rb / 64) * 4096, B + rb, ldb);
+        apply_inv64<1>(m, linv + (size_t)(rb / 64) * 4096, B + rb, ldb, ph ? ph + rb : nullptr, pl ? pl + rb : nullptr);
     }
 }
 // X = U^-1 B (backward), B = nb x 64 strip
@@ -469,15 +483,20 @@ __device__ __forceinline__ void strip_run(const Smem &m, const float *U, int ldu
 // kind 0: Cholesky row panel U(k,m) <- U_kk^-T U(k,m);  1: LU row panel U(k,n) <- L_kk^-1 .;
 // 2: LU column panel L(m,k) <- L(m,k) U_kk^-1.  grid (nb/64, trailing tiles).  binv: the
 // diagonal-block inverses of tile k (block_inverse_kernel).
+// ph, pl (row panels, optional): the packed BF16 (+ BF16x3 remainder) operand of the row panel,
+// trailing tile t - k - 1 at (t - k - 1) nb^2, written together with the solved values.
 __global__ void __launch_bounds__(NT, 2) panel_trsm_kernel(float *W, int n, int nb, int k, int kind,
-                                                          const float *binv) {
+                                                          const float *binv, __nv_bfloat16 *ph, __nv_bfloat16 *pl) {
     extern __shared__ __align__(16) float smem[];
     const Smem m = smem_parts(smem);
     const int t = k + 1 + blockIdx.y, s = blockIdx.x;
     const float *T = W + tile_off(n, nb, k, k);
-    if (kind == 0) strip_lut(m, T, nb, W + tile_off(n, nb, k, t) + (size_t)s * 64 * nb, nb, nb, binv);
+    const size_t po = (size_t)blockIdx.y * nb * nb + (size_t)s * 64 * nb;
+    __nv_bfloat16 *sh = ph ? ph + po : nullptr, *sl = pl ? pl + po : nullptr;
+    if (kind == 0) strip_lut(m, T, nb, W + tile_off(n, nb, k, t) + (size_t)s * 64 * nb, nb, nb, binv, sh, sl);
     else if (kind == 1)
-        strip_llu_inv(m, T, nb, W + tile_off(n, nb, k, t) + (size_t)s * 64 * nb, nb, nb, binv + (size_t)(nb / 64) * 4096);
+        strip_llu_inv(m, T, nb, W + tile_off(n, nb, k, t) + (size_t)s * 64 * nb, nb, nb, binv + (size_t)(nb / 64) * 4096,
+                      sh, sl);
     else strip_run(m, T, nb, W + tile_off(n, nb, t, k) + s * 64, nb, nb, binv);
 }
 
@@ -841,12 +860,16 @@ cudaError_t mps_half_update(float *T, int h, int ld, int alg, cudaStream_t s) {
                                                                                                         alg);
     return cudaGetLastError();
 }
-cudaError_t mps_panel_trsm(float *W, int n, int nb, int k, int kind, const float *binv, cudaStream_t s) {
+// ph / pl: optional packed BF16 row-panel operand written by the solve (kinds 0 and 1)
+cudaError_t mps_panel_trsm(float *W, int n, int nb, int k, int kind, const float *binv, cudaStream_t s, void *ph,
+                           void *pl) {
     const int ntr = n / nb - k - 1;
     if (ntr <= 0) return cudaSuccess;
     dim3 grid(nb / 64, ntr);
     note_launch();
-    mps::panel_trsm_kernel<<<grid, mps::NT, mps::SMEM_BYTES, s>>>(W, n, nb, k, kind, binv);
+    mps::panel_trsm_kernel<<<grid, mps::NT, mps::SMEM_BYTES, s>>>(W, n, nb, k, kind, binv,
+                                                                   kind == 2 ? nullptr : static_cast<__nv_bfloat16 *>(ph),
+                                                                   kind == 2 ? nullptr : static_cast<__nv_bfloat16 *>(pl));
     return cudaGetLastError();
 }
 cudaError_t mps_residual(const double *A, int n, int nb, const double *X, const double *B, double *R, int nrhs,
