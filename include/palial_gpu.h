@@ -403,6 +403,10 @@ int palial_dag_batch_validate(int count, const int *algs, const int *ns, const i
  * rows, nbl 64-row blocks per tile and direction kind (0 U^T, 1 U, 2 unit L) is deadlock-free
  * under in-order dispatch and its counters are consistent; else 1 + the first bad record. */
 int palial_gpu_row_groups(int n, int nb, int *gs, int *ge, int *due, int *kg, int max_groups);
+/* 0 when the host-buffer Cholesky's catch-up plan for those groups (update mode 0 BF16, 1 FP8,
+ * 2 BF16x3) waits for each group's data first, applies its skipped steps in order exactly once,
+ * joins it in time and covers the rows each next step needs; else a positive code. */
+int palial_gpu_check_arrival_plan(int n, int nb, int mode);
 int palial_gpu_check_solve_tasks(int mt, int nbl, int kind);
 
 #ifdef __cplusplus

@@ -136,6 +136,7 @@ def lib() -> ctypes.CDLL:
         h.palial_gpu_row_groups.argtypes = [i, i, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int),
                                             ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int), i]
         h.palial_gpu_check_solve_tasks.argtypes = [i, i, i]
+        h.palial_gpu_check_arrival_plan.argtypes = [i, i, i]
         h.palial_tiles_read.argtypes = [ctypes.c_char_p, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int),
                                         vp]
         _lib = h
@@ -352,3 +353,8 @@ def row_groups(n: int, nb: int) -> list[tuple[int, int, int, int]]:
 def check_solve_tasks(mt: int, nbl: int, kind: int) -> int:
     """0 when the refinement's triangular-solve task list is deadlock-free (host logic)."""
     return lib().palial_gpu_check_solve_tasks(mt, nbl, kind)
+
+
+def check_arrival_plan(n: int, nb: int, mode: int) -> int:
+    """0 when the host-buffer Cholesky's catch-up plan is consistent (host logic)."""
+    return lib().palial_gpu_check_arrival_plan(n, nb, mode)

@@ -165,6 +165,65 @@ static void row_groups(int n, int nb, int &ngroups, int *gs, int *ge, int *due, 
     }
 }
 
+// The rest-update stream's work per step under RowArrival, decided on the host: before step
+// k's rest update the actions pre[k] (group, step sk: apply step sk to the group's rows;
+// sk = -1: wait for the group's data), the rows [k + 2, present[k]) that rest update covers,
+// then the catch-up actions post[k].  A group joins (is covered by the rest updates) once its
+// data is due and it has steps 0..k-1, or at its deadline kg after the rest of them; catch-up
+// within a step's slack (the critical chain's time minus the rest update, in tile-pair
+// updates: about 0.8 ms per step, a BF16x3 pair update about 0.8 us at NB = 512, BF16 / FP8
+// a third; a pair costs NB^3, the chain about NB^2).
+struct ArrivalPlan {
+    std::vector<std::vector<std::pair<int, int>>> pre, post;
+    std::vector<int> present;
+};
+static ArrivalPlan plan_arrival(int mt, int nb, int mode, int ngroups, const int *gs, const int *ge, const int *due,
+                                const int *kg) {
+    ArrivalPlan pl;
+    pl.pre.resize(mt);
+    pl.post.resize(mt);
+    pl.present.assign(mt, mt);
+    int present = ge[0], next_group = 1;
+    int applied[64] = {};
+    bool waited[64] = {};
+    const long long chain_pairs = (mode == 2 ? 1000 : 3000) * 512 / nb;
+    const auto pairs_of = [&](int r0, int r1) {  // tile pairs (r, j >= r) of rows [r0, r1)
+        long long c = 0;
+        for (int r = r0; r < r1; r++) c += mt - r;
+        return c;
+    };
+    for (int k = 0; k + 1 < mt; k++) {
+        auto &pre = pl.pre[k], &post = pl.post[k];
+        const auto apply = [&](std::vector<std::pair<int, int>> &to, int gi, int sk) {
+            if (!waited[gi]) {
+                to.emplace_back(gi, -1);
+                waited[gi] = true;
+            }
+            to.emplace_back(gi, sk);
+            applied[gi] = sk + 1;
+        };
+        while (next_group < ngroups && ((due[next_group] <= k && applied[next_group] >= k) || kg[next_group] <= k)) {
+            for (int sk = applied[next_group]; sk < k; sk++) apply(pre, next_group, sk);
+            if (!waited[next_group]) {
+                pre.emplace_back(next_group, -1);
+                waited[next_group] = true;
+            }
+            present = ge[next_group];
+            next_group++;
+        }
+        pl.present[k] = present;
+        long long budget = std::max(chain_pairs / 5, chain_pairs - pairs_of(k + 2, present));
+        for (int gi = next_group; gi < ngroups && budget > 0 && due[gi] <= k; gi++) {
+            const long long cost = pairs_of(gs[gi], ge[gi]);
+            while (budget > 0 && applied[gi] <= k) {
+                apply(post, gi, applied[gi]);
+                budget -= cost;
+            }
+        }
+    }
+    return pl;
+}
+
 static cudaError_t lookahead_init() {
     if (g_la.hi) return cudaSuccess;
     int least = 0, greatest = 0;
@@ -206,14 +265,9 @@ int mp_factor(int alg, int prec, float *W, int n, int nb, cudaStream_t s, palial
         PALIAL_CK(cudaStreamWaitEvent(hi, g_arrival.ready[0], 0), "rows");
         PALIAL_CK(cudaStreamWaitEvent(lo, g_arrival.ready[0], 0), "rows");
     }
-    int present = arrive ? g_arrival.ge[0] : mt;  // tile rows the trailing updates cover
-    int next_group = 1;
-    int applied[64] = {};  // per group: steps 0..applied-1 applied
-    bool waited[64] = {};
-    // the critical chain's time per step in tile-pair updates of the trailing update (about
-    // 0.8 ms per step, a BF16x3 pair update about 0.8 us at NB = 512, BF16 / FP8 a third; a
-    // pair costs NB^3, the chain about NB^2)
-    const long long chain_pairs = (mode == 2 ? 1000 : 3000) * 512 / nb;
+    ArrivalPlan plan;
+    if (arrive)
+        plan = plan_arrival(mt, nb, mode, g_arrival.ngroups, g_arrival.gs, g_arrival.ge, g_arrival.due, g_arrival.kg);
     bool have_rest = false;
     for (int k = 0; k < mt; k++) {
         // the diagonal tile in FP32, one CTA (mp_diag.cu)
@@ -250,53 +304,30 @@ int mp_factor(int alg, int prec, float *W, int n, int nb, cudaStream_t s, palial
                       "update (rest)");
         } else {
             RowArrival &ar = g_arrival;
-            // step sk's update of group gi's rows (on lo, in step order)
-            const auto apply = [&](int gi, int sk) -> int {
-                if (!waited[gi]) {
-                    PALIAL_CK(cudaStreamWaitEvent(lo, ar.ready[gi], 0), "rows");
-                    waited[gi] = true;
+            // the planned actions (plan_arrival): group gi's data, or its step sk update, on lo
+            const auto run = [&](const std::vector<std::pair<int, int>> &acts) -> int {
+                for (const auto &a : acts) {
+                    const int gi = a.first, sk = a.second;
+                    if (sk < 0) {
+                        PALIAL_CK(cudaStreamWaitEvent(lo, ar.ready[gi], 0), "rows");
+                        continue;
+                    }
+                    float *ss = mb.scales.as<float>() + 2 * mt * sk;
+                    void *sh = buf(mb.pa_hi, sk), *sl = mode == 2 ? buf(mb.pa_lo, sk) : nullptr;
+                    PALIAL_CK(mp_update(mode, 1, W, n, nb, sk, sh, sl, sh, sl, ss, ss, status, lo, 3,
+                                        ar.gs[gi] - sk - 1, ar.ge[gi] - sk - 1),
+                              "update (arrived rows)");
                 }
-                float *ss = mb.scales.as<float>() + 2 * mt * sk;
-                void *sh = buf(mb.pa_hi, sk), *sl = mode == 2 ? buf(mb.pa_lo, sk) : nullptr;
-                PALIAL_CK(mp_update(mode, 1, W, n, nb, sk, sh, sl, sh, sl, ss, ss, status, lo, 3, ar.gs[gi] - sk - 1,
-                                    ar.ge[gi] - sk - 1),
-                          "update (arrived rows)");
-                applied[gi] = sk + 1;
                 return PALIAL_OK;
             };
-            const auto pairs_of = [&](int r0, int r1) {  // tile pairs (r, j >= r) of rows [r0, r1)
-                long long c = 0;
-                for (int r = r0; r < r1; r++) c += mt - r;
-                return c;
-            };
-            // a group whose data is due and that is caught up through step k-1 joins; a group at
-            // its deadline gets the rest of its skipped steps first
-            while (next_group < ar.ngroups &&
-                   ((ar.due[next_group] <= k && applied[next_group] >= k) || ar.kg[next_group] <= k)) {
-                for (int sk = applied[next_group]; sk < k; sk++) {
-                    const int rc2 = apply(next_group, sk);
-                    if (rc2) return rc2;
-                }
-                if (!waited[next_group]) {
-                    PALIAL_CK(cudaStreamWaitEvent(lo, ar.ready[next_group], 0), "rows");
-                    waited[next_group] = true;
-                }
-                present = ar.ge[next_group];
-                next_group++;
-            }
+            int rc2 = run(plan.pre[k]);
+            if (rc2) return rc2;
+            const int present = plan.present[k];
             if (present - k - 1 > 1)
                 PALIAL_CK(mp_update(mode, 1, W, n, nb, k, ah, al, bh, bl, sa, sb, status, lo, 3, 1, present - k - 1),
                           "update (rest)");
-            // catch-up of the next groups within this step's slack (in tile-pair updates)
-            long long budget = std::max(chain_pairs / 5, chain_pairs - pairs_of(k + 2, present));
-            for (int gi = next_group; gi < ar.ngroups && budget > 0 && ar.due[gi] <= k; gi++) {
-                const long long cost = pairs_of(ar.gs[gi], ar.ge[gi]);
-                while (budget > 0 && applied[gi] <= k) {
-                    const int rc2 = apply(gi, applied[gi]);
-                    if (rc2) return rc2;
-                    budget -= cost;
-                }
-            }
+            rc2 = run(plan.post[k]);
+            if (rc2) return rc2;
         }
         PALIAL_CK(cudaEventRecord(g_la.rest, lo), "event");
         have_rest = true;
@@ -1088,4 +1119,53 @@ extern "C" int palial_gpu_row_groups(int n, int nb, int *gs, int *ge, int *due, 
     int ng = 0;
     row_groups(n, nb, ng, gs, ge, due, kg);
     return ng;
+}
+
+// Checks the arrival plan for an n x n tile matrix (tile nb) and update mode: each group's data
+// is awaited before its first update, it receives steps 0..j-1 in order exactly once before it
+// joins at step j <= gs - 2, no update uses a panel not yet produced, and every rest update
+// covers the row the next step's first update needs.  0, or a positive code naming the
+// failed property.  Host only.
+extern "C" int palial_gpu_check_arrival_plan(int n, int nb, int mode) {
+    if (n <= 0 || nb <= 0 || n % nb || mode < 0 || mode > 2) return -1;
+    const int mt = n / nb;
+    if (mt <= 2) return 0;
+    int ng = 0, gs[64], ge[64], due[64], kg[64];
+    row_groups(n, nb, ng, gs, ge, due, kg);
+    const ArrivalPlan pl = plan_arrival(mt, nb, mode, ng, gs, ge, due, kg);
+    std::vector<int> applied(ng, 0), joined(ng, -1);
+    std::vector<char> waited(ng, 0);
+    joined[0] = 0;
+    waited[0] = 1;
+    int present = ge[0];
+    for (int k = 0; k + 1 < mt; k++) {
+        for (int half = 0; half < 2; half++) {
+            for (const auto &a : half ? pl.post[k] : pl.pre[k]) {
+                const int gi = a.first, sk = a.second;
+                if (gi <= 0 || gi >= ng || joined[gi] >= 0) return 1;  // only groups not joined
+                if (sk < 0) {
+                    if (waited[gi]) return 2;  // one wait per group
+                    waited[gi] = 1;
+                    continue;
+                }
+                if (!waited[gi]) return 3;               // data before the first update
+                if (sk != applied[gi] || sk > k) return 4;  // steps in order, panels exist
+                applied[gi]++;
+            }
+            if (half == 0) {  // groups that are caught up join this step's rest update
+                while (present < pl.present[k]) {
+                    int gi = 0;
+                    while (gi < ng && ge[gi] <= present) gi++;
+                    if (gi >= ng || !waited[gi] || applied[gi] != k || gs[gi] < k + 2) return 5;
+                    joined[gi] = k;
+                    present = ge[gi];
+                }
+                if (present != pl.present[k]) return 6;
+                if (present < std::min(mt, k + 3)) return 7;  // row k + 2 for the next step
+            }
+        }
+    }
+    for (int gi = 0; gi < ng; gi++)
+        if (joined[gi] < 0 || (gi > 0 && joined[gi] > gs[gi] - 2)) return 8;
+    return 0;
 }

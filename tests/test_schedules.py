@@ -30,3 +30,12 @@ def test_row_groups_cover_the_rows_and_join_in_time(n, nb):
 def test_row_groups_reject_bad_sizes():
     with pytest.raises(P.PalialError):
         P.row_groups(1000, 512)
+
+
+@pytest.mark.parametrize("mode", [0, 1, 2])
+@pytest.mark.parametrize("n,nb", [(32768, 512), (4096, 512), (1536, 512), (2048, 512), (16384, 1024),
+                                  (32768, 256), (65536, 512), (8192, 256)])
+def test_arrival_plan_is_consistent(n, nb, mode):
+    """Each group's data is awaited before its first update, its skipped steps are applied in
+    order exactly once, it joins by step gs - 2, and every rest update covers row k + 2."""
+    assert P.check_arrival_plan(n, nb, mode) == 0
