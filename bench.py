@@ -31,6 +31,9 @@ host cores) on the same metric, one bounded sample (N = 16384) per step.
 Cholesky, LU and QR; `--suite kappa` one line per kappa in {1e2, 1e6, 1e10}, algorithm and
 precision at N = 32768 (A = U diag(s) V^T, 64 Householder reflectors each side);
 `--suite kernels [--n N]` times the dominant kernels alone (the small case ncu captures run).
+`--suite batched` factors the uneven batch (2000 matrices, N log-uniform in [32, 2048)) in one
+FP64 launch, then times batched solves of it: FP64 factorizations vs block size and precision
+(FP32 + FP64 refinement, or FP64) autotuned per algorithm and size class.
 """
 from __future__ import annotations
 
@@ -284,6 +287,36 @@ def run_batched(args, P, torch, rank: int = 0, world: int = 1) -> None:
                                    for c in range(6) for j, bs in enumerate(B.CANDIDATE_BS)
                                    if rep["autotune_s"][c * 3 + j] >= 0},
                       "per_size_class_rank0": per_class}), flush=True)
+    run_batched_solve(args, rep["bs_of_class"], len(ns), world)
+
+
+def run_batched_solve(args, bs_fp64, count: int, world: int) -> None:
+    """Batched solves of the same synthetic batch (one right-hand side per matrix, uniform
+    [-1, 1)) to FP64-level backward error (1e-14 * N): (a) every matrix factored in FP64 with the
+    FP64 autotuner's block sizes, one FP64 refinement check; (b) block size and precision per
+    (algorithm, size class) from the solve autotuner: FP32 factorizations in one persistent
+    launch + FP64 refinement, FP64 where FP32 does not pay or does not converge, and an FP64
+    fallback of any matrix whose FP32 attempt fails.  Both timed as whole calls (copies,
+    factorizations, refinement loop).  Rank 0's share when run under torchrun."""
+    from palial_gb300 import batched as B
+    reps = max(3, args.steps)
+    fp64 = B.solve_synthetic(args.batch, seed=2, rank=0, world=world, autotune=False,
+                             bs12=list(bs_fp64) * 2, prec12=[0] * 12, reps=reps)
+    mixed = B.solve_synthetic(args.batch, seed=2, rank=0, world=world, autotune=True, reps=reps)
+    prec_name = {0: "fp64", 1: "fp32+ir"}
+    choice = {f"{('cholesky', 'lu')[k // 6]} {B.class_label(k % 6)}":
+              {"block": mixed["bs_of_class"][k], "precision": prec_name[mixed["prec_of_class"][k]]}
+              for k in range(12)}
+    print(json.dumps({"suite": "batched_solve", "matrices": count, "n_gpus": world, "rank0_matrices": mixed["count"],
+                      "fp64": {"seconds": fp64["seconds"], "matrices_per_s": fp64["matrices_per_s"],
+                               "tflops": fp64["tflops"], "max_backward_error": fp64["max_backward_error"],
+                               "converged": fp64["rc"] == 0},
+                      "mixed": {"seconds": mixed["seconds"], "matrices_per_s": mixed["matrices_per_s"],
+                                "tflops": mixed["tflops"], "max_backward_error": mixed["max_backward_error"],
+                                "max_refinement_steps": mixed["max_iters"], "fp64_fallbacks": mixed["fallbacks"],
+                                "converged": mixed["rc"] == 0, "autotune_seconds": mixed["autotune_seconds"],
+                                "choice": choice},
+                      "speedup_mixed_vs_fp64": fp64["seconds"] / mixed["seconds"]}), flush=True)
 
 
 def run_costmodel(args, P, torch) -> None:

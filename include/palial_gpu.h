@@ -46,6 +46,7 @@ extern "C" {
 #define PALIAL_PREC_FP8 2          /* trailing updates in FP8 e4m3, per-tile scale          */
 #define PALIAL_PREC_BF16X3 3       /* trailing updates as 3 BF16 products (split operands)  */
 #define PALIAL_PREC_AUTO 4         /* solve_ir: precision ladder BF16 -> BF16x3 -> FP64      */
+#define PALIAL_PREC_FP32 5         /* batched solves: FP32 factorization, FP64 refinement    */
 
 /* ---- descriptor ------------------------------------------------------------------------ */
 /* Same field order, types and meaning as the reference's MATRIX_desc
@@ -256,6 +257,33 @@ int palial_gpu_batched(int count, const int *algs, const int *ns, const int *nbs
                        double *completion_s, void *stream);
 int palial_gpu_gen_batch_matrix(double *dA, int kind, int n_true, int n_pad, int nb, uint64_t seed,
                                 void *stream);
+/* The same batched launch with FP32 tasks on FP32 tile-layout buffers (16-byte aligned): the
+ * FP32 factorizations of the batched mixed-precision solves.  A non-positive Cholesky pivot
+ * or an exact zero LU pivot does not stop the launch: breakdown[i] (optional, count ints)
+ * receives 0, or nonzero for matrix i (Cholesky: 1 + the first failing column). */
+int palial_gpu_batched_f32(int count, const int *algs, const int *ns, const int *nbs, const int *bss,
+                           float *const *dA, int *breakdown, const palial_opts *opts, palial_status *st,
+                           double *completion_s, void *stream);
+
+/* ---- batched solves (no reference counterpart) ------------------------------------------
+ * A_i x_i = b_i for `count` independent matrices to FP64-level normwise backward error
+ * |r|/(|A||x| + |b|) <= opts->ir_tol (0: 1e-14 * n_i), infinity norms.  Matrix i: device
+ * tile-layout buffer dA[i] (n = ns[i] <= 4096, tile nbs[i] = scheduler block, a multiple of 64
+ * dividing n; 16-byte aligned; not modified), right-hand side dB[i] and solution dX[i] (n
+ * doubles each).  precs[i] (NULL: all FP32): PALIAL_PREC_FP32 = the matrix is rounded to FP32
+ * and factored with the other FP32 matrices in ONE persistent launch, then refined with FP64
+ * residuals; PALIAL_PREC_FP64 = factored in FP64 (one launch for those).  An FP32 matrix whose
+ * factorization breaks down or whose refinement stalls (less than 2x per step, at most
+ * opts->ir_max_iter steps, 0 = 30) is refactored in FP64 and refined again.  iters[i]
+ * (optional): refinement steps, or -(steps + 1) for a matrix that fell back to FP64; berr[i]
+ * (optional): its final backward error.  st: seconds = wall time of the call, factor_seconds =
+ * the factorization launches, backward_error = the worst, ir_iters = the most steps,
+ * ntasks = the number of FP64 fallbacks.  Returns PALIAL_ERR_NOT_CONVERGED if a matrix stays
+ * above its tolerance; an FP64 Cholesky breakdown fails the call (PALIAL_ERR_NOT_SPD). */
+int palial_gpu_batched_solve(int count, const int *algs, const int *ns, const int *nbs,
+                             const double *const *dA, const double *const *dB, double *const *dX,
+                             const int *precs, const palial_opts *opts, palial_status *st, int *iters,
+                             double *berr, void *stream);
 
 /* ---- the synthetic uneven batch, its autotuner and its rank partition -----------------------
  * Batch of `count` matrices: N_i = floor(32 * 64^u_i), u_i uniform in [0,1) (splitmix64 of
@@ -287,6 +315,35 @@ int palial_gpu_batch_autotune(int count, const int *ns, const int *algs, uint64_
  * warm-up and `reps` timed batched launches (CUDA graph replay), and fill the report. */
 int palial_gpu_batch_synthetic(int count, uint64_t seed, int rank, int world, int autotune, const int *bs_of_class,
                                int reps, const palial_opts *opts, palial_status *st, palial_batch_report *rep);
+
+/* Batched solves of the synthetic batch (right-hand sides uniform [-1,1)), block size and
+ * factorization precision per (algorithm, size class), index alg * 6 + class. */
+typedef struct palial_batch_solve_report {
+    int count;                /* matrices solved by this rank                                */
+    int bs_of_class[12];      /* block (= tile) size per [alg * 6 + size class]              */
+    int prec_of_class[12];    /* 1 = FP32 factorization + FP64 refinement, 0 = FP64          */
+    int fallbacks;            /* most matrices refactored in FP64 in one timed solve         */
+    int max_iters;            /* most refinement steps of one matrix                         */
+    int not_converged;        /* 1 if a timed solve left a matrix above its tolerance        */
+    double seconds;           /* median wall time of one batched solve (every phase)         */
+    double matrices_per_s;
+    double tflops;            /* factorization flops (N^3/3, 2N^3/3) / seconds               */
+    double max_backward_error;
+    double autotune_seconds;
+    double autotune_s[72];    /* [alg*6 + class][precision 0,1][block 64,128,256] seconds;
+                                 -1 = not run, -2 = did not reach the tolerance              */
+} palial_batch_solve_report;
+/* Per (algorithm, size class), time the class's matrices alone with every block size (64,
+ * 128, 256 where it fits) and both precisions, and keep the fastest choice that reaches the
+ * tolerance on every matrix. */
+int palial_gpu_batch_solve_autotune(int count, const int *ns, const int *algs, uint64_t seed, int reps, int *bs12,
+                                    int *prec12, double *timings, palial_status *st);
+/* Generate this rank's share of the synthetic batch with right-hand sides, optionally autotune
+ * (else bs12 / prec12, NULL = block 64 below N = 512 and 128 above / FP32 everywhere), run one
+ * warm-up and `reps` timed batched solves, and fill the report. */
+int palial_gpu_batch_solve_synthetic(int count, uint64_t seed, int rank, int world, int autotune, const int *bs12,
+                                     const int *prec12, int reps, const palial_opts *opts, palial_status *st,
+                                     palial_batch_solve_report *rep);
 
 /* ---- generators (counter-based; the same bytes as the CPU oracle's generators) ------------ */
 /* uniform [-1,1): entry (i,j) from splitmix64 of seed/stream and i + j*rows.  Tile layout. */

@@ -23,7 +23,7 @@ ERR = {
     -7: "device allocation failed", 1: "exact zero pivot skipped",
 }
 ALG = {"cholesky": 0, "lu": 1, "qr": 2}
-PREC = {"fp64": 0, "bf16": 1, "fp8": 2, "bf16x3": 3, "auto": 4}
+PREC = {"fp64": 0, "bf16": 1, "fp8": 2, "bf16x3": 3, "auto": 4, "fp32": 5}
 PREC_NAME = {v: k for k, v in PREC.items()}
 PREC_NAME[100 + PREC["bf16x3"]] = "bf16x3-rbt"  # AUTO ladder rung: BF16x3 on the butterfly transform
 
@@ -127,6 +127,14 @@ def lib() -> ctypes.CDLL:
         h.palial_gpu_batch_autotune.argtypes = [i, vp, vp, ctypes.c_uint64, i, vp, vp, ctypes.POINTER(Status)]
         h.palial_gpu_batch_synthetic.argtypes = [i, ctypes.c_uint64, i, i, i, vp, i, ctypes.POINTER(Opts),
                                                  ctypes.POINTER(Status), vp]
+        h.palial_gpu_batched_f32.argtypes = [i, vp, vp, vp, vp, vp, vp, ctypes.POINTER(Opts), ctypes.POINTER(Status),
+                                             vp, vp]
+        h.palial_gpu_batched_solve.argtypes = [i, vp, vp, vp, vp, vp, vp, vp, ctypes.POINTER(Opts),
+                                               ctypes.POINTER(Status), vp, vp, vp]
+        h.palial_gpu_batch_solve_autotune.argtypes = [i, vp, vp, ctypes.c_uint64, i, vp, vp, vp,
+                                                      ctypes.POINTER(Status)]
+        h.palial_gpu_batch_solve_synthetic.argtypes = [i, ctypes.c_uint64, i, i, i, vp, vp, i, ctypes.POINTER(Opts),
+                                                       ctypes.POINTER(Status), vp]
         h.palial_gpu_colmajor_to_tiles.argtypes = [vp, ctypes.c_longlong, i, vp, i, i, d, vp]
         h.palial_gpu_tiles_to_colmajor.argtypes = [vp, i, i, vp, ctypes.c_longlong, i, vp]
         h.palial_gpu_solve_colmajor.argtypes = [i, i, vp, ctypes.c_longlong, vp, ctypes.c_longlong, vp,

@@ -10,6 +10,12 @@ persistent scheduler launch, optionally replayed from a CUDA graph.
 
 The autotuner times each size class alone with every candidate block size and keeps the
 fastest; the per-class choice is then used for the whole batch.
+
+Batched solves (``solve``, ``solve_synthetic``): A_i x_i = b_i to FP64-level backward error,
+each matrix factored in FP32 (all FP32 matrices in one persistent launch of the FP32 task
+scheduler) or FP64 and refined with FP64 residuals; a matrix whose FP32 factorization breaks
+down or whose refinement stalls is refactored in FP64.  The solve autotuner picks block size
+and precision per (algorithm, size class).
 """
 from __future__ import annotations
 
@@ -18,10 +24,18 @@ import math
 
 import numpy as np
 
-from . import PalialError, Status, lib, make_opts
+from . import PREC, PalialError, Status, lib, make_opts
 
 CLASS_EDGES = (32, 64, 128, 256, 512, 1024, 2048)
 CANDIDATE_BS = (64, 128, 256)
+
+
+class SolveReport(ctypes.Structure):
+    _fields_ = [("count", ctypes.c_int), ("bs_of_class", ctypes.c_int * 12), ("prec_of_class", ctypes.c_int * 12),
+                ("fallbacks", ctypes.c_int), ("max_iters", ctypes.c_int), ("not_converged", ctypes.c_int),
+                ("seconds", ctypes.c_double), ("matrices_per_s", ctypes.c_double), ("tflops", ctypes.c_double),
+                ("max_backward_error", ctypes.c_double), ("autotune_seconds", ctypes.c_double),
+                ("autotune_s", ctypes.c_double * 72)]
 
 
 class BatchReport(ctypes.Structure):
@@ -170,4 +184,62 @@ def synthetic(count: int = 2000, seed: int = 2, rank: int = 0, world: int = 1, a
     out = {f: getattr(rep, f) for f, _ in BatchReport._fields_}
     for f in ("bs_of_class", "count_of_class", "p50_ms", "p99_ms", "autotune_s"):
         out[f] = list(out[f])
+    return out
+
+
+def _ptrs(ptrs) -> ctypes.Array:
+    return (ctypes.c_void_p * max(1, len(ptrs)))(*[int(p) for p in ptrs])
+
+
+def factor_f32(algs, ns, nbs, ptrs, bss=None) -> tuple[Status, np.ndarray]:
+    """FP32 factorizations of FP32 tile-layout device buffers in one persistent launch (the
+    batched solves' factorization).  Returns (status, breakdown flags per matrix)."""
+    count = len(ns)
+    flags = (ctypes.c_int * max(1, count))()
+    st = Status()
+    rc = lib().palial_gpu_batched_f32(count, _ints(algs), _ints(ns), _ints(nbs), _ints(nbs if bss is None else bss),
+                                      _ptrs(ptrs), flags, ctypes.byref(make_opts()), ctypes.byref(st), None, None)
+    st.code = rc
+    if rc < 0:
+        raise PalialError(rc, st.message.decode(errors="replace"))
+    return st, np.array(flags[:count], dtype=np.int64)
+
+
+def solve(algs, ns, nbs, a_ptrs, b_ptrs, x_ptrs, precs=None, ir_tol: float = 0.0, ir_max_iter: int = 0,
+          allow_not_converged: bool = False) -> tuple[Status, np.ndarray, np.ndarray]:
+    """Batched solves A_i x_i = b_i (device buffers: A in the tile layout with tile nbs[i], b and
+    x of ns[i] doubles).  precs[i]: "fp32" (default) or "fp64" factorization.  Returns (status,
+    iters, backward errors); iters[i] < 0 marks a matrix refactored in FP64 after its FP32
+    attempt (-(steps + 1))."""
+    count = len(ns)
+    pr = None if precs is None else _ints([PREC[p] if isinstance(p, str) else int(p) for p in precs])
+    iters = (ctypes.c_int * max(1, count))()
+    berr = (ctypes.c_double * max(1, count))()
+    st = Status()
+    o = make_opts(ir_tol=ir_tol, ir_max_iter=ir_max_iter)
+    rc = lib().palial_gpu_batched_solve(count, _ints(algs), _ints(ns), _ints(nbs), _ptrs(a_ptrs), _ptrs(b_ptrs),
+                                        _ptrs(x_ptrs), pr, ctypes.byref(o), ctypes.byref(st), iters, berr, None)
+    st.code = rc
+    if rc < 0 and not (allow_not_converged and rc == -6):
+        raise PalialError(rc, st.message.decode(errors="replace"))
+    return st, np.array(iters[:count], dtype=np.int64), np.array(berr[:count], dtype=np.float64)
+
+
+def solve_synthetic(count: int = 2000, seed: int = 2, rank: int = 0, world: int = 1, autotune: bool = True,
+                    bs12=None, prec12=None, reps: int = 3) -> dict:
+    """Batched solves of this rank's share of the synthetic batch, inside the library; block and
+    precision per [alg * 6 + size class] from the autotuner or the arguments.  Returns the
+    report as a dict."""
+    rep = SolveReport()
+    st = Status()
+    b12 = (ctypes.c_int * 12)(*bs12) if bs12 is not None else None
+    p12 = (ctypes.c_int * 12)(*prec12) if prec12 is not None else None
+    rc = lib().palial_gpu_batch_solve_synthetic(count, ctypes.c_uint64(seed), rank, world, int(autotune), b12, p12,
+                                                reps, ctypes.byref(make_opts()), ctypes.byref(st), ctypes.byref(rep))
+    if rc and rc != -6:
+        raise PalialError(rc, st.message.decode(errors="replace"))
+    out = {f: getattr(rep, f) for f, _ in SolveReport._fields_}
+    for f in ("bs_of_class", "prec_of_class", "autotune_s"):
+        out[f] = list(out[f])
+    out["rc"] = rc
     return out

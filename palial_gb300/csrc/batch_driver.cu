@@ -20,6 +20,7 @@
 #include "host_state.hpp"
 
 namespace palial {
+cudaError_t launch_gen_dense(double *X, long long rows, int cols, uint64_t seed, int stream, cudaStream_t s);
 namespace {
 
 constexpr int kClassEdges[7] = {32, 64, 128, 256, 512, 1024, 2048};
@@ -86,6 +87,80 @@ int run_batch(BatchBufs &b, const palial_opts &o, palial_status *st, double *com
     ro.reserved[2] = 1;
     return palial_gpu_batched((int)b.ns.size(), b.algs.data(), b.np.data(), b.bs.data(), b.bs.data(), b.ptrs.data(),
                               &ro, st, completion, nullptr);
+}
+
+// Device copy of a (sub)batch for the batched solves: per matrix A (padded, tile = block
+// size of its (algorithm, size class)), b (uniform [-1, 1), stream 7 of the matrix's seed)
+// and x.  A and b are read only, so repeated solves need no reset.
+struct SolveBatch {
+    std::vector<int> ns, algs, np, bs, prec;
+    std::vector<const double *> A, B;
+    std::vector<double *> X;
+    double *buf = nullptr;
+    double flops = 0;
+    ~SolveBatch() {
+        if (buf) cudaFree(buf);
+    }
+};
+
+int make_solve_batch(SolveBatch &b, const std::vector<int> &idx, const std::vector<int> &ns,
+                     const std::vector<int> &algs, const int *bs12, const int *prec12, uint64_t seed,
+                     palial_status *st) {
+    std::vector<size_t> offa, offb, offx;
+    size_t elems = 0;
+    for (int i : idx) {
+        const int k = algs[i] * 6 + size_class(ns[i]);
+        b.ns.push_back(ns[i]);
+        b.algs.push_back(algs[i]);
+        b.bs.push_back(bs12[k]);
+        b.prec.push_back(prec12[k]);
+        b.np.push_back(padded(ns[i], bs12[k]));
+        const size_t np = (size_t)b.np.back();
+        offa.push_back(elems);
+        elems += (np * np + 3) / 4 * 4;
+        b.flops += algorithmic_flops(algs[i], ns[i]);
+    }
+    for (size_t j = 0; j < idx.size(); j++) {
+        offb.push_back(elems);
+        elems += ((size_t)b.np[j] + 3) / 4 * 4;
+        offx.push_back(elems);
+        elems += ((size_t)b.np[j] + 3) / 4 * 4;
+    }
+    PALIAL_CK(cudaMalloc(&b.buf, sizeof(double) * std::max<size_t>(4, elems)), "alloc solve batch");
+    for (size_t j = 0; j < idx.size(); j++) {
+        b.A.push_back(b.buf + offa[j]);
+        b.B.push_back(b.buf + offb[j]);
+        b.X.push_back(b.buf + offx[j]);
+        const uint64_t ms = seed * 100000ull + (uint64_t)idx[j];
+        const int rc = palial_gpu_gen_batch_matrix(b.buf + offa[j], b.algs[j] == 0 ? 1 : 0, b.ns[j], b.np[j], b.bs[j],
+                                                   ms, nullptr);
+        if (rc) return set_status(st, rc, "generating batch matrix %d", idx[j]);
+        PALIAL_CK(launch_gen_dense(b.buf + offb[j], b.np[j], 1, ms, 7, nullptr), "generating right-hand side");
+    }
+    PALIAL_CK(cudaDeviceSynchronize(), "generate solve batch");
+    return PALIAL_OK;
+}
+
+struct SolveResult {
+    double seconds = 0, worst = 0;
+    int fallbacks = 0, max_iters = 0, rc = 0;
+};
+
+int run_solve_batch(SolveBatch &b, const palial_opts &o, SolveResult &res, palial_status *st) {
+    const int count = (int)b.ns.size();
+    std::vector<int> prec(count), iters(count);
+    std::vector<double> berr(count);
+    for (int j = 0; j < count; j++) prec[j] = b.prec[j] ? PALIAL_PREC_FP32 : PALIAL_PREC_FP64;
+    palial_status s2;
+    const int rc = palial_gpu_batched_solve(count, b.algs.data(), b.np.data(), b.bs.data(), b.A.data(), b.B.data(),
+                                            b.X.data(), prec.data(), &o, &s2, iters.data(), berr.data(), nullptr);
+    if (rc < 0 && rc != PALIAL_ERR_NOT_CONVERGED) return set_status(st, rc, "batched solve: %s", s2.message);
+    res.rc = rc;
+    res.seconds = s2.seconds;
+    res.worst = s2.backward_error;
+    res.fallbacks = (int)s2.ntasks;
+    res.max_iters = s2.ir_iters;
+    return PALIAL_OK;
 }
 
 double percentile(std::vector<double> v, double q) {
@@ -241,6 +316,130 @@ int palial_gpu_batch_synthetic(int count, uint64_t seed, int rank, int world, in
         st->ntasks = s2.ntasks;
     }
     return set_status(st, PALIAL_OK);
+}
+
+int palial_gpu_batch_solve_autotune(int count, const int *ns, const int *algs, uint64_t seed, int reps, int *bs12,
+                                    int *prec12, double *timings, palial_status *st) {
+    if (st) memset(st, 0, sizeof *st);
+    if (count <= 0 || !ns || !algs || !bs12 || !prec12) return set_status(st, PALIAL_ERR_ARG, "empty batch");
+    int rc = ensure_init(st);
+    if (rc) return rc;
+    std::vector<int> vn(ns, ns + count), va(algs, algs + count);
+    palial_opts o;
+    palial_opts_default(&o);
+    if (timings)
+        for (int i = 0; i < 72; i++) timings[i] = -1;
+    for (int k = 0; k < 12; k++) {
+        const int a = k / 6, c = k % 6;
+        std::vector<int> idx;
+        for (int i = 0; i < count; i++)
+            if (va[i] == a && size_class(vn[i]) == c) idx.push_back(i);
+        bs12[k] = 64;
+        prec12[k] = 0;
+        if (idx.empty()) continue;
+        double best = 1e30;
+        for (int prec = 0; prec < 2; prec++)
+            for (int j = 0; j < 3; j++) {
+                const int bs = kCandidates[j];
+                if (bs > std::max(64, kClassEdges[c + 1])) continue;
+                int b12[12], p12[12];
+                for (int q = 0; q < 12; q++) {
+                    b12[q] = bs;
+                    p12[q] = prec;
+                }
+                SolveBatch b;
+                rc = make_solve_batch(b, idx, vn, va, b12, p12, seed, st);
+                if (rc) return rc;
+                double t = 1e30;
+                for (int r = 0; r <= std::max(1, reps); r++) {
+                    SolveResult res;
+                    rc = run_solve_batch(b, o, res, st);
+                    if (rc) return rc;
+                    // a choice must reach the tolerance on every matrix
+                    if (res.rc != PALIAL_OK) {
+                        t = 1e30;
+                        break;
+                    }
+                    if (r > 0) t = std::min(t, res.seconds);
+                }
+                if (timings) timings[k * 6 + prec * 3 + j] = t < 1e30 ? t : -2;
+                if (t < best) {
+                    best = t;
+                    bs12[k] = bs;
+                    prec12[k] = prec;
+                }
+            }
+    }
+    return set_status(st, PALIAL_OK);
+}
+
+int palial_gpu_batch_solve_synthetic(int count, uint64_t seed, int rank, int world, int autotune, const int *bs12_in,
+                                     const int *prec12_in, int reps, const palial_opts *opts, palial_status *st,
+                                     palial_batch_solve_report *rep) {
+    if (st) memset(st, 0, sizeof *st);
+    if (count <= 0 || world < 1 || rank < 0 || rank >= world || !rep)
+        return set_status(st, PALIAL_ERR_ARG, "bad batch arguments");
+    memset(rep, 0, sizeof *rep);
+    int rc = ensure_init(st);
+    if (rc) return rc;
+    palial_opts o;
+    palial_opts_default(&o);
+    if (opts) o = *opts;
+    std::vector<int> ns(count), algs(count), owner(count);
+    palial_gpu_batch_sizes(count, seed, ns.data(), algs.data());
+    palial_gpu_batch_partition(count, ns.data(), algs.data(), world, owner.data());
+    std::vector<int> idx, mns, malgs;
+    for (int i = 0; i < count; i++)
+        if (owner[i] == rank) {
+            idx.push_back(i);
+            mns.push_back(ns[i]);
+            malgs.push_back(algs[i]);
+        }
+    int bs12[12], prec12[12];
+    for (int k = 0; k < 12; k++) {
+        bs12[k] = bs12_in ? bs12_in[k] : (k % 6 < 4 ? 64 : 128);
+        prec12[k] = prec12_in ? prec12_in[k] : 1;
+    }
+    const auto t0 = std::chrono::steady_clock::now();
+    if (autotune && !idx.empty()) {
+        rc = palial_gpu_batch_solve_autotune((int)idx.size(), mns.data(), malgs.data(), seed, 1, bs12, prec12,
+                                             rep->autotune_s, st);
+        if (rc) return rc;
+    }
+    rep->autotune_seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    rep->count = (int)idx.size();
+    for (int k = 0; k < 12; k++) {
+        rep->bs_of_class[k] = bs12[k];
+        rep->prec_of_class[k] = prec12[k];
+    }
+    if (idx.empty()) return set_status(st, PALIAL_OK);
+    SolveBatch b;
+    rc = make_solve_batch(b, idx, ns, algs, bs12, prec12, seed, st);
+    if (rc) return rc;
+    SolveResult res;
+    rc = run_solve_batch(b, o, res, st);  // warm-up (allocations, DAGs)
+    if (rc) return rc;
+    std::vector<double> times;
+    for (int r = 0; r < std::max(1, reps); r++) {
+        rc = run_solve_batch(b, o, res, st);
+        if (rc) return rc;
+        times.push_back(res.seconds);
+        rep->max_backward_error = std::max(rep->max_backward_error, res.worst);
+        rep->fallbacks = std::max(rep->fallbacks, res.fallbacks);
+        rep->max_iters = std::max(rep->max_iters, res.max_iters);
+        if (res.rc != PALIAL_OK) rep->not_converged = 1;
+    }
+    const double t = percentile(times, 50);
+    rep->seconds = t;
+    rep->matrices_per_s = (double)idx.size() / t;
+    rep->tflops = b.flops / t * 1e-12;
+    if (st) {
+        st->seconds = t;
+        st->tflops = rep->tflops;
+        st->backward_error = rep->max_backward_error;
+    }
+    return set_status(st, rep->not_converged ? PALIAL_ERR_NOT_CONVERGED : PALIAL_OK,
+                      rep->not_converged ? "batched solve above its tolerance" : nullptr);
 }
 
 }  // extern "C"

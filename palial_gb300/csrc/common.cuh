@@ -49,9 +49,13 @@ struct alignas(16) Task {
 };
 static_assert(sizeof(Task) == 48, "Task record layout");
 
-// One matrix of a batched run: its own tile-layout buffer, sizes and counter range.
+// One matrix of a batched run: its own tile-layout buffer, sizes and counter range.  The FP64
+// scheduler reads A; the FP32 scheduler (batched mixed-precision solves) reads Af.
 struct MatInfo {
-    double *A;
+    union {
+        double *A;
+        float *Af;
+    };
     int n, nb, bs;
 };
 
@@ -80,6 +84,7 @@ struct SchedParams {
     int n, nb, bs;              // matrix size, tile size, block size
     unsigned long long timeout_ns;
     const MatInfo *mats;        // batched run: per-matrix buffers and sizes (else nullptr)
+    int *mat_status;            // FP32 batched run: per-matrix breakdown flags (else nullptr)
 };
 
 // Host: count of kernel launches made by the library (every launch wrapper calls this).

@@ -51,6 +51,26 @@ struct SchedCtx {
     }
 };
 
+// One lane of batched launches (FP64 or FP32 tasks): scheduler buffers, the device matrix
+// table and the CUDA graph captured for the last (DAG, table, trace) combination.
+struct BatchLane {
+    SchedCtx ctx;
+    DevBuf mats, flags;
+    cudaGraphExec_t graph = nullptr;
+    unsigned long long graph_uid = 0;
+    const void *graph_mats = nullptr;
+    const void *graph_trace = nullptr;
+    void release() {
+        ctx.release();
+        mats.release();
+        flags.release();
+        if (graph) cudaGraphExecDestroy(graph);
+        graph = nullptr;
+        graph_uid = 0;
+        graph_mats = graph_trace = nullptr;
+    }
+};
+
 struct TraceState {
     Dag dag;
     std::vector<TraceRec> recs;
@@ -62,13 +82,10 @@ struct State {
     int device = -1;
     int sms = 0;
     int occupancy = 1;
-    SchedCtx main, diag, batch;
-    DevBuf batch_mats;
+    int occupancy32 = 1;  // resident CTAs per SM of the FP32 batched scheduler
+    SchedCtx main, diag;
+    BatchLane lane64, lane32;  // batched launches with FP64 / FP32 tasks
     std::map<std::string, std::shared_ptr<Dag>> batch_dags;
-    cudaGraphExec_t batch_graph = nullptr;
-    unsigned long long batch_graph_uid = 0;
-    const void *batch_graph_mats = nullptr;
-    const void *batch_graph_trace = nullptr;
     DevBuf mat, smat, kbuf, probe;
     std::map<std::tuple<int, int, int, int, int, int, unsigned>, std::shared_ptr<Dag>> dags;
     unsigned long long next_uid = 1;
@@ -91,6 +108,8 @@ int fp64_trsolve(int alg, double *W, int n, int nb, const double *v, double *z, 
                  palial_status *st);
 // Free the layout bridges' padded buffers (palial_gpu_finalize).
 void layout_release();
+// Free the batched solves' workspaces (palial_gpu_finalize).
+void batch_solve_release();
 // Free the random butterflies (palial_gpu_finalize).
 void rbt_release();
 
@@ -106,8 +125,15 @@ std::shared_ptr<Dag> get_dag(int alg, int n, int nb, int bs, int priority, int w
 // Prepare a scheduler run (host: DAG upload, buffers) and return its launch parameters.
 int sched_prepare(SchedCtx &c, const std::shared_ptr<Dag> &dag, double *dA, double *dS, int workers, int trace,
                   double timeout_s, SchedParams &p, palial_status *st);
-// Enqueue it (asynchronous): clear counters and ticket (and status if clear_status), launch.
-cudaError_t sched_enqueue(SchedCtx &c, const SchedParams &p, int nobj, int workers, bool clear_status, cudaStream_t s);
+// Enqueue it (asynchronous): clear counters and ticket (and status if clear_status), launch
+// the FP64 scheduler (or the FP32 one of the batched mixed-precision solves when f32).
+cudaError_t sched_enqueue(SchedCtx &c, const SchedParams &p, int nobj, int workers, bool clear_status, cudaStream_t s,
+                          bool f32 = false);
+// One batched persistent launch over `count` matrices, synchronous.  bufs[i]: the matrix's
+// tile-layout buffer, double (FP64 tasks) or float (FP32 tasks: f32 = true).  FP32 runs
+// report breakdowns per matrix in flags (count ints, host; 0 = none) instead of failing.
+int batched_run(int count, const int *algs, const int *ns, const int *nbs, const int *bss, void *const *bufs, bool f32,
+                int *flags, const palial_opts *opts, palial_status *st, double *completion_s, cudaStream_t s);
 
 #define PALIAL_CK(call, what)                                  \
     do {                                                       \

@@ -32,6 +32,10 @@ cudaError_t sched_launch(const SchedParams &p, int grid, cudaStream_t s);
 long long sched_scratch_doubles(int alg, int n, int nb, int bs, int workers, long long *per_worker);
 cudaError_t tile_task_launch(int type, int nb, int ld, double *p0, double *p1, double *p2, double *p3, double *scratch,
                              int *status, cudaStream_t s);
+// sched_f32.cu
+cudaError_t sched32_configure();
+int sched32_occupancy();
+cudaError_t sched32_launch(const SchedParams &p, int grid, cudaStream_t s);
 // gen_check.cu
 cudaError_t launch_gen_uniform(double *A, int n, int nb, uint64_t seed, cudaStream_t s);
 cudaError_t launch_gen_refpattern(double *A, int n, int nb, uint64_t seed, cudaStream_t s);
@@ -154,12 +158,133 @@ int sched_prepare(SchedCtx &c, const std::shared_ptr<Dag> &dag, double *dA, doub
     return PALIAL_OK;
 }
 
-cudaError_t sched_enqueue(SchedCtx &c, const SchedParams &p, int nobj, int workers, bool clear_status, cudaStream_t s) {
+cudaError_t sched_enqueue(SchedCtx &c, const SchedParams &p, int nobj, int workers, bool clear_status, cudaStream_t s,
+                          bool f32) {
     cudaError_t e = cudaMemsetAsync(c.counters.ptr, 0, sizeof(unsigned) * (size_t)(nobj + 1), s);
     if (e == cudaSuccess && clear_status) e = cudaMemsetAsync(c.status.ptr, 0, sizeof(int) * ST_NSLOTS, s);
     if (e == cudaSuccess) e = cudaMemsetAsync(c.ticket.ptr, 0, 64, s);
-    if (e == cudaSuccess) e = sched_launch(p, workers, s);
+    if (e == cudaSuccess) e = f32 ? sched32_launch(p, workers, s) : sched_launch(p, workers, s);
     return e;
+}
+
+int batched_run(int count, const int *algs, const int *ns, const int *nbs, const int *bss, void *const *bufs, bool f32,
+                int *flags, const palial_opts *opts, palial_status *st, double *completion_s, cudaStream_t s) {
+    palial_opts o;
+    palial_opts_default(&o);
+    if (opts) o = *opts;
+    if (count <= 0 || !algs || !ns || !nbs || !bss || !bufs) return set_status(st, PALIAL_ERR_ARG, "empty batch");
+    int rc = ensure_init(st);
+    if (rc) return rc;
+    std::vector<BatchSpec> specs(count);
+    std::string key = std::to_string(o.priority) + ":";
+    double flops = 0;
+    for (int i = 0; i < count; i++) {
+        const int a = algs[i], n = ns[i], nb = nbs[i], bs = bss[i];
+        if ((a != 0 && a != 1) || n <= 0 || nb <= 0 || n % nb || nb % bs || bs % 64 || !bufs[i] ||
+            (f32 && (reinterpret_cast<uintptr_t>(bufs[i]) & 15)))
+            return set_status(st, PALIAL_ERR_ARG, "matrix %d: alg %d n %d nb %d bs %d", i, a, n, nb, bs);
+        specs[i] = BatchSpec{a, n, nb, bs};
+        key += std::to_string(a) + "," + std::to_string(n) + "," + std::to_string(nb) + "," + std::to_string(bs) + ";";
+        flops += algorithmic_flops(a, n);
+    }
+    BatchLane &lane = f32 ? g.lane32 : g.lane64;
+    const int workers = f32 ? g.sms * g.occupancy32 : g.sms;
+    std::shared_ptr<Dag> dag;
+    auto it = g.batch_dags.find(key);
+    if (it != g.batch_dags.end()) {
+        dag = it->second;
+    } else {
+        try {
+            dag = std::make_shared<Dag>(build_batch_dag(specs));
+            order_dag(*dag, o.priority, g.sms, 0);
+        } catch (const std::exception &ex) {
+            return set_status(st, PALIAL_ERR_ARG, "%s", ex.what());
+        }
+        dag->uid = g.next_uid++;
+        if (g.batch_dags.size() > 8) g.batch_dags.clear();
+        g.batch_dags[key] = dag;
+    }
+    std::vector<MatInfo> mats(count);
+    for (int i = 0; i < count; i++) {
+        mats[i] = MatInfo{};
+        if (f32) mats[i].Af = static_cast<float *>(bufs[i]);
+        else mats[i].A = static_cast<double *>(bufs[i]);
+        mats[i].n = ns[i];
+        mats[i].nb = nbs[i];
+        mats[i].bs = bss[i];
+    }
+    PALIAL_CK(lane.mats.ensure(sizeof(MatInfo) * count), "alloc matrix table");
+    PALIAL_CK(cudaMemcpyAsync(lane.mats.ptr, mats.data(), sizeof(MatInfo) * count, cudaMemcpyHostToDevice, s), "upload");
+    if (f32) {
+        PALIAL_CK(lane.flags.ensure(sizeof(int) * (size_t)count), "alloc breakdown flags");
+        PALIAL_CK(cudaMemsetAsync(lane.flags.ptr, 0, sizeof(int) * (size_t)count, s), "clear breakdown flags");
+    }
+    const bool want_trace = o.trace || completion_s;
+    SchedParams p;
+    rc = sched_prepare(lane.ctx, dag, nullptr, nullptr, workers, want_trace, o.timeout_s, p, st);
+    if (rc) return rc;
+    p.mats = lane.mats.as<MatInfo>();
+    p.mat_status = f32 ? lane.flags.as<int>() : nullptr;
+    const bool use_graph = o.reserved[2] == 1;
+    PALIAL_CK(cudaEventRecord(g.ev0, s), "event");
+    if (use_graph) {
+        // one CUDA graph per (DAG, matrix table): counter/ticket/status clears + the launch
+        const void *gkey = want_trace ? (const void *)lane.ctx.trace.ptr : nullptr;
+        if (!lane.graph || lane.graph_uid != dag->uid || lane.graph_mats != lane.mats.ptr || lane.graph_trace != gkey) {
+            if (lane.graph) cudaGraphExecDestroy(lane.graph);
+            lane.graph = nullptr;
+            cudaStream_t cs;
+            PALIAL_CK(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking), "stream");
+            cudaGraph_t graph;
+            PALIAL_CK(cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal), "capture");
+            cudaError_t e = sched_enqueue(lane.ctx, p, dag->nobj, workers, true, cs, f32);
+            cudaError_t e2 = cudaStreamEndCapture(cs, &graph);
+            cudaStreamDestroy(cs);
+            PALIAL_CK(e, "capture enqueue");
+            PALIAL_CK(e2, "end capture");
+            PALIAL_CK(cudaGraphInstantiate(&lane.graph, graph, 0), "instantiate");
+            cudaGraphDestroy(graph);
+            lane.graph_uid = dag->uid;
+            lane.graph_mats = lane.mats.ptr;
+            lane.graph_trace = gkey;
+        }
+        PALIAL_CK(cudaGraphLaunch(lane.graph, s), "graph launch");
+        note_launch();
+    } else {
+        PALIAL_CK(sched_enqueue(lane.ctx, p, dag->nobj, workers, true, s, f32), "launch");
+    }
+    PALIAL_CK(cudaEventRecord(g.ev1, s), "event");
+    PALIAL_CK(cudaEventSynchronize(g.ev1), "batched run");
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, g.ev0, g.ev1);
+    int hs[ST_NSLOTS];
+    PALIAL_CK(cudaMemcpy(hs, lane.ctx.status.ptr, sizeof hs, cudaMemcpyDeviceToHost), "status");
+    if (f32 && flags)
+        PALIAL_CK(cudaMemcpy(flags, lane.flags.ptr, sizeof(int) * (size_t)count, cudaMemcpyDeviceToHost), "flags");
+    if (st) {
+        st->seconds = ms * 1e-3;
+        st->tflops = flops / std::max(1e-12, st->seconds) * 1e-12;
+        st->ntasks = (long long)dag->records.size();
+    }
+    if (want_trace && hs[ST_CODE] == 0) {
+        std::vector<TraceRec> recs(dag->records.size());
+        PALIAL_CK(cudaMemcpy(recs.data(), lane.ctx.trace.ptr, sizeof(TraceRec) * recs.size(), cudaMemcpyDeviceToHost),
+                  "trace");
+        unsigned long long t0 = ~0ull;
+        for (const auto &r : recs) t0 = std::min(t0, r.t0);
+        if (completion_s) {
+            for (int i = 0; i < count; i++) completion_s[i] = 0;
+            for (size_t r = 0; r < recs.size(); r++) {
+                const uint32_t m = dag->records[r].mat;
+                completion_s[m] = std::max(completion_s[m], (double)(recs[r].t1 - t0) * 1e-9);
+            }
+        }
+    }
+    if (hs[ST_CODE] == PALIAL_ERR_NOT_SPD)
+        return set_status(st, PALIAL_ERR_NOT_SPD, "non-positive pivot in a batched Cholesky");
+    if (hs[ST_CODE] != 0) return set_status(st, hs[ST_CODE], "device error %d", hs[ST_CODE]);
+    if (hs[ST_ZEROPIV]) return set_status(st, PALIAL_WARN_ZERO_PIVOT, "exact zero pivot skipped");
+    return set_status(st, PALIAL_OK);
 }
 }  // namespace palial
 
@@ -205,7 +330,9 @@ int palial_gpu_init(int device) {
     if (mps_configure() != cudaSuccess) return PALIAL_ERR_CUDA;
     if (mpd_configure() != cudaSuccess) return PALIAL_ERR_CUDA;
     if (mpr_configure() != cudaSuccess) return PALIAL_ERR_CUDA;
+    if (sched32_configure() != cudaSuccess) return PALIAL_ERR_CUDA;
     g.occupancy = std::max(1, sched_occupancy());
+    g.occupancy32 = std::max(1, sched32_occupancy());
     if (!g.ev0) cudaEventCreate(&g.ev0);
     if (!g.ev1) cudaEventCreate(&g.ev1);
     g.init = true;
@@ -216,11 +343,10 @@ int palial_gpu_finalize(void) {
     if (!g.init) return PALIAL_OK;
     g.main.release();
     g.diag.release();
-    g.batch.release();
-    g.batch_mats.release();
+    g.lane64.release();
+    g.lane32.release();
     g.batch_dags.clear();
-    if (g.batch_graph) cudaGraphExecDestroy(g.batch_graph);
-    g.batch_graph = nullptr;
+    batch_solve_release();
     for (DevBuf *b : {&g.mat, &g.smat, &g.kbuf, &g.probe}) b->release();
     qr_solve_release();
     mpr_release();
@@ -561,107 +687,22 @@ int palial_gpu_gen_batch_matrix(double *dA, int kind, int n_true, int n_pad, int
 
 int palial_gpu_batched(int count, const int *algs, const int *ns, const int *nbs, const int *bss, double *const *dA,
                        const palial_opts *opts, palial_status *st, double *completion_s, void *stream) {
-    palial_opts o;
-    palial_opts_default(&o);
-    if (opts) o = *opts;
     if (st) memset(st, 0, sizeof *st);
     if (count <= 0 || !algs || !ns || !nbs || !bss || !dA) return set_status(st, PALIAL_ERR_ARG, "empty batch");
-    int rc = ensure_init(st);
-    if (rc) return rc;
-    std::vector<BatchSpec> specs(count);
-    std::string key = std::to_string(o.priority) + ":";
-    double flops = 0;
-    for (int i = 0; i < count; i++) {
-        const int a = algs[i], n = ns[i], nb = nbs[i], bs = bss[i];
-        if ((a != 0 && a != 1) || n <= 0 || nb <= 0 || n % nb || nb % bs || bs % 64 || !dA[i])
-            return set_status(st, PALIAL_ERR_ARG, "matrix %d: alg %d n %d nb %d bs %d", i, a, n, nb, bs);
-        specs[i] = BatchSpec{a, n, nb, bs};
-        key += std::to_string(a) + "," + std::to_string(n) + "," + std::to_string(nb) + "," + std::to_string(bs) + ";";
-        flops += algorithmic_flops(a, n);
-    }
-    std::shared_ptr<Dag> dag;
-    auto it = g.batch_dags.find(key);
-    if (it != g.batch_dags.end()) {
-        dag = it->second;
-    } else {
-        try {
-            dag = std::make_shared<Dag>(build_batch_dag(specs));
-            order_dag(*dag, o.priority, g.sms, 0);
-        } catch (const std::exception &ex) {
-            return set_status(st, PALIAL_ERR_ARG, "%s", ex.what());
-        }
-        dag->uid = g.next_uid++;
-        if (g.batch_dags.size() > 8) g.batch_dags.clear();
-        g.batch_dags[key] = dag;
-    }
-    std::vector<MatInfo> mats(count);
-    for (int i = 0; i < count; i++) mats[i] = MatInfo{dA[i], ns[i], nbs[i], bss[i]};
-    CK(g.batch_mats.ensure(sizeof(MatInfo) * count), "alloc matrix table");
-    cudaStream_t s = static_cast<cudaStream_t>(stream);
-    CK(cudaMemcpyAsync(g.batch_mats.ptr, mats.data(), sizeof(MatInfo) * count, cudaMemcpyHostToDevice, s), "upload");
-    const bool want_trace = o.trace || completion_s;
-    SchedParams p;
-    rc = sched_prepare(g.batch, dag, nullptr, nullptr, g.sms, want_trace, o.timeout_s, p, st);
-    if (rc) return rc;
-    p.mats = g.batch_mats.as<MatInfo>();
-    const bool use_graph = o.reserved[2] == 1;
-    CK(cudaEventRecord(g.ev0, s), "event");
-    if (use_graph) {
-        // one CUDA graph per (DAG, matrix table): counter/ticket/status clears + the launch
-        const void *gkey = want_trace ? (const void *)g.batch.trace.ptr : nullptr;
-        if (!g.batch_graph || g.batch_graph_uid != dag->uid || g.batch_graph_mats != g.batch_mats.ptr ||
-            g.batch_graph_trace != gkey) {
-            if (g.batch_graph) cudaGraphExecDestroy(g.batch_graph);
-            g.batch_graph = nullptr;
-            cudaStream_t cs;
-            CK(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking), "stream");
-            cudaGraph_t graph;
-            CK(cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal), "capture");
-            cudaError_t e = sched_enqueue(g.batch, p, dag->nobj, g.sms, true, cs);
-            cudaError_t e2 = cudaStreamEndCapture(cs, &graph);
-            cudaStreamDestroy(cs);
-            CK(e, "capture enqueue");
-            CK(e2, "end capture");
-            CK(cudaGraphInstantiate(&g.batch_graph, graph, 0), "instantiate");
-            cudaGraphDestroy(graph);
-            g.batch_graph_uid = dag->uid;
-            g.batch_graph_mats = g.batch_mats.ptr;
-            g.batch_graph_trace = gkey;
-        }
-        CK(cudaGraphLaunch(g.batch_graph, s), "graph launch");
-        note_launch();
-    } else {
-        CK(sched_enqueue(g.batch, p, dag->nobj, g.sms, true, s), "launch");
-    }
-    CK(cudaEventRecord(g.ev1, s), "event");
-    CK(cudaEventSynchronize(g.ev1), "batched run");
-    float ms = 0.f;
-    cudaEventElapsedTime(&ms, g.ev0, g.ev1);
-    int hs[ST_NSLOTS];
-    CK(cudaMemcpy(hs, g.batch.status.ptr, sizeof hs, cudaMemcpyDeviceToHost), "status");
-    if (st) {
-        st->seconds = ms * 1e-3;
-        st->tflops = flops / std::max(1e-12, st->seconds) * 1e-12;
-        st->ntasks = (long long)dag->records.size();
-    }
-    if (want_trace && hs[ST_CODE] == 0) {
-        std::vector<TraceRec> recs(dag->records.size());
-        CK(cudaMemcpy(recs.data(), g.batch.trace.ptr, sizeof(TraceRec) * recs.size(), cudaMemcpyDeviceToHost), "trace");
-        unsigned long long t0 = ~0ull;
-        for (const auto &r : recs) t0 = std::min(t0, r.t0);
-        if (completion_s) {
-            for (int i = 0; i < count; i++) completion_s[i] = 0;
-            for (size_t r = 0; r < recs.size(); r++) {
-                const uint32_t m = dag->records[r].mat;
-                completion_s[m] = std::max(completion_s[m], (double)(recs[r].t1 - t0) * 1e-9);
-            }
-        }
-    }
-    if (hs[ST_CODE] == PALIAL_ERR_NOT_SPD)
-        return set_status(st, PALIAL_ERR_NOT_SPD, "non-positive pivot in a batched Cholesky");
-    if (hs[ST_CODE] != 0) return set_status(st, hs[ST_CODE], "device error %d", hs[ST_CODE]);
-    if (hs[ST_ZEROPIV]) return set_status(st, PALIAL_WARN_ZERO_PIVOT, "exact zero pivot skipped");
-    return set_status(st, PALIAL_OK);
+    return batched_run(count, algs, ns, nbs, bss, reinterpret_cast<void *const *>(dA), false, nullptr, opts, st,
+                       completion_s, static_cast<cudaStream_t>(stream));
+}
+
+int palial_gpu_batched_f32(int count, const int *algs, const int *ns, const int *nbs, const int *bss, float *const *dA,
+                           int *breakdown, const palial_opts *opts, palial_status *st, double *completion_s,
+                           void *stream) {
+    if (st) memset(st, 0, sizeof *st);
+    if (count <= 0 || !algs || !ns || !nbs || !bss || !dA) return set_status(st, PALIAL_ERR_ARG, "empty batch");
+    std::vector<int> flags(count, 0);
+    const int rc = batched_run(count, algs, ns, nbs, bss, reinterpret_cast<void *const *>(dA), true, flags.data(), opts,
+                               st, completion_s, static_cast<cudaStream_t>(stream));
+    if (breakdown) std::copy(flags.begin(), flags.end(), breakdown);
+    return rc;
 }
 
 // ---- trace ----------------------------------------------------------------------------------
