@@ -1,7 +1,7 @@
 """Benchmark: tiled Cholesky at N = 32768, NB = 512 on one GB300 (per GPU).
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-                    [--suite fp64|kappa|batched|costmodel|kernels]
+                    [--suite fp64|kappa|batched|batched_solve|costmodel|kernels]
 
 A step is one solve A X = B (16 right-hand sides, uniform [-1, 1)) of a device-resident
 SPD matrix A = B B^T + N I (seed = rank; the reference's tile layout) by the mixed-precision
@@ -33,7 +33,8 @@ precision at N = 32768 (A = U diag(s) V^T, 64 Householder reflectors each side);
 `--suite kernels [--n N]` times the dominant kernels alone (the small case ncu captures run).
 `--suite batched` factors the uneven batch (2000 matrices, N log-uniform in [32, 2048)) in one
 FP64 launch, then times batched solves of it: FP64 factorizations vs block size and precision
-(FP32 + FP64 refinement, or FP64) autotuned per algorithm and size class.
+(FP32 + FP64 refinement, or FP64) autotuned per algorithm and size class; `--suite
+batched_solve` runs the solves alone (FP64 with the FP64 autotuner's measured block sizes).
 """
 from __future__ import annotations
 
@@ -51,6 +52,8 @@ sys.path.insert(0, ROOT)
 
 N, NB = 32768, 512
 CPU_N = 16384
+# block per size class that the FP64 batched autotuner picks on the synthetic batch (measured)
+FP64_BATCH_BLOCKS = (64, 128, 64, 64, 64, 64)
 METRIC = "TFLOP/s Cholesky/LU/QR N=32768: mixed-prec+IR vs FP64 tiled, both at FP64 acc"
 
 
@@ -304,18 +307,19 @@ def run_batched_solve(args, bs_fp64, count: int, world: int) -> None:
                              bs12=list(bs_fp64) * 2, prec12=[0] * 12, reps=reps)
     mixed = B.solve_synthetic(args.batch, seed=2, rank=0, world=world, autotune=True, reps=reps)
     prec_name = {0: "fp64", 1: "fp32+ir"}
+    phases = ("factor", "refine", "fp64_fallback")
     choice = {f"{('cholesky', 'lu')[k // 6]} {B.class_label(k % 6)}":
               {"block": mixed["bs_of_class"][k], "precision": prec_name[mixed["prec_of_class"][k]]}
               for k in range(12)}
     print(json.dumps({"suite": "batched_solve", "matrices": count, "n_gpus": world, "rank0_matrices": mixed["count"],
                       "fp64": {"seconds": fp64["seconds"], "matrices_per_s": fp64["matrices_per_s"],
                                "tflops": fp64["tflops"], "max_backward_error": fp64["max_backward_error"],
-                               "converged": fp64["rc"] == 0},
+                               "converged": fp64["rc"] == 0, "phases_s": dict(zip(phases, fp64["phase_seconds"]))},
                       "mixed": {"seconds": mixed["seconds"], "matrices_per_s": mixed["matrices_per_s"],
                                 "tflops": mixed["tflops"], "max_backward_error": mixed["max_backward_error"],
                                 "max_refinement_steps": mixed["max_iters"], "fp64_fallbacks": mixed["fallbacks"],
                                 "converged": mixed["rc"] == 0, "autotune_seconds": mixed["autotune_seconds"],
-                                "choice": choice},
+                                "phases_s": dict(zip(phases, mixed["phase_seconds"])), "choice": choice},
                       "speedup_mixed_vs_fp64": fp64["seconds"] / mixed["seconds"]}), flush=True)
 
 
@@ -444,6 +448,9 @@ def run_suite(args, P, torch) -> None:
     if args.suite == "batched":
         run_batched(args, P, torch)
         return
+    if args.suite == "batched_solve":
+        run_batched_solve(args, FP64_BATCH_BLOCKS, args.batch, 1)
+        return
     if args.suite == "fp64":
         for alg in ("cholesky", "lu", "qr"):
             for n in ((4096, 16384, 32768) if alg == "cholesky" else (16384, 32768)):
@@ -499,7 +506,8 @@ def main() -> None:
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--n", type=int, default=N)
     ap.add_argument("--precision", default="bf16x3")
-    ap.add_argument("--suite", default=None, choices=[None, "fp64", "kappa", "batched", "costmodel", "kernels"])
+    ap.add_argument("--suite", default=None, choices=[None, "fp64", "kappa", "batched", "batched_solve", "costmodel",
+                                                      "kernels"])
     ap.add_argument("--batch", type=int, default=2000)
     ap.add_argument("--no-fp64", action="store_true")
     args = ap.parse_args()
@@ -523,6 +531,10 @@ def main() -> None:
     P.init(local)
     if args.suite == "batched":
         run_batched(args, P, torch, rank, world)
+        return
+    if args.suite == "batched_solve":
+        if rank == 0:
+            run_batched_solve(args, FP64_BATCH_BLOCKS, args.batch, world)
         return
     if args.suite:
         if rank == 0:

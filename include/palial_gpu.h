@@ -332,6 +332,8 @@ typedef struct palial_batch_solve_report {
     double autotune_seconds;
     double autotune_s[72];    /* [alg*6 + class][precision 0,1][block 64,128,256] seconds;
                                  -1 = not run, -2 = did not reach the tolerance              */
+    double phase_seconds[3];  /* median run: copies + first factorizations, refinement,
+                                 FP64 fallback (copies, factorization, refinement)           */
 } palial_batch_solve_report;
 /* Per (algorithm, size class), time the class's matrices alone with every block size (64,
  * 128, 256 where it fits) and both precisions, and keep the fastest choice that reaches the

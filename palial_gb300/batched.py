@@ -35,7 +35,7 @@ class SolveReport(ctypes.Structure):
                 ("fallbacks", ctypes.c_int), ("max_iters", ctypes.c_int), ("not_converged", ctypes.c_int),
                 ("seconds", ctypes.c_double), ("matrices_per_s", ctypes.c_double), ("tflops", ctypes.c_double),
                 ("max_backward_error", ctypes.c_double), ("autotune_seconds", ctypes.c_double),
-                ("autotune_s", ctypes.c_double * 72)]
+                ("autotune_s", ctypes.c_double * 72), ("phase_seconds", ctypes.c_double * 3)]
 
 
 class BatchReport(ctypes.Structure):
@@ -239,7 +239,7 @@ def solve_synthetic(count: int = 2000, seed: int = 2, rank: int = 0, world: int 
     if rc and rc != -6:
         raise PalialError(rc, st.message.decode(errors="replace"))
     out = {f: getattr(rep, f) for f, _ in SolveReport._fields_}
-    for f in ("bs_of_class", "prec_of_class", "autotune_s"):
+    for f in ("bs_of_class", "prec_of_class", "autotune_s", "phase_seconds"):
         out[f] = list(out[f])
     out["rc"] = rc
     return out

@@ -142,7 +142,7 @@ int make_solve_batch(SolveBatch &b, const std::vector<int> &idx, const std::vect
 }
 
 struct SolveResult {
-    double seconds = 0, worst = 0;
+    double seconds = 0, worst = 0, phases[3] = {0, 0, 0};
     int fallbacks = 0, max_iters = 0, rc = 0;
 };
 
@@ -152,8 +152,8 @@ int run_solve_batch(SolveBatch &b, const palial_opts &o, SolveResult &res, palia
     std::vector<double> berr(count);
     for (int j = 0; j < count; j++) prec[j] = b.prec[j] ? PALIAL_PREC_FP32 : PALIAL_PREC_FP64;
     palial_status s2;
-    const int rc = palial_gpu_batched_solve(count, b.algs.data(), b.np.data(), b.bs.data(), b.A.data(), b.B.data(),
-                                            b.X.data(), prec.data(), &o, &s2, iters.data(), berr.data(), nullptr);
+    const int rc = batched_solve_run(count, b.algs.data(), b.np.data(), b.bs.data(), b.A.data(), b.B.data(),
+                                     b.X.data(), prec.data(), &o, &s2, iters.data(), berr.data(), res.phases, nullptr);
     if (rc < 0 && rc != PALIAL_ERR_NOT_CONVERGED) return set_status(st, rc, "batched solve: %s", s2.message);
     res.rc = rc;
     res.seconds = s2.seconds;
@@ -420,9 +420,11 @@ int palial_gpu_batch_solve_synthetic(int count, uint64_t seed, int rank, int wor
     rc = run_solve_batch(b, o, res, st);  // warm-up (allocations, DAGs)
     if (rc) return rc;
     std::vector<double> times;
+    std::vector<SolveResult> runs;
     for (int r = 0; r < std::max(1, reps); r++) {
         rc = run_solve_batch(b, o, res, st);
         if (rc) return rc;
+        runs.push_back(res);
         times.push_back(res.seconds);
         rep->max_backward_error = std::max(rep->max_backward_error, res.worst);
         rep->fallbacks = std::max(rep->fallbacks, res.fallbacks);
@@ -433,6 +435,11 @@ int palial_gpu_batch_solve_synthetic(int count, uint64_t seed, int rank, int wor
     rep->seconds = t;
     rep->matrices_per_s = (double)idx.size() / t;
     rep->tflops = b.flops / t * 1e-12;
+    // phases of the run closest to the median
+    size_t med = 0;
+    for (size_t r = 1; r < runs.size(); r++)
+        if (std::fabs(runs[r].seconds - t) < std::fabs(runs[med].seconds - t)) med = r;
+    for (int q = 0; q < 3; q++) rep->phase_seconds[q] = runs[med].phases[q];
     if (st) {
         st->seconds = t;
         st->tflops = rep->tflops;

@@ -513,16 +513,13 @@ void batch_solve_release() {
     for (DevBuf *b : {&w32, &w64, &w64b, &wr, &wnorm, &wmats, &wjobs, &wfirst, &wcopy}) b->release();
 }
 
-}  // namespace palial
-
-using namespace palial;
-
-extern "C" {
-
-int palial_gpu_batched_solve(int count, const int *algs, const int *ns, const int *nbs, const double *const *dA,
-                             const double *const *dB, double *const *dX, const int *precs, const palial_opts *opts,
-                             palial_status *st, int *iters, double *berr, void *stream) {
+int batched_solve_run(int count, const int *algs, const int *ns, const int *nbs, const double *const *dA,
+                      const double *const *dB, double *const *dX, const int *precs, const palial_opts *opts,
+                      palial_status *st, int *iters, double *berr, double *phases, void *stream) {
     if (st) memset(st, 0, sizeof *st);
+    double ph[3] = {0, 0, 0};
+    if (!phases) phases = ph;
+    for (int i = 0; i < 3; i++) phases[i] = 0;
     if (count <= 0 || !algs || !ns || !nbs || !dA || !dB || !dX) return set_status(st, PALIAL_ERR_ARG, "empty batch");
     for (int i = 0; i < count; i++) {
         const int p = precs ? precs[i] : PALIAL_PREC_FP32;
@@ -594,11 +591,15 @@ int palial_gpu_batched_solve(int count, const int *algs, const int *ns, const in
     if (rc) return rc;
     rc = sv.factor(m64, false);
     if (rc) return rc;
+    const auto t1 = std::chrono::steady_clock::now();
+    phases[0] = std::chrono::duration<double>(t1 - t0).count();
     std::vector<int> run;
     for (int i = 0; i < count; i++)
         if (sv.state[i] == 0) run.push_back(i);
     rc = sv.refine(run, max_iter);
     if (rc) return rc;
+    const auto t2 = std::chrono::steady_clock::now();
+    phases[1] = std::chrono::duration<double>(t2 - t1).count();
 
     // fallback phase: FP32 matrices that broke down or did not converge, refactored in FP64
     std::vector<int> fb;
@@ -631,7 +632,9 @@ int palial_gpu_batched_solve(int count, const int *algs, const int *ns, const in
         if (rc) return rc;
     }
     PALIAL_CK(cudaStreamSynchronize(s), "batched solve");
-    const double wall = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    const auto t3 = std::chrono::steady_clock::now();
+    phases[2] = std::chrono::duration<double>(t3 - t2).count();
+    const double wall = std::chrono::duration<double>(t3 - t0).count();
 
     int not_conv = 0, max_it = 0;
     double worst = 0, flops = 0;
@@ -656,6 +659,18 @@ int palial_gpu_batched_solve(int count, const int *algs, const int *ns, const in
         return set_status(st, PALIAL_ERR_NOT_CONVERGED, "%d of %d matrices above their tolerance (worst %.3g)",
                           not_conv, count, worst);
     return set_status(st, PALIAL_OK);
+}
+
+}  // namespace palial
+
+using namespace palial;
+
+extern "C" {
+
+int palial_gpu_batched_solve(int count, const int *algs, const int *ns, const int *nbs, const double *const *dA,
+                             const double *const *dB, double *const *dX, const int *precs, const palial_opts *opts,
+                             palial_status *st, int *iters, double *berr, void *stream) {
+    return batched_solve_run(count, algs, ns, nbs, dA, dB, dX, precs, opts, st, iters, berr, nullptr, stream);
 }
 
 }  // extern "C"

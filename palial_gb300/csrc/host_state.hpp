@@ -110,6 +110,11 @@ int fp64_trsolve(int alg, double *W, int n, int nb, const double *v, double *z, 
 void layout_release();
 // Free the batched solves' workspaces (palial_gpu_finalize).
 void batch_solve_release();
+// palial_gpu_batched_solve with the wall time of its phases (phases[3], optional): copies and
+// first factorizations, refinement, FP64 fallback (copies, factorization, refinement).
+int batched_solve_run(int count, const int *algs, const int *ns, const int *nbs, const double *const *dA,
+                      const double *const *dB, double *const *dX, const int *precs, const palial_opts *opts,
+                      palial_status *st, int *iters, double *berr, double *phases, void *stream);
 // Free the random butterflies (palial_gpu_finalize).
 void rbt_release();
 
