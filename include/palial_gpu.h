@@ -268,7 +268,8 @@ int palial_gpu_batched_f32(int count, const int *algs, const int *ns, const int 
 /* ---- batched solves (no reference counterpart) ------------------------------------------
  * A_i x_i = b_i for `count` independent matrices to FP64-level normwise backward error
  * |r|/(|A||x| + |b|) <= opts->ir_tol (0: 1e-14 * n_i), infinity norms.  Matrix i: device
- * tile-layout buffer dA[i] (n = ns[i] <= 4096, tile nbs[i] = scheduler block, a multiple of 64
+ * tile-layout buffer dA[i] holding the full matrix (both triangles, also for Cholesky: the
+ * residuals read all of it; n = ns[i] <= 4096, tile nbs[i] = scheduler block, a multiple of 64
  * dividing n; 16-byte aligned; not modified), right-hand side dB[i] and solution dX[i] (n
  * doubles each).  precs[i] (NULL: all FP32): PALIAL_PREC_FP32 = the matrix is rounded to FP32
  * and factored with the other FP32 matrices in ONE persistent launch, then refined with FP64

@@ -511,6 +511,7 @@ struct Solver {
 
 void batch_solve_release() {
     for (DevBuf *b : {&w32, &w64, &w64b, &wr, &wnorm, &wmats, &wjobs, &wfirst, &wcopy}) b->release();
+    g_configured = false;  // a later init (possibly another device) sets the attributes again
 }
 
 int batched_solve_run(int count, const int *algs, const int *ns, const int *nbs, const double *const *dA,
