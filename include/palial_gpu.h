@@ -184,6 +184,17 @@ int palial_gpu_mp_update_step(int alg, int precision, float *dW, int n, int nb, 
  * to the trailing tiles) followed by the blocked back-substitution with R. */
 int palial_gpu_qr_solve(int rows, int cols, int nb, const double *dA, const double *dB, double *dX, int nrhs,
                         double *dResid, const palial_opts *opts, palial_status *st, void *stream);
+/* Mixed-precision QR solve of a square system A X = B (n x n, nrhs <= 16; device buffers, A
+ * not modified): the flat-tree TS QR of the reference (the same GEQRT/TSQRT/UNMQR/TSMQR task
+ * DAG and R/V/T layout) computed in FP32 by the FP32 task scheduler, then FP64 refinement
+ * X += |R| R_f^-1 Q_f^T (R / |R|) with R = B - A X in FP64, until every column's normwise
+ * backward error |r_j|/(|A||x_j| + |b_j|) <= opts->ir_tol (0: 1e-14 * n).  NB: a multiple of
+ * 64 up to 512.  A refinement that does not halve the error per step (or exceeds
+ * opts->ir_max_iter, 0 = 30) hands the system to palial_gpu_qr_solve (FP64).  status:
+ * ir_iters, backward_error, factor_seconds, kappa_est = the precision that produced the
+ * result (PALIAL_PREC_FP32 or PALIAL_PREC_FP64). */
+int palial_gpu_qr_solve_ir(int n, int nb, const double *dA, const double *dB, double *dX, int nrhs,
+                           const palial_opts *opts, palial_status *st, void *stream);
 /* Same with host buffers (A in tile layout, B and X column-major, resid optional). */
 int palial_gpu_qr_solve_host(int rows, int cols, int nb, const double *A, const double *B, double *X, int nrhs,
                              double *resid, const palial_opts *opts, palial_status *st);
@@ -421,6 +432,10 @@ long long palial_dag_info(int alg, int n, int nb, int block, int priority, int n
  * sides); returns its number of task records, or -1 with the reason in msg.  type_counts
  * (optional, 16 entries) receives the logical task count per type. */
 long long palial_dag_qr_solve_validate(int rows, int cols, int nb, int nrhs, int nworkers, unsigned int seed,
+                                       long long *type_counts, char *msg, int msglen);
+/* The same for the apply-only QR solve DAG of the mixed-precision QR refinement (square n x n:
+ * Q^T on the extra tile column and the back-substitution, the factors already in place). */
+long long palial_dag_qr_apply_validate(int n, int nb, int nrhs, int nworkers, unsigned int seed,
                                        long long *type_counts, char *msg, int msglen);
 /* Validate a built DAG on the host: every wait is satisfiable by earlier tasks in dispatch
  * order, updates to each object are totally ordered, no read/write race; then emulate the

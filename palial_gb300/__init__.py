@@ -122,6 +122,10 @@ def lib() -> ctypes.CDLL:
         h.palial_dag_qr_solve_validate.restype = ctypes.c_longlong
         h.palial_dag_qr_solve_validate.argtypes = [i, i, i, i, i, ctypes.c_uint, ctypes.POINTER(ctypes.c_longlong),
                                                    ctypes.c_char_p, i]
+        h.palial_dag_qr_apply_validate.restype = ctypes.c_longlong
+        h.palial_dag_qr_apply_validate.argtypes = [i, i, i, i, ctypes.c_uint, ctypes.POINTER(ctypes.c_longlong),
+                                                   ctypes.c_char_p, i]
+        h.palial_gpu_qr_solve_ir.argtypes = [i, i, vp, vp, vp, i, ctypes.POINTER(Opts), ctypes.POINTER(Status), vp]
         h.palial_gpu_batch_sizes.argtypes = [i, ctypes.c_uint64, vp, vp]
         h.palial_gpu_batch_partition.argtypes = [i, vp, vp, i, vp]
         h.palial_gpu_batch_autotune.argtypes = [i, vp, vp, ctypes.c_uint64, i, vp, vp, ctypes.POINTER(Status)]
@@ -298,6 +302,28 @@ def qr_solve_dag(rows: int, cols: int, nb: int, nrhs: int, nworkers: int = 152, 
     msg = ctypes.create_string_buffer(256)
     nrec = lib().palial_dag_qr_solve_validate(rows, cols, nb, nrhs, nworkers, seed, counts, msg, 256)
     return {"records": nrec, "type_counts": list(counts), "message": msg.value.decode()}
+
+
+def qr_apply_dag(n: int, nb: int, nrhs: int, nworkers: int = 152, seed: int = 0) -> dict:
+    """Host only: build and validate the apply-only QR solve DAG of the mixed-precision QR
+    refinement (Q^T and R^-1 on the extra tile column); records and logical task counts."""
+    counts = (ctypes.c_longlong * 16)()
+    msg = ctypes.create_string_buffer(256)
+    nrec = lib().palial_dag_qr_apply_validate(n, nb, nrhs, nworkers, seed, counts, msg, 256)
+    return {"records": nrec, "type_counts": list(counts), "message": msg.value.decode()}
+
+
+def qr_solve_ir(d_a: int, n: int, nb: int, d_b: int, d_x: int, nrhs: int, stream: int = 0,
+                allow_not_converged: bool = False, **kw) -> Status:
+    """Mixed-precision QR solve of a square A X = B on device buffers (A tile layout, B and X
+    n x nrhs column-major): FP32 tile QR + FP64 refinement, the FP64 QR solve when the
+    refinement stalls.  status.kappa_est = the precision that produced X (5 FP32, 0 FP64)."""
+    st = Status()
+    rc = lib().palial_gpu_qr_solve_ir(n, nb, d_a, d_b, d_x, nrhs, ctypes.byref(make_opts(**kw)), ctypes.byref(st),
+                                      stream or None)
+    _check(rc, st, allow=(PALIAL_OK, -6) if allow_not_converged else (PALIAL_OK,))
+    st.code = rc
+    return st
 
 
 def mp_factor(alg: str, d_a: int, d_w: int, n: int, nb: int, stream: int = 0, **kw) -> Status:

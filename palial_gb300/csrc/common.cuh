@@ -85,6 +85,8 @@ struct SchedParams {
     unsigned long long timeout_ns;
     const MatInfo *mats;        // batched run: per-matrix buffers and sizes (else nullptr)
     int *mat_status;            // FP32 batched run: per-matrix breakdown flags (else nullptr)
+    float *Af, *Sf;             // FP32 scheduler on one matrix: factors and QR T factors
+    float *scratch_f;           // FP32 scheduler: per-worker scratch (scratch_per_worker floats)
 };
 
 // Host: count of kernel launches made by the library (every launch wrapper calls this).

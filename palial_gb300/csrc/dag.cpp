@@ -132,7 +132,7 @@ Dag build_dag(int alg, int n, int nb, int bs, const double *costs) {
     return d;
 }
 
-Dag build_qr_solve_dag(int rows, int cols, int nb, int nrhs) {
+Dag build_qr_solve_dag(int rows, int cols, int nb, int nrhs, bool apply_only) {
     Dag d;
     d.alg = 3;
     d.n = rows;
@@ -148,13 +148,17 @@ Dag build_qr_solve_dag(int rows, int cols, int nb, int nrhs) {
     auto obj = [mt](int i, int j) { return (uint32_t)(i + j * mt); };
     Builder b(d, mt * (nt + 1));
     for (int k = 0; k < nt; k++) {
-        b.emit(T_GEQRT, k, k, k, 1, {}, {obj(k, k)}, nullptr);
-        for (int j = k + 1; j < nt; j++) b.emit(T_UNMQR, k, 0, j, parts, {obj(k, k)}, {obj(k, j)}, nullptr);
+        if (!apply_only) {
+            b.emit(T_GEQRT, k, k, k, 1, {}, {obj(k, k)}, nullptr);
+            for (int j = k + 1; j < nt; j++) b.emit(T_UNMQR, k, 0, j, parts, {obj(k, k)}, {obj(k, j)}, nullptr);
+        }
         b.emit(T_UNMQR, k, 0, nt, rparts, {obj(k, k)}, {obj(k, nt)}, nullptr);
         for (int m = k + 1; m < mt; m++) {
-            b.emit(T_TSQRT, k, m, 0, 1, {}, {obj(k, k), obj(m, k)}, nullptr);
-            for (int j = k + 1; j < nt; j++)
-                b.emit(T_TSMQR, k, m, j, parts, {obj(m, k)}, {obj(k, j), obj(m, j)}, nullptr);
+            if (!apply_only) {
+                b.emit(T_TSQRT, k, m, 0, 1, {}, {obj(k, k), obj(m, k)}, nullptr);
+                for (int j = k + 1; j < nt; j++)
+                    b.emit(T_TSMQR, k, m, j, parts, {obj(m, k)}, {obj(k, j), obj(m, j)}, nullptr);
+            }
             b.emit(T_TSMQR, k, m, nt, rparts, {obj(m, k)}, {obj(k, nt), obj(m, nt)}, nullptr);
         }
     }

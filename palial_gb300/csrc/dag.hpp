@@ -48,8 +48,10 @@ Dag build_dag(int alg, int n, int nb, int bs, const double *costs = nullptr);
 // (rows >= cols, both multiples of nb) extended by one tile column holding nrhs <= nb
 // right-hand sides (tile column cols/nb of the rows x (cols + nb) tile layout), so the
 // UNMQR/TSMQR tasks apply Q^T to them inside the same launch; then the blocked
-// back-substitution R X = (Q^T B)(0:cols) with left-upper TRSM and GEMM tasks.
-Dag build_qr_solve_dag(int rows, int cols, int nb, int nrhs);
+// back-substitution R X = (Q^T B)(0:cols) with left-upper TRSM and GEMM tasks.  apply_only:
+// the factors are already in place; only Q^T B and the back-substitution are emitted (the
+// refinement steps of the mixed-precision QR solve).
+Dag build_qr_solve_dag(int rows, int cols, int nb, int nrhs, bool apply_only = false);
 // A X = B with the FP64 factors of a Cholesky (alg 0, U^T U) or no-pivot LU (alg 1) in the first
 // n / nb tile columns of an n x (n + nb) tile matrix whose last tile column holds B (nrhs <= nb
 // columns): forward substitution tasks (TRSM + GEMM on the extra column), then backward.

@@ -82,7 +82,8 @@ struct State {
     int device = -1;
     int sms = 0;
     int occupancy = 1;
-    int occupancy32 = 1;  // resident CTAs per SM of the FP32 batched scheduler
+    int occupancy32 = 1;     // resident CTAs per SM of the FP32 batched scheduler
+    int occupancy32_qr = 1;  // of the FP32 scheduler's one-matrix QR instance
     SchedCtx main, diag;
     BatchLane lane64, lane32;  // batched launches with FP64 / FP32 tasks
     std::map<std::string, std::shared_ptr<Dag>> batch_dags;
@@ -110,6 +111,8 @@ int fp64_trsolve(int alg, double *W, int n, int nb, const double *v, double *z, 
 void layout_release();
 // Free the batched solves' workspaces (palial_gpu_finalize).
 void batch_solve_release();
+// Free the mixed-precision QR solve's buffers and DAGs (palial_gpu_finalize).
+void mp_qr_release();
 // palial_gpu_batched_solve with the wall time of its phases (phases[3], optional): copies and
 // first factorizations, refinement, FP64 fallback (copies, factorization, refinement).
 int batched_solve_run(int count, const int *algs, const int *ns, const int *nbs, const double *const *dA,

@@ -34,7 +34,7 @@ cudaError_t tile_task_launch(int type, int nb, int ld, double *p0, double *p1, d
                              int *status, cudaStream_t s);
 // sched_f32.cu
 cudaError_t sched32_configure();
-int sched32_occupancy();
+int sched32_occupancy(bool qr);
 cudaError_t sched32_launch(const SchedParams &p, int grid, cudaStream_t s);
 // gen_check.cu
 cudaError_t launch_gen_uniform(double *A, int n, int nb, uint64_t seed, cudaStream_t s);
@@ -332,7 +332,8 @@ int palial_gpu_init(int device) {
     if (mpr_configure() != cudaSuccess) return PALIAL_ERR_CUDA;
     if (sched32_configure() != cudaSuccess) return PALIAL_ERR_CUDA;
     g.occupancy = std::max(1, sched_occupancy());
-    g.occupancy32 = std::max(1, sched32_occupancy());
+    g.occupancy32 = std::max(1, sched32_occupancy(false));
+    g.occupancy32_qr = std::max(1, sched32_occupancy(true));
     if (!g.ev0) cudaEventCreate(&g.ev0);
     if (!g.ev1) cudaEventCreate(&g.ev1);
     g.init = true;
@@ -347,6 +348,7 @@ int palial_gpu_finalize(void) {
     g.lane32.release();
     g.batch_dags.clear();
     batch_solve_release();
+    mp_qr_release();
     for (DevBuf *b : {&g.mat, &g.smat, &g.kbuf, &g.probe}) b->release();
     qr_solve_release();
     mpr_release();
@@ -841,6 +843,24 @@ int palial_dag_validate(int alg, int n, int nb, int block, int priority, int nwo
         const std::string r = validate_dag(d, nworkers, seed);
         if (msg && msglen > 0) snprintf(msg, msglen, "%s", r.c_str());
         return r.empty() ? 0 : 1;
+    } catch (const std::exception &ex) {
+        if (msg && msglen > 0) snprintf(msg, msglen, "%s", ex.what());
+        return -1;
+    }
+}
+
+long long palial_dag_qr_apply_validate(int n, int nb, int nrhs, int nworkers, unsigned int seed,
+                                       long long *type_counts, char *msg, int msglen) {
+    try {
+        Dag d = build_qr_solve_dag(n, n, nb, nrhs, true);
+        order_dag(d, 0, nworkers, seed);
+        if (type_counts) {
+            for (int i = 0; i < 16; i++) type_counts[i] = 0;
+            for (const auto &t : d.logical) type_counts[t.type]++;
+        }
+        const std::string r = validate_dag(d, nworkers, seed);
+        if (msg && msglen > 0) snprintf(msg, msglen, "%s", r.c_str());
+        return r.empty() ? (long long)d.records.size() : -1;
     } catch (const std::exception &ex) {
         if (msg && msglen > 0) snprintf(msg, msglen, "%s", ex.what());
         return -1;

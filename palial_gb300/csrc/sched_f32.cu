@@ -1,6 +1,7 @@
-// sched_f32.cu -- FP32 tasks of the batched mixed-precision solves: the tiled Cholesky
-// (reference src/cholesky.h) and no-pivot LU (src/lu.h, src/srclu) task records of the
-// persistent scheduler, run on FP32 copies of the matrices.
+// sched_f32.cu -- FP32 tasks of the persistent scheduler: the tiled Cholesky (reference
+// src/cholesky.h) and no-pivot LU (src/lu.h, src/srclu) of the batched mixed-precision solves,
+// and the flat-tree TS QR (src/qr.h, src/srcqr) with its solve tasks for the mixed-precision QR
+// solve of one matrix, run on FP32 copies of the matrices.
 //
 // Same dispatch as the FP64 scheduler (sched_f64.cu): one CTA = one worker, atomic ticket in
 // the host's dispatch order, bounded acquire waits on the completion counters, fence and
@@ -18,26 +19,36 @@
 
 #include "common.cuh"
 #include "tile_f32.cuh"
+#include "tile_qr.cuh"
 
 namespace palial {
 namespace sf32 {
 using namespace f32;
 
-// Dynamic shared memory (floats): Ds[64][65] | GEMM staging (2 * KC * SP)
+// Dynamic shared memory (floats): Ds[64][65] | GEMM staging (the larger of the Cholesky/LU
+// and the QR routines' needs) | QR reductions | QR tau
 constexpr int SM_DS = 0;
 constexpr int SM_G = 64 * DP + 4;  // 16-byte aligned staging (float4 stores)
-constexpr int SMEM_BYTES = (SM_G + GEMM_SMEM_FLOATS) * 4;
+constexpr int G_FLOATS = GEMM_SMEM_FLOATS > qrt::GEMM_SMEM ? GEMM_SMEM_FLOATS : qrt::GEMM_SMEM;
+constexpr int SM_RED = SM_G + G_FLOATS;
+constexpr int SM_TAU = SM_RED + qrt::RED;
+constexpr int SMEM_BATCH = (SM_G + GEMM_SMEM_FLOATS) * 4;  // Cholesky / LU tasks
+constexpr int SMEM_QR = (SM_TAU + qrt::MAX_NB) * 4;        // QR solve tasks
 static_assert((SM_G * 4) % 16 == 0, "staging alignment");
 
 struct Worker {
     float (*Ds)[DP];
     float *gsm;
+    qrt::QrSmem<float> q;
 };
 
 __device__ __forceinline__ Worker make_worker(float *smem) {
     Worker w;
     w.Ds = reinterpret_cast<float (*)[DP]>(smem + SM_DS);
     w.gsm = smem + SM_G;
+    w.q.gsm = smem + SM_G;
+    w.q.red = smem + SM_RED;
+    w.q.tau = smem + SM_TAU;
     return w;
 }
 
@@ -166,6 +177,16 @@ __device__ void trsm_run(const Worker &w, const float *U, float *B, int n, int l
         solve64<1>(w.Ds, B + (size_t)cb * ld, ld);
     }
 }
+// X = U^-1 B (U upper, B n x 64): row blocks bottom-up (the QR solve's back-substitution).
+__device__ void trsm_lun(const Worker &w, const float *U, float *B, int n, int ld) {
+    for (int rb = n - 64; rb >= 0; rb -= 64) {
+        if (rb + 64 < n)
+            cta_gemm<false, false>(64, 64, n - rb - 64, -1.f, U + rb + (size_t)(rb + 64) * ld, ld, B + rb + 64, ld,
+                                   B + rb, ld, w.gsm);
+        load_diag64(w.Ds, U + rb + (size_t)rb * ld, ld);
+        solve64<3>(w.Ds, B + rb, ld);
+    }
+}
 // X = L^-1 B (L unit lower, B n x 64): row blocks top-down.
 __device__ void trsm_llu(const Worker &w, const float *L, float *B, int n, int ld) {
     for (int rb = 0; rb < n; rb += 64) {
@@ -192,7 +213,12 @@ __device__ void record_error(const SchedParams &p, int code, int task, int m, in
     }
 }
 
-__device__ void run_task(const SchedParams &p, const Worker &w, const Task &t, int tid) {
+__device__ __forceinline__ float *ftile_ptr(float *A, int n, int nb, int m, int k) {
+    return A + (size_t)nb * nb * ((size_t)m + (size_t)(n / nb) * k);
+}
+
+// Batched Cholesky / LU tasks (p.mats, p.mat_status).
+__device__ void run_task_batch(const SchedParams &p, const Worker &w, const Task &t, int tid) {
     const MatInfo mi = p.mats[t.mat];
     float *A = mi.Af;
     const int n = mi.n, nb = mi.nb, bs = mi.bs, ld = nb;
@@ -243,14 +269,58 @@ __device__ void run_task(const SchedParams &p, const Worker &w, const Task &t, i
             break;
         }
         default:
-            // QR task types have no FP32 form; the host never sends them here
             if (threadIdx.x == 0) record_error(p, -2 /*PALIAL_ERR_ARG*/, tid, t.m, t.n, t.type);
             break;
     }
 }
 
-// Persistent scheduler over FP32 matrices (batched runs only: p.mats and p.mat_status set).
-__global__ void __launch_bounds__(NT, 2) sched_f32_kernel(SchedParams p) {
+// QR factorization and QR solve tasks of one matrix (p.Af, T factors in p.Sf, two nb x 64
+// scratch strips per worker in p.scratch_f), on NB tiles.
+__device__ void run_task_qr(const SchedParams &p, const Worker &w, const Task &t, int tid) {
+    float *A = p.Af;
+    const int n = p.n, nb = p.nb, ld = nb;
+    float *wscr = p.scratch_f + (size_t)blockIdx.x * (size_t)p.scratch_per_worker;
+    switch (t.type) {
+        case T_GEQRT:
+            qrt::geqrt(w.q, ftile_ptr(A, n, nb, t.k, t.k), nb, ld, ftile_ptr(p.Sf, n, nb, t.k, t.k), ld);
+            break;
+        case T_UNMQR:
+            qrt::unmqr_strip(w.q, ftile_ptr(A, n, nb, t.k, t.k), ftile_ptr(p.Sf, n, nb, t.k, t.k),
+                             ftile_ptr(A, n, nb, t.k, t.n) + (size_t)t.part * 64 * ld, nb, ld, wscr,
+                             wscr + (size_t)nb * 64);
+            break;
+        case T_TSQRT:
+            qrt::tsqrt(w.q, ftile_ptr(A, n, nb, t.k, t.k), ftile_ptr(A, n, nb, t.m, t.k), nb, ld,
+                       ftile_ptr(p.Sf, n, nb, t.m, t.k), ld);
+            break;
+        case T_TSMQR: {
+            const size_t off = (size_t)t.part * 64 * ld;
+            qrt::tsmqr_strip(w.q, ftile_ptr(A, n, nb, t.k, t.n) + off, ftile_ptr(A, n, nb, t.m, t.n) + off,
+                             ftile_ptr(A, n, nb, t.m, t.k), ftile_ptr(p.Sf, n, nb, t.m, t.k), nb, ld, wscr,
+                             wscr + (size_t)nb * 64);
+            break;
+        }
+        case T_TRSM_LUN:  // R X = Y on the extra tile column
+            trsm_lun(w, ftile_ptr(A, n, nb, t.k, t.k), ftile_ptr(A, n, nb, t.k, t.n) + (size_t)t.part * 64 * ld, nb, ld);
+            break;
+        case T_GEMM_NN: {  // Y_i -= R_ik X_k
+            const int c0 = t.part * 64;
+            cta_gemm<false, false>(nb, 64, nb, -1.f, ftile_ptr(A, n, nb, t.m, t.k), ld,
+                                   ftile_ptr(A, n, nb, t.k, t.n) + (size_t)c0 * ld, ld,
+                                   ftile_ptr(A, n, nb, t.m, t.n) + (size_t)c0 * ld, ld, w.gsm);
+            break;
+        }
+        default:
+            if (threadIdx.x == 0) record_error(p, -2 /*PALIAL_ERR_ARG*/, tid, t.m, t.n, t.type);
+            break;
+    }
+}
+
+// Persistent scheduler over FP32 matrices: a batch (QR = false: p.mats, p.mat_status;
+// Cholesky and LU tasks, two workers per SM) or one matrix's QR factorization / QR solve
+// (QR = true: p.Af, p.Sf, p.scratch_f; one worker per SM, registers for the reflectors).
+template <bool QR>
+__global__ void __launch_bounds__(NT, QR ? 1 : 2) sched_f32_kernel(SchedParams p) {
     extern __shared__ __align__(16) float smem[];
     Worker w = make_worker(smem);
     __shared__ int s_task, s_abort;
@@ -286,7 +356,8 @@ __global__ void __launch_bounds__(NT, 2) sched_f32_kernel(SchedParams p) {
         __syncthreads();
         if (s_abort) break;
         const long long c0 = clock64();
-        run_task(p, w, t, tid);
+        if (QR) run_task_qr(p, w, t, tid);
+        else run_task_batch(p, w, t, tid);
         __syncthreads();
         if (threadIdx.x == 0) {
             __threadfence();
@@ -307,18 +378,30 @@ __global__ void __launch_bounds__(NT, 2) sched_f32_kernel(SchedParams p) {
 }  // namespace sf32
 
 cudaError_t sched32_configure() {
-    return cudaFuncSetAttribute(sf32::sched_f32_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, sf32::SMEM_BYTES);
+    cudaError_t e = cudaFuncSetAttribute(sf32::sched_f32_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         sf32::SMEM_BATCH);
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(sf32::sched_f32_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 sf32::SMEM_QR);
+    return e;
 }
 
-int sched32_occupancy() {
+// resident CTAs per SM: the batched instance (qr = false) or the QR instance
+int sched32_occupancy(bool qr) {
     int blocks = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, sf32::sched_f32_kernel, f32::NT, sf32::SMEM_BYTES);
+    if (qr)
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, sf32::sched_f32_kernel<true>, f32::NT, sf32::SMEM_QR);
+    else
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, sf32::sched_f32_kernel<false>, f32::NT,
+                                                      sf32::SMEM_BATCH);
     return blocks;
 }
 
+// p.mats set: the batched Cholesky / LU instance; else the one-matrix QR instance
 cudaError_t sched32_launch(const SchedParams &p, int grid, cudaStream_t s) {
     note_launch();
-    sf32::sched_f32_kernel<<<grid, f32::NT, sf32::SMEM_BYTES, s>>>(p);
+    if (p.mats) sf32::sched_f32_kernel<false><<<grid, f32::NT, sf32::SMEM_BATCH, s>>>(p);
+    else sf32::sched_f32_kernel<true><<<grid, f32::NT, sf32::SMEM_QR, s>>>(p);
     return cudaGetLastError();
 }
 

@@ -47,6 +47,24 @@ def test_qr_solve_dag_rejects_bad_sizes(rows, cols, nb, nrhs):
     assert P.qr_solve_dag(rows, cols, nb, nrhs)["records"] == -1
 
 
+@pytest.mark.parametrize("n,nb,nrhs", [(512, 128, 1), (1024, 256, 16), (4096, 512, 16), (768, 128, 70)])
+def test_qr_apply_dag_valid_and_counts(n, nb, nrhs):
+    """The refinement steps' DAG: Q^T on the extra tile column and the back-substitution only
+    (no GEQRT/TSQRT, no update of the factor tiles), deadlock-free under ticket dispatch."""
+    for seed in (0, 5):
+        d = P.qr_apply_dag(n, nb, nrhs, nworkers=41, seed=seed)
+        assert d["records"] > 0, d["message"]
+    c = d["type_counts"]
+    mt, rparts = n // nb, (nrhs + 63) // 64
+    # GEQRT 8, UNMQR 9, TSQRT 10, TSMQR 11, TRSM_LUN 12, GEMM_NN 7
+    assert c[8] == 0 and c[10] == 0
+    assert c[9] == mt and c[11] == mt * (mt - 1) // 2
+    assert c[12] == mt and c[7] == mt * (mt - 1) // 2
+    assert sum(c) == c[7] + c[9] + c[11] + c[12]
+    assert d["records"] == rparts * sum(c)
+    assert P.qr_apply_dag(n, nb, 0)["records"] == -1
+
+
 def test_oracle_qr_solve_matches_lapack():
     """The oracle's solve path (reference QR algorithm, then Q^T b and R back-substitution)
     against numpy's LAPACK solve."""
