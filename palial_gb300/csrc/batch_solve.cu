@@ -390,15 +390,18 @@ struct Solver {
     }
 
     // factor the listed matrices (all of one precision) in one batched launch; FP32
-    // breakdowns are marked failed
+    // breakdowns are marked failed.  FP32 tasks run on the matrix's tile as the block; FP64
+    // tasks on 64-blocks inside it (the FP64 scheduler's fastest block on every size class of
+    // the synthetic batch: its FP64 pipe favours more, shorter tasks)
     int factor(const std::vector<int> &ms, bool f32) {
         if (ms.empty()) return PALIAL_OK;
-        std::vector<int> algs, ns, nbs;
+        std::vector<int> algs, ns, nbs, bss;
         std::vector<void *> bufs;
         for (int m : ms) {
             algs.push_back(mats[m].alg);
             ns.push_back(mats[m].n);
             nbs.push_back(mats[m].nb);
+            bss.push_back(f32 ? mats[m].nb : 64);
             bufs.push_back(const_cast<void *>(mats[m].F));
         }
         std::vector<int> flags(ms.size(), 0);
@@ -406,7 +409,7 @@ struct Solver {
         palial_opts_default(&o);
         palial_status s2;
         memset(&s2, 0, sizeof s2);
-        const int rc = batched_run((int)ms.size(), algs.data(), ns.data(), nbs.data(), nbs.data(), bufs.data(), f32,
+        const int rc = batched_run((int)ms.size(), algs.data(), ns.data(), nbs.data(), bss.data(), bufs.data(), f32,
                                    flags.data(), &o, &s2, nullptr, s);
         factor_s += s2.seconds;
         if (rc < 0) return set_status(st, rc, "batched factorization: %s", s2.message);

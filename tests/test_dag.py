@@ -92,6 +92,11 @@ def test_batch_dag_validates_and_isolates_matrices():
     buf = ctypes.create_string_buffer(256)
     rc = P.lib().palial_dag_batch_validate(60, arr(algs), arr(npad), arr(bs), arr(bs), 152, 5, buf, 256)
     assert rc == 0, buf.value
+    # 64-blocks inside larger tiles (the batched solves' FP64 factorizations)
+    tiles = [64 if n < 128 else (128 if n < 1024 else 256) for n in ns]
+    npad = [B.padded(int(n), t) for n, t in zip(ns, tiles)]
+    rc = P.lib().palial_dag_batch_validate(60, arr(algs), arr(npad), arr(tiles), arr([64] * 60), 152, 7, buf, 256)
+    assert rc == 0, buf.value
 
 
 def _names(alg, n, nb, block):
