@@ -236,6 +236,12 @@ int palial_gpu_tile_dormqr(int nb, const double *dV, const double *dT, double *d
 int palial_gpu_tile_dtsqrt(int nb, double *dA1, double *dA2, double *dT, int lda);
 int palial_gpu_tile_dtsmqr(int nb, double *dA1, double *dA2, const double *dV, const double *dT,
                            int lda);
+/* The FP32 forms of the four QR tile kernels (the mixed-precision QR's routines), same
+ * arguments on FP32 device tiles; nb a multiple of 64 up to 512. */
+int palial_gpu_tile_sgeqrt(int nb, float *dA, float *dT, int lda);
+int palial_gpu_tile_sormqr(int nb, const float *dV, const float *dT, float *dC, int lda);
+int palial_gpu_tile_stsqrt(int nb, float *dA1, float *dA2, float *dT, int lda);
+int palial_gpu_tile_stsmqr(int nb, float *dA1, float *dA2, const float *dV, const float *dT, int lda);
 /* TSMQR without any device allocation.  No counterpart in the reference: it exists for
  * callers that may not allocate device memory themselves -- code inside an application that
  * owns all device memory (its own pool or allocator, a fixed budget), or latency-critical

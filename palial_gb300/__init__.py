@@ -99,6 +99,10 @@ def lib() -> ctypes.CDLL:
         h.palial_gpu_tile_dtsqrt.argtypes = [i, vp, vp, vp, i]
         h.palial_gpu_tile_dtsmqr.argtypes = [i, vp, vp, vp, vp, i]
         h.palial_gpu_tile_dtsmqr_noalloc.argtypes = [i, vp, vp, vp, vp, i, vp]
+        h.palial_gpu_tile_sgeqrt.argtypes = [i, vp, vp, i]
+        h.palial_gpu_tile_sormqr.argtypes = [i, vp, vp, vp, i]
+        h.palial_gpu_tile_stsqrt.argtypes = [i, vp, vp, vp, i]
+        h.palial_gpu_tile_stsmqr.argtypes = [i, vp, vp, vp, vp, i]
         h.palial_gpu_error_string.restype = ctypes.c_char_p
         h.palial_gpu_kernel_launches.restype = ctypes.c_longlong
         h.palial_gpu_solve_ir.argtypes = [i, vp, i, i, vp, vp, i, ctypes.POINTER(Opts), ctypes.POINTER(Status), vp]

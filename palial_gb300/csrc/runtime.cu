@@ -36,6 +36,8 @@ cudaError_t tile_task_launch(int type, int nb, int ld, double *p0, double *p1, d
 cudaError_t sched32_configure();
 int sched32_occupancy(bool qr);
 cudaError_t sched32_launch(const SchedParams &p, int grid, cudaStream_t s);
+cudaError_t tile_qr_f32_launch(int type, int nb, int ld, float *p0, float *p1, float *p2, float *p3, float *scratch,
+                               cudaStream_t s);
 // gen_check.cu
 cudaError_t launch_gen_uniform(double *A, int n, int nb, uint64_t seed, cudaStream_t s);
 cudaError_t launch_gen_refpattern(double *A, int n, int nb, uint64_t seed, cudaStream_t s);
@@ -561,6 +563,31 @@ int palial_gpu_tile_dtsqrt(int nb, double *dA1, double *dA2, double *dT, int lda
 }
 int palial_gpu_tile_dtsmqr(int nb, double *dA1, double *dA2, const double *dV, const double *dT, int lda) {
     return tile_call(T_TSMQR, nb, lda, dA1, dA2, const_cast<double *>(dV), const_cast<double *>(dT));
+}
+
+// FP32 QR tile tasks (the mixed-precision QR's tile routines), one CTA, synchronous
+static int tile_qr_call(int type, int nb, int ld, float *p0, float *p1, float *p2, float *p3) {
+    palial_status *st = nullptr;
+    int rc = ensure_init(nullptr);
+    if (rc) return rc;
+    if (nb <= 0 || nb % 64 || nb > 512 || ld < nb || !p0 || !p1 || (type != T_GEQRT && !p2) ||
+        (type == T_TSMQR && !p3))
+        return PALIAL_ERR_ARG;
+    CK(g.main.scratch.ensure(sizeof(float) * ((size_t)2 * nb * 64)), "alloc scratch");
+    CK(tile_qr_f32_launch(type, nb, ld, p0, p1, p2, p3, static_cast<float *>(g.main.scratch.ptr), nullptr), "launch");
+    CK(cudaDeviceSynchronize(), "tile kernel");
+    return PALIAL_OK;
+}
+
+int palial_gpu_tile_sgeqrt(int nb, float *dA, float *dT, int lda) { return tile_qr_call(T_GEQRT, nb, lda, dA, dT, 0, 0); }
+int palial_gpu_tile_sormqr(int nb, const float *dV, const float *dT, float *dC, int lda) {
+    return tile_qr_call(T_UNMQR, nb, lda, const_cast<float *>(dV), const_cast<float *>(dT), dC, 0);
+}
+int palial_gpu_tile_stsqrt(int nb, float *dA1, float *dA2, float *dT, int lda) {
+    return tile_qr_call(T_TSQRT, nb, lda, dA1, dA2, dT, 0);
+}
+int palial_gpu_tile_stsmqr(int nb, float *dA1, float *dA2, const float *dV, const float *dT, int lda) {
+    return tile_qr_call(T_TSMQR, nb, lda, dA1, dA2, const_cast<float *>(dV), const_cast<float *>(dT));
 }
 
 // ---- generators --------------------------------------------------------------------------

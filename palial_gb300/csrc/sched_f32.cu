@@ -375,6 +375,35 @@ __global__ void __launch_bounds__(NT, QR ? 1 : 2) sched_f32_kernel(SchedParams p
     }
 }
 
+// One whole FP32 QR tile task on one CTA, for the single-tile C ABI entry points (the
+// reference's tile-kernel argument order): GEQRT (A, T), TSQRT (A1, A2, T), UNMQR (V, T, C),
+// TSMQR (A1, A2, V, T); ld >= nb; scratch: two nb x 64 strips.
+__global__ void __launch_bounds__(NT, 1) tile_qr_kernel(int type, int nb, int ld, float *p0, float *p1, float *p2,
+                                                        float *p3, float *scratch) {
+    extern __shared__ __align__(16) float smem[];
+    Worker w = make_worker(smem);
+    float *W = scratch, *W2 = scratch + (size_t)nb * 64;
+    switch (type) {
+        case T_GEQRT:
+            qrt::geqrt(w.q, p0, nb, ld, p1, ld);
+            break;
+        case T_TSQRT:
+            qrt::tsqrt(w.q, p0, p1, nb, ld, p2, ld);
+            break;
+        case T_UNMQR:
+            for (int q = 0; q < nb / 64; q++) qrt::unmqr_strip(w.q, p0, p1, p2 + (size_t)q * 64 * ld, nb, ld, W, W2);
+            break;
+        case T_TSMQR:
+            for (int q = 0; q < nb / 64; q++) {
+                const size_t off = (size_t)q * 64 * ld;
+                qrt::tsmqr_strip(w.q, p0 + off, p1 + off, p2, p3, nb, ld, W, W2);
+            }
+            break;
+        default:
+            break;
+    }
+}
+
 }  // namespace sf32
 
 cudaError_t sched32_configure() {
@@ -383,7 +412,16 @@ cudaError_t sched32_configure() {
     if (e == cudaSuccess)
         e = cudaFuncSetAttribute(sf32::sched_f32_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  sf32::SMEM_QR);
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(sf32::tile_qr_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, sf32::SMEM_QR);
     return e;
+}
+
+cudaError_t tile_qr_f32_launch(int type, int nb, int ld, float *p0, float *p1, float *p2, float *p3, float *scratch,
+                               cudaStream_t s) {
+    note_launch();
+    sf32::tile_qr_kernel<<<1, f32::NT, sf32::SMEM_QR, s>>>(type, nb, ld, p0, p1, p2, p3, scratch);
+    return cudaGetLastError();
 }
 
 // resident CTAs per SM: the batched instance (qr = false) or the QR instance
