@@ -470,8 +470,8 @@ def run_suite(args, P, torch) -> None:
                 torch.cuda.empty_cache()
         return
     n, nrhs = args.n, 16
-    b = torch.from_numpy(np.asfortranarray(
-        __import__("oracle.oracle", fromlist=["x"]).gen_uniform(5, n, nrhs, stream=2)).ravel(order="F")).cuda()
+    b = torch.empty(n * nrhs, dtype=torch.float64, device="cuda")
+    P.gen_dense(b.data_ptr(), n, nrhs, 5, P.STREAM_RHS)
     import ctypes
     for alg in ("cholesky", "lu"):
         for kappa in (1e2, 1e6, 1e10):
@@ -521,7 +521,6 @@ def main() -> None:
     import torch
 
     import palial_gb300 as P
-    from oracle import oracle as O
 
     n, nrhs = args.n, 16
     torch.cuda.set_device(local)
@@ -543,8 +542,8 @@ def main() -> None:
     stream = torch.cuda.current_stream()
     a0 = torch.empty(n * n, dtype=torch.float64, device="cuda")
     P.gen_spd(a0.data_ptr(), n, NB, seed=rank)
-    bh = np.asfortranarray(O.gen_uniform(5, n, nrhs, stream=O.STREAM_RHS))
-    b = torch.from_numpy(bh.ravel(order="F")).cuda()
+    b = torch.empty(n * nrhs, dtype=torch.float64, device="cuda")
+    P.gen_dense(b.data_ptr(), n, nrhs, 5, P.STREAM_RHS)  # uniform [-1, 1), column-major
     x = torch.zeros_like(b)
     torch.cuda.synchronize()
 
@@ -616,7 +615,7 @@ def main() -> None:
     torch.cuda.synchronize()
     host_np = host.numpy()
     xh = np.zeros((nrhs, n))
-    bhc = np.ascontiguousarray(bh.T)  # column-major n x nrhs == row-major nrhs x n
+    bhc = b.cpu().numpy().reshape(nrhs, n).copy()  # column-major n x nrhs == row-major nrhs x n
     e2e_times = []
     for i in range(1 + args.e2e_steps):
         barrier()

@@ -368,6 +368,9 @@ int palial_gpu_batch_solve_synthetic(int count, uint64_t seed, int rank, int wor
 /* ---- generators (counter-based; the same bytes as the CPU oracle's generators) ------------ */
 /* uniform [-1,1): entry (i,j) from splitmix64 of seed/stream and i + j*rows.  Tile layout. */
 int palial_gpu_gen_uniform(double *dA, int n, int nb, uint64_t seed, void *stream);
+/* Dense column-major rows x cols block uniform [-1,1) (right-hand sides): entry (i,j) from
+ * splitmix64 of seed / stream_id (2 = right-hand sides) and index i + j*rows. */
+int palial_gpu_gen_dense(double *dX, long long rows, int cols, uint64_t seed, int stream_id, void *stream);
 /* A = B B^T + n I, B = K/128, K integer in [-128,127] (exact integer arithmetic). */
 int palial_gpu_gen_spd(double *dA, int n, int nb, uint64_t seed, void *stream);
 

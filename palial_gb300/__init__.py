@@ -82,6 +82,7 @@ def lib() -> ctypes.CDLL:
                                     ctypes.POINTER(Status)]
         h.palial_gpu_gen_uniform.argtypes = [vp, i, i, ctypes.c_uint64, vp]
         h.palial_gpu_gen_spd.argtypes = [vp, i, i, ctypes.c_uint64, vp]
+        h.palial_gpu_gen_dense.argtypes = [vp, ctypes.c_longlong, i, ctypes.c_uint64, i, vp]
         h.palial_gpu_residual_probe.argtypes = [i, vp, vp, vp, i, i, i, ctypes.c_uint64, ctypes.POINTER(d)]
         h.palial_gpu_trace_dump.argtypes = [ctypes.c_char_p, ctypes.c_char_p]
         h.palial_gpu_trace_count.restype = ctypes.c_longlong
@@ -344,6 +345,15 @@ def gen_kappa(d_a: int, n: int, nb: int, kappa: float, symmetric: bool, seed: in
 
 def gen_uniform(d_a: int, n: int, nb: int, seed: int, stream: int = 0) -> None:
     _check(lib().palial_gpu_gen_uniform(d_a, n, nb, seed, stream or None), None)
+
+
+STREAM_RHS = 2  # generator stream of right-hand sides
+
+
+def gen_dense(d_x: int, rows: int, cols: int, seed: int, stream_id: int = STREAM_RHS, stream: int = 0) -> None:
+    """Dense column-major rows x cols uniform [-1, 1) block on the device (the generator the
+    right-hand sides of the benchmarks use)."""
+    _check(lib().palial_gpu_gen_dense(d_x, rows, cols, seed, stream_id, stream or None), None)
 
 
 def gen_spd(d_a: int, n: int, nb: int, seed: int, stream: int = 0) -> None:

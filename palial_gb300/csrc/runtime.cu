@@ -600,6 +600,15 @@ int palial_gpu_gen_uniform(double *dA, int n, int nb, uint64_t seed, void *strea
     return PALIAL_OK;
 }
 
+int palial_gpu_gen_dense(double *dX, long long rows, int cols, uint64_t seed, int stream_id, void *stream) {
+    palial_status *st = nullptr;
+    int rc = ensure_init(nullptr);
+    if (rc) return rc;
+    if (!dX || rows <= 0 || cols <= 0 || stream_id < 0) return PALIAL_ERR_ARG;
+    CK(launch_gen_dense(dX, rows, cols, seed, stream_id, static_cast<cudaStream_t>(stream)), "gen dense");
+    return PALIAL_OK;
+}
+
 int palial_gpu_gen_spd(double *dA, int n, int nb, uint64_t seed, void *stream) {
     palial_status *st = nullptr;
     int rc = ensure_init(nullptr);

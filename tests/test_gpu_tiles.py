@@ -126,3 +126,8 @@ def test_generators_bitwise_equal_to_oracle():
         P.gen_spd(d.data_ptr(), n, nb, 0)
         torch.cuda.synchronize()
         assert np.array_equal(d.cpu().numpy(), O.to_tiles(O.gen_spd(0, n), nb))
+    # the benchmarks' right-hand sides: column-major n x 16
+    r = torch.empty(1024 * 16, dtype=torch.float64, device="cuda")
+    P.gen_dense(r.data_ptr(), 1024, 16, 5, P.STREAM_RHS)
+    torch.cuda.synchronize()
+    assert np.array_equal(r.cpu().numpy(), O.gen_uniform(5, 1024, 16, stream=O.STREAM_RHS).ravel(order="F"))
