@@ -84,6 +84,13 @@ def class_label(c: int) -> str:
     return f"[{CLASS_EDGES[c]},{CLASS_EDGES[c + 1]})"
 
 
+def _dense(t: np.ndarray, n: int, nb: int) -> np.ndarray:
+    """Tile-layout buffer (tile (m, k) at nb*nb*(m + (n/nb)*k), column-major inside) -> the
+    dense n x n matrix indexed [row, col]."""
+    mt = n // nb
+    return np.ascontiguousarray(t.reshape(mt, mt, nb, nb).transpose(1, 3, 0, 2).reshape(n, n))
+
+
 def padded(n: int, bs: int) -> int:
     return int(math.ceil(n / bs) * bs)
 
@@ -136,16 +143,14 @@ class Batch:
 
     def factor(self, i: int) -> np.ndarray:
         """Factored matrix i, leading n x n block, as a dense [row, col] array (host)."""
-        from oracle.oracle import from_tiles  # noqa: WPS433 (layout helper only)
         t = self.buf[int(self.offs[i]):int(self.offs[i + 1])].cpu().numpy()
         n, npad, bs = int(self.ns[i]), int(self.np_[i]), int(self.bs[i])
-        return from_tiles(t, npad, bs)[:n, :n]
+        return _dense(t, npad, bs)[:n, :n]
 
     def original(self, i: int) -> np.ndarray:
-        from oracle.oracle import from_tiles  # noqa: WPS433
         t = self.pristine[int(self.offs[i]):int(self.offs[i + 1])].cpu().numpy()
         n, npad, bs = int(self.ns[i]), int(self.np_[i]), int(self.bs[i])
-        return from_tiles(t, npad, bs)[:n, :n]
+        return _dense(t, npad, bs)[:n, :n]
 
 
 def autotune(torch, ns, algs, candidates=CANDIDATE_BS, reps: int = 2, seed: int = 2) -> tuple[dict, dict]:
