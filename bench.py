@@ -1,7 +1,7 @@
 """Benchmark: tiled Cholesky at N = 32768, NB = 512 on one GB300 (per GPU).
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-                    [--suite fp64|kappa|batched|batched_solve|costmodel|kernels]
+                    [--suite fp64|kappa|batched|batched_solve|costmodel|kernels|qr_mixed]
 
 A step is one solve A X = B (16 right-hand sides, uniform [-1, 1)) of a device-resident
 SPD matrix A = B B^T + N I (seed = rank; the reference's tile layout) by the mixed-precision
@@ -35,6 +35,7 @@ precision at N = 32768 (A = U diag(s) V^T, 64 Householder reflectors each side);
 FP64 launch, then times batched solves of it: FP64 factorizations vs block size and precision
 (FP32 + FP64 refinement, or FP64) autotuned per algorithm and size class; `--suite
 batched_solve` runs the solves alone (FP64 with the FP64 autotuner's measured block sizes).
+`--suite qr_mixed` times the mixed-precision QR solve beside the FP64 QR solve (N = 16384, 32768).
 """
 from __future__ import annotations
 
@@ -437,6 +438,31 @@ def run_kernels(args, P, torch) -> None:
                       "diag_tile_call_s": t_diag}), flush=True)
 
 
+def run_qr_mixed(args, P, torch) -> None:
+    """QR solves of A X = B (A uniform [-1, 1), seed 1; 16 right-hand sides) at N = 16384 and
+    32768, NB = 512: the mixed-precision QR (FP32 tile QR + FP64 refinement) against the FP64 QR
+    solve of the same system; both whole calls on device buffers, TFLOP/s from 4N^3/3."""
+    nrhs = 16
+    for n in (16384, 32768):
+        da = torch.empty(n * n, dtype=torch.float64, device="cuda")
+        P.gen_uniform(da.data_ptr(), n, NB, 1)
+        b = torch.empty(n * nrhs, dtype=torch.float64, device="cuda")
+        P.gen_dense(b.data_ptr(), n, nrhs, 5, P.STREAM_RHS)
+        x = torch.zeros_like(b)
+        st = P.qr_solve_ir(da.data_ptr(), n, NB, b.data_ptr(), x.data_ptr(), nrhs, allow_not_converged=True)
+        line = {"suite": "qr_mixed", "n": n, "nb": NB, "nrhs": nrhs, "converged": st.code == 0,
+                "seconds": st.seconds, "factor_seconds": st.factor_seconds, "ir_iters": st.ir_iters,
+                "backward_error": st.backward_error, "tflops_fp64_equiv": 4.0 * n ** 3 / 3.0 / st.seconds * 1e-12,
+                "precision_used": "fp32" if int(st.kappa_est) == 5 else "fp64", "message": st.message.decode()}
+        x.zero_()
+        s64 = P.qr_solve(da.data_ptr(), n, n, NB, b.data_ptr(), x.data_ptr(), nrhs)
+        line["fp64_qr_solve"] = {"seconds": s64.seconds, "tflops": 4.0 * n ** 3 / 3.0 / s64.seconds * 1e-12}
+        line["speedup_over_fp64"] = s64.seconds / st.seconds
+        print(json.dumps(line), flush=True)
+        del da, b, x
+        torch.cuda.empty_cache()
+
+
 def run_suite(args, P, torch) -> None:
     import numpy as np
     if args.suite == "kernels":
@@ -450,6 +476,9 @@ def run_suite(args, P, torch) -> None:
         return
     if args.suite == "batched_solve":
         run_batched_solve(args, FP64_BATCH_BLOCKS, args.batch, 1)
+        return
+    if args.suite == "qr_mixed":
+        run_qr_mixed(args, P, torch)
         return
     if args.suite == "fp64":
         for alg in ("cholesky", "lu", "qr"):
@@ -507,7 +536,7 @@ def main() -> None:
     ap.add_argument("--n", type=int, default=N)
     ap.add_argument("--precision", default="bf16x3")
     ap.add_argument("--suite", default=None, choices=[None, "fp64", "kappa", "batched", "batched_solve", "costmodel",
-                                                      "kernels"])
+                                                      "kernels", "qr_mixed"])
     ap.add_argument("--batch", type=int, default=2000)
     ap.add_argument("--no-fp64", action="store_true")
     args = ap.parse_args()
