@@ -440,27 +440,33 @@ def run_kernels(args, P, torch) -> None:
 
 def run_qr_mixed(args, P, torch) -> None:
     """QR solves of A X = B (A uniform [-1, 1), seed 1; 16 right-hand sides) at N = 16384 and
-    32768, NB = 512: the mixed-precision QR (FP32 tile QR + FP64 refinement) against the FP64 QR
-    solve of the same system; both whole calls on device buffers, TFLOP/s from 4N^3/3."""
+    32768: the mixed-precision QR (FP32 tile QR + FP64 refinement) with NB = 512 and 256 (its
+    single-CTA TSQRT chain shortens with the tile) against the FP64 QR solve of the same system
+    at NB = 512; whole calls on device buffers, TFLOP/s from 4N^3/3."""
     nrhs = 16
     for n in (16384, 32768):
-        da = torch.empty(n * n, dtype=torch.float64, device="cuda")
-        P.gen_uniform(da.data_ptr(), n, NB, 1)
         b = torch.empty(n * nrhs, dtype=torch.float64, device="cuda")
         P.gen_dense(b.data_ptr(), n, nrhs, 5, P.STREAM_RHS)
         x = torch.zeros_like(b)
-        st = P.qr_solve_ir(da.data_ptr(), n, NB, b.data_ptr(), x.data_ptr(), nrhs, allow_not_converged=True)
-        line = {"suite": "qr_mixed", "n": n, "nb": NB, "nrhs": nrhs, "converged": st.code == 0,
-                "seconds": st.seconds, "factor_seconds": st.factor_seconds, "ir_iters": st.ir_iters,
-                "backward_error": st.backward_error, "tflops_fp64_equiv": 4.0 * n ** 3 / 3.0 / st.seconds * 1e-12,
-                "precision_used": "fp32" if int(st.kappa_est) == 5 else "fp64", "message": st.message.decode()}
-        x.zero_()
-        s64 = P.qr_solve(da.data_ptr(), n, n, NB, b.data_ptr(), x.data_ptr(), nrhs)
-        line["fp64_qr_solve"] = {"seconds": s64.seconds, "tflops": 4.0 * n ** 3 / 3.0 / s64.seconds * 1e-12}
-        line["speedup_over_fp64"] = s64.seconds / st.seconds
-        print(json.dumps(line), flush=True)
-        del da, b, x
-        torch.cuda.empty_cache()
+        for nb in (NB, 256):
+            da = torch.empty(n * n, dtype=torch.float64, device="cuda")
+            P.gen_uniform(da.data_ptr(), n, nb, 1)
+            x.zero_()
+            st = P.qr_solve_ir(da.data_ptr(), n, nb, b.data_ptr(), x.data_ptr(), nrhs, allow_not_converged=True)
+            line = {"suite": "qr_mixed", "n": n, "nb": nb, "nrhs": nrhs, "converged": st.code == 0,
+                    "seconds": st.seconds, "factor_seconds": st.factor_seconds, "ir_iters": st.ir_iters,
+                    "backward_error": st.backward_error,
+                    "tflops_fp64_equiv": 4.0 * n ** 3 / 3.0 / st.seconds * 1e-12,
+                    "precision_used": "fp32" if int(st.kappa_est) == 5 else "fp64", "message": st.message.decode()}
+            if nb == NB:
+                x.zero_()
+                s64 = P.qr_solve(da.data_ptr(), n, n, NB, b.data_ptr(), x.data_ptr(), nrhs)
+                line["fp64_qr_solve"] = {"seconds": s64.seconds, "tflops": 4.0 * n ** 3 / 3.0 / s64.seconds * 1e-12}
+                line["speedup_over_fp64"] = s64.seconds / st.seconds
+            print(json.dumps(line), flush=True)
+            del da
+            torch.cuda.empty_cache()
+        del b, x
 
 
 def run_suite(args, P, torch) -> None:
