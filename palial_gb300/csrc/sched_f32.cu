@@ -282,7 +282,7 @@ __device__ void run_task_qr(const SchedParams &p, const Worker &w, const Task &t
     float *wscr = p.scratch_f + (size_t)blockIdx.x * (size_t)p.scratch_per_worker;
     switch (t.type) {
         case T_GEQRT:
-            qrt::geqrt(w.q, ftile_ptr(A, n, nb, t.k, t.k), nb, ld, ftile_ptr(p.Sf, n, nb, t.k, t.k), ld);
+            qrt::geqrt(w.q, ftile_ptr(A, n, nb, t.k, t.k), nb, ld, ftile_ptr(p.Sf, n, nb, t.k, t.k), ld, wscr);
             break;
         case T_UNMQR:
             qrt::unmqr_strip(w.q, ftile_ptr(A, n, nb, t.k, t.k), ftile_ptr(p.Sf, n, nb, t.k, t.k),
@@ -291,7 +291,7 @@ __device__ void run_task_qr(const SchedParams &p, const Worker &w, const Task &t
             break;
         case T_TSQRT:
             qrt::tsqrt(w.q, ftile_ptr(A, n, nb, t.k, t.k), ftile_ptr(A, n, nb, t.m, t.k), nb, ld,
-                       ftile_ptr(p.Sf, n, nb, t.m, t.k), ld);
+                       ftile_ptr(p.Sf, n, nb, t.m, t.k), ld, wscr);
             break;
         case T_TSMQR: {
             const size_t off = (size_t)t.part * 64 * ld;
@@ -385,10 +385,10 @@ __global__ void __launch_bounds__(NT, 1) tile_qr_kernel(int type, int nb, int ld
     float *W = scratch, *W2 = scratch + (size_t)nb * 64;
     switch (type) {
         case T_GEQRT:
-            qrt::geqrt(w.q, p0, nb, ld, p1, ld);
+            qrt::geqrt(w.q, p0, nb, ld, p1, ld, scratch);
             break;
         case T_TSQRT:
-            qrt::tsqrt(w.q, p0, p1, nb, ld, p2, ld);
+            qrt::tsqrt(w.q, p0, p1, nb, ld, p2, ld, scratch);
             break;
         case T_UNMQR:
             for (int q = 0; q < nb / 64; q++) qrt::unmqr_strip(w.q, p0, p1, p2 + (size_t)q * 64 * ld, nb, ld, W, W2);

@@ -333,52 +333,115 @@ __device__ void larft(T *red, int nb, const T *tau, T *Tm, int ldt, Dot dot) {
     }
 }
 
-// GEQRT of an nb x nb tile: unblocked Householder QR (R upper, V below the diagonal), T into Tm.
-template <class T>
-__device__ void geqrt(const QrSmem<T> &w, T *A, int nb, int ld, T *Tm, int ldt) {
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    for (int i = 0; i < nb; i++) {
-        T *ci = A + (size_t)i * ld;
-        const T ti = larfg(w.red, ci + i, ci + i + 1, nb - i - 1);
-        if (threadIdx.x == 0) w.tau[i] = ti;
-        if (ti != T(0)) {
-            for (int j = i + 1 + warp; j < nb; j += NT / 32) {
-                T *cj = A + (size_t)j * ld;
-                reflect_col(ci, cj, cj + i, i + 1, nb, ti, lane);
-            }
-        }
-        __syncthreads();
+// Off-diagonal 64-blocks of the full compact-WY T after the panels: for every block column
+// Q (q0 = 64 Q), with the diagonal blocks T_Q already in place,
+//     T(0:q0, Q) = -T(0:q0, 0:q0) (Y_{0:q0}^T Y_Q) T_Q
+// (the product of two compact-WY blocks, Schreiber and Van Loan).  ytq(q0, Ys, ldy) writes
+// Y_{0:q0}^T Y_Q (q0 x 64) into Ys.  scr: two nb x 64 scratch blocks.
+template <class T, class YtQ>
+__device__ void assemble_t(const QrSmem<T> &w, int nb, T *Tm, int ldt, T *scr, YtQ ytq) {
+    T *Ys = scr, *Y2 = scr + (size_t)nb * 64;
+    for (int q0 = 64; q0 < nb; q0 += 64) {
+        ytq(q0, Ys, nb);
+        // Y2 = Ys T_Q (T_Q upper 64 x 64)
+        cta_gemm<T, false, false, M_NONE, M_UPPER>(q0, 64, 64, T(1), Ys, nb, Tm + q0 + (size_t)q0 * ldt, ldt, T(0),
+                                                   Y2, nb, w.gsm);
+        // T(0:q0, Q) = -T(0:q0, 0:q0) Y2 (upper)
+        cta_gemm<T, false, false, M_UPPER>(q0, 64, q0, T(-1), Tm, ldt, Y2, nb, T(0), Tm + (size_t)q0 * ldt, ldt, w.gsm);
     }
-    // z_j = <v_j, v_i> = A(i, j) + sum_{r > i} A(r, j) A(r, i), j < i
-    larft(w.red, nb, w.tau, Tm, ldt, [&](int j, int i, int ln) {
-        const T *cj = A + (size_t)j * ld, *ci = A + (size_t)i * ld;
-        T s = (ln == 0) ? ldg(cj + i) : T(0);
-        for (int r = i + 1 + ln; r < nb; r += 32) s = fma(ldg(cj + r), ldg(ci + r), s);
-        return s;
+}
+
+// GEQRT of an nb x nb tile (nb a multiple of 64): Householder QR blocked by 64-column panels.
+// Each panel is factored column by column (dlarfg, reflectors applied inside the panel only),
+// its 64 x 64 T block built (dlarft), and the trailing columns updated by the panel's block
+// reflector with CTA GEMMs (dlarfb); the full T is assembled at the end.  Output as the
+// unblocked dgeqr2 + dlarft: R upper, V below the diagonal (unit implicit), T upper in Tm.
+// scr: two nb x 64 scratch blocks.
+template <class T>
+__device__ void geqrt(const QrSmem<T> &w, T *A, int nb, int ld, T *Tm, int ldt, T *scr) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    T *W = scr, *W2 = scr + (size_t)nb * 64;
+    for (int p0 = 0; p0 < nb; p0 += 64) {
+        for (int i = p0; i < p0 + 64; i++) {
+            T *ci = A + (size_t)i * ld;
+            const T ti = larfg(w.red, ci + i, ci + i + 1, nb - i - 1);
+            if (threadIdx.x == 0) w.tau[i] = ti;
+            if (ti != T(0)) {
+                for (int j = i + 1 + warp; j < p0 + 64; j += NT / 32) {
+                    T *cj = A + (size_t)j * ld;
+                    reflect_col(ci, cj, cj + i, i + 1, nb, ti, lane);
+                }
+            }
+            __syncthreads();
+        }
+        // panel T: z_j = <v_j, v_i> = A(i, j) + sum_{r > i} A(r, j) A(r, i), j < i (global indices)
+        larft(w.red, 64, w.tau + p0, Tm + p0 + (size_t)p0 * ldt, ldt, [&](int j, int i, int ln) {
+            const T *cj = A + (size_t)(p0 + j) * ld, *ci = A + (size_t)(p0 + i) * ld;
+            T s = (ln == 0) ? ldg(cj + p0 + i) : T(0);
+            for (int r = p0 + i + 1 + ln; r < nb; r += 32) s = fma(ldg(cj + r), ldg(ci + r), s);
+            return s;
+        });
+        const int ncols = nb - p0 - 64;
+        if (ncols > 0) {
+            // C <- C - V T^T V^T C on the trailing columns (rows p0 .. nb - 1)
+            const T *V = A + p0 + (size_t)p0 * ld;
+            T *C = A + p0 + (size_t)(p0 + 64) * ld;
+            const T *Tp = Tm + p0 + (size_t)p0 * ldt;
+            cta_gemm<T, true, false, M_UNIT_LOWER>(64, ncols, nb - p0, T(1), V, ld, C, ld, T(0), W, 64, w.gsm);
+            cta_gemm<T, true, false, M_UPPER>(64, ncols, 64, T(1), Tp, ldt, W, 64, T(0), W2, 64, w.gsm);
+            cta_gemm<T, false, false, M_UNIT_LOWER>(nb - p0, ncols, 64, T(-1), V, ld, W2, 64, T(1), C, ld, w.gsm);
+        }
+    }
+    // Y_a^T Y_Q: V_Q is zero above row q0 and unit on its diagonal block
+    assemble_t(w, nb, Tm, ldt, scr, [&](int q0, T *Ys, int ldy) {
+        cta_gemm<T, true, false, M_NONE, M_UNIT_LOWER>(q0, 64, nb - q0, T(1), A + q0, ld, A + q0 + (size_t)q0 * ld, ld,
+                                                       T(0), Ys, ldy, w.gsm);
     });
 }
 
-// TSQRT: QR of [R = A1 upper; A2] column by column; A2 becomes V, T into Tm.  A1's strictly
-// lower part (the GEQRT reflectors) is neither read nor written.
+// TSQRT: QR of [R = A1 upper; A2], blocked like geqrt: panels of 64 columns factored column
+// by column (A2 becomes V, A1's upper triangle R), trailing columns of [A1; A2] updated by the
+// panel's block reflector [E; V] (E: rows p0 .. p0 + 63 of A1), T assembled at the end.  A1's
+// strictly lower part (the GEQRT reflectors) is neither read nor written.  scr: two nb x 64
+// scratch blocks.
 template <class T>
-__device__ void tsqrt(const QrSmem<T> &w, T *A1, T *A2, int nb, int ld, T *Tm, int ldt) {
+__device__ void tsqrt(const QrSmem<T> &w, T *A1, T *A2, int nb, int ld, T *Tm, int ldt, T *scr) {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    for (int i = 0; i < nb; i++) {
-        T *vi = A2 + (size_t)i * ld;
-        const T ti = larfg(w.red, A1 + i + (size_t)i * ld, vi, nb);
-        if (threadIdx.x == 0) w.tau[i] = ti;
-        if (ti != T(0)) {
-            for (int j = i + 1 + warp; j < nb; j += NT / 32)
-                reflect_col(vi, A2 + (size_t)j * ld, A1 + i + (size_t)j * ld, 0, nb, ti, lane);
+    T *W = scr, *W2 = scr + (size_t)nb * 64;
+    for (int p0 = 0; p0 < nb; p0 += 64) {
+        for (int i = p0; i < p0 + 64; i++) {
+            T *vi = A2 + (size_t)i * ld;
+            const T ti = larfg(w.red, A1 + i + (size_t)i * ld, vi, nb);
+            if (threadIdx.x == 0) w.tau[i] = ti;
+            if (ti != T(0)) {
+                for (int j = i + 1 + warp; j < p0 + 64; j += NT / 32)
+                    reflect_col(vi, A2 + (size_t)j * ld, A1 + i + (size_t)j * ld, 0, nb, ti, lane);
+            }
+            __syncthreads();
         }
-        __syncthreads();
+        // panel T: the identity parts are orthogonal, z_j = <A2(:, j), A2(:, i)>
+        larft(w.red, 64, w.tau + p0, Tm + p0 + (size_t)p0 * ldt, ldt, [&](int j, int i, int ln) {
+            const T *cj = A2 + (size_t)(p0 + j) * ld, *ci = A2 + (size_t)(p0 + i) * ld;
+            T s = T(0);
+            for (int r = ln; r < nb; r += 32) s = fma(ldg(cj + r), ldg(ci + r), s);
+            return s;
+        });
+        const int ncols = nb - p0 - 64;
+        if (ncols > 0) {
+            // W = C1 + V^T C2; W2 = T^T W; C1 -= W2; C2 -= V W2
+            const T *V = A2 + (size_t)p0 * ld;
+            T *C1 = A1 + p0 + (size_t)(p0 + 64) * ld, *C2 = A2 + (size_t)(p0 + 64) * ld;
+            const T *Tp = Tm + p0 + (size_t)p0 * ldt;
+            cta_axpby<T>(64, ncols, T(1), C1, ld, T(0), W, 64);
+            cta_gemm<T, true, false>(64, ncols, nb, T(1), V, ld, C2, ld, T(1), W, 64, w.gsm);
+            cta_gemm<T, true, false, M_UPPER>(64, ncols, 64, T(1), Tp, ldt, W, 64, T(0), W2, 64, w.gsm);
+            cta_axpby<T>(64, ncols, T(-1), W2, 64, T(1), C1, ld);
+            cta_gemm<T, false, false>(nb, ncols, 64, T(-1), V, ld, W2, 64, T(1), C2, ld, w.gsm);
+        }
     }
-    // the identity parts of [I; V] are orthogonal: z_j = <A2(:, j), A2(:, i)>
-    larft(w.red, nb, w.tau, Tm, ldt, [&](int j, int i, int ln) {
-        const T *cj = A2 + (size_t)j * ld, *ci = A2 + (size_t)i * ld;
-        T s = T(0);
-        for (int r = ln; r < nb; r += 32) s = fma(ldg(cj + r), ldg(ci + r), s);
-        return s;
+    // Y_a^T Y_Q = V_a^T V_Q (the identity parts touch disjoint rows of A1)
+    assemble_t(w, nb, Tm, ldt, scr, [&](int q0, T *Ys, int ldy) {
+        cta_gemm<T, true, false>(q0, 64, nb, T(1), A2, ld, A2 + (size_t)q0 * ld, ld, T(0), Ys, ldy, w.gsm);
     });
 }
 
