@@ -1,10 +1,13 @@
 // tile_qr.cuh -- the flat-tree TS QR tile routines of the reference (src/qr.h tasks over
 // src/srcqr: GEQRT = dgeqr2 + dlarft, UNMQR = dlarfb, TSQRT, TSMQR = dparfb/dpamm) for one CTA
 // of 256 threads, on element type T.  The mixed-precision QR runs them in FP32 inside the FP32
-// task scheduler; they restate the published algorithms (LAPACK dlarfg / dlarft 'F','C' /
-// dlarfb 'L','T','F','C'; the TS kernels of tile QR) with the same output layout as the FP64
-// routines of sched_f64.cu: R in the upper triangle, V below the diagonal (unit implicit) and
-// in the full TSQRT tiles, T upper triangular in S.
+// task scheduler.  They restate the published algorithms (LAPACK dlarfg / dlarft 'F','C' /
+// dlarfb 'L','T','F','C'; the TS kernels of tile QR; the compact-WY merge of Schreiber and Van
+// Loan) with the output layout of the FP64 routines of sched_f64.cu: R in the upper triangle,
+// V below the diagonal (unit implicit) and in the full TSQRT tiles, T upper triangular in S.
+// GEQRT and TSQRT are blocked by 64-column panels (the same reflectors and T as the unblocked
+// column sweep up to rounding): the per-column, latency-bound work stays inside a panel and the
+// rest runs as CTA GEMMs.
 #pragma once
 #include <cfloat>
 
