@@ -39,6 +39,10 @@
  *   --batch COUNT           the synthetic uneven batch: COUNT matrices, N log-uniform in
  *                           [32, 2048), half Cholesky half LU, one persistent launch
  *   --autotune              choose the block size per size class by timing (batch mode)
+ *   --solve                 batched solves of the batch (one uniform right-hand side each) to
+ *                           FP64-level backward error: FP32 factorizations in one persistent
+ *                           launch + FP64 refinement (FP64 fallback per matrix); with --autotune
+ *                           block size and precision per algorithm and size class
  */
 #define _GNU_SOURCE
 #include <getopt.h>
@@ -128,16 +132,45 @@ static int run_batch(int count, unsigned long long seed, int autotune, int quiet
     return 0;
 }
 
+static int run_batch_solve(int count, unsigned long long seed, int autotune, int quiet)
+{
+    palial_batch_solve_report rep;
+    palial_status st;
+    int rc = palial_gpu_batch_solve_synthetic(count, seed, 0, 1, autotune, NULL, NULL, 3, &palial_entry_opts, &st,
+                                              &rep);
+    if (rc && rc != PALIAL_ERR_NOT_CONVERGED) {
+        fprintf(stderr, "palial: batch solve failed: %s (%s)\n", palial_gpu_error_string(rc), st.message);
+        return 1;
+    }
+    if (!quiet) {
+        printf("{\"batch_solve\": %d, \"seed\": %llu, \"autotune\": %d, \"converged\": %s", rep.count, seed,
+               autotune, rc == PALIAL_OK ? "true" : "false");
+        json_num("seconds", rep.seconds, "%.6f");
+        json_num("matrices_per_s", rep.matrices_per_s, "%.1f");
+        json_num("tflops", rep.tflops, "%.4f");
+        json_num("max_backward_error", rep.max_backward_error, "%.3e");
+        printf(", \"max_refinement_steps\": %d, \"fp64_fallbacks\": %d, \"choice\": [", rep.max_iters,
+               rep.fallbacks);
+        static const int edges[7] = {32, 64, 128, 256, 512, 1024, 2048};
+        for (int k = 0; k < 12; k++)
+            printf("%s{\"alg\": \"%s\", \"n\": [%d, %d], \"block\": %d, \"precision\": \"%s\"}", k ? ", " : "",
+                   k < 6 ? "cholesky" : "lu", edges[k % 6], edges[k % 6 + 1], rep.bs_of_class[k],
+                   rep.prec_of_class[k] ? "fp32+ir" : "fp64");
+        printf("]}\n");
+    }
+    return rc ? 1 : 0;
+}
+
 int main(int argc, char *argv[])
 {
     char algorithm[16] = "";
-    int gen = 2, check = 0, quiet = 0, nrhs = 0, batch = 0, autotune = 0, clocks = 0, seed_given = 0;
+    int gen = 2, check = 0, quiet = 0, nrhs = 0, batch = 0, autotune = 0, clocks = 0, seed_given = 0, solve = 0;
     unsigned long long seed = 0;
     const char *trace = NULL, *trace_csv = NULL, *load = NULL, *save = NULL, *save_result = NULL;
     palial_opts_default(&palial_entry_opts);
     enum {
         O_GEN = 1000, O_SEED, O_BLOCK, O_PRIO, O_TRACE, O_TRACECSV, O_CHECK, O_QUIET, O_PREC, O_RHS, O_IRTOL,
-        O_IRMAX, O_GMRES, O_BATCH, O_AUTOTUNE, O_CLOCKS, O_BUTTERFLY, O_LOAD, O_SAVE, O_SAVERES
+        O_IRMAX, O_GMRES, O_BATCH, O_AUTOTUNE, O_CLOCKS, O_BUTTERFLY, O_LOAD, O_SAVE, O_SAVERES, O_SOLVE
     };
     struct option long_options[] = {
         {"Algorithm", required_argument, NULL, 'a'}, {"Matrix size", required_argument, NULL, 'm'},
@@ -151,7 +184,8 @@ int main(int argc, char *argv[])
         {"batch", required_argument, NULL, O_BATCH}, {"autotune", no_argument, NULL, O_AUTOTUNE},
         {"clocks", no_argument, NULL, O_CLOCKS},     {"butterfly", required_argument, NULL, O_BUTTERFLY},
         {"load", required_argument, NULL, O_LOAD},   {"save", required_argument, NULL, O_SAVE},
-        {"save-result", required_argument, NULL, O_SAVERES}, {NULL, no_argument, NULL, 0}};
+        {"save-result", required_argument, NULL, O_SAVERES}, {"solve", no_argument, NULL, O_SOLVE},
+        {NULL, no_argument, NULL, 0}};
     if (argc < 2) {
         printf("Missing arguments.\n");
         printf("Aborting...\n");
@@ -186,6 +220,7 @@ int main(int argc, char *argv[])
             case O_GMRES: palial_entry_opts.gmres = atoi(optarg); break;
             case O_BATCH: batch = atoi(optarg); break;
             case O_AUTOTUNE: autotune = 1; break;
+            case O_SOLVE: solve = 1; break;
             case O_CLOCKS: clocks = 1; palial_entry_opts.trace = 1; break;
             case O_BUTTERFLY:
                 palial_entry_opts.reserved[6] = 1;
@@ -201,7 +236,8 @@ int main(int argc, char *argv[])
         }
     }
     if (batch > 0) {
-        const int rc = run_batch(batch, seed_given ? seed : 2, autotune, quiet);
+        const int rc = solve ? run_batch_solve(batch, seed_given ? seed : 2, autotune, quiet)
+                             : run_batch(batch, seed_given ? seed : 2, autotune, quiet);
         palial_gpu_finalize();
         return rc;
     }

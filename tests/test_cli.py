@@ -83,6 +83,14 @@ def test_batch_mode():
 
 
 @pytest.mark.gpu
+def test_batch_solve_mode():
+    rc, out = run("--batch", "40", "--solve")
+    j = _json(out)
+    assert rc == 0 and j["batch_solve"] == 40 and j["converged"] and j["matrices_per_s"] > 0
+    assert j["max_backward_error"] <= 1e-14 * 2048 and len(j["choice"]) == 12
+
+
+@pytest.mark.gpu
 def test_trace_file(tmp_path):
     f = tmp_path / "t.txt"
     rc, out = run("-a", "cholesky", "-m", "2048", "-b", "512", "--block", "512", "--trace", str(f), "--quiet")
