@@ -18,6 +18,12 @@ The JSON line also carries:
                 same matrix: its TFLOP/s and the mixed/FP64 speed-up;
   e2e           the same solve through the host-buffer C ABI (palial_gpu_solve_ir_host on
                 pinned host memory: A and B copied in, X copied out, every step);
+  e2e_pageable  the same from a pageable (malloc'd) host buffer, as the reference's caller has;
+  kappa         config 3 at N = 32768, kappa = 1e6, Cholesky and LU: the precision ladder's
+                solve (rung used, refinement and GMRES steps, FP64-checked backward error,
+                forward error against the FP64 solve) beside the FP64 factorization's solve;
+  lu, qr        no-pivot LU (kappa = 1e2 matrix) and QR (uniform [-1, 1), seed 1) at N = 32768:
+                mixed-precision solve time beside the FP64 solve (--no-extra skips these three);
   roofline      the tcgen05 trailing-update kernel (the mixed path's tensor-core kernel),
                 timed live on the largest step (k = 0); bound chosen by its arithmetic
                 intensity against the measured ridge (BF16x3: tensor), achieved / measured
@@ -144,8 +150,8 @@ def fp64_peak_tflops(torch) -> float:
 
 def cpu_baseline_sample(nthreads: int, seed: int = 0, spd_host=None) -> tuple[float, float]:
     """Oracle OpenMP port (reference task DAG over OpenBLAS) on one N = CPU_N Cholesky."""
+    import numpy as np  # first: numpy's own BLAS keeps every host thread for the generator
     from oracle import oracle as O
-    import numpy as np
 
     a = spd_host if spd_host is not None else O.to_tiles(O.gen_spd(seed, CPU_N), NB)
     t = np.array(a, copy=True)
@@ -163,20 +169,30 @@ def spd_host_from_gpu(P, torch, n: int, seed: int):
     return h
 
 
+def headline_config(n: int, precision: str, world: int) -> dict:
+    """The workload both arms report on (the reference arm times a bounded sample of it)."""
+    return {"workload": f"mixed-precision Cholesky + IR, N={n}, NB={NB}, 16 RHS, {precision} "
+                        "trailing updates on tcgen05 (FP32 accumulate), FP32 diagonal tiles and "
+                        "panels, compensated-FP32 and update-form refinement residuals, FP64-checked backward "
+                        "error; SPD B*B^T+N*I seed=rank, device-resident; inputs 8.6 GB >> L2 (no flush needed)",
+            "n": n, "nb": NB, "nrhs": 16, "precision": precision, "parallelism": f"replicas x{world}"}
+
+
 def run_reference(args, rank: int, world: int) -> None:
+    """The reference's CPU implementation of the path (the oracle's OpenMP restatement of
+    src/cholesky.h over OpenBLAS, bit-identical to the reference's own build) on every host
+    core.  Input generated on the host by the oracle's generator; nothing of the GPU library is
+    loaded.  Each step is one FP64 Cholesky at N = CPU_N (about 2.4 s on 16 Arm cores): a
+    bounded sample of the N = 32768 workload, whose 8x larger run (about 20 s a step) would
+    hold the whole --steps/--warmup run for many minutes."""
     if rank != 0:
         return
     nthreads = os.cpu_count() or 1
+    import numpy as np  # noqa: F401  (before the oracle: numpy's BLAS keeps all host threads)
+    from oracle import oracle as O
+
+    spd = O.to_tiles(O.gen_spd(0, CPU_N), NB)
     times = []
-    spd = None
-    try:
-        import torch  # noqa: F401
-        if torch.cuda.is_available():
-            import palial_gb300 as P
-            P.init(0)
-            spd = spd_host_from_gpu(P, torch, CPU_N, 0)
-    except Exception:  # the CPU arm does not need a GPU: generate on the host instead
-        spd = None
     for i in range(args.warmup + args.steps):
         _, sec = cpu_baseline_sample(nthreads, spd_host=spd)
         if i >= args.warmup:
@@ -187,14 +203,30 @@ def run_reference(args, rank: int, world: int) -> None:
         "impl": "reference", "metric": METRIC, "value": value, "unit": "TFLOP/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": sec * 1e3, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": f"tiled Cholesky FP64, N={CPU_N} (bounded sample of N={N}), NB={NB}, "
-                               f"SPD B*B^T+N*I seed 0", "n": CPU_N, "nb": NB},
+        "config": headline_config(N, args.precision, world),
         "cpu_baseline": {"value": value, "unit": "TFLOP/s", "cores": nthreads, "kind": "port",
-                         "sample": f"one Cholesky N={CPU_N} NB={NB} per step: the oracle's OpenMP restatement "
-                                   "of reference src/cholesky.h over OpenBLAS, OMP_NUM_THREADS=all cores"},
+                         "sample": f"one FP64 Cholesky N={CPU_N} NB={NB} per step (bounded sample of the N={N} "
+                                   "workload, same SPD generator, seed 0): the oracle's OpenMP restatement of "
+                                   "reference src/cholesky.h over OpenBLAS, OMP_NUM_THREADS=all cores, "
+                                   "OPENBLAS_NUM_THREADS=1; input generated on the host"},
         "e2e": {"value": value, "unit": "TFLOP/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "native_libraries": in_tree_libraries(),
     }
     print(json.dumps(line), flush=True)
+
+
+def in_tree_libraries() -> list[str]:
+    """Shared objects of this repository mapped into the process (Linux /proc/self/maps)."""
+    found = set()
+    try:
+        with open("/proc/self/maps") as f:
+            for line in f:
+                path = line.split()[-1] if len(line.split()) >= 6 else ""
+                if path.endswith(".so") and path.startswith(ROOT):
+                    found.add(os.path.relpath(path, ROOT))
+    except OSError:
+        pass
+    return sorted(found)
 
 
 def fp64_backward_error(P, torch, a0, n: int, nb: int, x, b, nrhs: int) -> float:
@@ -258,6 +290,69 @@ def time_update_kernel(P, torch, n: int, precision: str = "bf16") -> dict:
     byts = pairs * NB * NB * 8.0 + r * NB * NB * (4.0 + 2.0 * packed)
     t = min(ts)
     return {"seconds": t, "flop": flop, "bytes": byts}
+
+
+def _solve(P, torch, alg: str, da, n: int, b, nrhs: int, precision: str, stream: int):
+    x = torch.zeros_like(b)
+    st = P.solve_ir(alg, da.data_ptr(), n, NB, b.data_ptr(), x.data_ptr(), nrhs, precision=precision,
+                    ir_max_iter=30, stream=stream, raise_on_error=False)
+    torch.cuda.synchronize()
+    return st, x
+
+
+def _fwd(torch, x, xref, nrhs: int) -> float:
+    """max_j ||x_j - xref_j||_inf / ||xref_j||_inf."""
+    xv, rv = x.view(nrhs, -1), xref.view(nrhs, -1)
+    return float(((xv - rv).abs().amax(dim=1) / rv.abs().amax(dim=1)).max())
+
+
+def config_keys(P, torch, n: int, b, nrhs: int, stream: int) -> dict:
+    """One run each of the metric's other configurations at N = n (untimed by the step loop;
+    each call's own wall time): config 3's kappa = 1e6 matrices (A = U diag(s) V^T, s geometric
+    from 1 to 1/kappa, 64 Householder reflectors each side; U = V for Cholesky) solved by the
+    precision ladder (AUTO) and by the FP64 factorization + FP64 refinement, with the backward
+    error recomputed by the FP64 residual and the forward error of the ladder's X against the
+    FP64 solve's; no-pivot LU at kappa = 1e2 (ladder vs FP64); the QR solve of the uniform
+    [-1, 1) matrix (seed 1) by the FP32 tile QR + FP64 refinement vs the FP64 QR solve."""
+    out = {}
+    da = torch.empty(n * n, dtype=torch.float64, device="cuda")
+    flop = {"cholesky": n ** 3 / 3.0, "lu": 2.0 * n ** 3 / 3.0, "qr": 4.0 * n ** 3 / 3.0}
+
+    def ladder_vs_fp64(alg: str, kappa: float) -> dict:
+        P.gen_kappa(da.data_ptr(), n, NB, kappa, alg == "cholesky", seed=7)
+        st, x = _solve(P, torch, alg, da, n, b, nrhs, "auto", stream)
+        eta = fp64_backward_error(P, torch, da, n, NB, x, b, nrhs)
+        st64, x64 = _solve(P, torch, alg, da, n, b, nrhs, "fp64", stream)
+        rec = {"kappa": kappa, "converged": st.code in (0, 1), "precision_used": P.PREC_NAME.get(st.precision_used),
+               "seconds": st.seconds, "tflops_fp64_equiv": flop[alg] / st.seconds * 1e-12,
+               "ir_iters": st.ir_iters, "gmres_iters": st.gmres_iters, "backward_error_fp64_check": eta,
+               "forward_error_vs_fp64_solve": _fwd(torch, x, x64, nrhs),
+               "fp64_solve": {"seconds": st64.seconds, "tflops": flop[alg] / st64.seconds * 1e-12,
+                              "converged": st64.code in (0, 1), "backward_error": st64.backward_error},
+               "speedup_over_fp64": st64.seconds / st.seconds}
+        del x, x64
+        return rec
+
+    out["kappa"] = {"n": n, "nb": NB, "nrhs": nrhs, "cholesky": ladder_vs_fp64("cholesky", 1e6),
+                    "lu": ladder_vs_fp64("lu", 1e6),
+                    "note": "forward error floor of any backward-stable solve is about kappa * 1e-16"}
+    out["lu"] = dict(ladder_vs_fp64("lu", 1e2), n=n, nb=NB, nrhs=nrhs, matrix="U diag(s) V^T, kappa 1e2")
+    P.gen_uniform(da.data_ptr(), n, NB, 1)
+    x = torch.zeros_like(b)
+    st = P.qr_solve_ir(da.data_ptr(), n, NB, b.data_ptr(), x.data_ptr(), nrhs, allow_not_converged=True)
+    eta = fp64_backward_error(P, torch, da, n, NB, x, b, nrhs)
+    x64 = torch.zeros_like(b)
+    s64 = P.qr_solve(da.data_ptr(), n, n, NB, b.data_ptr(), x64.data_ptr(), nrhs)
+    out["qr"] = {"n": n, "nb": NB, "nrhs": nrhs, "matrix": "uniform [-1, 1), seed 1",
+                 "converged": st.code == 0, "precision_used": P.PREC_NAME.get(st.precision_used),
+                 "seconds": st.seconds, "factor_seconds": st.factor_seconds,
+                 "tflops_fp64_equiv": flop["qr"] / st.seconds * 1e-12, "ir_iters": st.ir_iters,
+                 "backward_error_fp64_check": eta, "forward_error_vs_fp64_solve": _fwd(torch, x, x64, nrhs),
+                 "fp64_solve": {"seconds": s64.seconds, "tflops": flop["qr"] / s64.seconds * 1e-12},
+                 "speedup_over_fp64": s64.seconds / st.seconds}
+    del da, x, x64
+    torch.cuda.empty_cache()
+    return out
 
 
 def run_batched(args, P, torch, rank: int = 0, world: int = 1) -> None:
@@ -457,7 +552,7 @@ def run_qr_mixed(args, P, torch) -> None:
                     "seconds": st.seconds, "factor_seconds": st.factor_seconds, "ir_iters": st.ir_iters,
                     "backward_error": st.backward_error,
                     "tflops_fp64_equiv": 4.0 * n ** 3 / 3.0 / st.seconds * 1e-12,
-                    "precision_used": "fp32" if int(st.kappa_est) == 5 else "fp64", "message": st.message.decode()}
+                    "precision_used": "fp32" if st.precision_used == 5 else "fp64", "message": st.message.decode()}
             if nb == NB:
                 x.zero_()
                 s64 = P.qr_solve(da.data_ptr(), n, n, NB, b.data_ptr(), x.data_ptr(), nrhs)
@@ -512,7 +607,7 @@ def run_suite(args, P, torch) -> None:
         for kappa in (1e2, 1e6, 1e10):
             da = torch.empty(n * n, dtype=torch.float64, device="cuda")
             P.gen_kappa(da.data_ptr(), n, NB, kappa, alg == "cholesky", seed=7)
-            precs = ("bf16", "fp8", "bf16x3", "auto") + (("bf16x3-rbt",) if alg == "lu" else ())
+            precs = ("bf16", "fp8", "bf16x3", "tf32x3", "auto") + (("bf16x3-rbt",) if alg == "lu" else ())
             for prec in precs:
                 dx = torch.zeros_like(b)
                 o = P.make_opts(precision=prec.split("-")[0], ir_max_iter=30)
@@ -525,7 +620,7 @@ def run_suite(args, P, torch) -> None:
                                   "gmres_iters": st.gmres_iters, "backward_error": st.backward_error,
                                   "seconds": st.seconds, "factor_seconds": st.factor_seconds, "shift": st.shift,
                                   "tflops_fp64_equiv": st.tflops,
-                                  "precision_used": (P.PREC_NAME.get(int(st.kappa_est), prec)
+                                  "precision_used": (P.PREC_NAME.get(st.precision_used, prec)
                                                      if prec == "auto" else prec)}), flush=True)
             del da
             torch.cuda.empty_cache()
@@ -545,6 +640,7 @@ def main() -> None:
                                                       "kernels", "qr_mixed"])
     ap.add_argument("--batch", type=int, default=2000)
     ap.add_argument("--no-fp64", action="store_true")
+    ap.add_argument("--no-extra", action="store_true", help="skip the kappa / lu / qr keys")
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)
     rank, world, local = dist_info()
@@ -632,6 +728,9 @@ def main() -> None:
         del a
         torch.cuda.empty_cache()
 
+    # the metric's other configurations (kappa = 1e6 Cholesky / LU, LU, QR) at N = n, once each
+    extra = {} if args.no_extra else config_keys(P, torch, n, b, nrhs, stream.cuda_stream)
+
     # roofline: live timing of the tcgen05 update kernel at its largest step
     pk = peaks()
     upd = time_update_kernel(P, torch, n, args.precision)
@@ -661,7 +760,21 @@ def main() -> None:
             e2e_times.append(time.perf_counter() - t0)
     e2e_sec = sum(e2e_times) / len(e2e_times) if e2e_times else float("nan")
     e2e_value = world * flops(n) / e2e_sec * 1e-12
-    del host
+    # the same from pageable host memory, as the reference's own caller allocates it
+    # (posix_memalign, palial_src/main.c:110): numpy's buffer is ordinary malloc'd memory
+    page = np.empty(n * n)
+    page[:] = host_np
+    del host, host_np
+    page_times = []
+    for i in range(1 + max(1, args.e2e_steps // 2)):
+        barrier()
+        t0 = time.perf_counter()
+        P.solve_ir_host("cholesky", page, n, NB, bhc, xh, nrhs, precision=args.precision, raise_on_error=False)
+        barrier()
+        if i >= 1:
+            page_times.append(time.perf_counter() - t0)
+    page_sec = sum(page_times) / len(page_times)
+    del page
 
     if rank == 0:
         cpu = None
@@ -676,17 +789,18 @@ def main() -> None:
             "metric": METRIC, "value": value, "unit": "TFLOP/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": per_step * 1e3, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "bf16", "data": "synthetic",
-            "config": {"workload": f"mixed-precision Cholesky + IR, N={n}, NB={NB}, 16 RHS, {args.precision} "
-                                   "trailing updates on tcgen05 (FP32 accumulate), FP32 diagonal tiles and "
-                                   "panels, compensated-FP32 and update-form refinement residuals, FP64-checked backward error; SPD B*B^T+N*I seed=rank, device-resident; inputs 8.6 GB >> L2 "
-                                   "(no flush needed)",
-                       "n": n, "nb": NB, "nrhs": nrhs, "precision": args.precision,
-                       "parallelism": f"replicas x{world}"},
+            "config": headline_config(n, args.precision, world),
             "converged": converged, "backward_error": eta, "backward_error_fp64_check": eta_fp64,
             "ir_iters": launches,
             "fp64_tiled": fp64,
             "e2e": {"value": e2e_value, "unit": "TFLOP/s", "h2d_bytes_per_step": 8 * n * n + 8 * n * nrhs,
-                    "d2h_bytes_per_step": 8 * n * nrhs, "step_seconds": [round(t, 5) for t in e2e_times]},
+                    "d2h_bytes_per_step": 8 * n * nrhs, "step_seconds": [round(t, 5) for t in e2e_times],
+                    "host_buffer": "pinned (page-locked) A"},
+            "e2e_pageable": {"value": world * flops(n) / page_sec * 1e-12, "unit": "TFLOP/s",
+                             "h2d_bytes_per_step": 8 * n * n + 8 * n * nrhs, "d2h_bytes_per_step": 8 * n * nrhs,
+                             "step_seconds": [round(t, 5) for t in page_times],
+                             "host_buffer": "pageable A (numpy / malloc), as the reference's caller"},
+            **extra,
             "roofline": {"bound": bound, "achieved": achieved, "peak": peak, "unit": unit,
                          "frac": achieved / peak,
                          "hbm_gbs": gbs, "hbm_frac": gbs / pk.get("hbm_gbs", 6800.0),

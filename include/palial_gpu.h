@@ -47,6 +47,8 @@ extern "C" {
 #define PALIAL_PREC_BF16X3 3       /* trailing updates as 3 BF16 products (split operands)  */
 #define PALIAL_PREC_AUTO 4         /* solve_ir: precision ladder BF16 -> BF16x3 -> FP64      */
 #define PALIAL_PREC_FP32 5         /* batched solves: FP32 factorization, FP64 refinement    */
+#define PALIAL_PREC_TF32X3 6       /* trailing updates as 3 TF32 products (split operands):
+                                      FP32-level factors on tcgen05 (kind::tf32)            */
 
 /* ---- descriptor ------------------------------------------------------------------------ */
 /* Same field order, types and meaning as the reference's MATRIX_desc
@@ -93,6 +95,9 @@ typedef struct palial_status {
     double kappa_est;       /* condition estimate used to choose the method (-1: none) */
     double factor_seconds;  /* time of the factorization part (solve_ir)              */
     double shift;           /* diagonal shift used by a low-precision Cholesky        */
+    int precision_used;     /* solves: PALIAL_PREC_* of the factorization that produced X
+                               (+100: LU of the random-butterfly transform)           */
+    int fallbacks;          /* batched solves: matrices refactored in FP64            */
     char message[160];
 } palial_status;
 
@@ -149,9 +154,11 @@ int palial_gpu_factor_dev(int alg, double *dA, double *dS, int n, int nb, const 
  * full instead.  The status message counts the update-form residuals.
  * Opt-in stabilised LU (alg = PALIAL_ALG_LU, mixed precisions): opts->reserved[6] = 1 factors
  * the random-butterfly transform U^T A V (depth-2 recursive butterflies, Parker 1995) without
- * pivoting instead of A, refines against A (seed: opts->reserved[7], 0 = 1).  The AUTO ladder
- * for LU tries BF16, BF16x3, BF16x3 on the butterfly transform, then FP64; status.kappa_est
- * reports the rung that produced the result (PALIAL_PREC_*, + 100 for the butterfly rung). */
+ * pivoting instead of A, refines against A (seed: opts->reserved[7], 0 = 1).  PALIAL_PREC_AUTO
+ * runs a precision ladder: BF16x3 (at most 10 refinement steps and 30 GMRES iterations), then
+ * TF32x3 (FP32-level factors; 10 steps, 400 GMRES iterations), then the FP64 factorization;
+ * status.precision_used reports the rung that produced the result (PALIAL_PREC_*, + 100 for the
+ * butterfly transform). */
 int palial_gpu_solve_ir(int alg, const double *dA, int n, int nb, const double *dB, double *dX,
                         int nrhs, const palial_opts *opts, palial_status *st, void *stream);
 /* Same with host buffers: A in the reference's tile layout (descriptor), B and X n x nrhs
@@ -191,7 +198,7 @@ int palial_gpu_qr_solve(int rows, int cols, int nb, const double *dA, const doub
  * backward error |r_j|/(|A||x_j| + |b_j|) <= opts->ir_tol (0: 1e-14 * n).  NB: a multiple of
  * 64 up to 512.  A refinement that does not halve the error per step (or exceeds
  * opts->ir_max_iter, 0 = 30) hands the system to palial_gpu_qr_solve (FP64).  status:
- * ir_iters, backward_error, factor_seconds, kappa_est = the precision that produced the
+ * ir_iters, backward_error, factor_seconds, precision_used = the precision that produced the
  * result (PALIAL_PREC_FP32 or PALIAL_PREC_FP64). */
 int palial_gpu_qr_solve_ir(int n, int nb, const double *dA, const double *dB, double *dX, int nrhs,
                            const palial_opts *opts, palial_status *st, void *stream);
@@ -250,9 +257,11 @@ int palial_gpu_tile_stsmqr(int nb, float *dA1, float *dA2, const float *dV, cons
  * cudaStream_t as void*, NULL = default stream); the call only enqueues the kernel.
  * Limit: nb <= 512 (a multiple of 64); larger tiles return PALIAL_ERR_ARG.  Its scratch is a
  * fixed 512 KiB array inside the library, held by every GPU that loads it until the process
- * exits.  The first call on a device looks up that array's device address, so make that
- * first call before capturing a stream.  All calls share the one array: calls whose kernels
- * overlap on the GPU (unordered streams, other host threads) race on it. */
+ * exits.  The first call on a device looks up that array's device address (thread-safe), so
+ * make that first call before capturing a stream.  The address belongs to the device's context
+ * at that call: after cudaDeviceReset, call palial_gpu_finalize() before calling this again (it
+ * makes the next call look the address up anew).  All calls share the one array: calls whose
+ * kernels overlap on the GPU (unordered streams, other host threads) race on it. */
 int palial_gpu_tile_dtsmqr_noalloc(int nb, double *dA1, double *dA2, const double *dV,
                                    const double *dT, int lda, void *stream);
 /* kind for dtrsm: 0 = left upper trans non-unit (Cholesky), 1 = right upper no-trans non-unit

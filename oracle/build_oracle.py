@@ -19,7 +19,10 @@ import subprocess
 import sys
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-REF_DEFAULT = "/root/reference"
+# The reference checkout: $PALIAL_REFERENCE, else a "reference" directory beside this
+# repository (absent on machines without a checkout; the reference build is then skipped).
+REF_DEFAULT = os.environ.get("PALIAL_REFERENCE") or os.path.join(
+    os.path.dirname(os.path.dirname(os.path.realpath(HERE))), "reference")
 
 
 def find_openblas() -> str:

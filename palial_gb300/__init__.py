@@ -23,7 +23,7 @@ ERR = {
     -7: "device allocation failed", 1: "exact zero pivot skipped",
 }
 ALG = {"cholesky": 0, "lu": 1, "qr": 2}
-PREC = {"fp64": 0, "bf16": 1, "fp8": 2, "bf16x3": 3, "auto": 4, "fp32": 5}
+PREC = {"fp64": 0, "bf16": 1, "fp8": 2, "bf16x3": 3, "auto": 4, "fp32": 5, "tf32x3": 6}
 PREC_NAME = {v: k for k, v in PREC.items()}
 PREC_NAME[100 + PREC["bf16x3"]] = "bf16x3-rbt"  # AUTO ladder rung: BF16x3 on the butterfly transform
 
@@ -55,6 +55,7 @@ class Status(ctypes.Structure):
                 ("tflops", ctypes.c_double), ("ir_iters", ctypes.c_int), ("gmres_iters", ctypes.c_int),
                 ("backward_error", ctypes.c_double), ("kappa_est", ctypes.c_double),
                 ("factor_seconds", ctypes.c_double), ("shift", ctypes.c_double),
+                ("precision_used", ctypes.c_int), ("fallbacks", ctypes.c_int),
                 ("message", ctypes.c_char * 160)]
 
     def as_dict(self) -> dict:
@@ -322,7 +323,7 @@ def qr_solve_ir(d_a: int, n: int, nb: int, d_b: int, d_x: int, nrhs: int, stream
                 allow_not_converged: bool = False, **kw) -> Status:
     """Mixed-precision QR solve of a square A X = B on device buffers (A tile layout, B and X
     n x nrhs column-major): FP32 tile QR + FP64 refinement, the FP64 QR solve when the
-    refinement stalls.  status.kappa_est = the precision that produced X (5 FP32, 0 FP64)."""
+    refinement stalls.  status.precision_used = the precision that produced X (5 FP32, 0 FP64)."""
     st = Status()
     rc = lib().palial_gpu_qr_solve_ir(n, nb, d_a, d_b, d_x, nrhs, ctypes.byref(make_opts(**kw)), ctypes.byref(st),
                                       stream or None)

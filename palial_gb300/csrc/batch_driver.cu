@@ -158,7 +158,7 @@ int run_solve_batch(SolveBatch &b, const palial_opts &o, SolveResult &res, palia
     res.rc = rc;
     res.seconds = s2.seconds;
     res.worst = s2.backward_error;
-    res.fallbacks = (int)s2.ntasks;
+    res.fallbacks = s2.fallbacks;
     res.max_iters = s2.ir_iters;
     return PALIAL_OK;
 }

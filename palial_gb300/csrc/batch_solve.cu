@@ -657,7 +657,7 @@ int batched_solve_run(int count, const int *algs, const int *ns, const int *nbs,
         st->tflops = flops / std::max(1e-12, wall) * 1e-12;
         st->ir_iters = max_it;
         st->backward_error = worst;
-        st->ntasks = (long long)fb.size();  // matrices refactored in FP64
+        st->fallbacks = (int)fb.size();  // matrices refactored in FP64
     }
     if (not_conv)
         return set_status(st, PALIAL_ERR_NOT_CONVERGED, "%d of %d matrices above their tolerance (worst %.3g)",

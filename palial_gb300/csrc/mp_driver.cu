@@ -88,11 +88,17 @@ struct MpBufs {
 };
 MpBufs mb;
 
+// Update-kernel mode (mp_gemm.cu) of a PALIAL_PREC_* precision: 0 bf16, 1 fp8, 2 bf16x3, 3 tf32x3.
+int update_mode(int prec) {
+    return prec == PALIAL_PREC_FP8 ? 1 : prec == PALIAL_PREC_BF16X3 ? 2 : prec == PALIAL_PREC_TF32X3 ? 3 : 0;
+}
+
 double unit_roundoff(int prec) {
     switch (prec) {
         case PALIAL_PREC_BF16: return 0x1.0p-8;
         case PALIAL_PREC_FP8: return 0x1.0p-4;
         case PALIAL_PREC_BF16X3: return 0x1.0p-16;
+        case PALIAL_PREC_TF32X3: return 0x1.0p-21;
         default: return 0x1.0p-24;
     }
 }
@@ -186,7 +192,7 @@ static ArrivalPlan plan_arrival(int mt, int nb, int mode, int ngroups, const int
     int present = ge[0], next_group = 1;
     int applied[64] = {};
     bool waited[64] = {};
-    const long long chain_pairs = (mode == 2 ? 1000 : 3000) * 512 / nb;
+    const long long chain_pairs = (mode == 3 ? 500 : mode == 2 ? 1000 : 3000) * 512 / nb;
     const auto pairs_of = [&](int r0, int r1) {  // tile pairs (r, j >= r) of rows [r0, r1)
         long long c = 0;
         for (int r = r0; r < r1; r++) c += mt - r;
@@ -237,8 +243,9 @@ static cudaError_t lookahead_init() {
 
 int mp_factor(int alg, int prec, float *W, int n, int nb, cudaStream_t s, palial_status *st, int *zero_piv) {
     const int mt = n / nb;
-    const int mode = prec == PALIAL_PREC_FP8 ? 1 : prec == PALIAL_PREC_BF16X3 ? 2 : 0;
-    const size_t elem = (mode == 1) ? 1 : 2;
+    const int mode = update_mode(prec);
+    const bool split = mode == 2 || mode == 3;  // hi + lo operand copies
+    const size_t elem = (mode == 1) ? 1 : (mode == 3) ? 4 : 2;
     const size_t panel = (size_t)std::max(1, mt - 1) * nb * nb * elem;
     const bool arrive = g_arrival.on && alg == 0 && mt > 2;
     g_arrival.on = false;
@@ -246,7 +253,7 @@ int mp_factor(int alg, int prec, float *W, int n, int nb, cudaStream_t s, palial
     const int slots = arrive ? mt - 1 : 2;
     PALIAL_CK(mb.pa_hi.ensure(slots * panel), "alloc panel");
     PALIAL_CK(mb.pb_hi.ensure(2 * panel), "alloc panel");
-    if (mode == 2) {
+    if (split) {
         PALIAL_CK(mb.pa_lo.ensure(slots * panel), "alloc panel");
         PALIAL_CK(mb.pb_lo.ensure(2 * panel), "alloc panel");
     }
@@ -275,13 +282,13 @@ int mp_factor(int alg, int prec, float *W, int n, int nb, cudaStream_t s, palial
         if (k == mt - 1) break;
         const int par = arrive ? k : (k & 1);
         float *sa = mb.scales.as<float>() + 2 * mt * par, *sb = sa + mt;
-        void *ah = buf(mb.pa_hi, par), *al = mode == 2 ? buf(mb.pa_lo, par) : nullptr;
-        void *bh = buf(mb.pb_hi, k & 1), *bl = mode == 2 ? buf(mb.pb_lo, k & 1) : nullptr;
+        void *ah = buf(mb.pa_hi, par), *al = split ? buf(mb.pa_lo, par) : nullptr;
+        void *bh = buf(mb.pb_hi, k & 1), *bl = split ? buf(mb.pb_lo, k & 1) : nullptr;
         float *binv = mb.binv.as<float>();
         PALIAL_CK(mps_block_inverse(W, n, nb, k, alg == 0 ? 1 : 2, binv, hi), "diagonal block inverses");
         // BF16 / BF16x3: the row-panel solve writes the packed operand with its results; FP8
-        // needs per-tile scales first, so it packs in a separate pass
-        const bool fused = mode != 1;
+        // needs per-tile scales first and TF32x3 FP32 containers, so they pack in a separate pass
+        const bool fused = mode == 0 || mode == 2;
         if (alg == 0) {
             PALIAL_CK(mps_panel_trsm(W, n, nb, k, 0, binv, hi, fused ? ah : nullptr, fused ? al : nullptr), "panel trsm");
             if (!fused) PALIAL_CK(mp_pack_rows(mode, W, n, nb, k, ah, al, sa, hi), "pack");
@@ -313,7 +320,7 @@ int mp_factor(int alg, int prec, float *W, int n, int nb, cudaStream_t s, palial
                         continue;
                     }
                     float *ss = mb.scales.as<float>() + 2 * mt * sk;
-                    void *sh = buf(mb.pa_hi, sk), *sl = mode == 2 ? buf(mb.pa_lo, sk) : nullptr;
+                    void *sh = buf(mb.pa_hi, sk), *sl = split ? buf(mb.pa_lo, sk) : nullptr;
                     PALIAL_CK(mp_update(mode, 1, W, n, nb, sk, sh, sl, sh, sl, ss, ss, status, lo, 3,
                                         ar.gs[gi] - sk - 1, ar.ge[gi] - sk - 1),
                               "update (arrived rows)");
@@ -595,8 +602,8 @@ extern "C" int palial_gpu_mp_update_step(int alg, int precision, float *dW, int 
     int rc = ensure_init(nullptr);
     if (rc) return rc;
     const int mt = n / nb;
-    const int mode = precision == PALIAL_PREC_FP8 ? 1 : precision == PALIAL_PREC_BF16X3 ? 2 : 0;
-    const size_t panel = (size_t)std::max(1, mt - 1) * nb * nb * 2;
+    const int mode = update_mode(precision);
+    const size_t panel = (size_t)std::max(1, mt - 1) * nb * nb * 4;
     PALIAL_CK(mb.pa_hi.ensure(panel), "alloc");
     PALIAL_CK(mb.pa_lo.ensure(panel), "alloc");
     PALIAL_CK(mb.pb_hi.ensure(panel), "alloc");
@@ -921,42 +928,38 @@ static int solve_one(int alg, const double *dA, int n, int nb, const double *dB,
                       st ? st->ir_iters : it, shift, resid_updates);
 }
 
-// Precision ladder (PALIAL_PREC_AUTO): the cheapest update precision first; when refinement
-// misses the target, the factorization is redone one rung up (FP8 -> BF16 -> BF16x3 -> FP64).
-// The status reports the precision that converged (opts precision field of st->message) and
-// the total time of all attempts.
+// Precision ladder (PALIAL_PREC_AUTO): BF16x3 updates first (about 2^-16 per product, the
+// fastest rung on well-conditioned systems), then TF32x3 (FP32-level factors, about 2^-21),
+// then the FP64 factorization.  A rung that misses the target within its budget (refinement
+// steps and GMRES iterations) hands over to the next; the status reports the rung that
+// produced the result (precision_used) and the total time of all attempts.
 extern "C" int palial_gpu_solve_ir(int alg, const double *dA, int n, int nb, const double *dB, double *dX, int nrhs,
                                    const palial_opts *opts, palial_status *st, void *stream) {
     palial_opts o;
     palial_opts_default(&o);
     if (opts) o = *opts;
-    if (o.precision != PALIAL_PREC_AUTO) return solve_one(alg, dA, n, nb, dB, dX, nrhs, &o, st, stream);
-    // LU adds a BF16x3 rung on the random-butterfly transform before the FP64 factorization
-    static const int ladder_chol[] = {PALIAL_PREC_BF16, PALIAL_PREC_BF16X3, PALIAL_PREC_FP64, -1};
-    static const int ladder_lu[] = {PALIAL_PREC_BF16, PALIAL_PREC_BF16X3, 100 + PALIAL_PREC_BF16X3, PALIAL_PREC_FP64};
-    const int *ladder = alg == 1 ? ladder_lu : ladder_chol;
+    if (o.precision != PALIAL_PREC_AUTO) {
+        const int rc = solve_one(alg, dA, n, nb, dB, dX, nrhs, &o, st, stream);
+        if (st) st->precision_used = o.precision + (alg == 1 && o.reserved[6] == 1 && o.precision != PALIAL_PREC_FP64 ? 100 : 0);
+        return rc;
+    }
+    static const int ladder[] = {PALIAL_PREC_BF16X3, PALIAL_PREC_TF32X3, PALIAL_PREC_FP64};
     const auto t0 = std::chrono::steady_clock::now();
     int rc = PALIAL_ERR_NOT_CONVERGED;
     int used = -1;
-    for (int li = 0; li < 4 && ladder[li] >= 0; li++) {
-        const int prec = ladder[li] % 100;
-        o.precision = prec;
-        o.reserved[6] = ladder[li] >= 100 ? 1 : opts ? opts->reserved[6] : 0;
-        // lower rungs get a bounded effort: BF16 plain refinement that must contract 10x per
-        // step, BF16x3 at most 10 outer iterations and 100 GMRES steps
+    for (int li = 0; li < 3; li++) {
+        const int prec = ladder[li];
         palial_opts oo = o;
-        if (prec == PALIAL_PREC_BF16) {
-            // plain refinement only; leave as soon as it contracts by less than 10x per step
+        oo.precision = prec;
+        // lower rungs get a bounded effort: at most 10 refinement steps, GMRES restarts of
+        // (BF16x3) 30 or (TF32x3) 100 iterations and a total of 30 or 400
+        if (prec != PALIAL_PREC_FP64) {
             if (oo.ir_max_iter <= 0 || oo.ir_max_iter > 10) oo.ir_max_iter = 10;
-            oo.gmres = -1;
-            oo.reserved[5] = 1;
-        } else if (prec != PALIAL_PREC_FP64) {
-            if (oo.ir_max_iter <= 0 || oo.ir_max_iter > 10) oo.ir_max_iter = 10;
-            oo.reserved[1] = 50;
-            oo.reserved[3] = 100;
+            oo.reserved[1] = prec == PALIAL_PREC_BF16X3 ? 30 : 100;
+            oo.reserved[3] = prec == PALIAL_PREC_BF16X3 ? 30 : 400;
         }
         rc = solve_one(alg, dA, n, nb, dB, dX, nrhs, &oo, st, stream);
-        used = ladder[li];  // 100 + p: precision p on the random-butterfly transform
+        used = prec + (alg == 1 && oo.reserved[6] == 1 && prec != PALIAL_PREC_FP64 ? 100 : 0);
         if (rc >= 0) break;
         if (rc != PALIAL_ERR_NOT_CONVERGED && rc != PALIAL_ERR_NOT_SPD) break;
     }
@@ -964,7 +967,7 @@ extern "C" int palial_gpu_solve_ir(int alg, const double *dA, int n, int nb, con
     if (st) {
         st->seconds = st->total_seconds = total;
         st->tflops = algorithmic_flops(alg, n) / total * 1e-12;
-        st->kappa_est = (double)used;  // precision that produced the result (PALIAL_PREC_*)
+        st->precision_used = used;
     }
     return rc;
 }
@@ -1127,7 +1130,7 @@ extern "C" int palial_gpu_row_groups(int n, int nb, int *gs, int *ge, int *due, 
 // covers the row the next step's first update needs.  0, or a positive code naming the
 // failed property.  Host only.
 extern "C" int palial_gpu_check_arrival_plan(int n, int nb, int mode) {
-    if (n <= 0 || nb <= 0 || n % nb || mode < 0 || mode > 2) return -1;
+    if (n <= 0 || nb <= 0 || n % nb || mode < 0 || mode > 3) return -1;
     const int mt = n / nb;
     if (mt <= 2) return 0;
     int ng = 0, gs[64], ge[64], due[64], kg[64];

@@ -14,8 +14,10 @@
 //                  accumulator of 256 FP32 columns; tcgen05.commit frees ring slots;
 //   all 4 warps    epilogue: tcgen05.ld 32 lanes x 16 columns at a time, C -= scale * D with
 //                  coalesced FP32 loads/stores in the reference's tile layout.
-// Modes: BF16 (one MMA per K slice), FP8 e4m3 (per-tile scales applied in the epilogue) and
-// BF16X3 (operands split x = hi + lo in bf16; hi*hi + hi*lo + lo*hi accumulated in TMEM).
+// Modes: BF16 (one MMA per K slice), FP8 e4m3 (per-tile scales applied in the epilogue),
+// BF16X3 (operands split x = hi + lo in bf16; hi*hi + hi*lo + lo*hi accumulated in TMEM) and
+// TF32X3 (the same three products with x = hi + lo in TF32, kind::tf32: about 21 bits per
+// product, the FP32-level rung of the precision ladder).
 // Every mbarrier wait is bounded; on expiry the CTA records an error, drains its own TMA
 // copies and frees its TMEM before returning.
 #include <cuda.h>
@@ -36,25 +38,27 @@ constexpr int NTHR = 128;
 constexpr uint32_t TMEM_COLS = 256;
 constexpr uint32_t WAIT_LIMIT = 1u << 24;  // bounded spin (about a second with back-off)
 
-enum Mode { MODE_BF16 = 0, MODE_FP8 = 1, MODE_BF16X3 = 2 };
+enum Mode { MODE_BF16 = 0, MODE_FP8 = 1, MODE_BF16X3 = 2, MODE_TF32X3 = 3 };
 
 template <int MODE>
 struct Cfg {
-    static constexpr int NOPS = (MODE == MODE_BF16X3) ? 2 : 1;   // hi (+ lo) operand copies
-    // K = NB = 512 is only 8 (bf16) or 4 (fp8) stages.  2 CTAs share an SM (2 x 256 TMEM
-    // columns, 2 x 128 threads x 256 registers), so one CTA's epilogue overlaps the other's
-    // loads and MMAs: bf16 and fp8 keep a 2-stage ring (96 KB); BF16x3's stage holds four
-    // operand boxes (96 KB), so it runs one stage per CTA to fit two CTAs in shared memory.
-    static constexpr int STAGES = (MODE == MODE_BF16X3) ? 1 : 2;
+    static constexpr bool SPLIT = (MODE == MODE_BF16X3 || MODE == MODE_TF32X3);
+    static constexpr int NOPS = SPLIT ? 2 : 1;   // hi (+ lo) operand copies
+    // K = NB = 512 is only 8 (bf16), 4 (fp8) or 16 (tf32) stages.  2 CTAs share an SM (2 x 256
+    // TMEM columns, 2 x 128 threads x 256 registers), so one CTA's epilogue overlaps the
+    // other's loads and MMAs: bf16 and fp8 keep a 2-stage ring (96 KB); a split mode's stage
+    // holds four operand boxes (96 KB), so it runs one stage per CTA to fit two CTAs.
+    static constexpr int STAGES = SPLIT ? 1 : 2;
     static constexpr int A_BYTES = BM * KBYTES;                  // 16 KB
     static constexpr int B_BYTES = BN * KBYTES;                  // 32 KB
     static constexpr int STAGE_BYTES = NOPS * (A_BYTES + B_BYTES);
     static constexpr int SMEM = STAGES * STAGE_BYTES + 1024 /*align*/ + 256 /*barriers*/;
-    static constexpr int ELEM = (MODE == MODE_FP8) ? 1 : 2;     // bytes per element
+    static constexpr int ELEM = (MODE == MODE_FP8) ? 1 : (MODE == MODE_TF32X3) ? 4 : 2;  // bytes per element
     static constexpr int KELEMS = KBYTES / ELEM;                 // elements of K per stage
+    // operand format field: e4m3 0 (kind::f8f6f4), bf16 1 (kind::f16), tf32 2 (kind::tf32)
+    static constexpr uint32_t FMT = (MODE == MODE_FP8) ? 0u : (MODE == MODE_TF32X3) ? 2u : 1u;
     // instruction descriptor: D=F32, A/B format, K-major A and B, N>>3, M>>4
-    static constexpr uint32_t IDESC = (1u << 4) | ((MODE == MODE_FP8 ? 0u : 1u) << 7) |
-                                      ((MODE == MODE_FP8 ? 0u : 1u) << 10) | ((uint32_t)(BN >> 3) << 17) |
+    static constexpr uint32_t IDESC = (1u << 4) | (FMT << 7) | (FMT << 10) | ((uint32_t)(BN >> 3) << 17) |
                                       ((uint32_t)(BM >> 4) << 24);
 };
 
@@ -126,6 +130,11 @@ __device__ __forceinline__ void mma(uint32_t tmem_d, uint64_t a, uint64_t b, uin
         asm volatile(
             "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
             " tcgen05.mma.cta_group::1.kind::f8f6f4 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem_d),
+            "l"(a), "l"(b), "r"(Cfg<MODE>::IDESC), "r"(accumulate));
+    } else if (MODE == MODE_TF32X3) {
+        asm volatile(
+            "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+            " tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem_d),
             "l"(a), "l"(b), "r"(Cfg<MODE>::IDESC), "r"(accumulate));
     } else {
         asm volatile(
@@ -277,7 +286,7 @@ __global__ void __launch_bounds__(NTHR, 1)
             uint8_t *st = base + s * C::STAGE_BYTES;
             const uint64_t da = smem_desc(st), db = smem_desc(st + C::A_BYTES);
 #pragma unroll
-            for (int kk = 0; kk < KBYTES / 32; kk++) {
+            for (int kk = 0; kk < KBYTES / 32; kk++) {  // K slice: 32 bytes (16 bf16, 32 e4m3, 8 tf32)
                 const uint32_t acc = (kb | kk) ? 1u : 0u;
                 mma<MODE>(tmem, da + 2 * kk, db + 2 * kk, acc);  // +32 B per K slice
                 if (C::NOPS == 2) {
@@ -338,11 +347,34 @@ __global__ void __launch_bounds__(NTHR, 1)
 // ---------------------------------------------------------------------------------------
 // Panel packing: K-major low-precision copies of the step's panel.
 // ---------------------------------------------------------------------------------------
+// TF32 rounding of an FP32 value: round half away from zero to 10 explicit mantissa bits (the
+// magnitude bits are rounded by adding half a TF32 unit in the last place and clearing the 13
+// low bits; a carry into the exponent is the correct result).  x - tf32_round(x) is exact in
+// FP32, so x = hi + lo with both parts TF32 up to the 2 lowest bits of x.
+__device__ __forceinline__ float tf32_round(float x) {
+    return __uint_as_float((__float_as_uint(x) + 0x1000u) & 0xFFFFE000u);
+}
+
+// One packed element in mode MODE (0 bf16, 2 bf16 hi + lo, 3 tf32 hi + lo; e4m3 is handled by
+// the callers with its scale).
+__device__ __forceinline__ void pack_one(int mode, float x, void *hi, void *lo, size_t o) {
+    if (mode == 3) {
+        const float h = tf32_round(x);
+        static_cast<float *>(hi)[o] = h;
+        static_cast<float *>(lo)[o] = tf32_round(x - h);
+        return;
+    }
+    const __nv_bfloat16 h = __float2bfloat16_rn(x);
+    static_cast<__nv_bfloat16 *>(hi)[o] = h;
+    if (mode == 2) static_cast<__nv_bfloat16 *>(lo)[o] = __float2bfloat16_rn(x - __bfloat162float(h));
+}
+
 // Row panel k (Cholesky U(k, m) / LU U(k, n), m > k): packed row (m-k-1)*nb + j, col p =
 // tile (k, m) element (p, j): the tile's columns are already contiguous in p.
-// MODE 0: bf16; 2: bf16 hi + lo; 1: e4m3 with per-tile scale (max|x| / 448).
-__global__ void pack_rows_kernel(const float *W, int n, int nb, int k, int mode, __nv_bfloat16 *hi,
-                                 __nv_bfloat16 *lo, __nv_fp8_e4m3 *f8, float *scales) {
+// MODE 0: bf16; 2: bf16 hi + lo; 3: tf32 hi + lo (FP32 containers); 1: e4m3 with per-tile
+// scale (max|x| / 448).
+__global__ void pack_rows_kernel(const float *W, int n, int nb, int k, int mode, void *hi, void *lo,
+                                 float *scales) {
     const int t = blockIdx.y;                   // trailing tile index
     const int mt = n / nb;
     const float *tile = W + (size_t)nb * nb * ((size_t)k + (size_t)mt * (k + 1 + t));
@@ -367,20 +399,17 @@ __global__ void pack_rows_kernel(const float *W, int n, int nb, int k, int mode,
     }
     for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < nb * nb; e += gridDim.x * blockDim.x) {
         const float x = tile[e];
-        if (mode == 1) {
-            f8[out0 + e] = __nv_fp8_e4m3(x * inv);
-        } else {
-            const __nv_bfloat16 h = __float2bfloat16_rn(x);
-            hi[out0 + e] = h;
-            if (mode == 2) lo[out0 + e] = __float2bfloat16_rn(x - __bfloat162float(h));
-        }
+        if (mode == 1)
+            static_cast<__nv_fp8_e4m3 *>(hi)[out0 + e] = __nv_fp8_e4m3(x * inv);
+        else
+            pack_one(mode, x, hi, lo, out0 + e);
     }
 }
 
 // Column panel k (LU L(m, k), m > k): packed row (m-k-1)*nb + i, col p = tile (m, k)
 // element (i, p): a transpose, through shared memory 32 x 32 at a time.
-__global__ void pack_cols_kernel(const float *W, int n, int nb, int k, int mode, __nv_bfloat16 *hi,
-                                 __nv_bfloat16 *lo, __nv_fp8_e4m3 *f8, const float *scales) {
+__global__ void pack_cols_kernel(const float *W, int n, int nb, int k, int mode, void *hi, void *lo,
+                                 const float *scales) {
     __shared__ float s[32][33];
     const int t = blockIdx.z;
     const int mt = n / nb;
@@ -392,13 +421,10 @@ __global__ void pack_cols_kernel(const float *W, int n, int nb, int k, int mode,
     for (int r = threadIdx.y; r < 32; r += blockDim.y) {
         const float x = s[threadIdx.x][r];  // element (i0 + r, p0 + tx)
         const size_t o = (size_t)t * nb * nb + (size_t)(i0 + r) * nb + p0 + threadIdx.x;
-        if (mode == 1) {
-            f8[o] = __nv_fp8_e4m3(x * inv);
-        } else {
-            const __nv_bfloat16 h = __float2bfloat16_rn(x);
-            hi[o] = h;
-            if (mode == 2) lo[o] = __float2bfloat16_rn(x - __bfloat162float(h));
-        }
+        if (mode == 1)
+            static_cast<__nv_fp8_e4m3 *>(hi)[o] = __nv_fp8_e4m3(x * inv);
+        else
+            pack_one(mode, x, hi, lo, o);
     }
 }
 
@@ -449,7 +475,10 @@ cudaError_t make_map(CUtensorMap *m, const void *base, long long rows, int nb, i
     const cuuint64_t strides[1] = {(cuuint64_t)nb * elem_bytes};
     const cuuint32_t box[2] = {(cuuint32_t)(128 / elem_bytes), (cuuint32_t)box_rows};
     const cuuint32_t estr[2] = {1, 1};
-    const CUresult r = g_encode(m, elem_bytes == 1 ? CU_TENSOR_MAP_DATA_TYPE_UINT8 : CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2,
+    const CUtensorMapDataType dt = elem_bytes == 1   ? CU_TENSOR_MAP_DATA_TYPE_UINT8
+                                   : elem_bytes == 4 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT32
+                                                     : CU_TENSOR_MAP_DATA_TYPE_BFLOAT16;
+    const CUresult r = g_encode(m, dt, 2,
                                 const_cast<void *>(base), dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
                                 CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
                                 CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
@@ -498,7 +527,7 @@ cudaError_t launch_mode(const void *a_hi, const void *a_lo, const void *b_hi, co
 }
 }  // namespace
 
-// mode: 0 bf16, 1 fp8, 2 bf16x3.  a_*/b_*: packed operands (ntr*nb rows x nb), scales: per
+// mode: 0 bf16, 1 fp8, 2 bf16x3, 3 tf32x3.  a_*/b_*: packed operands (ntr*nb rows x nb), scales: per
 // trailing tile (fp8).  C: FP32 tile-layout matrix.
 cudaError_t mp_update(int mode, int upper, float *C, int n, int nb, int k, const void *a_hi, const void *a_lo,
                       const void *b_hi, const void *b_lo, const float *scale_a, const float *scale_b, int *status,
@@ -520,6 +549,8 @@ cudaError_t mp_update(int mode, int upper, float *C, int n, int nb, int k, const
     if (p.ntr <= 0) return cudaSuccess;
     if (mode == mp::MODE_BF16) return launch_mode<mp::MODE_BF16>(a_hi, nullptr, b_hi, nullptr, p, s);
     if (mode == mp::MODE_FP8) return launch_mode<mp::MODE_FP8>(a_hi, nullptr, b_hi, nullptr, p, s);
+    if (mode == mp::MODE_TF32X3) return launch_mode<mp::MODE_TF32X3>(a_hi, a_lo, b_hi, b_lo, p, s);
+    if (mode != mp::MODE_BF16X3) return cudaErrorInvalidValue;
     return launch_mode<mp::MODE_BF16X3>(a_hi, a_lo, b_hi, b_lo, p, s);
 }
 
@@ -530,9 +561,7 @@ cudaError_t mp_pack_rows(int mode, const float *W, int n, int nb, int k, void *h
     if (ntr <= 0) return cudaSuccess;
     dim3 grid(mode == 1 ? 1 : 16, ntr);
     note_launch();
-    mp::pack_rows_kernel<<<grid, 1024, 0, s>>>(W, n, nb, k, mode, static_cast<__nv_bfloat16 *>(hi),
-                                                static_cast<__nv_bfloat16 *>(lo), static_cast<__nv_fp8_e4m3 *>(hi),
-                                                scales);
+    mp::pack_rows_kernel<<<grid, 1024, 0, s>>>(W, n, nb, k, mode, hi, lo, scales);
     return cudaGetLastError();
 }
 
@@ -547,9 +576,7 @@ cudaError_t mp_pack_cols(int mode, const float *W, int n, int nb, int k, void *h
     }
     dim3 grid(nb / 32, nb / 32, ntr), block(32, 8);
     note_launch();
-    mp::pack_cols_kernel<<<grid, block, 0, s>>>(W, n, nb, k, mode, static_cast<__nv_bfloat16 *>(hi),
-                                                 static_cast<__nv_bfloat16 *>(lo), static_cast<__nv_fp8_e4m3 *>(hi),
-                                                 scales);
+    mp::pack_cols_kernel<<<grid, block, 0, s>>>(W, n, nb, k, mode, hi, lo, scales);
     return cudaGetLastError();
 }
 

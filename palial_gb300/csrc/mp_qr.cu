@@ -226,7 +226,8 @@ extern "C" int palial_gpu_qr_solve_ir(int n, int nb, const double *dA, const dou
         st->tflops = algorithmic_flops(2, n) / std::max(1e-12, wall) * 1e-12;
         st->ir_iters = steps;
         st->backward_error = worst;
-        st->kappa_est = rung;  // the precision that produced the result
+        st->kappa_est = -1.0;
+        st->precision_used = rung;  // the precision that produced the result
     }
     if (!converged)
         return set_status(st, PALIAL_ERR_NOT_CONVERGED, "QR refinement stopped at %.3g (tolerance %.3g)", worst, tol);

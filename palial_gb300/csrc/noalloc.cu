@@ -13,6 +13,9 @@
 // library keeps these 512.25 KiB until the process exits.
 #include <cuda_runtime.h>
 
+#include <atomic>
+#include <mutex>
+
 #include "../../include/palial_gpu.h"
 #include "common.cuh"
 
@@ -20,6 +23,7 @@ namespace palial {
 cudaError_t sched_configure();
 cudaError_t tile_task_launch(int type, int nb, int ld, double *p0, double *p1, double *p2, double *p3, double *scratch,
                              int *status, cudaStream_t s);
+void noalloc_reset();
 }  // namespace palial
 
 namespace {
@@ -33,8 +37,18 @@ constexpr int kMaxDevices = 64;
 static __device__ __align__(256) double g_tsmqr_scratch[kStripDoubles + kStatusDoubles];
 
 // Device address of g_tsmqr_scratch per device ordinal (nullptr until that device's set-up).
-double *g_scratch_addr[kMaxDevices] = {};
+// The set-up runs under g_setup_mutex, so host threads making their first call on a device
+// together look the address up once; later calls read the slot without locking.
+std::atomic<double *> g_scratch_addr[kMaxDevices] = {};
+std::mutex g_setup_mutex;
 }  // namespace
+
+// Forgets every device's set-up (palial_gpu_finalize): the next call on a device looks the
+// address up again in whatever context is current then (after a cudaDeviceReset, say).
+void palial::noalloc_reset() {
+    std::lock_guard<std::mutex> lock(g_setup_mutex);
+    for (auto &slot : g_scratch_addr) slot.store(nullptr, std::memory_order_release);
+}
 
 extern "C" int palial_gpu_tile_dtsmqr_noalloc(int nb, double *dA1, double *dA2, const double *dV, const double *dT,
                                               int lda, void *stream) {
@@ -46,17 +60,22 @@ extern "C" int palial_gpu_tile_dtsmqr_noalloc(int nb, double *dA1, double *dA2, 
         return PALIAL_ERR_NO_DEVICE;
     }
     if (dev < 0 || dev >= kMaxDevices) return PALIAL_ERR_ARG;
-    if (!g_scratch_addr[dev]) {
+    double *scratch = g_scratch_addr[dev].load(std::memory_order_acquire);
+    if (!scratch) {
         // First call on this device (which is current): find the array's device address and
         // allow the tile kernel its dynamic shared memory.  Neither step allocates memory.
-        void *p = nullptr;
-        cudaError_t e = cudaGetSymbolAddress(&p, g_tsmqr_scratch);
-        if (e != cudaSuccess || !p) return PALIAL_ERR_CUDA;
-        e = palial::sched_configure();
-        if (e != cudaSuccess) return PALIAL_ERR_CUDA;
-        g_scratch_addr[dev] = static_cast<double *>(p);
+        std::lock_guard<std::mutex> lock(g_setup_mutex);
+        scratch = g_scratch_addr[dev].load(std::memory_order_acquire);
+        if (!scratch) {
+            void *p = nullptr;
+            cudaError_t e = cudaGetSymbolAddress(&p, g_tsmqr_scratch);
+            if (e != cudaSuccess || !p) return PALIAL_ERR_CUDA;
+            e = palial::sched_configure();
+            if (e != cudaSuccess) return PALIAL_ERR_CUDA;
+            scratch = static_cast<double *>(p);
+            g_scratch_addr[dev].store(scratch, std::memory_order_release);
+        }
     }
-    double *scratch = g_scratch_addr[dev];
     // Nothing in the scratch has to start at zero: the kernel writes both strips in full
     // before reading them, and TSMQR never writes the status block.
     int *status = reinterpret_cast<int *>(scratch + kStripDoubles);

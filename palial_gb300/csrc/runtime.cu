@@ -288,6 +288,7 @@ int batched_run(int count, const int *algs, const int *ns, const int *nbs, const
     if (hs[ST_ZEROPIV]) return set_status(st, PALIAL_WARN_ZERO_PIVOT, "exact zero pivot skipped");
     return set_status(st, PALIAL_OK);
 }
+void noalloc_reset();  // noalloc.cu: forget the fixed scratch's per-device address
 }  // namespace palial
 
 using namespace palial;
@@ -343,6 +344,7 @@ int palial_gpu_init(int device) {
 }
 
 int palial_gpu_finalize(void) {
+    noalloc_reset();
     if (!g.init) return PALIAL_OK;
     g.main.release();
     g.diag.release();

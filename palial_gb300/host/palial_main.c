@@ -24,7 +24,7 @@
  *   --quiet                 no JSON line
  * Solve mode (A X = B with K seeded uniform right-hand sides instead of the bare factorization):
  *   --rhs K                 K right-hand sides (Cholesky/LU: 1..16, QR: 1..NB)
- *   --precision P           fp64 | bf16 | fp8 | bf16x3 | auto: trailing-update precision of the
+ *   --precision P           fp64 | bf16 | fp8 | bf16x3 | tf32x3 | auto: trailing-update precision of the
  *                           Cholesky/LU factorization, refined to FP64 accuracy (QR: fp64 only);
  *                           any precision other than fp64 implies --rhs 1 when --rhs is absent
  *   --ir-tol T, --ir-max N  refinement target backward error and iteration cap
@@ -65,18 +65,19 @@ static int parse_gen(const char *s)
     return 2;
 }
 
+/* PALIAL_PREC_* codes by name (index = code; 5 is the batched solves' FP32) */
+static const char *const precision_names[] = {"fp64", "bf16", "fp8", "bf16x3", "auto", "fp32", "tf32x3"};
+
 static int parse_precision(const char *s)
 {
-    static const char *names[] = {"fp64", "bf16", "fp8", "bf16x3", "auto"};
-    for (int i = 0; i < 5; i++)
-        if (!strcmp(s, names[i])) return i;
+    for (int i = 0; i < 7; i++)
+        if (i != PALIAL_PREC_FP32 && !strcmp(s, precision_names[i])) return i;
     return -1;
 }
 
 static const char *precision_name(int p)
 {
-    static const char *names[] = {"fp64", "bf16", "fp8", "bf16x3", "auto"};
-    return p >= 0 && p < 5 ? names[p] : "?";
+    return p >= 0 && p < 7 ? precision_names[p] : "?";
 }
 
 /* uniform [-1, 1) right-hand sides from splitmix64 (seed, index) */

@@ -22,3 +22,7 @@ def test_reference_arm_json_line():
     assert d["e2e"]["h2d_bytes_per_step"] == 0 and d["e2e"]["d2h_bytes_per_step"] == 0
     assert d["e2e"]["value"] == d["value"]
     assert "workload" in d["config"] and d["metric"]
+    # the headline's own workload (a bounded sample of it is timed), and no GPU library loaded
+    assert d["config"]["n"] == 32768 and d["config"]["nb"] == 512 and d["config"]["nrhs"] == 16
+    assert not any("palial_gpu" in lib for lib in d["native_libraries"]), d["native_libraries"]
+    assert any(lib.startswith("oracle") for lib in d["native_libraries"]), d["native_libraries"]

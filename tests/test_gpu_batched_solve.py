@@ -110,7 +110,7 @@ def test_batched_solve_reaches_fp64_backward_error():
     d = Dev(mats, [nb for _, _, nb, _ in spec])
     st, iters, berr = B.solve([a for a, *_ in spec], d.ns, d.nbs, d.ptrs, d.bptrs, d.xptrs,
                               precs=[p for *_, p in spec])
-    assert st.code == 0 and st.ntasks == 0
+    assert st.code == 0 and st.fallbacks == 0
     assert (iters >= 1).all() and st.ir_iters == iters.max()
     for i, (alg, n, _, prec) in enumerate(spec):
         x = d.x(i)
@@ -134,7 +134,7 @@ def test_batched_solve_falls_back_to_fp64():
     st, iters, berr = B.solve(algs, d.ns, d.nbs, d.ptrs, d.bptrs, d.xptrs)
     assert st.code == 0
     assert iters[0] < 0 and iters[1] < 0 and iters[2] > 0
-    assert st.ntasks == 2
+    assert st.fallbacks == 2
     for i in range(3):
         tol = 1e-14 * d.ns[i]
         assert berr[i] <= tol, (i, berr[i])

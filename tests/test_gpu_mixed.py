@@ -10,7 +10,12 @@ from oracle import oracle as O
 pytestmark = pytest.mark.gpu
 torch = pytest.importorskip("torch")
 
-PREC = {1: "bf16", 2: "fp8", 3: "bf16x3"}
+PREC = {1: "bf16", 2: "fp8", 3: "bf16x3", 6: "tf32x3"}
+
+
+def tf32(x):
+    """The kernel's TF32 rounding: half away from zero to 10 explicit mantissa bits."""
+    return ((x.view(torch.int32) + 0x1000) & ~0x1FFF).view(torch.float32)
 
 
 def quant(x, prec, nb):
@@ -31,6 +36,10 @@ def quant(x, prec, nb):
 
 def prod(a, b, prec, nb):
     """a: (nb x r1) operand whose columns are output rows, b: (nb x r2): returns a^T b."""
+    if prec == 6:
+        ah, bh = tf32(a), tf32(b)
+        al, bl = tf32(a - ah), tf32(b - bh)
+        return ah.T @ bh + ah.T @ bl + al.T @ bh
     if prec == 3:
         ah, al = quant(a, 3, nb)
         bh, bl = quant(b, 3, nb)
@@ -38,9 +47,13 @@ def prod(a, b, prec, nb):
     return quant(a, prec, nb).T @ quant(b, prec, nb)
 
 
-@pytest.mark.parametrize("prec", [1, 2, 3])
+@pytest.mark.parametrize("prec", [1, 2, 3, 6])
 @pytest.mark.parametrize("alg", [0, 1])
 def test_tcgen05_trailing_update(alg, prec):
+    """BF16 / FP8 / BF16x3: against torch's FP32 products of the same quantized operands
+    (relative 1e-4).  TF32x3 (kind::tf32, hi + lo split): against the FP64 product of the FP32
+    operands themselves, relative 4e-6 (FP32-level), and the split is checked exact up to the
+    two lowest bits."""
     n, nb, k = 1536, 512, 0
     a = torch.from_numpy(O.gen_uniform(21 + alg, n).astype(np.float32)).cuda()
     w = torch.from_numpy(O.to_tiles(a.cpu().numpy().astype(np.float64), nb).astype(np.float32)).cuda()
@@ -62,8 +75,28 @@ def test_tcgen05_trailing_update(alg, prec):
         for ti in range(k + 1, mt):
             for tj in range(k + 1, ti):
                 ref[ti * nb:(ti + 1) * nb, tj * nb:(tj + 1) * nb] = a[ti * nb:(ti + 1) * nb, tj * nb:(tj + 1) * nb]
-    err = float(torch.linalg.norm(got - ref) / torch.linalg.norm(upd))
-    assert err <= 1e-4, err
+    if prec == 6:
+        ad = a.double()
+        if alg == 0:
+            upd64 = ad[kk, r0:].T @ ad[kk, r0:]
+        else:
+            upd64 = ad[r0:, kk] @ ad[kk, r0:]
+        ref64 = ad.clone()
+        ref64[r0:, r0:] -= upd64
+        if alg == 0:
+            for ti in range(k + 1, n // nb):
+                for tj in range(k + 1, ti):
+                    ref64[ti * nb:(ti + 1) * nb, tj * nb:(tj + 1) * nb] = ad[ti * nb:(ti + 1) * nb, tj * nb:(tj + 1) * nb]
+        err = float(torch.linalg.norm(got.double() - ref64) / torch.linalg.norm(upd64))
+        hi = tf32(a)
+        lo = tf32(a - hi)
+        split = float(((a.double() - hi.double() - lo.double()).abs() / a.double().abs().clamp_min(1e-30)).max())
+        print(f"tf32x3 update: relative error {err:.3e} against FP64, split error {split:.3e}")
+        assert split <= 2.0 ** -21
+        assert err <= 4e-6, err
+    else:
+        err = float(torch.linalg.norm(got - ref) / torch.linalg.norm(upd))
+        assert err <= 1e-4, err
     # the panel itself and the leading tiles are untouched
     assert torch.equal(got[kk, :], a[kk, :]) and torch.equal(got[:, kk], a[:, kk])
 
@@ -75,7 +108,7 @@ def dominant(seed, n):
     return a
 
 
-@pytest.mark.parametrize("prec", ["bf16", "bf16x3", "fp8", "fp64"])
+@pytest.mark.parametrize("prec", ["bf16", "bf16x3", "tf32x3", "fp8", "fp64"])
 @pytest.mark.parametrize("alg", ["cholesky", "lu"])
 def test_solve_ir_reaches_fp64_backward_error(alg, prec):
     n, nb, nrhs = 2048, 512, 16
@@ -121,10 +154,36 @@ def test_kappa_sweep_small(alg, kappa):
     x = dx.cpu().numpy().reshape(nrhs, n).T
     xref = np.linalg.solve(a, b)
     fwd = np.max(np.abs(x - xref).max(0) / np.abs(xref).max(0))
-    print(f"{alg} kappa={kappa:.0e} code={st.code} prec={P.PREC_NAME.get(int(st.kappa_est))} iters={st.ir_iters} "
+    print(f"{alg} kappa={kappa:.0e} code={st.code} prec={P.PREC_NAME.get(st.precision_used)} iters={st.ir_iters} "
           f"gmres={st.gmres_iters} eta={st.backward_error:.3e} fwd={fwd:.3e} shift={st.shift:.2e} t={st.seconds:.3f}s")
     assert st.code in (0, 1), st.message
     assert st.backward_error <= 1e-14 * n
+
+
+@pytest.mark.parametrize("alg", ["cholesky", "lu"])
+def test_tf32x3_rung_converges_where_bf16x3_does_not(alg):
+    """kappa = 1e6 (LU) and 1e10 (Cholesky) at N = 8192: the FP32-level TF32x3 factors reach the
+    FP64-level target with GMRES-IR; the forward error against numpy's FP64 solution stays
+    within the conditioning's reach (kappa * 1e-15)."""
+    n, nb, nrhs = 8192, 512, 16
+    kappa = 1e6 if alg == "lu" else 1e10
+    da = torch.empty(n * n, dtype=torch.float64, device="cuda")
+    P.gen_kappa(da.data_ptr(), n, nb, kappa, alg == "cholesky", seed=7)
+    torch.cuda.synchronize()
+    b = O.gen_uniform(5, n, nrhs, stream=O.STREAM_RHS)
+    db = torch.from_numpy(np.asfortranarray(b).ravel(order="F")).cuda()
+    dx = torch.zeros_like(db)
+    st = P.solve_ir(alg, da.data_ptr(), n, nb, db.data_ptr(), dx.data_ptr(), nrhs, precision="tf32x3",
+                    ir_max_iter=10, raise_on_error=False)
+    a = O.from_tiles(da.cpu().numpy(), n, nb)
+    x = dx.cpu().numpy().reshape(nrhs, n).T
+    xref = np.linalg.solve(a, b)
+    fwd = float(np.max(np.abs(x - xref).max(0) / np.abs(xref).max(0)))
+    print(f"{alg} kappa={kappa:.0e} tf32x3: code={st.code} iters={st.ir_iters} gmres={st.gmres_iters} "
+          f"eta={st.backward_error:.3e} fwd={fwd:.3e} shift={st.shift:.2e} t={st.seconds:.3f}s")
+    assert st.code in (0, 1), st.message
+    assert st.backward_error <= 1e-14 * n
+    assert fwd <= kappa * 1e-15
 
 
 def test_non_finite_factor_is_not_reported_as_converged():

@@ -31,7 +31,7 @@ def test_fp32_qr_refined_to_fp64_backward_error(n, nb, nrhs):
     a = rng.uniform(-1, 1, (n, n))
     b = rng.uniform(-1, 1, (n, nrhs))
     st, x = _solve(a, b, nb)
-    assert st.code == 0 and st.kappa_est == 5, st.message  # FP32 QR sufficed
+    assert st.code == 0 and st.precision_used == 5, st.message  # FP32 QR sufficed
     assert 1 <= st.ir_iters <= 30
     assert st.backward_error <= 1e-14 * n
     assert _berr(a, x, b) <= 1e-14 * n
@@ -47,7 +47,7 @@ def test_ill_conditioned_system_falls_back_to_fp64_qr():
     a = (q1 * 1e10 ** (-np.arange(n) / (n - 1))) @ q2.T
     b = rng.uniform(-1, 1, (n, 2))
     st, x = _solve(a, b, nb)
-    assert st.code == 0 and st.kappa_est == 0, st.message  # the FP64 QR solve produced X
+    assert st.code == 0 and st.precision_used == 0, st.message  # the FP64 QR solve produced X
     assert _berr(a, x, b) <= 1e-14 * n
 
 

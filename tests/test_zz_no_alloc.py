@@ -49,6 +49,23 @@ def test_noalloc_tsmqr_matches_allocating_entry_point():
         assert _rel(n1, r1) <= 1e-12 and _rel(n2, r2) <= 1e-12, nb
 
 
+def test_noalloc_call_allocates_no_device_memory():
+    """After a warm-up call, further calls leave the device's free memory unchanged."""
+    lib = P.lib()
+    nb = 512
+    v, t, a1, a2 = _inputs(nb, 300)
+    dv, dt, n1, n2 = _dev(v), _dev(t), _dev(a1), _dev(a2)
+    args = (nb, n1.data_ptr(), n2.data_ptr(), dv.data_ptr(), dt.data_ptr(), nb, None)
+    assert lib.palial_gpu_tile_dtsmqr_noalloc(*args) == 0
+    torch.cuda.synchronize()
+    free0, _ = torch.cuda.mem_get_info()
+    for _ in range(3):
+        assert lib.palial_gpu_tile_dtsmqr_noalloc(*args) == 0
+    torch.cuda.synchronize()
+    free1, _ = torch.cuda.mem_get_info()
+    assert free1 == free0, (free0, free1)
+
+
 def test_noalloc_rejects_tiles_beyond_its_scratch():
     d = torch.zeros(1024 * 1024, dtype=torch.float64, device="cuda")
     p = d.data_ptr()
