@@ -179,6 +179,12 @@ int palial_gpu_mp_factor(int alg, const double *dA, float *dW, int n, int nb,
  * it: pack the step's panel(s) from dW in the given precision (1 bf16, 2 fp8, 3 bf16x3) and
  * apply C -= A_op B_op^T with the tcgen05 kernel (Cholesky: upper tile pairs; LU: all). */
 int palial_gpu_mp_update_step(int alg, int precision, float *dW, int n, int nb, int k);
+/* Which tcgen05 update kernel the mixed path launches (no reference counterpart): 0 one
+ * 128 x 256 output block per CTA (two CTAs per SM); 2 runs of consecutive blocks per CTA with
+ * double-buffered TMEM accumulators and a 192 KB load ring (one CTA per SM); 1 (default) runs
+ * whenever a launch has enough blocks for at least two per CTA.  Both give the same bits.
+ * Returns the previous setting (PALIAL_ERR_ARG for an unknown kind). */
+int palial_gpu_set_update_kernel(int kind);
 
 /* ---- linear solve and least squares through the tile QR (no reference counterpart) -------
  * A: rows x cols FP64 tile matrix on the device (rows >= cols, both multiples of nb, nb a

@@ -73,6 +73,7 @@ cudaError_t mps_symmetrize(double *X, int n, int nb, cudaStream_t s);
 cudaError_t launch_gen_dense(double *X, long long rows, int cols, uint64_t seed, int stream, cudaStream_t s);
 cudaError_t launch_sumsq(const double *X, long long len, double *partial, int blocks, cudaStream_t s);
 void mp_release();
+int set_update_kernel(int kind);
 }  // namespace palial
 
 using namespace palial;
@@ -594,6 +595,11 @@ extern "C" int palial_gpu_gen_kappa(double *dA, int n, int nb, double kappa, int
     if (symmetric) PALIAL_CK(mps_symmetrize(dA, n, nb, s), "symmetrize");
     PALIAL_CK(cudaStreamSynchronize(s), "gen kappa");
     return PALIAL_OK;
+}
+
+extern "C" int palial_gpu_set_update_kernel(int kind) {
+    if (kind < 0 || kind > 2) return PALIAL_ERR_ARG;
+    return palial::set_update_kernel(kind);
 }
 
 extern "C" int palial_gpu_mp_update_step(int alg, int precision, float *dW, int n, int nb, int k) {

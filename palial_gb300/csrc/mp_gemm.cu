@@ -345,6 +345,221 @@ __global__ void __launch_bounds__(NTHR, 1)
 }
 
 // ---------------------------------------------------------------------------------------
+// Tile runs: one CTA per SM works through `run` consecutive 128 x 256 output blocks with
+// double-buffered TMEM accumulators (2 x 256 columns), so the epilogue of one block overlaps
+// the MMAs of the next, and a 192 KB shared-memory ring (2 stages for the split modes, 4 for
+// BF16 / FP8) keeps TMA loads ahead of the MMAs.  Roles:
+//   warp 0 lane 0   TMA producer over the run's blocks and K stages (ring slots freed by the
+//                   MMA warp's tcgen05.commit on empty[s]);
+//   warp 1 lane 0   MMA issuer: block j accumulates into columns (j % 2) * 256, waits until
+//                   the epilogue has drained that accumulator (tempty), commits tfull;
+//   warps 2..5      epilogue: warp w reads TMEM lanes 32 * (w % 4) .. + 31 (the quarter its
+//                   warp index may access), C -= scale * D as in mp_update_kernel.
+// The CTA retires after its run (a few tens of microseconds), so kernels of the
+// high-priority stream (the factorization's critical chain) get SMs between runs.  The MMA
+// sequence and epilogue arithmetic per block equal mp_update_kernel's: the same bits.
+// ---------------------------------------------------------------------------------------
+constexpr int RUN_THREADS = 192;
+constexpr uint32_t RUN_TMEM_COLS = 512;
+
+template <int MODE>
+struct RunCfg {
+    using C = Cfg<MODE>;
+    static constexpr int STAGES = C::SPLIT ? 2 : 4;
+    static constexpr int SMEM = STAGES * C::STAGE_BYTES + 1024 /*align*/ + 256 /*barriers*/;
+};
+
+struct RunParams {
+    UpdateParams u;
+    long long nblocks;        // output blocks of the launch (pairs x sub-blocks)
+    int run;                  // blocks per CTA
+};
+
+__device__ __forceinline__ void block_coords(const UpdateParams &p, long long g, int &ti, int &tj, int &mi,
+                                             int &nj) {
+    const int sub_m = p.nb / BM, sub_n = p.nb / BN;
+    const int q = (int)(g / (sub_m * sub_n)), sub = (int)(g % (sub_m * sub_n));
+    decode_part(q, p.ntr, p.upper, p.part, ti, tj, p.r0);
+    mi = sub % sub_m;
+    nj = sub / sub_m;
+}
+
+__device__ __forceinline__ void mbar_arrive(uint64_t *bar) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
+
+template <int MODE>
+__global__ void __launch_bounds__(RUN_THREADS, 1)
+    mp_update_run_kernel(const __grid_constant__ CUtensorMap ta, const __grid_constant__ CUtensorMap tb,
+                         const __grid_constant__ CUtensorMap ta_lo, const __grid_constant__ CUtensorMap tb_lo,
+                         RunParams rp) {
+    using C = Cfg<MODE>;
+    constexpr int S = RunCfg<MODE>::STAGES;
+    const UpdateParams &p = rp.u;
+    extern __shared__ __align__(1024) uint8_t smem_raw[];
+    uint8_t *base = reinterpret_cast<uint8_t *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+    uint64_t *full = reinterpret_cast<uint64_t *>(base + S * C::STAGE_BYTES);
+    uint64_t *empty = full + S;
+    uint64_t *tfull = empty + S;   // [2] accumulator ready for the epilogue
+    uint64_t *tempty = tfull + 2;  // [2] accumulator drained by the epilogue (4 warp arrivals)
+    uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(tempty + 2);
+    __shared__ int s_abort;
+
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const long long g0 = (long long)blockIdx.x * rp.run;
+    const int nblk = (int)min((long long)rp.run, rp.nblocks - g0);
+    const int kstages = p.nb * C::ELEM / KBYTES;
+
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < S; s++) {
+            mbar_init(&full[s], 1);
+            mbar_init(&empty[s], 1);
+        }
+        for (int a = 0; a < 2; a++) {
+            mbar_init(&tfull[a], 1);
+            mbar_init(&tempty[a], 4);
+        }
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        s_abort = 0;
+    }
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
+                     "r"(RUN_TMEM_COLS));
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    const uint32_t tmem = *tmem_slot;
+
+    if (warp == 0) {
+        if (lane == 0) {
+            // ---- TMA producer ----
+            int it = 0;  // K stages issued over the whole run
+            for (int j = 0; j < nblk && !ld_volatile(&s_abort); j++) {
+                int ti, tj, mi, nj;
+                block_coords(p, g0 + j, ti, tj, mi, nj);
+                const int arow = ti * p.nb + mi * BM, brow = tj * p.nb + nj * BN;
+                for (int kb = 0; kb < kstages; kb++, it++) {
+                    const int s = it % S;
+                    if (it >= S && !mbar_wait(&empty[s], ((it / S) - 1) & 1)) {
+                        s_abort = 1;
+                        break;
+                    }
+                    uint8_t *st = base + s * C::STAGE_BYTES;
+                    mbar_expect_tx(&full[s], C::STAGE_BYTES);
+                    const int kx = kb * C::KELEMS;
+                    tma_load_2d(st, &ta, kx, arow, &full[s]);
+                    tma_load_2d(st + C::A_BYTES, &tb, kx, brow, &full[s]);
+                    if (C::NOPS == 2) {
+                        tma_load_2d(st + C::A_BYTES + C::B_BYTES, &ta_lo, kx, arow, &full[s]);
+                        tma_load_2d(st + 2 * C::A_BYTES + C::B_BYTES, &tb_lo, kx, brow, &full[s]);
+                    }
+                }
+            }
+            if (ld_volatile(&s_abort)) {
+                // drain: wait (bounded) for this CTA's own copies that may still be landing
+                for (int u = it - S < 0 ? 0 : it - S; u < it; u++) mbar_wait(&full[u % S], (u / S) & 1);
+            }
+        }
+    } else if (warp == 1) {
+        if (lane == 0) {
+            // ---- MMA issuer ----
+            int it = 0;
+            for (int j = 0; j < nblk; j++) {
+                const int acc = j & 1;
+                if (j >= 2 && !mbar_wait(&tempty[acc], ((j >> 1) - 1) & 1)) {
+                    s_abort = 1;
+                    break;
+                }
+                asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+                const uint32_t td = tmem + (uint32_t)(acc * 256);
+                bool ok = true;
+                for (int kb = 0; kb < kstages; kb++, it++) {
+                    const int s = it % S;
+                    if (ld_volatile(&s_abort) || !mbar_wait(&full[s], (it / S) & 1)) {
+                        ok = false;
+                        break;
+                    }
+                    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+                    uint8_t *st = base + s * C::STAGE_BYTES;
+                    const uint64_t da = smem_desc(st), db = smem_desc(st + C::A_BYTES);
+#pragma unroll
+                    for (int kk = 0; kk < KBYTES / 32; kk++) {
+                        const uint32_t accf = (kb | kk) ? 1u : 0u;
+                        mma<MODE>(td, da + 2 * kk, db + 2 * kk, accf);
+                        if (C::NOPS == 2) {
+                            const uint64_t dal = smem_desc(st + C::A_BYTES + C::B_BYTES);
+                            const uint64_t dbl = smem_desc(st + 2 * C::A_BYTES + C::B_BYTES);
+                            mma<MODE>(td, da + 2 * kk, dbl + 2 * kk, 1u);   // hi * lo
+                            mma<MODE>(td, dal + 2 * kk, db + 2 * kk, 1u);   // lo * hi
+                        }
+                    }
+                    mma_commit(&empty[s]);
+                }
+                if (!ok) {
+                    s_abort = 1;
+                    break;
+                }
+                mma_commit(&tfull[acc]);
+            }
+        }
+    } else {
+        // ---- epilogue: warps 2..5, thread = accumulator row of its TMEM lane quarter ----
+        const int lq = warp & 3;
+        const int mt = p.n / p.nb;
+        for (int j = 0; j < nblk; j++) {
+            const int acc = j & 1;
+            int ti, tj, mi, nj;
+            block_coords(p, g0 + j, ti, tj, mi, nj);
+            const int tr = p.k + 1 + ti, tc = p.k + 1 + tj;
+            float *ct = p.C + (size_t)p.nb * p.nb * ((size_t)tr + (size_t)mt * tc) +
+                        (size_t)(mi * BM + lq * 32 + lane) + (size_t)(nj * BN) * p.nb;
+            float cold[64];
+#pragma unroll
+            for (int c = 0; c < 64; c++) cold[c] = __ldcs(ct + (size_t)c * p.nb);
+            bool have = !ld_volatile(&s_abort) && mbar_wait(&tfull[acc], (j >> 1) & 1);
+            if (!have) {
+                if (lane == 0) atomicCAS(p.status + ST_CODE, 0, -4);
+                s_abort = 1;
+                break;
+            }
+            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+            float sc = 1.0f;
+            if (MODE == MODE_FP8 && p.scale_a) sc = p.scale_a[ti] * p.scale_b[tj];
+            const uint32_t trow = tmem + ((uint32_t)(lq * 32) << 16) + (uint32_t)(acc * 256);
+            for (int c0 = 0; c0 < BN; c0 += 64) {
+                float d[64];
+                tmem_ld16(trow + (uint32_t)c0, d);
+                tmem_ld16(trow + (uint32_t)(c0 + 16), d + 16);
+                tmem_ld16(trow + (uint32_t)(c0 + 32), d + 32);
+                tmem_ld16(trow + (uint32_t)(c0 + 48), d + 48);
+                if (c0 + 64 >= BN) {
+                    // the accumulator is fully read: hand it back to the MMA warp
+                    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+                    __syncwarp();
+                    if (lane == 0) mbar_arrive(&tempty[acc]);
+                }
+                float nxt[64];
+                if (c0 + 64 < BN) {
+#pragma unroll
+                    for (int c = 0; c < 64; c++) nxt[c] = __ldcs(ct + (size_t)(c0 + 64 + c) * p.nb);
+                }
+#pragma unroll
+                for (int c = 0; c < 64; c++) __stcs(ct + (size_t)(c0 + c) * p.nb, fmaf(-sc, d[c], cold[c]));
+                if (c0 + 64 < BN) {
+#pragma unroll
+                    for (int c = 0; c < 64; c++) cold[c] = nxt[c];
+                }
+            }
+        }
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(RUN_TMEM_COLS));
+}
+
+// ---------------------------------------------------------------------------------------
 // Panel packing: K-major low-precision copies of the step's panel.
 // ---------------------------------------------------------------------------------------
 // TF32 rounding of an FP32 value: round half away from zero to 10 explicit mantissa bits (the
@@ -485,6 +700,21 @@ cudaError_t make_map(CUtensorMap *m, const void *base, long long rows, int nb, i
     return r == CUDA_SUCCESS ? cudaSuccess : cudaErrorInvalidValue;
 }
 
+// Which update kernel runs: 0 one output block per CTA (mp_update_kernel), 2 tile runs
+// (mp_update_run_kernel) for every launch, 1 (default) tile runs when a launch has enough
+// blocks for runs of at least two per CTA.
+int g_update_kernel = 1;
+
+int sm_count() {
+    static int sms = 0;
+    if (!sms) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || sms <= 0) sms = 148;
+    }
+    return sms;
+}
+
 template <int MODE>
 cudaError_t launch_mode(const void *a_hi, const void *a_lo, const void *b_hi, const void *b_lo,
                         const mp::UpdateParams &p, cudaStream_t s) {
@@ -493,6 +723,9 @@ cudaError_t launch_mode(const void *a_hi, const void *a_lo, const void *b_hi, co
     if (!configured) {
         cudaError_t e = cudaFuncSetAttribute(mp::mp_update_kernel<MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                              C::SMEM);
+        if (e != cudaSuccess) return e;
+        e = cudaFuncSetAttribute(mp::mp_update_run_kernel<MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 mp::RunCfg<MODE>::SMEM);
         if (e != cudaSuccess) return e;
         configured = true;
     }
@@ -521,8 +754,21 @@ cudaError_t launch_mode(const void *a_hi, const void *a_lo, const void *b_hi, co
     const long long blocks = pairs * (p.nb / mp::BM) * (p.nb / mp::BN);
     if (blocks <= 0) return cudaSuccess;
     if (blocks > 0x7fffffffLL) return cudaErrorInvalidValue;
+    // blocks per CTA of the tile-run kernel: 8 (one 512 tile pair) down to 2, keeping at least
+    // two waves of CTAs over the SMs
+    const long long sms = sm_count();
+    int run = 8;
+    while (run > 1 && blocks < sms * run * 2) run /= 2;
+    if (g_update_kernel == 2 && run < 2) run = 2;
+    if (g_update_kernel == 0 || run < 2) {
+        note_launch();
+        mp::mp_update_kernel<MODE><<<(unsigned)blocks, mp::NTHR, C::SMEM, s>>>(ta, tb, tal, tbl, p);
+        return cudaGetLastError();
+    }
+    mp::RunParams rp{p, blocks, run};
     note_launch();
-    mp::mp_update_kernel<MODE><<<(unsigned)blocks, mp::NTHR, C::SMEM, s>>>(ta, tb, tal, tbl, p);
+    mp::mp_update_run_kernel<MODE><<<(unsigned)((blocks + run - 1) / run), mp::RUN_THREADS, mp::RunCfg<MODE>::SMEM, s>>>(
+        ta, tb, tal, tbl, rp);
     return cudaGetLastError();
 }
 }  // namespace
@@ -552,6 +798,13 @@ cudaError_t mp_update(int mode, int upper, float *C, int n, int nb, int k, const
     if (mode == mp::MODE_TF32X3) return launch_mode<mp::MODE_TF32X3>(a_hi, a_lo, b_hi, b_lo, p, s);
     if (mode != mp::MODE_BF16X3) return cudaErrorInvalidValue;
     return launch_mode<mp::MODE_BF16X3>(a_hi, a_lo, b_hi, b_lo, p, s);
+}
+
+// Update-kernel choice (palial_gpu_set_update_kernel): returns the previous setting.
+int set_update_kernel(int kind) {
+    const int old = g_update_kernel;
+    if (kind >= 0 && kind <= 2) g_update_kernel = kind;
+    return old;
 }
 
 // Pack the row panel k (tiles (k, m), m > k) of the FP32 tile matrix W.
