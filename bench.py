@@ -19,9 +19,10 @@ The JSON line also carries:
   e2e           the same solve through the host-buffer C ABI (palial_gpu_solve_ir_host on
                 pinned host memory: A and B copied in, X copied out, every step);
   e2e_pageable  the same from a pageable (malloc'd) host buffer, as the reference's caller has;
-  kappa         config 3 at N = 32768, kappa = 1e6, Cholesky and LU: the precision ladder's
-                solve (rung used, refinement and GMRES steps, FP64-checked backward error,
-                forward error against the FP64 solve) beside the FP64 factorization's solve;
+  kappa         config 3 at N = 32768: Cholesky at kappa = 1e6 and 1e10, LU at 1e6: the
+                precision ladder's solve (rung used, refinement and GMRES steps, FP64-checked
+                backward error, forward error against the FP64 solve) beside the FP64
+                factorization's solve;
   lu, qr        no-pivot LU (kappa = 1e2 matrix) and QR (uniform [-1, 1), seed 1) at N = 32768:
                 mixed-precision solve time beside the FP64 solve (--no-extra skips these three);
   roofline      the tcgen05 trailing-update kernel (the mixed path's tensor-core kernel),
@@ -333,9 +334,11 @@ def config_keys(P, torch, n: int, b, nrhs: int, stream: int) -> dict:
         del x, x64
         return rec
 
-    out["kappa"] = {"n": n, "nb": NB, "nrhs": nrhs, "cholesky": ladder_vs_fp64("cholesky", 1e6),
-                    "lu": ladder_vs_fp64("lu", 1e6),
-                    "note": "forward error floor of any backward-stable solve is about kappa * 1e-16"}
+    out["kappa"] = {"n": n, "nb": NB, "nrhs": nrhs,
+                    "cholesky": {"1e6": ladder_vs_fp64("cholesky", 1e6), "1e10": ladder_vs_fp64("cholesky", 1e10)},
+                    "lu": {"1e6": ladder_vs_fp64("lu", 1e6)},
+                    "note": "AUTO ladder BF16x3 -> TF32x3 -> FP64; the forward error a backward error eta "
+                            "allows is about kappa * eta (target eta <= 1e-14 * N)"}
     out["lu"] = dict(ladder_vs_fp64("lu", 1e2), n=n, nb=NB, nrhs=nrhs, matrix="U diag(s) V^T, kappa 1e2")
     P.gen_uniform(da.data_ptr(), n, NB, 1)
     x = torch.zeros_like(b)
@@ -760,6 +763,14 @@ def main() -> None:
             e2e_times.append(time.perf_counter() - t0)
     e2e_sec = sum(e2e_times) / len(e2e_times) if e2e_times else float("nan")
     e2e_value = world * flops(n) / e2e_sec * 1e-12
+    # the host link itself: a plain copy of A from the same pinned buffer, a few times
+    link = []
+    for _ in range(4):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        a0.copy_(host, non_blocking=True)
+        torch.cuda.synchronize()
+        link.append(round(8.0 * n * n / (time.perf_counter() - t0) * 1e-9, 1))
     # the same from pageable host memory, as the reference's own caller allocates it
     # (posix_memalign, palial_src/main.c:110): numpy's buffer is ordinary malloc'd memory
     page = np.empty(n * n)
@@ -795,7 +806,8 @@ def main() -> None:
             "fp64_tiled": fp64,
             "e2e": {"value": e2e_value, "unit": "TFLOP/s", "h2d_bytes_per_step": 8 * n * n + 8 * n * nrhs,
                     "d2h_bytes_per_step": 8 * n * nrhs, "step_seconds": [round(t, 5) for t in e2e_times],
-                    "host_buffer": "pinned (page-locked) A"},
+                    "host_buffer": "pinned (page-locked) A",
+                    "host_link_gbs_samples": link},
             "e2e_pageable": {"value": world * flops(n) / page_sec * 1e-12, "unit": "TFLOP/s",
                              "h2d_bytes_per_step": 8 * n * n + 8 * n * nrhs, "d2h_bytes_per_step": 8 * n * nrhs,
                              "step_seconds": [round(t, 5) for t in page_times],

@@ -155,8 +155,9 @@ int palial_gpu_factor_dev(int alg, double *dA, double *dS, int n, int nb, const 
  * Opt-in stabilised LU (alg = PALIAL_ALG_LU, mixed precisions): opts->reserved[6] = 1 factors
  * the random-butterfly transform U^T A V (depth-2 recursive butterflies, Parker 1995) without
  * pivoting instead of A, refines against A (seed: opts->reserved[7], 0 = 1).  PALIAL_PREC_AUTO
- * runs a precision ladder: BF16x3 (at most 10 refinement steps and 30 GMRES iterations), then
- * TF32x3 (FP32-level factors; 10 steps, 400 GMRES iterations), then the FP64 factorization;
+ * runs a precision ladder: BF16x3 (at most 10 refinement steps and 60 GMRES iterations; a
+ * Cholesky breakdown moves up at once), then TF32x3 (FP32-level factors; 20 steps, GMRES
+ * restarts of 200 and 600 iterations in all), then the FP64 factorization;
  * status.precision_used reports the rung that produced the result (PALIAL_PREC_*, + 100 for the
  * butterfly transform). */
 int palial_gpu_solve_ir(int alg, const double *dA, int n, int nb, const double *dB, double *dX,
@@ -182,7 +183,8 @@ int palial_gpu_mp_update_step(int alg, int precision, float *dW, int n, int nb, 
 /* Which tcgen05 update kernel the mixed path launches (no reference counterpart): 0 one
  * 128 x 256 output block per CTA (two CTAs per SM); 2 runs of consecutive blocks per CTA with
  * double-buffered TMEM accumulators and a 192 KB load ring (one CTA per SM); 1 (default) runs
- * whenever a launch has enough blocks for at least two per CTA.  Both give the same bits.
+ * for BF16x3 / TF32x3 (tensor-bound) and one block per CTA for BF16 / FP8 (bound by the FP32
+ * C traffic).  Both give the same bits.
  * Returns the previous setting (PALIAL_ERR_ARG for an unknown kind). */
 int palial_gpu_set_update_kernel(int kind);
 

@@ -718,7 +718,8 @@ static int solve_one(int alg, const double *dA, int n, int nb, const double *dB,
                 PALIAL_CK(mps_f64_to_f32(dA, W, n, nb, shift, s, attempt == 0 ? nrm + 120 : nullptr, alg == 0),
                           "convert");
             rc = mp_factor(alg, prec, W, n, nb, s, st, &zp);
-            if (rc != PALIAL_ERR_NOT_SPD || alg != 0) break;
+            // opts.reserved[5] bit 1: no shifted retry (a ladder rung hands a breakdown up)
+            if (rc != PALIAL_ERR_NOT_SPD || alg != 0 || (o.reserved[5] & 2)) break;
             if (anorm < 0) {
                 PALIAL_CK(wait_full_matrix(s), "matrix copy");
                 PALIAL_CK(cudaMemsetAsync(nrm, 0, sizeof(double), s), "norm A");
@@ -768,7 +769,7 @@ static int solve_one(int alg, const double *dA, int n, int nb, const double *dB,
     PALIAL_CK(cudaMemcpyAsync(mb.r.ptr, dB, sizeof(double) * (size_t)n * nrhs, cudaMemcpyDeviceToDevice, s), "r0");
     PALIAL_CK(cudaStreamSynchronize(s), "init");
     double eta = 1.0, eta_prev = 1e300;
-    int it = 0, gmres_total = 0;
+    int it = 0, gmres_total = 0, gmres_stalls = 0;
     bool converged = false;
     bool use_gmres = (o.gmres == 1);
     PALIAL_CK(mb.x32.ensure(sizeof(double) * (size_t)n * nrhs), "alloc d");
@@ -897,13 +898,18 @@ static int solve_one(int alg, const double *dA, int n, int nb, const double *dB,
             converged = true;
             break;
         }
-        if (o.reserved[5] == 1 && it >= 2 && eta > 0.1 * eta_prev) {
+        if ((o.reserved[5] & 1) && it >= 2 && eta > 0.1 * eta_prev) {
             break;  // a lower rung of the precision ladder that contracts slowly: move up
         }
         if (!use_gmres && it >= 2 && eta > 0.5 * eta_prev && o.gmres >= 0) {
             use_gmres = true;  // plain refinement contracts too slowly: switch to GMRES-IR
-        } else if (use_gmres && it >= 3 && eta > 0.9 * eta_prev) {
-            break;  // GMRES-IR stagnates as well
+            gmres_stalls = 0;
+        } else if (use_gmres && it >= 2) {
+            // GMRES-IR gets two outer steps that gain less than 10 % before it is given up:
+            // a GMRES cycle that met its inner tolerance may still leave the true residual
+            // above it when the preconditioner is poor, and the next cycle starts from there
+            gmres_stalls = eta > 0.9 * eta_prev ? gmres_stalls + 1 : 0;
+            if (gmres_stalls >= 2) break;
         } else if (!use_gmres && o.gmres < 0 && it >= 3 && eta > 0.9 * eta_prev) {
             break;
         }
@@ -957,12 +963,19 @@ extern "C" int palial_gpu_solve_ir(int alg, const double *dA, int n, int nb, con
         const int prec = ladder[li];
         palial_opts oo = o;
         oo.precision = prec;
-        // lower rungs get a bounded effort: at most 10 refinement steps, GMRES restarts of
-        // (BF16x3) 30 or (TF32x3) 100 iterations and a total of 30 or 400
-        if (prec != PALIAL_PREC_FP64) {
+        // lower rungs get a bounded effort.  BF16x3: at most 10 refinement steps, GMRES
+        // restarts of 50 and 60 iterations in all, and a Cholesky breakdown (a matrix beyond
+        // BF16x3's reach) goes up at once instead of being retried with a shift.  TF32x3: 20
+        // steps, restarts of 200, 600 iterations in all.
+        if (prec == PALIAL_PREC_BF16X3) {
             if (oo.ir_max_iter <= 0 || oo.ir_max_iter > 10) oo.ir_max_iter = 10;
-            oo.reserved[1] = prec == PALIAL_PREC_BF16X3 ? 30 : 100;
-            oo.reserved[3] = prec == PALIAL_PREC_BF16X3 ? 30 : 400;
+            oo.reserved[1] = 50;
+            oo.reserved[3] = 60;
+            oo.reserved[5] |= 2;
+        } else if (prec == PALIAL_PREC_TF32X3) {
+            if (oo.ir_max_iter <= 0 || oo.ir_max_iter > 20) oo.ir_max_iter = 20;
+            oo.reserved[1] = 200;
+            oo.reserved[3] = 600;
         }
         rc = solve_one(alg, dA, n, nb, dB, dX, nrhs, &oo, st, stream);
         used = prec + (alg == 1 && oo.reserved[6] == 1 && prec != PALIAL_PREC_FP64 ? 100 : 0);

@@ -701,8 +701,10 @@ cudaError_t make_map(CUtensorMap *m, const void *base, long long rows, int nb, i
 }
 
 // Which update kernel runs: 0 one output block per CTA (mp_update_kernel), 2 tile runs
-// (mp_update_run_kernel) for every launch, 1 (default) tile runs when a launch has enough
-// blocks for runs of at least two per CTA.
+// (mp_update_run_kernel) for every launch, 1 (default) tile runs for the split modes (three
+// products per K slice: tensor-bound, where overlapping the epilogue with the next block's
+// MMAs pays) and one block per CTA for BF16 / FP8 (HBM-bound on the C traffic, where two
+// CTAs' epilogues per SM keep more loads in flight).
 int g_update_kernel = 1;
 
 int sm_count() {
@@ -759,12 +761,12 @@ cudaError_t launch_mode(const void *a_hi, const void *a_lo, const void *b_hi, co
     const long long sms = sm_count();
     int run = 8;
     while (run > 1 && blocks < sms * run * 2) run /= 2;
-    if (g_update_kernel == 2 && run < 2) run = 2;
-    if (g_update_kernel == 0 || run < 2) {
+    if (g_update_kernel == 0 || (g_update_kernel == 1 && !C::SPLIT)) {
         note_launch();
         mp::mp_update_kernel<MODE><<<(unsigned)blocks, mp::NTHR, C::SMEM, s>>>(ta, tb, tal, tbl, p);
         return cudaGetLastError();
     }
+    if (run < 2) run = 2;  // small launches too: two blocks per CTA beat one block per CTA (measured)
     mp::RunParams rp{p, blocks, run};
     note_launch();
     mp::mp_update_run_kernel<MODE><<<(unsigned)((blocks + run - 1) / run), mp::RUN_THREADS, mp::RunCfg<MODE>::SMEM, s>>>(

@@ -3,14 +3,14 @@
 //
 // Solve T Y = R (16 right-hand sides, R and Y n x 16 FP32, ld n) by tile rows of the factor:
 //   APPLY(k, b):     Y_k[b] = op(D_k^-1)[b rows] R_k      (D_k^-1 the stored inverse of the
-//                                                           diagonal factor tile, 64-row block b)
+//                                                           diagonal factor tile, 32-row block b)
 //   UPDATE(k, t, b): R_t[b] -= op(W_kt)[b rows] Y_k       (t after k in the solve order)
 // with, per kind: 0 = Cholesky forward U^T y = r (op = transpose, W_kt = U(k,t), t > k);
 // 1 = backward U x = y (op = none, W_kt = U(t,k), t < k, k descending); 2 = LU forward
 // L y = r (unit L, op = none, W_kt = L(t,k), t > k).
 // Tasks run in one launch of persistent CTAs that take records in a fixed order (right-looking:
 // step k's applies, then its updates) with an atomic ticket and wait on completion
-// counters: per tile t the updates applied to it (APPLY waits for all of them), per 64-row
+// counters: per tile t the updates applied to it (APPLY waits for all of them), per 32-row
 // block the updates applied to it (updates into one block run in k order: deterministic
 // results), per tile k its applies (UPDATE(k, ..) waits for all of Y_k).  Every wait refers to
 // earlier records, so the dispatch cannot deadlock; every wait has a deadline and reports
@@ -47,14 +47,106 @@ struct RhsParams {
     unsigned long long timeout_ns;
 };
 
-constexpr int SMEM_BYTES = RW2_SMEM_FLOATS * 4;
+// Task body: a 32-row block of output rows against all K = NB of one factor tile.  The factor
+// slice (32 x NB FP32, read-only) is requested with cp.async BEFORE the task's dependency wait,
+// so its latency hides behind the wait; the right-hand-side block (NB x 16) follows once the
+// wait is met.  Both land in shared memory in one round trip each.  Thread (r = lane, g = warp)
+// accumulates row r over the K range g * NB/8 .. + NB/8 for all 16 columns (float4 reads of the
+// factor row and of each column, the columns broadcast across the warp); the 8 partial sums of
+// each output are then added in fixed order (deterministic).
+constexpr int RB = 32;                 // rows per task
+constexpr int KMAX = 512;              // largest NB
+constexpr int AP = KMAX + 4;           // pitch of a factor row [r][p] (float4-aligned, conflict-free)
+constexpr int BP = KMAX + 4;           // pitch of a right-hand-side column [j][p]
+constexpr int RED_P = RW + 1;          // pitch of the partial sums [g][r][j]
+constexpr int SMEM_FLOATS = RB * AP + RW * BP + (NT / 32) * RB * RED_P;
+constexpr int SMEM_BYTES = SMEM_FLOATS * 4;
+static_assert(RB * AP >= KMAX * RB, "factor slice fits either layout");
 
 __device__ __forceinline__ size_t tile_off(int n, int nb, int tm, int tn) {
     return (size_t)nb * nb * ((size_t)tm + (size_t)(n / nb) * tn);
 }
 
+__device__ __forceinline__ void cp_async16(void *dst, const void *src) {
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"((unsigned)__cvta_generic_to_shared(dst)),
+                 "l"(src)
+                 : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;" ::: "memory"); }
+
+// op(A)(i, p), i < 32, p < nb: TA: A[p + i * lda] (rows contiguous in p) -> As[i][p];
+// else A[i + p * lda] (32 contiguous rows per p) -> As[p][i] (pitch RB).
+template <bool TA>
+__device__ __forceinline__ void load_factor(float *As, const float *A, int lda, int nb) {
+    if (TA) {
+        const int per_row = nb / 4;  // 16-byte chunks per row
+        for (int c = threadIdx.x; c < RB * per_row; c += NT) {
+            const int i = c / per_row, q = c % per_row;
+            cp_async16(As + i * AP + q * 4, A + (size_t)q * 4 + (size_t)i * lda);
+        }
+    } else {
+        for (int c = threadIdx.x; c < nb * (RB / 4); c += NT) {
+            const int p = c / (RB / 4), q = c % (RB / 4);
+            cp_async16(As + p * RB + q * 4, A + (size_t)q * 4 + (size_t)p * lda);
+        }
+    }
+}
+
+// Bs[j][p] = B[p + j * ldb], j < 16, p < nb.
+__device__ __forceinline__ void load_rhs(float *Bs, const float *B, int ldb, int nb) {
+    const int per_col = nb / 4;
+    for (int c = threadIdx.x; c < RW * per_col; c += NT) {
+        const int j = c / per_col, q = c % per_col;
+        cp_async16(Bs + j * BP + q * 4, B + (size_t)q * 4 + (size_t)j * ldb);
+    }
+}
+
+// res[r][j] = sum_p op(A)(r, p) Bs[j][p] for the task's 32 rows: partial sums per warp, then
+// thread t adds the 8 partials of outputs (r, j) = (t % 32, t / 32) and (t % 32, t / 32 + 8).
+template <bool TA>
+__device__ __forceinline__ void block_product(const float *As, const float *Bs, float *red, int nb, float out[2]) {
+    const int r = threadIdx.x & 31, g = threadIdx.x >> 5;
+    const int kq = nb / (NT / 32);  // K per warp
+    float acc[RW];
+#pragma unroll
+    for (int j = 0; j < RW; j++) acc[j] = 0.f;
+    for (int p = g * kq; p < (g + 1) * kq; p += 4) {
+        float4 a;
+        if (TA) {
+            a = *reinterpret_cast<const float4 *>(As + r * AP + p);
+        } else {
+            a.x = As[(p + 0) * RB + r];
+            a.y = As[(p + 1) * RB + r];
+            a.z = As[(p + 2) * RB + r];
+            a.w = As[(p + 3) * RB + r];
+        }
+#pragma unroll
+        for (int j = 0; j < RW; j++) {
+            const float4 b = *reinterpret_cast<const float4 *>(Bs + j * BP + p);
+            acc[j] = fmaf(a.x, b.x, acc[j]);
+            acc[j] = fmaf(a.y, b.y, acc[j]);
+            acc[j] = fmaf(a.z, b.z, acc[j]);
+            acc[j] = fmaf(a.w, b.w, acc[j]);
+        }
+    }
+#pragma unroll
+    for (int j = 0; j < RW; j++) red[(g * RB + r) * RED_P + j] = acc[j];
+    __syncthreads();
+    const int j0 = threadIdx.x >> 5;
+#pragma unroll
+    for (int h = 0; h < 2; h++) {
+        const int j = j0 + 8 * h;
+        float v = 0.f;
+#pragma unroll
+        for (int q = 0; q < NT / 32; q++) v += red[(q * RB + r) * RED_P + j];
+        out[h] = v;
+    }
+}
+
 __global__ void __launch_bounds__(NT, 1) rhs_solve_kernel(RhsParams p) {
     extern __shared__ __align__(16) float smem[];
+    float *As = smem, *Bs = smem + RB * AP, *red = Bs + RW * BP;
     __shared__ int s_task, s_abort;
     const int n = p.n, nb = p.nb;
     for (;;) {
@@ -68,6 +160,21 @@ __global__ void __launch_bounds__(NT, 1) rhs_solve_kernel(RhsParams p) {
         const int id = s_task;
         if (id >= p.ntasks) break;
         const RhsTask t = p.tasks[id];
+        const int rb = t.b * RB;
+        // the factor slice does not depend on the wait: request it first
+        const float *A;
+        bool ta = p.kind == 0;
+        if (t.type == 0) {
+            const float *D = p.Dinv + (size_t)t.k * nb * nb;
+            A = ta ? D + (size_t)rb * nb : D + rb;
+        } else {
+            A = ta ? p.W + tile_off(n, nb, t.k, t.t) + (size_t)rb * nb : p.W + tile_off(n, nb, t.t, t.k) + rb;
+        }
+        if (ta)
+            load_factor<true>(As, A, nb, nb);
+        else
+            load_factor<false>(As, A, nb, nb);
+        cp_async_commit();
         if (threadIdx.x == 0) {
             const unsigned long long start = globaltimer_ns();
             for (int i = 0; i < t.nwait && !s_abort; i++) {
@@ -82,29 +189,36 @@ __global__ void __launch_bounds__(NT, 1) rhs_solve_kernel(RhsParams p) {
                         s_abort = 1;
                         break;
                     }
-                    __nanosleep(128);
+                    __nanosleep(64);
                 }
             }
         }
         __syncthreads();
-        if (s_abort) break;
-        const int rb = t.b * 64;
+        if (s_abort) {
+            cp_async_wait_all();  // no copy of this CTA left landing in shared memory
+            break;
+        }
+        // APPLY reads R_k, UPDATE reads Y_k (both n x 16, column-major)
+        load_rhs(Bs, (t.type == 0 ? p.R : p.Y) + (size_t)t.k * nb, n, nb);
+        cp_async_commit();
+        cp_async_wait_all();
+        __syncthreads();
+        float v[2];
+        if (ta)
+            block_product<true>(As, Bs, red, nb, v);
+        else
+            block_product<false>(As, Bs, red, nb, v);
+        const int r = threadIdx.x & 31, j0 = threadIdx.x >> 5;
         if (t.type == 0) {
             // Y_k[rb] = op(D_k^-1)[rb rows] R_k
-            const float *D = p.Dinv + (size_t)t.k * nb * nb;
-            float *out = p.Y + (size_t)t.k * nb + rb;
-            for (int e = threadIdx.x; e < 64 * RW; e += NT) out[(e & 63) + (size_t)(e >> 6) * n] = 0.f;
-            __syncthreads();
-            if (p.kind == 0) cta_gemm_rw128<true>(nb, 1.f, D + (size_t)rb * nb, nb, p.R + (size_t)t.k * nb, n, out, n, smem);
-            else cta_gemm_rw128<false>(nb, 1.f, D + rb, nb, p.R + (size_t)t.k * nb, n, out, n, smem);
+            float *out = p.Y + (size_t)t.k * nb + rb + r;
+            out[(size_t)j0 * n] = v[0];
+            out[(size_t)(j0 + 8) * n] = v[1];
         } else {
             // R_t[rb] -= op(W_kt)[rb rows] Y_k
-            float *Rt = p.R + (size_t)t.t * nb + rb;
-            const float *Yk = p.Y + (size_t)t.k * nb;
-            if (p.kind == 0)
-                cta_gemm_rw128<true>(nb, -1.f, p.W + tile_off(n, nb, t.k, t.t) + (size_t)rb * nb, nb, Yk, n, Rt, n, smem);
-            else
-                cta_gemm_rw128<false>(nb, -1.f, p.W + tile_off(n, nb, t.t, t.k) + rb, nb, Yk, n, Rt, n, smem);
+            float *out = p.R + (size_t)t.t * nb + rb + r;
+            out[(size_t)j0 * n] = __ldcg(out + (size_t)j0 * n) - v[0];
+            out[(size_t)(j0 + 8) * n] = __ldcg(out + (size_t)(j0 + 8) * n) - v[1];
         }
         __syncthreads();
         if (threadIdx.x == 0) {
@@ -117,10 +231,10 @@ __global__ void __launch_bounds__(NT, 1) rhs_solve_kernel(RhsParams p) {
 // Task list of one direction, right-looking with a lookahead of one tile: step k's updates of
 // the next tile come first, then that tile's applies (the critical path: they need only those
 // updates and the earlier steps'), then step k's updates of the remaining tiles.  Updates into
-// one 64-row block run in k order (deterministic sums).  Every wait refers to earlier records,
+// one row block run in k order (deterministic sums).  Every wait refers to earlier records,
 // so the in-order dispatch cannot deadlock.
 // Objects: [0, mt) updates into tile t; [mt, 2 mt) applies of tile k; [2 mt, 2 mt + mt * nbl)
-// updates into 64-row block (t, b).
+// updates into row block (t, b).
 std::vector<RhsTask> build_tasks(int mt, int nbl, int kind) {
     std::vector<RhsTask> v;
     const auto order = [&](int i) { return kind == 1 ? mt - 1 - i : i; };  // solve order
@@ -202,7 +316,8 @@ void mpr_release() {
 // stream s.  status: the factorization's status words (a timed-out wait is reported there).
 cudaError_t mpr_solve(const float *W, const float *Dinv, int n, int nb, int kind, float *R, float *Y, int *status,
                       cudaStream_t s) {
-    const int mt = n / nb, nbl = nb / 64;
+    if (nb % mpr::RB || nb > mpr::KMAX || nb % (4 * (f32::NT / 32))) return cudaErrorInvalidValue;
+    const int mt = n / nb, nbl = nb / mpr::RB;
     auto key = std::make_tuple(mt, nbl, kind);
     auto it = mpr::g_cache.find(key);
     if (it == mpr::g_cache.end()) {
