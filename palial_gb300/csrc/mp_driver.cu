@@ -769,9 +769,11 @@ static int solve_one(int alg, const double *dA, int n, int nb, const double *dB,
     PALIAL_CK(cudaMemcpyAsync(mb.r.ptr, dB, sizeof(double) * (size_t)n * nrhs, cudaMemcpyDeviceToDevice, s), "r0");
     PALIAL_CK(cudaStreamSynchronize(s), "init");
     double eta = 1.0, eta_prev = 1e300;
-    int it = 0, gmres_total = 0, gmres_stalls = 0;
+    int it = 0, gmres_total = 0, gmres_stalls = 0, last_inner = 0;
     bool converged = false;
-    bool use_gmres = (o.gmres == 1);
+    // GMRES-IR from the first step when the factorization needed a diagonal shift (A beyond the
+    // factor precision's reach: plain refinement with the shifted factors stagnates)
+    bool use_gmres = (o.gmres == 1) || (shift > 0.0 && o.gmres >= 0);
     PALIAL_CK(mb.x32.ensure(sizeof(double) * (size_t)n * nrhs), "alloc d");
     double *dcorr = mb.x32.as<double>();
     for (it = 1; it <= maxit; it++) {
@@ -785,6 +787,7 @@ static int solve_one(int alg, const double *dA, int n, int nb, const double *dB,
                        1e-4, s, st, &inner);
             if (rc) return rc;
             gmres_total += inner;
+            last_inner = inner;
             if (o.reserved[3] > 0 && gmres_total >= o.reserved[3]) {
                 it++;
                 break;  // GMRES budget of this attempt spent (precision ladder moves up)
@@ -910,6 +913,12 @@ static int solve_one(int alg, const double *dA, int n, int nb, const double *dB,
             // above it when the preconditioner is poor, and the next cycle starts from there
             gmres_stalls = eta > 0.9 * eta_prev ? gmres_stalls + 1 : 0;
             if (gmres_stalls >= 2) break;
+            // within a GMRES budget (opts.reserved[3]): give up as soon as the contraction of
+            // this step, continued, would need more GMRES iterations than are left
+            if (o.reserved[3] > 0 && eta < eta_prev && last_inner > 0) {
+                const double steps = std::ceil(std::log(tol / eta) / std::log(eta / eta_prev));
+                if (steps * last_inner > (double)(o.reserved[3] - gmres_total)) break;
+            }
         } else if (!use_gmres && o.gmres < 0 && it >= 3 && eta > 0.9 * eta_prev) {
             break;
         }

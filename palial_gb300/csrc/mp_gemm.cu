@@ -112,15 +112,18 @@ __device__ __forceinline__ void tma_load_2d(void *dst, const CUtensorMap *map, i
         : "memory");
 }
 
-// Shared-memory matrix descriptor: K-major, 128B swizzle, 8-row atoms 1024 B apart.
+// Shared-memory matrix descriptor: K-major, rows of SWB bytes of K swizzled in SWB-byte
+// atoms (128B swizzle: layout type 2, 64B: type 4), 8-row atoms 8 * SWB bytes apart.
+template <int SWB = 128>
 __device__ __forceinline__ uint64_t smem_desc(const void *p) {
+    static_assert(SWB == 128 || SWB == 64, "swizzle width");
     const uint32_t a = smem_u32(p);
     uint64_t d = 0;
-    d |= (uint64_t)((a & 0x3FFFF) >> 4);   // start address
-    d |= (uint64_t)1 << 16;                // leading byte offset (unused for swizzled K-major)
-    d |= (uint64_t)(1024 >> 4) << 32;      // stride byte offset: 8 rows x 128 B
-    d |= (uint64_t)1 << 46;                // descriptor version (sm_100 family)
-    d |= (uint64_t)2 << 61;                // SWIZZLE_128B
+    d |= (uint64_t)((a & 0x3FFFF) >> 4);            // start address
+    d |= (uint64_t)1 << 16;                         // leading byte offset (unused for swizzled K-major)
+    d |= (uint64_t)((8 * SWB) >> 4) << 32;          // stride byte offset: 8 rows x SWB bytes
+    d |= (uint64_t)1 << 46;                         // descriptor version (sm_100 family)
+    d |= (uint64_t)(SWB == 128 ? 2 : 4) << 61;      // SWIZZLE_128B / SWIZZLE_64B
     return d;
 }
 
@@ -362,11 +365,20 @@ __global__ void __launch_bounds__(NTHR, 1)
 constexpr int RUN_THREADS = 192;
 constexpr uint32_t RUN_TMEM_COLS = 512;
 
+// Stage geometry of the run kernel: 64 bytes of K per stage (one 64B-swizzled row), so the
+// 192 KB ring holds 4 stages for the split modes (8 otherwise): with 2 stages of 128 bytes the
+// MMA warp waited on TMA refills (ncu: tensor pipe 50 % of active cycles, neither L2 nor DRAM
+// busy); 4 shorter stages keep three refills in flight behind the one being consumed.
 template <int MODE>
 struct RunCfg {
     using C = Cfg<MODE>;
-    static constexpr int STAGES = C::SPLIT ? 2 : 4;
-    static constexpr int SMEM = STAGES * C::STAGE_BYTES + 1024 /*align*/ + 256 /*barriers*/;
+    static constexpr int KB = 64;                                  // bytes of K per stage
+    static constexpr int A_BYTES = BM * KB;                        // 8 KB
+    static constexpr int B_BYTES = BN * KB;                        // 16 KB
+    static constexpr int STAGE_BYTES = C::NOPS * (A_BYTES + B_BYTES);
+    static constexpr int STAGES = (192 * 1024) / STAGE_BYTES;      // 4 (split) or 8
+    static constexpr int KELEMS = KB / C::ELEM;
+    static constexpr int SMEM = STAGES * STAGE_BYTES + 1024 /*align*/ + 256 /*barriers*/;
 };
 
 struct RunParams {
@@ -394,11 +406,12 @@ __global__ void __launch_bounds__(RUN_THREADS, 1)
                          const __grid_constant__ CUtensorMap ta_lo, const __grid_constant__ CUtensorMap tb_lo,
                          RunParams rp) {
     using C = Cfg<MODE>;
-    constexpr int S = RunCfg<MODE>::STAGES;
+    using R = RunCfg<MODE>;
+    constexpr int S = R::STAGES;
     const UpdateParams &p = rp.u;
     extern __shared__ __align__(1024) uint8_t smem_raw[];
     uint8_t *base = reinterpret_cast<uint8_t *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
-    uint64_t *full = reinterpret_cast<uint64_t *>(base + S * C::STAGE_BYTES);
+    uint64_t *full = reinterpret_cast<uint64_t *>(base + S * R::STAGE_BYTES);
     uint64_t *empty = full + S;
     uint64_t *tfull = empty + S;   // [2] accumulator ready for the epilogue
     uint64_t *tempty = tfull + 2;  // [2] accumulator drained by the epilogue (4 warp arrivals)
@@ -408,7 +421,7 @@ __global__ void __launch_bounds__(RUN_THREADS, 1)
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const long long g0 = (long long)blockIdx.x * rp.run;
     const int nblk = (int)min((long long)rp.run, rp.nblocks - g0);
-    const int kstages = p.nb * C::ELEM / KBYTES;
+    const int kstages = p.nb * C::ELEM / R::KB;
 
     if (threadIdx.x == 0) {
         for (int s = 0; s < S; s++) {
@@ -446,14 +459,14 @@ __global__ void __launch_bounds__(RUN_THREADS, 1)
                         s_abort = 1;
                         break;
                     }
-                    uint8_t *st = base + s * C::STAGE_BYTES;
-                    mbar_expect_tx(&full[s], C::STAGE_BYTES);
-                    const int kx = kb * C::KELEMS;
+                    uint8_t *st = base + s * R::STAGE_BYTES;
+                    mbar_expect_tx(&full[s], R::STAGE_BYTES);
+                    const int kx = kb * R::KELEMS;
                     tma_load_2d(st, &ta, kx, arow, &full[s]);
-                    tma_load_2d(st + C::A_BYTES, &tb, kx, brow, &full[s]);
+                    tma_load_2d(st + R::A_BYTES, &tb, kx, brow, &full[s]);
                     if (C::NOPS == 2) {
-                        tma_load_2d(st + C::A_BYTES + C::B_BYTES, &ta_lo, kx, arow, &full[s]);
-                        tma_load_2d(st + 2 * C::A_BYTES + C::B_BYTES, &tb_lo, kx, brow, &full[s]);
+                        tma_load_2d(st + R::A_BYTES + R::B_BYTES, &ta_lo, kx, arow, &full[s]);
+                        tma_load_2d(st + 2 * R::A_BYTES + R::B_BYTES, &tb_lo, kx, brow, &full[s]);
                     }
                 }
             }
@@ -482,15 +495,15 @@ __global__ void __launch_bounds__(RUN_THREADS, 1)
                         break;
                     }
                     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-                    uint8_t *st = base + s * C::STAGE_BYTES;
-                    const uint64_t da = smem_desc(st), db = smem_desc(st + C::A_BYTES);
+                    uint8_t *st = base + s * R::STAGE_BYTES;
+                    const uint64_t da = smem_desc<R::KB>(st), db = smem_desc<R::KB>(st + R::A_BYTES);
 #pragma unroll
-                    for (int kk = 0; kk < KBYTES / 32; kk++) {
+                    for (int kk = 0; kk < R::KB / 32; kk++) {
                         const uint32_t accf = (kb | kk) ? 1u : 0u;
                         mma<MODE>(td, da + 2 * kk, db + 2 * kk, accf);
                         if (C::NOPS == 2) {
-                            const uint64_t dal = smem_desc(st + C::A_BYTES + C::B_BYTES);
-                            const uint64_t dbl = smem_desc(st + 2 * C::A_BYTES + C::B_BYTES);
+                            const uint64_t dal = smem_desc<R::KB>(st + R::A_BYTES + R::B_BYTES);
+                            const uint64_t dbl = smem_desc<R::KB>(st + 2 * R::A_BYTES + R::B_BYTES);
                             mma<MODE>(td, da + 2 * kk, dbl + 2 * kk, 1u);   // hi * lo
                             mma<MODE>(td, dal + 2 * kk, db + 2 * kk, 1u);   // lo * hi
                         }
@@ -682,20 +695,23 @@ cudaError_t get_encode() {
     return cudaSuccess;
 }
 
-// K-major packed operand: rows x nb elements, box = box_rows x 128 bytes, 128B swizzle.
-cudaError_t make_map(CUtensorMap *m, const void *base, long long rows, int nb, int elem_bytes, int box_rows) {
+// K-major packed operand: rows x nb elements, box = box_rows x swb bytes, swb-byte swizzle
+// (128 or 64).
+cudaError_t make_map(CUtensorMap *m, const void *base, long long rows, int nb, int elem_bytes, int box_rows,
+                     int swb = 128) {
     cudaError_t e = get_encode();
     if (e != cudaSuccess) return e;
     const cuuint64_t dims[2] = {(cuuint64_t)nb, (cuuint64_t)rows};
     const cuuint64_t strides[1] = {(cuuint64_t)nb * elem_bytes};
-    const cuuint32_t box[2] = {(cuuint32_t)(128 / elem_bytes), (cuuint32_t)box_rows};
+    const cuuint32_t box[2] = {(cuuint32_t)(swb / elem_bytes), (cuuint32_t)box_rows};
     const cuuint32_t estr[2] = {1, 1};
     const CUtensorMapDataType dt = elem_bytes == 1   ? CU_TENSOR_MAP_DATA_TYPE_UINT8
                                    : elem_bytes == 4 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT32
                                                      : CU_TENSOR_MAP_DATA_TYPE_BFLOAT16;
     const CUresult r = g_encode(m, dt, 2,
                                 const_cast<void *>(base), dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
-                                CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                                swb == 64 ? CU_TENSOR_MAP_SWIZZLE_64B : CU_TENSOR_MAP_SWIZZLE_128B,
+                                CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
                                 CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
     return r == CUDA_SUCCESS ? cudaSuccess : cudaErrorInvalidValue;
 }
@@ -767,6 +783,16 @@ cudaError_t launch_mode(const void *a_hi, const void *a_lo, const void *b_hi, co
         return cudaGetLastError();
     }
     if (run < 2) run = 2;  // small launches too: two blocks per CTA beat one block per CTA (measured)
+    constexpr int KB = mp::RunCfg<MODE>::KB;
+    if ((e = make_map(&ta, a_hi, rows, p.nb, eb, mp::BM, KB)) != cudaSuccess) return e;
+    if ((e = make_map(&tb, b_hi, rows, p.nb, eb, mp::BN, KB)) != cudaSuccess) return e;
+    if (C::NOPS == 2) {
+        if ((e = make_map(&tal, a_lo, rows, p.nb, eb, mp::BM, KB)) != cudaSuccess) return e;
+        if ((e = make_map(&tbl, b_lo, rows, p.nb, eb, mp::BN, KB)) != cudaSuccess) return e;
+    } else {
+        tal = ta;
+        tbl = tb;
+    }
     mp::RunParams rp{p, blocks, run};
     note_launch();
     mp::mp_update_run_kernel<MODE><<<(unsigned)((blocks + run - 1) / run), mp::RUN_THREADS, mp::RunCfg<MODE>::SMEM, s>>>(
