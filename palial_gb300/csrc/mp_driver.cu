@@ -22,6 +22,7 @@
 #include <chrono>
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <vector>
 
@@ -88,6 +89,15 @@ struct MpBufs {
     DevBuf dinv_u, dinv_l, stile;  // FP32 inverses of the diagonal factor tiles, solve scratch
 };
 MpBufs mb;
+
+// PALIAL_IR_TRACE=1 in the environment: one line per refinement step on stderr (diagnostics).
+bool ir_trace() {
+    static const bool on = [] {
+        const char *v = std::getenv("PALIAL_IR_TRACE");
+        return v && v[0] == '1';
+    }();
+    return on;
+}
 
 // Update-kernel mode (mp_gemm.cu) of a PALIAL_PREC_* precision: 0 bf16, 1 fp8, 2 bf16x3, 3 tf32x3.
 int update_mode(int prec) {
@@ -897,6 +907,9 @@ static int solve_one(int alg, const double *dA, int n, int nb, const double *dB,
             }
             fp64_phase = true;
         }
+        if (ir_trace())
+            std::fprintf(stderr, "palial ir: alg %d prec %d step %d eta %.3e gmres %d (+%d) %s\n", alg, prec, it, eta,
+                         gmres_total, use_gmres ? last_inner : 0, update_form ? "update-form" : "full");
         if (eta <= tol) {
             converged = true;
             break;
