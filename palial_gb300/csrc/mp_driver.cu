@@ -441,10 +441,13 @@ static cudaError_t apply_A(const double *A, int n, int nb, const double *X, cons
                            nullptr, s);
 }
 
-// GMRES on M^-1 A d = M^-1 r (left preconditioned, FP64 vectors, one Krylov space per
+// GMRES on A M^-1 y = r, d = M^-1 y (right preconditioned, FP64 vectors, one Krylov space per
 // right-hand side, classical Gram-Schmidt applied twice), restart length m, at most maxit
-// iterations; stops when every column's preconditioned residual drops by `rtol`.  d is
-// overwritten.  Returns PALIAL_OK and the iteration count in *iters.
+// iterations; a cycle stops when every column's residual ||r - A d||_2 has dropped by `rtol`.
+// Right preconditioning minimises the true residual itself, so a cycle never raises it (left
+// preconditioning minimises ||M^-1 (r - A d)||, which can grow the true residual when M^-1 is
+// large, as with the low-precision factors of an ill-conditioned A).  d is overwritten.
+// Returns PALIAL_OK and the iteration count in *iters.
 int gmres(int alg, const double *A, const float *W, int n, int nb, const double *r, double *d, int nrhs, int m,
           int maxit, double rtol, cudaStream_t s, palial_status *st, int *iters) {
     const size_t blk = (size_t)n * nrhs;
@@ -460,16 +463,12 @@ int gmres(int alg, const double *A, const float *W, int n, int nb, const double 
     int total = 0;
     bool done = false;
     while (!done && total < maxit) {
-        // z0 = M^-1 (r - A d)
-        if (total == 0) {
-            int rc = precondition(alg, W, n, nb, r, w, nrhs, dscale, hs, s, st);
-            if (rc) return rc;
-        } else {
-            PALIAL_CK(apply_A(A, n, nb, d, r, V, nrhs, s), "inner residual");
-            int rc = precondition(alg, W, n, nb, V, w, nrhs, dscale, hs, s, st);
-            if (rc) return rc;
-        }
-        // beta = ||z0||, V0 = z0 / beta
+        // the cycle's residual r - A d (the first cycle: r)
+        if (total == 0)
+            PALIAL_CK(cudaMemcpyAsync(w, r, sizeof(double) * blk, cudaMemcpyDeviceToDevice, s), "r0");
+        else
+            PALIAL_CK(apply_A(A, n, nb, d, r, w, nrhs, s), "inner residual");
+        // beta = ||r - A d||, V0 = (r - A d) / beta
         PALIAL_CK(mps_multi_dot(w, 1, w, n, nrhs, dH, s), "beta");
         PALIAL_CK(cudaMemcpyAsync(hh.data(), dH, sizeof(double) * nrhs, cudaMemcpyDeviceToHost, s), "beta");
         PALIAL_CK(cudaStreamSynchronize(s), "beta");
@@ -484,10 +483,10 @@ int gmres(int alg, const double *A, const float *W, int n, int nb, const double 
         for (int c = 0; c < nrhs; c++) gv[c][0] = beta[c];
         int j = 0;
         for (; j < m && total < maxit; j++, total++) {
-            // w = M^-1 A V_j
-            PALIAL_CK(apply_A(A, n, nb, V + blk * j, nullptr, tv, nrhs, s), "A v");
-            int rc = precondition(alg, W, n, nb, tv, w, nrhs, dscale, hs, s, st);
+            // w = A M^-1 V_j
+            int rc = precondition(alg, W, n, nb, V + blk * j, tv, nrhs, dscale, hs, s, st);
             if (rc) return rc;
+            PALIAL_CK(apply_A(A, n, nb, tv, nullptr, w, nrhs, s), "A z");
             // CGS twice: h = V^T w, w -= V h
             PALIAL_CK(mps_multi_dot(V, j + 1, w, n, nrhs, dH, s), "cgs");
             PALIAL_CK(mps_multi_axpy(V, j + 1, dH, w, n, nrhs, 0, s), "cgs");
@@ -529,7 +528,7 @@ int gmres(int alg, const double *A, const float *W, int n, int nb, const double 
                 break;
             }
         }
-        // y = R^-1 g per column, d += V y
+        // y = R^-1 g per column, d += M^-1 (V y)
         const int kdim = j;
         std::vector<double> ycoef((size_t)kdim * nrhs, 0.0);
         for (int c = 0; c < nrhs; c++) {
@@ -542,11 +541,12 @@ int gmres(int alg, const double *A, const float *W, int n, int nb, const double 
         }
         if (kdim > 0) {
             PALIAL_CK(cudaMemcpyAsync(dH, ycoef.data(), sizeof(double) * kdim * nrhs, cudaMemcpyHostToDevice, s), "y");
-            // w = V y ; d += w
-            PALIAL_CK(mps_multi_axpy(V, kdim, dH, w, n, nrhs, 1, s), "V y");
+            PALIAL_CK(mps_multi_axpy(V, kdim, dH, w, n, nrhs, 1, s), "V y");  // w = V y
+            int rc = precondition(alg, W, n, nb, w, tv, nrhs, dscale, hs, s, st);  // tv = M^-1 V y
+            if (rc) return rc;
             std::vector<double> ones(nrhs, -1.0);
             PALIAL_CK(cudaMemcpyAsync(dH2, ones.data(), sizeof(double) * nrhs, cudaMemcpyHostToDevice, s), "one");
-            PALIAL_CK(mps_multi_axpy(w, 1, dH2, d, n, nrhs, 0, s), "d += w");
+            PALIAL_CK(mps_multi_axpy(tv, 1, dH2, d, n, nrhs, 0, s), "d += z");
         }
         PALIAL_CK(cudaStreamSynchronize(s), "gmres cycle");
     }

@@ -59,9 +59,12 @@ constexpr int KMAX = 512;              // largest NB
 constexpr int AP = KMAX + 4;           // pitch of a factor row [r][p] (float4-aligned, conflict-free)
 constexpr int BP = KMAX + 4;           // pitch of a right-hand-side column [j][p]
 constexpr int RED_P = RW + 1;          // pitch of the partial sums [g][r][j]
-constexpr int SMEM_FLOATS = RB * AP + RW * BP + (NT / 32) * RB * RED_P;
+// the partial sums reuse the factor slice's space once the products are done: 99 KB per CTA,
+// two CTAs per SM (one computes while the other waits or loads)
+constexpr int SMEM_FLOATS = RB * AP + RW * BP;
 constexpr int SMEM_BYTES = SMEM_FLOATS * 4;
 static_assert(RB * AP >= KMAX * RB, "factor slice fits either layout");
+static_assert(RB * AP >= (NT / 32) * RB * RED_P, "partial sums fit in the factor slice's space");
 
 __device__ __forceinline__ size_t tile_off(int n, int nb, int tm, int tn) {
     return (size_t)nb * nb * ((size_t)tm + (size_t)(n / nb) * tn);
@@ -130,6 +133,7 @@ __device__ __forceinline__ void block_product(const float *As, const float *Bs, 
             acc[j] = fmaf(a.w, b.w, acc[j]);
         }
     }
+    __syncthreads();  // every warp is done with the factor slice: its space takes the partial sums
 #pragma unroll
     for (int j = 0; j < RW; j++) red[(g * RB + r) * RED_P + j] = acc[j];
     __syncthreads();
@@ -144,9 +148,9 @@ __device__ __forceinline__ void block_product(const float *As, const float *Bs, 
     }
 }
 
-__global__ void __launch_bounds__(NT, 1) rhs_solve_kernel(RhsParams p) {
+__global__ void __launch_bounds__(NT, 2) rhs_solve_kernel(RhsParams p) {
     extern __shared__ __align__(16) float smem[];
-    float *As = smem, *Bs = smem + RB * AP, *red = Bs + RW * BP;
+    float *As = smem, *Bs = smem + RB * AP, *red = smem;
     __shared__ int s_task, s_abort;
     const int n = p.n, nb = p.nb;
     for (;;) {
@@ -351,7 +355,7 @@ cudaError_t mpr_solve(const float *W, const float *Dinv, int n, int nb, int kind
     p.kind = kind;
     p.timeout_ns = 30ull * 1000000000ull;
     note_launch();
-    mpr::rhs_solve_kernel<<<g.sms, f32::NT, mpr::SMEM_BYTES, s>>>(p);  // one per SM (255 registers)
+    mpr::rhs_solve_kernel<<<2 * g.sms, f32::NT, mpr::SMEM_BYTES, s>>>(p);  // two per SM
     return cudaGetLastError();
 }
 
