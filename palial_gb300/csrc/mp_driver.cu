@@ -441,21 +441,24 @@ static cudaError_t apply_A(const double *A, int n, int nb, const double *X, cons
                            nullptr, s);
 }
 
-// GMRES on A M^-1 y = r, d = M^-1 y (right preconditioned, FP64 vectors, one Krylov space per
+// Flexible GMRES on A M^-1 y = r (right preconditioned, FP64 vectors, one Krylov space per
 // right-hand side, classical Gram-Schmidt applied twice), restart length m, at most maxit
 // iterations; a cycle stops when every column's residual ||r - A d||_2 has dropped by `rtol`.
-// Right preconditioning minimises the true residual itself, so a cycle never raises it (left
-// preconditioning minimises ||M^-1 (r - A d)||, which can grow the true residual when M^-1 is
-// large, as with the low-precision factors of an ill-conditioned A).  d is overwritten.
-// Returns PALIAL_OK and the iteration count in *iters.
+// Right preconditioning minimises the true residual itself (left preconditioning minimises
+// ||M^-1 (r - A d)||, which can grow the true residual when M^-1 is large, as with the
+// low-precision factors of an ill-conditioned A).  The preconditioned vectors z_j = M^-1 v_j
+// are kept and d = sum_j z_j y_j (flexible GMRES): M^-1 applied in FP32 is not linear in
+// floating point, so applying it once more to sum_j v_j y_j would not give the vector whose
+// residual the Arnoldi process minimised.  d is overwritten.  Returns PALIAL_OK and the
+// iteration count in *iters.
 int gmres(int alg, const double *A, const float *W, int n, int nb, const double *r, double *d, int nrhs, int m,
           int maxit, double rtol, cudaStream_t s, palial_status *st, int *iters) {
     const size_t blk = (size_t)n * nrhs;
-    PALIAL_CK(mb.krylov.ensure(sizeof(double) * blk * (m + 3)), "alloc krylov");
+    PALIAL_CK(mb.krylov.ensure(sizeof(double) * blk * (2 * m + 2)), "alloc krylov");
     PALIAL_CK(mb.hbuf.ensure(sizeof(double) * (size_t)(m + 2) * nrhs * 2), "alloc h");
     double *V = mb.krylov.as<double>();
-    double *w = V + blk * (m + 1);  // work vectors after the basis
-    double *tv = w + blk;
+    double *Z = V + blk * (m + 1);  // z_j = M^-1 v_j
+    double *w = Z + blk * m;        // work vector after the bases
     double *dH = mb.hbuf.as<double>(), *dH2 = dH + (size_t)(m + 2) * nrhs;
     double *dscale = mb.norms.as<double>() + 96;
     std::vector<double> hs(nrhs), hh((size_t)(m + 2) * nrhs), hh2((size_t)(m + 2) * nrhs);
@@ -483,10 +486,10 @@ int gmres(int alg, const double *A, const float *W, int n, int nb, const double 
         for (int c = 0; c < nrhs; c++) gv[c][0] = beta[c];
         int j = 0;
         for (; j < m && total < maxit; j++, total++) {
-            // w = A M^-1 V_j
-            int rc = precondition(alg, W, n, nb, V + blk * j, tv, nrhs, dscale, hs, s, st);
+            // z_j = M^-1 V_j, w = A z_j
+            int rc = precondition(alg, W, n, nb, V + blk * j, Z + blk * j, nrhs, dscale, hs, s, st);
             if (rc) return rc;
-            PALIAL_CK(apply_A(A, n, nb, tv, nullptr, w, nrhs, s), "A z");
+            PALIAL_CK(apply_A(A, n, nb, Z + blk * j, nullptr, w, nrhs, s), "A z");
             // CGS twice: h = V^T w, w -= V h
             PALIAL_CK(mps_multi_dot(V, j + 1, w, n, nrhs, dH, s), "cgs");
             PALIAL_CK(mps_multi_axpy(V, j + 1, dH, w, n, nrhs, 0, s), "cgs");
@@ -528,7 +531,7 @@ int gmres(int alg, const double *A, const float *W, int n, int nb, const double 
                 break;
             }
         }
-        // y = R^-1 g per column, d += M^-1 (V y)
+        // y = R^-1 g per column, d += Z y
         const int kdim = j;
         std::vector<double> ycoef((size_t)kdim * nrhs, 0.0);
         for (int c = 0; c < nrhs; c++) {
@@ -541,12 +544,10 @@ int gmres(int alg, const double *A, const float *W, int n, int nb, const double 
         }
         if (kdim > 0) {
             PALIAL_CK(cudaMemcpyAsync(dH, ycoef.data(), sizeof(double) * kdim * nrhs, cudaMemcpyHostToDevice, s), "y");
-            PALIAL_CK(mps_multi_axpy(V, kdim, dH, w, n, nrhs, 1, s), "V y");  // w = V y
-            int rc = precondition(alg, W, n, nb, w, tv, nrhs, dscale, hs, s, st);  // tv = M^-1 V y
-            if (rc) return rc;
+            PALIAL_CK(mps_multi_axpy(Z, kdim, dH, w, n, nrhs, 1, s), "Z y");  // w = Z y
             std::vector<double> ones(nrhs, -1.0);
             PALIAL_CK(cudaMemcpyAsync(dH2, ones.data(), sizeof(double) * nrhs, cudaMemcpyHostToDevice, s), "one");
-            PALIAL_CK(mps_multi_axpy(tv, 1, dH2, d, n, nrhs, 0, s), "d += z");
+            PALIAL_CK(mps_multi_axpy(w, 1, dH2, d, n, nrhs, 0, s), "d += Z y");
         }
         PALIAL_CK(cudaStreamSynchronize(s), "gmres cycle");
     }
