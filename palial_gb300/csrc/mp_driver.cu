@@ -927,6 +927,8 @@ static int solve_one(int alg, const double *dA, int n, int nb, const double *dB,
             // above it when the preconditioner is poor, and the next cycle starts from there
             gmres_stalls = eta > 0.9 * eta_prev ? gmres_stalls + 1 : 0;
             if (gmres_stalls >= 2) break;
+            // a GMRES step that doubles the error: the factors are no preconditioner for this A
+            if (eta > 2.0 * eta_prev) break;
             // within a GMRES budget (opts.reserved[3]): give up as soon as the contraction of
             // this step, continued, would need more GMRES iterations than are left
             if (o.reserved[3] > 0 && eta < eta_prev && last_inner > 0) {
