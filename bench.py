@@ -423,70 +423,70 @@ def run_batched_solve(args, bs_fp64, count: int, world: int) -> None:
 
 
 def run_costmodel(args, P, torch) -> None:
-    """The learned cost model: train the task-cost MLP on device traces of FP64 Cholesky / LU / QR sweeps,
-    report its prediction error on held-out runs, then factor N=49152 FP64 Cholesky with (a)
-    the learned block size + learned critical-path priorities and (b) the fallback (exhaustive
-    autotuner on a proxy size + static flop-model priorities), and report both makespans."""
+    """The learned cost model: train the task-cost MLP on device traces of FP64 Cholesky / LU / QR
+    sweeps (sweep_plan), report its per-task and per-run (makespan) prediction error on held-out
+    runs, then plan FP64 Cholesky at N = 49152: (a) the learned plan -- (NB, block) with the
+    smallest makespan predicted under the learned costs among plan_space, run with the learned
+    critical-path priorities; (b) the fallback -- the exhaustive autotuner over NB (default
+    block) timed at N = 49152 itself, static flop-model priorities.  Both makespans, the time
+    each method spent choosing, and whether the learned-priority factors equal the static ones
+    bit for bit (same plan, both orders)."""
     import numpy as np
-    from palial_gb300.costmodel import CostModel, exhaustive_block, trace_records
-    # N must be a multiple of NB (reference palial_src/main.c:101-105): 12288 takes all five
-    # NB values of the sweep, 8192 and 16384 the powers of two.
-    sweep = []
-    for alg in ("cholesky", "lu", "qr"):
-        for n in (8192, 12288, 16384):
-            for nb in (256, 384, 512, 768, 1024):
-                if n % nb or (alg == "qr" and n > 12288):
-                    continue
-                bs = nb if alg == "qr" else 0
-                sweep.append((alg, n, nb, bs))
-    xs, ys, tags = [], [], []
+    from palial_gb300.costmodel import COST_NBS, CostModel, exhaustive_nb, learned_run, plan_space, sweep_plan, trace_records
+    runs = [(alg, n, nb, bs) for alg in ("cholesky", "lu", "qr") for (n, nb, bs) in sweep_plan(alg)]
+    rng = np.random.default_rng(0)
+    xs, ys, tags, measured = [], [], [], []
     t0 = time.perf_counter()
-    for alg, n, nb, bs in sweep:
-        x, y = trace_records(torch, alg, n, nb, bs)
+    for alg, n, nb, bs in runs:
+        x, y, sec = trace_records(torch, alg, n, nb, bs, with_time=True)
+        if len(y) > 60000:  # bound the host memory of the largest runs
+            keep = np.sort(rng.choice(len(y), 60000, replace=False))
+            x, y = x[keep], y[keep]
         xs.append(x)
         ys.append(y)
         tags.append(np.full(len(y), len(tags)))
+        measured.append(sec)
     trace_s = time.perf_counter() - t0
     X, Y, T = np.concatenate(xs), np.concatenate(ys), np.concatenate(tags)
-    rng = np.random.default_rng(0)
-    held = set(rng.choice(len(sweep), 3, replace=False).tolist())   # whole runs held out
-    test = np.isin(T, list(held))
+    held = sorted(rng.choice(len(runs), 4, replace=False).tolist())   # whole runs held out
+    test = np.isin(T, held)
     train_idx = np.flatnonzero(~test)
-    if len(train_idx) > 200000:
-        train_idx = rng.choice(train_idx, 200000, replace=False)
+    if len(train_idx) > 400000:
+        train_idx = rng.choice(train_idx, 400000, replace=False)
     m = CostModel(seed=0)
     t1 = time.perf_counter()
-    loss = m.train(X[train_idx], Y[train_idx], epochs=30, batch=1024, lr=2e-3)
+    loss = m.fit(X[train_idx], Y[train_idx], epochs=40, batch=1024, lr=2e-3)
     train_s = time.perf_counter() - t1
-    pred = m.predict(X[test])
-    rel = np.abs(np.exp(pred - Y[test]) - 1.0)
-    nbig, nb, cands = 49152, 512, (128, 256, 512)
+    rel = np.abs(np.exp(m.predict_log_us(X[test]) - Y[test]) - 1.0)
     workers = P.lib().palial_gpu_sm_count()
-    learned_bs, predicted = m.choose_block(0, nbig, nb, cands, workers)
-    fb_bs, fb_times = exhaustive_block(torch, "cholesky", 16384, nb, cands)
-    a0 = torch.empty(nbig * nbig, dtype=torch.float64, device="cuda")
-    P.gen_spd(a0.data_ptr(), nbig, nb, 0)
-    a = torch.empty_like(a0)
-    m.register(0, nbig, nb, learned_bs, workers)
-    a.copy_(a0)
-    st_l = P.factor_dev("cholesky", a.data_ptr(), None, nbig, nb, block=learned_bs, priority=2)
-    res_l = P.residual_probe("cholesky", a0.data_ptr(), a.data_ptr(), nbig, nb, 4)
-    learned_bits = a.clone() if learned_bs == fb_bs else None
-    a.copy_(a0)
-    st_f = P.factor_dev("cholesky", a.data_ptr(), None, nbig, nb, block=fb_bs, priority=0)
-    res_f = P.residual_probe("cholesky", a0.data_ptr(), a.data_ptr(), nbig, nb, 4)
-    same_bits = bool(torch.equal(learned_bits, a)) if learned_bits is not None else None
-    print(json.dumps({"suite": "costmodel", "records_total": int(len(Y)), "records_train": int(len(train_idx)),
-                      "records_heldout": int(test.sum()), "trace_seconds": trace_s, "train_seconds": train_s,
-                      "train_loss_log_us": loss, "heldout_median_rel_error": float(np.median(rel)),
-                      "heldout_p90_rel_error": float(np.percentile(rel, 90)),
-                      "n": nbig, "nb": nb, "candidates": list(cands),
-                      "learned": {"block": learned_bs, "predicted_makespan_s": predicted,
-                                  "measured_makespan_s": st_l.seconds, "residual_probe": res_l},
-                      "fallback": {"block": fb_bs, "proxy_times_s_n16384": fb_times,
-                                   "measured_makespan_s": st_f.seconds, "residual_probe": res_f},
-                      "gain_fallback_over_learned": st_f.seconds / st_l.seconds,
-                      "factors_bitwise_identical_across_schedules": same_bits}), flush=True)
+    held_runs = []
+    for i in held:
+        alg, n, nb, bs = runs[i]
+        pred = m.predicted_makespan(["cholesky", "lu", "qr"].index(alg), n, nb, bs, workers)
+        held_runs.append({"alg": alg, "n": n, "nb": nb, "block": bs, "measured_s": measured[i], "predicted_s": pred,
+                          "rel_error": abs(pred / measured[i] - 1.0)})
+    # planning at the target size
+    nbig = args.costmodel_n
+    t2 = time.perf_counter()
+    preds = {(nb, bs): m.predicted_makespan(0, nbig, nb, bs, workers) for nb, bs in plan_space(nbig)}
+    plan = min(preds, key=preds.get)
+    plan_s = time.perf_counter() - t2
+    fb_nb, fb_times, fb_sums, fb_search_s = exhaustive_nb(torch, "cholesky", nbig, COST_NBS)
+    learned_s, learned_sum = learned_run(torch, m, "cholesky", nbig, plan[0], workers, block=plan[1])
+    static_s, static_sum = learned_run(torch, None, "cholesky", nbig, plan[0], workers, block=plan[1])
+    print(json.dumps({
+        "suite": "costmodel", "runs": len(runs), "records_total": int(len(Y)), "records_train": int(len(train_idx)),
+        "records_heldout": int(test.sum()), "trace_seconds": trace_s, "train_seconds": train_s,
+        "train_loss": loss, "heldout_median_rel_error": float(np.median(rel)),
+        "heldout_p90_rel_error": float(np.percentile(rel, 90)), "heldout_runs_makespan": held_runs,
+        "n": nbig, "plans": {f"nb{nb}/bs{bs}": v for (nb, bs), v in preds.items()},
+        "learned": {"nb": plan[0], "block": plan[1], "predicted_makespan_s": preds[plan], "choice_seconds": plan_s,
+                    "measured_makespan_s": learned_s, "static_priority_makespan_s": static_s},
+        "fallback": {"nb": fb_nb, "block": "default", "measured_s_by_nb": fb_times, "search_seconds": fb_search_s,
+                     "measured_makespan_s": fb_times[fb_nb]},
+        "gain_over_fallback_makespan": fb_times[fb_nb] / learned_s,
+        "gain_learned_over_static_priorities": static_s / learned_s,
+        "factors_bitwise_identical_across_priorities": learned_sum == static_sum}), flush=True)
 
 
 def run_kernels(args, P, torch) -> None:
@@ -528,12 +528,71 @@ def run_kernels(args, P, torch) -> None:
     P.gen_spd(t1.data_ptr(), NB, NB, 0)
     w1 = torch.empty(NB * NB, dtype=torch.float32, device="cuda")
     t_diag = best(lambda: P.mp_factor("cholesky", t1.data_ptr(), w1.data_ptr(), NB, NB, precision=args.precision))
-    print(json.dumps({"suite": "kernels", "n": n, "nb": NB, "precision": args.precision,
-                      "update_step0_s": upd["seconds"], "update_tflops": upd["flop"] / upd["seconds"] * 1e-12,
-                      "update_gbs": upd["bytes"] / upd["seconds"] * 1e-9,
-                      "residual_compensated_call_s": t_df, "residual_update_form_call_s": t_up,
-                      "residual_update_form_gbs": 8.0 * n * n / t_up * 1e-9,
-                      "diag_tile_call_s": t_diag}), flush=True)
+    line = {"suite": "kernels", "n": n, "nb": NB, "precision": args.precision,
+            "update_step0_s": upd["seconds"], "update_tflops": upd["flop"] / upd["seconds"] * 1e-12,
+            "update_gbs": upd["bytes"] / upd["seconds"] * 1e-9,
+            "residual_compensated_call_s": t_df, "residual_update_form_call_s": t_up,
+            "residual_update_form_gbs": 8.0 * n * n / t_up * 1e-9,
+            "diag_tile_call_s": t_diag}
+    if args.all_kernels:
+        line.update(every_kernel_once(P, torch, n))
+    print(json.dumps(line), flush=True)
+
+
+def every_kernel_once(P, torch, n: int) -> dict:
+    """One call of each remaining path of the library at size n (the small case the per-kernel
+    ncu captures select from): mixed-precision Cholesky and LU solves (diagonal tiles, panel
+    solves, block inverses, refinement solves and residuals), FP64 Cholesky / LU / QR on the
+    persistent scheduler, the FP32 QR solve (FP32 task scheduler), a batched FP32 solve of three
+    matrices (FP32 scheduler, batched residual and correction kernels) and a few MLP training
+    steps; wall seconds per call."""
+    import numpy as np
+    out = {}
+    nrhs = 16
+    b = torch.empty(n * nrhs, dtype=torch.float64, device="cuda")
+    P.gen_dense(b.data_ptr(), n, nrhs, 5, P.STREAM_RHS)
+    x = torch.zeros_like(b)
+    a = torch.empty(n * n, dtype=torch.float64, device="cuda")
+    for alg, prec in (("cholesky", "bf16x3"), ("lu", "tf32x3")):
+        P.gen_kappa(a.data_ptr(), n, NB, 1e2, alg == "cholesky", seed=7)
+        st = P.solve_ir(alg, a.data_ptr(), n, NB, b.data_ptr(), x.data_ptr(), nrhs, precision=prec, raise_on_error=False)
+        out[f"{alg}_{prec}_solve_s"] = st.seconds
+    for alg in ("cholesky", "lu", "qr"):
+        if alg == "cholesky":
+            P.gen_spd(a.data_ptr(), n, NB, 0)
+        else:
+            P.gen_uniform(a.data_ptr(), n, NB, 1)
+        s = torch.zeros_like(a) if alg == "qr" else None
+        st = P.factor_dev(alg, a.data_ptr(), s.data_ptr() if s is not None else None, n, NB)
+        out[f"{alg}_fp64_factor_s"] = st.seconds
+        del s
+    P.gen_uniform(a.data_ptr(), n, NB, 1)
+    x.zero_()
+    st = P.qr_solve_ir(a.data_ptr(), n, NB, b.data_ptr(), x.data_ptr(), nrhs, allow_not_converged=True)
+    out["qr_fp32_solve_s"] = st.seconds
+    del a
+    torch.cuda.empty_cache()
+    from palial_gb300 import batched as B
+    rng = np.random.default_rng(0)
+    sizes, nbs, algs = [512, 384, 256], [128, 128, 64], [0, 1, 0]
+    mats = []
+    for k, m in enumerate(sizes):
+        q = rng.uniform(-1, 1, (m, m))
+        mats.append(q @ q.T + m * np.eye(m) if algs[k] == 0 else q + m * np.eye(m))
+    tiles = [torch.from_numpy(np.ascontiguousarray(
+        mm.reshape(m // nb, nb, m // nb, nb).transpose(2, 0, 3, 1)).ravel()).cuda() for mm, m, nb in zip(mats, sizes, nbs)]
+    rhs = [torch.from_numpy(rng.uniform(-1, 1, m)).cuda() for m in sizes]
+    xs = [torch.zeros_like(r) for r in rhs]
+    t0 = time.perf_counter()
+    B.solve(algs, sizes, nbs, [t.data_ptr() for t in tiles], [r.data_ptr() for r in rhs], [v.data_ptr() for v in xs])
+    out["batched_solve_s"] = time.perf_counter() - t0
+    from palial_gb300.costmodel import CostModel
+    m = CostModel(seed=0)
+    xf = rng.uniform(-1, 1, (4096, m.nin)).astype(np.float32)
+    t0 = time.perf_counter()
+    m.train(xf, xf[:, 0].copy(), epochs=2, batch=512)
+    out["mlp_train_s"] = time.perf_counter() - t0
+    return out
 
 
 def run_qr_mixed(args, P, torch) -> None:
@@ -642,6 +701,8 @@ def main() -> None:
     ap.add_argument("--suite", default=None, choices=[None, "fp64", "kappa", "batched", "batched_solve", "costmodel",
                                                       "kernels", "qr_mixed"])
     ap.add_argument("--batch", type=int, default=2000)
+    ap.add_argument("--costmodel-n", type=int, default=49152, help="target size of the cost-model suite")
+    ap.add_argument("--all-kernels", action="store_true", help="kernels suite: also run every other path once")
     ap.add_argument("--no-fp64", action="store_true")
     ap.add_argument("--no-extra", action="store_true", help="skip the kappa / lu / qr keys")
     args = ap.parse_args()
