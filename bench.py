@@ -269,7 +269,7 @@ def time_update_kernel(P, torch, n: int, precision: str = "bf16") -> dict:
     """Live CUDA-event timing of one tcgen05 trailing update (step k = 0, the bench's update
     precision) on an FP32 tile matrix, pack included: tensor flops and algorithmic bytes per
     launch (C read + write in FP32, panel read once in FP32, packed operands written and read)."""
-    code = {"bf16": 1, "fp8": 2, "bf16x3": 3}.get(precision, 1)
+    code = {"bf16": 1, "fp8": 2, "bf16x3": 3, "tf32x3": 6}.get(precision, 1)
     w = torch.randn(n * n, dtype=torch.float32, device="cuda")
     for _ in range(2):
         P.lib().palial_gpu_mp_update_step(0, code, w.data_ptr(), n, NB, 0)
@@ -285,12 +285,12 @@ def time_update_kernel(P, torch, n: int, precision: str = "bf16") -> dict:
     torch.cuda.empty_cache()
     r = n // NB - 1
     pairs = r * (r + 1) // 2
-    products = 3 if code == 3 else 1
-    packed = {1: 2.0, 2: 1.0, 3: 4.0}[code]  # bytes per element of the packed panel(s)
+    products = 3 if code in (3, 6) else 1
+    packed = {1: 2.0, 2: 1.0, 3: 4.0, 6: 8.0}[code]  # bytes per element of the packed panel(s)
     flop = pairs * 2.0 * NB ** 3 * products
     byts = pairs * NB * NB * 8.0 + r * NB * NB * (4.0 + 2.0 * packed)
     t = min(ts)
-    return {"seconds": t, "flop": flop, "bytes": byts}
+    return {"seconds": t, "flop": flop, "bytes": byts, "products": products}
 
 
 def _solve(P, torch, alg: str, da, n: int, b, nrhs: int, precision: str, stream: int):
@@ -878,14 +878,18 @@ def main() -> None:
                          "frac": achieved / peak,
                          "hbm_gbs": gbs, "hbm_frac": gbs / pk.get("hbm_gbs", 6800.0),
                          # DRAM read + write of one launch: ncu (dram__bytes_read.sum +
-                         # dram__bytes_write.sum) on the BF16x3 update at N=8192, k=0 (120 tile
-                         # pairs, 141.7 + 67.0 MB, profiles/mixed_kernels_n8192.md), scaled by tile pairs
-                         "traffic": 208.7e6 / 120 * ((n // NB - 1) * (n // NB) // 2),
-                         "traffic_note": "ncu capture of the BF16x3 update at N=8192 step 0 (bench.py --suite "
-                                         "kernels --n 8192), scaled by tile pairs",
-                         "kernel": "mp_update_kernel<%s> (tcgen05, step k=0 of N=%d, pack included)" % (args.precision, n),
+                         # dram__bytes_write.sum) on the BF16x3 tile-run update at N=16384, k=0 (496
+                         # tile pairs, 576.8 + 469.0 MB, profiles/mp_update_run_n16384.md), scaled by tile pairs
+                         "traffic": 1045.8e6 / 496 * ((n // NB - 1) * (n // NB) // 2),
+                         "traffic_note": "ncu capture of the BF16x3 update at N=16384 step 0 (bench.py --suite "
+                                         "kernels --n 16384), scaled by tile pairs; algorithmic C bytes are 2 MB per pair",
+                         "kernel": "mp_update_run_kernel<%s> (tcgen05, step k=0 of N=%d, pack included)" % (args.precision, n),
                          "tensor_tflops": upd["flop"] / upd["seconds"] * 1e-12,
                          "tensor_frac_of_bf16_peak": upd["flop"] / upd["seconds"] * 1e-12 / pk.get("bf16_tflops", 1900.0),
+                         # the factorization's own flops (one product per tile pair): the BF16x3 split
+                         # spends two thirds of the tensor work on precision
+                         "algorithmic_tflops": upd["flop"] / upd["products"] / upd["seconds"] * 1e-12,
+                         "algorithmic_frac": upd["flop"] / upd["products"] / upd["seconds"] * 1e-12 / pk.get("bf16_tflops", 1900.0),
                          "peak_source": "MEASURED_PEAKS.json (of measured)" if "source" not in pk else "fallback"},
             "cpu_baseline": cpu,
             "clocks": clk.summary(),
