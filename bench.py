@@ -524,6 +524,8 @@ def run_kernels(args, P, torch) -> None:
                                                 1, None))
     t_up = best(lambda: lib.palial_gpu_residual(a.data_ptr(), n, NB, x.data_ptr(), None, r.data_ptr(), 16, 2,
                                                 None))
+    t_dig = best(lambda: lib.palial_gpu_residual(a.data_ptr(), n, NB, x.data_ptr(), b.data_ptr(), r.data_ptr(), 16,
+                                                 3, None))
     t1 = torch.empty(NB * NB, dtype=torch.float64, device="cuda")
     P.gen_spd(t1.data_ptr(), NB, NB, 0)
     w1 = torch.empty(NB * NB, dtype=torch.float32, device="cuda")
@@ -531,7 +533,8 @@ def run_kernels(args, P, torch) -> None:
     line = {"suite": "kernels", "n": n, "nb": NB, "precision": args.precision,
             "update_step0_s": upd["seconds"], "update_tflops": upd["flop"] / upd["seconds"] * 1e-12,
             "update_gbs": upd["bytes"] / upd["seconds"] * 1e-9,
-            "residual_compensated_call_s": t_df, "residual_update_form_call_s": t_up,
+            "residual_compensated_call_s": t_df, "residual_digits_call_s": t_dig,
+            "residual_update_form_call_s": t_up,
             "residual_update_form_gbs": 8.0 * n * n / t_up * 1e-9,
             "diag_tile_call_s": t_diag}
     if args.all_kernels:

@@ -143,9 +143,10 @@ int palial_gpu_factor_dev(int alg, double *dA, double *dS, int n, int nb, const 
  * norms) <= opts->ir_tol (default 1e-14 * n); GMRES-IR when plain refinement stagnates
  * (opts->gmres: -1 never, 0 automatic, 1 always).  NB must be a multiple of 256.
  * Returns PALIAL_ERR_NOT_CONVERGED (with the reached error in st) if the target is missed.
- * The refinement steers with a compensated-FP32 residual (operands split into 48-bit FP32
- * pairs, error-free products and sums, FP64 accumulation every 64 terms; its error is below
- * 1e-12 of the backward error's scale).  When the tolerance is below 1e-11 (or
+ * The refinement's full residuals are computed on the tensor cores from 48-bit digit
+ * expansions of A and X (exact BF16 digit products, exact chunk sums, 64-bit integer
+ * accumulation; palial_gpu_residual mode 3; opts->reserved[4] = 4 uses the compensated-FP32
+ * residual of mode 1 instead), with errors below 1e-12 of the backward error's scale.  When the tolerance is below 1e-11 (or
  * opts->reserved[4] = 2) convergence is confirmed with an FP64 residual; opts->reserved[4] =
  * 1 computes every residual in FP64.  Once a correction d is small (2^-17 ||d|| <= tol/4 ||x||
  * per column) the next residual is r - A d with FP32 products (one HBM-bound pass over A);
@@ -168,8 +169,10 @@ int palial_gpu_solve_ir_host(int alg, const palial_desc *A, const double *B, dou
                              const palial_opts *opts, palial_status *st);
 /* R = B - A X (B may be NULL: R = A X) on device buffers, A an FP64 tile matrix, X, B, R
  * n x nrhs column-major (nrhs <= 16): mode 0 in FP64, mode 1 with the compensated FP32
- * arithmetic the refinement steers with; mode 2 (B must be NULL) is the refinement's update
- * form R <- R - A X with FP32 products (|error| <= 2^-17 |A| |X| per entry). */
+ * arithmetic; mode 2 (B must be NULL) is the refinement's update form R <- R - A X with FP32
+ * products (|error| <= 2^-17 |A| |X| per entry); mode 3 the digit residual on the tensor cores
+ * (A and X as 48-bit integers in 8-bit BF16 digits, exact digit products and chunk sums, 64-bit
+ * integer accumulation; the refinement's full residual). */
 int palial_gpu_residual(const double *dA, int n, int nb, const double *dX, const double *dB, double *dR, int nrhs,
                         int mode, void *stream);
 /* The low-precision factorization alone: dW (n*n floats, tile layout) receives the FP32

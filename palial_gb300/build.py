@@ -24,7 +24,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVFLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr",
            "-Xcompiler", "-Wall", "-Xcompiler", "-Wno-unused-function"]
 
-SOURCES = ["sched_f64.cu", "gen_check.cu", "runtime.cu", "dag.cpp", "noalloc.cu", "mp_gemm.cu", "mp_solve.cu", "mp_driver.cu", "mlp.cu", "nvml_clock.cpp", "qr_solve.cu", "batch_driver.cu", "mp_diag.cu", "mp_rhs.cu", "layout.cu", "rbt.cu", "sched_f32.cu", "batch_solve.cu", "mp_qr.cu"]
+SOURCES = ["sched_f64.cu", "gen_check.cu", "runtime.cu", "dag.cpp", "noalloc.cu", "mp_gemm.cu", "mp_solve.cu", "mp_driver.cu", "mlp.cu", "nvml_clock.cpp", "qr_solve.cu", "batch_driver.cu", "mp_diag.cu", "mp_rhs.cu", "layout.cu", "rbt.cu", "sched_f32.cu", "batch_solve.cu", "mp_qr.cu", "mp_resid_digits.cu"]
 
 
 def nvcc() -> str:

@@ -75,6 +75,8 @@ cudaError_t launch_gen_dense(double *X, long long rows, int cols, uint64_t seed,
 cudaError_t launch_sumsq(const double *X, long long len, double *partial, int blocks, cudaStream_t s);
 void mp_release();
 int set_update_kernel(int kind);
+cudaError_t mrd_residual(const double *A, int n, int nb, const double *X, const double *colmax, const double *B,
+                         double *R, int nrhs, int sigma, uint32_t *Xd, int *tau, double *amax, cudaStream_t s);
 }  // namespace palial
 
 using namespace palial;
@@ -87,6 +89,7 @@ struct MpBufs {
     DevBuf xsplit;  // compensated residual: X as FP32 pairs (n x 16 float2) + 16 scale exponents
     DevBuf binv;    // inverses of the current diagonal tile's 64 x 64 diagonal blocks (panel solves)
     DevBuf dinv_u, dinv_l, stile;  // FP32 inverses of the diagonal factor tiles, solve scratch
+    DevBuf xdig;    // digit residual: X's BF16 digits in fragment order (n * 48 words) + 16 exponents
 };
 MpBufs mb;
 
@@ -387,6 +390,7 @@ int mp_prepare_solves(int alg, const float *W, int n, int nb, cudaStream_t s, pa
 // whether the factors are those of the random-butterfly transform.
 struct ResidCtx {
     bool df = false;
+    bool digits = false;      // the full residuals on the tensor cores (mp_resid_digits.cu)
     int sigma = 0;
     bool rbt = false;         // the factors are those of U^T A V (random butterflies, LU)
     double *f64 = nullptr;    // FP64 factors (n x (n + nb) tile matrix): FP64 triangular solves
@@ -427,18 +431,30 @@ int precondition(int alg, const float *W, int n, int nb, const double *v, double
     return PALIAL_OK;
 }
 
-// A X products of the refinement (B - A X, or A X with B = NULL): the compensated-FP32
-// residual when the current solve uses it (GMRES's inner products need far less than FP64),
-// else FP64.
+// The refinement's FP64-level full residual R = B - A X (B NULL: R = A X) in the solve's form:
+// the digit residual on the tensor cores (default), or the compensated-FP32 one
+// (opts.reserved[4] = 4).  colmax: per-column max |x|; amax_out (optional): ||A||_inf.
+static cudaError_t df_residual(const double *A, int n, int nb, const double *X, const double *colmax, const double *B,
+                               double *R, int nrhs, double *amax_out, cudaStream_t s) {
+    if (g_rctx.digits) {
+        uint32_t *xd = mb.xdig.as<uint32_t>();
+        return mrd_residual(A, n, nb, X, colmax, B, R, nrhs, g_rctx.sigma, xd,
+                            reinterpret_cast<int *>(xd + (size_t)n * 48), amax_out, s);
+    }
+    float2 *xs = mb.xsplit.as<float2>();
+    return mps_residual_df(A, n, nb, X, colmax, B, R, nrhs, g_rctx.sigma, xs, reinterpret_cast<int *>(xs + (size_t)n * 16),
+                           amax_out, s);
+}
+
+// A X products of the refinement (B - A X, or A X with B = NULL): the FP64-level residual of the
+// current solve's form (df_residual), else FP64.
 static cudaError_t apply_A(const double *A, int n, int nb, const double *X, const double *B, double *R, int nrhs,
                            cudaStream_t s) {
     if (!g_rctx.df) return mps_residual(A, n, nb, X, B, R, nrhs, nullptr, s);
     double *cm = mb.norms.as<double>() + 128;
     cudaError_t e = mps_colmax(X, n, nrhs, cm, s);
     if (e != cudaSuccess) return e;
-    float2 *xs = mb.xsplit.as<float2>();
-    return mps_residual_df(A, n, nb, X, cm, B, R, nrhs, g_rctx.sigma, xs, reinterpret_cast<int *>(xs + (size_t)n * 16),
-                           nullptr, s);
+    return df_residual(A, n, nb, X, cm, B, R, nrhs, nullptr, s);
 }
 
 // Flexible GMRES on A M^-1 y = r (right preconditioned, FP64 vectors, one Krylov space per
@@ -561,7 +577,7 @@ int gmres(int alg, const double *A, const float *W, int n, int nb, const double 
 void palial::mp_release() {
     for (DevBuf *b : {&mb.w, &mb.diag, &mb.pa_hi, &mb.pa_lo, &mb.pb_hi, &mb.pb_lo, &mb.scales, &mb.r, &mb.r32,
                       &mb.x32, &mb.norms, &mb.work, &mb.krylov, &mb.hbuf, &mb.gvec, &mb.y32, &mb.xsplit, &mb.binv,
-                      &mb.dinv_u, &mb.dinv_l, &mb.stile})
+                      &mb.dinv_u, &mb.dinv_l, &mb.stile, &mb.xdig})
         b->release();
 }
 
@@ -763,6 +779,8 @@ static int solve_one(int alg, const double *dA, int n, int nb, const double *dB,
     bool fp64_phase = false;
     constexpr double kDfConfirmBelow = 1e-11;
     g_rctx.df = use_df;
+    g_rctx.digits = use_df && o.reserved[4] != 4 && n <= (1 << 18);
+    if (g_rctx.digits) PALIAL_CK(mb.xdig.ensure(sizeof(uint32_t) * (size_t)n * 48 + 64 * sizeof(int)), "alloc digits");
     g_rctx.sigma = sigma;
     // status words of the refinement's solve launches (a timed-out wait is reported there)
     PALIAL_CK(g.diag.status.ensure(sizeof(int) * ST_NSLOTS + 64), "alloc status");
@@ -833,10 +851,8 @@ static int solve_one(int alg, const double *dA, int n, int nb, const double *dB,
         }
         const auto full_residual = [&](double *anorm_out) -> int {
             if (used_df) {
-                float2 *xs = mb.xsplit.as<float2>();
-                PALIAL_CK(mps_residual_df(dA, n, nb, dX, nrm + 33, dB, mb.r.as<double>(), nrhs, sigma, xs,
-                                          reinterpret_cast<int *>(xs + (size_t)n * 16), anorm_out, s),
-                          "residual (compensated FP32)");
+                PALIAL_CK(df_residual(dA, n, nb, dX, nrm + 33, dB, mb.r.as<double>(), nrhs, anorm_out, s),
+                          "residual (digits / compensated FP32)");
             } else {
                 PALIAL_CK(mps_residual(dA, n, nb, dX, dB, mb.r.as<double>(), nrhs, anorm_out, s), "residual");
             }
@@ -1020,7 +1036,7 @@ extern "C" int palial_gpu_solve_ir(int alg, const double *dA, int n, int nb, con
 // (mode 1, the refinement's steering residual); nrhs <= 16.
 extern "C" int palial_gpu_residual(const double *dA, int n, int nb, const double *dX, const double *dB, double *dR,
                                    int nrhs, int mode, void *stream) {
-    if (!dA || !dX || !dR || n <= 0 || nb <= 0 || n % nb || n % 64 || nrhs < 1 || nrhs > 16 || mode < 0 || mode > 2)
+    if (!dA || !dX || !dR || n <= 0 || nb <= 0 || n % nb || n % 64 || nrhs < 1 || nrhs > 16 || mode < 0 || mode > 3)
         return PALIAL_ERR_ARG;
     if (mode == 2 && dB) return PALIAL_ERR_ARG;  // update form: R <- R - A X in place
     palial_status st0;
@@ -1045,6 +1061,14 @@ extern "C" int palial_gpu_residual(const double *dA, int n, int nb, const double
     std::frexp(amax, &sigma);
     PALIAL_CK(mps_colmax(dX, n, nrhs, nrm + 33, s), "norm x");
     float2 *xs = mb.xsplit.as<float2>();
+    if (mode == 3) {
+        PALIAL_CK(mb.xdig.ensure(sizeof(uint32_t) * (size_t)n * 48 + 64 * sizeof(int)), "alloc digits");
+        uint32_t *xd = mb.xdig.as<uint32_t>();
+        PALIAL_CK(mrd_residual(dA, n, nb, dX, nrm + 33, dB, dR, nrhs, sigma, xd, reinterpret_cast<int *>(xd + (size_t)n * 48),
+                               nullptr, s),
+                  "residual (digits)");
+        return PALIAL_OK;
+    }
     if (mode == 2) {
         PALIAL_CK(mps_residual_update(dA, n, nb, dX, nrm + 33, dR, nrhs, sigma, reinterpret_cast<float *>(xs),
                                       reinterpret_cast<int *>(xs + (size_t)n * 16), s),

@@ -295,13 +295,44 @@ def test_compensated_residual_matches_fp64(kind):
     lib = P.lib()
     lib.palial_gpu_residual.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p,
                                         ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_void_p]
-    for mode, bound in ((0, 1e-14), (1, 1e-12)):
+    for mode, bound in ((0, 1e-14), (1, 1e-12), (3, 1e-13)):
         r = torch.zeros(nrhs, n, dtype=torch.float64, device="cuda")
         assert lib.palial_gpu_residual(da.data_ptr(), n, nb, x.data_ptr(), b.data_ptr(), r.data_ptr(), nrhs, mode,
                                        None) == 0
         torch.cuda.synchronize()
         err = ((r.t() - ref).abs().max(dim=0).values / scale).max().item()
         assert err <= bound, (mode, err)
+
+
+@pytest.mark.parametrize("nrhs", [16, 5, 1])
+def test_digit_residual_against_exact_products(nrhs):
+    """The digit residual (mode 3: A and X as 48-bit integers in BF16 digits on the tensor cores),
+    R = A X with B = NULL, against torch's FP64 product: entrywise |error| <= 2^-40 (|A| |X|)_i
+    (its own rounding) + 4 n 2^-53 (|A| |X|)_i (the FP64 reference's); a zero column stays
+    exactly zero and a column of scale 1e-30 is handled by its own exponent."""
+    import ctypes
+    n, nb = 2048, 512
+    da = torch.empty(n * n, dtype=torch.float64, device="cuda")
+    P.gen_kappa(da.data_ptr(), n, nb, 1e6, False, seed=5)
+    g = torch.Generator("cuda").manual_seed(9)
+    x = torch.rand(nrhs, n, dtype=torch.float64, device="cuda", generator=g) - 0.5
+    if nrhs > 3:
+        x[1] = 0.0
+        x[2] *= 1e-30
+    mt = n // nb
+    A = da.view(mt, mt, nb, nb).permute(1, 3, 0, 2).reshape(n, n)
+    lib = P.lib()
+    lib.palial_gpu_residual.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p,
+                                        ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_void_p]
+    r = torch.zeros(nrhs, n, dtype=torch.float64, device="cuda")
+    assert lib.palial_gpu_residual(da.data_ptr(), n, nb, x.data_ptr(), None, r.data_ptr(), nrhs, 3, None) == 0
+    torch.cuda.synchronize()
+    ref = A @ x.t()
+    bound = (2.0 ** -40 + 4 * n * 2.0 ** -53) * (A.abs() @ x.t().abs())
+    err = (r.t() - ref).abs()
+    assert bool((err <= bound).all()), float((err / bound.clamp_min(1e-300)).max())
+    if nrhs > 3:
+        assert bool((r[1] == 0).all())
 
 
 @pytest.mark.parametrize("nrhs", [16, 5])
