@@ -33,9 +33,9 @@ cudaError_t mp_update(int mode, int upper, float *C, int n, int nb, int k, const
                       const void *b_hi, const void *b_lo, const float *scale_a, const float *scale_b, int *status,
                       cudaStream_t s, int part = 0, int r0 = 0, int r1 = 0);
 cudaError_t mp_pack_rows(int mode, const float *W, int n, int nb, int k, void *hi, void *lo, float *scales,
-                         cudaStream_t s);
+                         cudaStream_t s, int t0 = 0, int count = -1);
 cudaError_t mp_pack_cols(int mode, const float *W, int n, int nb, int k, void *hi, void *lo, float *scales,
-                         cudaStream_t s);
+                         cudaStream_t s, int t0 = 0, int count = -1);
 cudaError_t mps_f64_to_f32(const double *A, float *W, int n, int nb, double shift, cudaStream_t s,
                            double *amax = nullptr, bool upper_only = false, int r0 = 0, int r1 = -1);
 cudaError_t mps_residual_df(const double *A, int n, int nb, const double *X, const double *colmax, const double *B,
@@ -45,7 +45,7 @@ cudaError_t mps_residual_update(const double *A, int n, int nb, const double *D,
 cudaError_t mps_tile_to_f64(const float *w, double *d, int nb, cudaStream_t s);
 cudaError_t mps_tile_to_f32(const double *d, float *w, int nb, int upper_only, cudaStream_t s);
 cudaError_t mps_panel_trsm(float *W, int n, int nb, int k, int kind, const float *binv, cudaStream_t s,
-                           void *ph = nullptr, void *pl = nullptr);
+                           void *ph = nullptr, void *pl = nullptr, int t0 = 0, int count = -1);
 cudaError_t mps_block_inverse(const float *W, int n, int nb, int k, int factors, float *binv, cudaStream_t s,
                               int blocks = 0);
 cudaError_t mps_residual(const double *A, int n, int nb, const double *X, const double *B, double *R, int nrhs,
@@ -119,14 +119,19 @@ double unit_roundoff(int prec) {
 
 // Low-precision factorization of W (FP32 tile layout, in place).  Returns PALIAL_OK,
 // PALIAL_ERR_NOT_SPD (Cholesky breakdown) or an error.
-// Lookahead: step k's critical chain (diagonal tile, panel, pack, the update of the next
-// step's tiles) runs on a high-priority stream; the rest of step k's trailing update runs on a
-// low-priority stream, overlapping step k+1's diagonal tile and panel.  The next step's first
-// update waits for it (both write the rows below).  Packed panels alternate between two
-// buffers so step k+1's pack never overwrites what step k's rest still reads.
+// Lookahead on three streams.  The diagonal tile of step k+1 needs only tile (k+1, k+1) after
+// step k, i.e. the first tile of panel k: so step k's critical chain (high priority) is the
+// diagonal tile, its block inverses, the first panel tile and the update of tile (k+1, k+1);
+// the rest of the panel and the rest of row (LU: and column) k+1 run beside it on a
+// middle-priority stream, and the rest of the trailing update on a low-priority stream,
+// overlapping the next steps.  Writers of one tile are ordered by events (the rest update of
+// step k-1 before step k's updates of row k+1; row k+1 before step k+1's panel).  Packed panels
+// and the diagonal blocks' inverses alternate between two buffers, so step k+1 never
+// overwrites what step k's streams still read.
 struct Lookahead {
-    cudaStream_t hi = nullptr, lo = nullptr;
+    cudaStream_t hi = nullptr, mid = nullptr, lo = nullptr;
     cudaEvent_t start = nullptr, packed = nullptr, rest = nullptr, join = nullptr;
+    cudaEvent_t binv = nullptr, first = nullptr, nextrow = nullptr, join_mid = nullptr;
 } g_la;
 
 // Host-buffer solves copy the tiles a Cholesky factorization reads (upper triangle) first
@@ -249,8 +254,11 @@ static cudaError_t lookahead_init() {
     int least = 0, greatest = 0;
     cudaError_t e = cudaDeviceGetStreamPriorityRange(&least, &greatest);
     if (e == cudaSuccess) e = cudaStreamCreateWithPriority(&g_la.hi, cudaStreamNonBlocking, greatest);
+    if (e == cudaSuccess)
+        e = cudaStreamCreateWithPriority(&g_la.mid, cudaStreamNonBlocking, greatest < least ? greatest + 1 : greatest);
     if (e == cudaSuccess) e = cudaStreamCreateWithPriority(&g_la.lo, cudaStreamNonBlocking, least);
-    for (cudaEvent_t *ev : {&g_la.start, &g_la.packed, &g_la.rest, &g_la.join})
+    for (cudaEvent_t *ev : {&g_la.start, &g_la.packed, &g_la.rest, &g_la.join, &g_la.binv, &g_la.first, &g_la.nextrow,
+                            &g_la.join_mid})
         if (e == cudaSuccess) e = cudaEventCreateWithFlags(ev, cudaEventDisableTiming);
     return e;
 }
@@ -272,57 +280,87 @@ int mp_factor(int alg, int prec, float *W, int n, int nb, cudaStream_t s, palial
         PALIAL_CK(mb.pb_lo.ensure(2 * panel), "alloc panel");
     }
     PALIAL_CK(mb.scales.ensure(sizeof(float) * (size_t)std::max(4, slots * 2) * (size_t)std::max(1, mt)), "alloc scales");
-    PALIAL_CK(mb.binv.ensure(sizeof(float) * 2 * (size_t)nb * 64), "alloc block inverses");
+    PALIAL_CK(mb.binv.ensure(sizeof(float) * 4 * (size_t)nb * 64), "alloc block inverses");  // two steps' worth
     PALIAL_CK(g.diag.status.ensure(sizeof(int) * ST_NSLOTS + 64), "alloc status");
     PALIAL_CK(lookahead_init(), "lookahead streams");
     PALIAL_CK(cudaMemsetAsync(g.diag.status.ptr, 0, sizeof(int) * ST_NSLOTS, s), "clear status");
     PALIAL_CK(cudaEventRecord(g_la.start, s), "event");
-    cudaStream_t hi = g_la.hi, lo = g_la.lo;
+    cudaStream_t hi = g_la.hi, mid = g_la.mid, lo = g_la.lo;
     PALIAL_CK(cudaStreamWaitEvent(hi, g_la.start, 0), "event");
+    PALIAL_CK(cudaStreamWaitEvent(mid, g_la.start, 0), "event");
     PALIAL_CK(cudaStreamWaitEvent(lo, g_la.start, 0), "event");
     int *status = g.diag.status.as<int>();
     auto buf = [&](const DevBuf &b, int par) { return static_cast<void *>(static_cast<uint8_t *>(b.ptr) + par * panel); };
     if (arrive) {
         PALIAL_CK(cudaStreamWaitEvent(hi, g_arrival.ready[0], 0), "rows");
+        PALIAL_CK(cudaStreamWaitEvent(mid, g_arrival.ready[0], 0), "rows");
         PALIAL_CK(cudaStreamWaitEvent(lo, g_arrival.ready[0], 0), "rows");
     }
     ArrivalPlan plan;
     if (arrive)
         plan = plan_arrival(mt, nb, mode, g_arrival.ngroups, g_arrival.gs, g_arrival.ge, g_arrival.due, g_arrival.kg);
-    bool have_rest = false;
+    bool have_rest = false, have_next = false;
+    // BF16 / BF16x3: the row-panel solve writes the packed operand with its results; FP8 needs
+    // per-tile scales first and TF32x3 FP32 containers, so they pack in a separate pass
+    const bool fused = mode == 0 || mode == 2;
+    const int upper = alg == 0 ? 1 : 0;
     for (int k = 0; k < mt; k++) {
-        // the diagonal tile in FP32, one CTA (mp_diag.cu)
-        PALIAL_CK(mpd_factor_tile(alg, W, n, nb, k, status, mb.binv.as<float>(), hi), "diag factor");
+        float *binv = mb.binv.as<float>() + (size_t)(k & 1) * 2 * nb * 64;
+        // the diagonal tile in FP32 (mp_diag.cu)
+        PALIAL_CK(mpd_factor_tile(alg, W, n, nb, k, status, binv, hi), "diag factor");
         if (k == mt - 1) break;
+        const int ntr = mt - k - 1;
         const int par = arrive ? k : (k & 1);
         float *sa = mb.scales.as<float>() + 2 * mt * par, *sb = sa + mt;
         void *ah = buf(mb.pa_hi, par), *al = split ? buf(mb.pa_lo, par) : nullptr;
         void *bh = buf(mb.pb_hi, k & 1), *bl = split ? buf(mb.pb_lo, k & 1) : nullptr;
-        float *binv = mb.binv.as<float>();
-        PALIAL_CK(mps_block_inverse(W, n, nb, k, alg == 0 ? 1 : 2, binv, hi), "diagonal block inverses");
-        // BF16 / BF16x3: the row-panel solve writes the packed operand with its results; FP8
-        // needs per-tile scales first and TF32x3 FP32 containers, so they pack in a separate pass
-        const bool fused = mode == 0 || mode == 2;
         if (alg == 0) {
-            PALIAL_CK(mps_panel_trsm(W, n, nb, k, 0, binv, hi, fused ? ah : nullptr, fused ? al : nullptr), "panel trsm");
-            if (!fused) PALIAL_CK(mp_pack_rows(mode, W, n, nb, k, ah, al, sa, hi), "pack");
             bh = ah;
             bl = al;
             sb = sa;
-        } else {
-            PALIAL_CK(mps_panel_trsm(W, n, nb, k, 1, binv, hi, fused ? bh : nullptr, fused ? bl : nullptr),
-                      "row panel trsm");
-            PALIAL_CK(mps_panel_trsm(W, n, nb, k, 2, binv, hi), "column panel trsm");
-            PALIAL_CK(mp_pack_cols(mode, W, n, nb, k, ah, al, sa, hi), "pack L");
-            if (!fused) PALIAL_CK(mp_pack_rows(mode, W, n, nb, k, bh, bl, sb, hi), "pack U");
         }
-        PALIAL_CK(cudaEventRecord(g_la.packed, hi), "event");
+        PALIAL_CK(mps_block_inverse(W, n, nb, k, alg == 0 ? 1 : 2, binv, hi), "diagonal block inverses");
+        PALIAL_CK(cudaEventRecord(g_la.binv, hi), "event");
+        // panel tiles [t0, t0 + cnt) on stream q, packed
+        const auto panel_part = [&](cudaStream_t q, int t0, int cnt) -> int {
+            if (alg == 0) {
+                PALIAL_CK(mps_panel_trsm(W, n, nb, k, 0, binv, q, fused ? ah : nullptr, fused ? al : nullptr, t0, cnt),
+                          "panel trsm");
+                if (!fused) PALIAL_CK(mp_pack_rows(mode, W, n, nb, k, ah, al, sa, q, t0, cnt), "pack");
+            } else {
+                PALIAL_CK(mps_panel_trsm(W, n, nb, k, 1, binv, q, fused ? bh : nullptr, fused ? bl : nullptr, t0, cnt),
+                          "row panel trsm");
+                PALIAL_CK(mps_panel_trsm(W, n, nb, k, 2, binv, q, nullptr, nullptr, t0, cnt), "column panel trsm");
+                PALIAL_CK(mp_pack_cols(mode, W, n, nb, k, ah, al, sa, q, t0, cnt), "pack L");
+                if (!fused) PALIAL_CK(mp_pack_rows(mode, W, n, nb, k, bh, bl, sb, q, t0, cnt), "pack U");
+            }
+            return PALIAL_OK;
+        };
+        // critical chain: the first panel tile (row k+1's tile (k, k+1) was updated by step k-1's
+        // row update), then tile (k+1, k+1) after step k-1's rest update
+        if (have_next) PALIAL_CK(cudaStreamWaitEvent(hi, g_la.nextrow, 0), "event");
+        int rc2 = panel_part(hi, 0, 1);
+        if (rc2) return rc2;
+        PALIAL_CK(cudaEventRecord(g_la.first, hi), "event");
         if (have_rest) PALIAL_CK(cudaStreamWaitEvent(hi, g_la.rest, 0), "event");
-        PALIAL_CK(mp_update(mode, alg == 0 ? 1 : 0, W, n, nb, k, ah, al, bh, bl, sa, sb, status, hi, 1), "update (next)");
+        PALIAL_CK(mp_update(mode, upper, W, n, nb, k, ah, al, bh, bl, sa, sb, status, hi, 4), "update (diagonal)");
+        // beside it: the rest of the panel, then the rest of row (LU: and column) k+1
+        PALIAL_CK(cudaStreamWaitEvent(mid, g_la.binv, 0), "event");
+        if (ntr > 1) {
+            rc2 = panel_part(mid, 1, -1);
+            if (rc2) return rc2;
+        }
+        PALIAL_CK(cudaStreamWaitEvent(mid, g_la.first, 0), "event");
+        PALIAL_CK(cudaEventRecord(g_la.packed, mid), "event");  // the whole panel k is packed
+        if (have_rest) PALIAL_CK(cudaStreamWaitEvent(mid, g_la.rest, 0), "event");
+        if (ntr > 1) PALIAL_CK(mp_update(mode, upper, W, n, nb, k, ah, al, bh, bl, sa, sb, status, mid, 5), "update (next)");
+        PALIAL_CK(cudaEventRecord(g_la.nextrow, mid), "event");
+        have_next = true;
+        // the rest of the trailing update
         PALIAL_CK(cudaStreamWaitEvent(lo, g_la.packed, 0), "event");
         if (!arrive) {
-            PALIAL_CK(mp_update(mode, alg == 0 ? 1 : 0, W, n, nb, k, ah, al, bh, bl, sa, sb, status, lo, 2),
-                      "update (rest)");
+            if (ntr > 1)
+                PALIAL_CK(mp_update(mode, upper, W, n, nb, k, ah, al, bh, bl, sa, sb, status, lo, 2), "update (rest)");
         } else {
             RowArrival &ar = g_arrival;
             // the planned actions (plan_arrival): group gi's data, or its step sk update, on lo
@@ -341,7 +379,7 @@ int mp_factor(int alg, int prec, float *W, int n, int nb, cudaStream_t s, palial
                 }
                 return PALIAL_OK;
             };
-            int rc2 = run(plan.pre[k]);
+            rc2 = run(plan.pre[k]);
             if (rc2) return rc2;
             const int present = plan.present[k];
             if (present - k - 1 > 1)
@@ -354,7 +392,9 @@ int mp_factor(int alg, int prec, float *W, int n, int nb, cudaStream_t s, palial
         have_rest = true;
     }
     PALIAL_CK(cudaEventRecord(g_la.join, lo), "event");
+    PALIAL_CK(cudaEventRecord(g_la.join_mid, mid), "event");
     PALIAL_CK(cudaStreamWaitEvent(hi, g_la.join, 0), "event");
+    PALIAL_CK(cudaStreamWaitEvent(hi, g_la.join_mid, 0), "event");
     PALIAL_CK(cudaEventRecord(g_la.join, hi), "event");
     PALIAL_CK(cudaStreamWaitEvent(s, g_la.join, 0), "event");
     int hs[ST_NSLOTS];

@@ -70,7 +70,8 @@ struct UpdateParams {
     int upper;                // 1: only tile pairs (ti <= tj) (Cholesky), 0: all (LU)
     int part;                 // 0: every pair; 1: the next step's tiles (row 0; LU also column
                               // 0); 2: all other pairs (lookahead split); 3 (upper only): the
-                              // pairs of trailing rows r0 <= ti < r1, row by row
+                              // pairs of trailing rows r0 <= ti < r1, row by row; 4: the pair
+                              // (0, 0) alone; 5: part 1 without the pair (0, 0)
     int r0, r1;               // part 3 row range (trailing-relative)
     const float *scale_a;     // FP8: per trailing tile scale of A_op rows (nullptr: 1)
     const float *scale_b;     // FP8: per trailing tile scale of B_op rows
@@ -182,6 +183,20 @@ __device__ __forceinline__ void decode_part(int q, int ntr, int upper, int part,
             tj = q;
         } else {
             ti = q - ntr + 1;
+            tj = 0;
+        }
+        return;
+    }
+    if (part == 4) {  // the next step's diagonal tile alone
+        ti = tj = 0;
+        return;
+    }
+    if (part == 5) {  // the next step's row (LU: and column) without its diagonal tile
+        if (upper || q < ntr - 1) {
+            ti = 0;
+            tj = q + 1;
+        } else {
+            ti = q - (ntr - 1) + 1;
             tj = 0;
         }
         return;
@@ -602,8 +617,8 @@ __device__ __forceinline__ void pack_one(int mode, float x, void *hi, void *lo, 
 // MODE 0: bf16; 2: bf16 hi + lo; 3: tf32 hi + lo (FP32 containers); 1: e4m3 with per-tile
 // scale (max|x| / 448).
 __global__ void pack_rows_kernel(const float *W, int n, int nb, int k, int mode, void *hi, void *lo,
-                                 float *scales) {
-    const int t = blockIdx.y;                   // trailing tile index
+                                 float *scales, int t0) {
+    const int t = t0 + blockIdx.y;              // trailing tile index
     const int mt = n / nb;
     const float *tile = W + (size_t)nb * nb * ((size_t)k + (size_t)mt * (k + 1 + t));
     const size_t out0 = (size_t)t * nb * nb;
@@ -637,9 +652,9 @@ __global__ void pack_rows_kernel(const float *W, int n, int nb, int k, int mode,
 // Column panel k (LU L(m, k), m > k): packed row (m-k-1)*nb + i, col p = tile (m, k)
 // element (i, p): a transpose, through shared memory 32 x 32 at a time.
 __global__ void pack_cols_kernel(const float *W, int n, int nb, int k, int mode, void *hi, void *lo,
-                                 const float *scales) {
+                                 const float *scales, int t0) {
     __shared__ float s[32][33];
-    const int t = blockIdx.z;
+    const int t = t0 + blockIdx.z;
     const int mt = n / nb;
     const float *tile = W + (size_t)nb * nb * ((size_t)(k + 1 + t) + (size_t)mt * k);
     const int i0 = blockIdx.x * 32, p0 = blockIdx.y * 32;
@@ -657,9 +672,9 @@ __global__ void pack_cols_kernel(const float *W, int n, int nb, int k, int mode,
 }
 
 // per-tile max-abs scales of the column panel (FP8 mode)
-__global__ void col_scales_kernel(const float *W, int n, int nb, int k, float *scales) {
+__global__ void col_scales_kernel(const float *W, int n, int nb, int k, float *scales, int t0) {
     __shared__ float red[32];
-    const int t = blockIdx.x;
+    const int t = t0 + blockIdx.x;
     const int mt = n / nb;
     const float *tile = W + (size_t)nb * nb * ((size_t)(k + 1 + t) + (size_t)mt * k);
     float mx = 0.f;
@@ -761,8 +776,10 @@ cudaError_t launch_mode(const void *a_hi, const void *a_lo, const void *b_hi, co
         tbl = tb;
     }
     const long long nt = p.ntr, ns = nt - 1;
-    long long pairs = p.part == 1 ? (p.upper ? nt : 2 * nt - 1)
+    long long pairs = p.part == 1   ? (p.upper ? nt : 2 * nt - 1)
                       : p.part == 2 ? (p.upper ? ns * (ns + 1) / 2 : ns * ns)
+                      : p.part == 4 ? 1
+                      : p.part == 5 ? (p.upper ? ns : 2 * ns)
                                     : (p.upper ? nt * (nt + 1) / 2 : nt * nt);
     if (p.part == 3) {
         if (!p.upper || p.r0 < 0 || p.r1 > p.ntr) return cudaErrorInvalidValue;
@@ -835,29 +852,35 @@ int set_update_kernel(int kind) {
     return old;
 }
 
-// Pack the row panel k (tiles (k, m), m > k) of the FP32 tile matrix W.
+// Pack the row panel k (tiles (k, m), m > k) of the FP32 tile matrix W: trailing tiles
+// [t0, t0 + count) (count < 0: to the end).
 cudaError_t mp_pack_rows(int mode, const float *W, int n, int nb, int k, void *hi, void *lo, float *scales,
-                         cudaStream_t s) {
+                         cudaStream_t s, int t0, int count) {
     const int ntr = n / nb - k - 1;
-    if (ntr <= 0) return cudaSuccess;
-    dim3 grid(mode == 1 ? 1 : 16, ntr);
+    if (count < 0) count = ntr - t0;
+    if (ntr <= 0 || count <= 0) return cudaSuccess;
+    if (t0 < 0 || t0 + count > ntr) return cudaErrorInvalidValue;
+    dim3 grid(mode == 1 ? 1 : 16, count);
     note_launch();
-    mp::pack_rows_kernel<<<grid, 1024, 0, s>>>(W, n, nb, k, mode, hi, lo, scales);
+    mp::pack_rows_kernel<<<grid, 1024, 0, s>>>(W, n, nb, k, mode, hi, lo, scales, t0);
     return cudaGetLastError();
 }
 
-// Pack the column panel k (tiles (m, k), m > k), transposed to K-major.
+// Pack the column panel k (tiles (m, k), m > k), transposed to K-major: trailing tiles
+// [t0, t0 + count) (count < 0: to the end).
 cudaError_t mp_pack_cols(int mode, const float *W, int n, int nb, int k, void *hi, void *lo, float *scales,
-                         cudaStream_t s) {
+                         cudaStream_t s, int t0, int count) {
     const int ntr = n / nb - k - 1;
-    if (ntr <= 0) return cudaSuccess;
+    if (count < 0) count = ntr - t0;
+    if (ntr <= 0 || count <= 0) return cudaSuccess;
+    if (t0 < 0 || t0 + count > ntr) return cudaErrorInvalidValue;
     if (mode == 1) {
         note_launch();
-        mp::col_scales_kernel<<<ntr, 1024, 0, s>>>(W, n, nb, k, scales);
+        mp::col_scales_kernel<<<count, 1024, 0, s>>>(W, n, nb, k, scales, t0);
     }
-    dim3 grid(nb / 32, nb / 32, ntr), block(32, 8);
+    dim3 grid(nb / 32, nb / 32, count), block(32, 8);
     note_launch();
-    mp::pack_cols_kernel<<<grid, block, 0, s>>>(W, n, nb, k, mode, hi, lo, scales);
+    mp::pack_cols_kernel<<<grid, block, 0, s>>>(W, n, nb, k, mode, hi, lo, scales, t0);
     return cudaGetLastError();
 }
 

@@ -486,12 +486,14 @@ __device__ __forceinline__ void strip_run(const Smem &m, const float *U, int ldu
 // ph, pl (row panels, optional): the packed BF16 (+ BF16x3 remainder) operand of the row panel,
 // trailing tile t - k - 1 at (t - k - 1) nb^2, written together with the solved values.
 __global__ void __launch_bounds__(NT, 2) panel_trsm_kernel(float *W, int n, int nb, int k, int kind,
-                                                          const float *binv, __nv_bfloat16 *ph, __nv_bfloat16 *pl) {
+                                                          const float *binv, __nv_bfloat16 *ph, __nv_bfloat16 *pl,
+                                                          int t0) {
     extern __shared__ __align__(16) float smem[];
     const Smem m = smem_parts(smem);
-    const int t = k + 1 + blockIdx.y, s = blockIdx.x;
+    const int tt = t0 + blockIdx.y;  // trailing tile index
+    const int t = k + 1 + tt, s = blockIdx.x;
     const float *T = W + tile_off(n, nb, k, k);
-    const size_t po = (size_t)blockIdx.y * nb * nb + (size_t)s * 64 * nb;
+    const size_t po = (size_t)tt * nb * nb + (size_t)s * 64 * nb;
     __nv_bfloat16 *sh = ph ? ph + po : nullptr, *sl = pl ? pl + po : nullptr;
     if (kind == 0) strip_lut(m, T, nb, W + tile_off(n, nb, k, t) + (size_t)s * 64 * nb, nb, nb, binv, sh, sl);
     else if (kind == 1)
@@ -862,14 +864,16 @@ cudaError_t mps_half_update(float *T, int h, int ld, int alg, cudaStream_t s) {
 }
 // ph / pl: optional packed BF16 row-panel operand written by the solve (kinds 0 and 1)
 cudaError_t mps_panel_trsm(float *W, int n, int nb, int k, int kind, const float *binv, cudaStream_t s, void *ph,
-                           void *pl) {
+                           void *pl, int t0, int count) {
     const int ntr = n / nb - k - 1;
-    if (ntr <= 0) return cudaSuccess;
-    dim3 grid(nb / 64, ntr);
+    if (count < 0) count = ntr - t0;
+    if (ntr <= 0 || count <= 0) return cudaSuccess;
+    if (t0 < 0 || t0 + count > ntr) return cudaErrorInvalidValue;
+    dim3 grid(nb / 64, count);
     note_launch();
     mps::panel_trsm_kernel<<<grid, mps::NT, mps::SMEM_BYTES, s>>>(W, n, nb, k, kind, binv,
                                                                    kind == 2 ? nullptr : static_cast<__nv_bfloat16 *>(ph),
-                                                                   kind == 2 ? nullptr : static_cast<__nv_bfloat16 *>(pl));
+                                                                   kind == 2 ? nullptr : static_cast<__nv_bfloat16 *>(pl), t0);
     return cudaGetLastError();
 }
 cudaError_t mps_residual(const double *A, int n, int nb, const double *X, const double *B, double *R, int nrhs,
