@@ -405,7 +405,7 @@ def run_batched_solve(args, bs_fp64, count: int, world: int) -> None:
     fp64 = B.solve_synthetic(args.batch, seed=2, rank=0, world=world, autotune=False,
                              bs12=list(bs_fp64) * 2, prec12=[0] * 12, reps=reps)
     mixed = B.solve_synthetic(args.batch, seed=2, rank=0, world=world, autotune=True, reps=reps)
-    prec_name = {0: "fp64", 1: "fp32+ir"}
+    prec_name = {0: "fp64", 1: "fp32+ir", 2: "bf16x3-update+ir"}
     phases = ("factor", "refine", "fp64_fallback")
     choice = {f"{('cholesky', 'lu')[k // 6]} {B.class_label(k % 6)}":
               {"block": mixed["bs_of_class"][k], "precision": prec_name[mixed["prec_of_class"][k]]}

@@ -207,7 +207,9 @@ int palial_gpu_qr_solve(int rows, int cols, int nb, const double *dA, const doub
  * DAG and R/V/T layout) computed in FP32 by the FP32 task scheduler, then FP64 refinement
  * X += |R| R_f^-1 Q_f^T (R / |R|) with R = B - A X in FP64, until every column's normwise
  * backward error |r_j|/(|A||x_j| + |b_j|) <= opts->ir_tol (0: 1e-14 * n).  NB: a multiple of
- * 64 up to 512.  A refinement that does not halve the error per step (or exceeds
+ * 64 up to 512.  opts->precision = PALIAL_PREC_BF16X3 runs TSMQR's two products with V on the
+ * warp tensor cores (BF16x3 split operands, FP32 accumulation) instead of FP32 FMAs.  A refinement
+ * that does not halve the error per step (or exceeds
  * opts->ir_max_iter, 0 = 30) hands the system to palial_gpu_qr_solve (FP64).  status:
  * ir_iters, backward_error, factor_seconds, precision_used = the precision that produced the
  * result (PALIAL_PREC_FP32 or PALIAL_PREC_FP64). */
@@ -310,13 +312,16 @@ int palial_gpu_batched_f32(int count, const int *algs, const int *ns, const int 
  * dividing n; 16-byte aligned; not modified), right-hand side dB[i] and solution dX[i] (n
  * doubles each).  precs[i] (NULL: all FP32): PALIAL_PREC_FP32 = the matrix is rounded to FP32
  * and factored with the other FP32 matrices in ONE persistent launch, then refined with FP64
- * residuals; PALIAL_PREC_FP64 = factored in FP64 (one launch for those).  An FP32 matrix whose
+ * residuals; PALIAL_PREC_BF16X3 = the same FP32 storage and launch with the update tasks'
+ * products (SYRK, GEMM) on the warp tensor cores as BF16x3 (split operands, three products, FP32
+ * accumulation; the "BF16-update" form); PALIAL_PREC_FP64 = factored in FP64 (one launch for
+ * those).  An FP32 or BF16x3 matrix whose
  * factorization breaks down or whose refinement stalls (less than 2x per step, at most
  * opts->ir_max_iter steps, 0 = 30) is refactored in FP64 and refined again.  iters[i]
  * (optional): refinement steps, or -(steps + 1) for a matrix that fell back to FP64; berr[i]
  * (optional): its final backward error.  st: seconds = wall time of the call, factor_seconds =
  * the factorization launches, backward_error = the worst, ir_iters = the most steps,
- * ntasks = the number of FP64 fallbacks.  Returns PALIAL_ERR_NOT_CONVERGED if a matrix stays
+ * fallbacks = the number of FP64 fallbacks.  Returns PALIAL_ERR_NOT_CONVERGED if a matrix stays
  * above its tolerance; an FP64 Cholesky breakdown fails the call (PALIAL_ERR_NOT_SPD). */
 int palial_gpu_batched_solve(int count, const int *algs, const int *ns, const int *nbs,
                              const double *const *dA, const double *const *dB, double *const *dX,
@@ -359,7 +364,8 @@ int palial_gpu_batch_synthetic(int count, uint64_t seed, int rank, int world, in
 typedef struct palial_batch_solve_report {
     int count;                /* matrices solved by this rank                                */
     int bs_of_class[12];      /* block (= tile) size per [alg * 6 + size class]              */
-    int prec_of_class[12];    /* 1 = FP32 factorization + FP64 refinement, 0 = FP64          */
+    int prec_of_class[12];    /* 1 = FP32 factorization + FP64 refinement, 2 = the same with its
+                                 updates as BF16x3 products on the tensor cores, 0 = FP64     */
     int fallbacks;            /* most matrices refactored in FP64 in one timed solve         */
     int max_iters;            /* most refinement steps of one matrix                         */
     int not_converged;        /* 1 if a timed solve left a matrix above its tolerance        */
@@ -368,7 +374,7 @@ typedef struct palial_batch_solve_report {
     double tflops;            /* factorization flops (N^3/3, 2N^3/3) / seconds               */
     double max_backward_error;
     double autotune_seconds;
-    double autotune_s[72];    /* [alg*6 + class][precision 0,1][block 64,128,256] seconds;
+    double autotune_s[108];   /* [alg*6 + class][precision 0,1,2][block 64,128,256] seconds;
                                  -1 = not run, -2 = did not reach the tolerance              */
     double phase_seconds[3];  /* median run: copies + first factorizations, refinement,
                                  FP64 fallback (copies, factorization, refinement)           */

@@ -35,7 +35,7 @@ class SolveReport(ctypes.Structure):
                 ("fallbacks", ctypes.c_int), ("max_iters", ctypes.c_int), ("not_converged", ctypes.c_int),
                 ("seconds", ctypes.c_double), ("matrices_per_s", ctypes.c_double), ("tflops", ctypes.c_double),
                 ("max_backward_error", ctypes.c_double), ("autotune_seconds", ctypes.c_double),
-                ("autotune_s", ctypes.c_double * 72), ("phase_seconds", ctypes.c_double * 3)]
+                ("autotune_s", ctypes.c_double * 108), ("phase_seconds", ctypes.c_double * 3)]
 
 
 class BatchReport(ctypes.Structure):
@@ -213,7 +213,8 @@ def factor_f32(algs, ns, nbs, ptrs, bss=None) -> tuple[Status, np.ndarray]:
 def solve(algs, ns, nbs, a_ptrs, b_ptrs, x_ptrs, precs=None, ir_tol: float = 0.0, ir_max_iter: int = 0,
           allow_not_converged: bool = False) -> tuple[Status, np.ndarray, np.ndarray]:
     """Batched solves A_i x_i = b_i (device buffers: A in the tile layout with tile nbs[i], b and
-    x of ns[i] doubles).  precs[i]: "fp32" (default) or "fp64" factorization.  Returns (status,
+    x of ns[i] doubles).  precs[i]: "fp32" (default), "bf16x3" (FP32 with its updates on the tensor
+    cores as BF16x3 products) or "fp64" factorization.  Returns (status,
     iters, backward errors); iters[i] < 0 marks a matrix refactored in FP64 after its FP32
     attempt (-(steps + 1))."""
     count = len(ns)

@@ -150,7 +150,9 @@ int run_solve_batch(SolveBatch &b, const palial_opts &o, SolveResult &res, palia
     const int count = (int)b.ns.size();
     std::vector<int> prec(count), iters(count);
     std::vector<double> berr(count);
-    for (int j = 0; j < count; j++) prec[j] = b.prec[j] ? PALIAL_PREC_FP32 : PALIAL_PREC_FP64;
+    // precision choice per matrix: 0 FP64, 1 FP32, 2 FP32 storage with BF16x3 tensor-core updates
+    for (int j = 0; j < count; j++)
+        prec[j] = b.prec[j] == 2 ? PALIAL_PREC_BF16X3 : b.prec[j] ? PALIAL_PREC_FP32 : PALIAL_PREC_FP64;
     palial_status s2;
     const int rc = batched_solve_run(count, b.algs.data(), b.np.data(), b.bs.data(), b.A.data(), b.B.data(),
                                      b.X.data(), prec.data(), &o, &s2, iters.data(), berr.data(), res.phases, nullptr);
@@ -328,7 +330,7 @@ int palial_gpu_batch_solve_autotune(int count, const int *ns, const int *algs, u
     palial_opts o;
     palial_opts_default(&o);
     if (timings)
-        for (int i = 0; i < 72; i++) timings[i] = -1;
+        for (int i = 0; i < 108; i++) timings[i] = -1;
     for (int k = 0; k < 12; k++) {
         const int a = k / 6, c = k % 6;
         std::vector<int> idx;
@@ -338,7 +340,7 @@ int palial_gpu_batch_solve_autotune(int count, const int *ns, const int *algs, u
         prec12[k] = 0;
         if (idx.empty()) continue;
         double best = 1e30;
-        for (int prec = 0; prec < 2; prec++)
+        for (int prec = 0; prec < 3; prec++)
             for (int j = 0; j < 3; j++) {
                 const int bs = kCandidates[j];
                 if (bs > std::max(64, kClassEdges[c + 1])) continue;
@@ -362,7 +364,7 @@ int palial_gpu_batch_solve_autotune(int count, const int *ns, const int *algs, u
                     }
                     if (r > 0) t = std::min(t, res.seconds);
                 }
-                if (timings) timings[k * 6 + prec * 3 + j] = t < 1e30 ? t : -2;
+                if (timings) timings[k * 9 + prec * 3 + j] = t < 1e30 ? t : -2;
                 if (t < best) {
                     best = t;
                     bs12[k] = bs;

@@ -351,6 +351,7 @@ struct Solver {
     std::vector<SolveMat> mats;
     std::vector<double> anorm, bnorm, berr, tol, eta_prev;
     std::vector<int> iters, state;  // state: 0 active, 1 converged, 2 failed
+    std::vector<int> tc;            // 1: FP32 factorization with its updates on the tensor cores (BF16x3)
     cudaStream_t s;
     palial_status *st;
     double factor_s = 0;
@@ -395,7 +396,7 @@ struct Solver {
     // the synthetic batch: its FP64 pipe favours more, shorter tasks)
     int factor(const std::vector<int> &ms, bool f32) {
         if (ms.empty()) return PALIAL_OK;
-        std::vector<int> algs, ns, nbs, bss;
+        std::vector<int> algs, ns, nbs, bss, tcs;
         std::vector<void *> bufs;
         for (int m : ms) {
             algs.push_back(mats[m].alg);
@@ -403,6 +404,7 @@ struct Solver {
             nbs.push_back(mats[m].nb);
             bss.push_back(f32 ? mats[m].nb : 64);
             bufs.push_back(const_cast<void *>(mats[m].F));
+            tcs.push_back(tc[m]);
         }
         std::vector<int> flags(ms.size(), 0);
         palial_opts o;
@@ -410,7 +412,7 @@ struct Solver {
         palial_status s2;
         memset(&s2, 0, sizeof s2);
         const int rc = batched_run((int)ms.size(), algs.data(), ns.data(), nbs.data(), bss.data(), bufs.data(), f32,
-                                   flags.data(), &o, &s2, nullptr, s);
+                                   flags.data(), &o, &s2, nullptr, s, tcs.data());
         factor_s += s2.seconds;
         if (rc < 0) return set_status(st, rc, "batched factorization: %s", s2.message);
         for (size_t j = 0; j < ms.size(); j++)
@@ -528,7 +530,8 @@ int batched_solve_run(int count, const int *algs, const int *ns, const int *nbs,
     for (int i = 0; i < count; i++) {
         const int p = precs ? precs[i] : PALIAL_PREC_FP32;
         if ((algs[i] != 0 && algs[i] != 1) || ns[i] <= 0 || ns[i] > MAX_N || nbs[i] <= 0 || nbs[i] % 64 ||
-            ns[i] % nbs[i] || !dA[i] || !dB[i] || !dX[i] || (p != PALIAL_PREC_FP32 && p != PALIAL_PREC_FP64) ||
+            ns[i] % nbs[i] || !dA[i] || !dB[i] || !dX[i] ||
+            (p != PALIAL_PREC_FP32 && p != PALIAL_PREC_FP64 && p != PALIAL_PREC_BF16X3) ||
             (reinterpret_cast<uintptr_t>(dA[i]) & 15))
             return set_status(st, PALIAL_ERR_ARG, "matrix %d: alg %d n %d nb %d precision %d (n <= %d, nb | n, 64 | nb)",
                               i, algs[i], ns[i], nbs[i], p, MAX_N);
@@ -548,7 +551,7 @@ int batched_solve_run(int count, const int *algs, const int *ns, const int *nbs,
     size_t n32 = 0, n64 = 0, nr = 0;
     for (int i = 0; i < count; i++) {
         const size_t el = (size_t)ns[i] * ns[i];
-        const bool f32 = !precs || precs[i] == PALIAL_PREC_FP32;
+        const bool f32 = !precs || precs[i] != PALIAL_PREC_FP64;
         off[i] = f32 ? n32 : n64;
         (f32 ? n32 : n64) += round_up(el, 4);
         offr[i] = nr;
@@ -570,10 +573,12 @@ int batched_solve_run(int count, const int *algs, const int *ns, const int *nbs,
     sv.tol.resize(count);
     sv.iters.assign(count, 0);
     sv.state.assign(count, 0);
+    sv.tc.assign(count, 0);
     std::vector<int> all(count), m32, m64;
     std::iota(all.begin(), all.end(), 0);
     for (int i = 0; i < count; i++) {
-        const bool f32 = !precs || precs[i] == PALIAL_PREC_FP32;
+        const bool f32 = !precs || precs[i] != PALIAL_PREC_FP64;
+        sv.tc[i] = (precs && precs[i] == PALIAL_PREC_BF16X3) ? 1 : 0;
         SolveMat &m = sv.mats[i];
         m.A = dA[i];
         m.b = dB[i];

@@ -57,6 +57,7 @@ struct MatInfo {
         float *Af;
     };
     int n, nb, bs;
+    int tc;                     // FP32 scheduler: update tasks on the warp tensor cores (BF16x3)
 };
 
 struct TraceRec {
@@ -87,6 +88,7 @@ struct SchedParams {
     int *mat_status;            // FP32 batched run: per-matrix breakdown flags (else nullptr)
     float *Af, *Sf;             // FP32 scheduler on one matrix: factors and QR T factors
     float *scratch_f;           // FP32 scheduler: per-worker scratch (scratch_per_worker floats)
+    int tc;                     // FP32 QR: TSMQR's products on the warp tensor cores (BF16x3)
 };
 
 // Host: count of kernel launches made by the library (every launch wrapper calls this).

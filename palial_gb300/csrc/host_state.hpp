@@ -141,7 +141,8 @@ cudaError_t sched_enqueue(SchedCtx &c, const SchedParams &p, int nobj, int worke
 // tile-layout buffer, double (FP64 tasks) or float (FP32 tasks: f32 = true).  FP32 runs
 // report breakdowns per matrix in flags (count ints, host; 0 = none) instead of failing.
 int batched_run(int count, const int *algs, const int *ns, const int *nbs, const int *bss, void *const *bufs, bool f32,
-                int *flags, const palial_opts *opts, palial_status *st, double *completion_s, cudaStream_t s);
+                int *flags, const palial_opts *opts, palial_status *st, double *completion_s, cudaStream_t s,
+                const int *tcs = nullptr);  // tcs[i] = 1: FP32 updates of matrix i on the tensor cores
 
 #define PALIAL_CK(call, what)                                  \
     do {                                                       \

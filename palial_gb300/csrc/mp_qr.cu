@@ -76,12 +76,13 @@ int grid_of(long long elems) {
 
 // One FP32 scheduler launch of dag over W / S, synchronous; returns the device status code.
 int run_f32(SchedCtx &c, const std::shared_ptr<Dag> &dag, float *W, float *S, int workers, double timeout_s,
-            cudaStream_t s, palial_status *st, double *seconds) {
+            cudaStream_t s, palial_status *st, double *seconds, bool tc = false) {
     SchedParams p;
     int rc = sched_prepare(c, dag, nullptr, nullptr, workers, 0, timeout_s, p, st);
     if (rc) return rc;
     p.Af = W;
     p.Sf = S;
+    p.tc = tc ? 1 : 0;
     p.scratch_f = reinterpret_cast<float *>(p.scratch);  // sized in doubles: twice the floats used
     PALIAL_CK(cudaEventRecord(g.ev0, s), "event");
     PALIAL_CK(sched_enqueue(c, p, dag->nobj, workers, true, s, true), "FP32 scheduler");
@@ -153,7 +154,8 @@ extern "C" int palial_gpu_qr_solve_ir(int n, int nb, const double *dA, const dou
     }
     const std::shared_ptr<Dag> adag = it->second;
     double factor_s = 0, apply_s = 0;
-    rc = run_f32(q_fac, fdag, W, S, workers, o.timeout_s, s, st, &factor_s);
+    // opts.precision = PALIAL_PREC_BF16X3: TSMQR's two products with V on the tensor cores
+    rc = run_f32(q_fac, fdag, W, S, workers, o.timeout_s, s, st, &factor_s, o.precision == PALIAL_PREC_BF16X3);
     if (rc) return rc;
 
     // refinement from X = 0 (R = B)

@@ -170,7 +170,8 @@ cudaError_t sched_enqueue(SchedCtx &c, const SchedParams &p, int nobj, int worke
 }
 
 int batched_run(int count, const int *algs, const int *ns, const int *nbs, const int *bss, void *const *bufs, bool f32,
-                int *flags, const palial_opts *opts, palial_status *st, double *completion_s, cudaStream_t s) {
+                int *flags, const palial_opts *opts, palial_status *st, double *completion_s, cudaStream_t s,
+                const int *tcs) {
     palial_opts o;
     palial_opts_default(&o);
     if (opts) o = *opts;
@@ -214,6 +215,7 @@ int batched_run(int count, const int *algs, const int *ns, const int *nbs, const
         mats[i].n = ns[i];
         mats[i].nb = nbs[i];
         mats[i].bs = bss[i];
+        mats[i].tc = (f32 && tcs) ? tcs[i] : 0;
     }
     PALIAL_CK(lane.mats.ensure(sizeof(MatInfo) * count), "alloc matrix table");
     PALIAL_CK(cudaMemcpyAsync(lane.mats.ptr, mats.data(), sizeof(MatInfo) * count, cudaMemcpyHostToDevice, s), "upload");

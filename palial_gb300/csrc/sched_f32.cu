@@ -222,6 +222,7 @@ __device__ void run_task_batch(const SchedParams &p, const Worker &w, const Task
     const MatInfo mi = p.mats[t.mat];
     float *A = mi.Af;
     const int n = mi.n, nb = mi.nb, bs = mi.bs, ld = nb;
+    const bool tc = mi.tc != 0;  // the update tasks' products on the tensor cores (BF16x3)
     switch (t.type) {
         case T_POTRF: {
             const int bad = potrf_upper(w, fblock_ptr(A, n, nb, bs, t.k, t.k), bs, ld);
@@ -237,7 +238,11 @@ __device__ void run_task_batch(const SchedParams &p, const Worker &w, const Task
             const float *X = fblock_ptr(A, n, nb, bs, t.k, t.m);
             float *C = fblock_ptr(A, n, nb, bs, t.m, t.m);
             const int c0 = t.part * 64;
-            cta_gemm<true, false>(c0 + 64, 64, bs, -1.f, X, ld, X + (size_t)c0 * ld, ld, C + (size_t)c0 * ld, ld, w.gsm);
+            if (tc)
+                cta_gemm<true, false, false, true>(c0 + 64, 64, bs, -1.f, X, ld, X + (size_t)c0 * ld, ld, C + (size_t)c0 * ld,
+                                                   ld, w.gsm);
+            else
+                cta_gemm<true, false>(c0 + 64, 64, bs, -1.f, X, ld, X + (size_t)c0 * ld, ld, C + (size_t)c0 * ld, ld, w.gsm);
             break;
         }
         case T_GEMM_TN: {
@@ -245,7 +250,11 @@ __device__ void run_task_batch(const SchedParams &p, const Worker &w, const Task
             const float *Xb = fblock_ptr(A, n, nb, bs, t.k, t.m);
             float *C = fblock_ptr(A, n, nb, bs, t.n, t.m);
             const int c0 = t.part * 64;
-            cta_gemm<true, false>(bs, 64, bs, -1.f, Xa, ld, Xb + (size_t)c0 * ld, ld, C + (size_t)c0 * ld, ld, w.gsm);
+            if (tc)
+                cta_gemm<true, false, false, true>(bs, 64, bs, -1.f, Xa, ld, Xb + (size_t)c0 * ld, ld, C + (size_t)c0 * ld,
+                                                   ld, w.gsm);
+            else
+                cta_gemm<true, false>(bs, 64, bs, -1.f, Xa, ld, Xb + (size_t)c0 * ld, ld, C + (size_t)c0 * ld, ld, w.gsm);
             break;
         }
         case T_GETRF: {
@@ -265,7 +274,11 @@ __device__ void run_task_batch(const SchedParams &p, const Worker &w, const Task
             const float *Xb = fblock_ptr(A, n, nb, bs, t.k, t.n);
             float *C = fblock_ptr(A, n, nb, bs, t.m, t.n);
             const int c0 = t.part * 64;
-            cta_gemm<false, false>(bs, 64, bs, -1.f, Xa, ld, Xb + (size_t)c0 * ld, ld, C + (size_t)c0 * ld, ld, w.gsm);
+            if (tc)
+                cta_gemm<false, false, false, true>(bs, 64, bs, -1.f, Xa, ld, Xb + (size_t)c0 * ld, ld, C + (size_t)c0 * ld,
+                                                    ld, w.gsm);
+            else
+                cta_gemm<false, false>(bs, 64, bs, -1.f, Xa, ld, Xb + (size_t)c0 * ld, ld, C + (size_t)c0 * ld, ld, w.gsm);
             break;
         }
         default:
@@ -297,7 +310,7 @@ __device__ void run_task_qr(const SchedParams &p, const Worker &w, const Task &t
             const size_t off = (size_t)t.part * 64 * ld;
             qrt::tsmqr_strip(w.q, ftile_ptr(A, n, nb, t.k, t.n) + off, ftile_ptr(A, n, nb, t.m, t.n) + off,
                              ftile_ptr(A, n, nb, t.m, t.k), ftile_ptr(p.Sf, n, nb, t.m, t.k), nb, ld, wscr,
-                             wscr + (size_t)nb * 64);
+                             wscr + (size_t)nb * 64, p.tc != 0);
             break;
         }
         case T_TRSM_LUN:  // R X = Y on the extra tile column

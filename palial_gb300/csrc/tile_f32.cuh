@@ -3,6 +3,7 @@
 // FP64 routines of tile_f64.cuh; loads bypass L1 (tiles are written by other SMs).
 #pragma once
 #include "common.cuh"
+#include "tc_gemm.cuh"
 
 namespace palial {
 namespace f32 {
@@ -80,12 +81,56 @@ __device__ __forceinline__ void stage_store(float (*Xs)[SP], const float4 (&v)[2
 }
 
 // C[M x N] += alpha * op(A) op(B) (beta = 1), dims multiples of 64 / 32.  KEEP_LOWER leaves
-// the entries below C's diagonal unchanged (an upper-triangle update).  Ends synced.
-template <bool TA, bool TB, bool KEEP_LOWER = false>
+// the entries below C's diagonal unchanged (an upper-triangle update).  TC: the products on the
+// warp tensor cores in BF16x3 (tc_gemm.cuh) instead of FP32 FMAs.  Ends synced.
+template <bool TA, bool TB, bool KEEP_LOWER = false, bool TC = false>
 __device__ __forceinline__ void cta_gemm(int M, int N, int K, float alpha, const float *A, int lda, const float *B, int ldb, float *C,
                          int ldc, float *smem) {
     float (*As)[SP] = reinterpret_cast<float (*)[SP]>(smem);
     float (*Bs)[SP] = reinterpret_cast<float (*)[SP]>(smem + KC * SP);
+    if (TC) {
+        for (int i0 = 0; i0 < M; i0 += BM)
+            for (int j0 = 0; j0 < N; j0 += BM) {
+                tcg::Frag f;
+                tcg::zero(f);
+                float4 ra[2], rb[2];
+                if (K > 0) {
+                    stage_load<TA>(ra, A, lda, i0, 0);
+                    stage_load<!TB>(rb, B, ldb, j0, 0);
+                }
+                for (int p0 = 0; p0 < K; p0 += KC) {
+                    stage_store<TA>(As, ra);
+                    stage_store<!TB>(Bs, rb);
+                    __syncthreads();
+                    if (p0 + KC < K) {
+                        stage_load<TA>(ra, A, lda, i0, p0 + KC);
+                        stage_load<!TB>(rb, B, ldb, j0, p0 + KC);
+                    }
+                    tcg::bf16x3_chunk<SP>(&As[0][0], &Bs[0][0], f);
+                    __syncthreads();
+                }
+                float cv[4][4];
+#pragma unroll
+                for (int nt = 0; nt < 4; nt++)
+#pragma unroll
+                    for (int e = 0; e < 4; e++) {
+                        int r, c;
+                        tcg::frag_coord(nt, e, r, c);
+                        cv[nt][e] = __ldcg(C + (size_t)(i0 + r) + (size_t)(j0 + c) * ldc);
+                    }
+#pragma unroll
+                for (int nt = 0; nt < 4; nt++)
+#pragma unroll
+                    for (int e = 0; e < 4; e++) {
+                        int r, c;
+                        tcg::frag_coord(nt, e, r, c);
+                        if (KEEP_LOWER && i0 + r > j0 + c) continue;
+                        C[(size_t)(i0 + r) + (size_t)(j0 + c) * ldc] = fmaf(alpha, f.acc[nt][e], cv[nt][e]);
+                    }
+            }
+        __syncthreads();
+        return;
+    }
     // thread: rows 4*tr .. 4*tr+3 (tr = t % 16, so a warp's 16 row groups are contiguous in a
     // column of C) and columns 4*tc .. 4*tc+3 (tc = t / 16)
     const int tr = threadIdx.x & 15, tc = threadIdx.x >> 4;

@@ -12,6 +12,7 @@
 #include <cfloat>
 
 #include "common.cuh"
+#include "tc_gemm.cuh"
 
 namespace palial {
 namespace qrt {
@@ -84,9 +85,56 @@ __device__ __forceinline__ void stage(T (*Xs)[SP], const T *X, int ld, int i0, i
 // stored operands (the K range shrinks to where op(A) is nonzero).  Ends synced.
 template <class T, bool TA, bool TB, int MA = M_NONE, int MB = M_NONE>
 __device__ void cta_gemm(int M, int N, int K, T alpha, const T *A, int lda, const T *B, int ldb, T beta, T *C,
-                         int ldc, T *smem) {
+                         int ldc, T *smem, bool tc = false) {
     T(*As)[SP] = reinterpret_cast<T(*)[SP]>(smem);
     T(*Bs)[SP] = reinterpret_cast<T(*)[SP]>(smem + KC * SP);
+    if constexpr (sizeof(T) == 4) {
+        if (tc) {  // FP32 data: the products on the warp tensor cores in BF16x3 (tc_gemm.cuh)
+            for (int i0 = 0; i0 < M; i0 += BM) {
+                int klo = 0, khi = K;
+                if (MA == M_UPPER) {
+                    if (TA) khi = min(K, i0 + BM);
+                    else klo = i0;
+                } else if (MA == M_UNIT_LOWER) {
+                    if (TA) klo = i0;
+                    else khi = min(K, i0 + BM);
+                }
+                klo = (klo / KC) * KC;
+                for (int j0 = 0; j0 < N; j0 += BM) {
+                    tcg::Frag f;
+                    tcg::zero(f);
+                    for (int p0 = klo; p0 < khi; p0 += KC) {
+                        stage<T, TA, MA>(As, A, lda, i0, p0, K);
+                        stage<T, !TB, MB>(Bs, B, ldb, j0, p0, K);
+                        __syncthreads();
+                        tcg::bf16x3_chunk<SP>(reinterpret_cast<const float *>(&As[0][0]),
+                                              reinterpret_cast<const float *>(&Bs[0][0]), f);
+                        __syncthreads();
+                    }
+                    T cv[4][4];
+#pragma unroll
+                    for (int nt = 0; nt < 4; nt++)
+#pragma unroll
+                        for (int e = 0; e < 4; e++) {
+                            int r, c;
+                            tcg::frag_coord(nt, e, r, c);
+                            cv[nt][e] = beta == T(0) ? T(0) : ldg(C + (size_t)(i0 + r) + (size_t)(j0 + c) * ldc);
+                        }
+#pragma unroll
+                    for (int nt = 0; nt < 4; nt++)
+#pragma unroll
+                        for (int e = 0; e < 4; e++) {
+                            int r, c;
+                            tcg::frag_coord(nt, e, r, c);
+                            const T v = alpha * f.acc[nt][e];
+                            C[(size_t)(i0 + r) + (size_t)(j0 + c) * ldc] = beta == T(0) ? v : fma(beta, cv[nt][e], v);
+                        }
+                }
+            }
+            __syncthreads();
+            return;
+        }
+    }
     const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
     for (int i0 = 0; i0 < M; i0 += BM) {
         int klo = 0, khi = K;
@@ -458,14 +506,16 @@ __device__ void unmqr_strip(const QrSmem<T> &w, const T *V, const T *Tm, T *C, i
 }
 
 // TSMQR strip: W = A1 + V^T A2; W2 = T^T W; A1 -= W2; A2 -= V W2, on a 64-column strip.
+// tc: FP32 data only, the two products with the dense V on the warp tensor cores (BF16x3); the
+// triangular T product stays in FP32.
 template <class T>
 __device__ void tsmqr_strip(const QrSmem<T> &w, T *A1, T *A2, const T *V, const T *Tm, int nb, int ld, T *W,
-                            T *W2) {
+                            T *W2, bool tc = false) {
     cta_axpby<T>(nb, 64, T(1), A1, ld, T(0), W, nb);
-    cta_gemm<T, true, false>(nb, 64, nb, T(1), V, ld, A2, ld, T(1), W, nb, w.gsm);
+    cta_gemm<T, true, false>(nb, 64, nb, T(1), V, ld, A2, ld, T(1), W, nb, w.gsm, tc);
     cta_gemm<T, true, false, M_UPPER>(nb, 64, nb, T(1), Tm, ld, W, nb, T(0), W2, nb, w.gsm);
     cta_axpby<T>(nb, 64, T(-1), W2, nb, T(1), A1, ld);
-    cta_gemm<T, false, false>(nb, 64, nb, T(-1), V, ld, W2, nb, T(1), A2, ld, w.gsm);
+    cta_gemm<T, false, false>(nb, 64, nb, T(-1), V, ld, W2, nb, T(1), A2, ld, w.gsm, tc);
 }
 
 }  // namespace qrt

@@ -156,7 +156,7 @@ static int run_batch_solve(int count, unsigned long long seed, int autotune, int
         for (int k = 0; k < 12; k++)
             printf("%s{\"alg\": \"%s\", \"n\": [%d, %d], \"block\": %d, \"precision\": \"%s\"}", k ? ", " : "",
                    k < 6 ? "cholesky" : "lu", edges[k % 6], edges[k % 6 + 1], rep.bs_of_class[k],
-                   rep.prec_of_class[k] ? "fp32+ir" : "fp64");
+                   rep.prec_of_class[k] == 2 ? "bf16x3-update+ir" : rep.prec_of_class[k] ? "fp32+ir" : "fp64");
         printf("]}\n");
     }
     return rc ? 1 : 0;

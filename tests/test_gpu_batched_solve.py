@@ -160,6 +160,26 @@ def test_synthetic_batched_solve_split_over_two_ranks():
         assert r["max_iters"] >= 1 and all(p == 1 for p in r["prec_of_class"])
 
 
+def test_bf16x3_update_form_reaches_fp64_target():
+    """The batched "BF16-update" form: FP32 storage, the SYRK / GEMM update tasks' products on the
+    warp tensor cores as BF16x3, FP64 refinement (FP64 fallback kept).  Every matrix reaches the
+    FP64-level target, and matches the FP32 form's solution within the refinement's reach."""
+    rng = np.random.default_rng(11)
+    sizes, nbs, algs = [512, 384, 256, 192], [128, 128, 64, 64], [0, 1, 0, 1]
+    mats = []
+    for a, m in zip(algs, sizes):
+        q = rng.uniform(-1, 1, (m, m))
+        mats.append(q @ q.T + m * np.eye(m) if a == 0 else q + m * np.eye(m))
+    d = Dev(mats, nbs)
+    st, iters, berr = B.solve(algs, sizes, nbs, d.ptrs, d.bptrs, d.xptrs, precs=["bf16x3"] * 4)
+    assert st.code == 0, st.message
+    for i, m in enumerate(mats):
+        ref = np.linalg.solve(m, d.b[i])
+        assert berr[i] <= 1e-14 * sizes[i], (i, berr[i])
+        assert np.linalg.norm(d.x(i) - ref) <= 1e-10 * np.linalg.norm(ref), i
+    print("bf16x3 update form: refinement steps", iters.tolist(), "backward errors", berr.tolist())
+
+
 def test_solve_autotune_keeps_the_fastest_converging_choice():
     r = B.solve_synthetic(24, seed=4, autotune=True, reps=1)
     assert r["rc"] == 0 and r["not_converged"] == 0
@@ -167,7 +187,7 @@ def test_solve_autotune_keeps_the_fastest_converging_choice():
     present = {(int(a), B.size_class(int(n))) for n, a in zip(ns, algs)}
     for a, c in present:
         k = a * 6 + c
-        times = r["autotune_s"][k * 6:(k + 1) * 6]
+        times = r["autotune_s"][k * 9:(k + 1) * 9]  # [precision 0, 1, 2][block 64, 128, 256]
         ok = [t for t in times if t >= 0]
         assert ok, (a, c)
         chosen = r["prec_of_class"][k] * 3 + B.CANDIDATE_BS.index(r["bs_of_class"][k])

@@ -39,6 +39,24 @@ def test_fp32_qr_refined_to_fp64_backward_error(n, nb, nrhs):
     assert np.linalg.norm(x - xr) <= 1e-8 * np.linalg.norm(xr)
 
 
+@pytest.mark.parametrize("n,nb,nrhs", [(1024, 256, 4), (2048, 512, 16)])
+def test_tensor_core_tsmqr_refined_to_fp64_backward_error(n, nb, nrhs):
+    """TSMQR's products with V on the warp tensor cores (BF16x3, precision="bf16x3"): the FP32
+    factors are a little less accurate, the refinement still reaches the FP64-level target from
+    them without the FP64 fallback, and the solution matches numpy's."""
+    rng = np.random.default_rng(n + 1)
+    a = rng.uniform(-1, 1, (n, n))
+    b = rng.uniform(-1, 1, (n, nrhs))
+    st, x = _solve(a, b, nb, precision="bf16x3")
+    assert st.code == 0 and st.precision_used == 5, st.message
+    assert st.backward_error <= 1e-14 * n and _berr(a, x, b) <= 1e-14 * n
+    xr = np.linalg.solve(a, b)
+    assert np.linalg.norm(x - xr) <= 1e-8 * np.linalg.norm(xr)
+    st32, _ = _solve(a, b, nb)
+    print(f"n={n}: tensor-core TSMQR {st.ir_iters} refinement steps, factor {st.factor_seconds:.4f} s; "
+          f"FP32 {st32.ir_iters} steps, factor {st32.factor_seconds:.4f} s")
+
+
 def test_ill_conditioned_system_falls_back_to_fp64_qr():
     n, nb = 512, 128
     rng = np.random.default_rng(9)
