@@ -601,8 +601,9 @@ def every_kernel_once(P, torch, n: int) -> dict:
 def run_qr_mixed(args, P, torch) -> None:
     """QR solves of A X = B (A uniform [-1, 1), seed 1; 16 right-hand sides) at N = 16384 and
     32768: the mixed-precision QR (FP32 tile QR + FP64 refinement) with NB = 512 and 256 (its
-    single-CTA TSQRT chain shortens with the tile) against the FP64 QR solve of the same system
-    at NB = 512; whole calls on device buffers, TFLOP/s from 4N^3/3."""
+    single-CTA TSQRT chain shortens with the tile), the same with its TSMQR products on the
+    tensor cores (precision bf16x3), against the FP64 QR solve of the same system at NB = 512;
+    whole calls on device buffers, TFLOP/s from 4N^3/3."""
     nrhs = 16
     for n in (16384, 32768):
         b = torch.empty(n * nrhs, dtype=torch.float64, device="cuda")
@@ -618,6 +619,13 @@ def run_qr_mixed(args, P, torch) -> None:
                     "backward_error": st.backward_error,
                     "tflops_fp64_equiv": 4.0 * n ** 3 / 3.0 / st.seconds * 1e-12,
                     "precision_used": "fp32" if st.precision_used == 5 else "fp64", "message": st.message.decode()}
+            x.zero_()
+            tc = P.qr_solve_ir(da.data_ptr(), n, nb, b.data_ptr(), x.data_ptr(), nrhs, allow_not_converged=True,
+                               precision="bf16x3")
+            line["tensor_core_tsmqr"] = {"converged": tc.code == 0, "seconds": tc.seconds,
+                                         "factor_seconds": tc.factor_seconds, "ir_iters": tc.ir_iters,
+                                         "backward_error": tc.backward_error,
+                                         "precision_used": {3: "bf16x3", 5: "fp32"}.get(tc.precision_used, "fp64")}
             if nb == NB:
                 x.zero_()
                 s64 = P.qr_solve(da.data_ptr(), n, n, NB, b.data_ptr(), x.data_ptr(), nrhs)

@@ -212,7 +212,7 @@ int palial_gpu_qr_solve(int rows, int cols, int nb, const double *dA, const doub
  * that does not halve the error per step (or exceeds
  * opts->ir_max_iter, 0 = 30) hands the system to palial_gpu_qr_solve (FP64).  status:
  * ir_iters, backward_error, factor_seconds, precision_used = the precision that produced the
- * result (PALIAL_PREC_FP32 or PALIAL_PREC_FP64). */
+ * result (PALIAL_PREC_FP32, PALIAL_PREC_BF16X3 for the tensor-core form, or PALIAL_PREC_FP64). */
 int palial_gpu_qr_solve_ir(int n, int nb, const double *dA, const double *dB, double *dX, int nrhs,
                            const palial_opts *opts, palial_status *st, void *stream);
 /* Same with host buffers (A in tile layout, B and X column-major, resid optional). */

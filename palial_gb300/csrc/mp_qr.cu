@@ -197,7 +197,7 @@ extern "C" int palial_gpu_qr_solve_ir(int n, int nb, const double *dA, const dou
         PALIAL_CK(mps_residual(dA, n, nb, dX, dB, R, nrhs, nullptr, s), "residual");
         PALIAL_CK(mps_colmax(dX, n, nrhs, xmax_d, s), "norm X");
     }
-    int rung = PALIAL_PREC_FP32;
+    int rung = o.precision == PALIAL_PREC_BF16X3 ? PALIAL_PREC_BF16X3 : PALIAL_PREC_FP32;
     if (!converged) {
         // the FP64 QR solve, then one FP64 residual check
         palial_status s2;
@@ -234,5 +234,6 @@ extern "C" int palial_gpu_qr_solve_ir(int n, int nb, const double *dA, const dou
     if (!converged)
         return set_status(st, PALIAL_ERR_NOT_CONVERGED, "QR refinement stopped at %.3g (tolerance %.3g)", worst, tol);
     return set_status(st, PALIAL_OK, "%s QR, %d refinement steps (%.3f s applying Q^T and R^-1)",
-                      rung == PALIAL_PREC_FP32 ? "FP32" : "FP64", steps, apply_s);
+                      rung == PALIAL_PREC_FP64 ? "FP64" : rung == PALIAL_PREC_FP32 ? "FP32" : "FP32 (BF16x3 TSMQR)",
+                      steps, apply_s);
 }

@@ -48,7 +48,7 @@ def test_tensor_core_tsmqr_refined_to_fp64_backward_error(n, nb, nrhs):
     a = rng.uniform(-1, 1, (n, n))
     b = rng.uniform(-1, 1, (n, nrhs))
     st, x = _solve(a, b, nb, precision="bf16x3")
-    assert st.code == 0 and st.precision_used == 5, st.message
+    assert st.code == 0 and st.precision_used == 3, st.message  # the tensor-core form sufficed
     assert st.backward_error <= 1e-14 * n and _berr(a, x, b) <= 1e-14 * n
     xr = np.linalg.solve(a, b)
     assert np.linalg.norm(x - xr) <= 1e-8 * np.linalg.norm(xr)
