@@ -17,7 +17,8 @@ The JSON line also carries:
   fp64_tiled    the plain FP64 tiled factorization (persistent scheduler, FP64 DFMA) of the
                 same matrix: its TFLOP/s and the mixed/FP64 speed-up;
   e2e           the same solve through the host-buffer C ABI (palial_gpu_solve_ir_host on
-                pinned host memory: A and B copied in, X copied out, every step);
+                pinned host memory: A's upper triangle (what Cholesky reads) and B copied in,
+                X copied out, every step);
   e2e_pageable  the same from a pageable (malloc'd) host buffer, as the reference's caller has;
   kappa         config 3 at N = 32768: Cholesky at kappa = 1e6 and 1e10, LU at 1e6: the
                 precision ladder's solve (rung used, refinement and GMRES steps, FP64-checked
@@ -859,6 +860,10 @@ def main() -> None:
     page_sec = sum(page_times) / len(page_times)
     del page
 
+    # the host-buffer Cholesky copies the upper triangle's tiles of A (the triangle the
+    # factorization reads; the lower one is written on the device from it) and B
+    mt = n // NB
+    h2d_bytes = 8 * NB * NB * mt * (mt + 1) // 2 + 8 * n * nrhs
     if rank == 0:
         cpu = None
         if not args.no_cpu:
@@ -876,12 +881,12 @@ def main() -> None:
             "converged": converged, "backward_error": eta, "backward_error_fp64_check": eta_fp64,
             "ir_iters": launches,
             "fp64_tiled": fp64,
-            "e2e": {"value": e2e_value, "unit": "TFLOP/s", "h2d_bytes_per_step": 8 * n * n + 8 * n * nrhs,
+            "e2e": {"value": e2e_value, "unit": "TFLOP/s", "h2d_bytes_per_step": h2d_bytes,
                     "d2h_bytes_per_step": 8 * n * nrhs, "step_seconds": [round(t, 5) for t in e2e_times],
                     "host_buffer": "pinned (page-locked) A",
                     "host_link_gbs_samples": link},
             "e2e_pageable": {"value": world * flops(n) / page_sec * 1e-12, "unit": "TFLOP/s",
-                             "h2d_bytes_per_step": 8 * n * n + 8 * n * nrhs, "d2h_bytes_per_step": 8 * n * nrhs,
+                             "h2d_bytes_per_step": h2d_bytes, "d2h_bytes_per_step": 8 * n * nrhs,
                              "step_seconds": [round(t, 5) for t in page_times],
                              "host_buffer": "pageable A (numpy / malloc), as the reference's caller"},
             **extra,

@@ -153,6 +153,8 @@ int palial_gpu_factor_dev(int alg, double *dA, double *dS, int n, int nb, const 
  * their error bounds are summed and convergence requires backward error + bound <= tol (else
  * the residual is recomputed in full).  opts->reserved[4] = 3 computes every residual in
  * full instead.  The status message counts the update-form residuals.
+ * With BF16x3 updates the row / column panels' block products also run as BF16x3 on the warp
+ * tensor cores (opts->reserved[5] bit 3 keeps them in FP32 FMAs).
  * Opt-in stabilised LU (alg = PALIAL_ALG_LU, mixed precisions): opts->reserved[6] = 1 factors
  * the random-butterfly transform U^T A V (depth-2 recursive butterflies, Parker 1995) without
  * pivoting instead of A, refines against A (seed: opts->reserved[7], 0 = 1).  PALIAL_PREC_AUTO
@@ -164,7 +166,10 @@ int palial_gpu_factor_dev(int alg, double *dA, double *dS, int n, int nb, const 
 int palial_gpu_solve_ir(int alg, const double *dA, int n, int nb, const double *dB, double *dX,
                         int nrhs, const palial_opts *opts, palial_status *st, void *stream);
 /* Same with host buffers: A in the reference's tile layout (descriptor), B and X n x nrhs
- * column-major in host memory; includes the host<->device copies. */
+ * column-major in host memory; includes the host<->device copies.  Cholesky (N a multiple of
+ * NB, NB a multiple of 32) reads only the upper triangle of A, as the factorization does: the
+ * lower triangle is never copied, and the residuals use the symmetric matrix the upper
+ * triangle defines (the device-buffer entry point reads all of A for its residuals). */
 int palial_gpu_solve_ir_host(int alg, const palial_desc *A, const double *B, double *X, int nrhs,
                              const palial_opts *opts, palial_status *st);
 /* R = B - A X (B may be NULL: R = A X) on device buffers, A an FP64 tile matrix, X, B, R
@@ -190,6 +195,13 @@ int palial_gpu_mp_update_step(int alg, int precision, float *dW, int n, int nb, 
  * C traffic).  Both give the same bits.
  * Returns the previous setting (PALIAL_ERR_ARG for an unknown kind). */
 int palial_gpu_set_update_kernel(int kind);
+/* SMs (0..64) the mixed factorization's rest-of-trailing-update launches leave free for the
+ * critical chain's kernels on the high-priority stream (the tile-run kernel then launches at
+ * most SMs - sms CTAs with longer runs), in the steps whose trailing matrix has fewer than
+ * below_rows tile rows (0: every step).  Default 24 SMs in every step.  Same bits for every
+ * setting.  Returns the previous number of SMs (PALIAL_ERR_ARG for sms outside 0..64 or
+ * below_rows < 0). */
+int palial_gpu_set_update_reserve(int sms, int below_rows);
 
 /* ---- linear solve and least squares through the tile QR (no reference counterpart) -------
  * A: rows x cols FP64 tile matrix on the device (rows >= cols, both multiples of nb, nb a

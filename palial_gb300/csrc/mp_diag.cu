@@ -31,8 +31,14 @@ constexpr int MT = 8;     // micro-tile edge
 constexpr int PP = 65;    // pitch of the staged panel columns
 
 __host__ __device__ constexpr int chunk_k(int nb) { return nb <= 512 ? 32 : 16; }
-// shared memory (floats): Ds[64][65] + two staged chunks of chunk_k x (nb - 64)
-__host__ __device__ constexpr int smem_floats(int nb) { return 64 * DP + 2 * chunk_k(nb) * (nb - 64) + 64; }
+// staging area after Ds (floats): two chunks of chunk_k x (nb - 64) for the trailing update, and
+// for nb <= 512 room for the whole panel (nb - 64 columns at pitch PP) so that its columns are
+// solved in one pass
+__host__ __device__ constexpr int stage_floats(int nb) {
+    return (nb <= 512 && (nb - 64) * PP > 2 * chunk_k(nb) * (nb - 64)) ? (nb - 64) * PP : 2 * chunk_k(nb) * (nb - 64);
+}
+// shared memory (floats): Ds[64][65] + the staging area + a flag word
+__host__ __device__ constexpr int smem_floats(int nb) { return 64 * DP + stage_floats(nb) + 64; }
 
 // ---- 64 x 64 diagonal block in shared memory ---------------------------------------------
 // Ds[c][r] = A(r, c).  Blocked by 16: the 16 x 16 diagonal block is factored by warp 0 in
@@ -41,34 +47,43 @@ __host__ __device__ constexpr int smem_floats(int nb) { return 64 * DP + 2 * chu
 // threads (thread t: column q = t / 8, rows i = t % 8 + 8 j).
 constexpr unsigned FULL = 0xffffffffu;
 
-// Cholesky of the 16 x 16 block at (c0, c0) by lanes 0..15 of warp 0 in shared memory (lane l
-// updates column c0 + l; warp-level syncs only).  Returns the first failing pivot or -1
-// (warp-uniform).
-__device__ __forceinline__ int chol16_warp(float (*Ds)[DP], int c0) {
-    const int l = threadIdx.x & 31;
-    float *col = &Ds[c0 + (l & 15)][c0];
-    for (int p = 0; p < 16; p++) {
-        const float d = Ds[c0 + p][c0 + p];
-        if (!(d > 0.f)) return p;
+// Cholesky of the 16 x 16 block at (c0, c0) by warp 0: lane l < 16 keeps column c0 + l in
+// registers (rows c0 .. c0 + 15); the pivot and the factor row U(p, .) travel by shuffles.  The
+// arithmetic per entry is that of a shared-memory sweep: U(p, l) = a(p, l) * rsqrt(d), U(p, p) =
+// d * rsqrt(d), a(i, l) = fma(-U(p, i), U(p, l), a(i, l)) for p < i <= l.  The pivot steps are
+// template-unrolled so that the column stays in registers.
+template <int P>
+__device__ __forceinline__ void chol16_pivot(float (&c)[16], int lc, int &fail) {
+    if constexpr (P < 16) {
+        const float d = __shfl_sync(FULL, c[P], P);
+        if (!(d > 0.f) && fail < 0) fail = P;
         const float ri = rsqrtf(d);
-        if (l > p && l < 16) col[p] *= ri;  // U(p, l)
-        __syncwarp();
-        if (l == p) col[p] = d * ri;
-        if (l > p && l < 16) {
-            const float u = col[p];
-            float rv[16], cv[16];
+        c[P] = lc > P ? c[P] * ri : (lc == P ? d * ri : c[P]);
+        const float u = c[P];
 #pragma unroll
-            for (int i = 0; i < 16; i++) {
-                rv[i] = Ds[c0 + i][c0 + p];  // U(p, i)
-                cv[i] = col[i];
-            }
-#pragma unroll
-            for (int i = 0; i < 16; i++)
-                if (i > p && i <= l) col[i] = fmaf(-rv[i], u, cv[i]);
+        for (int i = P + 1; i < 16; i++) {
+            const float upi = __shfl_sync(FULL, c[P], i);  // U(P, i) from lane i
+            if (i <= lc) c[i] = fmaf(-upi, u, c[i]);
         }
-        __syncwarp();
+        chol16_pivot<P + 1>(c, lc, fail);
     }
-    return -1;
+}
+
+// Returns the first failing pivot or -1 (warp-uniform).
+__device__ __forceinline__ int chol16_warp(float (*Ds)[DP], int c0) {
+    const int l = threadIdx.x & 31, lc = l & 15;
+    float *col = &Ds[c0 + lc][c0];
+    float c[16];
+#pragma unroll
+    for (int i = 0; i < 16; i++) c[i] = col[i];
+    int fail = -1;
+    chol16_pivot<0>(c, lc, fail);
+    if (l < 16) {
+#pragma unroll
+        for (int i = 0; i < 16; i++) col[i] = c[i];
+    }
+    __syncwarp();
+    return fail;
 }
 
 // No-pivot LU of the 16 x 16 block at (c0, c0) by lanes 0..15 of warp 0 in shared memory,
@@ -364,7 +379,7 @@ __global__ void __launch_bounds__(NT, 1) diag_factor_kernel(float *T, int nb, in
     const int kc = chunk_k(nb);
     float *As = smem + 64 * DP;
     float *Bs = As + (size_t)kc * (nb - 64);
-    int *sflag = reinterpret_cast<int *>(Bs + (size_t)kc * (nb - 64));
+    int *sflag = reinterpret_cast<int *>(As + stage_floats(nb));
     if (ld_volatile(status + ST_CODE) != 0) return;
     if (threadIdx.x == 0) status[6] = k;  // current step (error reports of later kernels)
     int zero = 0;
@@ -403,19 +418,43 @@ __global__ void __launch_bounds__(NT, 1) diag_factor_kernel(float *T, int nb, in
         // solves one column, Ps[c][i] with an odd pitch so the threads' columns do not share banks)
         {
             float *Ps = As;  // the trailing update's chunk space is free here
-            const int cwmax = (2 * kc * (nb - 64)) / PP;
+            const int cwmax = stage_floats(nb) / PP;
             for (int c0 = 0; c0 < m; c0 += cwmax) {
                 const int cw = min(cwmax, m - c0);
-                for (int e = threadIdx.x; e < cw * 64; e += NT)
-                    Ps[(e >> 6) * PP + (e & 63)] = A12[(e & 63) + (size_t)(c0 + (e >> 6)) * ld];
+                // 16-byte loads, four per thread in flight before the shared stores (the panel
+                // comes from L2: one latency per batch instead of one per element)
+                const int nv = cw * 16;  // float4 per 64-row column: 16
+                for (int e0 = threadIdx.x; e0 < nv; e0 += 4 * NT) {
+                    float4 v[4];
+#pragma unroll
+                    for (int u = 0; u < 4; u++) {
+                        const int e = e0 + u * NT;
+                        if (e < nv)
+                            v[u] = *reinterpret_cast<const float4 *>(A12 + 4 * (e & 15) + (size_t)(c0 + (e >> 4)) * ld);
+                    }
+#pragma unroll
+                    for (int u = 0; u < 4; u++) {
+                        const int e = e0 + u * NT;
+                        if (e < nv) {
+                            float *d = Ps + (e >> 4) * PP + 4 * (e & 15);
+                            d[0] = v[u].x;
+                            d[1] = v[u].y;
+                            d[2] = v[u].z;
+                            d[3] = v[u].w;
+                        }
+                    }
+                }
                 __syncthreads();
                 for (int c = threadIdx.x; c < cw; c += NT) {
                     if (ALG == 0) solve_vec<0>(Ds, Ps + c * PP, 1);
                     else solve_vec<1>(Ds, Ps + c * PP, 1);
                 }
                 __syncthreads();
-                for (int e = threadIdx.x; e < cw * 64; e += NT)
-                    A12[(e & 63) + (size_t)(c0 + (e >> 6)) * ld] = Ps[(e >> 6) * PP + (e & 63)];
+                for (int e = threadIdx.x; e < nv; e += NT) {
+                    const float *d = Ps + (e >> 4) * PP + 4 * (e & 15);
+                    *reinterpret_cast<float4 *>(A12 + 4 * (e & 15) + (size_t)(c0 + (e >> 4)) * ld) =
+                        make_float4(d[0], d[1], d[2], d[3]);
+                }
                 __syncthreads();
             }
         }
@@ -430,13 +469,25 @@ __global__ void __launch_bounds__(NT, 1) diag_factor_kernel(float *T, int nb, in
             // 4 consecutive kk of one column (float4) and a warp covers 32 consecutive columns,
             // so the shared stores of a warp hit 32 different banks
             auto stage = [&](int k0) {
-                for (int e = threadIdx.x; e < (kc / 4) * m; e += NT) {
-                    const int i = e % m, kq = 4 * (e / m);
-                    const float4 v = *reinterpret_cast<const float4 *>(A12 + (k0 + kq) + (size_t)i * ld);
-                    As[(size_t)(kq + 0) * m + i] = v.x;
-                    As[(size_t)(kq + 1) * m + i] = v.y;
-                    As[(size_t)(kq + 2) * m + i] = v.z;
-                    As[(size_t)(kq + 3) * m + i] = v.w;
+                const int nv = (kc / 4) * m;
+                for (int e0 = threadIdx.x; e0 < nv; e0 += 4 * NT) {
+                    float4 v[4];  // four loads in flight per thread
+#pragma unroll
+                    for (int u = 0; u < 4; u++) {
+                        const int e = e0 + u * NT;
+                        if (e < nv) v[u] = *reinterpret_cast<const float4 *>(A12 + (k0 + 4 * (e / m)) + (size_t)(e % m) * ld);
+                    }
+#pragma unroll
+                    for (int u = 0; u < 4; u++) {
+                        const int e = e0 + u * NT;
+                        if (e < nv) {
+                            const int i = e % m, kq = 4 * (e / m);
+                            As[(size_t)(kq + 0) * m + i] = v[u].x;
+                            As[(size_t)(kq + 1) * m + i] = v[u].y;
+                            As[(size_t)(kq + 2) * m + i] = v[u].z;
+                            As[(size_t)(kq + 3) * m + i] = v[u].w;
+                        }
+                    }
                 }
             };
             trailing<true>(C, ld, m, kc, As, As, stage);

@@ -43,9 +43,10 @@ cudaError_t mps_residual_df(const double *A, int n, int nb, const double *X, con
 cudaError_t mps_residual_update(const double *A, int n, int nb, const double *D, const double *colmax, double *R,
                                 int nrhs, int sigma, float *Ds, int *tau, cudaStream_t s);
 cudaError_t mps_tile_to_f64(const float *w, double *d, int nb, cudaStream_t s);
+cudaError_t mps_mirror_upper(double *A, int n, int nb, cudaStream_t s);
 cudaError_t mps_tile_to_f32(const double *d, float *w, int nb, int upper_only, cudaStream_t s);
 cudaError_t mps_panel_trsm(float *W, int n, int nb, int k, int kind, const float *binv, cudaStream_t s,
-                           void *ph = nullptr, void *pl = nullptr, int t0 = 0, int count = -1);
+                           void *ph = nullptr, void *pl = nullptr, int t0 = 0, int count = -1, bool tc = false);
 cudaError_t mps_block_inverse(const float *W, int n, int nb, int k, int factors, float *binv, cudaStream_t s,
                               int blocks = 0);
 cudaError_t mps_residual(const double *A, int n, int nb, const double *X, const double *B, double *R, int nrhs,
@@ -75,6 +76,7 @@ cudaError_t launch_gen_dense(double *X, long long rows, int cols, uint64_t seed,
 cudaError_t launch_sumsq(const double *X, long long len, double *partial, int blocks, cudaStream_t s);
 void mp_release();
 int set_update_kernel(int kind);
+int set_update_reserve(int sms, int below_rows);
 cudaError_t mrd_residual(const double *A, int n, int nb, const double *X, const double *colmax, const double *B,
                          double *R, int nrhs, int sigma, uint32_t *Xd, int *tau, double *amax, cudaStream_t s);
 }  // namespace palial
@@ -101,6 +103,58 @@ bool ir_trace() {
     }();
     return on;
 }
+
+// PALIAL_FACTOR_TRACE=1: the device times at which the mixed factorization's three streams pass
+// the marks of each step (ms from the start), one line per step on stderr after the
+// factorization (diagnostics; timing events on every mark).
+struct FactorTrace {
+    enum { DIAG0, DIAG1, BINV, FIRST, PAIR, REST_PANEL, ROW0, ROW1, REST0, REST1, NMARK };
+    bool on = false;
+    cudaEvent_t t0 = nullptr;
+    std::vector<cudaEvent_t> pool;
+    std::vector<std::pair<int, int>> tags;  // (step, mark) of pool[i]
+    size_t used = 0;
+    cudaError_t begin(cudaStream_t s) {
+        static const bool env = [] {
+            const char *v = std::getenv("PALIAL_FACTOR_TRACE");
+            return v && v[0] == '1';
+        }();
+        on = env;
+        used = 0;
+        tags.clear();
+        if (!on) return cudaSuccess;
+        cudaError_t e = t0 ? cudaSuccess : cudaEventCreate(&t0);
+        return e == cudaSuccess ? cudaEventRecord(t0, s) : e;
+    }
+    cudaError_t mark(cudaStream_t q, int k, int m) {
+        if (!on) return cudaSuccess;
+        if (used == pool.size()) {
+            pool.push_back(nullptr);
+            const cudaError_t e = cudaEventCreate(&pool.back());
+            if (e != cudaSuccess) return e;
+        }
+        tags.push_back({k, m});
+        return cudaEventRecord(pool[used++], q);
+    }
+    void print(int mt) {
+        if (!on) return;
+        std::vector<float> t((size_t)mt * NMARK, -1.f);
+        for (size_t i = 0; i < used; i++) {
+            float ms = -1.f;
+            if (cudaEventElapsedTime(&ms, t0, pool[i]) == cudaSuccess) t[(size_t)tags[i].first * NMARK + tags[i].second] = ms;
+        }
+        std::fprintf(stderr, "[factor] k: diag0 diag1 binv first pair | rest_panel row0 row1 | rest0 rest1 (ms)\n");
+        for (int k = 0; k < mt; k++) {
+            const float *r = &t[(size_t)k * NMARK];
+            std::fprintf(stderr, "[factor] %d: %.3f %.3f %.3f %.3f %.3f | %.3f %.3f %.3f | %.3f %.3f\n", k, r[0], r[1], r[2],
+                         r[3], r[4], r[5], r[6], r[7], r[8], r[9]);
+        }
+    }
+} g_ftrace;
+
+// opts.reserved[5] bit 3 of the running solve: the panels of a BF16x3 factorization in FP32 FMAs
+// instead of BF16x3 on the tensor cores.
+bool g_panel_fp32 = false;
 
 // Update-kernel mode (mp_gemm.cu) of a PALIAL_PREC_* precision: 0 bf16, 1 fp8, 2 bf16x3, 3 tf32x3.
 int update_mode(int prec) {
@@ -285,6 +339,7 @@ int mp_factor(int alg, int prec, float *W, int n, int nb, cudaStream_t s, palial
     PALIAL_CK(lookahead_init(), "lookahead streams");
     PALIAL_CK(cudaMemsetAsync(g.diag.status.ptr, 0, sizeof(int) * ST_NSLOTS, s), "clear status");
     PALIAL_CK(cudaEventRecord(g_la.start, s), "event");
+    PALIAL_CK(g_ftrace.begin(s), "trace");
     cudaStream_t hi = g_la.hi, mid = g_la.mid, lo = g_la.lo;
     PALIAL_CK(cudaStreamWaitEvent(hi, g_la.start, 0), "event");
     PALIAL_CK(cudaStreamWaitEvent(mid, g_la.start, 0), "event");
@@ -303,11 +358,16 @@ int mp_factor(int alg, int prec, float *W, int n, int nb, cudaStream_t s, palial
     // BF16 / BF16x3: the row-panel solve writes the packed operand with its results; FP8 needs
     // per-tile scales first and TF32x3 FP32 containers, so they pack in a separate pass
     const bool fused = mode == 0 || mode == 2;
+    // BF16x3 updates: the panels' block products on the warp tensor cores in BF16x3 too
+    // (opts.reserved[5] bit 3 keeps them in FP32)
+    const bool panel_tc = mode == 2 && !g_panel_fp32;
     const int upper = alg == 0 ? 1 : 0;
     for (int k = 0; k < mt; k++) {
         float *binv = mb.binv.as<float>() + (size_t)(k & 1) * 2 * nb * 64;
         // the diagonal tile in FP32 (mp_diag.cu)
+        PALIAL_CK(g_ftrace.mark(hi, k, FactorTrace::DIAG0), "trace");
         PALIAL_CK(mpd_factor_tile(alg, W, n, nb, k, status, binv, hi), "diag factor");
+        PALIAL_CK(g_ftrace.mark(hi, k, FactorTrace::DIAG1), "trace");
         if (k == mt - 1) break;
         const int ntr = mt - k - 1;
         const int par = arrive ? k : (k & 1);
@@ -321,16 +381,19 @@ int mp_factor(int alg, int prec, float *W, int n, int nb, cudaStream_t s, palial
         }
         PALIAL_CK(mps_block_inverse(W, n, nb, k, alg == 0 ? 1 : 2, binv, hi), "diagonal block inverses");
         PALIAL_CK(cudaEventRecord(g_la.binv, hi), "event");
+        PALIAL_CK(g_ftrace.mark(hi, k, FactorTrace::BINV), "trace");
         // panel tiles [t0, t0 + cnt) on stream q, packed
         const auto panel_part = [&](cudaStream_t q, int t0, int cnt) -> int {
             if (alg == 0) {
-                PALIAL_CK(mps_panel_trsm(W, n, nb, k, 0, binv, q, fused ? ah : nullptr, fused ? al : nullptr, t0, cnt),
+                PALIAL_CK(mps_panel_trsm(W, n, nb, k, 0, binv, q, fused ? ah : nullptr, fused ? al : nullptr, t0, cnt,
+                                         panel_tc),
                           "panel trsm");
                 if (!fused) PALIAL_CK(mp_pack_rows(mode, W, n, nb, k, ah, al, sa, q, t0, cnt), "pack");
             } else {
-                PALIAL_CK(mps_panel_trsm(W, n, nb, k, 1, binv, q, fused ? bh : nullptr, fused ? bl : nullptr, t0, cnt),
+                PALIAL_CK(mps_panel_trsm(W, n, nb, k, 1, binv, q, fused ? bh : nullptr, fused ? bl : nullptr, t0, cnt,
+                                         panel_tc),
                           "row panel trsm");
-                PALIAL_CK(mps_panel_trsm(W, n, nb, k, 2, binv, q, nullptr, nullptr, t0, cnt), "column panel trsm");
+                PALIAL_CK(mps_panel_trsm(W, n, nb, k, 2, binv, q, nullptr, nullptr, t0, cnt, panel_tc), "column panel trsm");
                 PALIAL_CK(mp_pack_cols(mode, W, n, nb, k, ah, al, sa, q, t0, cnt), "pack L");
                 if (!fused) PALIAL_CK(mp_pack_rows(mode, W, n, nb, k, bh, bl, sb, q, t0, cnt), "pack U");
             }
@@ -342,22 +405,28 @@ int mp_factor(int alg, int prec, float *W, int n, int nb, cudaStream_t s, palial
         int rc2 = panel_part(hi, 0, 1);
         if (rc2) return rc2;
         PALIAL_CK(cudaEventRecord(g_la.first, hi), "event");
+        PALIAL_CK(g_ftrace.mark(hi, k, FactorTrace::FIRST), "trace");
         if (have_rest) PALIAL_CK(cudaStreamWaitEvent(hi, g_la.rest, 0), "event");
         PALIAL_CK(mp_update(mode, upper, W, n, nb, k, ah, al, bh, bl, sa, sb, status, hi, 4), "update (diagonal)");
+        PALIAL_CK(g_ftrace.mark(hi, k, FactorTrace::PAIR), "trace");
         // beside it: the rest of the panel, then the rest of row (LU: and column) k+1
         PALIAL_CK(cudaStreamWaitEvent(mid, g_la.binv, 0), "event");
         if (ntr > 1) {
             rc2 = panel_part(mid, 1, -1);
             if (rc2) return rc2;
         }
+        PALIAL_CK(g_ftrace.mark(mid, k, FactorTrace::REST_PANEL), "trace");
         PALIAL_CK(cudaStreamWaitEvent(mid, g_la.first, 0), "event");
         PALIAL_CK(cudaEventRecord(g_la.packed, mid), "event");  // the whole panel k is packed
         if (have_rest) PALIAL_CK(cudaStreamWaitEvent(mid, g_la.rest, 0), "event");
+        PALIAL_CK(g_ftrace.mark(mid, k, FactorTrace::ROW0), "trace");
         if (ntr > 1) PALIAL_CK(mp_update(mode, upper, W, n, nb, k, ah, al, bh, bl, sa, sb, status, mid, 5), "update (next)");
         PALIAL_CK(cudaEventRecord(g_la.nextrow, mid), "event");
+        PALIAL_CK(g_ftrace.mark(mid, k, FactorTrace::ROW1), "trace");
         have_next = true;
         // the rest of the trailing update
         PALIAL_CK(cudaStreamWaitEvent(lo, g_la.packed, 0), "event");
+        PALIAL_CK(g_ftrace.mark(lo, k, FactorTrace::REST0), "trace");
         if (!arrive) {
             if (ntr > 1)
                 PALIAL_CK(mp_update(mode, upper, W, n, nb, k, ah, al, bh, bl, sa, sb, status, lo, 2), "update (rest)");
@@ -389,6 +458,7 @@ int mp_factor(int alg, int prec, float *W, int n, int nb, cudaStream_t s, palial
             if (rc2) return rc2;
         }
         PALIAL_CK(cudaEventRecord(g_la.rest, lo), "event");
+        PALIAL_CK(g_ftrace.mark(lo, k, FactorTrace::REST1), "trace");
         have_rest = true;
     }
     PALIAL_CK(cudaEventRecord(g_la.join, lo), "event");
@@ -400,6 +470,7 @@ int mp_factor(int alg, int prec, float *W, int n, int nb, cudaStream_t s, palial
     int hs[ST_NSLOTS];
     PALIAL_CK(cudaMemcpyAsync(hs, g.diag.status.ptr, sizeof hs, cudaMemcpyDeviceToHost, s), "status");
     PALIAL_CK(cudaStreamSynchronize(s), "factorization");
+    g_ftrace.print(mt);
     if (zero_piv) *zero_piv = hs[ST_ZEROPIV];
     if (hs[ST_CODE] == PALIAL_ERR_NOT_SPD) {
         if (st) {
@@ -669,6 +740,11 @@ extern "C" int palial_gpu_set_update_kernel(int kind) {
     return palial::set_update_kernel(kind);
 }
 
+extern "C" int palial_gpu_set_update_reserve(int sms, int below_rows) {
+    if (sms < 0 || sms > 64 || below_rows < 0) return PALIAL_ERR_ARG;
+    return palial::set_update_reserve(sms, below_rows);
+}
+
 extern "C" int palial_gpu_mp_update_step(int alg, int precision, float *dW, int n, int nb, int k) {
     palial_status *st = nullptr;
     if ((alg != 0 && alg != 1) || !dW || n % nb || nb % 256 || k < 0 || k >= n / nb) return PALIAL_ERR_ARG;
@@ -717,6 +793,7 @@ extern "C" int palial_gpu_mp_factor(int alg, const double *dA, float *dW, int n,
     PALIAL_CK(mps_f64_to_f32(dA, dW, n, nb, 0.0, s), "convert");
     const auto t0 = std::chrono::steady_clock::now();
     int zp = 0;
+    g_panel_fp32 = (o.reserved[5] & 8) != 0;
     rc = mp_factor(alg, o.precision, dW, n, nb, s, st, &zp);
     if (st) st->seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
     if (rc) return set_status(st, rc, "mixed factorization failed");
@@ -784,6 +861,7 @@ static int solve_one(int alg, const double *dA, int n, int nb, const double *dB,
             else if (!(arrived_conv && attempt == 0))
                 PALIAL_CK(mps_f64_to_f32(dA, W, n, nb, shift, s, attempt == 0 ? nrm + 120 : nullptr, alg == 0),
                           "convert");
+            g_panel_fp32 = (o.reserved[5] & 8) != 0;
             rc = mp_factor(alg, prec, W, n, nb, s, st, &zp);
             // opts.reserved[5] bit 1: no shifted retry (a ladder rung hands a breakdown up)
             if (rc != PALIAL_ERR_NOT_SPD || alg != 0 || (o.reserved[5] & 2)) break;
@@ -1145,11 +1223,14 @@ static int solve_ir_host_impl(int alg, const palial_desc *A, const double *B, do
     if (opts) oo = *opts;
     const bool mixed = oo.precision != PALIAL_PREC_FP64;
     if (alg == 0 && mt > 2 && n % nb == 0 && nb % 256 == 0 && mixed && oo.reserved[4] != 1) {
-        // Cholesky reads only the upper triangle.  Mixed precision: it arrives in groups of tile
-        // rows (row r's tiles (r, j >= r): one strided copy), each converted to the FP32 working
-        // copy on the copy stream, and the factorization starts on the first group (RowArrival);
-        // the lower triangle (for the residuals) follows.  The host link is the bottleneck, so
-        // the copies run back to back on one stream.
+        // Cholesky reads only the upper triangle (the reference's dpotrf / dtrsm / dsyrk calls
+        // take 'U'), and only the upper triangle crosses the host link: it arrives in groups of
+        // tile rows (row r's tiles (r, j >= r): one strided copy), each converted to the FP32
+        // working copy on the copy stream, and the factorization starts on the first group
+        // (RowArrival).  The residuals read the symmetric matrix the upper triangle defines: its
+        // lower triangle is written on the device from the upper one (one HBM pass behind the
+        // last group), as a solver given uplo = 'U' treats A.  The host link is the bottleneck,
+        // so the copies run back to back on one stream.
         if (!g_sc.copy) {
             PALIAL_CK(cudaStreamCreateWithFlags(&g_sc.copy, cudaStreamNonBlocking), "copy stream");
             PALIAL_CK(cudaEventCreateWithFlags(&g_sc.upper, cudaEventDisableTiming), "copy event");
@@ -1174,15 +1255,12 @@ static int solve_ir_host_impl(int alg, const palial_desc *A, const double *B, do
         }
         ar.on = true;
         PALIAL_CK(cudaEventRecord(g_sc.upper, g_sc.copy), "copy A");
-        for (int j = 0; j + 1 < mt; j++)
-            PALIAL_CK(cudaMemcpyAsync(dA + te * (mt * j + j + 1), hA + te * (mt * j + j + 1),
-                                      sizeof(double) * te * (mt - 1 - j), cudaMemcpyHostToDevice, g_sc.copy),
-                      "copy A (lower)");
+        PALIAL_CK(mps_mirror_upper(dA, n, nb, g_sc.copy), "lower triangle");
         PALIAL_CK(cudaEventRecord(g_sc.full, g_sc.copy), "copy A");
         g_full_ready = g_sc.full;
     } else if (alg == 0 && mt > 1 && n % nb == 0) {
-        // FP64 Cholesky: the upper triangle (tile column j's tiles 0..j are contiguous) first,
-        // the rest on the copy stream behind it
+        // FP64 Cholesky: the upper triangle (tile column j's tiles 0..j are contiguous), the
+        // lower triangle written from it on the device (copied, for tiles not a multiple of 32)
         if (!g_sc.copy) {
             PALIAL_CK(cudaStreamCreateWithFlags(&g_sc.copy, cudaStreamNonBlocking), "copy stream");
             PALIAL_CK(cudaEventCreateWithFlags(&g_sc.upper, cudaEventDisableTiming), "copy event");
@@ -1194,10 +1272,13 @@ static int solve_ir_host_impl(int alg, const palial_desc *A, const double *B, do
                       "copy A (upper)");
         PALIAL_CK(cudaEventRecord(g_sc.upper, nullptr), "copy A");
         PALIAL_CK(cudaStreamWaitEvent(g_sc.copy, g_sc.upper, 0), "copy A");
-        for (int j = 0; j + 1 < mt; j++)
-            PALIAL_CK(cudaMemcpyAsync(dA + te * (mt * j + j + 1), hA + te * (mt * j + j + 1),
-                                      sizeof(double) * te * (mt - 1 - j), cudaMemcpyHostToDevice, g_sc.copy),
-                      "copy A (lower)");
+        if (nb % 32 == 0)
+            PALIAL_CK(mps_mirror_upper(dA, n, nb, g_sc.copy), "lower triangle");
+        else
+            for (int j = 0; j + 1 < mt; j++)
+                PALIAL_CK(cudaMemcpyAsync(dA + te * (mt * j + j + 1), hA + te * (mt * j + j + 1),
+                                          sizeof(double) * te * (mt - 1 - j), cudaMemcpyHostToDevice, g_sc.copy),
+                          "copy A (lower)");
         PALIAL_CK(cudaEventRecord(g_sc.full, g_sc.copy), "copy A");
         g_full_ready = g_sc.full;
     } else {

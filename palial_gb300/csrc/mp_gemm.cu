@@ -737,6 +737,10 @@ cudaError_t make_map(CUtensorMap *m, const void *base, long long rows, int nb, i
 // MMAs pays) and one block per CTA for BF16 / FP8 (HBM-bound on the C traffic, where two
 // CTAs' epilogues per SM keep more loads in flight).
 int g_update_kernel = 1;
+// SMs the rest update (part 2) leaves free for the high-priority chain and the panel solves
+// beside it: 24 of 152 measured best at N = 32768, NB = 512 (0: none held back)
+int g_update_reserve = 24;
+int g_update_reserve_below = 0;  // ... only for trailing matrices of fewer tile rows (0: always)
 
 int sm_count() {
     static int sms = 0;
@@ -800,6 +804,13 @@ cudaError_t launch_mode(const void *a_hi, const void *a_lo, const void *b_hi, co
         return cudaGetLastError();
     }
     if (run < 2) run = 2;  // small launches too: two blocks per CTA beat one block per CTA (measured)
+    // the rest update (part 2) with SMs held back for the critical chain's kernels: at most
+    // sms - reserve CTAs, each taking a longer run of consecutive blocks
+    if (p.part == 2 && g_update_reserve > 0 && g_update_reserve < sms &&
+        (g_update_reserve_below <= 0 || p.ntr < g_update_reserve_below)) {
+        const long long cap = sms - g_update_reserve;
+        if ((blocks + run - 1) / run > cap) run = (int)((blocks + cap - 1) / cap);
+    }
     constexpr int KB = mp::RunCfg<MODE>::KB;
     if ((e = make_map(&ta, a_hi, rows, p.nb, eb, mp::BM, KB)) != cudaSuccess) return e;
     if ((e = make_map(&tb, b_hi, rows, p.nb, eb, mp::BN, KB)) != cudaSuccess) return e;
@@ -849,6 +860,15 @@ cudaError_t mp_update(int mode, int upper, float *C, int n, int nb, int k, const
 int set_update_kernel(int kind) {
     const int old = g_update_kernel;
     if (kind >= 0 && kind <= 2) g_update_kernel = kind;
+    return old;
+}
+
+// SMs the rest update leaves to the critical chain (palial_gpu_set_update_reserve): returns the
+// previous setting.
+int set_update_reserve(int sms, int below_rows) {
+    const int old = g_update_reserve;
+    if (sms >= 0) g_update_reserve = sms;
+    g_update_reserve_below = below_rows;
     return old;
 }
 

@@ -41,15 +41,16 @@ constexpr int NT = 128;      // 4 warps x 16 rows
 constexpr int KC = 32;       // K chunk between integer folds
 
 // 48-bit rounded integer of v * 2^(47 - sc) (|v| < 2^sc), from the bit pattern; *bad set for
-// Inf / NaN.
+// Inf / NaN and for |v| >= 2^sc (a value the scale does not cover: the result is then
+// reported as NaN instead of a wrapped integer).
 __device__ __forceinline__ long long to_v48(double v, int sc, bool &bad) {
     const unsigned long long bits = (unsigned long long)__double_as_longlong(v);
     const int E = (int)((bits >> 52) & 0x7FF);
-    bad |= (E == 0x7FF);
     if (E == 0) return 0;  // zero or subnormal: below 2^-1022, far under 2^(sc - 48)
     const unsigned long long mant = (bits & 0xFFFFFFFFFFFFFull) | 0x10000000000000ull;
-    const int shift = 1028 + sc - E;  // >= 6 when |v| < 2^sc
-    if (shift >= 64 || shift <= 0) return 0;
+    const int shift = 1028 + sc - E;  // >= 6 exactly when |v| < 2^sc
+    bad |= (E == 0x7FF) | (shift < 6);
+    if (shift >= 64 || shift < 6) return 0;
     const long long m = (long long)((mant + (1ull << (shift - 1))) >> shift);
     return (bits >> 63) ? -m : m;
 }

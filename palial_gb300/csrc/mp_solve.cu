@@ -43,11 +43,19 @@ __global__ void f64_to_f32_kernel(const double *__restrict__ a, float *__restric
         const size_t base = (size_t)t * te;
         const int end = min(te, (ch + 1) * kConvChunk);
         const bool diag = shift_diag != 0.0 && tr == tc;
+        // a symmetric matrix held as its upper triangle: the max skips the strictly lower
+        // entries of the diagonal tiles (they need not hold A's values)
+        const bool lower_skip = upper_only && tr == tc;
 #pragma unroll 4
         for (int i = ch * kConvChunk + 2 * threadIdx.x; i < end; i += 2 * blockDim.x) {
             double2 v = *reinterpret_cast<const double2 *>(a + base + i);  // te even: 16-byte aligned
-            const unsigned long long b0 = (unsigned long long)__double_as_longlong(v.x) & 0x7FFFFFFFFFFFFFFFull;
-            const unsigned long long b1 = (unsigned long long)__double_as_longlong(v.y) & 0x7FFFFFFFFFFFFFFFull;
+            unsigned long long b0 = (unsigned long long)__double_as_longlong(v.x) & 0x7FFFFFFFFFFFFFFFull;
+            unsigned long long b1 = (unsigned long long)__double_as_longlong(v.y) & 0x7FFFFFFFFFFFFFFFull;
+            if (lower_skip) {  // entries i, i + 1 share column i / nb (nb even)
+                const int r = i % nb, c = i / nb;
+                b0 = r > c ? 0ull : b0;
+                b1 = r + 1 > c ? 0ull : b1;
+            }
             mx = b0 > mx ? b0 : mx;
             mx = b1 > mx ? b1 : mx;
             if (diag) {
@@ -63,6 +71,41 @@ __global__ void f64_to_f32_kernel(const double *__restrict__ a, float *__restric
             mx = y > mx ? y : mx;
         }
         if ((threadIdx.x & 31) == 0) atomicMax(reinterpret_cast<unsigned long long *>(amax), mx);
+    }
+}
+
+// ---- the lower triangle of a symmetric matrix from its upper triangle ---------------------
+// A(i, j) <- A(j, i) for every i > j of an n x n tile-layout matrix (nb a multiple of 32):
+// host-buffer Cholesky solves copy only the upper triangle (the triangle the factorization
+// reads) and rebuild the rest on the device for the residuals.  One CTA per 32 x 32 block
+// (bi, bj), bi >= bj, of the lower triangle in a grid-stride loop: the mirror block (bj, bi)
+// is read along its columns into shared memory and written along the destination's columns.
+// On a diagonal block only the strictly lower entries are written, from the strictly upper
+// ones read before the barrier.
+__device__ __forceinline__ size_t sym_off(int n, int nb, int r, int c) {
+    const int mt = n / nb;
+    return (size_t)nb * nb * ((size_t)(r / nb) + (size_t)mt * (c / nb)) + (size_t)(r % nb) + (size_t)(c % nb) * nb;
+}
+
+__global__ void __launch_bounds__(256) mirror_upper_kernel(double *__restrict__ a, int n, int nb) {
+    __shared__ double s[32][33];  // s[column][row] of the source block
+    const int nbk = n / 32;
+    const long long items = (long long)nbk * (nbk + 1) / 2;  // block it = bi (bi + 1) / 2 + bj
+    const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
+    for (long long it = blockIdx.x; it < items; it += gridDim.x) {
+        int bi = (int)((sqrt(8.0 * (double)it + 1.0) - 1.0) * 0.5);
+        while ((long long)bi * (bi + 1) / 2 > it) bi--;
+        while ((long long)(bi + 1) * (bi + 2) / 2 <= it) bi++;
+        const int bj = (int)(it - (long long)bi * (bi + 1) / 2);
+        const int r0 = 32 * bj, c0 = 32 * bi;  // source block: rows r0.., columns c0.. (upper)
+#pragma unroll
+        for (int q = ty; q < 32; q += 8) s[q][tx] = a[sym_off(n, nb, r0 + tx, c0 + q)];
+        __syncthreads();
+        // destination (c0 + tx, r0 + q) = source (r0 + q, c0 + tx) = s[tx][q]
+#pragma unroll
+        for (int q = ty; q < 32; q += 8)
+            if (bi != bj || tx > q) a[sym_off(n, nb, c0 + tx, r0 + q)] = s[tx][q];
+        __syncthreads();
     }
 }
 
@@ -435,20 +478,25 @@ __device__ __forceinline__ void apply_inv64(const Smem &m, const float *X, float
 // X = U^-T B, B = nb x 64 strip (ld), U upper nb x nb (ld_u); uinv: inverses of U's 64 x 64
 // diagonal blocks
 // (ph, pl: optional packed BF16 copy of the strip, same layout, written with the results)
+// tc: the block updates on the warp tensor cores (BF16x3 operands, FP32 accumulation; the panels
+// of a factorization whose trailing updates are BF16x3), else FP32 FMAs.
 __device__ __forceinline__ void strip_lut(const Smem &m, const float *U, int ldu, float *B, int ldb, int nb,
                                           const float *uinv, __nv_bfloat16 *ph = nullptr,
-                                          __nv_bfloat16 *pl = nullptr) {
+                                          __nv_bfloat16 *pl = nullptr, bool tc = false) {
     for (int rb = 0; rb < nb; rb += 64) {
-        if (rb > 0) cta_gemm<true, false>(64, 64, rb, -1.f, U + (size_t)rb * ldu, ldu, B, ldb, B + rb, ldb, m.g);
+        if (rb > 0 && tc)
+            cta_gemm<true, false, false, true>(64, 64, rb, -1.f, U + (size_t)rb * ldu, ldu, B, ldb, B + rb, ldb, m.g);
+        else if (rb > 0) cta_gemm<true, false>(64, 64, rb, -1.f, U + (size_t)rb * ldu, ldu, B, ldb, B + rb, ldb, m.g);
         apply_inv64<0>(m, uinv + (size_t)(rb / 64) * 4096, B + rb, ldb, ph ? ph + rb : nullptr, pl ? pl + rb : nullptr);
     }
 }
 // X = L^-1 B (unit lower) with L's diagonal-block inverses linv
 __device__ __forceinline__ void strip_llu_inv(const Smem &m, const float *L, int ldl, float *B, int ldb, int nb,
                                               const float *linv, __nv_bfloat16 *ph = nullptr,
-                                              __nv_bfloat16 *pl = nullptr) {
+                                              __nv_bfloat16 *pl = nullptr, bool tc = false) {
     for (int rb = 0; rb < nb; rb += 64) {
-        if (rb > 0) cta_gemm<false, false>(64, 64, rb, -1.f, L + rb, ldl, B, ldb, B + rb, ldb, m.g);
+        if (rb > 0 && tc) cta_gemm<false, false, false, true>(64, 64, rb, -1.f, L + rb, ldl, B, ldb, B + rb, ldb, m.g);
+        else if (rb > 0) cta_gemm<false, false>(64, 64, rb, -1.f, L + rb, ldl, B, ldb, B + rb, ldb, m.g);
         apply_inv64<1>(m, linv + (size_t)(rb / 64) * 4096, B + rb, ldb, ph ? ph + rb : nullptr, pl ? pl + rb : nullptr);
     }
 }
@@ -472,9 +520,12 @@ __device__ __forceinline__ void strip_llu(const Smem &m, const float *L, int ldl
 }
 // X = B U^-1, B = 64 x nb row strip, with U's diagonal-block inverses uinv
 __device__ __forceinline__ void strip_run(const Smem &m, const float *U, int ldu, float *B, int ldb, int nb,
-                                          const float *uinv) {
+                                          const float *uinv, bool tc = false) {
     for (int cb = 0; cb < nb; cb += 64) {
-        if (cb > 0)
+        if (cb > 0 && tc)
+            cta_gemm<false, false, false, true>(64, 64, cb, -1.f, B, ldb, U + (size_t)cb * ldu, ldu, B + (size_t)cb * ldb,
+                                                ldb, m.g);
+        else if (cb > 0)
             cta_gemm<false, false>(64, 64, cb, -1.f, B, ldb, U + (size_t)cb * ldu, ldu, B + (size_t)cb * ldb, ldb, m.g);
         apply_inv64<2>(m, uinv + (size_t)(cb / 64) * 4096, B + (size_t)cb * ldb, ldb);
     }
@@ -487,7 +538,7 @@ __device__ __forceinline__ void strip_run(const Smem &m, const float *U, int ldu
 // trailing tile t - k - 1 at (t - k - 1) nb^2, written together with the solved values.
 __global__ void __launch_bounds__(NT, 2) panel_trsm_kernel(float *W, int n, int nb, int k, int kind,
                                                           const float *binv, __nv_bfloat16 *ph, __nv_bfloat16 *pl,
-                                                          int t0) {
+                                                          int t0, int tc) {
     extern __shared__ __align__(16) float smem[];
     const Smem m = smem_parts(smem);
     const int tt = t0 + blockIdx.y;  // trailing tile index
@@ -495,11 +546,11 @@ __global__ void __launch_bounds__(NT, 2) panel_trsm_kernel(float *W, int n, int 
     const float *T = W + tile_off(n, nb, k, k);
     const size_t po = (size_t)tt * nb * nb + (size_t)s * 64 * nb;
     __nv_bfloat16 *sh = ph ? ph + po : nullptr, *sl = pl ? pl + po : nullptr;
-    if (kind == 0) strip_lut(m, T, nb, W + tile_off(n, nb, k, t) + (size_t)s * 64 * nb, nb, nb, binv, sh, sl);
+    if (kind == 0) strip_lut(m, T, nb, W + tile_off(n, nb, k, t) + (size_t)s * 64 * nb, nb, nb, binv, sh, sl, tc != 0);
     else if (kind == 1)
         strip_llu_inv(m, T, nb, W + tile_off(n, nb, k, t) + (size_t)s * 64 * nb, nb, nb, binv + (size_t)(nb / 64) * 4096,
-                      sh, sl);
-    else strip_run(m, T, nb, W + tile_off(n, nb, t, k) + s * 64, nb, nb, binv);
+                      sh, sl, tc != 0);
+    else strip_run(m, T, nb, W + tile_off(n, nb, t, k) + s * 64, nb, nb, binv, tc != 0);
 }
 
 // ---- two-level factorization of a diagonal tile (NB >= 512) ---------------------------------
@@ -801,6 +852,17 @@ cudaError_t mps_f64_to_f32(const double *A, float *W, int n, int nb, double shif
         A, W, n, nb, shift, upper_only ? 1 : 0, r0, r1 < 0 ? n / nb : r1, amax);
     return cudaGetLastError();
 }
+// The lower triangle of the symmetric tile-layout matrix A from its upper triangle.
+cudaError_t mps_mirror_upper(double *A, int n, int nb, cudaStream_t s) {
+    if (n <= 0 || nb <= 0 || nb % 32 || n % nb) return cudaErrorInvalidValue;
+    const long long blocks = (long long)(n / 32) * (n / 32 + 1) / 2;
+    int sms = 0, dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    note_launch();
+    mps::mirror_upper_kernel<<<(int)std::min<long long>(blocks, (long long)std::max(1, sms) * 8), 256, 0, s>>>(A, n, nb);
+    return cudaGetLastError();
+}
 // R = B - A X in compensated FP32 (see residual_df_kernel); sigma: |a_ij| < 2^sigma for all
 // entries.  Xs (n x 16 float2) and tau (16 ints) are scratch; colmax = per-column max |x|.
 cudaError_t mps_residual_df(const double *A, int n, int nb, const double *X, const double *colmax, const double *B,
@@ -864,7 +926,7 @@ cudaError_t mps_half_update(float *T, int h, int ld, int alg, cudaStream_t s) {
 }
 // ph / pl: optional packed BF16 row-panel operand written by the solve (kinds 0 and 1)
 cudaError_t mps_panel_trsm(float *W, int n, int nb, int k, int kind, const float *binv, cudaStream_t s, void *ph,
-                           void *pl, int t0, int count) {
+                           void *pl, int t0, int count, bool tc) {
     const int ntr = n / nb - k - 1;
     if (count < 0) count = ntr - t0;
     if (ntr <= 0 || count <= 0) return cudaSuccess;
@@ -873,7 +935,8 @@ cudaError_t mps_panel_trsm(float *W, int n, int nb, int k, int kind, const float
     note_launch();
     mps::panel_trsm_kernel<<<grid, mps::NT, mps::SMEM_BYTES, s>>>(W, n, nb, k, kind, binv,
                                                                    kind == 2 ? nullptr : static_cast<__nv_bfloat16 *>(ph),
-                                                                   kind == 2 ? nullptr : static_cast<__nv_bfloat16 *>(pl), t0);
+                                                                   kind == 2 ? nullptr : static_cast<__nv_bfloat16 *>(pl), t0,
+                                                                   tc ? 1 : 0);
     return cudaGetLastError();
 }
 cudaError_t mps_residual(const double *A, int n, int nb, const double *X, const double *B, double *R, int nrhs,

@@ -502,3 +502,78 @@ def test_host_solve_matches_device_solve(alg, prec):
     sth = P.solve_ir_host(alg, host_a.numpy(), n, nb, np.ascontiguousarray(b.T), xh, nrhs, precision=prec)
     assert sth.code == 0 and sth.ir_iters == st.ir_iters
     assert np.array_equal(xh, dx.cpu().numpy().reshape(nrhs, n))
+
+
+@pytest.mark.parametrize("prec", ["bf16x3", "fp64"])
+def test_host_cholesky_reads_only_the_upper_triangle(prec):
+    """Host-buffer Cholesky copies only the upper triangle and writes the lower one on the
+    device from it: with NaN everywhere below the diagonal of the caller's buffer, the solve
+    returns exactly the device-resident solve's X for the full symmetric matrix."""
+    n, nb, nrhs = 4096, 512, 4
+    a = O.gen_spd(0, n)
+    b = O.gen_uniform(5, n, nrhs, stream=O.STREAM_RHS)
+    da = torch.from_numpy(O.to_tiles(a, nb)).cuda()
+    db = torch.from_numpy(np.asfortranarray(b).ravel(order="F")).cuda()
+    dx = torch.zeros_like(db)
+    st = P.solve_ir("cholesky", da.data_ptr(), n, nb, db.data_ptr(), dx.data_ptr(), nrhs, precision=prec)
+    assert st.code == 0
+    upper = a.copy()
+    upper[np.tril_indices(n, -1)] = np.nan
+    host_a = torch.from_numpy(O.to_tiles(upper, nb)).pin_memory()
+    xh = np.zeros((nrhs, n))
+    sth = P.solve_ir_host("cholesky", host_a.numpy(), n, nb, np.ascontiguousarray(b.T), xh, nrhs, precision=prec)
+    assert sth.code == 0 and sth.ir_iters == st.ir_iters, sth.message
+    assert np.array_equal(xh, dx.cpu().numpy().reshape(nrhs, n))
+
+
+def test_update_reserve_gives_the_same_bits():
+    """The SMs the rest-of-update launches leave to the critical chain change the launch shape
+    only: the solution is bit-identical for every setting; bad settings are refused."""
+    lib = P.lib()
+    err_arg = -1  # PALIAL_ERR_ARG
+    assert lib.palial_gpu_set_update_reserve(-1, 0) == err_arg
+    assert lib.palial_gpu_set_update_reserve(8, -1) == err_arg
+    n, nb, nrhs = 8192, 512, 4
+    da = torch.empty(n * n, dtype=torch.float64, device="cuda")
+    P.gen_spd(da.data_ptr(), n, nb, seed=3)
+    db = torch.empty(n * nrhs, dtype=torch.float64, device="cuda")
+    P.gen_dense(db.data_ptr(), n, nrhs, 5, P.STREAM_RHS)
+    xs = []
+    old = lib.palial_gpu_set_update_reserve(0, 0)
+    try:
+        for sms, below in ((0, 0), (24, 0), (60, 0), (16, 8)):
+            lib.palial_gpu_set_update_reserve(sms, below)
+            dx = torch.zeros_like(db)
+            st = P.solve_ir("cholesky", da.data_ptr(), n, nb, db.data_ptr(), dx.data_ptr(), nrhs, precision="bf16x3")
+            assert st.code == 0
+            xs.append(dx)
+    finally:
+        lib.palial_gpu_set_update_reserve(old, 0)
+    assert all(torch.equal(xs[0], x) for x in xs[1:])
+
+
+@pytest.mark.parametrize("alg", ["cholesky", "lu"])
+def test_fp32_and_tensor_core_panels_both_reach_the_target(alg):
+    """BF16x3 factorizations solve their panels' block products as BF16x3 on the warp tensor
+    cores by default; opts.reserved[5] bit 3 keeps them in FP32.  Both refine to the FP64-level
+    backward error in the same small number of steps."""
+    import ctypes
+    n, nb, nrhs = 4096, 512, 4
+    a = O.gen_spd(0, n) if alg == "cholesky" else dominant(3, n)
+    b = O.gen_uniform(5, n, nrhs, stream=O.STREAM_RHS)
+    da = torch.from_numpy(O.to_tiles(a, nb)).cuda()
+    db = torch.from_numpy(np.asfortranarray(b).ravel(order="F")).cuda()
+    iters = []
+    for bit in (0, 8):
+        dx = torch.zeros_like(db)
+        o = P.make_opts(precision="bf16x3")
+        o.reserved[5] = bit
+        st = P.Status()
+        rc = P.lib().palial_gpu_solve_ir(P.ALG[alg], da.data_ptr(), n, nb, db.data_ptr(), dx.data_ptr(), nrhs,
+                                         ctypes.byref(o), ctypes.byref(st), None)
+        assert rc == 0, st.message
+        assert st.backward_error <= 1e-14 * n
+        x = dx.cpu().numpy().reshape(nrhs, n).T
+        assert np.linalg.norm(x - np.linalg.solve(a, b)) <= 1e-9 * np.linalg.norm(x)
+        iters.append(st.ir_iters)
+    assert max(iters) <= 3, iters
