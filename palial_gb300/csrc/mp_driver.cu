@@ -77,8 +77,9 @@ cudaError_t launch_sumsq(const double *X, long long len, double *partial, int bl
 void mp_release();
 int set_update_kernel(int kind);
 int set_update_reserve(int sms, int below_rows);
+size_t mrd_scratch_bytes(int n);
 cudaError_t mrd_residual(const double *A, int n, int nb, const double *X, const double *colmax, const double *B,
-                         double *R, int nrhs, int sigma, uint32_t *Xd, int *tau, double *amax, cudaStream_t s);
+                         double *R, int nrhs, int sigma, void *scratch, double *amax, cudaStream_t s);
 }  // namespace palial
 
 using namespace palial;
@@ -91,7 +92,7 @@ struct MpBufs {
     DevBuf xsplit;  // compensated residual: X as FP32 pairs (n x 16 float2) + 16 scale exponents
     DevBuf binv;    // inverses of the current diagonal tile's 64 x 64 diagonal blocks (panel solves)
     DevBuf dinv_u, dinv_l, stile;  // FP32 inverses of the diagonal factor tiles, solve scratch
-    DevBuf xdig;    // digit residual: X's BF16 digits in fragment order (n * 48 words) + 16 exponents
+    DevBuf xdig;    // digit residual scratch (mrd_scratch_bytes): X's digits, exponents, integer sums
 };
 MpBufs mb;
 
@@ -548,9 +549,7 @@ int precondition(int alg, const float *W, int n, int nb, const double *v, double
 static cudaError_t df_residual(const double *A, int n, int nb, const double *X, const double *colmax, const double *B,
                                double *R, int nrhs, double *amax_out, cudaStream_t s) {
     if (g_rctx.digits) {
-        uint32_t *xd = mb.xdig.as<uint32_t>();
-        return mrd_residual(A, n, nb, X, colmax, B, R, nrhs, g_rctx.sigma, xd,
-                            reinterpret_cast<int *>(xd + (size_t)n * 48), amax_out, s);
+        return mrd_residual(A, n, nb, X, colmax, B, R, nrhs, g_rctx.sigma, mb.xdig.ptr, amax_out, s);
     }
     float2 *xs = mb.xsplit.as<float2>();
     return mps_residual_df(A, n, nb, X, colmax, B, R, nrhs, g_rctx.sigma, xs, reinterpret_cast<int *>(xs + (size_t)n * 16),
@@ -898,7 +897,7 @@ static int solve_one(int alg, const double *dA, int n, int nb, const double *dB,
     constexpr double kDfConfirmBelow = 1e-11;
     g_rctx.df = use_df;
     g_rctx.digits = use_df && o.reserved[4] != 4 && n <= (1 << 18);
-    if (g_rctx.digits) PALIAL_CK(mb.xdig.ensure(sizeof(uint32_t) * (size_t)n * 48 + 64 * sizeof(int)), "alloc digits");
+    if (g_rctx.digits) PALIAL_CK(mb.xdig.ensure(mrd_scratch_bytes(n)), "alloc digits");
     g_rctx.sigma = sigma;
     // status words of the refinement's solve launches (a timed-out wait is reported there)
     PALIAL_CK(g.diag.status.ensure(sizeof(int) * ST_NSLOTS + 64), "alloc status");
@@ -1180,11 +1179,8 @@ extern "C" int palial_gpu_residual(const double *dA, int n, int nb, const double
     PALIAL_CK(mps_colmax(dX, n, nrhs, nrm + 33, s), "norm x");
     float2 *xs = mb.xsplit.as<float2>();
     if (mode == 3) {
-        PALIAL_CK(mb.xdig.ensure(sizeof(uint32_t) * (size_t)n * 48 + 64 * sizeof(int)), "alloc digits");
-        uint32_t *xd = mb.xdig.as<uint32_t>();
-        PALIAL_CK(mrd_residual(dA, n, nb, dX, nrm + 33, dB, dR, nrhs, sigma, xd, reinterpret_cast<int *>(xd + (size_t)n * 48),
-                               nullptr, s),
-                  "residual (digits)");
+        PALIAL_CK(mb.xdig.ensure(mrd_scratch_bytes(n)), "alloc digits");
+        PALIAL_CK(mrd_residual(dA, n, nb, dX, nrm + 33, dB, dR, nrhs, sigma, mb.xdig.ptr, nullptr, s), "residual (digits)");
         return PALIAL_OK;
     }
     if (mode == 2) {

@@ -804,9 +804,10 @@ cudaError_t launch_mode(const void *a_hi, const void *a_lo, const void *b_hi, co
         return cudaGetLastError();
     }
     if (run < 2) run = 2;  // small launches too: two blocks per CTA beat one block per CTA (measured)
-    // the rest update (part 2) with SMs held back for the critical chain's kernels: at most
-    // sms - reserve CTAs, each taking a longer run of consecutive blocks
-    if (p.part == 2 && g_update_reserve > 0 && g_update_reserve < sms &&
+    // the rest update (part 2, or its row ranges while row groups arrive: part 3) with SMs held
+    // back for the critical chain's kernels: at most sms - reserve CTAs, each taking a longer
+    // run of consecutive blocks
+    if ((p.part == 2 || p.part == 3) && g_update_reserve > 0 && g_update_reserve < sms &&
         (g_update_reserve_below <= 0 || p.ntr < g_update_reserve_below)) {
         const long long cap = sms - g_update_reserve;
         if ((blocks + run - 1) / run > cap) run = (int)((blocks + cap - 1) / cap);
