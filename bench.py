@@ -7,8 +7,9 @@ A step is one solve A X = B (16 right-hand sides, uniform [-1, 1)) of a device-r
 SPD matrix A = B B^T + N I (seed = rank; the reference's tile layout) by the mixed-precision
 path: BF16x3 trailing updates on tcgen05 (operands split into BF16 hi + lo, three products,
 FP32 accumulation; --precision bf16 / fp8 select one product), FP32 diagonal tiles and
-panels, compensated-FP32 refinement residuals (FP64 accumulation; once the correction is
-small, the update form r - A d with FP32 products) and refinement to the FP64-level normwise
+panels (BF16x3 block products), the exact-digit tensor-core residual (48-bit digit expansions,
+integer accumulation; once the correction is small, the update form r - A d with FP32
+products) and refinement to the FP64-level normwise
 backward error (<= 1e-14 * N), checked after the timed region with the FP64 residual.  value = FP64-equivalent algorithmic flops (N^3/3) / time to solution
 (factorization + refinement), summed over ranks (replicas, no collective on the data path).
 Inputs (8.6 GB) are far larger than L2 (129 MB): no flush is needed.
@@ -174,9 +175,10 @@ def spd_host_from_gpu(P, torch, n: int, seed: int):
 def headline_config(n: int, precision: str, world: int) -> dict:
     """The workload both arms report on (the reference arm times a bounded sample of it)."""
     return {"workload": f"mixed-precision Cholesky + IR, N={n}, NB={NB}, 16 RHS, {precision} "
-                        "trailing updates on tcgen05 (FP32 accumulate), FP32 diagonal tiles and "
-                        "panels, compensated-FP32 and update-form refinement residuals, FP64-checked backward "
-                        "error; SPD B*B^T+N*I seed=rank, device-resident; inputs 8.6 GB >> L2 (no flush needed)",
+                        "trailing updates on tcgen05 (FP32 accumulate), FP32 diagonal tiles, FP32 "
+                        "panels with BF16x3 block products, exact-digit tensor-core and update-form "
+                        "refinement residuals, FP64-checked backward error; SPD B*B^T+N*I seed=rank, "
+                        "device-resident; inputs 8.6 GB >> L2 (no flush needed)",
             "n": n, "nb": NB, "nrhs": 16, "precision": precision, "parallelism": f"replicas x{world}"}
 
 
