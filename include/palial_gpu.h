@@ -195,6 +195,11 @@ int palial_gpu_mp_update_step(int alg, int precision, float *dW, int n, int nb, 
  * C traffic).  Both give the same bits.
  * Returns the previous setting (PALIAL_ERR_ARG for an unknown kind). */
 int palial_gpu_set_update_kernel(int kind);
+/* Which kernel factors the mixed path's 256 x 256 Cholesky blocks (the halves of a 512 diagonal
+ * tile, or 256 tiles): 1 (default) keeps the block's upper triangle in shared memory for the
+ * whole factorization, 0 stages 64-column pieces from global memory.  Same bits.  Returns the
+ * previous setting (PALIAL_ERR_ARG for an unknown kind). */
+int palial_gpu_set_diag_kernel(int kind);
 /* SMs (0..64) the mixed factorization's rest-of-trailing-update launches leave free for the
  * critical chain's kernels on the high-priority stream (the tile-run kernel then launches at
  * most SMs - sms CTAs with longer runs), in the steps whose trailing matrix has fewer than

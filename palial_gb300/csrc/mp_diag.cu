@@ -514,11 +514,133 @@ __global__ void __launch_bounds__(NT, 1) diag_factor_kernel(float *T, int nb, in
     if (ALG == 1 && zero && threadIdx.x == 0) atomicOr(status + ST_ZEROPIV, 1);
 }
 
+// ---- Cholesky of a 256 x 256 block held in shared memory -----------------------------------
+// The upper triangle (32896 floats, packed by columns: column c's rows 0..c at c (c + 1) / 2)
+// stays in shared memory for the whole factorization: one load and one store of the block,
+// no global traffic between the 64-column steps (their latency grows when the trailing update
+// loads HBM beside this kernel).  Per step: the 64 x 64 diagonal block through Ds (chol64), the
+// row panel solved in place in its packed columns (solve_vec, one column per thread), the panel
+// transposed into UT[p][i] once, and the trailing upper triangle updated from UT with 8 x 8
+// register tiles (K = 64 in one pass).  The operations and their order per entry are those of
+// diag_factor_kernel<0>, so the factors are bit-identical.
+constexpr int H256 = 256;
+constexpr int PK256 = H256 * (H256 + 1) / 2;
+constexpr int UTP = 196;  // pitch of UT rows (float4-aligned)
+constexpr int SMEM256_FLOATS = PK256 + 64 * DP + 64 * UTP + 64;
+
+__device__ __forceinline__ int poff(int c) { return (c * (c + 1)) >> 1; }
+
+__global__ void __launch_bounds__(NT, 1) chol256_smem_kernel(float *T, int ld, int k, int col0, int *status) {
+    extern __shared__ __align__(16) float smem[];
+    float *P = smem;
+    float (*Ds)[DP] = reinterpret_cast<float (*)[DP]>(smem + PK256);
+    float *UT = smem + PK256 + 64 * DP;
+    int *sflag = reinterpret_cast<int *>(UT + 64 * UTP);
+    if (ld_volatile(status + ST_CODE) != 0) return;
+    if (threadIdx.x == 0) status[6] = k;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    // load the upper triangle, one warp per column (rows in 32-row pieces, all loads of a
+    // column in flight)
+    for (int c = warp; c < H256; c += NT / 32) {
+        const float *src = T + (size_t)c * ld;
+        float v[8];
+#pragma unroll
+        for (int j = 0; j < 8; j++) v[j] = (32 * j + lane <= c) ? __ldcg(src + 32 * j + lane) : 0.f;
+#pragma unroll
+        for (int j = 0; j < 8; j++)
+            if (32 * j + lane <= c) P[poff(c) + 32 * j + lane] = v[j];
+    }
+    __syncthreads();
+    const int q8 = threadIdx.x >> 3, i8 = threadIdx.x & 7;
+    for (int j0 = 0; j0 < H256; j0 += 64) {
+        for (int e = threadIdx.x; e < 4096; e += NT) {
+            const int r = e & 63, c = e >> 6;
+            Ds[c][r] = r <= c ? P[poff(j0 + c) + j0 + r] : 0.f;
+        }
+        __syncthreads();
+        const int bad = chol64(Ds, sflag);
+        if (bad >= 0) {
+            if (threadIdx.x == 0 && atomicCAS(status + ST_CODE, 0, -3 /*PALIAL_ERR_NOT_SPD*/) == 0) {
+                status[ST_COL] = col0 + j0 + bad;
+                status[ST_M] = status[ST_N] = k;
+                status[6] = k;
+                __threadfence();
+            }
+            return;
+        }
+        for (int e = threadIdx.x; e < 4096; e += NT) {
+            const int r = e & 63, c = e >> 6;
+            if (r <= c) P[poff(j0 + c) + j0 + r] = Ds[c][r];
+        }
+        const int m = H256 - j0 - 64;
+        if (m == 0) break;
+        __syncthreads();
+        // row panel U12 = U11^-T A12 in place: column j0 + 64 + c, rows j0 .. j0 + 63
+        for (int c = threadIdx.x; c < m; c += NT) solve_vec<0>(Ds, P + poff(j0 + 64 + c) + j0, 1);
+        __syncthreads();
+        // UT[p][i] = U12(p, i)
+        for (int e = threadIdx.x; e < 64 * m; e += NT) {
+            const int pr = e & 63, i = e >> 6;
+            UT[pr * UTP + i] = P[poff(j0 + 64 + i) + j0 + pr];
+        }
+        __syncthreads();
+        // A22(i, q) -= sum_p U12(p, i) U12(p, q), i <= q: 8 x 8 micro-tiles (bi <= bj)
+        const int mb = m / MT, tiles = mb * (mb + 1) / 2;
+        for (int u = threadIdx.x; u < tiles; u += NT) {
+            int bj = 0, rem = u;  // column block bj holds bj + 1 micro-tiles
+            while (bj < mb && rem > bj) {
+                rem -= bj + 1;
+                bj++;
+            }
+            const int bi = rem;
+            float acc[MT][MT];
+#pragma unroll
+            for (int i = 0; i < MT; i++)
+#pragma unroll
+                for (int j = 0; j < MT; j++) acc[i][j] = 0.f;
+#pragma unroll 4
+            for (int pr = 0; pr < 64; pr++) {
+                const float4 a0 = *reinterpret_cast<const float4 *>(UT + pr * UTP + bi * MT);
+                const float4 a1 = *reinterpret_cast<const float4 *>(UT + pr * UTP + bi * MT + 4);
+                const float4 b0 = *reinterpret_cast<const float4 *>(UT + pr * UTP + bj * MT);
+                const float4 b1 = *reinterpret_cast<const float4 *>(UT + pr * UTP + bj * MT + 4);
+                const float a[MT] = {a0.x, a0.y, a0.z, a0.w, a1.x, a1.y, a1.z, a1.w};
+                const float b[MT] = {b0.x, b0.y, b0.z, b0.w, b1.x, b1.y, b1.z, b1.w};
+#pragma unroll
+                for (int i = 0; i < MT; i++)
+#pragma unroll
+                    for (int j = 0; j < MT; j++) acc[i][j] = fmaf(a[i], b[j], acc[i][j]);
+            }
+#pragma unroll
+            for (int j = 0; j < MT; j++) {
+                const int q = j0 + 64 + bj * MT + j;
+                float *col = P + poff(q) + j0 + 64 + bi * MT;
+#pragma unroll
+                for (int i = 0; i < MT; i++)
+                    if (bi < bj || i <= j) col[i] -= acc[i][j];
+            }
+        }
+        __syncthreads();
+    }
+    (void)q8;
+    (void)i8;
+    // store the upper triangle back
+    for (int c = warp; c < H256; c += NT / 32) {
+        float *dst = T + (size_t)c * ld;
+#pragma unroll
+        for (int j = 0; j < 8; j++)
+            if (32 * j + lane <= c) dst[32 * j + lane] = P[poff(c) + 32 * j + lane];
+    }
+}
+
 }  // namespace mpd
 
 cudaError_t mpd_configure() {
     const int bytes = mpd::smem_floats(1024) * 4;
     cudaError_t e = cudaFuncSetAttribute(mpd::diag_factor_kernel<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    if (e != cudaSuccess) return e;
+    e = cudaFuncSetAttribute(mpd::chol256_smem_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             mpd::SMEM256_FLOATS * 4);
     if (e != cudaSuccess) return e;
     return cudaFuncSetAttribute(mpd::diag_factor_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
 }
@@ -527,6 +649,15 @@ cudaError_t mps_block_inverse(const float *W, int n, int nb, int k, int factors,
                               int blocks);
 cudaError_t mps_half_panel(float *T, int h, int ld, const float *binv, int alg, cudaStream_t s);
 cudaError_t mps_half_update(float *T, int h, int ld, int alg, cudaStream_t s);
+
+// Cholesky blocks of 256 by the shared-memory-resident kernel (1, default) or the staged one (0);
+// the two give the same bits (palial_gpu_set_diag_kernel).
+int g_chol_smem = 1;
+int set_diag_kernel(int kind) {
+    const int old = g_chol_smem;
+    if (kind == 0 || kind == 1) g_chol_smem = kind;
+    return old;
+}
 
 // Factor diagonal tile k of the FP32 tile matrix W (n x n, tile nb) in place.  Tiles of
 // NB >= 512 go two-level: A11 (h = NB/2) in one CTA; on many CTAs the off-diagonal blocks
@@ -543,7 +674,9 @@ cudaError_t mpd_factor_tile(int alg, float *W, int n, int nb, int k, int *status
         const int bytes = mpd::smem_floats(h) * 4;
         cudaError_t e;
         note_launch();
-        if (alg == 0) mpd::diag_factor_kernel<0><<<1, mpd::NT, bytes, s>>>(T, h, nb, k, 0, status);
+        if (alg == 0 && h == mpd::H256 && g_chol_smem)
+            mpd::chol256_smem_kernel<<<1, mpd::NT, mpd::SMEM256_FLOATS * 4, s>>>(T, nb, k, 0, status);
+        else if (alg == 0) mpd::diag_factor_kernel<0><<<1, mpd::NT, bytes, s>>>(T, h, nb, k, 0, status);
         else mpd::diag_factor_kernel<1><<<1, mpd::NT, bytes, s>>>(T, h, nb, k, 0, status);
         e = cudaGetLastError();
         if (e == cudaSuccess) e = mps_block_inverse(W, n, nb, k, alg == 0 ? 1 : 2, binv, s, h / 64);
@@ -551,13 +684,19 @@ cudaError_t mpd_factor_tile(int alg, float *W, int n, int nb, int k, int *status
         if (e == cudaSuccess) e = mps_half_update(T, h, nb, alg, s);
         if (e != cudaSuccess) return e;
         note_launch();
-        if (alg == 0) mpd::diag_factor_kernel<0><<<1, mpd::NT, bytes, s>>>(T + (size_t)h * (nb + 1), h, nb, k, h, status);
+        if (alg == 0 && h == mpd::H256 && g_chol_smem)
+            mpd::chol256_smem_kernel<<<1, mpd::NT, mpd::SMEM256_FLOATS * 4, s>>>(T + (size_t)h * (nb + 1), nb, k, h,
+                                                                                status);
+        else if (alg == 0)
+            mpd::diag_factor_kernel<0><<<1, mpd::NT, bytes, s>>>(T + (size_t)h * (nb + 1), h, nb, k, h, status);
         else mpd::diag_factor_kernel<1><<<1, mpd::NT, bytes, s>>>(T + (size_t)h * (nb + 1), h, nb, k, h, status);
         return cudaGetLastError();
     }
     const int bytes = mpd::smem_floats(nb) * 4;
     note_launch();
-    if (alg == 0) mpd::diag_factor_kernel<0><<<1, mpd::NT, bytes, s>>>(T, nb, nb, k, 0, status);
+    if (alg == 0 && nb == mpd::H256 && g_chol_smem)
+        mpd::chol256_smem_kernel<<<1, mpd::NT, mpd::SMEM256_FLOATS * 4, s>>>(T, nb, k, 0, status);
+    else if (alg == 0) mpd::diag_factor_kernel<0><<<1, mpd::NT, bytes, s>>>(T, nb, nb, k, 0, status);
     else mpd::diag_factor_kernel<1><<<1, mpd::NT, bytes, s>>>(T, nb, nb, k, 0, status);
     return cudaGetLastError();
 }

@@ -76,6 +76,7 @@ cudaError_t launch_gen_dense(double *X, long long rows, int cols, uint64_t seed,
 cudaError_t launch_sumsq(const double *X, long long len, double *partial, int blocks, cudaStream_t s);
 void mp_release();
 int set_update_kernel(int kind);
+int set_diag_kernel(int kind);
 int set_update_reserve(int sms, int below_rows);
 size_t mrd_scratch_bytes(int n);
 cudaError_t mrd_residual(const double *A, int n, int nb, const double *X, const double *colmax, const double *B,
@@ -737,6 +738,11 @@ extern "C" int palial_gpu_gen_kappa(double *dA, int n, int nb, double kappa, int
 extern "C" int palial_gpu_set_update_kernel(int kind) {
     if (kind < 0 || kind > 2) return PALIAL_ERR_ARG;
     return palial::set_update_kernel(kind);
+}
+
+extern "C" int palial_gpu_set_diag_kernel(int kind) {
+    if (kind < 0 || kind > 1) return PALIAL_ERR_ARG;
+    return palial::set_diag_kernel(kind);
 }
 
 extern "C" int palial_gpu_set_update_reserve(int sms, int below_rows) {

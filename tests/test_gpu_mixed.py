@@ -577,3 +577,27 @@ def test_fp32_and_tensor_core_panels_both_reach_the_target(alg):
         assert np.linalg.norm(x - np.linalg.solve(a, b)) <= 1e-9 * np.linalg.norm(x)
         iters.append(st.ir_iters)
     assert max(iters) <= 3, iters
+
+
+@pytest.mark.parametrize("nb", [256, 512])
+def test_shared_memory_diagonal_kernel_gives_the_same_bits(nb):
+    """The 256 x 256 Cholesky blocks factored with their upper triangle resident in shared
+    memory give the factors of the staged kernel bit for bit (NB = 512: the two halves of each
+    diagonal tile; NB = 256: whole tiles)."""
+    n = 2048
+    a = O.gen_spd(0, n)
+    da = torch.from_numpy(O.to_tiles(a, nb)).cuda()
+    lib = P.lib()
+    outs = []
+    old = lib.palial_gpu_set_diag_kernel(0)
+    try:
+        for kind in (0, 1):
+            lib.palial_gpu_set_diag_kernel(kind)
+            w = torch.empty(n * n, dtype=torch.float32, device="cuda")
+            P.mp_factor("cholesky", da.data_ptr(), w.data_ptr(), n, nb, precision="bf16x3")
+            outs.append(w)
+    finally:
+        lib.palial_gpu_set_diag_kernel(old)
+    u = O.from_tiles(outs[0].double().cpu().numpy(), n, nb)
+    assert np.array_equal(np.triu(u), np.triu(O.from_tiles(outs[1].double().cpu().numpy(), n, nb)))
+    assert np.linalg.norm(np.triu(u).T @ np.triu(u) - a) <= 1e-3 * np.linalg.norm(a)
