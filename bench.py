@@ -317,7 +317,8 @@ def config_keys(P, torch, n: int, b, nrhs: int, stream: int) -> dict:
     precision ladder (AUTO) and by the FP64 factorization + FP64 refinement, with the backward
     error recomputed by the FP64 residual and the forward error of the ladder's X against the
     FP64 solve's; no-pivot LU at kappa = 1e2 (ladder vs FP64); the QR solve of the uniform
-    [-1, 1) matrix (seed 1) by the FP32 tile QR + FP64 refinement vs the FP64 QR solve."""
+    [-1, 1) matrix (seed 1) by the FP32 tile QR (TSMQR's products with V as BF16x3 on the warp
+    tensor cores) + FP64 refinement vs the FP64 QR solve."""
     out = {}
     da = torch.empty(n * n, dtype=torch.float64, device="cuda")
     flop = {"cholesky": n ** 3 / 3.0, "lu": 2.0 * n ** 3 / 3.0, "qr": 4.0 * n ** 3 / 3.0}
@@ -345,7 +346,8 @@ def config_keys(P, torch, n: int, b, nrhs: int, stream: int) -> dict:
     out["lu"] = dict(ladder_vs_fp64("lu", 1e2), n=n, nb=NB, nrhs=nrhs, matrix="U diag(s) V^T, kappa 1e2")
     P.gen_uniform(da.data_ptr(), n, NB, 1)
     x = torch.zeros_like(b)
-    st = P.qr_solve_ir(da.data_ptr(), n, NB, b.data_ptr(), x.data_ptr(), nrhs, allow_not_converged=True)
+    st = P.qr_solve_ir(da.data_ptr(), n, NB, b.data_ptr(), x.data_ptr(), nrhs, allow_not_converged=True,
+                       precision="bf16x3")
     eta = fp64_backward_error(P, torch, da, n, NB, x, b, nrhs)
     x64 = torch.zeros_like(b)
     s64 = P.qr_solve(da.data_ptr(), n, n, NB, b.data_ptr(), x64.data_ptr(), nrhs)
@@ -658,7 +660,7 @@ def run_suite(args, P, torch) -> None:
         run_qr_mixed(args, P, torch)
         return
     if args.suite == "fp64":
-        for alg in ("cholesky", "lu", "qr"):
+        for alg in ((args.alg,) if args.alg else ("cholesky", "lu", "qr")):
             for n in ((4096, 16384, 32768) if alg == "cholesky" else (16384, 32768)):
                 d0 = torch.empty(n * n, dtype=torch.float64, device="cuda")
                 if alg == "cholesky":
@@ -719,6 +721,7 @@ def main() -> None:
     ap.add_argument("--all-kernels", action="store_true", help="kernels suite: also run every other path once")
     ap.add_argument("--no-fp64", action="store_true")
     ap.add_argument("--no-extra", action="store_true", help="skip the kappa / lu / qr keys")
+    ap.add_argument("--alg", default=None, choices=[None, "cholesky", "lu", "qr"], help="fp64 suite: one algorithm")
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)
     rank, world, local = dist_info()

@@ -459,15 +459,25 @@ __device__ void unmqr_strip(const Worker &w, const double *V, const double *T, d
     cta_gemm<false, false, M_UNIT_LOWER>(nb, 64, nb, -1.0, V, ld, W2, nb, 1.0, C, ld, w.gsm);
 }
 
-// TSMQR strip (reference src/srcqr/dtsmqr.h -> dparfb.h -> dpamm.h, L = 0):
-// W = A1 + V^T A2; W2 = T^T W; A1 -= W2; A2 -= V W2, on a 64-column strip.
+// TSMQR strip (reference src/srcqr/dtsmqr.h -> dparfb.h -> dpamm.h, L = 0): the block
+// reflector [I; V] T [I; V]^T applied as Q^T to [A1; A2] on a 64-column strip.  The
+// reference forms W = A1 + V^T A2, W2 = T^T W, A1 -= W2, A2 -= V W2 with the whole NB x NB T
+// (5 NB^2 flops per column).  Here the reflectors go in groups of 64, first to last: Q is the
+// product of the groups' block reflectors, whose T factors are the 64 x 64 diagonal blocks of T
+// (the compact WY form built forward, column by column), so for each group b
+//   W = A1[b rows] + V[:, b]^T A2;  W2 = T_bb^T W;  A1[b rows] -= W2;  A2 -= V[:, b] W2
+// gives the same transformation in 4 NB^2 + 64 NB flops per column (17 % fewer at NB = 512).
+// W, W2: 64 x 64 scratch.
 __device__ void tsmqr_strip(const Worker &w, double *A1, double *A2, const double *V, const double *T, int nb,
                             int ld, double *W, double *W2) {
-    cta_axpby(nb, 64, 1.0, A1, ld, 0.0, W, nb);
-    cta_gemm<true, false>(nb, 64, nb, 1.0, V, ld, A2, ld, 1.0, W, nb, w.gsm);
-    cta_gemm<true, false, M_UPPER>(nb, 64, nb, 1.0, T, ld, W, nb, 0.0, W2, nb, w.gsm);
-    cta_axpby(nb, 64, -1.0, W2, nb, 1.0, A1, ld);
-    cta_gemm<false, false>(nb, 64, nb, -1.0, V, ld, W2, nb, 1.0, A2, ld, w.gsm);
+    for (int b = 0; b < nb; b += 64) {
+        const double *Vb = V + (size_t)b * ld;
+        cta_axpby(64, 64, 1.0, A1 + b, ld, 0.0, W, 64);
+        cta_gemm<true, false>(64, 64, nb, 1.0, Vb, ld, A2, ld, 1.0, W, 64, w.gsm);
+        cta_gemm<true, false, M_UPPER>(64, 64, 64, 1.0, T + b + (size_t)b * ld, ld, W, 64, 0.0, W2, 64, w.gsm);
+        cta_axpby(64, 64, -1.0, W2, 64, 1.0, A1 + b, ld);
+        cta_gemm<false, false>(nb, 64, 64, -1.0, Vb, ld, W2, 64, 1.0, A2, ld, w.gsm);
+    }
 }
 
 // ---------------------------------------------------------------------------------------

@@ -505,17 +505,25 @@ __device__ void unmqr_strip(const QrSmem<T> &w, const T *V, const T *Tm, T *C, i
     cta_gemm<T, false, false, M_UNIT_LOWER>(nb, 64, nb, T(-1), V, ld, W2, nb, T(1), C, ld, w.gsm);
 }
 
-// TSMQR strip: W = A1 + V^T A2; W2 = T^T W; A1 -= W2; A2 -= V W2, on a 64-column strip.
+// TSMQR strip: Q^T = (I - [I; V] T [I; V]^T)^T applied to [A1; A2] on a 64-column strip, the
+// reflectors in groups of 64, first to last, each with its 64 x 64 diagonal block of T (the T
+// factor of that group in the forward column-wise compact WY form):
+//   W = A1[b rows] + V[:, b]^T A2;  W2 = T_bb^T W;  A1[b rows] -= W2;  A2 -= V[:, b] W2.
+// The same transformation as W = A1 + V^T A2, W2 = T^T W, A1 -= W2, A2 -= V W2 with the whole
+// T, in 4 NB^2 + 64 NB instead of 5 NB^2 flops per column.  W, W2: 64 x 64 scratch.
 // tc: FP32 data only, the two products with the dense V on the warp tensor cores (BF16x3); the
 // triangular T product stays in FP32.
 template <class T>
 __device__ void tsmqr_strip(const QrSmem<T> &w, T *A1, T *A2, const T *V, const T *Tm, int nb, int ld, T *W,
                             T *W2, bool tc = false) {
-    cta_axpby<T>(nb, 64, T(1), A1, ld, T(0), W, nb);
-    cta_gemm<T, true, false>(nb, 64, nb, T(1), V, ld, A2, ld, T(1), W, nb, w.gsm, tc);
-    cta_gemm<T, true, false, M_UPPER>(nb, 64, nb, T(1), Tm, ld, W, nb, T(0), W2, nb, w.gsm);
-    cta_axpby<T>(nb, 64, T(-1), W2, nb, T(1), A1, ld);
-    cta_gemm<T, false, false>(nb, 64, nb, T(-1), V, ld, W2, nb, T(1), A2, ld, w.gsm, tc);
+    for (int b = 0; b < nb; b += 64) {
+        const T *Vb = V + (size_t)b * ld;
+        cta_axpby<T>(64, 64, T(1), A1 + b, ld, T(0), W, 64);
+        cta_gemm<T, true, false>(64, 64, nb, T(1), Vb, ld, A2, ld, T(1), W, 64, w.gsm, tc);
+        cta_gemm<T, true, false, M_UPPER>(64, 64, 64, T(1), Tm + b + (size_t)b * ld, ld, W, 64, T(0), W2, 64, w.gsm);
+        cta_axpby<T>(64, 64, T(-1), W2, 64, T(1), A1 + b, ld);
+        cta_gemm<T, false, false>(nb, 64, 64, T(-1), Vb, ld, W2, 64, T(1), A2, ld, w.gsm, tc);
+    }
 }
 
 }  // namespace qrt
