@@ -402,8 +402,9 @@ def run_batched_solve(args, bs_fp64, count: int, world: int) -> None:
     [-1, 1)) to FP64-level backward error (1e-14 * N): (a) every matrix factored in FP64 with the
     FP64 autotuner's block sizes, one FP64 refinement check; (b) block size and precision per
     (algorithm, size class) from the solve autotuner: FP32 factorizations in one persistent
-    launch + FP64 refinement, FP64 where FP32 does not pay or does not converge, and an FP64
-    fallback of any matrix whose FP32 attempt fails.  Both timed as whole calls (copies,
+    launch + FP64 refinement, FP64 where FP32 does not pay or does not converge; an LU matrix
+    whose FP32 attempt fails gets a second FP32 attempt on its random-butterfly transform, and
+    any matrix still failing an FP64 fallback.  Both timed as whole calls (copies,
     factorizations, refinement loop).  Rank 0's share when run under torchrun."""
     from palial_gb300 import batched as B
     reps = max(3, args.steps)
@@ -422,6 +423,7 @@ def run_batched_solve(args, bs_fp64, count: int, world: int) -> None:
                       "mixed": {"seconds": mixed["seconds"], "matrices_per_s": mixed["matrices_per_s"],
                                 "tflops": mixed["tflops"], "max_backward_error": mixed["max_backward_error"],
                                 "max_refinement_steps": mixed["max_iters"], "fp64_fallbacks": mixed["fallbacks"],
+                                "butterfly_solves": mixed["butterflies"],
                                 "converged": mixed["rc"] == 0, "autotune_seconds": mixed["autotune_seconds"],
                                 "phases_s": dict(zip(phases, mixed["phase_seconds"])), "choice": choice},
                       "speedup_mixed_vs_fp64": fp64["seconds"] / mixed["seconds"]}), flush=True)

@@ -98,6 +98,8 @@ typedef struct palial_status {
     int precision_used;     /* solves: PALIAL_PREC_* of the factorization that produced X
                                (+100: LU of the random-butterfly transform)           */
     int fallbacks;          /* batched solves: matrices refactored in FP64            */
+    int butterflies;        /* batched solves: no-pivot LU matrices solved on their
+                               random-butterfly transform after FP32 LU failed          */
     char message[160];
 } palial_status;
 
@@ -384,6 +386,7 @@ typedef struct palial_batch_solve_report {
     int prec_of_class[12];    /* 1 = FP32 factorization + FP64 refinement, 2 = the same with its
                                  updates as BF16x3 products on the tensor cores, 0 = FP64     */
     int fallbacks;            /* most matrices refactored in FP64 in one timed solve         */
+    int butterflies;          /* most LU matrices solved on their butterfly transform         */
     int max_iters;            /* most refinement steps of one matrix                         */
     int not_converged;        /* 1 if a timed solve left a matrix above its tolerance        */
     double seconds;           /* median wall time of one batched solve (every phase)         */

@@ -55,7 +55,7 @@ class Status(ctypes.Structure):
                 ("tflops", ctypes.c_double), ("ir_iters", ctypes.c_int), ("gmres_iters", ctypes.c_int),
                 ("backward_error", ctypes.c_double), ("kappa_est", ctypes.c_double),
                 ("factor_seconds", ctypes.c_double), ("shift", ctypes.c_double),
-                ("precision_used", ctypes.c_int), ("fallbacks", ctypes.c_int),
+                ("precision_used", ctypes.c_int), ("fallbacks", ctypes.c_int), ("butterflies", ctypes.c_int),
                 ("message", ctypes.c_char * 160)]
 
     def as_dict(self) -> dict:

@@ -32,7 +32,8 @@ CANDIDATE_BS = (64, 128, 256)
 
 class SolveReport(ctypes.Structure):
     _fields_ = [("count", ctypes.c_int), ("bs_of_class", ctypes.c_int * 12), ("prec_of_class", ctypes.c_int * 12),
-                ("fallbacks", ctypes.c_int), ("max_iters", ctypes.c_int), ("not_converged", ctypes.c_int),
+                ("fallbacks", ctypes.c_int), ("butterflies", ctypes.c_int), ("max_iters", ctypes.c_int),
+                ("not_converged", ctypes.c_int),
                 ("seconds", ctypes.c_double), ("matrices_per_s", ctypes.c_double), ("tflops", ctypes.c_double),
                 ("max_backward_error", ctypes.c_double), ("autotune_seconds", ctypes.c_double),
                 ("autotune_s", ctypes.c_double * 108), ("phase_seconds", ctypes.c_double * 3)]

@@ -143,7 +143,7 @@ int make_solve_batch(SolveBatch &b, const std::vector<int> &idx, const std::vect
 
 struct SolveResult {
     double seconds = 0, worst = 0, phases[3] = {0, 0, 0};
-    int fallbacks = 0, max_iters = 0, rc = 0;
+    int fallbacks = 0, butterflies = 0, max_iters = 0, rc = 0;
 };
 
 int run_solve_batch(SolveBatch &b, const palial_opts &o, SolveResult &res, palial_status *st) {
@@ -161,6 +161,7 @@ int run_solve_batch(SolveBatch &b, const palial_opts &o, SolveResult &res, palia
     res.seconds = s2.seconds;
     res.worst = s2.backward_error;
     res.fallbacks = s2.fallbacks;
+    res.butterflies = s2.butterflies;
     res.max_iters = s2.ir_iters;
     return PALIAL_OK;
 }
@@ -430,6 +431,7 @@ int palial_gpu_batch_solve_synthetic(int count, uint64_t seed, int rank, int wor
         times.push_back(res.seconds);
         rep->max_backward_error = std::max(rep->max_backward_error, res.worst);
         rep->fallbacks = std::max(rep->fallbacks, res.fallbacks);
+        rep->butterflies = std::max(rep->butterflies, res.butterflies);
         rep->max_iters = std::max(rep->max_iters, res.max_iters);
         if (res.rc != PALIAL_OK) rep->not_converged = 1;
     }

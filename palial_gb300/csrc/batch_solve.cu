@@ -22,6 +22,7 @@
 #include <numeric>
 #include <vector>
 
+#include "rbt.cuh"
 #include "host_state.hpp"
 
 namespace palial {
@@ -40,6 +41,7 @@ struct SolveMat {
     double *x;        // solution
     double *r;        // residual
     const void *F;    // factors (float or double), same layout as A
+    const float *rnd; // LU of the random-butterfly transform U^T A V: the 4n randoms (else null)
     int n, nb, alg, f32;
 };
 
@@ -308,6 +310,14 @@ __global__ void __launch_bounds__(NTS) correction_kernel(const SolveMat *mats, c
     const double inv = 1.0 / scale;
     for (int i = threadIdx.x; i < n; i += NTS) v[i] = (T)(M.r[i] * inv);
     __syncthreads();
+    if constexpr (sizeof(T) == 4) {
+        if (M.rnd) {  // factors of U^T A V: v <- U^T v
+            const int q = n / 4;
+            const rbt::Rand U = rbt::rand_view(M.rnd, n);
+            for (int i = threadIdx.x; i < q; i += NTS) rbt::wt4(U, i, q, v[i], v[i + q], v[i + 2 * q], v[i + 3 * q]);
+            __syncthreads();
+        }
+    }
     for (int rb = 0; rb < n; rb += 64) {  // forward
         if (M.alg == 0) {
             if (rb) column_update<T>(f, rb, v);
@@ -321,6 +331,15 @@ __global__ void __launch_bounds__(NTS) correction_kernel(const SolveMat *mats, c
         if (rb + 64 < n) row_update<T>(f, rb, rb + 64, n, v, part);
         diag_solve<T, 3>(f, rb, v, Ds);
     }
+    if constexpr (sizeof(T) == 4) {
+        if (M.rnd) {  // z = V y
+            __syncthreads();
+            const int q = n / 4;
+            const rbt::Rand Vr = rbt::rand_view(M.rnd + 2 * n, n);
+            for (int i = threadIdx.x; i < q; i += NTS) rbt::w4(Vr, i, q, v[i], v[i + q], v[i + 2 * q], v[i + 3 * q]);
+            __syncthreads();
+        }
+    }
     for (int i = threadIdx.x; i < n; i += NTS) M.x[i] = (jb.y ? 0.0 : M.x[i]) + scale * (double)v[i];
 }
 
@@ -330,7 +349,7 @@ size_t correction_smem(int nmax) {
 }
 
 // ---- host ---------------------------------------------------------------------------------
-DevBuf w32, w64, w64b, wr, wnorm, wmats, wjobs, wfirst, wcopy;
+DevBuf w32, w64, w64b, wr, wnorm, wmats, wjobs, wfirst, wcopy, wrand;
 
 bool g_configured = false;
 cudaError_t configure() {
@@ -515,7 +534,7 @@ struct Solver {
 }  // namespace
 
 void batch_solve_release() {
-    for (DevBuf *b : {&w32, &w64, &w64b, &wr, &wnorm, &wmats, &wjobs, &wfirst, &wcopy}) b->release();
+    for (DevBuf *b : {&w32, &w64, &w64b, &wr, &wnorm, &wmats, &wjobs, &wfirst, &wcopy, &wrand}) b->release();
     g_configured = false;  // a later init (possibly another device) sets the attributes again
 }
 
@@ -585,6 +604,7 @@ int batched_solve_run(int count, const int *algs, const int *ns, const int *nbs,
         m.x = dX[i];
         m.r = wr.as<double>() + offr[i];
         m.F = f32 ? (const void *)(w32.as<float>() + off[i]) : (const void *)(w64.as<double>() + off[i]);
+        m.rnd = nullptr;
         m.n = ns[i];
         m.nb = nbs[i];
         m.alg = algs[i];
@@ -610,7 +630,45 @@ int batched_solve_run(int count, const int *algs, const int *ns, const int *nbs,
     const auto t2 = std::chrono::steady_clock::now();
     phases[1] = std::chrono::duration<double>(t2 - t1).count();
 
-    // fallback phase: FP32 matrices that broke down or did not converge, refactored in FP64
+    // fallback phase.  First the no-pivot LU matrices FP32 could not handle (pivot growth):
+    // FP32 LU of their random-butterfly transform U^T A V (Parker 1995: no pivoting needed with
+    // high probability), refined against A with z = V (LU)^-1 U^T r.  Then every FP32 matrix
+    // still failing is refactored in FP64.  opts.reserved[6] = -1 skips the butterfly stage.
+    std::vector<int> rb;
+    for (int i = 0; i < count; i++)
+        if (sv.state[i] == 2 && sv.mats[i].f32 && algs[i] == 1 && o.reserved[6] != -1) rb.push_back(i);
+    int butterflies = 0;
+    if (!rb.empty()) {
+        std::vector<size_t> offq(rb.size());
+        size_t nq = 0;
+        for (size_t j = 0; j < rb.size(); j++) {
+            offq[j] = nq;
+            nq += 4 * (size_t)ns[rb[j]];
+        }
+        std::vector<float> hq(nq);
+        for (size_t j = 0; j < rb.size(); j++) rbt_randoms(ns[rb[j]], 1, hq.data() + offq[j]);
+        PALIAL_CK(wrand.ensure(sizeof(float) * nq), "alloc butterflies");
+        PALIAL_CK(cudaMemcpyAsync(wrand.ptr, hq.data(), sizeof(float) * nq, cudaMemcpyHostToDevice, s), "butterflies");
+        for (size_t j = 0; j < rb.size(); j++) {
+            SolveMat &m = sv.mats[rb[j]];
+            m.rnd = wrand.as<float>() + offq[j];
+            PALIAL_CK(rbt_transform_matrix_with(m.A, static_cast<float *>(const_cast<void *>(m.F)), m.n, m.nb, m.rnd, s),
+                      "butterfly transform");
+            sv.state[rb[j]] = 0;
+        }
+        PALIAL_CK(cudaStreamSynchronize(s), "butterflies");  // hq is released on return
+        rc = sv.upload_table();
+        if (rc) return rc;
+        rc = sv.factor(rb, true);
+        if (rc) return rc;
+        std::vector<int> again;
+        for (int i : rb)
+            if (sv.state[i] == 0) again.push_back(i);
+        rc = sv.refine(again, max_iter);
+        if (rc) return rc;
+        for (int i : rb)
+            if (sv.state[i] == 1) butterflies++;
+    }
     std::vector<int> fb;
     for (int i = 0; i < count; i++)
         if (sv.state[i] == 2 && sv.mats[i].f32) fb.push_back(i);
@@ -626,6 +684,7 @@ int batched_solve_run(int count, const int *algs, const int *ns, const int *nbs,
             SolveMat &m = sv.mats[fb[j]];
             m.F = w64b.as<double>() + offb[j];
             m.f32 = 0;
+            m.rnd = nullptr;
             sv.state[fb[j]] = 0;
         }
         rc = sv.upload_table();
@@ -663,6 +722,7 @@ int batched_solve_run(int count, const int *algs, const int *ns, const int *nbs,
         st->ir_iters = max_it;
         st->backward_error = worst;
         st->fallbacks = (int)fb.size();  // matrices refactored in FP64
+        st->butterflies = butterflies;    // LU matrices solved on their butterfly transform
     }
     if (not_conv)
         return set_status(st, PALIAL_ERR_NOT_CONVERGED, "%d of %d matrices above their tolerance (worst %.3g)",

@@ -21,43 +21,15 @@
 #include <vector>
 
 #include "host_state.hpp"
+#include "rbt.cuh"
 
 namespace palial {
 namespace {
 
-constexpr float kInvSqrt2f = 0.70710678118654752f;
-
-struct Rand {  // device pointers into one transform's 2n randoms
-    const float *a0, *a1, *b0, *b1;  // b0, b1: [2][n/4]
-};
-__host__ __device__ inline Rand rand_view(const float *base, int n) {
-    Rand r;
-    r.a0 = base;
-    r.a1 = base + n / 2;
-    r.b0 = base + n;
-    r.b1 = base + n + n / 2;
-    return r;
-}
-
-// W^T applied to the group (transposed butterflies: level 2, then level 1)
-__device__ __forceinline__ void wt4(const Rand &R, int i, int q, float &x0, float &x1, float &x2, float &x3) {
-    const float y0 = R.b0[i] * (x0 + x1) * kInvSqrt2f, y1 = R.b1[i] * (x0 - x1) * kInvSqrt2f;
-    const float y2 = R.b0[q + i] * (x2 + x3) * kInvSqrt2f, y3 = R.b1[q + i] * (x2 - x3) * kInvSqrt2f;
-    x0 = R.a0[i] * (y0 + y2) * kInvSqrt2f;
-    x2 = R.a1[i] * (y0 - y2) * kInvSqrt2f;
-    x1 = R.a0[q + i] * (y1 + y3) * kInvSqrt2f;
-    x3 = R.a1[q + i] * (y1 - y3) * kInvSqrt2f;
-}
-// W applied to the group (level 1, then level 2)
-__device__ __forceinline__ void w4(const Rand &R, int i, int q, float &x0, float &x1, float &x2, float &x3) {
-    const float y0 = (R.a0[i] * x0 + R.a1[i] * x2) * kInvSqrt2f, y2 = (R.a0[i] * x0 - R.a1[i] * x2) * kInvSqrt2f;
-    const float y1 = (R.a0[q + i] * x1 + R.a1[q + i] * x3) * kInvSqrt2f;
-    const float y3 = (R.a0[q + i] * x1 - R.a1[q + i] * x3) * kInvSqrt2f;
-    x0 = (R.b0[i] * y0 + R.b1[i] * y1) * kInvSqrt2f;
-    x1 = (R.b0[i] * y0 - R.b1[i] * y1) * kInvSqrt2f;
-    x2 = (R.b0[q + i] * y2 + R.b1[q + i] * y3) * kInvSqrt2f;
-    x3 = (R.b0[q + i] * y2 - R.b1[q + i] * y3) * kInvSqrt2f;
-}
+using rbt::Rand;
+using rbt::rand_view;
+using rbt::w4;
+using rbt::wt4;
 
 __device__ __forceinline__ size_t toff(int n, int nb, int r, int c) {
     return (size_t)nb * nb * ((size_t)(r / nb) + (size_t)(n / nb) * (c / nb)) + (size_t)(r % nb) + (size_t)(c % nb) * nb;
@@ -146,16 +118,21 @@ int grid_for(long long elems) {
 
 }  // namespace
 
-// The randoms for size n from seed (host generated, splitmix64 counter-based; cached).
+// The 4n randoms of size n from seed: exp(r / 10), r uniform [-1/2, 1/2) (splitmix64).
+void rbt_randoms(int n, uint64_t seed, float *h) {
+    const uint64_t key = mix(seed * 0xD1B54A32D192ED03ull + 11ull);
+    for (size_t i = 0; i < (size_t)4 * n; i++) {
+        const double u = (double)(mix(key + i) >> 11) * 0x1.0p-53 - 0.5;  // uniform [-1/2, 1/2)
+        h[i] = (float)std::exp(u / 10.0);
+    }
+}
+
+// The randoms for size n from seed (host generated; cached).
 cudaError_t rbt_prepare(int n, uint64_t seed) {
     if (n % 4) return cudaErrorInvalidValue;
     if (g_rand_n == n && g_rand_seed == seed && g_rand.ptr) return cudaSuccess;
     std::vector<float> h((size_t)4 * n);
-    const uint64_t key = mix(seed * 0xD1B54A32D192ED03ull + 11ull);
-    for (size_t i = 0; i < h.size(); i++) {
-        const double u = (double)(mix(key + i) >> 11) * 0x1.0p-53 - 0.5;  // uniform [-1/2, 1/2)
-        h[i] = (float)std::exp(u / 10.0);
-    }
+    rbt_randoms(n, seed, h.data());
     cudaError_t e = g_rand.ensure(sizeof(float) * h.size());
     if (e != cudaSuccess) return e;
     e = cudaMemcpy(g_rand.ptr, h.data(), sizeof(float) * h.size(), cudaMemcpyHostToDevice);
@@ -168,6 +145,18 @@ cudaError_t rbt_prepare(int n, uint64_t seed) {
 void rbt_release() {
     g_rand.release();
     g_rand_n = 0;
+}
+
+// W = float(U^T A V) with the randoms at rnd (4n floats).
+cudaError_t rbt_transform_matrix_with(const double *A, float *W, int n, int nb, const float *rnd, cudaStream_t s) {
+    if (n % 4 || n % nb) return cudaErrorInvalidValue;
+    note_launch();
+    rbt_left_kernel<<<grid_for((long long)n / 4 * n), 256, 0, s>>>(A, W, n, nb, rand_view(rnd, n), nullptr);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    note_launch();
+    rbt_right_kernel<<<grid_for((long long)n / 4 * n), 256, 0, s>>>(W, n, nb, rand_view(rnd + 2 * n, n));
+    return cudaGetLastError();
 }
 
 // W = float(U^T A V) (tile layout), amax of A as for the plain conversion.

@@ -150,8 +150,8 @@ static int run_batch_solve(int count, unsigned long long seed, int autotune, int
         json_num("matrices_per_s", rep.matrices_per_s, "%.1f");
         json_num("tflops", rep.tflops, "%.4f");
         json_num("max_backward_error", rep.max_backward_error, "%.3e");
-        printf(", \"max_refinement_steps\": %d, \"fp64_fallbacks\": %d, \"choice\": [", rep.max_iters,
-               rep.fallbacks);
+        printf(", \"max_refinement_steps\": %d, \"fp64_fallbacks\": %d, \"butterfly_solves\": %d, \"choice\": [",
+               rep.max_iters, rep.fallbacks, rep.butterflies);
         static const int edges[7] = {32, 64, 128, 256, 512, 1024, 2048};
         for (int k = 0; k < 12; k++)
             printf("%s{\"alg\": \"%s\", \"n\": [%d, %d], \"block\": %d, \"precision\": \"%s\"}", k ? ", " : "",

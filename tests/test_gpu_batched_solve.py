@@ -192,3 +192,23 @@ def test_solve_autotune_keeps_the_fastest_converging_choice():
         assert ok, (a, c)
         chosen = r["prec_of_class"][k] * 3 + B.CANDIDATE_BS.index(r["bs_of_class"][k])
         assert times[chosen] == min(ok), (a, c, times)
+
+
+def test_batched_lu_failing_in_fp32_is_solved_on_its_butterfly_transform():
+    """A no-pivot LU matrix whose FP32 factorization meets a tiny pivot (pivot growth beyond
+    FP32) gets a second FP32 attempt on U^T A V (random butterflies): it reaches the FP64-level
+    tolerance without the FP64 fallback, and the solution matches numpy's."""
+    rng = np.random.default_rng(11)
+    n = 256
+    a = rng.uniform(-1, 1, (n, n))
+    a[0, 0] = 1e-9  # a leading pivot FP32 cannot factor without growth
+    mats = [a, _spd(128, rng)]
+    d = Dev(mats, [64, 64])
+    st, iters, berr = B.solve([1, 0], d.ns, d.nbs, d.ptrs, d.bptrs, d.xptrs)
+    assert st.code == 0, st.message
+    assert st.butterflies == 1 and st.fallbacks == 0, (st.butterflies, st.fallbacks)
+    assert iters[0] > 0
+    for i in range(2):
+        assert berr[i] <= 1e-14 * d.ns[i], (i, berr[i])
+        xr = np.linalg.solve(mats[i], d.b[i])
+        assert np.linalg.norm(d.x(i) - xr) <= 1e-9 * np.linalg.norm(xr), i
