@@ -233,16 +233,19 @@ def solve(algs, ns, nbs, a_ptrs, b_ptrs, x_ptrs, precs=None, ir_tol: float = 0.0
 
 
 def solve_synthetic(count: int = 2000, seed: int = 2, rank: int = 0, world: int = 1, autotune: bool = True,
-                    bs12=None, prec12=None, reps: int = 3) -> dict:
+                    bs12=None, prec12=None, reps: int = 3, butterflies: int = 0) -> dict:
     """Batched solves of this rank's share of the synthetic batch, inside the library; block and
-    precision per [alg * 6 + size class] from the autotuner or the arguments.  Returns the
-    report as a dict."""
+    precision per [alg * 6 + size class] from the autotuner or the arguments.  butterflies: 0 =
+    an FP32 LU that fails gets a second attempt on its random-butterfly transform, 1 = every
+    FP32 LU on its transform from the start, -1 = never.  Returns the report as a dict."""
     rep = SolveReport()
     st = Status()
     b12 = (ctypes.c_int * 12)(*bs12) if bs12 is not None else None
     p12 = (ctypes.c_int * 12)(*prec12) if prec12 is not None else None
+    o = make_opts()
+    o.reserved[6] = butterflies
     rc = lib().palial_gpu_batch_solve_synthetic(count, ctypes.c_uint64(seed), rank, world, int(autotune), b12, p12,
-                                                reps, ctypes.byref(make_opts()), ctypes.byref(st), ctypes.byref(rep))
+                                                reps, ctypes.byref(o), ctypes.byref(st), ctypes.byref(rep))
     if rc and rc != -6:
         raise PalialError(rc, st.message.decode(errors="replace"))
     out = {f: getattr(rep, f) for f, _ in SolveReport._fields_}

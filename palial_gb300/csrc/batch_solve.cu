@@ -612,10 +612,46 @@ int batched_solve_run(int count, const int *algs, const int *ns, const int *nbs,
         sv.tol[i] = o.ir_tol > 0 ? o.ir_tol : 1e-14 * ns[i];
         (f32 ? m32 : m64).push_back(i);
     }
+    // U^T A V (float) into the FP32 factor buffers of the listed matrices, each with its own 4n
+    // randoms (seed 1)
+    std::vector<float> hq;
+    const auto butterfly = [&](const std::vector<int> &ms) -> int {
+        std::vector<size_t> offq(ms.size());
+        size_t nq = 0;
+        for (size_t j = 0; j < ms.size(); j++) {
+            offq[j] = nq;
+            nq += 4 * (size_t)ns[ms[j]];
+        }
+        hq.assign(nq, 0.f);
+        for (size_t j = 0; j < ms.size(); j++) rbt_randoms(ns[ms[j]], 1, hq.data() + offq[j]);
+        PALIAL_CK(wrand.ensure(sizeof(float) * nq), "alloc butterflies");
+        PALIAL_CK(cudaMemcpyAsync(wrand.ptr, hq.data(), sizeof(float) * nq, cudaMemcpyHostToDevice, s), "butterflies");
+        for (size_t j = 0; j < ms.size(); j++) {
+            SolveMat &m = sv.mats[ms[j]];
+            m.rnd = wrand.as<float>() + offq[j];
+            PALIAL_CK(rbt_transform_matrix_with(m.A, static_cast<float *>(const_cast<void *>(m.F)), m.n, m.nb, m.rnd, s),
+                      "butterfly transform");
+            sv.state[ms[j]] = 0;
+        }
+        PALIAL_CK(cudaStreamSynchronize(s), "butterflies");  // hq is reused
+        return PALIAL_OK;
+    };
     rc = sv.upload_table();
     if (rc) return rc;
     rc = sv.copy(all);
     if (rc) return rc;
+    // opts.reserved[6] = 1: every FP32 LU matrix on its butterfly transform from the start
+    if (o.reserved[6] == 1) {
+        std::vector<int> lu32;
+        for (int i : m32)
+            if (algs[i] == 1) lu32.push_back(i);
+        if (!lu32.empty()) {
+            rc = butterfly(lu32);
+            if (rc) return rc;
+            rc = sv.upload_table();
+            if (rc) return rc;
+        }
+    }
     rc = sv.factor(m32, true);
     if (rc) return rc;
     rc = sv.factor(m64, false);
@@ -633,30 +669,16 @@ int batched_solve_run(int count, const int *algs, const int *ns, const int *nbs,
     // fallback phase.  First the no-pivot LU matrices FP32 could not handle (pivot growth):
     // FP32 LU of their random-butterfly transform U^T A V (Parker 1995: no pivoting needed with
     // high probability), refined against A with z = V (LU)^-1 U^T r.  Then every FP32 matrix
-    // still failing is refactored in FP64.  opts.reserved[6] = -1 skips the butterfly stage.
+    // still failing is refactored in FP64.  opts.reserved[6] = -1 skips the butterfly stage (and
+    // matrices already on their butterfly transform go straight to FP64).
     std::vector<int> rb;
     for (int i = 0; i < count; i++)
-        if (sv.state[i] == 2 && sv.mats[i].f32 && algs[i] == 1 && o.reserved[6] != -1) rb.push_back(i);
+        if (sv.state[i] == 2 && sv.mats[i].f32 && algs[i] == 1 && !sv.mats[i].rnd && o.reserved[6] != -1)
+            rb.push_back(i);
     int butterflies = 0;
     if (!rb.empty()) {
-        std::vector<size_t> offq(rb.size());
-        size_t nq = 0;
-        for (size_t j = 0; j < rb.size(); j++) {
-            offq[j] = nq;
-            nq += 4 * (size_t)ns[rb[j]];
-        }
-        std::vector<float> hq(nq);
-        for (size_t j = 0; j < rb.size(); j++) rbt_randoms(ns[rb[j]], 1, hq.data() + offq[j]);
-        PALIAL_CK(wrand.ensure(sizeof(float) * nq), "alloc butterflies");
-        PALIAL_CK(cudaMemcpyAsync(wrand.ptr, hq.data(), sizeof(float) * nq, cudaMemcpyHostToDevice, s), "butterflies");
-        for (size_t j = 0; j < rb.size(); j++) {
-            SolveMat &m = sv.mats[rb[j]];
-            m.rnd = wrand.as<float>() + offq[j];
-            PALIAL_CK(rbt_transform_matrix_with(m.A, static_cast<float *>(const_cast<void *>(m.F)), m.n, m.nb, m.rnd, s),
-                      "butterfly transform");
-            sv.state[rb[j]] = 0;
-        }
-        PALIAL_CK(cudaStreamSynchronize(s), "butterflies");  // hq is released on return
+        rc = butterfly(rb);
+        if (rc) return rc;
         rc = sv.upload_table();
         if (rc) return rc;
         rc = sv.factor(rb, true);
@@ -666,9 +688,9 @@ int batched_solve_run(int count, const int *algs, const int *ns, const int *nbs,
             if (sv.state[i] == 0) again.push_back(i);
         rc = sv.refine(again, max_iter);
         if (rc) return rc;
-        for (int i : rb)
-            if (sv.state[i] == 1) butterflies++;
     }
+    for (int i = 0; i < count; i++)
+        if (sv.state[i] == 1 && sv.mats[i].rnd) butterflies++;
     std::vector<int> fb;
     for (int i = 0; i < count; i++)
         if (sv.state[i] == 2 && sv.mats[i].f32) fb.push_back(i);
