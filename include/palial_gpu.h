@@ -197,6 +197,10 @@ int palial_gpu_mp_update_step(int alg, int precision, float *dW, int n, int nb, 
  * C traffic).  Both give the same bits.
  * Returns the previous setting (PALIAL_ERR_ARG for an unknown kind). */
 int palial_gpu_set_update_kernel(int kind);
+/* The mixed path's FP32 working copy: W = float(A) rounded to nearest even (tile layout, n x n,
+ * tile nb), the upper tiles only when upper_only (the conversion of a solve; no reference
+ * counterpart).  Device buffers, synchronous. */
+int palial_gpu_f64_to_f32(const double *dA, float *dW, int n, int nb, int upper_only);
 /* Which kernel factors the mixed path's 256 x 256 Cholesky blocks (the halves of a 512 diagonal
  * tile, or 256 tiles): 1 (default) keeps the block's upper triangle in shared memory for the
  * whole factorization, 0 stages 64-column pieces from global memory.  Same bits.  Returns the

@@ -740,6 +740,16 @@ extern "C" int palial_gpu_set_update_kernel(int kind) {
     return palial::set_update_kernel(kind);
 }
 
+extern "C" int palial_gpu_f64_to_f32(const double *dA, float *dW, int n, int nb, int upper_only) {
+    if (!dA || !dW || n <= 0 || nb <= 0 || n % nb || (nb * nb) % 2) return PALIAL_ERR_ARG;
+    palial_status *st = nullptr;
+    int rc = ensure_init(st);
+    if (rc) return rc;
+    PALIAL_CK(mps_f64_to_f32(dA, dW, n, nb, 0.0, nullptr, nullptr, upper_only != 0), "convert");
+    PALIAL_CK(cudaStreamSynchronize(nullptr), "convert");
+    return PALIAL_OK;
+}
+
 extern "C" int palial_gpu_set_diag_kernel(int kind) {
     if (kind < 0 || kind > 1) return PALIAL_ERR_ARG;
     return palial::set_diag_kernel(kind);

@@ -27,6 +27,21 @@ __device__ __forceinline__ size_t tile_off(int n, int nb, int tm, int tn) {
 // are 8192-element chunks of tiles; upper_only skips the tiles below the diagonal (Cholesky
 // reads only the upper triangle, which a caller may have copied in first).
 constexpr int kConvChunk = 8192;
+// float(d) rounded to nearest even by integer operations on the bit pattern (the FP64 -> FP32
+// conversion instruction runs on this part's FP64 pipe, 2 per clock per SM, which would bound a
+// streaming conversion); zero, subnormal, overflowing and non-finite results take the
+// conversion instruction (rare, so the branch costs nothing).
+__device__ __forceinline__ float d2f_rne(double d) {
+    const unsigned long long b = (unsigned long long)__double_as_longlong(d);
+    const int e32 = (int)((b >> 52) & 0x7FF) - 1023 + 127;
+    if (e32 < 1 || e32 > 254) return (float)d;
+    const unsigned hi23 = (unsigned)(b >> 29) & 0x7FFFFFu;
+    const unsigned rem = (unsigned)b & 0x1FFFFFFFu;  // the 29 dropped mantissa bits
+    unsigned f = ((unsigned)e32 << 23) | hi23;
+    f += (rem > 0x10000000u) | ((rem == 0x10000000u) & (hi23 & 1u));  // a carry reaches the exponent
+    return __uint_as_float(f | ((unsigned)(b >> 32) & 0x80000000u));
+}
+
 __global__ void f64_to_f32_kernel(const double *__restrict__ a, float *__restrict__ w, int n, int nb,
                                   double shift_diag, int upper_only, int r0, int r1, double *amax) {
     const int mt = n / nb;
@@ -62,7 +77,7 @@ __global__ void f64_to_f32_kernel(const double *__restrict__ a, float *__restric
                 if (i % (nb + 1) == 0) v.x += shift_diag;
                 if ((i + 1) % (nb + 1) == 0) v.y += shift_diag;
             }
-            *reinterpret_cast<float2 *>(w + base + i) = make_float2((float)v.x, (float)v.y);
+            *reinterpret_cast<float2 *>(w + base + i) = make_float2(d2f_rne(v.x), d2f_rne(v.y));
         }
     }
     if (amax) {

@@ -1,6 +1,8 @@
 """Mixed precision: the tcgen05 trailing update against a torch FP32 reference computed from
 the same quantized operands, and mixed-precision factorization + iterative refinement
 against numpy's FP64 solution (backward error gate 1e-14 * N, the target of the path)."""
+import ctypes
+
 import numpy as np
 import pytest
 
@@ -601,3 +603,27 @@ def test_shared_memory_diagonal_kernel_gives_the_same_bits(nb):
     u = O.from_tiles(outs[0].double().cpu().numpy(), n, nb)
     assert np.array_equal(np.triu(u), np.triu(O.from_tiles(outs[1].double().cpu().numpy(), n, nb)))
     assert np.linalg.norm(np.triu(u).T @ np.triu(u) - a) <= 1e-3 * np.linalg.norm(a)
+
+
+def test_fp64_to_fp32_conversion_rounds_like_the_hardware():
+    """The working-copy conversion rounds by integer operations on the bit pattern: equal bits to
+    torch's FP32 cast (round to nearest even) on random values, exact ties in both directions,
+    values near the FP32 overflow and underflow limits, zeros and non-finite values."""
+    n, nb = 512, 256
+    g = torch.Generator().manual_seed(3)
+    a = torch.randn(n * n, dtype=torch.float64, generator=g) * torch.exp2(torch.randint(-60, 60, (n * n,),
+                                                                                        generator=g).double())
+    # exact ties: 24 significant bits + a 1 in the 25th place, odd and even last kept bit
+    m = torch.randint(1 << 23, 1 << 24, (4096,), generator=g, dtype=torch.int64)
+    ties = (m.double() * 2 + 1) * torch.exp2(torch.randint(-100, 100, (4096,), generator=g).double() - 24)
+    a[:4096] = ties
+    special = torch.tensor([0.0, -0.0, 3.4e38, -3.4e38, 3.4028235e38, 1e39, -1e39, 1.2e-38, 1e-40, -1e-44, 1e-50,
+                            float("inf"), -float("inf"), float("nan")], dtype=torch.float64)
+    a[4096:4096 + len(special)] = special
+    da = a.cuda()
+    w = torch.empty(n * n, dtype=torch.float32, device="cuda")
+    assert P.lib().palial_gpu_f64_to_f32(ctypes.c_void_p(da.data_ptr()), ctypes.c_void_p(w.data_ptr()), n, nb, 0) == 0
+    ref = a.float()
+    got = w.cpu()
+    same = (got.view(torch.int32) == ref.view(torch.int32)) | (torch.isnan(got) & torch.isnan(ref))
+    assert bool(same.all()), int((~same).sum())
