@@ -553,9 +553,10 @@ def every_kernel_once(P, torch, n: int) -> dict:
     """One call of each remaining path of the library at size n (the small case the per-kernel
     ncu captures select from): mixed-precision Cholesky and LU solves (diagonal tiles, panel
     solves, block inverses, refinement solves and residuals), FP64 Cholesky / LU / QR on the
-    persistent scheduler, the FP32 QR solve (FP32 task scheduler), a batched FP32 solve of three
-    matrices (FP32 scheduler, batched residual and correction kernels) and a few MLP training
-    steps; wall seconds per call."""
+    persistent scheduler, the FP32 QR solve (FP32 task scheduler; also with the tensor-core
+    TSMQR), the host-buffer Cholesky solve, a batched FP32 solve of four matrices (FP32
+    scheduler, batched residual and correction kernels, one LU on its butterfly transform) and a
+    few MLP training steps; wall seconds per call."""
     import numpy as np
     out = {}
     nrhs = 16
@@ -580,15 +581,29 @@ def every_kernel_once(P, torch, n: int) -> dict:
     x.zero_()
     st = P.qr_solve_ir(a.data_ptr(), n, NB, b.data_ptr(), x.data_ptr(), nrhs, allow_not_converged=True)
     out["qr_fp32_solve_s"] = st.seconds
-    del a
+    x.zero_()
+    st = P.qr_solve_ir(a.data_ptr(), n, NB, b.data_ptr(), x.data_ptr(), nrhs, allow_not_converged=True,
+                       precision="bf16x3")
+    out["qr_fp32_tensor_core_solve_s"] = st.seconds
+    # the host-buffer Cholesky solve (upper triangle copied, lower written on the device)
+    P.gen_spd(a.data_ptr(), n, NB, 0)
+    host = torch.empty(n * n, dtype=torch.float64, pin_memory=True)
+    host.copy_(a)
+    bh = b.cpu().numpy().reshape(nrhs, n).copy()
+    xh = np.zeros((nrhs, n))
+    st = P.solve_ir_host("cholesky", host.numpy(), n, NB, bh, xh, nrhs, precision="bf16x3", raise_on_error=False)
+    out["cholesky_host_solve_s"] = st.seconds
+    del a, host
     torch.cuda.empty_cache()
     from palial_gb300 import batched as B
     rng = np.random.default_rng(0)
-    sizes, nbs, algs = [512, 384, 256], [128, 128, 64], [0, 1, 0]
+    sizes, nbs, algs = [512, 384, 256, 256], [128, 128, 64, 64], [0, 1, 0, 1]
     mats = []
     for k, m in enumerate(sizes):
         q = rng.uniform(-1, 1, (m, m))
         mats.append(q @ q.T + m * np.eye(m) if algs[k] == 0 else q + m * np.eye(m))
+    mats[3] = rng.uniform(-1, 1, (256, 256))
+    mats[3][0, 0] = 1e-9  # FP32 no-pivot LU fails: the butterfly stage solves it
     tiles = [torch.from_numpy(np.ascontiguousarray(
         mm.reshape(m // nb, nb, m // nb, nb).transpose(2, 0, 3, 1)).ravel()).cuda() for mm, m, nb in zip(mats, sizes, nbs)]
     rhs = [torch.from_numpy(rng.uniform(-1, 1, m)).cuda() for m in sizes]

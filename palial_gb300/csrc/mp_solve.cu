@@ -27,19 +27,35 @@ __device__ __forceinline__ size_t tile_off(int n, int nb, int tm, int tn) {
 // are 8192-element chunks of tiles; upper_only skips the tiles below the diagonal (Cholesky
 // reads only the upper triangle, which a caller may have copied in first).
 constexpr int kConvChunk = 8192;
-// float(d) rounded to nearest even by integer operations on the bit pattern (the FP64 -> FP32
-// conversion instruction runs on this part's FP64 pipe, 2 per clock per SM, which would bound a
-// streaming conversion); zero, subnormal, overflowing and non-finite results take the
-// conversion instruction (rare, so the branch costs nothing).
+// float(d) rounded to nearest even by integer operations on the bit pattern only (the FP64 ->
+// FP32 conversion instruction runs on this part's FP64 pipe, 2 per clock per SM, which would
+// bound a streaming conversion): normal results keep the top 23 of the 52 mantissa bits and
+// round on the 29 dropped ones (a carry reaches the exponent, and past the largest finite value
+// gives infinity); results below the normal range shift the 53-bit significand into the
+// subnormal field with the same rounding; Inf stays Inf, NaN becomes the quiet NaN.
 __device__ __forceinline__ float d2f_rne(double d) {
     const unsigned long long b = (unsigned long long)__double_as_longlong(d);
-    const int e32 = (int)((b >> 52) & 0x7FF) - 1023 + 127;
-    if (e32 < 1 || e32 > 254) return (float)d;
-    const unsigned hi23 = (unsigned)(b >> 29) & 0x7FFFFFu;
-    const unsigned rem = (unsigned)b & 0x1FFFFFFFu;  // the 29 dropped mantissa bits
-    unsigned f = ((unsigned)e32 << 23) | hi23;
-    f += (rem > 0x10000000u) | ((rem == 0x10000000u) & (hi23 & 1u));  // a carry reaches the exponent
-    return __uint_as_float(f | ((unsigned)(b >> 32) & 0x80000000u));
+    const unsigned sign = (unsigned)(b >> 32) & 0x80000000u;
+    const int E = (int)((b >> 52) & 0x7FF);
+    const int e32 = E - 1023 + 127;
+    const unsigned long long mant = b & 0xFFFFFFFFFFFFFull;
+    // normal range
+    const unsigned hi23 = (unsigned)(mant >> 29);
+    const unsigned rem = (unsigned)mant & 0x1FFFFFFFu;
+    unsigned fn = ((unsigned)e32 << 23) | hi23;
+    fn += (rem > 0x10000000u) | ((rem == 0x10000000u) & (hi23 & 1u));
+    // below it: significand >> (30 - e32) (1 + 52 bits; nothing survives a shift of 54 or more)
+    const int sh = 30 - e32;
+    const unsigned long long sig = mant | 0x10000000000000ull;
+    unsigned fs = 0;
+    if (E != 0 && e32 < 1 && sh < 54) {  // sh >= 30 here
+        const unsigned long long q = sig >> sh, r = sig & ((1ull << sh) - 1), half = 1ull << (sh - 1);
+        fs = (unsigned)q + ((r > half) | ((r == half) & (unsigned)(q & 1)));
+    }
+    unsigned f = e32 >= 1 ? fn : fs;
+    if (e32 > 254) f = 0x7F800000u;                            // overflow
+    if (E == 0x7FF) f = mant ? 0x7FC00000u : 0x7F800000u;      // NaN, Inf
+    return __uint_as_float(f | sign);
 }
 
 __global__ void f64_to_f32_kernel(const double *__restrict__ a, float *__restrict__ w, int n, int nb,
@@ -108,7 +124,7 @@ __global__ void __launch_bounds__(256) mirror_upper_kernel(double *__restrict__ 
     const long long items = (long long)nbk * (nbk + 1) / 2;  // block it = bi (bi + 1) / 2 + bj
     const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
     for (long long it = blockIdx.x; it < items; it += gridDim.x) {
-        int bi = (int)((sqrt(8.0 * (double)it + 1.0) - 1.0) * 0.5);
+        int bi = (int)((sqrtf(8.0f * (float)it + 1.0f) - 1.0f) * 0.5f);  // an estimate: corrected below
         while ((long long)bi * (bi + 1) / 2 > it) bi--;
         while ((long long)(bi + 1) * (bi + 2) / 2 <= it) bi++;
         const int bj = (int)(it - (long long)bi * (bi + 1) / 2);
