@@ -456,10 +456,13 @@ int mp_factor(int alg, int prec, float *W, int n, int nb, cudaStream_t s, palial
             if (present - k - 1 > 1)
                 PALIAL_CK(mp_update(mode, 1, W, n, nb, k, ah, al, bh, bl, sa, sb, status, lo, 3, 1, present - k - 1),
                           "update (rest)");
+            // the next step's chain waits for the rows up to present only: the catch-up below
+            // touches rows of groups that have not joined (at or past present)
+            PALIAL_CK(cudaEventRecord(g_la.rest, lo), "event");
             rc2 = run(plan.post[k]);
             if (rc2) return rc2;
         }
-        PALIAL_CK(cudaEventRecord(g_la.rest, lo), "event");
+        if (!arrive) PALIAL_CK(cudaEventRecord(g_la.rest, lo), "event");
         PALIAL_CK(g_ftrace.mark(lo, k, FactorTrace::REST1), "trace");
         have_rest = true;
     }
