@@ -160,7 +160,7 @@ int palial_gpu_factor_dev(int alg, double *dA, double *dS, int n, int nb, const 
  * Opt-in stabilised LU (alg = PALIAL_ALG_LU, mixed precisions): opts->reserved[6] = 1 factors
  * the random-butterfly transform U^T A V (depth-2 recursive butterflies, Parker 1995) without
  * pivoting instead of A, refines against A (seed: opts->reserved[7], 0 = 1).  PALIAL_PREC_AUTO
- * runs a precision ladder: BF16x3 (at most 10 refinement steps and 60 GMRES iterations; a
+ * runs a precision ladder: BF16x3 (at most 10 refinement steps and 36 GMRES iterations; a
  * Cholesky breakdown moves up at once), then TF32x3 (FP32-level factors; 20 steps, GMRES
  * restarts of 200 and 600 iterations in all), then the FP64 factorization;
  * status.precision_used reports the rung that produced the result (PALIAL_PREC_*, + 100 for the

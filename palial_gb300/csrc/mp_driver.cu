@@ -1140,14 +1140,17 @@ extern "C" int palial_gpu_solve_ir(int alg, const double *dA, int n, int nb, con
         const int prec = ladder[li];
         palial_opts oo = o;
         oo.precision = prec;
-        // lower rungs get a bounded effort.  BF16x3: at most 10 refinement steps, GMRES
-        // restarts of 50 and 60 iterations in all, and a Cholesky breakdown (a matrix beyond
-        // BF16x3's reach) goes up at once instead of being retried with a shift.  TF32x3: 20
-        // steps, restarts of 200, 600 iterations in all.
+        // lower rungs get a bounded effort.  BF16x3: at most 10 refinement steps and 36 GMRES
+        // iterations in all (a GMRES iteration, a full residual and two triangular solves,
+        // costs about a twelfth of a factorization: the budget lets a system that a BF16x3
+        // preconditioner handles in a few cycles finish, and one that projects past it moves
+        // up early), and a Cholesky breakdown (a matrix beyond BF16x3's reach) goes up at once
+        // instead of being retried with a shift.  TF32x3: 20 steps, restarts of 200, 600
+        // iterations in all.
         if (prec == PALIAL_PREC_BF16X3) {
             if (oo.ir_max_iter <= 0 || oo.ir_max_iter > 10) oo.ir_max_iter = 10;
-            oo.reserved[1] = 50;
-            oo.reserved[3] = 60;
+            oo.reserved[1] = 36;
+            oo.reserved[3] = 36;
             oo.reserved[5] |= 2;
         } else if (prec == PALIAL_PREC_TF32X3) {
             if (oo.ir_max_iter <= 0 || oo.ir_max_iter > 20) oo.ir_max_iter = 20;
