@@ -101,21 +101,40 @@ def test_fp32_qr_tile_kernels_match_the_oracle(nb):
     L.orc_dgeqrt(nb, ra.ctypes.data_as(dp), nb, rt.ctypes.data_as(dp), nb, tau.ctypes.data_as(dp), work.ctypes.data_as(dp))
     da, dt = _dev32(a), _dev32(np.zeros((nb, nb)))
     assert lib.palial_gpu_tile_sgeqrt(nb, da.data_ptr(), dt.data_ptr(), nb) == 0
-    assert _rel(_host(da, nb), ra) <= 1e-3 and _rel(np.triu(_host(dt, nb)), np.triu(rt)) <= 1e-3
+    # the backward error of the GPU's own factors: Q R = A and Q^T Q = I to a small multiple of
+    # u_32 (measured at most 1.4e-6 at nb = 512), and the factors against the oracle's
+    g, gt = _host(da, nb), np.triu(_host(dt, nb))
+    v = np.tril(g, -1) + np.eye(nb)
+    q = np.eye(nb) - v @ gt @ v.T
+    back = _rel(q @ np.triu(g), a)
+    orth = np.linalg.norm(q.T @ q - np.eye(nb)) / np.sqrt(nb)
+    fwd_r, fwd_t = _rel(g, ra), _rel(gt, np.triu(rt))
+    print(f"nb={nb}: GEQRT backward {back:.2e}, orthogonality {orth:.2e}, forward R/V {fwd_r:.2e}, T {fwd_t:.2e}")
+    assert back <= 1e-5 and orth <= 1e-5, (back, orth)
+    assert fwd_r <= 2e-5 and fwd_t <= 2e-5  # measured at most 2.7e-6 (nb = 512)
     c = O.gen_uniform(10, nb).astype(np.float32).astype(np.float64)
     rc = np.asfortranarray(c.copy())
     L.orc_dormqr(nb, ra.ctypes.data_as(dp), nb, rt.ctypes.data_as(dp), nb, rc.ctypes.data_as(dp), nb, work.ctypes.data_as(dp))
     dc = _dev32(c)
     assert lib.palial_gpu_tile_sormqr(nb, _dev32(ra).data_ptr(), _dev32(rt).data_ptr(), dc.data_ptr(), nb) == 0
-    assert _rel(_host(dc, nb), rc) <= 1e-4
+    e_orm = _rel(_host(dc, nb), rc)  # applying a given Q is forward stable: ~ u_32
+    print(f"nb={nb}: ORMQR {e_orm:.2e}")
+    assert e_orm <= 1e-5, e_orm
     a2 = O.gen_uniform(11, nb).astype(np.float32).astype(np.float64)
     r1, r2, t2 = np.asfortranarray(ra.copy()), np.asfortranarray(a2.copy()), np.zeros((nb, nb), order="F")
     L.orc_dtsqrt(nb, r1.ctypes.data_as(dp), nb, r2.ctypes.data_as(dp), nb, t2.ctypes.data_as(dp), nb,
                  tau.ctypes.data_as(dp), work.ctypes.data_as(dp))
     d1, d2, dt2 = _dev32(ra), _dev32(a2), _dev32(np.zeros((nb, nb)))
     assert lib.palial_gpu_tile_stsqrt(nb, d1.data_ptr(), d2.data_ptr(), dt2.data_ptr(), nb) == 0
-    assert _rel(_host(d1, nb), r1) <= 1e-3 and _rel(_host(d2, nb), r2) <= 1e-3
-    assert _rel(np.triu(_host(dt2, nb)), np.triu(t2)) <= 1e-3
+    # backward error of the TS factorization: Q [R1; 0] = [R_in; A2] with Q = I - [I; V] T [I; V]^T
+    g1, g2, gt2 = np.triu(_host(d1, nb)), _host(d2, nb), np.triu(_host(dt2, nb))
+    w = np.vstack([np.eye(nb), g2])
+    q2 = np.eye(2 * nb) - w @ gt2 @ w.T
+    back2 = np.linalg.norm(q2 @ np.vstack([g1, np.zeros((nb, nb))]) - np.vstack([np.triu(ra), a2])) / \
+        np.linalg.norm(np.vstack([np.triu(ra), a2]))
+    print(f"nb={nb}: TSQRT backward {back2:.2e}, forward R {_rel(g1, np.triu(r1)):.2e}")
+    assert back2 <= 1e-5, back2
+    assert _rel(_host(d1, nb), r1) <= 2e-5 and _rel(g2, r2) <= 2e-5 and _rel(gt2, np.triu(t2)) <= 2e-5
     b1 = O.gen_uniform(12, nb).astype(np.float32).astype(np.float64)
     b2 = O.gen_uniform(13, nb).astype(np.float32).astype(np.float64)
     s1, s2 = np.asfortranarray(b1.copy()), np.asfortranarray(b2.copy())
@@ -124,4 +143,6 @@ def test_fp32_qr_tile_kernels_match_the_oracle(nb):
     e1, e2 = _dev32(b1), _dev32(b2)
     assert lib.palial_gpu_tile_stsmqr(nb, e1.data_ptr(), e2.data_ptr(), _dev32(r2).data_ptr(), _dev32(t2).data_ptr(),
                                       nb) == 0
-    assert _rel(_host(e1, nb), s1) <= 1e-4 and _rel(_host(e2, nb), s2) <= 1e-4
+    e_ts = max(_rel(_host(e1, nb), s1), _rel(_host(e2, nb), s2))
+    print(f"nb={nb}: TSMQR {e_ts:.2e}")
+    assert e_ts <= 1e-5, e_ts
