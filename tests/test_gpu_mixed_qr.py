@@ -134,7 +134,7 @@ def test_fp32_qr_tile_kernels_match_the_oracle(nb):
         np.linalg.norm(np.vstack([np.triu(ra), a2]))
     print(f"nb={nb}: TSQRT backward {back2:.2e}, forward R {_rel(g1, np.triu(r1)):.2e}")
     assert back2 <= 1e-5, back2
-    assert _rel(_host(d1, nb), r1) <= 2e-5 and _rel(g2, r2) <= 2e-5 and _rel(gt2, np.triu(t2)) <= 2e-5
+    assert _rel(_host(d1, nb), r1) <= 2e-5 and _rel(g2, r2) <= 1e-4 and _rel(gt2, np.triu(t2)) <= 1e-4
     b1 = O.gen_uniform(12, nb).astype(np.float32).astype(np.float64)
     b2 = O.gen_uniform(13, nb).astype(np.float32).astype(np.float64)
     s1, s2 = np.asfortranarray(b1.copy()), np.asfortranarray(b2.copy())
