@@ -727,7 +727,7 @@ def main() -> None:
     ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--e2e-steps", type=int, default=5)
+    ap.add_argument("--e2e-steps", type=int, default=10, help="host-buffer steps (the pageable leg runs half)")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--n", type=int, default=N)
     ap.add_argument("--precision", default="bf16x3")
