@@ -693,6 +693,26 @@ void palial::mp_release() {
                       &mb.x32, &mb.norms, &mb.work, &mb.krylov, &mb.hbuf, &mb.gvec, &mb.y32, &mb.xsplit, &mb.binv,
                       &mb.dinv_u, &mb.dinv_l, &mb.stile, &mb.xdig})
         b->release();
+    // the streams and events belong to the context current when they were made: forget them
+    // (the next solve makes new ones), so a later context on this device is not handed stale ones
+    for (cudaStream_t *q : {&g_la.hi, &g_la.mid, &g_la.lo, &g_sc.copy}) {
+        if (*q) cudaStreamDestroy(*q);
+        *q = nullptr;
+    }
+    for (cudaEvent_t *ev : {&g_la.start, &g_la.packed, &g_la.rest, &g_la.join, &g_la.binv, &g_la.first, &g_la.nextrow,
+                            &g_la.join_mid, &g_sc.upper, &g_sc.full, &g_ftrace.t0}) {
+        if (*ev) cudaEventDestroy(*ev);
+        *ev = nullptr;
+    }
+    for (cudaEvent_t &ev : g_arrival.ready) {
+        if (ev) cudaEventDestroy(ev);
+        ev = nullptr;
+    }
+    for (cudaEvent_t ev : g_ftrace.pool) cudaEventDestroy(ev);
+    g_ftrace.pool.clear();
+    g_ftrace.tags.clear();
+    g_ftrace.used = 0;
+    g_full_ready = nullptr;
 }
 
 extern "C" int palial_gpu_gen_kappa(double *dA, int n, int nb, double kappa, int symmetric, uint64_t seed,
